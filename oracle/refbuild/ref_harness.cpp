@@ -1,0 +1,217 @@
+// C-callable harness around the StarPolymersMD reference classes, compiled
+// together with the reference's own unmodified sources (see Makefile) into
+// oracle/_ref/libsmpc_ref.so. Test infrastructure only: it lets Python build a
+// system at library level the way star-polymers/src/mpc_test.cpp:73-110 and
+// star-polymers/src/star-polymers.cpp:352-404 do, run the driver loop body
+// (star-polymers.cpp:466,530,534: propagate, then MPC::step), and read or
+// overwrite the state, the cell occupancies and the recorded random draws.
+#include <cstring>
+#include <vector>
+
+#include "Box.h"
+#include "MPC.h"
+#include "Thermostat_None.h"
+#include "rand_tape.h"
+
+namespace {
+
+// Exposes the protected cell-list state of MPC (MPC.h:28-41) for read-out.
+class HarnessMPC : public MPC {
+ public:
+  using MPC::MPC;
+  unsigned cells() const { return NumberOfCells + 1; }
+  unsigned cell_total(unsigned i) const { return static_cast<unsigned>(MPCCellList[i].size()); }
+  unsigned cell_fluid(unsigned i) const { return MPCCellListFluidParticles[i]; }
+  double get_delrx() const { return delrx; }
+  void set_delrx(double d) { delrx = d; }
+};
+
+struct RefSys {
+  Box* box = nullptr;
+  HarnessMPC* mpc = nullptr;
+  Thermostat_None* thermo = nullptr;
+};
+
+int g_probe_counter = 0;
+double probe_next() { return static_cast<double>(g_probe_counter++); }
+
+}  // namespace
+
+extern "C" {
+
+RefSys* ref_create(int Lx, int Ly, int Lz, double T, double lambda, int Nc, double shear,
+                   unsigned step_update, int amc) {
+  RefSys* s = new RefSys();
+  s->box = new Box(Lx, Ly, Lz, T, lambda);
+  s->mpc = new HarnessMPC(*s->box, T, Nc, shear, step_update, amc != 0);
+  return s;
+}
+
+void ref_destroy(RefSys* s) {
+  delete s->thermo;
+  delete s->mpc;
+  delete s->box;
+  delete s;
+}
+
+void ref_box_size(RefSys* s, int* L) {
+  for (int i = 0; i < 3; ++i) L[i] = s->box->BoxSize[i];
+}
+
+void ref_add_star(RefSys* s, unsigned A, unsigned B, unsigned arms, double mass) {
+  s->box->add_star(A, B, arms, mass);
+}
+
+void ref_make_thermostat(RefSys* s, double dt) {
+  delete s->thermo;
+  s->thermo = new Thermostat_None{*s->box, dt};
+}
+
+void ref_mpc_initialize(RefSys* s) { s->mpc->initialize(); }
+
+long ref_n_fluid(RefSys* s) { return static_cast<long>(s->mpc->Fluid.size()); }
+
+int ref_n_mono(RefSys* s) {
+  int n = 0;
+  for (auto& mol : s->box->Molecules) n += static_cast<int>(mol.Monomers.size());
+  return n;
+}
+
+void ref_get_fluid(RefSys* s, double* pos, double* vel) {
+  long i = 0;
+  for (auto& p : s->mpc->Fluid) {
+    for (int d = 0; d < 3; ++d) {
+      pos[3 * i + d] = p.Position(d);
+      vel[3 * i + d] = p.Velocity(d);
+    }
+    ++i;
+  }
+}
+
+void ref_set_fluid(RefSys* s, const double* pos, const double* vel) {
+  long i = 0;
+  for (auto& p : s->mpc->Fluid) {
+    for (int d = 0; d < 3; ++d) {
+      p.Position(d) = pos[3 * i + d];
+      p.Velocity(d) = vel[3 * i + d];
+    }
+    ++i;
+  }
+}
+
+void ref_get_monomers(RefSys* s, double* pos, double* vel, double* force, double* mass,
+                      int* amphi, int* anchor) {
+  int i = 0;
+  for (auto& mol : s->box->Molecules) {
+    for (auto& m : mol.Monomers) {
+      for (int d = 0; d < 3; ++d) {
+        if (pos) pos[3 * i + d] = m.Position(d);
+        if (vel) vel[3 * i + d] = m.Velocity(d);
+        if (force) force[3 * i + d] = m.Force(d);
+      }
+      if (mass) mass[i] = m.Mass;
+      if (amphi) amphi[i] = m.AmphiType ? 1 : 0;
+      if (anchor) anchor[i] = m.Anchor ? 1 : 0;
+      ++i;
+    }
+  }
+}
+
+// Overwrites monomer positions and velocities, then rebuilds the Verlet lists
+// and forces exactly as the Thermostat_None constructor does
+// (Thermostat_None.cpp:5-12).
+void ref_set_monomers(RefSys* s, const double* pos, const double* vel) {
+  int i = 0;
+  for (auto& mol : s->box->Molecules) {
+    for (auto& m : mol.Monomers) {
+      for (int d = 0; d < 3; ++d) {
+        m.Position(d) = pos[3 * i + d];
+        m.Velocity(d) = vel[3 * i + d];
+      }
+      ++i;
+    }
+  }
+  s->box->update_VerletLists();
+  s->box->calculate_forces_verlet();
+}
+
+// Directed FENE bonds as stored in MDParticle::Neighbors (Particle.h:57),
+// global monomer indices. Returns the number of bonds; src/dst may be null.
+int ref_get_bonds(RefSys* s, int* src, int* dst) {
+  std::vector<const MDParticle*> base;
+  int off = 0;
+  std::vector<int> mol_off;
+  for (auto& mol : s->box->Molecules) {
+    mol_off.push_back(off);
+    off += static_cast<int>(mol.Monomers.size());
+  }
+  int nb = 0;
+  int mi = 0;
+  for (auto& mol : s->box->Molecules) {
+    const MDParticle* first = mol.Monomers.data();
+    for (unsigned k = 0; k < mol.Monomers.size(); ++k) {
+      for (auto* nbp : mol.Monomers[k].Neighbors) {
+        if (src) src[nb] = mol_off[mi] + static_cast<int>(k);
+        if (dst) dst[nb] = mol_off[mi] + static_cast<int>(nbp - first);
+        ++nb;
+      }
+    }
+    ++mi;
+  }
+  return nb;
+}
+
+void ref_propagate(RefSys* s, int calc_epot) { s->thermo->propagate(calc_epot != 0); }
+
+void ref_mpc_step(RefSys* s, long t, double dt) { s->mpc->step(t, dt); }
+
+unsigned ref_n_cells(RefSys* s) { return s->mpc->cells(); }
+
+void ref_cell_counts(RefSys* s, unsigned* total, unsigned* fluid) {
+  const unsigned n = s->mpc->cells();
+  for (unsigned i = 0; i < n; ++i) {
+    if (total) total[i] = s->mpc->cell_total(i);
+    if (fluid) fluid[i] = s->mpc->cell_fluid(i);
+  }
+}
+
+double ref_delrx(RefSys* s) { return s->mpc->get_delrx(); }
+void ref_set_delrx(RefSys* s, double d) { s->mpc->set_delrx(d); }
+
+double ref_temperature(RefSys* s) { return s->mpc->calculateCurrentTemperature(); }
+
+double ref_epot(RefSys* s) {
+  double e = 0.0;
+  for (auto& mol : s->box->Molecules) e += mol.Epot;
+  return e;
+}
+
+// Box::center_of_mass_reference_frame + calculate_gyration_tensor
+// (Box.cpp:81-102, 330-353): out[0] = R_g, out[1..9] = G (column-major).
+void ref_gyration(RefSys* s, double* out) {
+  s->box->center_of_mass_reference_frame();
+  auto g = s->box->calculate_gyration_tensor();
+  out[0] = std::get<0>(g);
+  const Matrix3d& m = std::get<1>(g);
+  for (int i = 0; i < 9; ++i) out[1 + i] = m.data()[i];
+}
+
+// Runs the star-polymers.cpp loop body (lines 466/530 then 534) for
+// t = t0 .. t0+n-1 without output; used to time the reference.
+void ref_run(RefSys* s, long t0, long n, double mpc_dt, int with_md) {
+  for (long t = t0; t < t0 + n; ++t) {
+    if (with_md) s->thermo->propagate(false);
+    s->mpc->step(t, mpc_dt);
+  }
+}
+
+// Reports which draw of "Vector3d(f() - 0.5, f() - 0.5, f() - 0.5)" lands in
+// each component under this compiler (argument evaluation order is
+// unspecified in C++); MPC.cpp:123 builds the grid shift this way.
+void ref_shift_arg_order(int* order3) {
+  g_probe_counter = 0;
+  Vector3d v(probe_next() - 0.5, probe_next() - 0.5, probe_next() - 0.5);
+  for (int i = 0; i < 3; ++i) order3[i] = static_cast<int>(v(i) + 0.5);
+}
+
+}  // extern "C"

@@ -1,0 +1,847 @@
+/*
+ * smpc_oracle.c -- CPU restatement of the StarPolymersMD MD/MPC step.
+ * TEST INFRASTRUCTURE ONLY (see smpc_oracle.h). Build with -ffp-contract=off:
+ * every expression below is written in the reference's evaluation order and
+ * must not be fused.
+ *
+ * Philox stream layout (restated independently of the CUDA code):
+ *   key            = { lo32(seed), hi32(seed) }
+ *   block(c,s,k)   = Philox4x32-10(ctr = { c, lo32(s), hi32(s), k }, key)  -> w0..w3
+ *   U53(lo,hi)     = ((hi:lo) >> 11) * 2^-53 + 2^-54            (open interval)
+ *   uA = U53(w0,w1), uB = U53(w2,w3)
+ *   cell c, collision s:  block(c,s,0) -> u_phi = uA, u_theta = uB
+ *   gamma for cell c:     iteration i uses block(c,s,1+2i) for a Box-Muller
+ *                         normal z = sqrt(-2 ln uA) cos(2 pi uB) and block(c,s,2+2i)
+ *                         for the acceptance uniform uA (Marsaglia & Tsang 2000)
+ *   grid shift:           c = 0xFFFFFFFF: block(c,s,0) -> (uA-1/2, uB-1/2),
+ *                         block(c,s,1) -> uA-1/2 for z
+ * Philox4x32-10 is Salmon et al., "Parallel random numbers: as easy as 1, 2,
+ * 3" (SC'11): multipliers 0xD2511F53 / 0xCD9E8D57, Weyl key increments
+ * 0x9E3779B9 / 0xBB67AE85, ten rounds.
+ */
+#include "smpc_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+struct smpc_orc {
+  orc_params p;
+  double delrx;
+  int shear_on;
+  double rot_c, rot_s;
+  unsigned n_cell; /* NumberOfCells + 1 */
+
+  long n_f;
+  double* fx; /* [3*n_f] */
+  double* fv;
+
+  int n_m;
+  double* mx;
+  double* mv;
+  double* mf;
+  double* mxv; /* VerletPosition */
+  double* mm;  /* mass */
+  unsigned char* amphi;
+  unsigned char* anchor;
+  int n_mol;
+  int* mol_start;
+
+  int n_bond;
+  int* bsrc;
+  int* bdst;
+  int* bond_first; /* CSR over source monomer: [n_m+1] */
+
+  /* Verlet lists: CSR in the reference's list order */
+  int* vl_start;
+  int* vl_idx;
+  long vl_cap;
+  double com_pos[3];
+  double com_vel[3];
+  int cs[3];      /* Box::CellSize */
+  double csl[3];  /* Box::CellSideLength */
+  int* vcell_head; /* per Verlet cell: head of a singly linked list */
+  int* vcell_next;
+  int verlet_rebuilds;
+  double* epot_mol;
+
+  /* MPC cell lists */
+  unsigned* c_tot;
+  unsigned* c_fl;
+  unsigned* c_start;
+  long* c_mem; /* >= 0 fluid index, < 0: -(m+1) monomer index */
+
+  int rng_mode;
+  const double* inj_shift;
+  const double* inj_gamma;
+  const double* inj_uphi;
+  const double* inj_utheta;
+  uint64_t seed;
+  uint64_t step_ctr;
+
+  int err;
+};
+
+/* ------------------------------------------------------------------ Philox */
+
+static inline uint32_t mulhilo32(uint32_t a, uint32_t b, uint32_t* hi) {
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  *hi = (uint32_t)(p >> 32);
+  return (uint32_t)p;
+}
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, hi1;
+    uint32_t lo0 = mulhilo32(0xD2511F53u, c0, &hi0);
+    uint32_t lo1 = mulhilo32(0xCD9E8D57u, c2, &hi1);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n1 = lo1;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    uint32_t n3 = lo0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static inline double u53(uint32_t lo, uint32_t hi) {
+  uint64_t b = (((uint64_t)hi << 32) | (uint64_t)lo) >> 11;
+  return (double)b * 0x1.0p-53 + 0x1.0p-54;
+}
+
+static void philox_block(uint64_t seed, uint32_t cell, uint64_t step, uint32_t k, double* uA,
+                         double* uB) {
+  uint32_t ctr[4] = {cell, (uint32_t)step, (uint32_t)(step >> 32), k};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t w[4];
+  orc_philox4x32_10(ctr, key, w);
+  *uA = u53(w[0], w[1]);
+  if (uB) *uB = u53(w[2], w[3]);
+}
+
+double orc_philox_gamma(uint64_t seed, uint64_t step, uint32_t cell, double shape) {
+  const double d = shape - 1.0 / 3.0;
+  const double c = 1.0 / sqrt(9.0 * d);
+  for (uint32_t it = 0; it < 64; ++it) {
+    double a, b, u;
+    philox_block(seed, cell, step, 1u + 2u * it, &a, &b);
+    const double x = sqrt(-2.0 * log(a)) * cos(2.0 * M_PI * b);
+    double v = 1.0 + c * x;
+    if (v <= 0.0) continue;
+    v = v * v * v;
+    philox_block(seed, cell, step, 2u + 2u * it, &u, NULL);
+    const double x2 = x * x;
+    if (u < 1.0 - 0.0331 * (x2 * x2)) return d * v;
+    if (log(u) < 0.5 * x2 + d * (1.0 - v + log(v))) return d * v;
+  }
+  return d;
+}
+
+/* --------------------------------------------------------------- potentials
+ * Potentials.h:14-120, evaluation order kept. */
+
+static inline double fene_force(double r2) { return -30.0 / (1.0 - (r2 / 2.25)); }
+static inline double fene_anchor_force(double r2) { return -30.0 / (1.0 - (r2 / 20.25)); }
+static inline double fene_pot(double r2) { return -15.0 * 2.25 * log(1.0 - r2 / 2.25); }
+static inline double fene_anchor_pot(double r2) { return -15.0 * 20.25 * log(1.0 - r2 / 20.25); }
+
+static inline double aa_force(double r2) {
+  double force = 0.0;
+  if (r2 < 1.0594631) {
+    double rm2 = 1.0 / r2;
+    double rm24 = rm2 * rm2 * rm2;
+    rm24 *= rm24;
+    rm24 *= rm24;
+    force = 192.0 * rm2 * rm24 * (rm24 - 0.5);
+  }
+  return force;
+}
+
+static inline double aa_pot(double r2) {
+  double pot = 0.0;
+  if (r2 < 1.0594631) {
+    double rm24 = 1.0 / r2;
+    rm24 *= rm24 * rm24;
+    rm24 *= rm24;
+    rm24 *= rm24;
+    pot = 4.0 * rm24 * (rm24 - 1.0) + 1.0;
+  }
+  return pot;
+}
+
+static inline double bb_force(double r2, double lambda) {
+  double force = 0.0;
+  if (r2 < 1.0594631) {
+    double rm2 = 1.0 / r2;
+    double rm24 = rm2 * rm2 * rm2;
+    rm24 *= rm24;
+    rm24 *= rm24;
+    force = 192.0 * rm2 * rm24 * (rm24 - 0.5);
+  } else if (r2 < 2.25) {
+    double rm2 = 1.0 / r2;
+    double rm24 = rm2 * rm2 * rm2;
+    rm24 *= rm24;
+    rm24 *= rm24;
+    force = 192.0 * lambda * rm2 * rm24 * (rm24 - 0.5);
+  }
+  return force;
+}
+
+static inline double bb_pot(double r2, double lambda) {
+  double pot = 0.0;
+  if (r2 < 1.0594631) {
+    double rm24 = 1.0 / r2;
+    rm24 *= rm24 * rm24;
+    rm24 *= rm24;
+    rm24 *= rm24;
+    pot = 4.0 * rm24 * (rm24 - 1.0) + 1.0 - lambda;
+  } else if (r2 < 2.25) {
+    double rm24 = 1.0 / r2;
+    rm24 *= rm24 * rm24;
+    rm24 *= rm24;
+    rm24 *= rm24;
+    pot = 4.0 * lambda * (rm24 * (rm24 - 1.0) - 0.0000593);
+  }
+  return pot;
+}
+
+/* 12-6 preset used by the benchmark configurations: WCA core (r_c = 2^(1/6))
+ * for every pair, plus lambda-scaled LJ attraction out to r = 2.5 for BB pairs
+ * (potential shifted to zero at 2.5). Same functional form as the reference's
+ * 48-24 pair (Potentials.h:57-120) with exponents 12/6. */
+static inline double lj_force_core(double r2) {
+  double rm2 = 1.0 / r2;
+  double rm6 = rm2 * rm2 * rm2;
+  return 48.0 * rm2 * rm6 * (rm6 - 0.5);
+}
+static inline double lj_pot_core(double r2) {
+  double rm6 = 1.0 / r2;
+  rm6 *= rm6 * rm6;
+  return 4.0 * rm6 * (rm6 - 1.0);
+}
+#define LJ126_RC2_REP 1.2599210498948732 /* 2^(1/3) */
+#define LJ126_RC2_ATT 6.25
+#define LJ126_SHIFT (-0.016316891136)    /* 4 (2.5^-12 - 2.5^-6) */
+
+static inline double pair_force(int pot, int bb, double r2, double lambda) {
+  if (pot == ORC_POT_REF4824) return bb ? bb_force(r2, lambda) : aa_force(r2);
+  if (r2 < LJ126_RC2_REP) return lj_force_core(r2);
+  if (bb && r2 < LJ126_RC2_ATT) return lambda * lj_force_core(r2);
+  return 0.0;
+}
+static inline double pair_pot(int pot, int bb, double r2, double lambda) {
+  if (pot == ORC_POT_REF4824) return bb ? bb_pot(r2, lambda) : aa_pot(r2);
+  if (r2 < LJ126_RC2_REP) return lj_pot_core(r2) + 1.0 - (bb ? lambda : 0.0);
+  if (bb && r2 < LJ126_RC2_ATT) return lambda * (lj_pot_core(r2) - LJ126_SHIFT);
+  return 0.0;
+}
+
+/* ------------------------------------------------------------------ set-up */
+
+smpc_orc* orc_create(const orc_params* p, long n_fluid, int n_mono, int n_mol,
+                     const int* mol_start) {
+  smpc_orc* o = (smpc_orc*)calloc(1, sizeof(smpc_orc));
+  if (!o) return NULL;
+  o->p = *p;
+  o->shear_on = (p->shear != 0.0);
+  o->rot_c = cos(130.0 * M_PI / 180.0); /* MPC.cpp:23-24 */
+  o->rot_s = sin(130.0 * M_PI / 180.0);
+  o->n_cell = (unsigned)(p->L[0] * p->L[1] * p->L[2]);
+  o->n_f = n_fluid;
+  o->n_m = n_mono;
+  o->fx = (double*)calloc((size_t)(3 * n_fluid + 3), sizeof(double));
+  o->fv = (double*)calloc((size_t)(3 * n_fluid + 3), sizeof(double));
+  size_t m3 = (size_t)(3 * n_mono + 3);
+  o->mx = (double*)calloc(m3, sizeof(double));
+  o->mv = (double*)calloc(m3, sizeof(double));
+  o->mf = (double*)calloc(m3, sizeof(double));
+  o->mxv = (double*)calloc(m3, sizeof(double));
+  o->mm = (double*)calloc((size_t)n_mono + 1, sizeof(double));
+  o->amphi = (unsigned char*)calloc((size_t)n_mono + 1, 1);
+  o->anchor = (unsigned char*)calloc((size_t)n_mono + 1, 1);
+  o->n_mol = n_mol;
+  o->mol_start = (int*)calloc((size_t)n_mol + 1, sizeof(int));
+  if (mol_start) memcpy(o->mol_start, mol_start, sizeof(int) * (size_t)(n_mol + 1));
+  o->epot_mol = (double*)calloc((size_t)n_mol + 1, sizeof(double));
+  o->vl_start = (int*)calloc((size_t)n_mono + 1, sizeof(int));
+  o->vl_cap = 64L * (n_mono + 1);
+  o->vl_idx = (int*)malloc(sizeof(int) * (size_t)o->vl_cap);
+  o->vcell_next = (int*)malloc(sizeof(int) * (size_t)(n_mono + 1));
+  o->bond_first = (int*)calloc((size_t)n_mono + 2, sizeof(int));
+  /* Box.cpp:20-25: Verlet cell grid of int(L/VerletRadius) cells per axis. */
+  long ncv = 1;
+  for (int d = 0; d < 3; ++d) {
+    o->cs[d] = (int)(p->L[d] / 2.0);
+    if (o->cs[d] < 1) o->cs[d] = 1;
+    o->csl[d] = p->L[d] / (double)o->cs[d];
+    ncv *= o->cs[d];
+  }
+  o->vcell_head = (int*)malloc(sizeof(int) * (size_t)ncv);
+  o->c_tot = (unsigned*)calloc(o->n_cell, sizeof(unsigned));
+  o->c_fl = (unsigned*)calloc(o->n_cell, sizeof(unsigned));
+  o->c_start = (unsigned*)calloc((size_t)o->n_cell + 1, sizeof(unsigned));
+  o->c_mem = (long*)malloc(sizeof(long) * (size_t)(n_fluid + n_mono + 1));
+  if (!o->fx || !o->fv || !o->mx || !o->vl_idx || !o->vcell_head || !o->c_mem) o->err |= ORC_ERR_ALLOC;
+  o->rng_mode = ORC_RNG_INJECT;
+  return o;
+}
+
+void orc_destroy(smpc_orc* o) {
+  if (!o) return;
+  free(o->fx); free(o->fv); free(o->mx); free(o->mv); free(o->mf); free(o->mxv); free(o->mm);
+  free(o->amphi); free(o->anchor); free(o->mol_start); free(o->epot_mol);
+  free(o->bsrc); free(o->bdst); free(o->bond_first); free(o->vl_start); free(o->vl_idx);
+  free(o->vcell_head); free(o->vcell_next); free(o->c_tot); free(o->c_fl); free(o->c_start);
+  free(o->c_mem);
+  free(o);
+}
+
+int orc_error(const smpc_orc* o) { return o->err; }
+void orc_clear_error(smpc_orc* o) { o->err = 0; }
+
+void orc_set_fluid(smpc_orc* o, const double* pos, const double* vel) {
+  memcpy(o->fx, pos, sizeof(double) * 3 * (size_t)o->n_f);
+  memcpy(o->fv, vel, sizeof(double) * 3 * (size_t)o->n_f);
+}
+void orc_get_fluid(const smpc_orc* o, double* pos, double* vel) {
+  if (pos) memcpy(pos, o->fx, sizeof(double) * 3 * (size_t)o->n_f);
+  if (vel) memcpy(vel, o->fv, sizeof(double) * 3 * (size_t)o->n_f);
+}
+
+void orc_set_monomers(smpc_orc* o, const double* pos, const double* vel, const double* force,
+                      const double* mass, const int* amphi, const int* anchor) {
+  size_t n3 = sizeof(double) * 3 * (size_t)o->n_m;
+  if (pos) memcpy(o->mx, pos, n3);
+  if (vel) memcpy(o->mv, vel, n3);
+  if (force) memcpy(o->mf, force, n3);
+  for (int i = 0; i < o->n_m; ++i) {
+    if (mass) o->mm[i] = mass[i];
+    if (amphi) o->amphi[i] = (unsigned char)(amphi[i] != 0);
+    if (anchor) o->anchor[i] = (unsigned char)(anchor[i] != 0);
+  }
+}
+
+void orc_get_monomers(const smpc_orc* o, double* pos, double* vel, double* force) {
+  size_t n3 = sizeof(double) * 3 * (size_t)o->n_m;
+  if (pos) memcpy(pos, o->mx, n3);
+  if (vel) memcpy(vel, o->mv, n3);
+  if (force) memcpy(force, o->mf, n3);
+}
+
+void orc_set_bonds(smpc_orc* o, int n_bond, const int* src, const int* dst) {
+  free(o->bsrc);
+  free(o->bdst);
+  o->n_bond = n_bond;
+  o->bsrc = (int*)malloc(sizeof(int) * (size_t)(n_bond + 1));
+  o->bdst = (int*)malloc(sizeof(int) * (size_t)(n_bond + 1));
+  memset(o->bond_first, 0, sizeof(int) * (size_t)(o->n_m + 2));
+  /* Bonds arrive grouped by source monomer in Neighbors order. */
+  for (int b = 0; b < n_bond; ++b) {
+    o->bsrc[b] = src[b];
+    o->bdst[b] = dst[b];
+    o->bond_first[src[b] + 1]++;
+  }
+  for (int i = 0; i < o->n_m; ++i) o->bond_first[i + 1] += o->bond_first[i];
+}
+
+double orc_delrx(const smpc_orc* o) { return o->delrx; }
+void orc_set_delrx(smpc_orc* o, double d) { o->delrx = d; }
+
+void orc_set_inject(smpc_orc* o, const double* shift3, const double* gamma, const double* u_phi,
+                    const double* u_theta) {
+  o->rng_mode = ORC_RNG_INJECT;
+  o->inj_shift = shift3;
+  o->inj_gamma = gamma;
+  o->inj_uphi = u_phi;
+  o->inj_utheta = u_theta;
+}
+
+void orc_set_philox(smpc_orc* o, uint64_t seed, uint64_t collision_counter) {
+  o->rng_mode = ORC_RNG_PHILOX;
+  o->seed = seed;
+  o->step_ctr = collision_counter;
+}
+uint64_t orc_collision_counter(const smpc_orc* o) { return o->step_ctr; }
+
+/* -------------------------------------------------------- Box: Verlet/MD */
+
+/* Box::center_of_mass_reference_frame (Box.cpp:81-102): only the COM of
+ * molecule 0 is kept (COM_Pos / COM_Vel). */
+static void com_frame(smpc_orc* o) {
+  if (o->n_mol < 1) return;
+  double c[3] = {0, 0, 0}, cv[3] = {0, 0, 0};
+  int b = o->mol_start[0], e = o->mol_start[1];
+  for (int i = b; i < e; ++i) {
+    for (int d = 0; d < 3; ++d) {
+      c[d] += o->mx[3 * i + d];
+      cv[d] += o->mv[3 * i + d];
+    }
+  }
+  unsigned n = (unsigned)(e - b);
+  for (int d = 0; d < 3; ++d) {
+    o->com_pos[d] = c[d] / n;
+    o->com_vel[d] = cv[d] / n;
+  }
+}
+
+static inline int vcell_of(const smpc_orc* o, int i, int* cn) {
+  for (int d = 0; d < 3; ++d)
+    cn[d] = (int)((o->mx[3 * i + d] - o->com_pos[d] + o->p.L[d] * 0.5) / o->csl[d]);
+  return !(cn[0] < 0 || cn[0] >= o->cs[0] || cn[1] < 0 || cn[1] >= o->cs[1] || cn[2] < 0 ||
+           cn[2] >= o->cs[2]);
+}
+
+/* Box::update_VerletLists (Box.cpp:105-180). Cell contents are forward_lists
+ * filled with push_front and each VerletList is filled with push_front, so
+ * the final list order is the reverse of the traversal order; that order is
+ * reproduced here so force sums match bit for bit. */
+static void update_verlet(smpc_orc* o) {
+  o->verlet_rebuilds++;
+  const int n = o->n_m;
+  const long ncv = (long)o->cs[0] * o->cs[1] * o->cs[2];
+  for (long c = 0; c < ncv; ++c) o->vcell_head[c] = -1;
+  com_frame(o);
+  int cn[3];
+  for (int i = 0; i < n; ++i) {
+    if (!vcell_of(o, i, cn)) {
+      o->err |= ORC_ERR_VERLET_CELL;
+      continue;
+    }
+    for (int d = 0; d < 3; ++d) o->mxv[3 * i + d] = o->mx[3 * i + d];
+    long c = ((long)cn[0] * o->cs[1] + cn[1]) * o->cs[2] + cn[2];
+    o->vcell_next[i] = o->vcell_head[c]; /* push_front */
+    o->vcell_head[c] = i;
+  }
+  const double rv2 = o->p.r_verlet * o->p.r_verlet;
+  long fill = 0;
+  int* tmp = (int*)malloc(sizeof(int) * (size_t)(n + 1));
+  for (int i = 0; i < n; ++i) {
+    o->vl_start[i] = (int)fill;
+    int cnt = 0;
+    if (vcell_of(o, i, cn)) {
+      for (int j = cn[0] - 1; j < cn[0] + 2; ++j) {
+        if (j < 0 || j >= o->cs[0]) continue;
+        for (int k = cn[1] - 1; k < cn[1] + 2; ++k) {
+          if (k < 0 || k >= o->cs[1]) continue;
+          for (int l = cn[2] - 1; l < cn[2] + 2; ++l) {
+            if (l < 0 || l >= o->cs[2]) continue;
+            long c = ((long)j * o->cs[1] + k) * o->cs[2] + l;
+            for (int q = o->vcell_head[c]; q >= 0; q = o->vcell_next[q]) {
+              if (q == i) continue;
+              double dx = o->mx[3 * q] - o->mx[3 * i];
+              double dy = o->mx[3 * q + 1] - o->mx[3 * i + 1];
+              double dz = o->mx[3 * q + 2] - o->mx[3 * i + 2];
+              double r2 = (dx * dx + dy * dy) + dz * dz;
+              if (r2 <= rv2) tmp[cnt++] = q;
+            }
+          }
+        }
+      }
+    }
+    if (fill + cnt > o->vl_cap) {
+      o->vl_cap = 2 * (fill + cnt) + 64;
+      o->vl_idx = (int*)realloc(o->vl_idx, sizeof(int) * (size_t)o->vl_cap);
+    }
+    for (int t = cnt - 1; t >= 0; --t) o->vl_idx[fill++] = tmp[t]; /* push_front order */
+  }
+  o->vl_start[n] = (int)fill;
+  free(tmp);
+}
+
+/* Box::check_VerletLists (Box.cpp:182-194). */
+static void check_verlet(smpc_orc* o) {
+  const double lim = (o->p.r_verlet - o->p.r_cut) * 0.5;
+  for (int i = 0; i < o->n_m; ++i) {
+    double dx = o->mx[3 * i] - o->mxv[3 * i];
+    double dy = o->mx[3 * i + 1] - o->mxv[3 * i + 1];
+    double dz = o->mx[3 * i + 2] - o->mxv[3 * i + 2];
+    if (sqrt((dx * dx + dy * dy) + dz * dz) > lim) {
+      update_verlet(o);
+      return;
+    }
+  }
+}
+
+/* Box::calculate_forces_verlet (Box.cpp:243-286). */
+static void forces_verlet(smpc_orc* o, int calc_epot) {
+  for (int m = 0; m < o->n_mol; ++m) o->epot_mol[m] = 0.0;
+  for (int i = 0; i < 3 * o->n_m; ++i) o->mf[i] = o->mf[i] * 0.0;
+  const double lambda = o->p.lambda;
+  const int pot = o->p.potential;
+  for (int m = 0; m < o->n_mol; ++m) {
+    double ep = 0.0;
+    for (int i = o->mol_start[m]; i < o->mol_start[m + 1]; ++i) {
+      double* fi = o->mf + 3 * i;
+      const double* xi = o->mx + 3 * i;
+      for (int t = o->vl_start[i]; t < o->vl_start[i + 1]; ++t) {
+        const int j = o->vl_idx[t];
+        const double* xj = o->mx + 3 * j;
+        double d0 = xj[0] - xi[0], d1 = xj[1] - xi[1], d2 = xj[2] - xi[2];
+        double r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+        int bb = (o->amphi[i] == 1 && o->amphi[j] == 1);
+        if (calc_epot) ep += 0.5 * pair_pot(pot, bb, r2, lambda);
+        double fa = pair_force(pot, bb, r2, lambda);
+        fi[0] -= d0 * fa;
+        fi[1] -= d1 * fa;
+        fi[2] -= d2 * fa;
+      }
+      for (int b = o->bond_first[i]; b < o->bond_first[i + 1]; ++b) {
+        const int j = o->bdst[b];
+        const double* xj = o->mx + 3 * j;
+        double d0 = xj[0] - xi[0], d1 = xj[1] - xi[1], d2 = xj[2] - xi[2];
+        double r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+        double fa;
+        if (o->anchor[i]) {
+          if (calc_epot) ep += fene_anchor_pot(r2);
+          fa = fene_anchor_force(r2);
+        } else {
+          if (calc_epot) ep += fene_pot(r2);
+          fa = fene_force(r2);
+        }
+        double f0 = d0 * fa, f1 = d1 * fa, f2 = d2 * fa;
+        fi[0] -= f0;
+        fi[1] -= f1;
+        fi[2] -= f2;
+        o->mf[3 * j] += f0;
+        o->mf[3 * j + 1] += f1;
+        o->mf[3 * j + 2] += f2;
+      }
+    }
+    o->epot_mol[m] = ep;
+  }
+}
+
+void orc_init_md(smpc_orc* o) {
+  update_verlet(o);
+  forces_verlet(o, 0);
+}
+
+/* Thermostat_None::propagate (Thermostat_None.cpp:21-38). */
+void orc_propagate(smpc_orc* o, int calc_epot) {
+  const double dt = o->p.md_dt;
+  const double dth = dt * 0.50;
+  for (int i = 0; i < o->n_m; ++i) {
+    for (int d = 0; d < 3; ++d) {
+      o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
+      o->mx[3 * i + d] += o->mv[3 * i + d] * dt;
+    }
+  }
+  check_verlet(o);
+  forces_verlet(o, calc_epot);
+  for (int i = 0; i < o->n_m; ++i)
+    for (int d = 0; d < 3; ++d) o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
+}
+
+double orc_epot(const smpc_orc* o) {
+  double e = 0.0;
+  for (int m = 0; m < o->n_mol; ++m) e += o->epot_mol[m];
+  return e;
+}
+
+int orc_verlet_rebuilds(const smpc_orc* o) { return o->verlet_rebuilds; }
+
+/* ----------------------------------------------------------------- MPC */
+
+/* MPC::LEBC (MPC.cpp:421-429) and MPC::wrap(Particle&) (MPC.cpp:487-490). */
+static inline void wrap_particle(const smpc_orc* o, double* x, double* v) {
+  const double Lx = o->p.L[0], Ly = o->p.L[1], Lz = o->p.L[2];
+  if (o->shear_on) {
+    double cy = round(x[1] / Ly);
+    x[0] -= Lx * round(x[0] / Lx);
+    x[0] -= cy * o->delrx;
+    x[0] -= Lx * round(x[0] / Lx);
+    x[1] -= Ly * cy;
+    x[2] -= Lz * round(x[2] / Lz);
+    v[0] -= cy * o->p.shear * Ly;
+  } else {
+    x[0] -= round(x[0] / Lx) * Lx;
+    x[1] -= round(x[1] / Ly) * Ly;
+    x[2] -= round(x[2] / Lz) * Lz;
+  }
+}
+
+/* MPC::check_bounds (MPC.cpp:160-190). */
+static void check_bounds(smpc_orc* o) {
+  int out = 0;
+  for (int i = 0; i < o->n_m && !out; ++i)
+    for (int d = 0; d < 3; ++d)
+      if (fabs(o->mx[3 * i + d]) >= (o->p.L[d] * 0.5 - 0.5)) {
+        out = 1;
+        break;
+      }
+  if (!out || o->n_mol < 1) return;
+  double com[3] = {0, 0, 0}, comv[3] = {0, 0, 0};
+  int b = o->mol_start[0], e = o->mol_start[1];
+  for (int i = b; i < e; ++i)
+    for (int d = 0; d < 3; ++d) {
+      com[d] += o->mx[3 * i + d];
+      comv[d] += o->mv[3 * i + d];
+    }
+  unsigned n = (unsigned)(e - b);
+  for (int d = 0; d < 3; ++d) {
+    com[d] /= n;
+    comv[d] /= n;
+  }
+  for (int i = 0; i < o->n_m; ++i)
+    for (int d = 0; d < 3; ++d) {
+      o->mx[3 * i + d] -= com[d];
+      o->mv[3 * i + d] -= comv[d];
+    }
+  for (long i = 0; i < o->n_f; ++i) {
+    for (int d = 0; d < 3; ++d) {
+      o->fx[3 * i + d] -= com[d];
+      o->fv[3 * i + d] -= comv[d];
+    }
+    wrap_particle(o, o->fx + 3 * i, o->fv + 3 * i);
+  }
+}
+
+/* MPC::sort cell index formula (MPC.cpp:209,225). */
+static inline unsigned cell_index(const smpc_orc* o, const double* x) {
+  const int Lx = o->p.L[0], Ly = o->p.L[1], Lz = o->p.L[2];
+  int c = (int)(x[0] + Lx * 0.5) + Lx * (int)(x[1] + Ly * 0.5) + Lx * Ly * (int)(x[2] + Lz * 0.5);
+  return (unsigned)c;
+}
+
+/* MPC::sort (MPC.cpp:201-237) as a stable counting sort: per cell, fluid in
+ * Fluid order then monomers in molecule order, exactly the push_back order. */
+static void mpc_sort(smpc_orc* o) {
+  const unsigned nc = o->n_cell;
+  const unsigned last = nc - 1; /* NumberOfCells */
+  memset(o->c_tot, 0, sizeof(unsigned) * nc);
+  memset(o->c_fl, 0, sizeof(unsigned) * nc);
+  unsigned* key = (unsigned*)malloc(sizeof(unsigned) * (size_t)(o->n_f + o->n_m + 1));
+  for (long i = 0; i < o->n_f; ++i) {
+    unsigned c = cell_index(o, o->fx + 3 * i);
+    key[i] = c;
+    if (c > last) {
+      o->err |= ORC_ERR_FLUID_CELL;
+      continue;
+    }
+    o->c_tot[c]++;
+    o->c_fl[c]++;
+  }
+  for (int m = 0; m < o->n_m; ++m) {
+    unsigned c = cell_index(o, o->mx + 3 * m);
+    key[o->n_f + m] = c;
+    if (c > last) {
+      o->err |= ORC_ERR_MONO_CELL;
+      continue;
+    }
+    o->c_tot[c]++;
+  }
+  unsigned acc = 0;
+  for (unsigned c = 0; c < nc; ++c) {
+    o->c_start[c] = acc;
+    acc += o->c_tot[c];
+  }
+  o->c_start[nc] = acc;
+  unsigned* fillp = (unsigned*)malloc(sizeof(unsigned) * nc);
+  memcpy(fillp, o->c_start, sizeof(unsigned) * nc);
+  for (long i = 0; i < o->n_f; ++i)
+    if (key[i] <= last) o->c_mem[fillp[key[i]]++] = i;
+  for (int m = 0; m < o->n_m; ++m)
+    if (key[o->n_f + m] <= last) o->c_mem[fillp[key[o->n_f + m]]++] = -(long)m - 1;
+  free(fillp);
+  free(key);
+}
+
+static inline double* pvel(smpc_orc* o, long id) {
+  return id >= 0 ? o->fv + 3 * id : o->mv + 3 * (-id - 1);
+}
+static inline double pmass(const smpc_orc* o, long id) {
+  return id >= 0 ? 1.0 : o->mm[-id - 1];
+}
+
+/* MPC::calculateCMV (MPC.cpp:314-322). */
+static void cell_cmv(smpc_orc* o, unsigned c, double* cmv) {
+  cmv[0] = cmv[1] = cmv[2] = 0.0;
+  double tm = 0.0;
+  for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
+    long id = o->c_mem[k];
+    const double* v = pvel(o, id);
+    double m = pmass(o, id);
+    cmv[0] += v[0] * m;
+    cmv[1] += v[1] * m;
+    cmv[2] += v[2] * m;
+    tm += m;
+  }
+  if (tm > 0) {
+    cmv[0] /= tm;
+    cmv[1] /= tm;
+    cmv[2] /= tm;
+  }
+}
+
+/* MPC::thermostat (MPC.cpp:273-299). */
+static void cell_thermostat(smpc_orc* o, unsigned c, const double* cmv) {
+  double ekin = 0.0;
+  unsigned count = 0;
+  for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
+    long id = o->c_mem[k];
+    const double* v = pvel(o, id);
+    double d0 = v[0] - cmv[0], d1 = v[1] - cmv[1], d2 = v[2] - cmv[2];
+    ekin += pmass(o, id) * ((d0 * d0 + d1 * d1) + d2 * d2);
+    count++;
+  }
+  if (count < 2) return;
+  ekin *= 0.5;
+  double g;
+  if (o->rng_mode == ORC_RNG_INJECT) {
+    g = o->inj_gamma ? o->inj_gamma[c] * 1.0 : 0.0;
+    /* injected values are Gamma(1.5(n-1), kT) variates as drawn */
+  } else {
+    g = orc_philox_gamma(o->seed, o->step_ctr, c, 1.5 * (count - 1)) * o->p.kT;
+  }
+  double scaling = sqrt(g / ekin);
+  for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
+    double* v = pvel(o, o->c_mem[k]);
+    for (int d = 0; d < 3; ++d) v[d] = scaling * v[d] + (1 - scaling) * cmv[d];
+  }
+}
+
+/* MPC::collide (MPC.cpp:239-270), angular-momentum variant off. */
+static void cell_collide(smpc_orc* o, unsigned c, const double* cmv) {
+  double uphi, uth;
+  if (o->rng_mode == ORC_RNG_INJECT) {
+    uphi = o->inj_uphi[c];
+    uth = o->inj_utheta[c];
+  } else {
+    philox_block(o->seed, c, o->step_ctr, 0u, &uphi, &uth);
+  }
+  const double phi = 2. * M_PI * (uphi);
+  const double theta = 2. * (uth - 0.5);
+  double a[3];
+  a[0] = sqrt(1 - theta * theta) * cos(phi);
+  a[1] = sqrt(1 - theta * theta) * sin(phi);
+  a[2] = theta;
+  const double cc = o->rot_c, ss = o->rot_s;
+  double R[3][3];
+  R[0][0] = a[0] * a[0] + (1 - a[0] * a[0]) * cc;
+  R[0][1] = a[0] * a[1] * (1 - cc) - a[2] * ss;
+  R[0][2] = a[0] * a[2] * (1 - cc) + a[1] * ss;
+  R[1][0] = a[0] * a[1] * (1 - cc) + a[2] * ss;
+  R[1][1] = a[1] * a[1] + (1 - a[1] * a[1]) * cc;
+  R[1][2] = a[1] * a[2] * (1 - cc) - a[0] * ss;
+  R[2][0] = a[0] * a[2] * (1 - cc) - a[1] * ss;
+  R[2][1] = a[1] * a[2] * (1 - cc) + a[0] * ss;
+  R[2][2] = a[2] * a[2] + (1 - a[2] * a[2]) * cc;
+  for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
+    double* v = pvel(o, o->c_mem[k]);
+    double d0 = v[0] - cmv[0], d1 = v[1] - cmv[1], d2 = v[2] - cmv[2];
+    double r0 = (R[0][0] * d0 + R[0][1] * d1) + R[0][2] * d2;
+    double r1 = (R[1][0] * d0 + R[1][1] * d1) + R[1][2] * d2;
+    double r2 = (R[2][0] * d0 + R[2][1] * d1) + R[2][2] * d2;
+    v[0] = cmv[0] + r0;
+    v[1] = cmv[1] + r1;
+    v[2] = cmv[2] + r2;
+  }
+}
+
+/* MPC::shiftParticles (MPC.cpp:301-311). */
+static void shift_particles(smpc_orc* o, const double* s) {
+  for (long i = 0; i < o->n_f; ++i) {
+    double* x = o->fx + 3 * i;
+    x[0] += s[0];
+    x[1] += s[1];
+    x[2] += s[2];
+    wrap_particle(o, x, o->fv + 3 * i);
+  }
+  for (int m = 0; m < o->n_m; ++m) {
+    double* x = o->mx + 3 * m;
+    x[0] += s[0];
+    x[1] += s[1];
+    x[2] += s[2];
+  }
+}
+
+/* MPC::step (MPC.cpp:116-142). */
+void orc_mpc_step(smpc_orc* o, long t, double dt) {
+  o->delrx += o->p.shear * o->p.L[1] * (dt * o->p.delrx_dt_scale);
+  o->delrx -= o->p.L[0] * round(o->delrx / o->p.L[0]);
+  if (t % (long)o->p.step_update) return;
+  check_bounds(o);
+  for (long i = 0; i < o->n_f; ++i) { /* MPC::streaming (MPC.cpp:192-197) */
+    double* x = o->fx + 3 * i;
+    const double* v = o->fv + 3 * i;
+    x[0] += v[0] * dt;
+    x[1] += v[1] * dt;
+    x[2] += v[2] * dt;
+    wrap_particle(o, x, o->fv + 3 * i);
+  }
+  double shift[3];
+  if (o->rng_mode == ORC_RNG_INJECT) {
+    if (!o->inj_shift || !o->inj_uphi || !o->inj_utheta) {
+      o->err |= ORC_ERR_INJECT;
+      return;
+    }
+    for (int d = 0; d < 3; ++d) shift[d] = o->inj_shift[d];
+  } else {
+    double a, b, c;
+    philox_block(o->seed, 0xFFFFFFFFu, o->step_ctr, 0u, &a, &b);
+    philox_block(o->seed, 0xFFFFFFFFu, o->step_ctr, 1u, &c, NULL);
+    shift[0] = a - 0.5;
+    shift[1] = b - 0.5;
+    shift[2] = c - 0.5;
+  }
+  shift_particles(o, shift);
+  mpc_sort(o);
+  for (unsigned c = 0; c < o->n_cell; ++c) {
+    double cmv[3];
+    cell_cmv(o, c, cmv);
+    cell_thermostat(o, c, cmv);
+    cell_collide(o, c, cmv);
+  }
+  shift[0] = -shift[0];
+  shift[1] = -shift[1];
+  shift[2] = -shift[2];
+  shift_particles(o, shift);
+  if (o->rng_mode == ORC_RNG_PHILOX) o->step_ctr++;
+}
+
+void orc_run(smpc_orc* o, long t0, long n, double mpc_dt, int with_md) {
+  for (long t = t0; t < t0 + n; ++t) {
+    if (with_md) orc_propagate(o, 0);
+    orc_mpc_step(o, t, mpc_dt);
+  }
+}
+
+/* MPC::calculateEkinInCell / EkinTotal / CurrentTemperature / filledCells
+ * (MPC.cpp:384-418) on the cell lists of the last collision. */
+double orc_temperature(smpc_orc* o) {
+  double ekin_tot = 0.0;
+  unsigned filled = 0;
+  for (unsigned c = 0; c < o->n_cell; ++c) {
+    double cmv[3];
+    cell_cmv(o, c, cmv);
+    double ekin = 0.0;
+    unsigned nfl = o->c_fl[c];
+    for (unsigned k = 0; k < nfl; ++k) {
+      long id = o->c_mem[o->c_start[c] + k];
+      const double* v = pvel(o, id);
+      double d0 = v[0] - cmv[0], d1 = v[1] - cmv[1], d2 = v[2] - cmv[2];
+      ekin += pmass(o, id) * ((d0 * d0 + d1 * d1) + d2 * d2);
+    }
+    ekin *= 0.5;
+    ekin_tot += ekin;
+    if (nfl > 0) filled++;
+  }
+  return 2. * ekin_tot / (3. * (unsigned)((unsigned)o->n_f - filled));
+}
+
+unsigned orc_n_cells(const smpc_orc* o) { return o->n_cell; }
+
+void orc_cell_counts(const smpc_orc* o, unsigned* total, unsigned* fluid) {
+  for (unsigned c = 0; c < o->n_cell; ++c) {
+    if (total) total[c] = o->c_tot[c];
+    if (fluid) fluid[c] = o->c_fl[c];
+  }
+}

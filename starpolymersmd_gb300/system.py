@@ -1,0 +1,179 @@
+"""System construction: star topology, initial conditions and replica tables.
+
+Index layout and bond order follow the reference's star builder
+(star-polymers/lib/Molecules/Molecule.cpp:126-176): the core (anchor) is
+monomer 0; bead k (1..A+B) of arm a is monomer a*(A+B)+k; beads with k > A are
+solvophobic (AmphiType 1); the directed FENE bonds are core -> first bead of
+every arm (stored by MDParticle::set_neighbor with push_front, so the core
+lists its arms in reverse order, Particle.cpp:38-40) and bead k -> bead k+1.
+"""
+from __future__ import annotations
+
+import dataclasses
+import json
+import math
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Star:
+    """Topology and state of one star polymer (reference index layout)."""
+    arms: int
+    A: int
+    B: int
+    mass: float
+    pos: np.ndarray          # (N, 3)
+    vel: np.ndarray          # (N, 3)
+    amphi: np.ndarray        # (N,) int32, 1 = solvophobic
+    anchor: np.ndarray       # (N,) int32, 1 = core
+    bond_src: np.ndarray     # directed bonds (MDParticle::Neighbors order)
+    bond_dst: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return 1 + self.arms * (self.A + self.B)
+
+
+def star_topology(arms: int, A: int, B: int):
+    """Types, anchor flags and directed bonds of a star (Molecule.cpp:126-176)."""
+    npa = A + B
+    n = 1 + arms * npa
+    amphi = np.zeros(n, dtype=np.int32)
+    anchor = np.zeros(n, dtype=np.int32)
+    anchor[0] = 1
+    src, dst = [], []
+    # core -> first bead of each arm, pushed to the front: reverse arm order
+    for a in reversed(range(arms)):
+        src.append(0)
+        dst.append(a * npa + 1)
+    for a in range(arms):
+        for k in range(1, npa + 1):
+            idx = a * npa + k
+            if k > A:
+                amphi[idx] = 1
+            if k < npa:
+                src.append(idx)
+                dst.append(idx + 1)
+    # group by source monomer, keeping per-source order (Neighbors lists)
+    order = sorted(range(len(src)), key=lambda b: (src[b], b))
+    return (amphi, anchor, np.array([src[b] for b in order], dtype=np.int32),
+            np.array([dst[b] for b in order], dtype=np.int32))
+
+
+def saw_star(arms: int, n_arm: int, rng: np.random.Generator, bond: float = 1.0,
+             anchor_bond: float = 2.0, r_min: float = 1.0, max_tries: int = 5000,
+             centre=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Self-avoiding random-walk star grown from ``centre``.
+
+    Each arm starts ``anchor_bond`` from the core in a random direction and
+    adds beads at distance ``bond``; a bead is accepted when it is farther
+    than ``r_min`` from every bead placed so far.
+    """
+    pos = [np.asarray(centre, dtype=np.float64)]
+    P = np.zeros((1 + arms * n_arm, 3))
+    P[0] = pos[0]
+    count = 1
+
+    def free(q):
+        d = P[:count] - q
+        return bool(np.all(np.einsum("ij,ij->i", d, d) > r_min * r_min))
+
+    for _ in range(arms):
+        for _t in range(max_tries):
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            q = P[0] + d * anchor_bond
+            if free(q):
+                break
+        else:
+            raise RuntimeError("could not place arm root")
+        P[count] = q
+        count += 1
+        prev = q
+        for _k in range(1, n_arm):
+            for _t in range(max_tries):
+                s = rng.normal(size=3)
+                s /= np.linalg.norm(s)
+                q = prev + s * bond
+                if free(q):
+                    break
+            else:
+                raise RuntimeError("self-avoiding walk got stuck")
+            P[count] = q
+            count += 1
+            prev = q
+    return P
+
+
+def thermal_velocities(n: int, mass: float, kT: float, rng: np.random.Generator) -> np.ndarray:
+    """Maxwell-Boltzmann velocities with zero mean."""
+    v = rng.normal(scale=math.sqrt(kT / mass), size=(n, 3))
+    v -= v.mean(axis=0)
+    return v
+
+
+def make_star(arms: int, n_arm: int, solvophobic_fraction: float, mass: float, kT: float,
+              rng: np.random.Generator, bond: float = 1.0, anchor_bond: float = 2.0,
+              r_min: float = 1.0, centre=(0.0, 0.0, 0.0)) -> Star:
+    B = int(round(solvophobic_fraction * n_arm))
+    A = n_arm - B
+    amphi, anch, src, dst = star_topology(arms, A, B)
+    pos = saw_star(arms, n_arm, rng, bond=bond, anchor_bond=anchor_bond, r_min=r_min,
+                   centre=centre)
+    vel = thermal_velocities(len(pos), mass, kT, rng)
+    return Star(arms, A, B, mass, pos, vel, amphi, anch, src, dst)
+
+
+def uniform_fluid(L: Sequence[int], n_c: int, kT: float, rng: np.random.Generator,
+                  reference_velocities: bool = False):
+    """Solvent at n_c particles per cell: positions uniform in the box.
+
+    Velocities are Maxwell-Boltzmann at kT, or with ``reference_velocities``
+    uniform in [-1/2, 1/2) minus their mean as MPC::initialize does
+    (MPC.cpp:34-55).
+    """
+    n = int(n_c * L[0] * L[1] * L[2])
+    pos = (rng.random((n, 3)) - 0.5) * np.asarray(L, dtype=np.float64)
+    if reference_velocities:
+        vel = rng.random((n, 3)) - 0.5
+        vel -= vel.mean(axis=0)
+    else:
+        vel = thermal_velocities(n, 1.0, kT, rng)
+    return pos, vel
+
+
+@dataclasses.dataclass
+class ReplicaSpec:
+    """Parameters of one independent system (one box, its stars, its solvent)."""
+    L: int
+    arms: int
+    n_arm: int
+    solvophobic_fraction: float
+    shear: float
+    seed: int
+    n_c: int = 10
+    mono_mass: float = 5.0
+    kT: float = 1.0
+    n_stars: int = 1
+
+
+def batched_replica_table(n: int = 256, seed: int = 1) -> List[ReplicaSpec]:
+    """Uneven replica set: f ~ U{3..12}, N_arm ~ U{10..60}, solvophobic fraction
+    ~ U[0.2, 0.8], cubic L ~ U{16..40}, shear log-uniform in [1e-3, 0.5],
+    distinct seeds 1..n; drawn from numpy's default generator seeded with 1."""
+    rng = np.random.default_rng(seed)
+    f = rng.integers(3, 13, size=n)
+    na = rng.integers(10, 61, size=n)
+    frac = rng.uniform(0.2, 0.8, size=n)
+    L = rng.integers(16, 41, size=n)
+    shear = np.exp(rng.uniform(math.log(1e-3), math.log(0.5), size=n))
+    return [ReplicaSpec(L=int(L[i]), arms=int(f[i]), n_arm=int(na[i]),
+                        solvophobic_fraction=float(frac[i]), shear=float(shear[i]),
+                        seed=i + 1) for i in range(n)]
+
+
+def replica_table_json(specs: Sequence[ReplicaSpec]) -> str:
+    return json.dumps([dataclasses.asdict(s) for s in specs], indent=0)
