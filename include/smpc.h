@@ -1,0 +1,167 @@
+/*
+ * smpc.h -- C ABI of the GB300 (sm_103a) coupled MD/MPC step for
+ * StarPolymersMD-style systems: star polymers in an SRD/MPC solvent with
+ * Lees-Edwards shear. Plain pointers and sizes only; every call returns 0 on
+ * success or a positive SMPC_E* code (smpc_last_error() gives the message).
+ * Nothing throws across this boundary. One context drives one GPU stream and
+ * is not re-entrant; calls are asynchronous except the get/observable calls.
+ *
+ * A context holds one or many independent replicas (boxes). The reference
+ * interfaces each entry point replaces are cited per function; the reference
+ * binds them through its C++ classes, see INTEGRATION.md for the adapter.
+ */
+#ifndef SMPC_H
+#define SMPC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMPC_ABI_VERSION 1
+
+/* return codes */
+enum {
+  SMPC_OK = 0,
+  SMPC_E_ARG = 1,         /* invalid argument */
+  SMPC_E_CUDA = 2,        /* CUDA runtime failure */
+  SMPC_E_DEVICE = 3,      /* a kernel raised the device error word (see smpc_error_word) */
+  SMPC_E_STATE = 4,       /* call not valid in the current state */
+  SMPC_E_UNSUPPORTED = 5  /* configuration outside what this build implements */
+};
+
+/* device error word bits (smpc_error_word) */
+enum {
+  SMPC_ERR_FLUID_CELL = 1,    /* solvent cell index out of range (MPC.cpp:211-219) */
+  SMPC_ERR_MONO_CELL = 2,     /* monomer cell index out of range (MPC.cpp:227-234) */
+  SMPC_ERR_NEIGHBOR_OVF = 4,  /* Verlet list capacity exceeded */
+  SMPC_ERR_NONFINITE = 8,     /* non-finite velocity after a collision */
+  SMPC_ERR_GAMMA_ITERS = 32,  /* gamma sampler iteration limit */
+  SMPC_ERR_FENE = 64,         /* FENE bond at or beyond R0 (Potentials.h:29,50) */
+  SMPC_ERR_KEY_MISMATCH = 128 /* internal consistency check of the collide kernel */
+};
+
+enum { SMPC_FP64 = 0, SMPC_FP32 = 1 };
+enum { SMPC_RNG_INJECT = 0, SMPC_RNG_PHILOX = 1 };
+enum { SMPC_POT_REF4824 = 0, SMPC_POT_LJ126 = 1 };
+enum { SMPC_MONOBIN_REFERENCE = 0, SMPC_MONOBIN_WRAPPED = 1 };
+enum { SMPC_DELRX_REFERENCE = 0, SMPC_DELRX_PHYSICAL = 1 };
+
+/* One independent box (MPC + Box + Thermostat_None of the reference). */
+typedef struct {
+  int L[3];               /* box edge in MPC cells (Box.cpp:14-19; odd L is allowed here) */
+  int n_fluid;            /* solvent particles (MPC.cpp:17: N_c * cells) */
+  int n_mono;             /* monomers of all molecules of this box */
+  int mol0_size;          /* monomers of molecule 0, the recentring reference (MPC.cpp:175-176) */
+  double kT;              /* MPC temperature (MPC.cpp:12) */
+  double shear;           /* Lees-Edwards shear rate (MPC.cpp:13) */
+  double h;               /* collision time step: streaming time of MPC::step(t, h) */
+  double md_dt;           /* velocity-Verlet step (Thermostat_None) */
+  double lambda;          /* BB attraction (Box.cpp:7) */
+  double r_cut;           /* Verlet cut-off (Box.cpp:8) */
+  double r_verlet;        /* Verlet radius (Box.cpp:9) */
+  double solvent_mass;    /* 1.0 in the reference (MPC.cpp:30) */
+  uint64_t seed;          /* Philox key of this box */
+  int potential;          /* SMPC_POT_* */
+  int pad;
+} smpc_replica_desc;
+
+typedef struct {
+  int precision;          /* SMPC_FP64 (reference parity) or SMPC_FP32 (fast path) */
+  int rng;                /* SMPC_RNG_INJECT or SMPC_RNG_PHILOX */
+  int mono_bin;           /* SMPC_MONOBIN_*: reference bins monomers unwrapped (MPC.cpp:223-225) */
+  int delrx_mode;         /* SMPC_DELRX_*: reference advances delrx by shear*Ly*dt per MD step */
+  int step_update;        /* collide when t % step_update == 0 (MPC.cpp:119); MD substeps per cycle */
+  int max_neighbors;      /* Verlet list capacity per monomer (0: default 192) */
+  int strict_cells;       /* 1: reference cell formula + range error; 0: clamp into the box */
+  int device;             /* CUDA device ordinal */
+} smpc_options;
+
+/* Draws injected for one collision of every replica (reference parity):
+ * shift[3*n_rep] (grid shift as constructed at MPC.cpp:123), and per global
+ * cell (replicas concatenated in order, cells in MPC::sort order) the gamma
+ * variate Gamma(1.5(n-1), kT) for cells with n >= 2 and the raw uniforms of
+ * phi = 2 pi u and theta = 2(u - 1/2) (MPC.cpp:244-245, 289). */
+typedef struct {
+  const double* shift;
+  const double* gamma;
+  const double* u_phi;
+  const double* u_theta;
+} smpc_inject;
+
+typedef struct smpc_ctx smpc_ctx;
+
+/* Replaces the MPC / Box / Thermostat_None constructors
+ * (MPC.cpp:10-32, Box.cpp:4-27, Thermostat_None.cpp:5-12): allocates device
+ * state for n_rep boxes. */
+int smpc_create(const smpc_replica_desc* reps, int n_rep, const smpc_options* opt,
+                smpc_ctx** out);
+void smpc_destroy(smpc_ctx* ctx);
+const char* smpc_last_error(const smpc_ctx* ctx);
+int smpc_n_cells(const smpc_ctx* ctx, int rep);
+
+/* MPC::initialize / Fluid vector (MPC.h:43, MPC.cpp:34-55): x,y,z interleaved. */
+int smpc_set_fluid(smpc_ctx* ctx, int rep, const double* pos, const double* vel);
+/* MPC::print_fluid_complete read-out (MPC.cpp:570-579). */
+int smpc_get_fluid(smpc_ctx* ctx, int rep, double* pos, double* vel);
+/* Box::Molecules state (Box.h:50, Particle.h:48-82). */
+int smpc_set_monomers(smpc_ctx* ctx, int rep, const double* pos, const double* vel,
+                      const double* force, const double* mass, const int* amphi,
+                      const int* anchor);
+int smpc_get_monomers(smpc_ctx* ctx, int rep, double* pos, double* vel, double* force);
+/* MDParticle::Neighbors, directed (Particle.h:57, Molecule.cpp:146-157). */
+int smpc_set_bonds(smpc_ctx* ctx, int rep, int n_bond, const int* src, const int* dst);
+/* Thermostat_None constructor body: Verlet lists + forces (Thermostat_None.cpp:9-11). */
+int smpc_init_md(smpc_ctx* ctx);
+
+/* n x Thermostat_None::propagate(calc_epot) for every replica
+ * (Thermostat_None.cpp:21-38); the potential energy of the last substep is
+ * kept when calc_epot != 0 (Box::print_Epot, Box.cpp:605-613). */
+int smpc_md_substeps(smpc_ctx* ctx, int n, int calc_epot);
+/* MPC::step(t, dt) for every replica (MPC.cpp:116-142): delrx advance on every
+ * call, a collision when t % step_update == 0. inj may be NULL only in
+ * Philox mode. */
+int smpc_mpc_step(smpc_ctx* ctx, long t, double dt, const smpc_inject* inj);
+/* n fused cycles of (step_update MD substeps + one collision) with Philox
+ * draws, launched as a captured CUDA graph. */
+int smpc_cycles(smpc_ctx* ctx, int n);
+
+/* Same cycles launched on the context stream with CUDA events around every
+ * phase (phase_ms[8]: MD substeps, cycle begin, monomer prep, solvent bin,
+ * scan, perm, collide, cycle end; summed over the n cycles) and the total
+ * elapsed time from the first to the last event. */
+int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, double* total_ms);
+/* smpc_cycles bracketed by CUDA events on the context stream (ms). */
+int smpc_time_cycles(smpc_ctx* ctx, int n, double* total_ms);
+/* Solvent initial state generated on the device (MPC::initialize,
+ * MPC.cpp:34-55): positions uniform in the box; velocities uniform in
+ * [-1/2, 1/2) when reference_velocities != 0, else Maxwell-Boltzmann at kT. */
+int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int reference_velocities);
+
+/* Observables. */
+int smpc_temperature(smpc_ctx* ctx, int rep, double* out);   /* MPC.cpp:405-409 */
+int smpc_epot(smpc_ctx* ctx, int rep, double* out);          /* sum of Molecule::Epot */
+/* Temperature of every replica (out[n_rep]) from one kernel launch. */
+int smpc_temperature_all(smpc_ctx* ctx, double* out);
+/* Monomer positions/velocities of all replicas (concatenated, x,y,z
+ * interleaved): the Box::Molecules state a host-side driver reads and writes
+ * between steps (star-polymers.cpp:466-519). Masses and types are kept. */
+int smpc_set_monomer_state_all(smpc_ctx* ctx, const double* pos, const double* vel);
+int smpc_get_monomer_state_all(smpc_ctx* ctx, double* pos, double* vel, double* force);
+int smpc_delrx(smpc_ctx* ctx, int rep, double* out);
+int smpc_set_delrx(smpc_ctx* ctx, int rep, double delrx);
+/* Cell occupancies of the last collision: MPCCellList sizes and
+ * MPCCellListFluidParticles (MPC.h:40-41). */
+int smpc_cell_counts(smpc_ctx* ctx, int rep, unsigned* total, unsigned* fluid);
+int smpc_set_collision_counter(smpc_ctx* ctx, uint64_t counter);
+int smpc_verlet_rebuilds(smpc_ctx* ctx, int rep, int* out);
+
+/* Device error word (0 = clean) and its first offender; clears it. */
+int smpc_error_word(smpc_ctx* ctx, unsigned* word, unsigned* info3);
+int smpc_synchronize(smpc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

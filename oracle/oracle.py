@@ -51,7 +51,7 @@ class OrcParams(C.Structure):
                 ("step_update", C.c_uint), ("angular_momentum", C.c_int),
                 ("lambda_", C.c_double), ("md_dt", C.c_double), ("r_cut", C.c_double),
                 ("r_verlet", C.c_double), ("potential", C.c_int),
-                ("delrx_dt_scale", C.c_double)]
+                ("delrx_dt_scale", C.c_double), ("mono_wrap", C.c_int)]
 
 
 _lib = None
@@ -111,7 +111,7 @@ class OracleSystem:
 
     def __init__(self, L, kT, shear, step_update, n_fluid, n_mono=0, mol_start=(0,),
                  lambda_=1.0, md_dt=0.01, r_cut=1.5, r_verlet=2.0, potential=POT_REF4824,
-                 delrx_dt_scale=1.0):
+                 delrx_dt_scale=1.0, mono_wrap=0):
         self.lib = _oracle_lib()
         p = OrcParams()
         for d in range(3):
@@ -120,6 +120,7 @@ class OracleSystem:
         p.angular_momentum = 0
         p.lambda_, p.md_dt, p.r_cut, p.r_verlet = lambda_, md_dt, r_cut, r_verlet
         p.potential, p.delrx_dt_scale = potential, delrx_dt_scale
+        p.mono_wrap = int(mono_wrap)
         self.L = tuple(int(x) for x in L)
         self.n_fluid, self.n_mono = int(n_fluid), int(n_mono)
         ms = np.ascontiguousarray(mol_start, dtype=np.int32)

@@ -65,6 +65,8 @@ struct smpc_orc {
   int cs[3];      /* Box::CellSize */
   double csl[3];  /* Box::CellSideLength */
   int* vcell_head; /* per Verlet cell: head of a singly linked list */
+  long vcell_cap;
+  double grid_lo[3]; /* non-reference presets: grid origin (bounding box) */
   int* vcell_next;
   int verlet_rebuilds;
   double* epot_mol;
@@ -74,6 +76,7 @@ struct smpc_orc {
   unsigned* c_fl;
   unsigned* c_start;
   long* c_mem; /* >= 0 fluid index, < 0: -(m+1) monomer index */
+  int* m_img;  /* Lees-Edwards image index of each monomer when binned wrapped */
 
   int rng_mode;
   const double* inj_shift;
@@ -285,10 +288,12 @@ smpc_orc* orc_create(const orc_params* p, long n_fluid, int n_mono, int n_mol,
     ncv *= o->cs[d];
   }
   o->vcell_head = (int*)malloc(sizeof(int) * (size_t)ncv);
+  o->vcell_cap = ncv;
   o->c_tot = (unsigned*)calloc(o->n_cell, sizeof(unsigned));
   o->c_fl = (unsigned*)calloc(o->n_cell, sizeof(unsigned));
   o->c_start = (unsigned*)calloc((size_t)o->n_cell + 1, sizeof(unsigned));
   o->c_mem = (long*)malloc(sizeof(long) * (size_t)(n_fluid + n_mono + 1));
+  o->m_img = (int*)calloc((size_t)n_mono + 1, sizeof(int));
   if (!o->fx || !o->fv || !o->mx || !o->vl_idx || !o->vcell_head || !o->c_mem) o->err |= ORC_ERR_ALLOC;
   o->rng_mode = ORC_RNG_INJECT;
   return o;
@@ -301,6 +306,7 @@ void orc_destroy(smpc_orc* o) {
   free(o->bsrc); free(o->bdst); free(o->bond_first); free(o->vl_start); free(o->vl_idx);
   free(o->vcell_head); free(o->vcell_next); free(o->c_tot); free(o->c_fl); free(o->c_start);
   free(o->c_mem);
+  free(o->m_img);
   free(o);
 }
 
@@ -393,8 +399,12 @@ static void com_frame(smpc_orc* o) {
 }
 
 static inline int vcell_of(const smpc_orc* o, int i, int* cn) {
-  for (int d = 0; d < 3; ++d)
-    cn[d] = (int)((o->mx[3 * i + d] - o->com_pos[d] + o->p.L[d] * 0.5) / o->csl[d]);
+  if (o->p.potential != ORC_POT_REF4824) {
+    for (int d = 0; d < 3; ++d) cn[d] = (int)((o->mx[3 * i + d] - o->grid_lo[d]) / o->csl[d]);
+  } else {
+    for (int d = 0; d < 3; ++d)
+      cn[d] = (int)((o->mx[3 * i + d] - o->com_pos[d] + o->p.L[d] * 0.5) / o->csl[d]);
+  }
   return !(cn[0] < 0 || cn[0] >= o->cs[0] || cn[1] < 0 || cn[1] >= o->cs[1] || cn[2] < 0 ||
            cn[2] >= o->cs[2]);
 }
@@ -406,9 +416,33 @@ static inline int vcell_of(const smpc_orc* o, int i, int* cn) {
 static void update_verlet(smpc_orc* o) {
   o->verlet_rebuilds++;
   const int n = o->n_m;
+  com_frame(o);
+  if (o->p.potential != ORC_POT_REF4824 && n > 0) {
+    /* cells of side >= r_verlet over the monomers' bounding box */
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) lo[d] = hi[d] = o->mx[d];
+    for (int i = 1; i < n; ++i)
+      for (int d = 0; d < 3; ++d) {
+        if (o->mx[3 * i + d] < lo[d]) lo[d] = o->mx[3 * i + d];
+        if (o->mx[3 * i + d] > hi[d]) hi[d] = o->mx[3 * i + d];
+      }
+    long need = 1;
+    for (int d = 0; d < 3; ++d) {
+      o->grid_lo[d] = lo[d] - 1e-6;
+      double ext = hi[d] - lo[d] + 2e-6;
+      o->cs[d] = (int)(ext / o->p.r_verlet);
+      if (o->cs[d] < 1) o->cs[d] = 1;
+      o->csl[d] = ext / o->cs[d];
+      if (o->csl[d] < o->p.r_verlet) { o->cs[d] = o->cs[d] > 1 ? o->cs[d] - 1 : 1; o->csl[d] = ext / o->cs[d]; }
+      need *= o->cs[d];
+    }
+    if (need > o->vcell_cap) {
+      o->vcell_head = (int*)realloc(o->vcell_head, sizeof(int) * (size_t)need);
+      o->vcell_cap = need;
+    }
+  }
   const long ncv = (long)o->cs[0] * o->cs[1] * o->cs[2];
   for (long c = 0; c < ncv; ++c) o->vcell_head[c] = -1;
-  com_frame(o);
   int cn[3];
   for (int i = 0; i < n; ++i) {
     if (!vcell_of(o, i, cn)) {
@@ -630,7 +664,23 @@ static void mpc_sort(smpc_orc* o) {
     o->c_fl[c]++;
   }
   for (int m = 0; m < o->n_m; ++m) {
-    unsigned c = cell_index(o, o->mx + 3 * m);
+    unsigned c;
+    if (o->p.mono_wrap) {
+      /* bin at the periodic image; clamp faces like the fast path */
+      double x[3] = {o->mx[3 * m], o->mx[3 * m + 1], o->mx[3 * m + 2]}, dv = 0.0;
+      o->m_img[m] = (int)round(x[1] / o->p.L[1]);
+      wrap_particle(o, x, &dv);
+      int ci[3];
+      for (int d = 0; d < 3; ++d) {
+        ci[d] = (int)(x[d] + o->p.L[d] * 0.5);
+        if (ci[d] < 0) ci[d] = 0;
+        if (ci[d] >= o->p.L[d]) ci[d] = o->p.L[d] - 1;
+      }
+      c = (unsigned)(ci[0] + o->p.L[0] * (ci[1] + o->p.L[1] * ci[2]));
+    } else {
+      o->m_img[m] = 0;
+      c = cell_index(o, o->mx + 3 * m);
+    }
     key[o->n_f + m] = c;
     if (c > last) {
       o->err |= ORC_ERR_MONO_CELL;
@@ -794,12 +844,17 @@ void orc_mpc_step(smpc_orc* o, long t, double dt) {
   }
   shift_particles(o, shift);
   mpc_sort(o);
+  const double sLy = o->p.shear * o->p.L[1];
+  if (o->p.mono_wrap)
+    for (int m = 0; m < o->n_m; ++m) o->mv[3 * m] -= o->m_img[m] * sLy;
   for (unsigned c = 0; c < o->n_cell; ++c) {
     double cmv[3];
     cell_cmv(o, c, cmv);
     cell_thermostat(o, c, cmv);
     cell_collide(o, c, cmv);
   }
+  if (o->p.mono_wrap)
+    for (int m = 0; m < o->n_m; ++m) o->mv[3 * m] += o->m_img[m] * sLy;
   shift[0] = -shift[0];
   shift[1] = -shift[1];
   shift[2] = -shift[2];

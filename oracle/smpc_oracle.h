@@ -57,6 +57,8 @@ typedef struct {
   int potential;         /* ORC_POT_REF4824 (reference) or ORC_POT_LJ126 */
   double delrx_dt_scale; /* 1.0: delrx advances by shear*Ly*dt per call as MPC.cpp:117;
                             1/step_update: physical advance */
+  int mono_wrap;         /* 0: monomers binned unwrapped (MPC.cpp:223-225);
+                            1: binned at their Lees-Edwards periodic image */
 } orc_params;
 
 typedef struct smpc_orc smpc_orc;

@@ -1,0 +1,16 @@
+// FP64 reference-parity instantiation. Built with -fmad=false so every
+// multiply and add rounds separately, in the reference's order.
+#define SMPC_REAL double
+#define SMPC_COLLIDE_NT 128
+#define SMPC_COLLIDE_CT 128
+#define SMPC_COLLIDE_PPT 12
+#define SMPC_BIN_NT 256
+#define SMPC_MD_NT 256
+#define SMPC_MD_MPT 4
+#include "kernels_impl.cuh"
+
+namespace smpc {
+int fluid_slots_per_tile() { return 4096; }
+int temperature_cells_per_tile() { return 512; }
+int md_max_monomers() { return SMPC_MD_NT * SMPC_MD_MPT; }
+}  // namespace smpc

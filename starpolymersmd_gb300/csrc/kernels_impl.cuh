@@ -1,0 +1,82 @@
+// Launch wrappers shared by kernels_fp64.cu and kernels_fp32.cu; each of
+// those defines SMPC_REAL and the tile constants and includes this file once.
+#pragma once
+#include "launch.h"
+#include "md_kernels.cuh"
+#include "mpc_kernels.cuh"
+
+namespace smpc {
+
+typedef SMPC_REAL Real;
+
+template <>
+int collide_cells_per_tile<Real>() {
+  return SMPC_COLLIDE_CT;
+}
+
+template <>
+void launch_cycle_begin<Real>(const RepInfo* reps, RepDyn* dyn, int n_rep, int n_adv,
+                              double adv_scale, int gen_shift, cudaStream_t st) {
+  k_cycle_begin<Real><<<(n_rep + 127) / 128, 128, 0, st>>>(reps, dyn, n_rep, n_adv, adv_scale,
+                                                           gen_shift);
+}
+
+template <>
+void launch_cycle_end<Real>(RepDyn* dyn, int n_rep, cudaStream_t st) {
+  k_cycle_end<Real><<<(n_rep + 127) / 128, 128, 0, st>>>(dyn, n_rep);
+}
+
+template <>
+void launch_init_solvent<Real>(const RepInfo* reps, int rep, int slot_cap, Real* pos, Real* vel,
+                               unsigned long long seed, double kT, int ref_vel, cudaStream_t st) {
+  if (slot_cap == 0) return;
+  k_init_solvent<Real><<<(slot_cap + 255) / 256, 256, 0, st>>>(reps, rep, pos, vel, seed, kT,
+                                                              ref_vel);
+}
+
+template <>
+void launch_mono_prep<Real>(const RepInfo* reps, RepDyn* dyn, int n_rep, Real* mpos, Real* mvel,
+                            uint2* mkey, int* mimg, uint32_t* count, ErrorState* err,
+                            int mono_bin, int strict, cudaStream_t st) {
+  k_mono_prep<Real, 256><<<n_rep, 256, 0, st>>>(reps, dyn, mpos, mvel, mkey, mimg, count, err,
+                                                mono_bin, strict);
+}
+
+template <>
+void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
+                            const RepDyn* dyn, const Real* pos, const Real* vel, uint2* keys,
+                            uint32_t* count, ErrorState* err, int strict, cudaStream_t st) {
+  if (n_tiles == 0) return;
+  k_fluid_bin<Real, SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, dyn, pos, vel,
+                                                                  keys, count, err, strict);
+}
+
+template <>
+void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
+  if (a.n_tiles == 0) return;
+  k_collide<Real, SMPC_COLLIDE_NT, SMPC_COLLIDE_CT, SMPC_COLLIDE_PPT>
+      <<<a.n_tiles, SMPC_COLLIDE_NT, 0, st>>>(
+          a.tiles, a.reps, a.dyn, a.off, a.perm, a.pos_in, a.vel_in, a.pos_out, a.vel_out, a.mpos,
+          a.mvel, a.mkey, a.mimg, a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.rot_c, a.rot_s,
+          a.strict, a.mono_bin, a.err);
+}
+
+template <>
+void launch_temperature<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
+                              const uint32_t* off, const uint32_t* perm, const Real* vel_cur,
+                              const Real* mpos, const Real* mvel, const int* mimg, int mono_bin,
+                              TempPartial* partial, cudaStream_t st) {
+  if (n_tiles == 0) return;
+  k_temperature<Real, 128><<<n_tiles, 128, 0, st>>>(tiles, reps, off, perm, vel_cur, mpos, mvel,
+                                                    mimg, mono_bin, partial);
+}
+
+template <>
+void launch_md<Real>(const MdArgs& a, int n_rep, Real* mpos, Real* mvel, Real* mfrc, Real* mver,
+                     cudaStream_t st) {
+  if (n_rep == 0) return;
+  k_md_substeps<Real, SMPC_MD_NT, SMPC_MD_MPT><<<n_rep, SMPC_MD_NT, 0, st>>>(a, mpos, mvel, mfrc,
+                                                                          mver);
+}
+
+}  // namespace smpc

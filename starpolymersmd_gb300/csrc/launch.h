@@ -1,0 +1,79 @@
+// Host-side launch entry points for the kernels, instantiated once per
+// precision (kernels_fp64.cu compiled with -fmad=false for reference parity,
+// kernels_fp32.cu for the fast path).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "smpc_device.cuh"
+
+namespace smpc {
+
+struct MdArgs;
+
+template <typename R>
+struct CollideArgs {
+  const Tile* tiles;
+  int n_tiles;
+  const RepInfo* reps;
+  const RepDyn* dyn;
+  const uint32_t* off;
+  const uint32_t* perm;
+  const R* pos_in;
+  const R* vel_in;
+  R* pos_out;
+  R* vel_out;
+  const R* mpos;
+  R* mvel;
+  const uint2* mkey;
+  const int* mimg;
+  const double* inj_gamma;
+  const double* inj_uphi;
+  const double* inj_utheta;
+  int rng;
+  double rot_c;
+  double rot_s;
+  int strict;
+  int mono_bin;
+  ErrorState* err;
+};
+
+// Tile geometry chosen per precision (register budget of k_collide).
+template <typename R>
+int collide_cells_per_tile();
+int fluid_slots_per_tile();
+int temperature_cells_per_tile();
+int md_max_monomers();
+
+template <typename R>
+void launch_cycle_begin(const RepInfo* reps, RepDyn* dyn, int n_rep, int n_adv, double adv_scale,
+                        int gen_shift, cudaStream_t st);
+template <typename R>
+void launch_cycle_end(RepDyn* dyn, int n_rep, cudaStream_t st);
+template <typename R>
+void launch_init_solvent(const RepInfo* reps, int rep, int slot_cap, R* pos, R* vel,
+                         unsigned long long seed, double kT, int ref_vel, cudaStream_t st);
+template <typename R>
+void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* mvel, uint2* mkey,
+                      int* mimg, uint32_t* count, ErrorState* err, int mono_bin, int strict,
+                      cudaStream_t st);
+template <typename R>
+void launch_fluid_bin(const Tile* tiles, int n_tiles, const RepInfo* reps, const RepDyn* dyn,
+                      const R* pos, const R* vel, uint2* keys, uint32_t* count, ErrorState* err,
+                      int strict, cudaStream_t st);
+template <typename R>
+void launch_collide(const CollideArgs<R>& a, cudaStream_t st);
+template <typename R>
+void launch_temperature(const Tile* tiles, int n_tiles, const RepInfo* reps, const uint32_t* off,
+                        const uint32_t* perm, const R* vel_cur, const R* mpos, const R* mvel,
+                        const int* mimg, int mono_bin, TempPartial* partial, cudaStream_t st);
+template <typename R>
+void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, cudaStream_t st);
+
+void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* grand, int n_cells,
+                 cudaStream_t st);
+int scan_tile_count(int n_cells);
+void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_mono,
+                       const uint32_t* off, uint32_t* perm, cudaStream_t st);
+
+}  // namespace smpc

@@ -1,0 +1,267 @@
+// Monomer velocity-Verlet substeps (Thermostat_None::propagate,
+// star-polymers/lib/Thermostats/Thermostat_None.cpp:21-38) with the
+// displacement-triggered Verlet list (Box::check_VerletLists /
+// update_VerletLists, star-polymers/lib/Box.cpp:105-194) and the FENE + pair
+// forces (Box::calculate_forces_verlet, Box.cpp:243-286; potentials
+// star-polymers/lib/Molecules/Potentials.h:14-120).
+//
+// One CTA per replica runs all n substeps of a call: positions live in
+// shared memory (other threads read them for forces), each thread owns up to
+// MPT monomers in registers (v, F, Verlet reference position). Forces are
+// computed per bead over its own Verlet list and its own undirected bond
+// list, so no atomics and no write conflicts; the reference's directed bond
+// (F_src -= f d, F_dst += f d) is the same force seen from both ends.
+#pragma once
+#include <stdint.h>
+
+#include "mpc_kernels.cuh"
+#include "smpc_device.cuh"
+
+namespace smpc {
+
+// Pair force magnitude f such that F_i -= f (x_j - x_i).
+template <typename R>
+__device__ __forceinline__ R pair_force(int pot, bool bb, R r2, R lambda) {
+  if (pot == POT_REF4824) {
+    // TypeAA_Force / TypeBB_Force (Potentials.h:57-120)
+    if (r2 < R(1.0594631)) {
+      const R rm2 = R(1) / r2;
+      R rm24 = rm2 * rm2 * rm2;
+      rm24 *= rm24;
+      rm24 *= rm24;
+      return R(192.0) * rm2 * rm24 * (rm24 - R(0.5));
+    }
+    if (bb && r2 < R(2.25)) {
+      const R rm2 = R(1) / r2;
+      R rm24 = rm2 * rm2 * rm2;
+      rm24 *= rm24;
+      rm24 *= rm24;
+      return R(192.0) * lambda * rm2 * rm24 * (rm24 - R(0.5));
+    }
+    return R(0);
+  }
+  // 12-6 preset: WCA core for all pairs, lambda-scaled LJ attraction to 2.5 for BB
+  if (r2 < R(1.2599210498948732) || (bb && r2 < R(6.25))) {
+    const R rm2 = R(1) / r2;
+    const R rm6 = rm2 * rm2 * rm2;
+    const R f = R(48.0) * rm2 * rm6 * (rm6 - R(0.5));
+    return r2 < R(1.2599210498948732) ? f : lambda * f;
+  }
+  return R(0);
+}
+
+template <typename R>
+__device__ __forceinline__ R pair_pot(int pot, bool bb, R r2, R lambda) {
+  if (pot == POT_REF4824) {
+    if (r2 < R(1.0594631)) {
+      R rm24 = R(1) / r2;
+      rm24 *= rm24 * rm24;
+      rm24 *= rm24;
+      rm24 *= rm24;
+      return R(4.0) * rm24 * (rm24 - R(1.0)) + R(1.0) - (bb ? lambda : R(0));
+    }
+    if (bb && r2 < R(2.25)) {
+      R rm24 = R(1) / r2;
+      rm24 *= rm24 * rm24;
+      rm24 *= rm24;
+      rm24 *= rm24;
+      return R(4.0) * lambda * (rm24 * (rm24 - R(1.0)) - R(0.0000593));
+    }
+    return R(0);
+  }
+  if (r2 < R(1.2599210498948732) || (bb && r2 < R(6.25))) {
+    R rm6 = R(1) / r2;
+    rm6 *= rm6 * rm6;
+    const R u = R(4.0) * rm6 * (rm6 - R(1.0));
+    if (r2 < R(1.2599210498948732)) return u + R(1.0) - (bb ? lambda : R(0));
+    return lambda * (u - R(-0.016316891136));
+  }
+  return R(0);
+}
+
+// FENE (Potentials.h:24-55): anchor bonds (core) use R0^2 = 20.25.
+template <typename R>
+__device__ __forceinline__ R fene_force(bool anchor, R r2) {
+  return anchor ? R(-30.0) / (R(1.0) - (r2 / R(20.25))) : R(-30.0) / (R(1.0) - (r2 / R(2.25)));
+}
+template <typename R>
+__device__ __forceinline__ R fene_pot(bool anchor, R r2) {
+  return anchor ? R(-15.0) * R(20.25) * log(R(1.0) - r2 / R(20.25))
+                : R(-15.0) * R(2.25) * log(R(1.0) - r2 / R(2.25));
+}
+
+struct MdArgs {
+  const RepInfo* reps;
+  RepDyn* dyn;
+  const int* bond_start;   // CSR over global monomers
+  const int2* bonds;       // (partner, anchor-bond flag)
+  int* nlist;              // [max_nb][n_mono_total], transposed for coalescing
+  int* ncount;             // [n_mono_total]
+  int n_mono_total;
+  int max_nb;
+  int n_steps;             // substeps in this launch; 0 = build lists + forces only
+  int calc_epot;
+  int force_rebuild;
+  ErrorState* err;
+};
+
+template <typename R, int NT, int MPT>
+__global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, R* mfrc,
+                                                    R* mver) {
+  constexpr int CAP = NT * MPT;
+  __shared__ R sx[CAP], sy[CAP], sz[CAP];
+  __shared__ unsigned char s_amphi[CAP];
+  __shared__ int s_rebuild;
+  __shared__ double s_red[NT / 32];
+  const int r = blockIdx.x;
+  const RepInfo ri = a.reps[r];
+  const int n = ri.n_mono;
+  if (n == 0) return;
+  const int b = ri.mono_base;
+  const R dt = static_cast<R>(ri.md_dt);
+  const R dth = dt * R(0.50);
+  const R lambda = static_cast<R>(ri.lambda);
+  const R rv2 = static_cast<R>(ri.r_verlet) * static_cast<R>(ri.r_verlet);
+  const R lim = (static_cast<R>(ri.r_verlet) - static_cast<R>(ri.r_cut)) * R(0.5);
+  const int pot = ri.potential;
+
+  R x[MPT][3], v[MPT][3], f[MPT][3], xv[MPT][3], m[MPT];
+  int anc[MPT];
+#pragma unroll
+  for (int k = 0; k < MPT; ++k) {
+    const int i = threadIdx.x + k * NT;
+    if (i < n) {
+      const R4<R> p = ld4_rw(mpos, b + i), vv = ld4_rw(mvel, b + i), ff = ld4_rw(mfrc, b + i),
+                  pv = ld4_rw(mver, b + i);
+      x[k][0] = p.x; x[k][1] = p.y; x[k][2] = p.z; m[k] = p.w;
+      v[k][0] = vv.x; v[k][1] = vv.y; v[k][2] = vv.z;
+      const int flags = static_cast<int>(vv.w);
+      s_amphi[i] = static_cast<unsigned char>(flags & 1);
+      anc[k] = (flags >> 1) & 1;
+      f[k][0] = ff.x; f[k][1] = ff.y; f[k][2] = ff.z;
+      xv[k][0] = pv.x; xv[k][1] = pv.y; xv[k][2] = pv.z;
+      sx[i] = p.x; sy[i] = p.y; sz[i] = p.z;
+    }
+  }
+  if (threadIdx.x == 0) s_rebuild = a.force_rebuild;
+  __syncthreads();
+  int rebuilds = 0;
+  double epot = 0.0;
+  const int total_steps = a.n_steps > 0 ? a.n_steps : 1;
+  for (int step = 0; step < total_steps; ++step) {
+    if (a.n_steps > 0) {
+      // kick + drift (Thermostat_None.cpp:22-27)
+#pragma unroll
+      for (int k = 0; k < MPT; ++k) {
+        const int i = threadIdx.x + k * NT;
+        if (i < n) {
+          for (int d = 0; d < 3; ++d) {
+            v[k][d] += (f[k][d] / m[k]) * dth;
+            x[k][d] += v[k][d] * dt;
+          }
+          sx[i] = x[k][0]; sy[i] = x[k][1]; sz[i] = x[k][2];
+          const R d0 = x[k][0] - xv[k][0], d1 = x[k][1] - xv[k][1], d2 = x[k][2] - xv[k][2];
+          if (sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim) s_rebuild = 1;
+        }
+      }
+    }
+    __syncthreads();
+    const int rebuild = s_rebuild;
+    if (rebuild) {
+      // Verlet lists: every other bead within r_verlet (Box.cpp:146-179), all pairs
+      ++rebuilds;
+#pragma unroll
+      for (int k = 0; k < MPT; ++k) {
+        const int i = threadIdx.x + k * NT;
+        if (i < n) {
+          int cnt = 0;
+          for (int j = 0; j < n; ++j) {
+            if (j == i) continue;
+            const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
+            if ((d0 * d0 + d1 * d1) + d2 * d2 <= rv2) {
+              if (cnt < a.max_nb) a.nlist[static_cast<size_t>(cnt) * a.n_mono_total + b + i] = b + j;
+              ++cnt;
+            }
+          }
+          if (cnt > a.max_nb) {
+            raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(b + i),
+                        static_cast<uint32_t>(cnt));
+            cnt = a.max_nb;
+          }
+          a.ncount[b + i] = cnt;
+          xv[k][0] = x[k][0]; xv[k][1] = x[k][1]; xv[k][2] = x[k][2];
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_rebuild = 0;
+    const bool want_epot = a.calc_epot && (step == total_steps - 1);
+    // forces (Box.cpp:243-286)
+#pragma unroll
+    for (int k = 0; k < MPT; ++k) {
+      const int i = threadIdx.x + k * NT;
+      if (i < n) {
+        R F0 = R(0), F1 = R(0), F2 = R(0);
+        const bool ai = s_amphi[i] != 0;
+        const int cnt = a.ncount[b + i];
+        for (int q = 0; q < cnt; ++q) {
+          const int j = a.nlist[static_cast<size_t>(q) * a.n_mono_total + b + i] - b;
+          const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
+          const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+          const bool bb = ai && s_amphi[j] != 0;
+          const R fa = pair_force<R>(pot, bb, r2, lambda);
+          F0 -= d0 * fa;
+          F1 -= d1 * fa;
+          F2 -= d2 * fa;
+          if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
+        }
+        for (int e = a.bond_start[b + i]; e < a.bond_start[b + i + 1]; ++e) {
+          const int2 bd = a.bonds[e];
+          const int j = bd.x - b;
+          const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
+          const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+          const bool anch = bd.y != 0;
+          if (r2 >= (anch ? R(20.25) : R(2.25)))
+            raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + i), static_cast<uint32_t>(b + j));
+          const R fa = fene_force<R>(anch, r2);
+          F0 -= d0 * fa;
+          F1 -= d1 * fa;
+          F2 -= d2 * fa;
+          if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2));
+        }
+        f[k][0] = F0; f[k][1] = F1; f[k][2] = F2;
+        if (a.n_steps > 0)
+          for (int d = 0; d < 3; ++d) v[k][d] += (f[k][d] / m[k]) * dth;  // second half-kick
+      }
+    }
+    __syncthreads();  // positions are rewritten by the next drift
+  }
+  // write back
+#pragma unroll
+  for (int k = 0; k < MPT; ++k) {
+    const int i = threadIdx.x + k * NT;
+    if (i < n) {
+      R4<R> p = ld4_rw(mpos, b + i);
+      p.x = x[k][0]; p.y = x[k][1]; p.z = x[k][2];
+      st4(mpos, b + i, p);
+      R4<R> vv = ld4_rw(mvel, b + i);
+      vv.x = v[k][0]; vv.y = v[k][1]; vv.z = v[k][2];
+      st4(mvel, b + i, vv);
+      st4(mfrc, b + i, R4<R>{f[k][0], f[k][1], f[k][2], R(0)});
+      st4(mver, b + i, R4<R>{xv[k][0], xv[k][1], xv[k][2], R(0)});
+    }
+  }
+  if (a.calc_epot) {
+    for (int o = 16; o > 0; o >>= 1) epot += __shfl_down_sync(0xFFFFFFFFu, epot, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = epot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < NT / 32; ++w) s += s_red[w];
+      a.dyn[r].epot = s;
+    }
+  }
+  if (threadIdx.x == 0) a.dyn[r].verlet_rebuilds += rebuilds;
+}
+
+}  // namespace smpc

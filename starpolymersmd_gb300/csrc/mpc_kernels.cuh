@@ -1,0 +1,825 @@
+// MPC (SRD) collision-step kernels, templated on the storage/arithmetic type
+// R (double for the FP64 reference-parity path, float for the fast path).
+//
+// One collision (MPC::step, star-polymers/lib/Hydrodynamics/MPC.cpp:116-142):
+//   k_cycle_begin  delrx advance (MPC.cpp:117-118) + Philox grid shift   [graph mode]
+//   k_mono_prep    check_bounds recentring (MPC.cpp:160-190), monomer grid shift
+//                  (MPC.cpp:306-310) and monomer binning (MPC.cpp:221-236)
+//   k_fluid_bin    recentre/stream/shift/LE-wrap each solvent particle
+//                  (MPC.cpp:183-197, 301-305, 421-429) and bin it: cell key and
+//                  rank from one warp-aggregated atomic per (warp, cell)
+//   scan           exclusive prefix of the cell counts (scan.cu)
+//   k_build_perm   counting-sort scatter: sorted position -> source
+//   k_collide      per tile of cells: gathers its particles, recomputes their
+//                  streamed/shifted state, reduces per-cell momentum, mass and
+//                  kinetic energy with warp-shuffle segmented scans into shared
+//                  memory (int64 fixed point on the fast path), draws the MBS
+//                  thermostat and the rotation (MPC.cpp:239-299), applies them,
+//                  undoes the shift (MPC.cpp:139-140) and writes the solvent back
+//                  in cell order (next step's input is cell-sorted).
+#pragma once
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "philox.cuh"
+#include "smpc_device.cuh"
+
+namespace smpc {
+
+// ------------------------------------------------------------ load / store
+
+template <typename R>
+struct R4 {
+  R x, y, z, w;
+};
+
+__device__ __forceinline__ R4<float> ld4(const float* p, size_t i) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
+  return R4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ R4<double> ld4(const double* p, size_t i) {
+  const double2* q = reinterpret_cast<const double2*>(p) + 2 * i;
+  const double2 a = __ldg(q), b = __ldg(q + 1);
+  return R4<double>{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ R4<float> ld4_rw(const float* p, size_t i) {
+  const float4 v = reinterpret_cast<const float4*>(p)[i];
+  return R4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ R4<double> ld4_rw(const double* p, size_t i) {
+  const double2* q = reinterpret_cast<const double2*>(p) + 2 * i;
+  const double2 a = q[0], b = q[1];
+  return R4<double>{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void st4(float* p, size_t i, const R4<float>& v) {
+  reinterpret_cast<float4*>(p)[i] = make_float4(v.x, v.y, v.z, v.w);
+}
+__device__ __forceinline__ void st4(double* p, size_t i, const R4<double>& v) {
+  double2* q = reinterpret_cast<double2*>(p) + 2 * i;
+  q[0] = make_double2(v.x, v.y);
+  q[1] = make_double2(v.z, v.w);
+}
+
+__device__ __forceinline__ uint32_t slot_id(float w) { return __float_as_uint(w); }
+__device__ __forceinline__ uint32_t slot_id(double w) {
+  return w < 0.0 ? SLOT_EMPTY : static_cast<uint32_t>(w);
+}
+template <typename R>
+__device__ __forceinline__ R make_slot_id(uint32_t id);
+template <>
+__device__ __forceinline__ float make_slot_id<float>(uint32_t id) { return __uint_as_float(id); }
+template <>
+__device__ __forceinline__ double make_slot_id<double>(uint32_t id) {
+  return id == SLOT_EMPTY ? -1.0 : static_cast<double>(id);
+}
+
+// ------------------------------------------------------- box geometry
+
+// Explicitly rounded arithmetic for the particle frame transform. These are
+// never contracted into FMAs, so k_fluid_bin and k_collide (which recomputes
+// the transform) produce bit-identical coordinates and cell keys in both
+// precisions, whatever the surrounding code is optimised into.
+__device__ __forceinline__ float r_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float r_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float r_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float r_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double r_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double r_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double r_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double r_div(double a, double b) { return __ddiv_rn(a, b); }
+
+// Per-replica constants in the working precision. The FP64 path follows the
+// reference's operation order exactly (-fmad=false): round-half-away,
+// division by L, (cy*shear)*Ly. The FP32 path uses the same operations.
+template <typename R>
+struct Geo {
+  R L[3];
+  R half[3];
+  int Li[3];
+  R shear;
+  R delrx;
+  bool shear_on;
+  int wrap_mono;
+};
+
+template <typename R>
+__device__ __forceinline__ Geo<R> make_geo(const RepInfo& ri, const RepDyn& dn, int mono_bin) {
+  Geo<R> g;
+  for (int d = 0; d < 3; ++d) {
+    g.L[d] = static_cast<R>(ri.L[d]);
+    g.half[d] = static_cast<R>(ri.L[d]) * R(0.5);
+    g.Li[d] = ri.L[d];
+  }
+  g.shear = static_cast<R>(ri.shear);
+  g.delrx = static_cast<R>(dn.delrx);
+  g.shear_on = (ri.shear != 0.0);
+  g.wrap_mono = mono_bin;
+  return g;
+}
+
+// MPC::wrap(Particle&) -> LEBC (MPC.cpp:421-429) or periodic wrap (MPC.cpp:473-478).
+template <typename R>
+__device__ __forceinline__ void le_wrap(const Geo<R>& g, R& x, R& y, R& z, R& vx) {
+  if (g.shear_on) {
+    const R cy = round(r_div(y, g.L[1]));
+    x = r_sub(x, r_mul(g.L[0], round(r_div(x, g.L[0]))));
+    x = r_sub(x, r_mul(cy, g.delrx));
+    x = r_sub(x, r_mul(g.L[0], round(r_div(x, g.L[0]))));
+    y = r_sub(y, r_mul(g.L[1], cy));
+    z = r_sub(z, r_mul(g.L[2], round(r_div(z, g.L[2]))));
+    vx = r_sub(vx, r_mul(r_mul(cy, g.shear), g.L[1]));
+  } else {
+    x = r_sub(x, r_mul(round(r_div(x, g.L[0])), g.L[0]));
+    y = r_sub(y, r_mul(round(r_div(y, g.L[1])), g.L[1]));
+    z = r_sub(z, r_mul(round(r_div(z, g.L[2])), g.L[2]));
+  }
+}
+
+// Cell index of MPC::sort (MPC.cpp:209). strict: the reference's formula,
+// aliasing included, range-checked only against the last cell like the
+// reference; otherwise every axis index is clamped into the box (the fast
+// path: positions exactly on the upper face round onto L in FP32).
+template <typename R>
+__device__ __forceinline__ uint32_t cell_of(const Geo<R>& g, R x, R y, R z, bool strict) {
+  int ix = static_cast<int>(r_add(x, g.half[0]));
+  int iy = static_cast<int>(r_add(y, g.half[1]));
+  int iz = static_cast<int>(r_add(z, g.half[2]));
+  if (strict) {
+    const int c = ix + g.Li[0] * iy + g.Li[0] * g.Li[1] * iz;
+    return static_cast<uint32_t>(c);
+  }
+  ix = min(max(ix, 0), g.Li[0] - 1);
+  iy = min(max(iy, 0), g.Li[1] - 1);
+  iz = min(max(iz, 0), g.Li[2] - 1);
+  return static_cast<uint32_t>(ix + g.Li[0] * (iy + g.Li[1] * iz));
+}
+
+__device__ __forceinline__ void raise_error(ErrorState* e, uint32_t bit, uint32_t a, uint32_t b) {
+  const uint32_t old = atomicOr(&e->word, bit);
+  if ((old & bit) == 0) {
+    e->info[0] = bit;
+    e->info[1] = a;
+    e->info[2] = b;
+  }
+}
+
+// Solvent particle from its stored state to the shifted collision frame:
+// [recentre: x -= COM, v -= COMV, wrap] -> stream x += v h, wrap -> x += s, wrap.
+template <typename R>
+__device__ __forceinline__ void fluid_to_collision_frame(const Geo<R>& g, const RepDyn& dn,
+                                                         R h, R4<R>& x, R4<R>& v) {
+  if (dn.recentre) {
+    x.x = r_sub(x.x, static_cast<R>(dn.com[0]));
+    x.y = r_sub(x.y, static_cast<R>(dn.com[1]));
+    x.z = r_sub(x.z, static_cast<R>(dn.com[2]));
+    v.x = r_sub(v.x, static_cast<R>(dn.comv[0]));
+    v.y = r_sub(v.y, static_cast<R>(dn.comv[1]));
+    v.z = r_sub(v.z, static_cast<R>(dn.comv[2]));
+    le_wrap(g, x.x, x.y, x.z, v.x);
+  }
+  x.x = r_add(x.x, r_mul(v.x, h));
+  x.y = r_add(x.y, r_mul(v.y, h));
+  x.z = r_add(x.z, r_mul(v.z, h));
+  le_wrap(g, x.x, x.y, x.z, v.x);
+  x.x = r_add(x.x, static_cast<R>(dn.shift[0]));
+  x.y = r_add(x.y, static_cast<R>(dn.shift[1]));
+  x.z = r_add(x.z, static_cast<R>(dn.shift[2]));
+  le_wrap(g, x.x, x.y, x.z, v.x);
+}
+
+// Warp-aggregated rank: one atomicAdd per distinct key in the warp. All 32
+// lanes must call it (key KEY_NONE for idle lanes).
+__device__ __forceinline__ uint32_t warp_rank(uint32_t* count, uint32_t key) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (static_cast<int>(lane) == leader && key != KEY_NONE) base = atomicAdd(count + key, __popc(peers));
+  base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// ------------------------------------------------------------ kernels
+
+// Graph mode: advance delrx n_sub times exactly as MPC.cpp:117-118 does on
+// every MD step, draw this collision's grid shift from Philox, and latch the
+// collision counter. One thread per replica.
+template <typename R>
+__global__ void k_cycle_begin(const RepInfo* reps, RepDyn* dyn, int n_rep, int n_adv,
+                              double adv_scale, int gen_shift) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rep) return;
+  const RepInfo ri = reps[r];
+  RepDyn& dn = dyn[r];
+  double d = dn.delrx;
+  const double Lx = static_cast<double>(ri.L[0]);
+  const double adv_dt = __dmul_rn(ri.h, adv_scale);
+  if (n_adv > 0) dn.h = ri.h;
+  for (int s = 0; s < n_adv; ++s) {
+    d = __dadd_rn(d, __dmul_rn(__dmul_rn(ri.shear, static_cast<double>(ri.L[1])), adv_dt));
+    d = __dsub_rn(d, __dmul_rn(Lx, round(__ddiv_rn(d, Lx))));
+  }
+  dn.delrx = d;
+  if (gen_shift) {
+    const unsigned long long step = dn.step;
+    const Uniform2<double> a = philox_uniforms<double>(ri.seed, 0xFFFFFFFFu, step, 0u);
+    const Uniform2<double> b = philox_uniforms<double>(ri.seed, 0xFFFFFFFFu, step, 1u);
+    dn.shift[0] = a.a - 0.5;
+    dn.shift[1] = a.b - 0.5;
+    dn.shift[2] = b.a - 0.5;
+  }
+}
+
+template <typename R>
+__global__ void k_cycle_end(RepDyn* dyn, int n_rep) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n_rep) dyn[r].step += 1ull;
+}
+
+// Solvent initial state on the device for one replica: positions uniform in
+// the box, velocities Maxwell-Boltzmann at kT (or, with ref_vel, uniform in
+// [-1/2, 1/2) as MPC::initialize draws them, MPC.cpp:37-41; the mean is not
+// removed here). Counter-based: particle i of replica seed s always gets the
+// same values. Slots past n_fluid become holes.
+template <typename R>
+__global__ void k_init_solvent(const RepInfo* reps, int rep, R* pos, R* vel,
+                               unsigned long long seed, double kT, int ref_vel) {
+  const RepInfo ri = reps[rep];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ri.slot_cap) return;
+  const size_t slot = static_cast<size_t>(ri.slot_base) + i;
+  if (i >= ri.n_fluid) {
+    st4(pos, slot, R4<R>{R(0), R(0), R(0), make_slot_id<R>(SLOT_EMPTY)});
+    st4(vel, slot, R4<R>{R(0), R(0), R(0), R(0)});
+    return;
+  }
+  const Uniform2<double> a = philox_uniforms<double>(seed, static_cast<uint32_t>(i), 0xA11CEull, 0u);
+  const Uniform2<double> b = philox_uniforms<double>(seed, static_cast<uint32_t>(i), 0xA11CEull, 1u);
+  const Uniform2<double> c = philox_uniforms<double>(seed, static_cast<uint32_t>(i), 0xA11CEull, 2u);
+  const Uniform2<double> d = philox_uniforms<double>(seed, static_cast<uint32_t>(i), 0xA11CEull, 3u);
+  R4<R> x{static_cast<R>((a.a - 0.5) * ri.L[0]), static_cast<R>((a.b - 0.5) * ri.L[1]),
+          static_cast<R>((b.a - 0.5) * ri.L[2]), make_slot_id<R>(static_cast<uint32_t>(i))};
+  R4<R> v;
+  if (ref_vel) {
+    v = R4<R>{static_cast<R>(b.b - 0.5), static_cast<R>(c.a - 0.5), static_cast<R>(c.b - 0.5), R(0)};
+  } else {
+    const double sd = sqrt(kT / ri.solvent_mass);
+    const double r1 = sqrt(-2.0 * log(b.b)), r2 = sqrt(-2.0 * log(c.b));
+    const double t1 = 6.283185307179586 * c.a, t2 = 6.283185307179586 * d.a;
+    v = R4<R>{static_cast<R>(sd * r1 * cos(t1)), static_cast<R>(sd * r1 * sin(t1)),
+              static_cast<R>(sd * r2 * cos(t2)), R(0)};
+  }
+  st4(pos, slot, x);
+  st4(vel, slot, v);
+}
+
+// One CTA per replica: MPC::check_bounds, then shift and bin the monomers.
+template <typename R, int NT>
+__global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* dyn, R* mpos,
+                                                  R* mvel, uint2* mkey, int* mimg,
+                                                  uint32_t* count, ErrorState* err,
+                                                  int mono_bin, int strict) {
+  const int r = blockIdx.x;
+  const RepInfo ri = reps[r];
+  __shared__ int s_out;
+  if (threadIdx.x == 0) s_out = 0;
+  __syncthreads();
+  const int b = ri.mono_base, n = ri.n_mono;
+  // MPC.cpp:166: any monomer with |x_d| >= L_d/2 - 0.5 triggers recentring
+  for (int i = threadIdx.x; i < n; i += NT) {
+    const R4<R> x = ld4_rw(mpos, b + i);
+    const R xs[3] = {x.x, x.y, x.z};
+    for (int d = 0; d < 3; ++d)
+      if (fabs(xs[d]) >= (static_cast<R>(ri.L[d]) * R(0.5) - R(0.5))) s_out = 1;
+  }
+  __syncthreads();
+  RepDyn& dn = dyn[r];
+  const int out = s_out && ri.mol0_size > 0;
+  if (threadIdx.x == 0) {
+    dn.recentre = out;
+    if (out) {
+      // Molecule::calculate_center_of_mass[_velocity] (Molecule.cpp:139-155):
+      // sequential sums over molecule 0, as the reference does.
+      double c[3] = {0, 0, 0}, cv[3] = {0, 0, 0};
+      for (int i = 0; i < ri.mol0_size; ++i) {
+        const R4<R> x = ld4_rw(mpos, b + i);
+        const R4<R> v = ld4_rw(mvel, b + i);
+        c[0] = __dadd_rn(c[0], static_cast<double>(x.x));
+        c[1] = __dadd_rn(c[1], static_cast<double>(x.y));
+        c[2] = __dadd_rn(c[2], static_cast<double>(x.z));
+        cv[0] = __dadd_rn(cv[0], static_cast<double>(v.x));
+        cv[1] = __dadd_rn(cv[1], static_cast<double>(v.y));
+        cv[2] = __dadd_rn(cv[2], static_cast<double>(v.z));
+      }
+      const double nm = static_cast<double>(static_cast<unsigned>(ri.mol0_size));
+      for (int d = 0; d < 3; ++d) {
+        dn.com[d] = __ddiv_rn(c[d], nm);
+        dn.comv[d] = __ddiv_rn(cv[d], nm);
+      }
+    }
+  }
+  __syncthreads();
+  const Geo<R> g = make_geo<R>(ri, dn, mono_bin);
+  const R s0 = static_cast<R>(dn.shift[0]), s1 = static_cast<R>(dn.shift[1]),
+          s2 = static_cast<R>(dn.shift[2]);
+  const R c0 = static_cast<R>(dn.com[0]), c1 = static_cast<R>(dn.com[1]),
+          c2 = static_cast<R>(dn.com[2]);
+  const R cv0 = static_cast<R>(dn.comv[0]), cv1 = static_cast<R>(dn.comv[1]),
+          cv2 = static_cast<R>(dn.comv[2]);
+  const int iters = (n + NT - 1) / NT;
+  for (int it = 0; it < iters; ++it) {
+    const int i = it * NT + threadIdx.x;
+    uint32_t key = KEY_NONE;
+    R4<R> x{}, v{};
+    int img = 0;
+    if (i < n) {
+      x = ld4_rw(mpos, b + i);
+      v = ld4_rw(mvel, b + i);
+      if (out) {
+        x.x -= c0; x.y -= c1; x.z -= c2;
+        v.x -= cv0; v.y -= cv1; v.z -= cv2;
+        st4(mvel, b + i, v);
+      }
+      x.x += s0; x.y += s1; x.z += s2;  // shiftParticles, monomers unwrapped
+      R wx = x.x, wy = x.y, wz = x.z, dvx = R(0);
+      if (mono_bin == MONOBIN_WRAPPED) {
+        img = static_cast<int>(round(wy / g.L[1]));
+        le_wrap(g, wx, wy, wz, dvx);
+      }
+      const uint32_t c = cell_of(g, wx, wy, wz, strict != 0);
+      if (c >= static_cast<uint32_t>(ri.n_cell)) {
+        raise_error(err, ERR_MONO_CELL, static_cast<uint32_t>(r), static_cast<uint32_t>(i));
+      } else {
+        key = static_cast<uint32_t>(ri.cell_base) + c;
+      }
+      // undo the shift right away: nothing reads monomer positions in between
+      x.x += -s0; x.y += -s1; x.z += -s2;
+      st4(mpos, b + i, x);
+    }
+    const uint32_t rank = warp_rank(count, key);
+    if (i < n) {
+      mkey[b + i] = make_uint2(key, rank);
+      mimg[b + i] = img;
+    }
+  }
+}
+
+// Stream, shift, wrap and bin every solvent slot of a slot tile.
+template <typename R, int NT>
+__global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepInfo* reps,
+                                                  const RepDyn* dyn, const R* __restrict__ pos,
+                                                  const R* __restrict__ vel,
+                                                  uint2* __restrict__ keys, uint32_t* count,
+                                                  ErrorState* err, int strict) {
+  const Tile t = tiles[blockIdx.x];
+  const RepInfo& ri = reps[t.rep];
+  const RepDyn dn = dyn[t.rep];
+  const Geo<R> g = make_geo<R>(ri, dn, 0);
+  const R h = static_cast<R>(dn.h);
+  const uint32_t cbase = static_cast<uint32_t>(ri.cell_base);
+  const uint32_t ncell = static_cast<uint32_t>(ri.n_cell);
+  for (int base = t.begin; base < t.end; base += NT) {
+    const int i = base + threadIdx.x;
+    uint32_t key = KEY_NONE;
+    if (i < t.end) {
+      R4<R> x = ld4(pos, i);
+      if (slot_id(x.w) != SLOT_EMPTY) {
+        R4<R> v = ld4(vel, i);
+        fluid_to_collision_frame(g, dn, h, x, v);
+        const uint32_t c = cell_of(g, x.x, x.y, x.z, strict != 0);
+        if (c >= ncell) {
+          raise_error(err, ERR_FLUID_CELL, static_cast<uint32_t>(t.rep), static_cast<uint32_t>(i));
+        } else {
+          key = cbase + c;
+        }
+      }
+    }
+    const uint32_t rank = warp_rank(count, key);
+    if (i < t.end) keys[i] = make_uint2(key, rank);
+  }
+}
+
+// perm[off[key] + rank] = source for every binned solvent slot and monomer.
+__global__ void k_build_perm(const uint2* __restrict__ keys, int n_slots,
+                             const uint2* __restrict__ mkey, int n_mono,
+                             const uint32_t* __restrict__ off, uint32_t* __restrict__ perm);
+
+// --------------------------------------------------------- collide
+
+template <typename R>
+struct AccT;
+template <>
+struct AccT<double> {
+  typedef double type;
+};
+template <>
+struct AccT<float> {
+  typedef long long type;  // 2^32 fixed point: exact, order-independent sums
+};
+
+constexpr float kFixScale = 4294967296.0f;  // 2^32
+constexpr float kFixInv = 2.3283064365386963e-10f;  // 2^-32
+
+template <typename R>
+__device__ __forceinline__ typename AccT<R>::type to_acc(R v);
+template <>
+__device__ __forceinline__ double to_acc<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ long long to_acc<float>(float v) {
+  return __float2ll_rn(v * kFixScale);
+}
+
+// Segmented inclusive scan over lanes holding consecutive sorted particles;
+// the last lane of each run adds the run total into smem[key*Q + q].
+template <typename T, int Q>
+__device__ __forceinline__ void seg_reduce_to_smem(int key, T (&val)[Q], T* smem) {
+  const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int k_up = __shfl_up_sync(0xFFFFFFFFu, key, o);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const T up = __shfl_up_sync(0xFFFFFFFFu, val[q], o);
+      if (lane >= static_cast<unsigned>(o) && k_up == key) val[q] += up;
+    }
+  }
+  const int k_dn = __shfl_down_sync(0xFFFFFFFFu, key, 1);
+  const bool tail = (lane == 31u) || (k_dn != key);
+  if (tail && key >= 0) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) atomicAdd(reinterpret_cast<typename std::conditional<std::is_same<T, double>::value, double, unsigned long long>::type*>(smem + key * Q + q),
+                                          static_cast<typename std::conditional<std::is_same<T, double>::value, double, unsigned long long>::type>(val[q]));
+  }
+}
+
+template <typename R>
+struct Particle {
+  R4<R> x;  // collision-frame position (solvent only)
+  R4<R> v;  // collision-frame velocity
+  R m;
+  int lc;   // local cell in the tile, -1 for an idle lane
+  uint32_t src;
+};
+
+// Everything k_collide needs to turn a sorted position into a particle.
+template <typename R>
+struct CollideCtx {
+  const uint32_t* __restrict__ perm;
+  const R* __restrict__ pos;
+  const R* __restrict__ vel;
+  const R* mpos;
+  R* mvel;
+  const uint2* mkey;
+  const int* mimg;
+  Geo<R> g;
+  RepDyn dn;
+  R h;
+  R solvent_mass;
+  uint32_t cbase;
+  uint32_t c0;
+  int nc;
+  bool strict;
+  ErrorState* err;
+};
+
+template <typename R>
+__device__ __forceinline__ void load_particle(Particle<R>& P, uint32_t p, uint32_t p1,
+                                              const CollideCtx<R>& C) {
+  P.lc = -1;
+  if (p >= p1) return;
+  const uint32_t src = C.perm[p];
+  P.src = src;
+  if (src & MONO_BIT) {
+    const uint32_t m = src & ~MONO_BIT;
+    P.v = ld4_rw(C.mvel, m);
+    P.m = ld4_rw(C.mpos, m).w;
+    if (C.g.wrap_mono == MONOBIN_WRAPPED)
+      P.v.x -= static_cast<R>(C.mimg[m]) * C.g.shear * C.g.L[1];
+    P.lc = static_cast<int>(C.mkey[m].x - C.c0);
+  } else {
+    P.x = ld4(C.pos, src);
+    P.v = ld4(C.vel, src);
+    fluid_to_collision_frame(C.g, C.dn, C.h, P.x, P.v);
+    P.m = C.solvent_mass;
+    const uint32_t c = cell_of(C.g, P.x.x, P.x.y, P.x.z, C.strict);
+    P.lc = static_cast<int>(C.cbase + c - C.c0);
+  }
+  if (P.lc < 0 || P.lc >= C.nc) {  // cannot happen when binning and recompute agree
+    raise_error(C.err, ERR_KEY_MISMATCH, p, src);
+    P.lc = -1;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void acc_momentum(const Particle<R>& P,
+                                             typename AccT<R>::type* s_acc) {
+  typedef typename AccT<R>::type A;
+  A val[4];
+  if (P.lc >= 0) {
+    val[0] = to_acc<R>(P.v.x * P.m);
+    val[1] = to_acc<R>(P.v.y * P.m);
+    val[2] = to_acc<R>(P.v.z * P.m);
+    val[3] = to_acc<R>(P.m);
+  } else {
+    val[0] = val[1] = val[2] = val[3] = A(0);
+  }
+  seg_reduce_to_smem<A, 4>(P.lc, val, s_acc);
+}
+
+template <typename R>
+__device__ __forceinline__ void acc_energy(const Particle<R>& P, const R* s_cmv,
+                                           typename AccT<R>::type* s_e) {
+  typedef typename AccT<R>::type A;
+  A val[1] = {A(0)};
+  if (P.lc >= 0) {
+    const R d0 = P.v.x - s_cmv[3 * P.lc], d1 = P.v.y - s_cmv[3 * P.lc + 1],
+            d2 = P.v.z - s_cmv[3 * P.lc + 2];
+    val[0] = to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2));
+  }
+  seg_reduce_to_smem<A, 1>(P.lc, val, s_e);
+}
+
+// Thermostat + rotation of one particle, then the unshift/wrap and store.
+template <typename R>
+__device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, const R* s_cmv,
+                                                const R* s_rot, const R* s_scale,
+                                                const CollideCtx<R>& C, R* pos_out, R* vel_out,
+                                                ErrorState* err) {
+  if (P.lc < 0) return;
+  const R* cm = s_cmv + 3 * P.lc;
+  const R* M = s_rot + 9 * P.lc;
+  const R sc = s_scale[P.lc];
+  R vx = P.v.x, vy = P.v.y, vz = P.v.z;
+  R d0, d1, d2;
+  if (std::is_same<R, double>::value) {
+    // MPC.cpp:291 then MPC.cpp:267, in the reference's operation order
+    if (sc >= R(0)) {
+      vx = sc * vx + (R(1) - sc) * cm[0];
+      vy = sc * vy + (R(1) - sc) * cm[1];
+      vz = sc * vz + (R(1) - sc) * cm[2];
+    }
+    d0 = vx - cm[0];
+    d1 = vy - cm[1];
+    d2 = vz - cm[2];
+  } else {
+    const R f = sc >= R(0) ? sc : R(1);
+    d0 = (vx - cm[0]) * f;
+    d1 = (vy - cm[1]) * f;
+    d2 = (vz - cm[2]) * f;
+  }
+  vx = cm[0] + ((M[0] * d0 + M[1] * d1) + M[2] * d2);
+  vy = cm[1] + ((M[3] * d0 + M[4] * d1) + M[5] * d2);
+  vz = cm[2] + ((M[6] * d0 + M[7] * d1) + M[8] * d2);
+  if (!(isfinite(vx) && isfinite(vy) && isfinite(vz)))
+    raise_error(err, ERR_NONFINITE, p, P.src);
+  if (P.src & MONO_BIT) {
+    const uint32_t m = P.src & ~MONO_BIT;
+    if (C.g.wrap_mono == MONOBIN_WRAPPED)
+      vx += static_cast<R>(C.mimg[m]) * C.g.shear * C.g.L[1];
+    R4<R> v = ld4_rw(C.mvel, m);
+    v.x = vx;
+    v.y = vy;
+    v.z = vz;
+    st4(C.mvel, m, v);
+    R4<R> hole{R(0), R(0), R(0), make_slot_id<R>(SLOT_EMPTY)};
+    st4(pos_out, p, hole);
+  } else {
+    R4<R> x = P.x;
+    x.x += -static_cast<R>(C.dn.shift[0]);
+    x.y += -static_cast<R>(C.dn.shift[1]);
+    x.z += -static_cast<R>(C.dn.shift[2]);
+    le_wrap(C.g, x.x, x.y, x.z, vx);
+    st4(pos_out, p, x);
+    st4(vel_out, p, R4<R>{vx, vy, vz, R(0)});
+  }
+}
+
+// One CTA per tile of <= CT cells of one replica. Particles are held in
+// registers (PPT per thread); a tile larger than NT*PPT particles reloads
+// the excess in every phase (correct, slower).
+template <typename R, int NT, int CT, int PPT>
+__global__ void __launch_bounds__(NT) k_collide(
+    const Tile* tiles, const RepInfo* reps, const RepDyn* dyn, const uint32_t* __restrict__ off,
+    const uint32_t* __restrict__ perm, const R* __restrict__ pos_in,
+    const R* __restrict__ vel_in, R* __restrict__ pos_out, R* __restrict__ vel_out,
+    const R* mpos, R* mvel, const uint2* mkey, const int* mimg, const double* inj_gamma,
+    const double* inj_uphi, const double* inj_utheta, int rng, double rot_c, double rot_s,
+    int strict, int mono_bin, ErrorState* err) {
+  typedef typename AccT<R>::type A;
+  __shared__ A s_acc[CT * 4];
+  __shared__ A s_e[CT];
+  __shared__ R s_cmv[CT * 3];
+  __shared__ R s_rot[CT * 9];
+  __shared__ R s_scale[CT];
+  __shared__ uint32_t s_off[CT + 1];
+
+  const Tile t = tiles[blockIdx.x];
+  const RepInfo& ri = reps[t.rep];
+  CollideCtx<R> C;
+  C.perm = perm;
+  C.pos = pos_in;
+  C.vel = vel_in;
+  C.mpos = mpos;
+  C.mvel = mvel;
+  C.mkey = mkey;
+  C.mimg = mimg;
+  C.dn = dyn[t.rep];
+  C.g = make_geo<R>(ri, C.dn, mono_bin);
+  C.h = static_cast<R>(C.dn.h);
+  C.solvent_mass = static_cast<R>(ri.solvent_mass);
+  C.cbase = static_cast<uint32_t>(ri.cell_base);
+  C.c0 = static_cast<uint32_t>(t.begin);
+  C.strict = strict != 0;
+  const int nc = t.end - t.begin;
+  C.nc = nc;
+  C.err = err;
+
+  for (int i = threadIdx.x; i <= nc; i += NT) s_off[i] = off[t.begin + i];
+  for (int i = threadIdx.x; i < nc * 4; i += NT) s_acc[i] = A(0);
+  for (int i = threadIdx.x; i < nc; i += NT) s_e[i] = A(0);
+  __syncthreads();
+  const uint32_t p0 = s_off[0], p1 = s_off[nc];
+
+  // phase A: per-cell momentum and mass (MPC::calculateCMV, MPC.cpp:314-322)
+  Particle<R> cache[PPT];
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    cache[k].lc = -1;
+    if (p0 + k * NT < p1) {
+      load_particle(cache[k], p0 + k * NT + threadIdx.x, p1, C);
+      acc_momentum(cache[k], s_acc);
+    }
+  }
+  for (uint32_t base = p0 + PPT * NT; base < p1; base += NT) {
+    Particle<R> P;
+    load_particle(P, base + threadIdx.x, p1, C);
+    acc_momentum(P, s_acc);
+  }
+  __syncthreads();
+  for (int lc = threadIdx.x; lc < nc; lc += NT) {
+    R cm[3];
+    if (std::is_same<R, double>::value) {
+      const R mt = static_cast<R>(s_acc[4 * lc + 3]);
+      for (int d = 0; d < 3; ++d) {
+        cm[d] = static_cast<R>(s_acc[4 * lc + d]);
+        if (mt > R(0)) cm[d] /= mt;
+      }
+    } else {
+      const float mt = static_cast<float>(s_acc[4 * lc + 3]) * kFixInv;
+      for (int d = 0; d < 3; ++d) {
+        const float pd = static_cast<float>(s_acc[4 * lc + d]) * kFixInv;
+        cm[d] = mt > 0.f ? static_cast<R>(pd / mt) : R(0);
+      }
+    }
+    s_cmv[3 * lc] = cm[0];
+    s_cmv[3 * lc + 1] = cm[1];
+    s_cmv[3 * lc + 2] = cm[2];
+  }
+  __syncthreads();
+
+  // phase B: kinetic energy relative to the cell velocity (MPC.cpp:277-280)
+#pragma unroll
+  for (int k = 0; k < PPT; ++k)
+    if (p0 + k * NT < p1) acc_energy(cache[k], s_cmv, s_e);
+  for (uint32_t base = p0 + PPT * NT; base < p1; base += NT) {
+    Particle<R> P;
+    load_particle(P, base + threadIdx.x, p1, C);
+    acc_energy(P, s_cmv, s_e);
+  }
+  __syncthreads();
+
+  // per-cell draws: MBS scaling (MPC.cpp:287-289) and rotation (MPC.cpp:244-257)
+  for (int lc = threadIdx.x; lc < nc; lc += NT) {
+    const uint32_t cg = C.c0 + lc;
+    const uint32_t cl = cg - C.cbase;
+    const uint32_t n = s_off[lc + 1] - s_off[lc];
+    R scale = R(-1);
+    if (n >= 2u) {
+      R ekin;
+      if (std::is_same<R, double>::value) {
+        ekin = static_cast<R>(s_e[lc]);
+        ekin *= R(0.5);
+      } else {
+        ekin = static_cast<R>(static_cast<float>(s_e[lc]) * kFixInv * 0.5f);
+      }
+      R gv;
+      if (rng == RNG_INJECT) {
+        gv = static_cast<R>(inj_gamma[cg]);
+      } else {
+        bool ok = true;
+        gv = philox_gamma<R>(ri.seed, cl, C.dn.step,
+                             static_cast<R>(1.5) * static_cast<R>(n - 1u), &ok) *
+             static_cast<R>(ri.kT);
+        if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, n);
+      }
+      scale = (ekin > R(0)) ? sqrt(gv / ekin) : R(1);
+    }
+    s_scale[lc] = scale;
+    R uphi, uth;
+    if (rng == RNG_INJECT) {
+      uphi = static_cast<R>(inj_uphi[cg]);
+      uth = static_cast<R>(inj_utheta[cg]);
+    } else {
+      const Uniform2<R> u = philox_uniforms<R>(ri.seed, cl, C.dn.step, 0u);
+      uphi = u.a;
+      uth = u.b;
+    }
+    const R two_pi = R(6.283185307179586476925286766559);
+    const R phi = two_pi * uphi;
+    const R theta = R(2) * (uth - R(0.5));
+    const R st = sqrt(R(1) - theta * theta);
+    R sphi, cphi;
+    sincos(phi, &sphi, &cphi);
+    const R a0 = st * cphi, a1 = st * sphi, a2 = theta;
+    const R c = static_cast<R>(rot_c), s = static_cast<R>(rot_s);
+    R* M = s_rot + 9 * lc;
+    M[0] = a0 * a0 + (R(1) - a0 * a0) * c;
+    M[1] = a0 * a1 * (R(1) - c) - a2 * s;
+    M[2] = a0 * a2 * (R(1) - c) + a1 * s;
+    M[3] = a0 * a1 * (R(1) - c) + a2 * s;
+    M[4] = a1 * a1 + (R(1) - a1 * a1) * c;
+    M[5] = a1 * a2 * (R(1) - c) - a0 * s;
+    M[6] = a0 * a2 * (R(1) - c) - a1 * s;
+    M[7] = a1 * a2 * (R(1) - c) + a0 * s;
+    M[8] = a2 * a2 + (R(1) - a2 * a2) * c;
+  }
+  __syncthreads();
+
+  // phase C: apply, undo the grid shift, write back in cell order
+#pragma unroll
+  for (int k = 0; k < PPT; ++k)
+    if (p0 + k * NT < p1)
+      apply_collision(cache[k], p0 + k * NT + threadIdx.x, s_cmv, s_rot, s_scale, C, pos_out,
+                      vel_out, err);
+  for (uint32_t base = p0 + PPT * NT; base < p1; base += NT) {
+    Particle<R> P;
+    load_particle(P, base + threadIdx.x, p1, C);
+    apply_collision(P, base + threadIdx.x, s_cmv, s_rot, s_scale, C, pos_out, vel_out, err);
+  }
+}
+
+// Solvent temperature on the last collision's cells (MPC.cpp:384-418):
+// CMV over every particle of a cell, kinetic energy over its solvent only.
+// One thread per cell; per-tile FP64 partial sums.
+template <typename R, int NT>
+__global__ void __launch_bounds__(NT) k_temperature(
+    const Tile* tiles, const RepInfo* reps, const uint32_t* __restrict__ off,
+    const uint32_t* __restrict__ perm, const R* __restrict__ vel_cur, const R* mpos,
+    const R* mvel, const int* mimg, int mono_bin, TempPartial* partial) {
+  __shared__ double s_e[NT];
+  __shared__ unsigned s_f[NT];
+  const Tile t = tiles[blockIdx.x];
+  const RepInfo& ri = reps[t.rep];
+  const double shearLy = ri.shear * static_cast<double>(ri.L[1]);
+  double e_sum = 0.0;
+  unsigned filled = 0;
+  for (int c = t.begin + threadIdx.x; c < t.end; c += NT) {
+    const uint32_t a = off[c], b = off[c + 1];
+    double px = 0, py = 0, pz = 0, mt = 0;
+    unsigned nf = 0;
+    for (uint32_t p = a; p < b; ++p) {
+      const uint32_t src = perm[p];
+      double vx, vy, vz, m;
+      if (src & MONO_BIT) {
+        const uint32_t mi = src & ~MONO_BIT;
+        const R4<R> v = ld4_rw(mvel, mi);
+        m = static_cast<double>(ld4_rw(mpos, mi).w);
+        vx = v.x; vy = v.y; vz = v.z;
+        if (mono_bin == MONOBIN_WRAPPED) vx -= static_cast<double>(mimg[mi]) * shearLy;
+      } else {
+        const R4<R> v = ld4(vel_cur, p);
+        m = ri.solvent_mass;
+        vx = v.x; vy = v.y; vz = v.z;
+        ++nf;
+      }
+      px += vx * m; py += vy * m; pz += vz * m; mt += m;
+    }
+    if (mt > 0) { px /= mt; py /= mt; pz /= mt; }
+    double ek = 0.0;
+    for (uint32_t p = a; p < b; ++p) {
+      if (perm[p] & MONO_BIT) continue;
+      const R4<R> v = ld4(vel_cur, p);
+      const double d0 = v.x - px, d1 = v.y - py, d2 = v.z - pz;
+      ek += ri.solvent_mass * ((d0 * d0 + d1 * d1) + d2 * d2);
+    }
+    e_sum += ek * 0.5;
+    filled += nf > 0 ? 1u : 0u;
+  }
+  s_e[threadIdx.x] = e_sum;
+  s_f[threadIdx.x] = filled;
+  __syncthreads();
+  for (int s = NT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s_e[threadIdx.x] += s_e[threadIdx.x + s];
+      s_f[threadIdx.x] += s_f[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x].ekin = s_e[0];
+    partial[blockIdx.x].filled = s_f[0];
+  }
+}
+
+}  // namespace smpc

@@ -1,0 +1,139 @@
+// Counting-sort support: exclusive prefix sum of the per-cell counts and the
+// scatter that turns (cell, rank) keys into a cell-ordered permutation. This
+// replaces MPC::sort's vector<vector<MPCParticle*>> push_back cell lists
+// (star-polymers/lib/Hydrodynamics/MPC.cpp:201-237) with integer arithmetic.
+//
+// Scan: three launches over C cells: per-tile scan (2048 cells / CTA, count
+// is re-zeroed for the next collision while it is read), scan of the tile
+// totals (one CTA), add of the tile bases. off[C] receives the total.
+#include <stdint.h>
+
+#include "launch.h"
+#include "mpc_kernels.cuh"
+
+namespace smpc {
+
+constexpr int SCAN_NT = 256;
+constexpr int SCAN_IPT = 8;
+constexpr int SCAN_TILE = SCAN_NT * SCAN_IPT;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sums[SCAN_NT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t s = lane < SCAN_NT / 32 ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < SCAN_NT / 32) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  const uint32_t before = (w > 0 ? warp_sums[w - 1] : 0u) + x - v;
+  *total = warp_sums[SCAN_NT / 32 - 1];
+  return before;
+}
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_tiles(uint32_t* __restrict__ count,
+                                                        uint32_t* __restrict__ off,
+                                                        uint32_t* __restrict__ tile_sum, int n) {
+  const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
+  uint32_t c[SCAN_IPT];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; ++k) {
+    const int i = base + k;
+    c[k] = i < n ? count[i] : 0u;
+    s += c[k];
+  }
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; ++k)
+    if (base + k < n) count[base + k] = 0u;
+  uint32_t total;
+  uint32_t run = block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; ++k) {
+    const int i = base + k;
+    if (i < n) off[i] = run;
+    run += c[k];
+  }
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// Exclusive scan of up to SCAN_TILE tile totals in one CTA.
+__global__ void __launch_bounds__(SCAN_NT) k_scan_tile_sums(uint32_t* __restrict__ tile_sum,
+                                                            int n_tiles,
+                                                            uint32_t* __restrict__ grand) {
+  uint32_t carry = 0;
+  for (int chunk = 0; chunk < n_tiles; chunk += SCAN_TILE) {
+    const int base = chunk + threadIdx.x * SCAN_IPT;
+    uint32_t c[SCAN_IPT];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+      c[k] = base + k < n_tiles ? tile_sum[base + k] : 0u;
+      s += c[k];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(s, &total) + carry;
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+      if (base + k < n_tiles) tile_sum[base + k] = run;
+      run += c[k];
+    }
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *grand = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_add(uint32_t* __restrict__ off,
+                                                      const uint32_t* __restrict__ tile_base,
+                                                      const uint32_t* __restrict__ grand, int n) {
+  const int i = blockIdx.x * SCAN_NT + threadIdx.x;
+  if (i < n) off[i] += tile_base[i / SCAN_TILE];
+  if (i == n) off[n] = *grand;
+}
+
+__global__ void k_build_perm(const uint2* __restrict__ keys, int n_slots,
+                             const uint2* __restrict__ mkey, int n_mono,
+                             const uint32_t* __restrict__ off, uint32_t* __restrict__ perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_slots) {
+    const uint2 k = keys[i];
+    if (k.x != KEY_NONE) perm[off[k.x] + k.y] = static_cast<uint32_t>(i);
+  } else if (i < n_slots + n_mono) {
+    const int m = i - n_slots;
+    const uint2 k = mkey[m];
+    if (k.x != KEY_NONE) perm[off[k.x] + k.y] = MONO_BIT | static_cast<uint32_t>(m);
+  }
+}
+
+int scan_tile_count(int n_cells) { return (n_cells + SCAN_TILE - 1) / SCAN_TILE; }
+
+void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* grand,
+                 int n_cells, cudaStream_t st) {
+  const int tiles = scan_tile_count(n_cells);
+  k_scan_tiles<<<tiles, SCAN_NT, 0, st>>>(count, off, tile_sum, n_cells);
+  k_scan_tile_sums<<<1, SCAN_NT, 0, st>>>(tile_sum, tiles, grand);
+  k_scan_add<<<(n_cells + 1 + SCAN_NT - 1) / SCAN_NT, SCAN_NT, 0, st>>>(off, tile_sum, grand,
+                                                                       n_cells);
+}
+
+void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_mono,
+                       const uint32_t* off, uint32_t* perm, cudaStream_t st) {
+  const int n = n_slots + n_mono;
+  if (n == 0) return;
+  k_build_perm<<<(n + 255) / 256, 256, 0, st>>>(keys, n_slots, mkey, n_mono, off, perm);
+}
+
+}  // namespace smpc

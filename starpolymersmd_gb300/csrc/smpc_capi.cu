@@ -1,0 +1,1033 @@
+// C-ABI implementation (include/smpc.h): device context, uploads/downloads,
+// the step-by-step reference-compatible calls and the graph-captured fused
+// cycle. All device memory is allocated at creation (and when bonds are
+// uploaded); the step calls allocate nothing.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/smpc.h"
+#include "launch.h"
+#include "md_kernels.cuh"
+#include "smpc_device.cuh"
+
+using smpc::ErrorState;
+using smpc::RepDyn;
+using smpc::RepInfo;
+using smpc::TempPartial;
+using smpc::Tile;
+
+struct smpc_ctx {
+  smpc_options opt{};
+  int n_rep = 0;
+  std::vector<RepInfo> reps;
+  std::vector<RepDyn> dyn;  // host mirror: delrx, shift, h are host-owned in step mode
+  std::vector<int> n_fluid, mol0;
+  long long total_cells = 0, total_slots = 0, total_mono = 0;
+  cudaStream_t st = nullptr;
+  int device = 0;
+  size_t real_size = 8;
+
+  RepInfo* d_reps = nullptr;
+  RepDyn* d_dyn = nullptr;
+  Tile* d_bin_tiles = nullptr;
+  int n_bin_tiles = 0;
+  Tile* d_col_tiles = nullptr;
+  int n_col_tiles = 0;
+  std::vector<Tile> h_tmp_tiles;
+  Tile* d_tmp_tiles = nullptr;
+  TempPartial* d_tpart = nullptr;
+
+  void* d_pos[2] = {nullptr, nullptr};
+  void* d_vel[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint2* d_keys = nullptr;
+  uint32_t* d_perm = nullptr;
+  uint32_t* d_count = nullptr;
+  uint32_t* d_off = nullptr;
+  uint32_t* d_tsum = nullptr;
+  uint32_t* d_grand = nullptr;
+
+  void* d_mpos = nullptr;
+  void* d_mvel = nullptr;
+  void* d_mfrc = nullptr;
+  void* d_mver = nullptr;
+  uint2* d_mkey = nullptr;
+  int* d_mimg = nullptr;
+  int* d_bond_start = nullptr;
+  int2* d_bonds = nullptr;
+  int* d_nlist = nullptr;
+  int* d_ncount = nullptr;
+  std::vector<std::vector<int>> bsrc, bdst;
+  std::vector<std::vector<int>> anchor;
+
+  double* d_inj = nullptr;  // gamma | u_phi | u_theta, total_cells each
+  ErrorState* d_err = nullptr;
+  double rot_c = 0, rot_s = 0;
+  int max_nb = 192;
+  bool collided = false;
+  bool md_ready = false;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  std::string err;
+  // host staging reused across calls
+  void* h_stage = nullptr;          // pinned: 3 x 4 x total_mono Reals
+  std::vector<double> h_mass;       // per monomer (pos.w)
+  std::vector<double> h_flags;      // amphi + 2*anchor (vel.w)
+  std::vector<TempPartial> stage_t;
+};
+
+namespace {
+
+int fail(smpc_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CU(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(ctx, SMPC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+}
+
+int check_rep(smpc_ctx* ctx, int rep) {
+  if (!ctx) return SMPC_E_ARG;
+  if (rep < 0 || rep >= ctx->n_rep) return fail(ctx, SMPC_E_ARG, "replica index out of range");
+  return SMPC_OK;
+}
+
+// Host copy of the RepDyn fields the host owns (delrx, shift[3], h): the
+// leading 40 bytes of each record, written with one strided copy.
+constexpr size_t kHostDynBytes = offsetof(RepDyn, com);
+
+int upload_host_dyn(smpc_ctx* ctx) {
+  CU(cudaMemcpy2DAsync(ctx->d_dyn, sizeof(RepDyn), ctx->dyn.data(), sizeof(RepDyn), kHostDynBytes,
+                       ctx->n_rep, cudaMemcpyHostToDevice, ctx->st));
+  return SMPC_OK;
+}
+
+template <typename R>
+smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur);
+
+template <typename R>
+int launch_collision(smpc_ctx* ctx, int rng, int cur) {
+  const int strict = ctx->opt.strict_cells;
+  R* pos_in = static_cast<R*>(ctx->d_pos[cur]);
+  R* vel_in = static_cast<R*>(ctx->d_vel[cur]);
+  R* pos_out = static_cast<R*>(ctx->d_pos[cur ^ 1]);
+  R* vel_out = static_cast<R*>(ctx->d_vel[cur ^ 1]);
+  smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
+                            static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
+                            ctx->d_err, ctx->opt.mono_bin, strict, ctx->st);
+  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, pos_in,
+                            vel_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
+  smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
+                    static_cast<int>(ctx->total_cells), ctx->st);
+  smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
+                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->st);
+  smpc::launch_collide<R>(collide_args<R>(ctx, rng, cur), ctx->st);
+  return SMPC_OK;
+}
+
+template <typename R>
+smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
+  R* pos_in = static_cast<R*>(ctx->d_pos[cur]);
+  R* vel_in = static_cast<R*>(ctx->d_vel[cur]);
+  R* pos_out = static_cast<R*>(ctx->d_pos[cur ^ 1]);
+  R* vel_out = static_cast<R*>(ctx->d_vel[cur ^ 1]);
+  const int strict = ctx->opt.strict_cells;
+  smpc::CollideArgs<R> a;
+  a.tiles = ctx->d_col_tiles;
+  a.n_tiles = ctx->n_col_tiles;
+  a.reps = ctx->d_reps;
+  a.dyn = ctx->d_dyn;
+  a.off = ctx->d_off;
+  a.perm = ctx->d_perm;
+  a.pos_in = pos_in;
+  a.vel_in = vel_in;
+  a.pos_out = pos_out;
+  a.vel_out = vel_out;
+  a.mpos = static_cast<R*>(ctx->d_mpos);
+  a.mvel = static_cast<R*>(ctx->d_mvel);
+  a.mkey = ctx->d_mkey;
+  a.mimg = ctx->d_mimg;
+  a.inj_gamma = ctx->d_inj;
+  a.inj_uphi = ctx->d_inj + ctx->total_cells;
+  a.inj_utheta = ctx->d_inj + 2 * ctx->total_cells;
+  a.rng = rng;
+  a.rot_c = ctx->rot_c;
+  a.rot_s = ctx->rot_s;
+  a.strict = strict;
+  a.mono_bin = ctx->opt.mono_bin;
+  a.err = ctx->d_err;
+  return a;
+}
+
+template <typename R>
+int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
+  if (ctx->total_mono == 0) return SMPC_OK;
+  smpc::MdArgs a;
+  a.reps = ctx->d_reps;
+  a.dyn = ctx->d_dyn;
+  a.bond_start = ctx->d_bond_start;
+  a.bonds = ctx->d_bonds;
+  a.nlist = ctx->d_nlist;
+  a.ncount = ctx->d_ncount;
+  a.n_mono_total = static_cast<int>(ctx->total_mono);
+  a.max_nb = ctx->max_nb;
+  a.n_steps = n;
+  a.calc_epot = calc_epot;
+  a.force_rebuild = force_rebuild;
+  a.err = ctx->d_err;
+  smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
+                     static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->st);
+  return SMPC_OK;
+}
+
+// Phases of one fused cycle, in launch order (smpc_cycles_profiled).
+enum { PH_MD = 0, PH_BEGIN, PH_MONO, PH_BIN, PH_SCAN, PH_PERM, PH_COLLIDE, PH_END, PH_COUNT };
+
+template <typename R>
+int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
+  const int nsub = ctx->opt.step_update;
+  const int strict = ctx->opt.strict_cells;
+  const double adv = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / nsub : 1.0;
+  R* pos_in = static_cast<R*>(ctx->d_pos[cur]);
+  R* vel_in = static_cast<R*>(ctx->d_vel[cur]);
+  cudaEventRecord(ev[0], ctx->st);
+  launch_md_steps<R>(ctx, nsub, 0, 0);
+  cudaEventRecord(ev[1 + PH_MD], ctx->st);
+  smpc::launch_cycle_begin<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, nsub, adv, 1, ctx->st);
+  cudaEventRecord(ev[1 + PH_BEGIN], ctx->st);
+  smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
+                            static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
+                            ctx->d_err, ctx->opt.mono_bin, strict, ctx->st);
+  cudaEventRecord(ev[1 + PH_MONO], ctx->st);
+  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, pos_in,
+                            vel_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
+  cudaEventRecord(ev[1 + PH_BIN], ctx->st);
+  smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
+                    static_cast<int>(ctx->total_cells), ctx->st);
+  cudaEventRecord(ev[1 + PH_SCAN], ctx->st);
+  smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
+                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->st);
+  cudaEventRecord(ev[1 + PH_PERM], ctx->st);
+  smpc::CollideArgs<R> a = collide_args<R>(ctx, smpc::RNG_PHILOX, cur);
+  smpc::launch_collide<R>(a, ctx->st);
+  cudaEventRecord(ev[1 + PH_COLLIDE], ctx->st);
+  smpc::launch_cycle_end<R>(ctx->d_dyn, ctx->n_rep, ctx->st);
+  cudaEventRecord(ev[1 + PH_END], ctx->st);
+  return SMPC_OK;
+}
+
+template <typename R>
+int record_cycle(smpc_ctx* ctx, int cur) {
+  const int nsub = ctx->opt.step_update;
+  launch_md_steps<R>(ctx, nsub, 0, 0);
+  double adv = 1.0;
+  if (ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL) adv = 1.0 / nsub;
+  // h is per replica; k_cycle_begin advances delrx by shear*Ly*h*adv per MD step
+  smpc::launch_cycle_begin<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, nsub, adv, 1, ctx->st);
+  launch_collision<R>(ctx, smpc::RNG_PHILOX, cur);
+  smpc::launch_cycle_end<R>(ctx->d_dyn, ctx->n_rep, ctx->st);
+  return SMPC_OK;
+}
+
+template <typename R>
+void to_r4(const double* p3, double w, R* out, size_t i) {
+  out[4 * i + 0] = static_cast<R>(p3[3 * i + 0]);
+  out[4 * i + 1] = static_cast<R>(p3[3 * i + 1]);
+  out[4 * i + 2] = static_cast<R>(p3[3 * i + 2]);
+  out[4 * i + 3] = static_cast<R>(w);
+}
+
+template <typename R>
+uint32_t id_of(R w);
+template <>
+uint32_t id_of<float>(float w) {
+  uint32_t u;
+  std::memcpy(&u, &w, 4);
+  return u;
+}
+template <>
+uint32_t id_of<double>(double w) {
+  return w < 0 ? smpc::SLOT_EMPTY : static_cast<uint32_t>(w);
+}
+template <typename R>
+R id_to_w(uint32_t id);
+template <>
+float id_to_w<float>(uint32_t id) {
+  float f;
+  std::memcpy(&f, &id, 4);
+  return f;
+}
+template <>
+double id_to_w<double>(uint32_t id) {
+  return id == smpc::SLOT_EMPTY ? -1.0 : static_cast<double>(id);
+}
+
+template <typename R>
+int set_fluid_t(smpc_ctx* ctx, int rep, const double* pos, const double* vel) {
+  const RepInfo& ri = ctx->reps[rep];
+  std::vector<R> p(4 * static_cast<size_t>(ri.slot_cap)), v(4 * static_cast<size_t>(ri.slot_cap));
+  for (int i = 0; i < ri.slot_cap; ++i) {
+    if (i < ri.n_fluid) {
+      to_r4<R>(pos, 0.0, p.data(), i);
+      p[4 * i + 3] = id_to_w<R>(static_cast<uint32_t>(i));
+      to_r4<R>(vel, 0.0, v.data(), i);
+    } else {
+      for (int d = 0; d < 3; ++d) p[4 * i + d] = v[4 * i + d] = R(0);
+      p[4 * i + 3] = id_to_w<R>(smpc::SLOT_EMPTY);
+      v[4 * i + 3] = R(0);
+    }
+  }
+  const size_t off = 4 * static_cast<size_t>(ri.slot_base);
+  const size_t bytes = p.size() * sizeof(R);
+  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_pos[ctx->cur]) + off, p.data(), bytes,
+                     cudaMemcpyHostToDevice, ctx->st));
+  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_vel[ctx->cur]) + off, v.data(), bytes,
+                     cudaMemcpyHostToDevice, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+template <typename R>
+int get_fluid_t(smpc_ctx* ctx, int rep, double* pos, double* vel) {
+  const RepInfo& ri = ctx->reps[rep];
+  std::vector<R> p(4 * static_cast<size_t>(ri.slot_cap)), v(4 * static_cast<size_t>(ri.slot_cap));
+  const size_t off = 4 * static_cast<size_t>(ri.slot_base);
+  const size_t bytes = p.size() * sizeof(R);
+  CU(cudaMemcpyAsync(p.data(), static_cast<R*>(ctx->d_pos[ctx->cur]) + off, bytes,
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaMemcpyAsync(v.data(), static_cast<R*>(ctx->d_vel[ctx->cur]) + off, bytes,
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  int seen = 0;
+  for (int i = 0; i < ri.slot_cap; ++i) {
+    const uint32_t id = id_of<R>(p[4 * i + 3]);
+    if (id == smpc::SLOT_EMPTY) continue;
+    if (id >= static_cast<uint32_t>(ri.n_fluid))
+      return fail(ctx, SMPC_E_STATE, "corrupt solvent slot id");
+    for (int d = 0; d < 3; ++d) {
+      if (pos) pos[3 * static_cast<size_t>(id) + d] = static_cast<double>(p[4 * i + d]);
+      if (vel) vel[3 * static_cast<size_t>(id) + d] = static_cast<double>(v[4 * i + d]);
+    }
+    ++seen;
+  }
+  if (seen != ri.n_fluid)
+    return fail(ctx, SMPC_E_DEVICE, "solvent particles lost (" + std::to_string(seen) + " of " +
+                                        std::to_string(ri.n_fluid) + "); see smpc_error_word");
+  return SMPC_OK;
+}
+
+template <typename R>
+int set_monomers_t(smpc_ctx* ctx, int rep, const double* pos, const double* vel,
+                   const double* force, const double* mass, const int* amphi, const int* anchor) {
+  const RepInfo& ri = ctx->reps[rep];
+  const size_t n = static_cast<size_t>(ri.n_mono);
+  std::vector<R> p(4 * n), v(4 * n), f(4 * n), pv(4 * n);
+  ctx->anchor[rep].assign(n, 0);
+  for (size_t i = 0; i < n; ++i) {
+    const int fl = (amphi ? (amphi[i] != 0) : 0) + 2 * (anchor ? (anchor[i] != 0) : 0);
+    ctx->anchor[rep][i] = anchor ? (anchor[i] != 0) : 0;
+    ctx->h_mass[ri.mono_base + i] = mass ? mass[i] : 1.0;
+    ctx->h_flags[ri.mono_base + i] = static_cast<double>(fl);
+    to_r4<R>(pos, mass ? mass[i] : 1.0, p.data(), i);
+    to_r4<R>(vel, static_cast<double>(fl), v.data(), i);
+    if (force) {
+      to_r4<R>(force, 0.0, f.data(), i);
+    } else {
+      for (int d = 0; d < 4; ++d) f[4 * i + d] = R(0);
+    }
+    to_r4<R>(pos, 0.0, pv.data(), i);
+  }
+  const size_t off = 4 * static_cast<size_t>(ri.mono_base);
+  const size_t bytes = 4 * n * sizeof(R);
+  if (n == 0) return SMPC_OK;
+  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_mpos) + off, p.data(), bytes, cudaMemcpyHostToDevice, ctx->st));
+  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_mvel) + off, v.data(), bytes, cudaMemcpyHostToDevice, ctx->st));
+  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_mfrc) + off, f.data(), bytes, cudaMemcpyHostToDevice, ctx->st));
+  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_mver) + off, pv.data(), bytes, cudaMemcpyHostToDevice, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+template <typename R>
+int get_monomers_t(smpc_ctx* ctx, int rep, double* pos, double* vel, double* force) {
+  const RepInfo& ri = ctx->reps[rep];
+  const size_t n = static_cast<size_t>(ri.n_mono);
+  if (n == 0) return SMPC_OK;
+  std::vector<R> p(4 * n), v(4 * n), f(4 * n);
+  const size_t off = 4 * static_cast<size_t>(ri.mono_base);
+  const size_t bytes = 4 * n * sizeof(R);
+  CU(cudaMemcpyAsync(p.data(), static_cast<R*>(ctx->d_mpos) + off, bytes, cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaMemcpyAsync(v.data(), static_cast<R*>(ctx->d_mvel) + off, bytes, cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaMemcpyAsync(f.data(), static_cast<R*>(ctx->d_mfrc) + off, bytes, cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  for (size_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      if (pos) pos[3 * i + d] = static_cast<double>(p[4 * i + d]);
+      if (vel) vel[3 * i + d] = static_cast<double>(v[4 * i + d]);
+      if (force) force[3 * i + d] = static_cast<double>(f[4 * i + d]);
+    }
+  return SMPC_OK;
+}
+
+// All replicas' monomers in one transfer each way (replicas concatenated),
+// through pinned staging buffers allocated at creation. Masses and type flags
+// (the .w lanes) come from the host copy kept by smpc_set_monomers.
+template <typename R>
+int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, double* pos_out,
+                   double* vel_out, double* force_out) {
+  const size_t n = static_cast<size_t>(ctx->total_mono);
+  if (n == 0) return SMPC_OK;
+  R* p = static_cast<R*>(ctx->h_stage);
+  R* v = p + 4 * n;
+  R* f = v + 4 * n;
+  if (pos_in) {
+    for (size_t i = 0; i < n; ++i) {
+      for (int d = 0; d < 3; ++d) {
+        p[4 * i + d] = static_cast<R>(pos_in[3 * i + d]);
+        v[4 * i + d] = static_cast<R>(vel_in[3 * i + d]);
+      }
+      p[4 * i + 3] = static_cast<R>(ctx->h_mass[i]);
+      v[4 * i + 3] = static_cast<R>(ctx->h_flags[i]);
+    }
+    CU(cudaMemcpyAsync(ctx->d_mpos, p, 4 * n * sizeof(R), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_mvel, v, 4 * n * sizeof(R), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaStreamSynchronize(ctx->st));
+    return SMPC_OK;
+  }
+  CU(cudaMemcpyAsync(p, ctx->d_mpos, 4 * n * sizeof(R), cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaMemcpyAsync(v, ctx->d_mvel, 4 * n * sizeof(R), cudaMemcpyDeviceToHost, ctx->st));
+  if (force_out)
+    CU(cudaMemcpyAsync(f, ctx->d_mfrc, 4 * n * sizeof(R), cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  for (size_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      if (pos_out) pos_out[3 * i + d] = static_cast<double>(p[4 * i + d]);
+      if (vel_out) vel_out[3 * i + d] = static_cast<double>(v[4 * i + d]);
+      if (force_out) force_out[3 * i + d] = static_cast<double>(f[4 * i + d]);
+    }
+  return SMPC_OK;
+}
+
+template <typename R>
+int temperature_all_t(smpc_ctx* ctx, double* out) {
+  if (!ctx->collided) return fail(ctx, SMPC_E_STATE, "no collision has run yet (no cell lists)");
+  const int nt = static_cast<int>(ctx->h_tmp_tiles.size());
+  smpc::launch_temperature<R>(ctx->d_tmp_tiles, nt, ctx->d_reps, ctx->d_off, ctx->d_perm,
+                              static_cast<R*>(ctx->d_vel[ctx->cur]), static_cast<R*>(ctx->d_mpos),
+                              static_cast<R*>(ctx->d_mvel), ctx->d_mimg, ctx->opt.mono_bin,
+                              ctx->d_tpart, ctx->st);
+  ctx->stage_t.resize(nt);
+  CU(cudaMemcpyAsync(ctx->stage_t.data(), ctx->d_tpart, nt * sizeof(TempPartial),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  std::vector<double> e(ctx->n_rep, 0.0);
+  std::vector<unsigned> filled(ctx->n_rep, 0);
+  for (int t = 0; t < nt; ++t) {
+    e[ctx->h_tmp_tiles[t].rep] += ctx->stage_t[t].ekin;
+    filled[ctx->h_tmp_tiles[t].rep] += ctx->stage_t[t].filled;
+  }
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    const unsigned nf = static_cast<unsigned>(ctx->reps[r].n_fluid);
+    out[r] = 2. * e[r] / (3. * static_cast<unsigned>(nf - filled[r]));
+  }
+  return SMPC_OK;
+}
+
+template <typename R>
+int temperature_t(smpc_ctx* ctx, int rep, double* out) {
+  if (!ctx->collided) return fail(ctx, SMPC_E_STATE, "no collision has run yet (no cell lists)");
+  // tiles of this replica only
+  int first = -1, count = 0;
+  for (size_t t = 0; t < ctx->h_tmp_tiles.size(); ++t)
+    if (ctx->h_tmp_tiles[t].rep == rep) {
+      if (first < 0) first = static_cast<int>(t);
+      ++count;
+    }
+  smpc::launch_temperature<R>(ctx->d_tmp_tiles + first, count, ctx->d_reps, ctx->d_off,
+                              ctx->d_perm, static_cast<R*>(ctx->d_vel[ctx->cur]),
+                              static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
+                              ctx->d_mimg, ctx->opt.mono_bin, ctx->d_tpart, ctx->st);
+  std::vector<TempPartial> part(count);
+  CU(cudaMemcpyAsync(part.data(), ctx->d_tpart, count * sizeof(TempPartial),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  double e = 0.0;
+  unsigned filled = 0;
+  for (auto& p : part) {
+    e += p.ekin;
+    filled += p.filled;
+  }
+  const unsigned nf = static_cast<unsigned>(ctx->reps[rep].n_fluid);
+  *out = 2. * e / (3. * static_cast<unsigned>(nf - filled));
+  return SMPC_OK;
+}
+
+std::vector<Tile> make_tiles(const std::vector<RepInfo>& reps, bool cells, int per_tile) {
+  std::vector<Tile> t;
+  for (size_t r = 0; r < reps.size(); ++r) {
+    const int b = cells ? reps[r].cell_base : reps[r].slot_base;
+    const int n = cells ? reps[r].n_cell : reps[r].slot_cap;
+    for (int s = 0; s < n; s += per_tile) t.push_back(Tile{static_cast<int>(r), b + s, b + std::min(n, s + per_tile), 0});
+  }
+  return t;
+}
+
+template <typename R>
+int create_buffers(smpc_ctx* ctx) {
+  const size_t S = static_cast<size_t>(ctx->total_slots), M = static_cast<size_t>(ctx->total_mono),
+               C = static_cast<size_t>(ctx->total_cells);
+  for (int k = 0; k < 2; ++k) {
+    CU(dalloc(reinterpret_cast<R**>(&ctx->d_pos[k]), 4 * S));
+    CU(dalloc(reinterpret_cast<R**>(&ctx->d_vel[k]), 4 * S));
+  }
+  CU(dalloc(&ctx->d_keys, S));
+  CU(dalloc(&ctx->d_perm, S + M));
+  CU(dalloc(&ctx->d_count, C));
+  CU(cudaMemset(ctx->d_count, 0, C * sizeof(uint32_t)));
+  CU(dalloc(&ctx->d_off, C + 1));
+  CU(dalloc(&ctx->d_tsum, static_cast<size_t>(smpc::scan_tile_count(static_cast<int>(C)))));
+  CU(dalloc(&ctx->d_grand, 1));
+  CU(dalloc(reinterpret_cast<R**>(&ctx->d_mpos), 4 * M));
+  CU(dalloc(reinterpret_cast<R**>(&ctx->d_mvel), 4 * M));
+  CU(dalloc(reinterpret_cast<R**>(&ctx->d_mfrc), 4 * M));
+  CU(dalloc(reinterpret_cast<R**>(&ctx->d_mver), 4 * M));
+  CU(dalloc(&ctx->d_mkey, M));
+  CU(dalloc(&ctx->d_mimg, M));
+  CU(dalloc(&ctx->d_ncount, M));
+  CU(cudaMemset(ctx->d_ncount, 0, (M ? M : 1) * sizeof(int)));
+  CU(dalloc(&ctx->d_nlist, static_cast<size_t>(ctx->max_nb) * M));
+  CU(dalloc(&ctx->d_bond_start, M + 1));
+  CU(cudaMemset(ctx->d_bond_start, 0, (M + 1) * sizeof(int)));
+  CU(dalloc(&ctx->d_inj, 3 * C));
+  CU(cudaMemset(ctx->d_inj, 0, 3 * C * sizeof(double)));
+  CU(cudaMallocHost(&ctx->h_stage, (12 * M + 4) * sizeof(R)));
+  ctx->h_mass.assign(M, 1.0);
+  ctx->h_flags.assign(M, 0.0);
+  return SMPC_OK;
+}
+
+int upload_bonds(smpc_ctx* ctx) {
+  // undirected CSR over global monomers; entry (partner, anchor flag of the
+  // directed bond's source: the core owns its bonds, Molecule.cpp:146)
+  const size_t M = static_cast<size_t>(ctx->total_mono);
+  std::vector<std::vector<int2>> adj(M);
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    const int b = ctx->reps[r].mono_base;
+    for (size_t k = 0; k < ctx->bsrc[r].size(); ++k) {
+      const int s = ctx->bsrc[r][k], d = ctx->bdst[r][k];
+      const int anch = ctx->anchor[r].empty() ? 0 : ctx->anchor[r][s];
+      adj[b + s].push_back(make_int2(b + d, anch));
+      adj[b + d].push_back(make_int2(b + s, anch));
+    }
+  }
+  std::vector<int> start(M + 1, 0);
+  std::vector<int2> flat;
+  for (size_t i = 0; i < M; ++i) {
+    start[i] = static_cast<int>(flat.size());
+    flat.insert(flat.end(), adj[i].begin(), adj[i].end());
+  }
+  start[M] = static_cast<int>(flat.size());
+  if (ctx->d_bonds) cudaFree(ctx->d_bonds);
+  ctx->d_bonds = nullptr;
+  CU(dalloc(&ctx->d_bonds, flat.size()));
+  if (!flat.empty())
+    CU(cudaMemcpy(ctx->d_bonds, flat.data(), flat.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ctx->d_bond_start, start.data(), (M + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  return SMPC_OK;
+}
+
+void free_all(smpc_ctx* ctx) {
+  for (int k = 0; k < 2; ++k) {
+    if (ctx->graph[k]) cudaGraphExecDestroy(ctx->graph[k]);
+    cudaFree(ctx->d_pos[k]);
+    cudaFree(ctx->d_vel[k]);
+  }
+  void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
+                  ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
+                  ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
+                  ctx->d_mimg, ctx->d_bond_start, ctx->d_bonds, ctx->d_nlist, ctx->d_ncount,
+                  ctx->d_inj, ctx->d_err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+}
+
+template <typename R>
+int dispatch_collision(smpc_ctx* ctx, int rng) {
+  launch_collision<R>(ctx, rng, ctx->cur);
+  if (rng == SMPC_RNG_PHILOX) smpc::launch_cycle_end<R>(ctx->d_dyn, ctx->n_rep, ctx->st);
+  ctx->cur ^= 1;
+  ctx->collided = true;
+  return SMPC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* opt,
+                smpc_ctx** out) {
+  if (!descs || n_rep <= 0 || !opt || !out) return SMPC_E_ARG;
+  *out = nullptr;
+  smpc_ctx* ctx = new smpc_ctx();
+  ctx->opt = *opt;
+  if (ctx->opt.step_update <= 0) ctx->opt.step_update = 1;
+  if (ctx->opt.max_neighbors > 0) ctx->max_nb = ctx->opt.max_neighbors;
+  ctx->n_rep = n_rep;
+  ctx->device = opt->device;
+  ctx->real_size = opt->precision == SMPC_FP64 ? 8 : 4;
+  ctx->rot_c = std::cos(130.0 * M_PI / 180.0);  // MPC.cpp:23-24
+  ctx->rot_s = std::sin(130.0 * M_PI / 180.0);
+  auto bail = [&](int code, const std::string& msg) {
+    // creation failed: report through stderr-free path and release everything
+    free_all(ctx);
+    delete ctx;
+    (void)msg;
+    return code;
+  };
+  if (opt->precision != SMPC_FP64 && opt->precision != SMPC_FP32) return bail(SMPC_E_ARG, "precision");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return bail(SMPC_E_CUDA, "cudaSetDevice");
+  long long cells = 0, slots = 0, mono = 0;
+  for (int r = 0; r < n_rep; ++r) {
+    const smpc_replica_desc& d = descs[r];
+    if (d.L[0] <= 0 || d.L[1] <= 0 || d.L[2] <= 0 || d.n_fluid < 0 || d.n_mono < 0)
+      return bail(SMPC_E_ARG, "replica geometry");
+    if (d.n_mono > smpc::md_max_monomers()) return bail(SMPC_E_UNSUPPORTED, "too many monomers");
+    RepInfo ri{};
+    for (int k = 0; k < 3; ++k) ri.L[k] = d.L[k];
+    ri.n_cell = d.L[0] * d.L[1] * d.L[2];
+    ri.cell_base = static_cast<int>(cells);
+    ri.slot_base = static_cast<int>(slots);
+    ri.slot_cap = d.n_fluid + d.n_mono;
+    ri.n_fluid = d.n_fluid;
+    ri.mono_base = static_cast<int>(mono);
+    ri.n_mono = d.n_mono;
+    ri.mol0_size = d.mol0_size;
+    ri.shear = d.shear;
+    ri.kT = d.kT;
+    ri.h = d.h;
+    ri.md_dt = d.md_dt;
+    ri.lambda = d.lambda;
+    ri.r_cut = d.r_cut;
+    ri.r_verlet = d.r_verlet;
+    ri.solvent_mass = d.solvent_mass > 0 ? d.solvent_mass : 1.0;
+    ri.seed = d.seed;
+    ri.potential = d.potential;
+    ri.n_sub = ctx->opt.step_update;
+    cells += ri.n_cell;
+    slots += ri.slot_cap;
+    mono += ri.n_mono;
+    ctx->reps.push_back(ri);
+    RepDyn dn{};
+    dn.h = d.h;
+    ctx->dyn.push_back(dn);
+  }
+  if (slots + mono >= 0x7FFFFFFFll || cells >= 0x7FFFFFFFll) return bail(SMPC_E_UNSUPPORTED, "too large");
+  ctx->total_cells = cells;
+  ctx->total_slots = slots;
+  ctx->total_mono = mono;
+  ctx->bsrc.resize(n_rep);
+  ctx->bdst.resize(n_rep);
+  ctx->anchor.resize(n_rep);
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(SMPC_E_CUDA, "stream");
+  int rc = opt->precision == SMPC_FP64 ? create_buffers<double>(ctx) : create_buffers<float>(ctx);
+  if (rc) return bail(rc, ctx->err);
+  const int ct = opt->precision == SMPC_FP64 ? smpc::collide_cells_per_tile<double>()
+                                             : smpc::collide_cells_per_tile<float>();
+  std::vector<Tile> bin = make_tiles(ctx->reps, false, smpc::fluid_slots_per_tile());
+  std::vector<Tile> col = make_tiles(ctx->reps, true, ct);
+  ctx->h_tmp_tiles = make_tiles(ctx->reps, true, smpc::temperature_cells_per_tile());
+  ctx->n_bin_tiles = static_cast<int>(bin.size());
+  ctx->n_col_tiles = static_cast<int>(col.size());
+  bool ok = dalloc(&ctx->d_reps, n_rep) == cudaSuccess && dalloc(&ctx->d_dyn, n_rep) == cudaSuccess &&
+            dalloc(&ctx->d_bin_tiles, bin.size()) == cudaSuccess &&
+            dalloc(&ctx->d_col_tiles, col.size()) == cudaSuccess &&
+            dalloc(&ctx->d_tmp_tiles, ctx->h_tmp_tiles.size()) == cudaSuccess &&
+            dalloc(&ctx->d_tpart, ctx->h_tmp_tiles.size()) == cudaSuccess &&
+            dalloc(&ctx->d_err, 1) == cudaSuccess;
+  if (!ok) return bail(SMPC_E_CUDA, "alloc");
+  ok = cudaMemcpy(ctx->d_reps, ctx->reps.data(), n_rep * sizeof(RepInfo), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(ctx->d_dyn, ctx->dyn.data(), n_rep * sizeof(RepDyn), cudaMemcpyHostToDevice) == cudaSuccess &&
+       (bin.empty() || cudaMemcpy(ctx->d_bin_tiles, bin.data(), bin.size() * sizeof(Tile), cudaMemcpyHostToDevice) == cudaSuccess) &&
+       (col.empty() || cudaMemcpy(ctx->d_col_tiles, col.data(), col.size() * sizeof(Tile), cudaMemcpyHostToDevice) == cudaSuccess) &&
+       (ctx->h_tmp_tiles.empty() || cudaMemcpy(ctx->d_tmp_tiles, ctx->h_tmp_tiles.data(), ctx->h_tmp_tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice) == cudaSuccess) &&
+       cudaMemset(ctx->d_err, 0, sizeof(ErrorState)) == cudaSuccess;
+  if (!ok) return bail(SMPC_E_CUDA, "upload");
+  // empty solvent state until smpc_set_fluid: every slot a hole
+  for (int r = 0; r < n_rep; ++r) {
+    std::vector<double> z(3 * static_cast<size_t>(ctx->reps[r].n_fluid) + 3, 0.0);
+    rc = opt->precision == SMPC_FP64 ? set_fluid_t<double>(ctx, r, z.data(), z.data())
+                                     : set_fluid_t<float>(ctx, r, z.data(), z.data());
+    if (rc) return bail(rc, ctx->err);
+  }
+  *out = ctx;
+  return SMPC_OK;
+}
+
+void smpc_destroy(smpc_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  free_all(ctx);
+  delete ctx;
+}
+
+const char* smpc_last_error(const smpc_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int smpc_n_cells(const smpc_ctx* ctx, int rep) {
+  if (!ctx || rep < 0 || rep >= ctx->n_rep) return -1;
+  return ctx->reps[rep].n_cell;
+}
+
+int smpc_set_fluid(smpc_ctx* ctx, int rep, const double* pos, const double* vel) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (!pos || !vel) return fail(ctx, SMPC_E_ARG, "null buffer");
+  return ctx->opt.precision == SMPC_FP64 ? set_fluid_t<double>(ctx, rep, pos, vel)
+                                         : set_fluid_t<float>(ctx, rep, pos, vel);
+}
+
+int smpc_get_fluid(smpc_ctx* ctx, int rep, double* pos, double* vel) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  return ctx->opt.precision == SMPC_FP64 ? get_fluid_t<double>(ctx, rep, pos, vel)
+                                         : get_fluid_t<float>(ctx, rep, pos, vel);
+}
+
+int smpc_set_monomers(smpc_ctx* ctx, int rep, const double* pos, const double* vel,
+                      const double* force, const double* mass, const int* amphi,
+                      const int* anchor) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (ctx->reps[rep].n_mono > 0 && (!pos || !vel)) return fail(ctx, SMPC_E_ARG, "null buffer");
+  ctx->md_ready = false;
+  return ctx->opt.precision == SMPC_FP64
+             ? set_monomers_t<double>(ctx, rep, pos, vel, force, mass, amphi, anchor)
+             : set_monomers_t<float>(ctx, rep, pos, vel, force, mass, amphi, anchor);
+}
+
+int smpc_get_monomers(smpc_ctx* ctx, int rep, double* pos, double* vel, double* force) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  return ctx->opt.precision == SMPC_FP64 ? get_monomers_t<double>(ctx, rep, pos, vel, force)
+                                         : get_monomers_t<float>(ctx, rep, pos, vel, force);
+}
+
+int smpc_set_bonds(smpc_ctx* ctx, int rep, int n_bond, const int* src, const int* dst) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (n_bond < 0 || (n_bond > 0 && (!src || !dst))) return fail(ctx, SMPC_E_ARG, "bonds");
+  const int n = ctx->reps[rep].n_mono;
+  ctx->bsrc[rep].assign(src, src + n_bond);
+  ctx->bdst[rep].assign(dst, dst + n_bond);
+  for (int k = 0; k < n_bond; ++k)
+    if (src[k] < 0 || src[k] >= n || dst[k] < 0 || dst[k] >= n)
+      return fail(ctx, SMPC_E_ARG, "bond index out of range");
+  ctx->md_ready = false;
+  return SMPC_OK;
+}
+
+int smpc_init_md(smpc_ctx* ctx) {
+  if (!ctx) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  if (int rc = upload_bonds(ctx)) return rc;
+  int rc = ctx->opt.precision == SMPC_FP64 ? launch_md_steps<double>(ctx, 0, 0, 1)
+                                           : launch_md_steps<float>(ctx, 0, 0, 1);
+  if (rc) return rc;
+  CU(cudaGetLastError());
+  ctx->md_ready = true;
+  return SMPC_OK;
+}
+
+int smpc_md_substeps(smpc_ctx* ctx, int n, int calc_epot) {
+  if (!ctx || n < 0) return SMPC_E_ARG;
+  if (ctx->total_mono > 0 && !ctx->md_ready) return fail(ctx, SMPC_E_STATE, "smpc_init_md not called");
+  if (n == 0) return SMPC_OK;
+  int rc = ctx->opt.precision == SMPC_FP64 ? launch_md_steps<double>(ctx, n, calc_epot, 0)
+                                           : launch_md_steps<float>(ctx, n, calc_epot, 0);
+  if (rc) return rc;
+  CU(cudaGetLastError());
+  return SMPC_OK;
+}
+
+int smpc_mpc_step(smpc_ctx* ctx, long t, double dt, const smpc_inject* inj) {
+  if (!ctx) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  const int su = ctx->opt.step_update;
+  const double scale = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / su : 1.0;
+  // MPC.cpp:117-118 on every call, FP64, on the host
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    RepDyn& dn = ctx->dyn[r];
+    const RepInfo& ri = ctx->reps[r];
+    dn.delrx += ri.shear * ri.L[1] * (dt * scale);
+    dn.delrx -= ri.L[0] * std::round(dn.delrx / ri.L[0]);
+    dn.h = dt;
+  }
+  if (t % su) return upload_host_dyn(ctx);
+  const int rng = ctx->opt.rng;
+  if (rng == SMPC_RNG_INJECT) {
+    if (!inj || !inj->shift || !inj->gamma || !inj->u_phi || !inj->u_theta)
+      return fail(ctx, SMPC_E_ARG, "inject mode needs shift, gamma, u_phi and u_theta");
+    for (int r = 0; r < ctx->n_rep; ++r)
+      for (int d = 0; d < 3; ++d) ctx->dyn[r].shift[d] = inj->shift[3 * r + d];
+    const size_t C = static_cast<size_t>(ctx->total_cells);
+    CU(cudaMemcpyAsync(ctx->d_inj, inj->gamma, C * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_inj + C, inj->u_phi, C * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_inj + 2 * C, inj->u_theta, C * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  }
+  if (int rc = upload_host_dyn(ctx)) return rc;
+  if (rng == SMPC_RNG_PHILOX) {
+    // device draws the shift from this collision's counter
+    if (ctx->opt.precision == SMPC_FP64)
+      smpc::launch_cycle_begin<double>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, 0, 0.0, 1, ctx->st);
+    else
+      smpc::launch_cycle_begin<float>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, 0, 0.0, 1, ctx->st);
+  }
+  int rc = ctx->opt.precision == SMPC_FP64 ? dispatch_collision<double>(ctx, rng)
+                                           : dispatch_collision<float>(ctx, rng);
+  if (rc) return rc;
+  CU(cudaGetLastError());
+  if (rng == SMPC_RNG_INJECT) CU(cudaStreamSynchronize(ctx->st));  // injected buffers are borrowed
+  return SMPC_OK;
+}
+
+int smpc_cycles(smpc_ctx* ctx, int n) {
+  if (!ctx || n < 0) return SMPC_E_ARG;
+  if (ctx->opt.rng != SMPC_RNG_PHILOX) return fail(ctx, SMPC_E_STATE, "fused cycles need Philox draws");
+  if (ctx->total_mono > 0 && !ctx->md_ready) return fail(ctx, SMPC_E_STATE, "smpc_init_md not called");
+  cudaSetDevice(ctx->device);
+  // the host mirror of delrx is authoritative between calls
+  if (int rc = upload_host_dyn(ctx)) return rc;
+  const double scale = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / ctx->opt.step_update : 1.0;
+  for (int i = 0; i < n; ++i) {
+    const int cur = ctx->cur;
+    if (!ctx->graph[cur]) {
+      cudaGraph_t g;
+      CU(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+      int rc = ctx->opt.precision == SMPC_FP64 ? record_cycle<double>(ctx, cur)
+                                               : record_cycle<float>(ctx, cur);
+      cudaError_t e = cudaStreamEndCapture(ctx->st, &g);
+      if (rc) return rc;
+      if (e != cudaSuccess) return fail(ctx, SMPC_E_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&ctx->graph[cur], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return fail(ctx, SMPC_E_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+    }
+    CU(cudaGraphLaunch(ctx->graph[cur], ctx->st));
+    ctx->cur ^= 1;
+    ctx->collided = true;
+    // mirror the device's delrx advance (k_cycle_begin), same FP64 operations
+    for (int r = 0; r < ctx->n_rep; ++r) {
+      const RepInfo& ri = ctx->reps[r];
+      RepDyn& dn = ctx->dyn[r];
+      for (int s = 0; s < ctx->opt.step_update; ++s) {
+        dn.delrx += ri.shear * ri.L[1] * (ri.h * scale);
+        dn.delrx -= ri.L[0] * std::round(dn.delrx / ri.L[0]);
+      }
+      dn.h = ri.h;
+    }
+  }
+  return SMPC_OK;
+}
+
+int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, double* total_ms) {
+  if (!ctx || n <= 0 || !phase_ms || n_phases < PH_COUNT || !total_ms) return SMPC_E_ARG;
+  if (ctx->opt.rng != SMPC_RNG_PHILOX) return fail(ctx, SMPC_E_STATE, "fused cycles need Philox draws");
+  if (ctx->total_mono > 0 && !ctx->md_ready) return fail(ctx, SMPC_E_STATE, "smpc_init_md not called");
+  cudaSetDevice(ctx->device);
+  if (int rc = upload_host_dyn(ctx)) return rc;
+  const double scale = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / ctx->opt.step_update : 1.0;
+  std::vector<cudaEvent_t> ev(static_cast<size_t>(n) * (PH_COUNT + 1));
+  for (auto& e : ev) CU(cudaEventCreate(&e));
+  for (int i = 0; i < n; ++i) {
+    if (ctx->opt.precision == SMPC_FP64)
+      profiled_cycle<double>(ctx, ctx->cur, ev.data() + static_cast<size_t>(i) * (PH_COUNT + 1));
+    else
+      profiled_cycle<float>(ctx, ctx->cur, ev.data() + static_cast<size_t>(i) * (PH_COUNT + 1));
+    ctx->cur ^= 1;
+    ctx->collided = true;
+    for (int r = 0; r < ctx->n_rep; ++r) {
+      const RepInfo& ri = ctx->reps[r];
+      RepDyn& dn = ctx->dyn[r];
+      for (int s = 0; s < ctx->opt.step_update; ++s) {
+        dn.delrx += ri.shear * ri.L[1] * (ri.h * scale);
+        dn.delrx -= ri.L[0] * std::round(dn.delrx / ri.L[0]);
+      }
+      dn.h = ri.h;
+    }
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->st);
+  for (int p = 0; p < n_phases; ++p) phase_ms[p] = 0.0;
+  *total_ms = 0.0;
+  if (e == cudaSuccess) {
+    for (int i = 0; i < n; ++i) {
+      cudaEvent_t* c = ev.data() + static_cast<size_t>(i) * (PH_COUNT + 1);
+      for (int p = 0; p < PH_COUNT; ++p) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c[p], c[p + 1]);
+        phase_ms[p] += ms;
+      }
+    }
+    float tot = 0.f;
+    cudaEventElapsedTime(&tot, ev.front(), ev.back());
+    *total_ms = tot;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return fail(ctx, SMPC_E_CUDA, cudaGetErrorString(e));
+  return SMPC_OK;
+}
+
+int smpc_time_cycles(smpc_ctx* ctx, int n, double* total_ms) {
+  if (!ctx || n <= 0 || !total_ms) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  CU(cudaEventRecord(a, ctx->st));
+  int rc = smpc_cycles(ctx, n);
+  CU(cudaEventRecord(b, ctx->st));
+  cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0.f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(ctx, SMPC_E_CUDA, cudaGetErrorString(e));
+  *total_ms = ms;
+  return SMPC_OK;
+}
+
+int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int reference_velocities) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  cudaSetDevice(ctx->device);
+  const RepInfo& ri = ctx->reps[rep];
+  if (ctx->opt.precision == SMPC_FP64)
+    smpc::launch_init_solvent<double>(ctx->d_reps, rep, ri.slot_cap, static_cast<double*>(ctx->d_pos[ctx->cur]),
+                                      static_cast<double*>(ctx->d_vel[ctx->cur]), seed, ri.kT,
+                                      reference_velocities, ctx->st);
+  else
+    smpc::launch_init_solvent<float>(ctx->d_reps, rep, ri.slot_cap, static_cast<float*>(ctx->d_pos[ctx->cur]),
+                                     static_cast<float*>(ctx->d_vel[ctx->cur]), seed, ri.kT,
+                                     reference_velocities, ctx->st);
+  CU(cudaGetLastError());
+  return SMPC_OK;
+}
+
+int smpc_temperature(smpc_ctx* ctx, int rep, double* out) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (!out) return fail(ctx, SMPC_E_ARG, "null out");
+  return ctx->opt.precision == SMPC_FP64 ? temperature_t<double>(ctx, rep, out)
+                                         : temperature_t<float>(ctx, rep, out);
+}
+
+int smpc_temperature_all(smpc_ctx* ctx, double* out) {
+  if (!ctx || !out) return SMPC_E_ARG;
+  return ctx->opt.precision == SMPC_FP64 ? temperature_all_t<double>(ctx, out)
+                                         : temperature_all_t<float>(ctx, out);
+}
+
+int smpc_set_monomer_state_all(smpc_ctx* ctx, const double* pos, const double* vel) {
+  if (!ctx || !pos || !vel) return SMPC_E_ARG;
+  return ctx->opt.precision == SMPC_FP64 ? monomers_all_t<double>(ctx, pos, vel, nullptr, nullptr, nullptr)
+                                         : monomers_all_t<float>(ctx, pos, vel, nullptr, nullptr, nullptr);
+}
+
+int smpc_get_monomer_state_all(smpc_ctx* ctx, double* pos, double* vel, double* force) {
+  if (!ctx) return SMPC_E_ARG;
+  return ctx->opt.precision == SMPC_FP64 ? monomers_all_t<double>(ctx, nullptr, nullptr, pos, vel, force)
+                                         : monomers_all_t<float>(ctx, nullptr, nullptr, pos, vel, force);
+}
+
+int smpc_epot(smpc_ctx* ctx, int rep, double* out) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  RepDyn dn;
+  CU(cudaMemcpyAsync(&dn, ctx->d_dyn + rep, sizeof(RepDyn), cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  *out = dn.epot;
+  return SMPC_OK;
+}
+
+int smpc_verlet_rebuilds(smpc_ctx* ctx, int rep, int* out) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  RepDyn dn;
+  CU(cudaMemcpyAsync(&dn, ctx->d_dyn + rep, sizeof(RepDyn), cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  *out = dn.verlet_rebuilds;
+  return SMPC_OK;
+}
+
+int smpc_delrx(smpc_ctx* ctx, int rep, double* out) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  *out = ctx->dyn[rep].delrx;
+  return SMPC_OK;
+}
+
+int smpc_set_delrx(smpc_ctx* ctx, int rep, double delrx) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  ctx->dyn[rep].delrx = delrx;
+  return upload_host_dyn(ctx);
+}
+
+int smpc_set_collision_counter(smpc_ctx* ctx, uint64_t counter) {
+  if (!ctx) return SMPC_E_ARG;
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    CU(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->d_dyn + r) + offsetof(RepDyn, step), &counter,
+                       sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->st));
+  }
+  CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+int smpc_cell_counts(smpc_ctx* ctx, int rep, unsigned* total, unsigned* fluid) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (!ctx->collided) return fail(ctx, SMPC_E_STATE, "no collision has run yet");
+  const RepInfo& ri = ctx->reps[rep];
+  std::vector<uint32_t> off(ri.n_cell + 1);
+  CU(cudaMemcpyAsync(off.data(), ctx->d_off + ri.cell_base, (ri.n_cell + 1) * sizeof(uint32_t),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  std::vector<uint2> mk(ri.n_mono);
+  if (ri.n_mono)
+    CU(cudaMemcpyAsync(mk.data(), ctx->d_mkey + ri.mono_base, ri.n_mono * sizeof(uint2),
+                       cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  std::vector<unsigned> mono(ri.n_cell, 0);
+  for (auto& k : mk)
+    if (k.x != smpc::KEY_NONE) mono[k.x - ri.cell_base]++;
+  for (int c = 0; c < ri.n_cell; ++c) {
+    const unsigned tot = off[c + 1] - off[c];
+    if (total) total[c] = tot;
+    if (fluid) fluid[c] = tot - mono[c];
+  }
+  return SMPC_OK;
+}
+
+int smpc_error_word(smpc_ctx* ctx, unsigned* word, unsigned* info3) {
+  if (!ctx) return SMPC_E_ARG;
+  ErrorState e;
+  CU(cudaMemcpyAsync(&e, ctx->d_err, sizeof(ErrorState), cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaMemsetAsync(ctx->d_err, 0, sizeof(ErrorState), ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  if (word) *word = e.word;
+  if (info3)
+    for (int k = 0; k < 3; ++k) info3[k] = e.info[k];
+  return SMPC_OK;
+}
+
+int smpc_synchronize(smpc_ctx* ctx) {
+  if (!ctx) return SMPC_E_ARG;
+  CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+}  // extern "C"

@@ -64,48 +64,67 @@ def star_topology(arms: int, A: int, B: int):
 
 
 def saw_star(arms: int, n_arm: int, rng: np.random.Generator, bond: float = 1.0,
-             anchor_bond: float = 2.0, r_min: float = 1.0, max_tries: int = 5000,
-             centre=(0.0, 0.0, 0.0)) -> np.ndarray:
+             anchor_bond: float = 2.0, r_min: float = 1.0, outward_bias: float = 0.5,
+             max_tries: int = 400, centre=(0.0, 0.0, 0.0)) -> np.ndarray:
     """Self-avoiding random-walk star grown from ``centre``.
 
-    Each arm starts ``anchor_bond`` from the core in a random direction and
-    adds beads at distance ``bond``; a bead is accepted when it is farther
-    than ``r_min`` from every bead placed so far.
+    Arm roots sit ``anchor_bond`` from the core on a Fibonacci sphere (randomly
+    rotated); the arms then grow round-robin, one bead per arm per round, each
+    step of length ``bond`` in a random direction with an ``outward_bias``
+    toward the radial direction. A bead is accepted when it is farther than
+    ``r_min`` from every bead placed so far except its bonded predecessor.
+    Bead order in the result is the reference's star layout: core, then arm
+    by arm from the core outward.
     """
-    pos = [np.asarray(centre, dtype=np.float64)]
-    P = np.zeros((1 + arms * n_arm, 3))
-    P[0] = pos[0]
+    c = np.asarray(centre, dtype=np.float64)
+    n = 1 + arms * n_arm
+    placed = np.zeros((n, 3))
+    placed[0] = c
     count = 1
-
-    def free(q):
-        d = P[:count] - q
-        return bool(np.all(np.einsum("ij,ij->i", d, d) > r_min * r_min))
-
-    for _ in range(arms):
-        for _t in range(max_tries):
-            d = rng.normal(size=3)
-            d /= np.linalg.norm(d)
-            q = P[0] + d * anchor_bond
-            if free(q):
-                break
-        else:
-            raise RuntimeError("could not place arm root")
-        P[count] = q
+    arm_beads = [[] for _ in range(arms)]
+    # roots on a randomly rotated Fibonacci sphere
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    golden = math.pi * (3.0 - math.sqrt(5.0))
+    for a in range(arms):
+        z = 1.0 - 2.0 * (a + 0.5) / arms
+        r = math.sqrt(max(0.0, 1.0 - z * z))
+        d = q @ np.array([r * math.cos(golden * a), r * math.sin(golden * a), z])
+        p = c + d * anchor_bond
+        placed[count] = p
         count += 1
-        prev = q
-        for _k in range(1, n_arm):
+        arm_beads[a].append(p)
+
+    def free(x, skip):
+        dd = placed[:count] - x
+        ok = np.einsum("ij,ij->i", dd, dd) > r_min * r_min
+        ok[skip] = True  # the bonded predecessor sits at the bond length
+        return bool(np.all(ok))
+
+    last_index = list(range(1, arms + 1))
+    for _k in range(1, n_arm):
+        for a in range(arms):
+            prev = arm_beads[a][-1]
+            radial = prev - c
+            radial /= max(np.linalg.norm(radial), 1e-12)
             for _t in range(max_tries):
                 s = rng.normal(size=3)
                 s /= np.linalg.norm(s)
-                q = prev + s * bond
-                if free(q):
+                s = s + outward_bias * radial
+                s /= np.linalg.norm(s)
+                x = prev + s * bond
+                if free(x, last_index[a]):
                     break
             else:
                 raise RuntimeError("self-avoiding walk got stuck")
-            P[count] = q
+            placed[count] = x
+            last_index[a] = count
             count += 1
-            prev = q
-    return P
+            arm_beads[a].append(x)
+    out = np.zeros((n, 3))
+    out[0] = c
+    for a in range(arms):
+        out[1 + a * n_arm: 1 + (a + 1) * n_arm] = np.asarray(arm_beads[a])
+    return out
 
 
 def thermal_velocities(n: int, mass: float, kT: float, rng: np.random.Generator) -> np.ndarray:

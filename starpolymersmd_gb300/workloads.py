@@ -1,0 +1,101 @@
+"""Benchmark / long-run workloads built on the C ABI.
+
+Named by what they are:
+  single_star_50   one star f=10, N_arm=40 (50% solvophobic), 50^3 cells at
+                   rho=10 (1.25M solvent), monomer mass 5, shear 0.05
+  batched_256      256 independent boxes: f ~ U{3..12}, N_arm ~ U{10..60},
+                   solvophobic fraction ~ U[0.2,0.8], L ~ U{16..40}, shear
+                   log-uniform in [1e-3, 0.5], seeds 1..256 (system.batched_replica_table)
+  single_star_20   one star f=6, N_arm=20, 20^3 cells (80k solvent), the
+                   CPU-runnable case
+All use h = 0.1, MD dt = 0.01 (10 substeps per collision), kT = 1, solvent
+mass 1 and the 12-6 pair preset (WCA core, LJ attraction to 2.5 between
+solvophobic beads) with Verlet skin 0.3. Solvent initial states are drawn on
+the device (uniform positions, Maxwell-Boltzmann velocities); stars are
+self-avoiding walks from the box centre.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import List, Sequence
+
+import numpy as np
+
+from . import capi, system
+
+H = 0.1
+MD_DT = 0.01
+N_SUB = 10
+R_CUT_LJ = 2.5
+SKIN = 0.3
+MAX_NB = 256
+
+
+@dataclasses.dataclass
+class Built:
+    ctx: capi.Context
+    specs: List[system.ReplicaSpec]
+    stars: List[system.Star]
+    n_fluid: List[int]
+    n_mono: List[int]
+
+    @property
+    def particles(self) -> int:
+        return int(sum(self.n_fluid) + sum(self.n_mono))
+
+    @property
+    def n_rep(self) -> int:
+        return len(self.specs)
+
+    def close(self):
+        self.ctx.close()
+
+
+def replica_desc(spec: system.ReplicaSpec, star: system.Star) -> dict:
+    L = spec.L
+    return dict(L=(L, L, L), n_fluid=spec.n_c * L ** 3, n_mono=star.n, mol0_size=star.n,
+                kT=spec.kT, shear=spec.shear, h=H, md_dt=MD_DT, seed=spec.seed,
+                potential=capi.POT_LJ126, r_cut=R_CUT_LJ, r_verlet=R_CUT_LJ + SKIN,
+                **{"lambda": 1.0})
+
+
+def build(specs: Sequence[system.ReplicaSpec], precision=capi.FP32, rng_mode=capi.RNG_PHILOX,
+          mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL) -> Built:
+    stars = []
+    for spec in specs:
+        rng = np.random.default_rng(1000 + spec.seed)
+        stars.append(system.make_star(spec.arms, spec.n_arm, spec.solvophobic_fraction,
+                                      spec.mono_mass, spec.kT, rng, bond=0.97, anchor_bond=2.0,
+                                      r_min=1.0))
+    descs = [replica_desc(s, st) for s, st in zip(specs, stars)]
+    ctx = capi.Context(descs, precision=precision, rng=rng_mode, mono_bin=mono_bin,
+                       delrx_mode=delrx_mode, step_update=N_SUB, max_neighbors=MAX_NB,
+                       strict_cells=0)
+    for k, (spec, st) in enumerate(zip(specs, stars)):
+        ctx.init_solvent(k, seed=spec.seed)
+        ctx.set_monomers(k, st.pos, st.vel, np.zeros_like(st.pos), np.full(st.n, st.mass),
+                         st.amphi, st.anchor)
+        ctx.set_bonds(k, st.bond_src, st.bond_dst)
+    ctx.init_md()
+    ctx.synchronize()
+    return Built(ctx, list(specs), stars, [d["n_fluid"] for d in descs], [st.n for st in stars])
+
+
+def single_star_50(precision=capi.FP32, shear=0.05, **kw) -> Built:
+    spec = system.ReplicaSpec(L=50, arms=10, n_arm=40, solvophobic_fraction=0.5, shear=shear,
+                              seed=1)
+    return build([spec], precision=precision, **kw)
+
+
+def single_star_20(precision=capi.FP32, shear=0.05, **kw) -> Built:
+    spec = system.ReplicaSpec(L=20, arms=6, n_arm=20, solvophobic_fraction=0.5, shear=shear,
+                              seed=1)
+    return build([spec], precision=precision, **kw)
+
+
+def batched_256(precision=capi.FP32, n=256, **kw) -> Built:
+    return build(system.batched_replica_table(n), precision=precision, **kw)
+
+
+WORKLOADS = {"batched_256": batched_256, "single_star_50": single_star_50,
+             "single_star_20": single_star_20}

@@ -1,0 +1,192 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the oracle.
+
+FP64 path: bit-exact cell occupancies; positions, velocities, forces,
+temperature and potential energy within 1e-12 of the reference (relative to
+each array's scale), the Lees-Edwards offset bit-exact. FP32 path: stated
+tolerances against the FP64 oracle on identical injected draws.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from starpolymersmd_gb300 import capi
+from tests import golden_replay as gr
+from tests import gpu_helpers as H
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[:-4] for p in FIXTURES])
+def test_fp64_replays_reference_fixture(path):
+    fx = gr.load(path)
+    star = gr.has_star(fx)
+    coll = gr.collision_index(fx)
+    with H.fixture_context(fx) as ctx:
+        if star:
+            _, _, f0 = ctx.get_monomers(0)
+            H.close64(f0, fx["mono_force0"])
+        for t in range(int(fx["n_loop"])):
+            if star and int(fx["with_md"]):
+                ctx.md_substeps(1, calc_epot=True)
+                H.close64(ctx.epot(0), fx["epot"][t])
+            if not int(fx["md_only"]):
+                k = coll.get(t)
+                if k is not None:
+                    ctx.mpc_step(t, float(fx["h"]), fx["shift"][k], np.nan_to_num(fx["gamma"][k]),
+                                 fx["u_phi"][k], fx["u_theta"][k])
+                    ctx.raise_on_device_error()
+                    tot, fl = ctx.cell_counts(0)
+                    np.testing.assert_array_equal(tot, fx["count_total"][k])
+                    np.testing.assert_array_equal(fl, fx["count_fluid"][k])
+                    p, v = ctx.get_fluid(0)
+                    H.close64(p, fx["fluid_pos"][k])
+                    H.close64(v, fx["fluid_vel"][k])
+                    H.close64(ctx.temperature(0), fx["temperature"][k])
+                else:
+                    ctx.mpc_step(t, float(fx["h"]))
+            assert ctx.delrx(0) == fx["delrx"][t]
+            if star:
+                p, v, f = ctx.get_monomers(0)
+                H.close64(p, fx["mono_pos"][t])
+                H.close64(v, fx["mono_vel"][t])
+                H.close64(f, fx["mono_force"][t], rtol=1e-11)
+        ctx.raise_on_device_error()
+
+
+@pytest.mark.parametrize("shear", [0.0, 0.05])
+def test_fp64_philox_matches_oracle(shear):
+    # production draws (Philox + Marsaglia-Tsang) on both sides, 3 cycles of
+    # 10 MD substeps + 1 collision through the step-by-step API
+    L, su, h = 10, 10, 0.1
+    star, fpos, fvel = H.small_star_system(L=L, shear=shear)
+    o = H.oracle_for(star, fpos, fvel, L, 1.0, shear, su)
+    o.set_philox(seed=77, counter=5)
+    with H.context_for(star, fpos, fvel, L, 1.0, shear, su, rng=capi.RNG_PHILOX, seed=77) as ctx:
+        ctx.set_collision_counter(5)
+        for t in range(0, 3 * su + 1):
+            o.propagate(False)
+            o.mpc_step(t, h)
+            ctx.md_substeps(1)
+            ctx.mpc_step(t, h)
+        ctx.raise_on_device_error()
+        tot, fl = ctx.cell_counts(0)
+        otot, ofl = o.cell_counts()
+        np.testing.assert_array_equal(tot, otot)
+        np.testing.assert_array_equal(fl, ofl)
+        p, v = ctx.get_fluid(0)
+        op, ov = o.get_fluid()
+        H.close64(p, op)
+        H.close64(v, ov)
+        mp, mv, mf = ctx.get_monomers(0)
+        omp, omv, omf = o.get_monomers()
+        H.close64(mp, omp)
+        H.close64(mv, omv)
+        H.close64(ctx.temperature(0), o.temperature())
+        assert ctx.delrx(0) == o.delrx
+
+
+def test_fp64_graph_cycles_match_stepwise():
+    # smpc_cycles (captured graph, device-side delrx and shift) against the
+    # same cycles issued call by call
+    L, su, h = 8, 10, 0.1
+    star, fpos, fvel = H.small_star_system(L=L, shear=0.1, seed=5)
+    kw = dict(rng=capi.RNG_PHILOX, seed=9)
+    with H.context_for(star, fpos, fvel, L, 1.0, 0.1, su, **kw) as a, \
+            H.context_for(star, fpos, fvel, L, 1.0, 0.1, su, **kw) as b:
+        # call-by-call: cycles start right after a collision, so the first
+        # cycle is t = 1..10 with the collision at t = 10
+        for t in range(1, 3 * su + 1):
+            a.md_substeps(1)
+            a.mpc_step(t, h)
+        b.cycles(3)
+        b.synchronize()
+        a.raise_on_device_error()
+        b.raise_on_device_error()
+        pa, va = a.get_fluid(0)
+        pb, vb = b.get_fluid(0)
+        H.close64(pb, pa)
+        H.close64(vb, va)
+        ma = a.get_monomers(0)
+        mb = b.get_monomers(0)
+        for x, y in zip(mb, ma):
+            H.close64(x, y)
+        assert a.delrx(0) == b.delrx(0)
+
+
+def test_fp32_matches_fp64_oracle_on_injected_draws(golden_dir):
+    fx = gr.load(os.path.join(golden_dir, "star_mpc_L12.npz"))
+    coll = gr.collision_index(fx)
+    L = fx["L"]
+    with H.fixture_context(fx, precision=capi.FP32) as ctx:
+        for t in range(int(fx["n_loop"])):
+            ctx.md_substeps(1)
+            k = coll.get(t)
+            if k is not None:
+                ctx.mpc_step(t, float(fx["h"]), fx["shift"][k], np.nan_to_num(fx["gamma"][k]),
+                             fx["u_phi"][k], fx["u_theta"][k])
+                ctx.raise_on_device_error()
+                p, v = ctx.get_fluid(0)
+                dp = np.abs(H.wrapped_diff(p, fx["fluid_pos"][k], L)).max(axis=1)
+                dv = np.abs(v - fx["fluid_vel"][k]).max(axis=1)
+                vs = np.abs(fx["fluid_vel"][k]).max()
+                # A particle within FP32 rounding of a cell face may land in the
+                # neighbouring cell, which changes the collision of the two cells
+                # involved; all other particles must agree to FP32 accuracy.
+                bad = (dp > H.FP32_POS_ATOL * L.max()) | (dv > H.FP32_VEL_RTOL * vs)
+                assert bad.mean() < 0.005, (bad.sum(), dp.max(), dv.max())
+                tot, _ = ctx.cell_counts(0)
+                assert np.count_nonzero(tot != fx["count_total"][k]) <= 4
+                assert tot.sum() == fx["count_total"][k].sum()
+            else:
+                ctx.mpc_step(t, float(fx["h"]))
+        mp, mv, _ = ctx.get_monomers(0)
+        assert np.abs(mp - fx["mono_pos"][-1]).max() < 1e-3
+        assert np.abs(mv - fx["mono_vel"][-1]).max() < 1e-2
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.FP32])
+def test_collision_conserves_total_momentum(precision):
+    # no shear, no recentring: streaming and shifting leave velocities alone
+    # and every cell's collision conserves its momentum
+    L = 12
+    star, fpos, fvel = H.small_star_system(L=L, shear=0.0, seed=11, n_arm=4)
+    with H.context_for(star, fpos, fvel, L, 1.0, 0.0, 1, rng=capi.RNG_PHILOX,
+                       precision=precision) as ctx:
+        m = star.mass
+
+        def momentum():
+            _, v = ctx.get_fluid(0)
+            _, mv, _ = ctx.get_monomers(0)
+            return v.sum(axis=0) + m * mv.sum(axis=0), np.abs(v).sum() + m * np.abs(mv).sum()
+
+        p0, scale = momentum()
+        for t in range(5):
+            ctx.mpc_step(t, 0.1)
+        ctx.raise_on_device_error()
+        p1, _ = momentum()
+        tol = 1e-12 if precision == capi.FP64 else 2e-6
+        assert np.abs(p1 - p0).max() < tol * scale
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.FP32])
+def test_thermostat_holds_temperature(precision):
+    # MBS thermostat at kT = 1 from a cold start (uniform velocities, kT_init = 1/12)
+    L = 10
+    rng = np.random.default_rng(4)
+    from starpolymersmd_gb300 import system
+    fpos, fvel = system.uniform_fluid((L, L, L), 10, 1.0, rng, reference_velocities=True)
+    rep = dict(L=(L, L, L), n_fluid=len(fpos), kT=1.0, shear=0.0, h=0.1, seed=21)
+    with capi.Context([rep], precision=precision, rng=capi.RNG_PHILOX, step_update=1) as ctx:
+        ctx.set_fluid(0, fpos, fvel)
+        temps = []
+        for t in range(60):
+            ctx.mpc_step(t, 0.1)
+            if t >= 20:
+                temps.append(ctx.temperature(0))
+        ctx.raise_on_device_error()
+        assert abs(np.mean(temps) - 1.0) < 0.01
