@@ -136,12 +136,12 @@ def thermal_velocities(n: int, mass: float, kT: float, rng: np.random.Generator)
 
 def make_star(arms: int, n_arm: int, solvophobic_fraction: float, mass: float, kT: float,
               rng: np.random.Generator, bond: float = 1.0, anchor_bond: float = 2.0,
-              r_min: float = 1.0, centre=(0.0, 0.0, 0.0)) -> Star:
+              r_min: float = 1.0, centre=(0.0, 0.0, 0.0), outward_bias: float = 0.5) -> Star:
     B = int(round(solvophobic_fraction * n_arm))
     A = n_arm - B
     amphi, anch, src, dst = star_topology(arms, A, B)
     pos = saw_star(arms, n_arm, rng, bond=bond, anchor_bond=anchor_bond, r_min=r_min,
-                   centre=centre)
+                   centre=centre, outward_bias=outward_bias)
     vel = thermal_velocities(len(pos), mass, kT, rng)
     return Star(arms, A, B, mass, pos, vel, amphi, anch, src, dst)
 

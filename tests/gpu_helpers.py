@@ -45,9 +45,18 @@ def fixture_context(fx, precision=capi.FP64):
 
 def small_star_system(L=10, n_c=10, arms=3, n_arm=6, frac=0.5, shear=0.05, seed=3,
                       mass=5.0, kT=1.0, potential=capi.POT_REF4824):
-    """Seeded SAW star in a uniform solvent (reference velocity init)."""
+    """Seeded compact SAW star in a uniform solvent (reference velocity init).
+
+    The star must fit the reference's box-bounded Verlet grid and its
+    unwrapped monomer binning, so walks are unbiased and regrown until the
+    star stays 1.5 cells inside the box."""
     rng = np.random.default_rng(seed)
-    star = system.make_star(arms, n_arm, frac, mass, kT, rng, bond=1.01)
+    for _ in range(200):
+        star = system.make_star(arms, n_arm, frac, mass, kT, rng, bond=1.01, outward_bias=0.0)
+        if np.abs(star.pos).max() < L / 2 - 1.5:
+            break
+    else:
+        raise RuntimeError("no compact star found")
     fpos, fvel = system.uniform_fluid((L, L, L), n_c, kT, rng, reference_velocities=True)
     return star, fpos, fvel
 

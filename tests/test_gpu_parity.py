@@ -74,6 +74,7 @@ def test_fp64_philox_matches_oracle(shear):
             ctx.md_substeps(1)
             ctx.mpc_step(t, h)
         ctx.raise_on_device_error()
+        assert o.error() == 0
         tot, fl = ctx.cell_counts(0)
         otot, ofl = o.cell_counts()
         np.testing.assert_array_equal(tot, otot)
@@ -190,3 +191,91 @@ def test_thermostat_holds_temperature(precision):
                 temps.append(ctx.temperature(0))
         ctx.raise_on_device_error()
         assert abs(np.mean(temps) - 1.0) < 0.01
+
+
+def _batch_specs():
+    from starpolymersmd_gb300 import system
+    return [system.ReplicaSpec(L=9, arms=3, n_arm=5, solvophobic_fraction=0.4, shear=0.2, seed=31),
+            system.ReplicaSpec(L=12, arms=4, n_arm=6, solvophobic_fraction=0.6, shear=0.01, seed=32),
+            system.ReplicaSpec(L=7, arms=3, n_arm=3, solvophobic_fraction=0.5, shear=0.0, seed=33)]
+
+
+def _batch_run(precision, cycles=2):
+    """Uneven replicas in one context (production options) and one oracle per
+    replica with the same options; returns both final states."""
+    from starpolymersmd_gb300 import system, workloads as W
+    specs = _batch_specs()
+    stars, fluids, descs = [], [], []
+    for s in specs:
+        rng = np.random.default_rng(500 + s.seed)
+        st = system.make_star(s.arms, s.n_arm, s.solvophobic_fraction, s.mono_mass, s.kT, rng,
+                              bond=0.97)
+        fp, fv = system.uniform_fluid((s.L,) * 3, s.n_c, s.kT, rng)
+        stars.append(st)
+        fluids.append((fp, fv))
+        descs.append(W.replica_desc(s, st))
+    ctx = capi.Context(descs, precision=precision, rng=capi.RNG_PHILOX,
+                       mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL,
+                       step_update=W.N_SUB, max_neighbors=W.MAX_NB, strict_cells=0)
+    oracles = []
+    for k, (s, st, (fp, fv)) in enumerate(zip(specs, stars, fluids)):
+        ctx.set_fluid(k, fp, fv)
+        ctx.set_monomers(k, st.pos, st.vel, np.zeros_like(st.pos), np.full(st.n, st.mass),
+                         st.amphi, st.anchor)
+        ctx.set_bonds(k, st.bond_src, st.bond_dst)
+        o = orc.OracleSystem((s.L,) * 3, s.kT, s.shear, W.N_SUB, len(fp), st.n, mol_start=[0, st.n],
+                             lambda_=1.0, md_dt=W.MD_DT, r_cut=W.R_CUT_LJ,
+                             r_verlet=W.R_CUT_LJ + W.SKIN, potential=orc.POT_LJ126,
+                             delrx_dt_scale=1.0 / W.N_SUB, mono_wrap=1)
+        o.set_fluid(fp, fv)
+        o.set_monomers(st.pos, st.vel, np.zeros_like(st.pos), np.full(st.n, st.mass), st.amphi,
+                       st.anchor)
+        o.set_bonds(st.bond_src, st.bond_dst)
+        o.init_md()
+        o.set_philox(s.seed, 0)
+        oracles.append(o)
+    ctx.init_md()
+    ctx.cycles(cycles)
+    ctx.synchronize()
+    ctx.raise_on_device_error()
+    for o in oracles:
+        o.run(1, W.N_SUB * cycles, W.H, True)
+        assert o.error() == 0
+    return ctx, oracles, specs
+
+
+def test_batched_fp64_matches_independent_oracles():
+    ctx, oracles, specs = _batch_run(capi.FP64)
+    with ctx:
+        for k, (o, s) in enumerate(zip(oracles, specs)):
+            tot, _ = ctx.cell_counts(k)
+            otot, _ = o.cell_counts()
+            np.testing.assert_array_equal(tot, otot)
+            p, v = ctx.get_fluid(k)
+            op, ov = o.get_fluid()
+            H.close64(p, op)
+            H.close64(v, ov)
+            mp, mv, _ = ctx.get_monomers(k)
+            omp, omv, _ = o.get_monomers()
+            H.close64(mp, omp, rtol=1e-11)
+            H.close64(mv, omv, rtol=1e-11)
+            H.close64(ctx.temperature(k), o.temperature())
+            assert ctx.delrx(k) == o.delrx
+
+
+def test_batched_fp32_tracks_fp64_oracle():
+    # FP32 state, fixed-point cell sums and FP32 Philox uniforms/gamma against
+    # the FP64 oracle on the same counter-based stream: all but a few per cent
+    # of the solvent (cells whose gamma acceptance or face assignment flips
+    # under FP32 rounding) must agree to FP32 accuracy after two cycles.
+    ctx, oracles, specs = _batch_run(capi.FP32)
+    with ctx:
+        for k, (o, s) in enumerate(zip(oracles, specs)):
+            p, v = ctx.get_fluid(k)
+            op, ov = o.get_fluid()
+            dp = np.abs(H.wrapped_diff(p, op, (s.L,) * 3)).max(axis=1)
+            dv = np.abs(v - ov).max(axis=1)
+            vs = np.abs(ov).max()
+            bad = (dp > 1e-4 * s.L) | (dv > 1e-3 * vs)
+            assert bad.mean() < 0.03, (k, bad.mean())
+            assert abs(ctx.temperature(k) - o.temperature()) < 0.01
