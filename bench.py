@@ -155,9 +155,8 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
         pick = pick[:max_replicas]
 
     def make(spec):
-        rng = np.random.default_rng(1000 + spec.seed)
-        st = system.make_star(spec.arms, spec.n_arm, spec.solvophobic_fraction, spec.mono_mass,
-                              spec.kT, rng, bond=0.97)
+        rng = np.random.default_rng(2000 + spec.seed)
+        st = W.compact_star(spec)
         L = spec.L
         fpos, fvel = system.uniform_fluid((L, L, L), spec.n_c, spec.kT, rng)
         o = orc.OracleSystem((L, L, L), spec.kT, spec.shear, W.N_SUB, len(fpos), st.n,

@@ -533,6 +533,11 @@ static void forces_verlet(smpc_orc* o, int calc_epot) {
         double d0 = xj[0] - xi[0], d1 = xj[1] - xi[1], d2 = xj[2] - xi[2];
         double r2 = (d0 * d0 + d1 * d1) + d2 * d2;
         double fa;
+        if (pot != ORC_POT_REF4824) {
+          /* 12-6 preset: FENE argument capped at 0.98 R0^2 (finite, restoring) */
+          const double cap = (o->anchor[i] ? 20.25 : 2.25) * 0.98;
+          if (r2 > cap) r2 = cap;
+        }
         if (o->anchor[i]) {
           if (calc_epot) ep += fene_anchor_pot(r2);
           fa = fene_anchor_force(r2);

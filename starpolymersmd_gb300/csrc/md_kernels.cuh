@@ -221,13 +221,21 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
           const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
           const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
           const bool anch = bd.y != 0;
-          if (r2 >= (anch ? R(20.25) : R(2.25)))
-            raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + i), static_cast<uint32_t>(b + j));
-          const R fa = fene_force<R>(anch, r2);
+          R r2f = r2;
+          if (pot == POT_REF4824) {
+            // reference FENE: beyond R0 the force changes sign (Potentials.h:24-55)
+            if (r2 >= (anch ? R(20.25) : R(2.25)))
+              raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + i), static_cast<uint32_t>(b + j));
+          } else {
+            // 12-6 preset: FENE argument capped at 0.98 R0^2 (finite, restoring)
+            const R cap = (anch ? R(20.25) : R(2.25)) * R(0.98);
+            if (r2f > cap) r2f = cap;
+          }
+          const R fa = fene_force<R>(anch, r2f);
           F0 -= d0 * fa;
           F1 -= d1 * fa;
           F2 -= d2 * fa;
-          if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2));
+          if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2f));
         }
         f[k][0] = F0; f[k][1] = F1; f[k][2] = F2;
         if (a.n_steps > 0)

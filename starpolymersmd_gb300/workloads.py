@@ -51,6 +51,26 @@ class Built:
         self.ctx.close()
 
 
+def compact_star(spec: system.ReplicaSpec, tries: int = 20) -> system.Star:
+    """Self-avoiding-walk star with a mild outward bias; among a few seeded
+    attempts the one with the smallest extent (most fit inside the box)."""
+    rng = np.random.default_rng(1000 + spec.seed)
+    best = None
+    for _ in range(tries):
+        try:
+            st = system.make_star(spec.arms, spec.n_arm, spec.solvophobic_fraction,
+                                  spec.mono_mass, spec.kT, rng, bond=0.97, anchor_bond=2.0,
+                                  r_min=1.0, outward_bias=0.15)
+        except RuntimeError:  # a trapped walk: draw again
+            continue
+        ext = float(np.abs(st.pos).max())
+        if best is None or ext < best[0]:
+            best = (ext, st)
+        if ext < spec.L / 2 - 1.0:
+            break
+    return best[1]
+
+
 def replica_desc(spec: system.ReplicaSpec, star: system.Star) -> dict:
     L = spec.L
     return dict(L=(L, L, L), n_fluid=spec.n_c * L ** 3, n_mono=star.n, mol0_size=star.n,
@@ -61,12 +81,7 @@ def replica_desc(spec: system.ReplicaSpec, star: system.Star) -> dict:
 
 def build(specs: Sequence[system.ReplicaSpec], precision=capi.FP32, rng_mode=capi.RNG_PHILOX,
           mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL) -> Built:
-    stars = []
-    for spec in specs:
-        rng = np.random.default_rng(1000 + spec.seed)
-        stars.append(system.make_star(spec.arms, spec.n_arm, spec.solvophobic_fraction,
-                                      spec.mono_mass, spec.kT, rng, bond=0.97, anchor_bond=2.0,
-                                      r_min=1.0))
+    stars = [compact_star(spec) for spec in specs]
     descs = [replica_desc(s, st) for s, st in zip(specs, stars)]
     ctx = capi.Context(descs, precision=precision, rng=rng_mode, mono_bin=mono_bin,
                        delrx_mode=delrx_mode, step_update=N_SUB, max_neighbors=MAX_NB,
