@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched_256")
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 ratio, e2e, CPU baseline")
+    ap.add_argument("--replicas", type=int, default=0,
+                    help="batched_256 only: use the first N replicas (small profiling case)")
     return ap.parse_args()
 
 
@@ -199,7 +201,10 @@ def run_ours(args, world, rank, local, dist):
     from starpolymersmd_gb300 import capi, workloads as W
 
     t_build = time.perf_counter()
-    built = W.WORKLOADS[args.workload](precision=capi.FP32)
+    if args.replicas and args.workload == "batched_256":
+        built = W.batched_256(precision=capi.FP32, n=args.replicas)
+    else:
+        built = W.WORKLOADS[args.workload](precision=capi.FP32)
     ctx = built.ctx
     build_s = time.perf_counter() - t_build
     units = built.particles
