@@ -109,7 +109,8 @@ def single_star_20(precision=capi.FP32, shear=0.05, **kw) -> Built:
 
 
 def batched_256(precision=capi.FP32, n=256, **kw) -> Built:
-    return build(system.batched_replica_table(n), precision=precision, **kw)
+    """The 256-replica table, or its first n replicas."""
+    return build(system.batched_replica_table(256)[:n], precision=precision, **kw)
 
 
 WORKLOADS = {"batched_256": batched_256, "single_star_50": single_star_50,
