@@ -1,8 +1,8 @@
 // FP32 fast-path instantiation: float4 state, int64 fixed-point cell sums.
 #define SMPC_REAL float
 #define SMPC_COLLIDE_NT 256
-#define SMPC_COLLIDE_CT 256
-#define SMPC_COLLIDE_PPT 12
+#define SMPC_COLLIDE_CT 128
+#define SMPC_COLLIDE_CAP 1536
 #define SMPC_BIN_NT 256
 #define SMPC_MD_NT 256
 #define SMPC_MD_MPT 4

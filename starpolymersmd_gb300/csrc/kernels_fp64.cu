@@ -2,8 +2,8 @@
 // multiply and add rounds separately, in the reference's order.
 #define SMPC_REAL double
 #define SMPC_COLLIDE_NT 128
-#define SMPC_COLLIDE_CT 128
-#define SMPC_COLLIDE_PPT 12
+#define SMPC_COLLIDE_CT 64
+#define SMPC_COLLIDE_CAP 768
 #define SMPC_BIN_NT 256
 #define SMPC_MD_NT 256
 #define SMPC_MD_MPT 4

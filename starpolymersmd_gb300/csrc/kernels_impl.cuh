@@ -27,11 +27,10 @@ void launch_cycle_end<Real>(RepDyn* dyn, int n_rep, cudaStream_t st) {
 }
 
 template <>
-void launch_init_solvent<Real>(const RepInfo* reps, int rep, int slot_cap, Real* pos, Real* vel,
+void launch_init_solvent<Real>(const RepInfo* reps, int rep, int slot_cap, Real* rec,
                                unsigned long long seed, double kT, int ref_vel, cudaStream_t st) {
   if (slot_cap == 0) return;
-  k_init_solvent<Real><<<(slot_cap + 255) / 256, 256, 0, st>>>(reps, rep, pos, vel, seed, kT,
-                                                              ref_vel);
+  k_init_solvent<Real><<<(slot_cap + 255) / 256, 256, 0, st>>>(reps, rep, rec, seed, kT, ref_vel);
 }
 
 template <>
@@ -44,30 +43,35 @@ void launch_mono_prep<Real>(const RepInfo* reps, RepDyn* dyn, int n_rep, Real* m
 
 template <>
 void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
-                            const RepDyn* dyn, const Real* pos, const Real* vel, uint2* keys,
-                            uint32_t* count, ErrorState* err, int strict, cudaStream_t st) {
+                            const RepDyn* dyn, const Real* rec, uint2* keys, uint32_t* count,
+                            ErrorState* err, int strict, cudaStream_t st) {
   if (n_tiles == 0) return;
-  k_fluid_bin<Real, SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, dyn, pos, vel,
-                                                                  keys, count, err, strict);
+  k_fluid_bin<Real, SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, dyn, rec, keys,
+                                                                  count, err, strict);
 }
 
 template <>
 void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
   if (a.n_tiles == 0) return;
-  k_collide<Real, SMPC_COLLIDE_NT, SMPC_COLLIDE_CT, SMPC_COLLIDE_PPT>
-      <<<a.n_tiles, SMPC_COLLIDE_NT, 0, st>>>(
-          a.tiles, a.reps, a.dyn, a.off, a.perm, a.pos_in, a.vel_in, a.pos_out, a.vel_out, a.mpos,
-          a.mvel, a.mkey, a.mimg, a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.rot_c, a.rot_s,
-          a.strict, a.mono_bin, a.err);
+  auto kern = k_collide<Real, SMPC_COLLIDE_NT, SMPC_COLLIDE_CT, SMPC_COLLIDE_CAP>;
+  const size_t dyn = collide_dyn_smem<Real>(SMPC_COLLIDE_CAP);
+  static bool configured = false;  // the attribute is per function, set once
+  if (!configured) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn));
+    configured = true;
+  }
+  kern<<<a.n_tiles, SMPC_COLLIDE_NT, dyn, st>>>(
+      a.tiles, a.reps, a.dyn, a.off, a.perm, a.st_in, a.st_out, a.mpos, a.mvel, a.mkey, a.mimg,
+      a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.rot_c, a.rot_s, a.strict, a.mono_bin, a.err);
 }
 
 template <>
 void launch_temperature<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
-                              const uint32_t* off, const uint32_t* perm, const Real* vel_cur,
+                              const uint32_t* off, const uint32_t* perm, const Real* rec_cur,
                               const Real* mpos, const Real* mvel, const int* mimg, int mono_bin,
                               TempPartial* partial, cudaStream_t st) {
   if (n_tiles == 0) return;
-  k_temperature<Real, 128><<<n_tiles, 128, 0, st>>>(tiles, reps, off, perm, vel_cur, mpos, mvel,
+  k_temperature<Real, 128><<<n_tiles, 128, 0, st>>>(tiles, reps, off, perm, rec_cur, mpos, mvel,
                                                     mimg, mono_bin, partial);
 }
 

@@ -19,10 +19,8 @@ struct CollideArgs {
   const RepDyn* dyn;
   const uint32_t* off;
   const uint32_t* perm;
-  const R* pos_in;
-  const R* vel_in;
-  R* pos_out;
-  R* vel_out;
+  const R* st_in;   // solvent slot records (position, velocity)
+  R* st_out;
   const R* mpos;
   R* mvel;
   const uint2* mkey;
@@ -51,7 +49,7 @@ void launch_cycle_begin(const RepInfo* reps, RepDyn* dyn, int n_rep, int n_adv, 
 template <typename R>
 void launch_cycle_end(RepDyn* dyn, int n_rep, cudaStream_t st);
 template <typename R>
-void launch_init_solvent(const RepInfo* reps, int rep, int slot_cap, R* pos, R* vel,
+void launch_init_solvent(const RepInfo* reps, int rep, int slot_cap, R* rec,
                          unsigned long long seed, double kT, int ref_vel, cudaStream_t st);
 template <typename R>
 void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* mvel, uint2* mkey,
@@ -59,13 +57,13 @@ void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* m
                       cudaStream_t st);
 template <typename R>
 void launch_fluid_bin(const Tile* tiles, int n_tiles, const RepInfo* reps, const RepDyn* dyn,
-                      const R* pos, const R* vel, uint2* keys, uint32_t* count, ErrorState* err,
-                      int strict, cudaStream_t st);
+                      const R* rec, uint2* keys, uint32_t* count, ErrorState* err, int strict,
+                      cudaStream_t st);
 template <typename R>
 void launch_collide(const CollideArgs<R>& a, cudaStream_t st);
 template <typename R>
 void launch_temperature(const Tile* tiles, int n_tiles, const RepInfo* reps, const uint32_t* off,
-                        const uint32_t* perm, const R* vel_cur, const R* mpos, const R* mvel,
+                        const uint32_t* perm, const R* rec_cur, const R* mpos, const R* mvel,
                         const int* mimg, int mono_bin, TempPartial* partial, cudaStream_t st);
 template <typename R>
 void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, cudaStream_t st);

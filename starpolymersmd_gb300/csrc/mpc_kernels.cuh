@@ -61,6 +61,18 @@ __device__ __forceinline__ void st4(double* p, size_t i, const R4<double>& v) {
   q[1] = make_double2(v.z, v.w);
 }
 
+// Solvent slot records: position then velocity of slot i are adjacent
+// (8 Reals, 32 B in FP32), so a gathered particle is one 32-byte sector.
+template <typename R>
+__device__ __forceinline__ R4<R> ld_pos(const R* st, size_t i) { return ld4(st, 2 * i); }
+template <typename R>
+__device__ __forceinline__ R4<R> ld_vel(const R* st, size_t i) { return ld4(st, 2 * i + 1); }
+template <typename R>
+__device__ __forceinline__ void st_rec(R* st, size_t i, const R4<R>& x, const R4<R>& v) {
+  st4(st, 2 * i, x);
+  st4(st, 2 * i + 1, v);
+}
+
 __device__ __forceinline__ uint32_t slot_id(float w) { return __float_as_uint(w); }
 __device__ __forceinline__ uint32_t slot_id(double w) {
   return w < 0.0 ? SLOT_EMPTY : static_cast<uint32_t>(w);
@@ -92,6 +104,8 @@ __device__ __forceinline__ double r_div(double a, double b) { return __ddiv_rn(a
 // Per-replica constants in the working precision. The FP64 path follows the
 // reference's operation order exactly (-fmad=false): round-half-away,
 // division by L, (cy*shear)*Ly. The FP32 path uses the same operations.
+// Everything is converted to R once per thread block, so the FP32 hot loops
+// never touch the (slow on GB300) FP64 pipe.
 template <typename R>
 struct Geo {
   R L[3];
@@ -101,6 +115,12 @@ struct Geo {
   R delrx;
   bool shear_on;
   int wrap_mono;
+  // this collision's frame: grid shift, streaming time, recentring
+  R shift[3];
+  R com[3];
+  R comv[3];
+  R h;
+  bool recentre;
 };
 
 template <typename R>
@@ -110,11 +130,16 @@ __device__ __forceinline__ Geo<R> make_geo(const RepInfo& ri, const RepDyn& dn, 
     g.L[d] = static_cast<R>(ri.L[d]);
     g.half[d] = static_cast<R>(ri.L[d]) * R(0.5);
     g.Li[d] = ri.L[d];
+    g.shift[d] = static_cast<R>(dn.shift[d]);
+    g.com[d] = static_cast<R>(dn.com[d]);
+    g.comv[d] = static_cast<R>(dn.comv[d]);
   }
   g.shear = static_cast<R>(ri.shear);
   g.delrx = static_cast<R>(dn.delrx);
   g.shear_on = (ri.shear != 0.0);
   g.wrap_mono = mono_bin;
+  g.h = static_cast<R>(dn.h);
+  g.recentre = dn.recentre != 0;
   return g;
 }
 
@@ -167,24 +192,23 @@ __device__ __forceinline__ void raise_error(ErrorState* e, uint32_t bit, uint32_
 // Solvent particle from its stored state to the shifted collision frame:
 // [recentre: x -= COM, v -= COMV, wrap] -> stream x += v h, wrap -> x += s, wrap.
 template <typename R>
-__device__ __forceinline__ void fluid_to_collision_frame(const Geo<R>& g, const RepDyn& dn,
-                                                         R h, R4<R>& x, R4<R>& v) {
-  if (dn.recentre) {
-    x.x = r_sub(x.x, static_cast<R>(dn.com[0]));
-    x.y = r_sub(x.y, static_cast<R>(dn.com[1]));
-    x.z = r_sub(x.z, static_cast<R>(dn.com[2]));
-    v.x = r_sub(v.x, static_cast<R>(dn.comv[0]));
-    v.y = r_sub(v.y, static_cast<R>(dn.comv[1]));
-    v.z = r_sub(v.z, static_cast<R>(dn.comv[2]));
+__device__ __forceinline__ void fluid_to_collision_frame(const Geo<R>& g, R4<R>& x, R4<R>& v) {
+  if (g.recentre) {
+    x.x = r_sub(x.x, g.com[0]);
+    x.y = r_sub(x.y, g.com[1]);
+    x.z = r_sub(x.z, g.com[2]);
+    v.x = r_sub(v.x, g.comv[0]);
+    v.y = r_sub(v.y, g.comv[1]);
+    v.z = r_sub(v.z, g.comv[2]);
     le_wrap(g, x.x, x.y, x.z, v.x);
   }
-  x.x = r_add(x.x, r_mul(v.x, h));
-  x.y = r_add(x.y, r_mul(v.y, h));
-  x.z = r_add(x.z, r_mul(v.z, h));
+  x.x = r_add(x.x, r_mul(v.x, g.h));
+  x.y = r_add(x.y, r_mul(v.y, g.h));
+  x.z = r_add(x.z, r_mul(v.z, g.h));
   le_wrap(g, x.x, x.y, x.z, v.x);
-  x.x = r_add(x.x, static_cast<R>(dn.shift[0]));
-  x.y = r_add(x.y, static_cast<R>(dn.shift[1]));
-  x.z = r_add(x.z, static_cast<R>(dn.shift[2]));
+  x.x = r_add(x.x, g.shift[0]);
+  x.y = r_add(x.y, g.shift[1]);
+  x.z = r_add(x.z, g.shift[2]);
   le_wrap(g, x.x, x.y, x.z, v.x);
 }
 
@@ -243,15 +267,15 @@ __global__ void k_cycle_end(RepDyn* dyn, int n_rep) {
 // removed here). Counter-based: particle i of replica seed s always gets the
 // same values. Slots past n_fluid become holes.
 template <typename R>
-__global__ void k_init_solvent(const RepInfo* reps, int rep, R* pos, R* vel,
-                               unsigned long long seed, double kT, int ref_vel) {
+__global__ void k_init_solvent(const RepInfo* reps, int rep, R* st, unsigned long long seed,
+                               double kT, int ref_vel) {
   const RepInfo ri = reps[rep];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ri.slot_cap) return;
   const size_t slot = static_cast<size_t>(ri.slot_base) + i;
   if (i >= ri.n_fluid) {
-    st4(pos, slot, R4<R>{R(0), R(0), R(0), make_slot_id<R>(SLOT_EMPTY)});
-    st4(vel, slot, R4<R>{R(0), R(0), R(0), R(0)});
+    st_rec(st, slot, R4<R>{R(0), R(0), R(0), make_slot_id<R>(SLOT_EMPTY)},
+           R4<R>{R(0), R(0), R(0), R(0)});
     return;
   }
   const Uniform2<double> a = philox_uniforms<double>(seed, static_cast<uint32_t>(i), 0xA11CEull, 0u);
@@ -270,8 +294,7 @@ __global__ void k_init_solvent(const RepInfo* reps, int rep, R* pos, R* vel,
     v = R4<R>{static_cast<R>(sd * r1 * cos(t1)), static_cast<R>(sd * r1 * sin(t1)),
               static_cast<R>(sd * r2 * cos(t2)), R(0)};
   }
-  st4(pos, slot, x);
-  st4(vel, slot, v);
+  st_rec(st, slot, x, v);
 }
 
 // One CTA per replica: MPC::check_bounds, then shift and bin the monomers.
@@ -296,7 +319,33 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
   __syncthreads();
   RepDyn& dn = dyn[r];
   const int out = s_out && ri.mol0_size > 0;
-  if (threadIdx.x == 0) {
+  if (!std::is_same<R, double>::value && out) {
+    // fast path: block-parallel centre of mass (FP64 sums, order free)
+    __shared__ double s_c[6];
+    if (threadIdx.x < 6) s_c[threadIdx.x] = 0.0;
+    __syncthreads();
+    double c[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < ri.mol0_size; i += NT) {
+      const R4<R> x = ld4_rw(mpos, b + i);
+      const R4<R> v = ld4_rw(mvel, b + i);
+      c[0] += x.x; c[1] += x.y; c[2] += x.z;
+      c[3] += v.x; c[4] += v.y; c[5] += v.z;
+    }
+    for (int q = 0; q < 6; ++q) {
+      double t = c[q];
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, o);
+      if ((threadIdx.x & 31) == 0) atomicAdd(&s_c[q], t);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      dn.recentre = 1;
+      const double nm = static_cast<double>(ri.mol0_size);
+      for (int d = 0; d < 3; ++d) {
+        dn.com[d] = s_c[d] / nm;
+        dn.comv[d] = s_c[3 + d] / nm;
+      }
+    }
+  } else if (threadIdx.x == 0) {
     dn.recentre = out;
     if (out) {
       // Molecule::calculate_center_of_mass[_velocity] (Molecule.cpp:139-155):
@@ -365,38 +414,47 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
   }
 }
 
-// Stream, shift, wrap and bin every solvent slot of a slot tile.
+// Stream, shift, wrap and bin every solvent slot of a slot tile. Each thread
+// first loads U records (U independent 32-byte loads in flight), then bins
+// them one by one with the warp-aggregated rank atomic.
 template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepInfo* reps,
-                                                  const RepDyn* dyn, const R* __restrict__ pos,
-                                                  const R* __restrict__ vel,
+                                                  const RepDyn* dyn, const R* __restrict__ st,
                                                   uint2* __restrict__ keys, uint32_t* count,
                                                   ErrorState* err, int strict) {
+  constexpr int U = 4;
   const Tile t = tiles[blockIdx.x];
   const RepInfo& ri = reps[t.rep];
   const RepDyn dn = dyn[t.rep];
   const Geo<R> g = make_geo<R>(ri, dn, 0);
-  const R h = static_cast<R>(dn.h);
   const uint32_t cbase = static_cast<uint32_t>(ri.cell_base);
   const uint32_t ncell = static_cast<uint32_t>(ri.n_cell);
-  for (int base = t.begin; base < t.end; base += NT) {
-    const int i = base + threadIdx.x;
-    uint32_t key = KEY_NONE;
-    if (i < t.end) {
-      R4<R> x = ld4(pos, i);
-      if (slot_id(x.w) != SLOT_EMPTY) {
-        R4<R> v = ld4(vel, i);
-        fluid_to_collision_frame(g, dn, h, x, v);
-        const uint32_t c = cell_of(g, x.x, x.y, x.z, strict != 0);
+  for (int base = t.begin; base < t.end; base += NT * U) {
+    R4<R> x[U], v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = base + u * NT + threadIdx.x;
+      if (i < t.end) {
+        x[u] = ld_pos(st, i);
+        v[u] = ld_vel(st, i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = base + u * NT + threadIdx.x;
+      uint32_t key = KEY_NONE;
+      if (i < t.end && slot_id(x[u].w) != SLOT_EMPTY) {
+        fluid_to_collision_frame(g, x[u], v[u]);
+        const uint32_t c = cell_of(g, x[u].x, x[u].y, x[u].z, strict != 0);
         if (c >= ncell) {
           raise_error(err, ERR_FLUID_CELL, static_cast<uint32_t>(t.rep), static_cast<uint32_t>(i));
         } else {
           key = cbase + c;
         }
       }
+      const uint32_t rank = warp_rank(count, key);
+      if (i < t.end) keys[i] = make_uint2(key, rank);
     }
-    const uint32_t rank = warp_rank(count, key);
-    if (i < t.end) keys[i] = make_uint2(key, rank);
   }
 }
 
@@ -425,10 +483,33 @@ template <typename R>
 __device__ __forceinline__ typename AccT<R>::type to_acc(R v);
 template <>
 __device__ __forceinline__ double to_acc<double>(double v) { return v; }
+// v * 2^32 rounded to an integer, built from two 32-bit conversions (the
+// 64-bit float<->int conversions run on the FP64 pipe, which is narrow on
+// GB300): hi = trunc(v * 2^16) is exact, the remainder v * 2^16 - hi is exact
+// in FP32, and its rounding at 2^-16 gives the low bits. Valid for |v| < 2^15.
 template <>
 __device__ __forceinline__ long long to_acc<float>(float v) {
-  return __float2ll_rn(v * kFixScale);
+  const float a = v * 65536.0f;
+  const int hi = __float2int_rz(a);
+  const int lo = __float2int_rn((a - static_cast<float>(hi)) * 65536.0f);
+  return static_cast<long long>(hi) * 65536ll + lo;
 }
+
+// int64 2^32 fixed point back to float (two 32-bit conversions).
+__device__ __forceinline__ float acc_to_float(long long a) {
+  const int hi = static_cast<int>(a >> 32);
+  const unsigned lo = static_cast<unsigned>(a & 0xFFFFFFFFll);
+  return static_cast<float>(hi) + static_cast<float>(lo) * kFixInv;
+}
+
+template <typename T>
+struct AtomT {
+  typedef unsigned long long type;
+};
+template <>
+struct AtomT<double> {
+  typedef double type;
+};
 
 // Segmented inclusive scan over lanes holding consecutive sorted particles;
 // the last lane of each run adds the run total into smem[key*Q + q].
@@ -447,34 +528,38 @@ __device__ __forceinline__ void seg_reduce_to_smem(int key, T (&val)[Q], T* smem
   const int k_dn = __shfl_down_sync(0xFFFFFFFFu, key, 1);
   const bool tail = (lane == 31u) || (k_dn != key);
   if (tail && key >= 0) {
+    typedef typename AtomT<T>::type AT;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) atomicAdd(reinterpret_cast<typename std::conditional<std::is_same<T, double>::value, double, unsigned long long>::type*>(smem + key * Q + q),
-                                          static_cast<typename std::conditional<std::is_same<T, double>::value, double, unsigned long long>::type>(val[q]));
+    for (int q = 0; q < Q; ++q)
+      atomicAdd(reinterpret_cast<AT*>(smem + key * Q + q), static_cast<AT>(val[q]));
   }
 }
 
+// A particle of a collide tile in the collision frame.
 template <typename R>
 struct Particle {
-  R4<R> x;  // collision-frame position (solvent only)
-  R4<R> v;  // collision-frame velocity
+  R4<R> x;   // shifted, wrapped position (solvent); .w: particle id
+  R4<R> v;   // velocity in the primary box frame
   R m;
-  int lc;   // local cell in the tile, -1 for an idle lane
+  int lc;    // local cell in the tile, -1 for an idle lane
   uint32_t src;
 };
 
-// Everything k_collide needs to turn a sorted position into a particle.
+__device__ __forceinline__ float pack_src(float, uint32_t s) { return __uint_as_float(s); }
+__device__ __forceinline__ double pack_src(double, uint32_t s) { return static_cast<double>(s); }
+__device__ __forceinline__ uint32_t unpack_src(float w) { return __float_as_uint(w); }
+__device__ __forceinline__ uint32_t unpack_src(double w) { return static_cast<uint32_t>(w); }
+
 template <typename R>
 struct CollideCtx {
   const uint32_t* __restrict__ perm;
-  const R* __restrict__ pos;
-  const R* __restrict__ vel;
+  const R* __restrict__ st;
   const R* mpos;
   R* mvel;
   const uint2* mkey;
   const int* mimg;
   Geo<R> g;
   RepDyn dn;
-  R h;
   R solvent_mass;
   uint32_t cbase;
   uint32_t c0;
@@ -483,39 +568,53 @@ struct CollideCtx {
   ErrorState* err;
 };
 
+// Reconstructs sorted position p of the tile from global memory (the gather
+// stage and the overflow path share it).
 template <typename R>
-__device__ __forceinline__ void load_particle(Particle<R>& P, uint32_t p, uint32_t p1,
-                                              const CollideCtx<R>& C) {
-  P.lc = -1;
-  if (p >= p1) return;
-  const uint32_t src = C.perm[p];
-  P.src = src;
-  if (src & MONO_BIT) {
-    const uint32_t m = src & ~MONO_BIT;
-    P.v = ld4_rw(C.mvel, m);
-    P.m = ld4_rw(C.mpos, m).w;
+__device__ __forceinline__ void finish_particle(Particle<R>& P, uint32_t p, const CollideCtx<R>& C) {
+  if (P.src & MONO_BIT) {
+    const uint32_t m = P.src & ~MONO_BIT;
     if (C.g.wrap_mono == MONOBIN_WRAPPED)
-      P.v.x -= static_cast<R>(C.mimg[m]) * C.g.shear * C.g.L[1];
+      P.v.x = r_sub(P.v.x, r_mul(r_mul(static_cast<R>(C.mimg[m]), C.g.shear), C.g.L[1]));
     P.lc = static_cast<int>(C.mkey[m].x - C.c0);
   } else {
-    P.x = ld4(C.pos, src);
-    P.v = ld4(C.vel, src);
-    fluid_to_collision_frame(C.g, C.dn, C.h, P.x, P.v);
+    fluid_to_collision_frame(C.g, P.x, P.v);
     P.m = C.solvent_mass;
     const uint32_t c = cell_of(C.g, P.x.x, P.x.y, P.x.z, C.strict);
     P.lc = static_cast<int>(C.cbase + c - C.c0);
   }
   if (P.lc < 0 || P.lc >= C.nc) {  // cannot happen when binning and recompute agree
-    raise_error(C.err, ERR_KEY_MISMATCH, p, src);
+    raise_error(C.err, ERR_KEY_MISMATCH, p, P.src);
     P.lc = -1;
   }
 }
 
 template <typename R>
-__device__ __forceinline__ void acc_momentum(const Particle<R>& P,
-                                             typename AccT<R>::type* s_acc) {
+__device__ __forceinline__ void fetch_raw(Particle<R>& P, uint32_t src, const CollideCtx<R>& C) {
+  P.src = src;
+  if (src & MONO_BIT) {
+    const uint32_t m = src & ~MONO_BIT;
+    P.v = ld4_rw(C.mvel, m);
+    P.m = ld4_rw(C.mpos, m).w;
+  } else {
+    P.x = ld_pos(C.st, src);
+    P.v = ld_vel(C.st, src);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void load_particle(Particle<R>& P, uint32_t p, uint32_t p1,
+                                              const CollideCtx<R>& C) {
+  P.lc = -1;
+  if (p >= p1) return;
+  fetch_raw(P, C.perm[p], C);
+  finish_particle(P, p, C);
+}
+
+template <typename R>
+__device__ __forceinline__ void momentum_terms(const Particle<R>& P,
+                                               typename AccT<R>::type (&val)[4]) {
   typedef typename AccT<R>::type A;
-  A val[4];
   if (P.lc >= 0) {
     val[0] = to_acc<R>(P.v.x * P.m);
     val[1] = to_acc<R>(P.v.y * P.m);
@@ -524,27 +623,23 @@ __device__ __forceinline__ void acc_momentum(const Particle<R>& P,
   } else {
     val[0] = val[1] = val[2] = val[3] = A(0);
   }
-  seg_reduce_to_smem<A, 4>(P.lc, val, s_acc);
 }
 
 template <typename R>
-__device__ __forceinline__ void acc_energy(const Particle<R>& P, const R* s_cmv,
-                                           typename AccT<R>::type* s_e) {
+__device__ __forceinline__ typename AccT<R>::type energy_term(const Particle<R>& P,
+                                                              const R* s_cmv) {
   typedef typename AccT<R>::type A;
-  A val[1] = {A(0)};
-  if (P.lc >= 0) {
-    const R d0 = P.v.x - s_cmv[3 * P.lc], d1 = P.v.y - s_cmv[3 * P.lc + 1],
-            d2 = P.v.z - s_cmv[3 * P.lc + 2];
-    val[0] = to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2));
-  }
-  seg_reduce_to_smem<A, 1>(P.lc, val, s_e);
+  if (P.lc < 0) return A(0);
+  const R d0 = P.v.x - s_cmv[3 * P.lc], d1 = P.v.y - s_cmv[3 * P.lc + 1],
+          d2 = P.v.z - s_cmv[3 * P.lc + 2];
+  return to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2));
 }
 
 // Thermostat + rotation of one particle, then the unshift/wrap and store.
 template <typename R>
 __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, const R* s_cmv,
                                                 const R* s_rot, const R* s_scale,
-                                                const CollideCtx<R>& C, R* pos_out, R* vel_out,
+                                                const CollideCtx<R>& C, R* st_out,
                                                 ErrorState* err) {
   if (P.lc < 0) return;
   const R* cm = s_cmv + 3 * P.lc;
@@ -576,57 +671,72 @@ __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, cons
   if (P.src & MONO_BIT) {
     const uint32_t m = P.src & ~MONO_BIT;
     if (C.g.wrap_mono == MONOBIN_WRAPPED)
-      vx += static_cast<R>(C.mimg[m]) * C.g.shear * C.g.L[1];
+      vx = r_add(vx, r_mul(r_mul(static_cast<R>(C.mimg[m]), C.g.shear), C.g.L[1]));
     R4<R> v = ld4_rw(C.mvel, m);
     v.x = vx;
     v.y = vy;
     v.z = vz;
     st4(C.mvel, m, v);
-    R4<R> hole{R(0), R(0), R(0), make_slot_id<R>(SLOT_EMPTY)};
-    st4(pos_out, p, hole);
+    st_rec(st_out, p, R4<R>{R(0), R(0), R(0), make_slot_id<R>(SLOT_EMPTY)},
+           R4<R>{R(0), R(0), R(0), R(0)});
   } else {
     R4<R> x = P.x;
-    x.x += -static_cast<R>(C.dn.shift[0]);
-    x.y += -static_cast<R>(C.dn.shift[1]);
-    x.z += -static_cast<R>(C.dn.shift[2]);
-    le_wrap(C.g, x.x, x.y, x.z, vx);
-    st4(pos_out, p, x);
-    st4(vel_out, p, R4<R>{vx, vy, vz, R(0)});
+    x.x = r_add(x.x, -C.g.shift[0]);
+    x.y = r_add(x.y, -C.g.shift[1]);
+    x.z = r_add(x.z, -C.g.shift[2]);
+    le_wrap(C.g, x.x, x.y, x.z, vx);  // x.w: the particle id, carried through
+    st_rec(st_out, p, x, R4<R>{vx, vy, vz, R(0)});
   }
 }
 
-// One CTA per tile of <= CT cells of one replica. Particles are held in
-// registers (PPT per thread); a tile larger than NT*PPT particles reloads
-// the excess in every phase (correct, slower).
-template <typename R, int NT, int CT, int PPT>
+// Dynamic shared memory of k_collide: CAP staged particles (position and
+// velocity records, 16-bit local cell).
+template <typename R>
+constexpr size_t collide_dyn_smem(int cap) {
+  return static_cast<size_t>(cap) * (2 * sizeof(R4<R>) + sizeof(short));
+}
+
+// One CTA per tile of <= CT cells of one replica.
+//  stage  : gather the tile's particles (perm -> 32-byte records, GU loads in
+//           flight per thread), recompute their collision-frame state, keep
+//           them in shared memory;
+//  reduce : per-cell momentum and mass, then kinetic energy about the cell
+//           velocity, by warp-shuffle segmented scans + shared atomics;
+//  draw   : one thread per cell: MBS scale factor and rotation matrix;
+//  apply  : rotate/scale, undo the shift, write the tile back in cell order.
+// A tile holding more than CAP particles processes the excess straight from
+// global memory in every phase (correct, slower).
+template <typename R, int NT, int CT, int CAP>
 __global__ void __launch_bounds__(NT) k_collide(
     const Tile* tiles, const RepInfo* reps, const RepDyn* dyn, const uint32_t* __restrict__ off,
-    const uint32_t* __restrict__ perm, const R* __restrict__ pos_in,
-    const R* __restrict__ vel_in, R* __restrict__ pos_out, R* __restrict__ vel_out,
+    const uint32_t* __restrict__ perm, const R* __restrict__ st_in, R* __restrict__ st_out,
     const R* mpos, R* mvel, const uint2* mkey, const int* mimg, const double* inj_gamma,
     const double* inj_uphi, const double* inj_utheta, int rng, double rot_c, double rot_s,
     int strict, int mono_bin, ErrorState* err) {
   typedef typename AccT<R>::type A;
+  constexpr int GU = 4;
   __shared__ A s_acc[CT * 4];
   __shared__ A s_e[CT];
   __shared__ R s_cmv[CT * 3];
   __shared__ R s_rot[CT * 9];
   __shared__ R s_scale[CT];
   __shared__ uint32_t s_off[CT + 1];
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  R4<R>* s_x = reinterpret_cast<R4<R>*>(s_dyn);
+  R4<R>* s_v = s_x + CAP;
+  short* s_lc = reinterpret_cast<short*>(s_v + CAP);
 
   const Tile t = tiles[blockIdx.x];
   const RepInfo& ri = reps[t.rep];
   CollideCtx<R> C;
   C.perm = perm;
-  C.pos = pos_in;
-  C.vel = vel_in;
+  C.st = st_in;
   C.mpos = mpos;
   C.mvel = mvel;
   C.mkey = mkey;
   C.mimg = mimg;
   C.dn = dyn[t.rep];
   C.g = make_geo<R>(ri, C.dn, mono_bin);
-  C.h = static_cast<R>(C.dn.h);
   C.solvent_mass = static_cast<R>(ri.solvent_mass);
   C.cbase = static_cast<uint32_t>(ri.cell_base);
   C.c0 = static_cast<uint32_t>(t.begin);
@@ -640,21 +750,60 @@ __global__ void __launch_bounds__(NT) k_collide(
   for (int i = threadIdx.x; i < nc; i += NT) s_e[i] = A(0);
   __syncthreads();
   const uint32_t p0 = s_off[0], p1 = s_off[nc];
+  const int n = static_cast<int>(p1 - p0);
+  const int nloc = n < CAP ? n : CAP;
 
-  // phase A: per-cell momentum and mass (MPC::calculateCMV, MPC.cpp:314-322)
-  Particle<R> cache[PPT];
+  // stage
+  for (int base = 0; base < nloc; base += NT * GU) {
+    uint32_t src[GU];
 #pragma unroll
-  for (int k = 0; k < PPT; ++k) {
-    cache[k].lc = -1;
-    if (p0 + k * NT < p1) {
-      load_particle(cache[k], p0 + k * NT + threadIdx.x, p1, C);
-      acc_momentum(cache[k], s_acc);
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      src[u] = j < nloc ? perm[p0 + j] : 0u;
+    }
+    Particle<R> P[GU];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      if (j < nloc) fetch_raw(P[u], src[u], C);
+    }
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      if (j < nloc) {
+        finish_particle(P[u], p0 + j, C);
+        R4<R> x = P[u].x;  // solvent: .w keeps the particle id
+        if (P[u].src & MONO_BIT) x.w = pack_src(R(0), P[u].src);
+        R4<R> v = P[u].v;
+        v.w = P[u].m;
+        s_x[j] = x;
+        s_v[j] = v;
+        s_lc[j] = static_cast<short>(P[u].lc);
+      }
     }
   }
-  for (uint32_t base = p0 + PPT * NT; base < p1; base += NT) {
+  __syncthreads();
+
+  // reduce: momentum and mass (MPC::calculateCMV, MPC.cpp:314-322)
+  for (int base = 0; base < nloc; base += NT) {
+    const int j = base + threadIdx.x;
     Particle<R> P;
-    load_particle(P, base + threadIdx.x, p1, C);
-    acc_momentum(P, s_acc);
+    P.lc = -1;
+    if (j < nloc) {
+      P.v = s_v[j];
+      P.m = P.v.w;
+      P.lc = s_lc[j];
+    }
+    A val[4];
+    momentum_terms(P, val);
+    seg_reduce_to_smem<A, 4>(P.lc, val, s_acc);
+  }
+  for (int base = CAP; base < n; base += NT) {
+    Particle<R> P;
+    load_particle(P, p0 + base + threadIdx.x, p1, C);
+    A val[4];
+    momentum_terms(P, val);
+    seg_reduce_to_smem<A, 4>(P.lc, val, s_acc);
   }
   __syncthreads();
   for (int lc = threadIdx.x; lc < nc; lc += NT) {
@@ -666,9 +815,9 @@ __global__ void __launch_bounds__(NT) k_collide(
         if (mt > R(0)) cm[d] /= mt;
       }
     } else {
-      const float mt = static_cast<float>(s_acc[4 * lc + 3]) * kFixInv;
+      const float mt = acc_to_float(s_acc[4 * lc + 3]);
       for (int d = 0; d < 3; ++d) {
-        const float pd = static_cast<float>(s_acc[4 * lc + d]) * kFixInv;
+        const float pd = acc_to_float(s_acc[4 * lc + d]);
         cm[d] = mt > 0.f ? static_cast<R>(pd / mt) : R(0);
       }
     }
@@ -678,30 +827,40 @@ __global__ void __launch_bounds__(NT) k_collide(
   }
   __syncthreads();
 
-  // phase B: kinetic energy relative to the cell velocity (MPC.cpp:277-280)
-#pragma unroll
-  for (int k = 0; k < PPT; ++k)
-    if (p0 + k * NT < p1) acc_energy(cache[k], s_cmv, s_e);
-  for (uint32_t base = p0 + PPT * NT; base < p1; base += NT) {
+  // reduce: kinetic energy about the cell velocity (MPC.cpp:277-280)
+  for (int base = 0; base < nloc; base += NT) {
+    const int j = base + threadIdx.x;
     Particle<R> P;
-    load_particle(P, base + threadIdx.x, p1, C);
-    acc_energy(P, s_cmv, s_e);
+    P.lc = -1;
+    if (j < nloc) {
+      P.v = s_v[j];
+      P.m = P.v.w;
+      P.lc = s_lc[j];
+    }
+    A val[1] = {energy_term(P, s_cmv)};
+    seg_reduce_to_smem<A, 1>(P.lc, val, s_e);
+  }
+  for (int base = CAP; base < n; base += NT) {
+    Particle<R> P;
+    load_particle(P, p0 + base + threadIdx.x, p1, C);
+    A val[1] = {energy_term(P, s_cmv)};
+    seg_reduce_to_smem<A, 1>(P.lc, val, s_e);
   }
   __syncthreads();
 
-  // per-cell draws: MBS scaling (MPC.cpp:287-289) and rotation (MPC.cpp:244-257)
+  // draw: MBS scaling (MPC.cpp:287-289) and rotation (MPC.cpp:244-257)
   for (int lc = threadIdx.x; lc < nc; lc += NT) {
     const uint32_t cg = C.c0 + lc;
     const uint32_t cl = cg - C.cbase;
-    const uint32_t n = s_off[lc + 1] - s_off[lc];
+    const uint32_t nn = s_off[lc + 1] - s_off[lc];
     R scale = R(-1);
-    if (n >= 2u) {
+    if (nn >= 2u) {
       R ekin;
       if (std::is_same<R, double>::value) {
         ekin = static_cast<R>(s_e[lc]);
         ekin *= R(0.5);
       } else {
-        ekin = static_cast<R>(static_cast<float>(s_e[lc]) * kFixInv * 0.5f);
+        ekin = static_cast<R>(acc_to_float(s_e[lc]) * 0.5f);
       }
       R gv;
       if (rng == RNG_INJECT) {
@@ -709,9 +868,9 @@ __global__ void __launch_bounds__(NT) k_collide(
       } else {
         bool ok = true;
         gv = philox_gamma<R>(ri.seed, cl, C.dn.step,
-                             static_cast<R>(1.5) * static_cast<R>(n - 1u), &ok) *
+                             static_cast<R>(1.5) * static_cast<R>(nn - 1u), &ok) *
              static_cast<R>(ri.kT);
-        if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, n);
+        if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
       }
       scale = (ekin > R(0)) ? sqrt(gv / ekin) : R(1);
     }
@@ -728,10 +887,10 @@ __global__ void __launch_bounds__(NT) k_collide(
     const R two_pi = R(6.283185307179586476925286766559);
     const R phi = two_pi * uphi;
     const R theta = R(2) * (uth - R(0.5));
-    const R st = sqrt(R(1) - theta * theta);
+    const R stt = sqrt(R(1) - theta * theta);
     R sphi, cphi;
     sincos(phi, &sphi, &cphi);
-    const R a0 = st * cphi, a1 = st * sphi, a2 = theta;
+    const R a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
     const R c = static_cast<R>(rot_c), s = static_cast<R>(rot_s);
     R* M = s_rot + 9 * lc;
     M[0] = a0 * a0 + (R(1) - a0 * a0) * c;
@@ -746,16 +905,20 @@ __global__ void __launch_bounds__(NT) k_collide(
   }
   __syncthreads();
 
-  // phase C: apply, undo the grid shift, write back in cell order
-#pragma unroll
-  for (int k = 0; k < PPT; ++k)
-    if (p0 + k * NT < p1)
-      apply_collision(cache[k], p0 + k * NT + threadIdx.x, s_cmv, s_rot, s_scale, C, pos_out,
-                      vel_out, err);
-  for (uint32_t base = p0 + PPT * NT; base < p1; base += NT) {
+  // apply
+  for (int j = threadIdx.x; j < nloc; j += NT) {
     Particle<R> P;
-    load_particle(P, base + threadIdx.x, p1, C);
-    apply_collision(P, base + threadIdx.x, s_cmv, s_rot, s_scale, C, pos_out, vel_out, err);
+    P.x = s_x[j];
+    P.v = s_v[j];
+    P.m = P.v.w;
+    P.lc = s_lc[j];
+    P.src = unpack_src(P.x.w);  // solvent id (no MONO_BIT) or MONO_BIT | monomer
+    apply_collision(P, p0 + j, s_cmv, s_rot, s_scale, C, st_out, err);
+  }
+  for (int base = CAP; base < n; base += NT) {
+    Particle<R> P;
+    load_particle(P, p0 + base + threadIdx.x, p1, C);
+    apply_collision(P, p0 + base + threadIdx.x, s_cmv, s_rot, s_scale, C, st_out, err);
   }
 }
 
@@ -765,7 +928,7 @@ __global__ void __launch_bounds__(NT) k_collide(
 template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_temperature(
     const Tile* tiles, const RepInfo* reps, const uint32_t* __restrict__ off,
-    const uint32_t* __restrict__ perm, const R* __restrict__ vel_cur, const R* mpos,
+    const uint32_t* __restrict__ perm, const R* __restrict__ st_cur, const R* mpos,
     const R* mvel, const int* mimg, int mono_bin, TempPartial* partial) {
   __shared__ double s_e[NT];
   __shared__ unsigned s_f[NT];
@@ -788,7 +951,7 @@ __global__ void __launch_bounds__(NT) k_temperature(
         vx = v.x; vy = v.y; vz = v.z;
         if (mono_bin == MONOBIN_WRAPPED) vx -= static_cast<double>(mimg[mi]) * shearLy;
       } else {
-        const R4<R> v = ld4(vel_cur, p);
+        const R4<R> v = ld_vel(st_cur, p);
         m = ri.solvent_mass;
         vx = v.x; vy = v.y; vz = v.z;
         ++nf;
@@ -799,7 +962,7 @@ __global__ void __launch_bounds__(NT) k_temperature(
     double ek = 0.0;
     for (uint32_t p = a; p < b; ++p) {
       if (perm[p] & MONO_BIT) continue;
-      const R4<R> v = ld4(vel_cur, p);
+      const R4<R> v = ld_vel(st_cur, p);
       const double d0 = v.x - px, d1 = v.y - py, d2 = v.z - pz;
       ek += ri.solvent_mass * ((d0 * d0 + d1 * d1) + d2 * d2);
     }

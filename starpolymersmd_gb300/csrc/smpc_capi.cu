@@ -42,8 +42,7 @@ struct smpc_ctx {
   Tile* d_tmp_tiles = nullptr;
   TempPartial* d_tpart = nullptr;
 
-  void* d_pos[2] = {nullptr, nullptr};
-  void* d_vel[2] = {nullptr, nullptr};
+  void* d_rec[2] = {nullptr, nullptr};  // solvent slot records: 8 Reals (pos, vel) each
   int cur = 0;
   uint2* d_keys = nullptr;
   uint32_t* d_perm = nullptr;
@@ -122,15 +121,12 @@ smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur);
 template <typename R>
 int launch_collision(smpc_ctx* ctx, int rng, int cur) {
   const int strict = ctx->opt.strict_cells;
-  R* pos_in = static_cast<R*>(ctx->d_pos[cur]);
-  R* vel_in = static_cast<R*>(ctx->d_vel[cur]);
-  R* pos_out = static_cast<R*>(ctx->d_pos[cur ^ 1]);
-  R* vel_out = static_cast<R*>(ctx->d_vel[cur ^ 1]);
+  const R* rec_in = static_cast<const R*>(ctx->d_rec[cur]);
   smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
                             static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
                             ctx->d_err, ctx->opt.mono_bin, strict, ctx->st);
-  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, pos_in,
-                            vel_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
+  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, rec_in,
+                            ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
   smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
@@ -141,10 +137,6 @@ int launch_collision(smpc_ctx* ctx, int rng, int cur) {
 
 template <typename R>
 smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
-  R* pos_in = static_cast<R*>(ctx->d_pos[cur]);
-  R* vel_in = static_cast<R*>(ctx->d_vel[cur]);
-  R* pos_out = static_cast<R*>(ctx->d_pos[cur ^ 1]);
-  R* vel_out = static_cast<R*>(ctx->d_vel[cur ^ 1]);
   const int strict = ctx->opt.strict_cells;
   smpc::CollideArgs<R> a;
   a.tiles = ctx->d_col_tiles;
@@ -153,10 +145,8 @@ smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
   a.dyn = ctx->d_dyn;
   a.off = ctx->d_off;
   a.perm = ctx->d_perm;
-  a.pos_in = pos_in;
-  a.vel_in = vel_in;
-  a.pos_out = pos_out;
-  a.vel_out = vel_out;
+  a.st_in = static_cast<const R*>(ctx->d_rec[cur]);
+  a.st_out = static_cast<R*>(ctx->d_rec[cur ^ 1]);
   a.mpos = static_cast<R*>(ctx->d_mpos);
   a.mvel = static_cast<R*>(ctx->d_mvel);
   a.mkey = ctx->d_mkey;
@@ -202,8 +192,7 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
   const int nsub = ctx->opt.step_update;
   const int strict = ctx->opt.strict_cells;
   const double adv = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / nsub : 1.0;
-  R* pos_in = static_cast<R*>(ctx->d_pos[cur]);
-  R* vel_in = static_cast<R*>(ctx->d_vel[cur]);
+  const R* rec_in = static_cast<const R*>(ctx->d_rec[cur]);
   cudaEventRecord(ev[0], ctx->st);
   launch_md_steps<R>(ctx, nsub, 0, 0);
   cudaEventRecord(ev[1 + PH_MD], ctx->st);
@@ -213,8 +202,8 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
                             static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
                             ctx->d_err, ctx->opt.mono_bin, strict, ctx->st);
   cudaEventRecord(ev[1 + PH_MONO], ctx->st);
-  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, pos_in,
-                            vel_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
+  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, rec_in,
+                            ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
   cudaEventRecord(ev[1 + PH_BIN], ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
@@ -279,24 +268,23 @@ double id_to_w<double>(uint32_t id) {
 template <typename R>
 int set_fluid_t(smpc_ctx* ctx, int rep, const double* pos, const double* vel) {
   const RepInfo& ri = ctx->reps[rep];
-  std::vector<R> p(4 * static_cast<size_t>(ri.slot_cap)), v(4 * static_cast<size_t>(ri.slot_cap));
+  std::vector<R> rec(8 * static_cast<size_t>(ri.slot_cap));
   for (int i = 0; i < ri.slot_cap; ++i) {
+    R* p = rec.data() + 8 * static_cast<size_t>(i);
     if (i < ri.n_fluid) {
-      to_r4<R>(pos, 0.0, p.data(), i);
-      p[4 * i + 3] = id_to_w<R>(static_cast<uint32_t>(i));
-      to_r4<R>(vel, 0.0, v.data(), i);
+      for (int d = 0; d < 3; ++d) {
+        p[d] = static_cast<R>(pos[3 * static_cast<size_t>(i) + d]);
+        p[4 + d] = static_cast<R>(vel[3 * static_cast<size_t>(i) + d]);
+      }
+      p[3] = id_to_w<R>(static_cast<uint32_t>(i));
+      p[7] = R(0);
     } else {
-      for (int d = 0; d < 3; ++d) p[4 * i + d] = v[4 * i + d] = R(0);
-      p[4 * i + 3] = id_to_w<R>(smpc::SLOT_EMPTY);
-      v[4 * i + 3] = R(0);
+      for (int d = 0; d < 8; ++d) p[d] = R(0);
+      p[3] = id_to_w<R>(smpc::SLOT_EMPTY);
     }
   }
-  const size_t off = 4 * static_cast<size_t>(ri.slot_base);
-  const size_t bytes = p.size() * sizeof(R);
-  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_pos[ctx->cur]) + off, p.data(), bytes,
-                     cudaMemcpyHostToDevice, ctx->st));
-  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_vel[ctx->cur]) + off, v.data(), bytes,
-                     cudaMemcpyHostToDevice, ctx->st));
+  CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_rec[ctx->cur]) + 8 * static_cast<size_t>(ri.slot_base),
+                     rec.data(), rec.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->st));
   CU(cudaStreamSynchronize(ctx->st));
   return SMPC_OK;
 }
@@ -304,23 +292,20 @@ int set_fluid_t(smpc_ctx* ctx, int rep, const double* pos, const double* vel) {
 template <typename R>
 int get_fluid_t(smpc_ctx* ctx, int rep, double* pos, double* vel) {
   const RepInfo& ri = ctx->reps[rep];
-  std::vector<R> p(4 * static_cast<size_t>(ri.slot_cap)), v(4 * static_cast<size_t>(ri.slot_cap));
-  const size_t off = 4 * static_cast<size_t>(ri.slot_base);
-  const size_t bytes = p.size() * sizeof(R);
-  CU(cudaMemcpyAsync(p.data(), static_cast<R*>(ctx->d_pos[ctx->cur]) + off, bytes,
-                     cudaMemcpyDeviceToHost, ctx->st));
-  CU(cudaMemcpyAsync(v.data(), static_cast<R*>(ctx->d_vel[ctx->cur]) + off, bytes,
-                     cudaMemcpyDeviceToHost, ctx->st));
+  std::vector<R> rec(8 * static_cast<size_t>(ri.slot_cap));
+  CU(cudaMemcpyAsync(rec.data(), static_cast<R*>(ctx->d_rec[ctx->cur]) + 8 * static_cast<size_t>(ri.slot_base),
+                     rec.size() * sizeof(R), cudaMemcpyDeviceToHost, ctx->st));
   CU(cudaStreamSynchronize(ctx->st));
   int seen = 0;
   for (int i = 0; i < ri.slot_cap; ++i) {
-    const uint32_t id = id_of<R>(p[4 * i + 3]);
+    const R* p = rec.data() + 8 * static_cast<size_t>(i);
+    const uint32_t id = id_of<R>(p[3]);
     if (id == smpc::SLOT_EMPTY) continue;
     if (id >= static_cast<uint32_t>(ri.n_fluid))
       return fail(ctx, SMPC_E_STATE, "corrupt solvent slot id");
     for (int d = 0; d < 3; ++d) {
-      if (pos) pos[3 * static_cast<size_t>(id) + d] = static_cast<double>(p[4 * i + d]);
-      if (vel) vel[3 * static_cast<size_t>(id) + d] = static_cast<double>(v[4 * i + d]);
+      if (pos) pos[3 * static_cast<size_t>(id) + d] = static_cast<double>(p[d]);
+      if (vel) vel[3 * static_cast<size_t>(id) + d] = static_cast<double>(p[4 + d]);
     }
     ++seen;
   }
@@ -427,7 +412,7 @@ int temperature_all_t(smpc_ctx* ctx, double* out) {
   if (!ctx->collided) return fail(ctx, SMPC_E_STATE, "no collision has run yet (no cell lists)");
   const int nt = static_cast<int>(ctx->h_tmp_tiles.size());
   smpc::launch_temperature<R>(ctx->d_tmp_tiles, nt, ctx->d_reps, ctx->d_off, ctx->d_perm,
-                              static_cast<R*>(ctx->d_vel[ctx->cur]), static_cast<R*>(ctx->d_mpos),
+                              static_cast<R*>(ctx->d_rec[ctx->cur]), static_cast<R*>(ctx->d_mpos),
                               static_cast<R*>(ctx->d_mvel), ctx->d_mimg, ctx->opt.mono_bin,
                               ctx->d_tpart, ctx->st);
   ctx->stage_t.resize(nt);
@@ -458,7 +443,7 @@ int temperature_t(smpc_ctx* ctx, int rep, double* out) {
       ++count;
     }
   smpc::launch_temperature<R>(ctx->d_tmp_tiles + first, count, ctx->d_reps, ctx->d_off,
-                              ctx->d_perm, static_cast<R*>(ctx->d_vel[ctx->cur]),
+                              ctx->d_perm, static_cast<R*>(ctx->d_rec[ctx->cur]),
                               static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
                               ctx->d_mimg, ctx->opt.mono_bin, ctx->d_tpart, ctx->st);
   std::vector<TempPartial> part(count);
@@ -490,10 +475,7 @@ template <typename R>
 int create_buffers(smpc_ctx* ctx) {
   const size_t S = static_cast<size_t>(ctx->total_slots), M = static_cast<size_t>(ctx->total_mono),
                C = static_cast<size_t>(ctx->total_cells);
-  for (int k = 0; k < 2; ++k) {
-    CU(dalloc(reinterpret_cast<R**>(&ctx->d_pos[k]), 4 * S));
-    CU(dalloc(reinterpret_cast<R**>(&ctx->d_vel[k]), 4 * S));
-  }
+  for (int k = 0; k < 2; ++k) CU(dalloc(reinterpret_cast<R**>(&ctx->d_rec[k]), 8 * S));
   CU(dalloc(&ctx->d_keys, S));
   CU(dalloc(&ctx->d_perm, S + M));
   CU(dalloc(&ctx->d_count, C));
@@ -553,8 +535,7 @@ int upload_bonds(smpc_ctx* ctx) {
 void free_all(smpc_ctx* ctx) {
   for (int k = 0; k < 2; ++k) {
     if (ctx->graph[k]) cudaGraphExecDestroy(ctx->graph[k]);
-    cudaFree(ctx->d_pos[k]);
-    cudaFree(ctx->d_vel[k]);
+    cudaFree(ctx->d_rec[k]);
   }
   void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
@@ -913,12 +894,12 @@ int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int reference_veloc
   cudaSetDevice(ctx->device);
   const RepInfo& ri = ctx->reps[rep];
   if (ctx->opt.precision == SMPC_FP64)
-    smpc::launch_init_solvent<double>(ctx->d_reps, rep, ri.slot_cap, static_cast<double*>(ctx->d_pos[ctx->cur]),
-                                      static_cast<double*>(ctx->d_vel[ctx->cur]), seed, ri.kT,
+    smpc::launch_init_solvent<double>(ctx->d_reps, rep, ri.slot_cap,
+                                      static_cast<double*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
                                       reference_velocities, ctx->st);
   else
-    smpc::launch_init_solvent<float>(ctx->d_reps, rep, ri.slot_cap, static_cast<float*>(ctx->d_pos[ctx->cur]),
-                                     static_cast<float*>(ctx->d_vel[ctx->cur]), seed, ri.kT,
+    smpc::launch_init_solvent<float>(ctx->d_reps, rep, ri.slot_cap,
+                                     static_cast<float*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
                                      reference_velocities, ctx->st);
   CU(cudaGetLastError());
   return SMPC_OK;
