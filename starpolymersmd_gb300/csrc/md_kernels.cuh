@@ -86,8 +86,8 @@ __device__ __forceinline__ R fene_force(bool anchor, R r2) {
 }
 template <typename R>
 __device__ __forceinline__ R fene_pot(bool anchor, R r2) {
-  return anchor ? R(-15.0) * R(20.25) * log(R(1.0) - r2 / R(20.25))
-                : R(-15.0) * R(2.25) * log(R(1.0) - r2 / R(2.25));
+  return anchor ? R(-15.0) * R(20.25) * r_log(R(1.0) - r2 / R(20.25))
+                : R(-15.0) * R(2.25) * r_log(R(1.0) - r2 / R(2.25));
 }
 
 struct MdArgs {
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
           }
           sx[i] = x[k][0]; sy[i] = x[k][1]; sz[i] = x[k][2];
           const R d0 = x[k][0] - xv[k][0], d1 = x[k][1] - xv[k][1], d2 = x[k][2] - xv[k][2];
-          if (sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim) s_rebuild = 1;
+          if (r_sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim) s_rebuild = 1;
         }
       }
     }

@@ -147,17 +147,17 @@ __device__ __forceinline__ Geo<R> make_geo(const RepInfo& ri, const RepDyn& dn, 
 template <typename R>
 __device__ __forceinline__ void le_wrap(const Geo<R>& g, R& x, R& y, R& z, R& vx) {
   if (g.shear_on) {
-    const R cy = round(r_div(y, g.L[1]));
-    x = r_sub(x, r_mul(g.L[0], round(r_div(x, g.L[0]))));
+    const R cy = r_round(r_div(y, g.L[1]));
+    x = r_sub(x, r_mul(g.L[0], r_round(r_div(x, g.L[0]))));
     x = r_sub(x, r_mul(cy, g.delrx));
-    x = r_sub(x, r_mul(g.L[0], round(r_div(x, g.L[0]))));
+    x = r_sub(x, r_mul(g.L[0], r_round(r_div(x, g.L[0]))));
     y = r_sub(y, r_mul(g.L[1], cy));
-    z = r_sub(z, r_mul(g.L[2], round(r_div(z, g.L[2]))));
+    z = r_sub(z, r_mul(g.L[2], r_round(r_div(z, g.L[2]))));
     vx = r_sub(vx, r_mul(r_mul(cy, g.shear), g.L[1]));
   } else {
-    x = r_sub(x, r_mul(round(r_div(x, g.L[0])), g.L[0]));
-    y = r_sub(y, r_mul(round(r_div(y, g.L[1])), g.L[1]));
-    z = r_sub(z, r_mul(round(r_div(z, g.L[2])), g.L[2]));
+    x = r_sub(x, r_mul(r_round(r_div(x, g.L[0])), g.L[0]));
+    y = r_sub(y, r_mul(r_round(r_div(y, g.L[1])), g.L[1]));
+    z = r_sub(z, r_mul(r_round(r_div(z, g.L[2])), g.L[2]));
   }
 }
 
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
     const R4<R> x = ld4_rw(mpos, b + i);
     const R xs[3] = {x.x, x.y, x.z};
     for (int d = 0; d < 3; ++d)
-      if (fabs(xs[d]) >= (static_cast<R>(ri.L[d]) * R(0.5) - R(0.5))) s_out = 1;
+      if (r_fabs(xs[d]) >= (static_cast<R>(ri.L[d]) * R(0.5) - R(0.5))) s_out = 1;
   }
   __syncthreads();
   RepDyn& dn = dyn[r];
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
       x.x += s0; x.y += s1; x.z += s2;  // shiftParticles, monomers unwrapped
       R wx = x.x, wy = x.y, wz = x.z, dvx = R(0);
       if (mono_bin == MONOBIN_WRAPPED) {
-        img = static_cast<int>(round(wy / g.L[1]));
+        img = static_cast<int>(r_round(wy / g.L[1]));
         le_wrap(g, wx, wy, wz, dvx);
       }
       const uint32_t c = cell_of(g, wx, wy, wz, strict != 0);
@@ -666,7 +666,7 @@ __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, cons
   vx = cm[0] + ((M[0] * d0 + M[1] * d1) + M[2] * d2);
   vy = cm[1] + ((M[3] * d0 + M[4] * d1) + M[5] * d2);
   vz = cm[2] + ((M[6] * d0 + M[7] * d1) + M[8] * d2);
-  if (!(isfinite(vx) && isfinite(vy) && isfinite(vz)))
+  if (!(r_isfinite(vx) && r_isfinite(vy) && r_isfinite(vz)))
     raise_error(err, ERR_NONFINITE, p, P.src);
   if (P.src & MONO_BIT) {
     const uint32_t m = P.src & ~MONO_BIT;
@@ -872,7 +872,7 @@ __global__ void __launch_bounds__(NT) k_collide(
              static_cast<R>(ri.kT);
         if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
       }
-      scale = (ekin > R(0)) ? sqrt(gv / ekin) : R(1);
+      scale = (ekin > R(0)) ? r_sqrt(gv / ekin) : R(1);
     }
     s_scale[lc] = scale;
     R uphi, uth;
@@ -887,9 +887,9 @@ __global__ void __launch_bounds__(NT) k_collide(
     const R two_pi = R(6.283185307179586476925286766559);
     const R phi = two_pi * uphi;
     const R theta = R(2) * (uth - R(0.5));
-    const R stt = sqrt(R(1) - theta * theta);
+    const R stt = r_sqrt(R(1) - theta * theta);
     R sphi, cphi;
-    sincos(phi, &sphi, &cphi);
+    r_sincos(phi, &sphi, &cphi);
     const R a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
     const R c = static_cast<R>(rot_c), s = static_cast<R>(rot_s);
     R* M = s_rot + 9 * lc;

@@ -19,6 +19,8 @@
 #pragma once
 #include <stdint.h>
 
+#include "precision.cuh"
+
 namespace smpc {
 
 struct Philox4 {
@@ -97,11 +99,11 @@ __device__ __forceinline__ R philox_gamma(unsigned long long seed, uint32_t cell
                                           unsigned long long step, R shape, bool* ok) {
   const R third = R(1) / R(3);
   const R d = shape - third;
-  const R c = R(1) / sqrt(R(9) * d);
+  const R c = R(1) / r_sqrt(R(9) * d);
   const R two_pi = R(6.283185307179586476925286766559);
   for (uint32_t it = 0; it < 64u; ++it) {
     const Uniform2<R> n = philox_uniforms<R>(seed, cell, step, 1u + 2u * it);
-    const R x = sqrt(R(-2) * log(n.a)) * cos(two_pi * n.b);
+    const R x = r_sqrt(R(-2) * r_log(n.a)) * r_cos(two_pi * n.b);
     R v = R(1) + c * x;
     if (v <= R(0)) continue;
     v = v * v * v;
@@ -111,7 +113,7 @@ __device__ __forceinline__ R philox_gamma(unsigned long long seed, uint32_t cell
       *ok = true;
       return d * v;
     }
-    if (log(u) < R(0.5) * x2 + d * (R(1) - v + log(v))) {
+    if (r_log(u) < R(0.5) * x2 + d * (R(1) - v + r_log(v))) {
       *ok = true;
       return d * v;
     }
