@@ -2,7 +2,7 @@
 #define SMPC_REAL float
 #define SMPC_COLLIDE_NT 256
 #define SMPC_COLLIDE_CT 128
-#define SMPC_COLLIDE_CAP 1536
+#define SMPC_COLLIDE_CAP 1408
 #define SMPC_BIN_NT 256
 #define SMPC_MD_NT 256
 #define SMPC_MD_MPT 4

@@ -10,13 +10,13 @@
 //                  rank from one warp-aggregated atomic per (warp, cell)
 //   scan           exclusive prefix of the cell counts (scan.cu)
 //   k_build_perm   counting-sort scatter: sorted position -> source
-//   k_collide      per tile of cells: gathers its particles, recomputes their
-//                  streamed/shifted state, reduces per-cell momentum, mass and
-//                  kinetic energy with warp-shuffle segmented scans into shared
-//                  memory (int64 fixed point on the fast path), draws the MBS
-//                  thermostat and the rotation (MPC.cpp:239-299), applies them,
-//                  undoes the shift (MPC.cpp:139-140) and writes the solvent back
-//                  in cell order (next step's input is cell-sorted).
+//   k_collide      per tile of cells: gathers its particles into shared memory,
+//                  recomputes their streamed/shifted state, reduces per-cell
+//                  momentum, mass and kinetic energy (one thread per cell over
+//                  the staged particles; int64 fixed point on the fast path),
+//                  draws the MBS thermostat and the rotation (MPC.cpp:239-299),
+//                  applies them, undoes the shift (MPC.cpp:139-140) and writes
+//                  the solvent back in cell order (next step's input is sorted).
 #pragma once
 #include <stdint.h>
 
@@ -158,6 +158,36 @@ __device__ __forceinline__ void le_wrap(const Geo<R>& g, R& x, R& y, R& z, R& vx
     x = r_sub(x, r_mul(r_round(r_div(x, g.L[0])), g.L[0]));
     y = r_sub(y, r_mul(r_round(r_div(y, g.L[1])), g.L[1]));
     z = r_sub(z, r_mul(r_round(r_div(z, g.L[2])), g.L[2]));
+  }
+}
+
+// FP32 fast path: one conditional image shift per axis, exact (x - L is
+// exact for x in [L/2, 2L]) and free of division and rounding. Valid while
+// every coordinate is within 1.5 L of the origin, which one streaming step
+// (|v| h < L) and one grid shift keep true; otherwise the general formula.
+// Coordinates exactly at -L/2 stay at -L/2 (the general formula maps them to
+// +L/2); both are the same face of the periodic box.
+__device__ __forceinline__ float wrap1f(float x, float L, float half) {
+  return x >= half ? r_sub(x, L) : (x < -half ? r_add(x, L) : x);
+}
+__device__ __forceinline__ void le_wrap(const Geo<float>& g, float& x, float& y, float& z,
+                                        float& vx) {
+  if (!(fabsf(x) < 1.5f * g.L[0] && fabsf(y) < 1.5f * g.L[1] && fabsf(z) < 1.5f * g.L[2])) {
+    le_wrap<float>(g, x, y, z, vx);
+    return;
+  }
+  if (g.shear_on) {
+    const float cy = y >= g.half[1] ? 1.0f : (y < -g.half[1] ? -1.0f : 0.0f);
+    x = wrap1f(x, g.L[0], g.half[0]);
+    x = r_sub(x, r_mul(cy, g.delrx));
+    x = wrap1f(x, g.L[0], g.half[0]);
+    y = r_sub(y, r_mul(g.L[1], cy));
+    z = wrap1f(z, g.L[2], g.half[2]);
+    vx = r_sub(vx, r_mul(r_mul(cy, g.shear), g.L[1]));
+  } else {
+    x = wrap1f(x, g.L[0], g.half[0]);
+    y = wrap1f(y, g.L[1], g.half[1]);
+    z = wrap1f(z, g.L[2], g.half[2]);
   }
 }
 
@@ -415,8 +445,9 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
 }
 
 // Stream, shift, wrap and bin every solvent slot of a slot tile. Each thread
-// first loads U records (U independent 32-byte loads in flight), then bins
-// them one by one with the warp-aggregated rank atomic.
+// loads U records (U independent 32-byte loads in flight), computes their
+// keys, then takes ranks with warp-aggregated atomics whose U round trips
+// overlap (all atomics are issued before any result is consumed).
 template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepInfo* reps,
                                                   const RepDyn* dyn, const R* __restrict__ st,
@@ -429,6 +460,8 @@ __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepIn
   const Geo<R> g = make_geo<R>(ri, dn, 0);
   const uint32_t cbase = static_cast<uint32_t>(ri.cell_base);
   const uint32_t ncell = static_cast<uint32_t>(ri.n_cell);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
   for (int base = t.begin; base < t.end; base += NT * U) {
     R4<R> x[U], v[U];
 #pragma unroll
@@ -439,21 +472,36 @@ __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepIn
         v[u] = ld_vel(st, i);
       }
     }
+    uint32_t key[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int i = base + u * NT + threadIdx.x;
-      uint32_t key = KEY_NONE;
+      key[u] = KEY_NONE;
       if (i < t.end && slot_id(x[u].w) != SLOT_EMPTY) {
         fluid_to_collision_frame(g, x[u], v[u]);
         const uint32_t c = cell_of(g, x[u].x, x[u].y, x[u].z, strict != 0);
         if (c >= ncell) {
           raise_error(err, ERR_FLUID_CELL, static_cast<uint32_t>(t.rep), static_cast<uint32_t>(i));
         } else {
-          key = cbase + c;
+          key[u] = cbase + c;
         }
       }
-      const uint32_t rank = warp_rank(count, key);
-      if (i < t.end) keys[i] = make_uint2(key, rank);
+    }
+    unsigned peers[U];
+    uint32_t rbase[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) peers[u] = __match_any_sync(0xFFFFFFFFu, key[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      rbase[u] = 0u;
+      if (lane == static_cast<unsigned>(__ffs(peers[u]) - 1) && key[u] != KEY_NONE)
+        rbase[u] = atomicAdd(count + key[u], __popc(peers[u]));
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, rbase[u], __ffs(peers[u]) - 1);
+      const int i = base + u * NT + threadIdx.x;
+      if (i < t.end) keys[i] = make_uint2(key[u], b0 + __popc(peers[u] & below));
     }
   }
 }
@@ -500,39 +548,6 @@ __device__ __forceinline__ float acc_to_float(long long a) {
   const int hi = static_cast<int>(a >> 32);
   const unsigned lo = static_cast<unsigned>(a & 0xFFFFFFFFll);
   return static_cast<float>(hi) + static_cast<float>(lo) * kFixInv;
-}
-
-template <typename T>
-struct AtomT {
-  typedef unsigned long long type;
-};
-template <>
-struct AtomT<double> {
-  typedef double type;
-};
-
-// Segmented inclusive scan over lanes holding consecutive sorted particles;
-// the last lane of each run adds the run total into smem[key*Q + q].
-template <typename T, int Q>
-__device__ __forceinline__ void seg_reduce_to_smem(int key, T (&val)[Q], T* smem) {
-  const unsigned lane = threadIdx.x & 31u;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int k_up = __shfl_up_sync(0xFFFFFFFFu, key, o);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const T up = __shfl_up_sync(0xFFFFFFFFu, val[q], o);
-      if (lane >= static_cast<unsigned>(o) && k_up == key) val[q] += up;
-    }
-  }
-  const int k_dn = __shfl_down_sync(0xFFFFFFFFu, key, 1);
-  const bool tail = (lane == 31u) || (k_dn != key);
-  if (tail && key >= 0) {
-    typedef typename AtomT<T>::type AT;
-#pragma unroll
-    for (int q = 0; q < Q; ++q)
-      atomicAdd(reinterpret_cast<AT*>(smem + key * Q + q), static_cast<AT>(val[q]));
-  }
 }
 
 // A particle of a collide tile in the collision frame.
@@ -611,30 +626,6 @@ __device__ __forceinline__ void load_particle(Particle<R>& P, uint32_t p, uint32
   finish_particle(P, p, C);
 }
 
-template <typename R>
-__device__ __forceinline__ void momentum_terms(const Particle<R>& P,
-                                               typename AccT<R>::type (&val)[4]) {
-  typedef typename AccT<R>::type A;
-  if (P.lc >= 0) {
-    val[0] = to_acc<R>(P.v.x * P.m);
-    val[1] = to_acc<R>(P.v.y * P.m);
-    val[2] = to_acc<R>(P.v.z * P.m);
-    val[3] = to_acc<R>(P.m);
-  } else {
-    val[0] = val[1] = val[2] = val[3] = A(0);
-  }
-}
-
-template <typename R>
-__device__ __forceinline__ typename AccT<R>::type energy_term(const Particle<R>& P,
-                                                              const R* s_cmv) {
-  typedef typename AccT<R>::type A;
-  if (P.lc < 0) return A(0);
-  const R d0 = P.v.x - s_cmv[3 * P.lc], d1 = P.v.y - s_cmv[3 * P.lc + 1],
-          d2 = P.v.z - s_cmv[3 * P.lc + 2];
-  return to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2));
-}
-
 // Thermostat + rotation of one particle, then the unshift/wrap and store.
 template <typename R>
 __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, const R* s_cmv,
@@ -696,16 +687,40 @@ constexpr size_t collide_dyn_smem(int cap) {
   return static_cast<size_t>(cap) * (2 * sizeof(R4<R>) + sizeof(short));
 }
 
+// Staged particle j of the tile (shared memory), or, past the staging
+// capacity, reconstructed from global memory.
+template <typename R, int CAP>
+__device__ __forceinline__ void tile_particle(Particle<R>& P, int j, int nloc, uint32_t p0,
+                                              uint32_t p1, const R4<R>* s_x, const R4<R>* s_v,
+                                              const short* s_lc, const CollideCtx<R>& C) {
+  if (j < nloc) {
+    P.x = s_x[j];
+    P.v = s_v[j];
+    P.m = P.v.w;
+    P.lc = s_lc[j];
+    P.src = unpack_src(P.x.w);  // solvent id (no MONO_BIT) or MONO_BIT | monomer
+  } else {
+    load_particle(P, p0 + j, p1, C);
+  }
+}
+
+// Mass in 2^16 fixed point (exact for masses on a 2^-16 grid, order-free).
+__device__ __forceinline__ int mass_fix(float m) { return __float2int_rn(m * 65536.0f); }
+
 // One CTA per tile of <= CT cells of one replica.
 //  stage  : gather the tile's particles (perm -> 32-byte records, GU loads in
 //           flight per thread), recompute their collision-frame state, keep
 //           them in shared memory;
-//  reduce : per-cell momentum and mass, then kinetic energy about the cell
-//           velocity, by warp-shuffle segmented scans + shared atomics;
-//  draw   : one thread per cell: MBS scale factor and rotation matrix;
+//  cells  : one thread per cell walks its particles twice -- momentum and
+//           mass (MPC::calculateCMV, MPC.cpp:314-322), then kinetic energy
+//           about the cell velocity (MPC.cpp:277-280) -- with int64 fixed-point
+//           sums on the fast path (exact, independent of particle order) and
+//           the reference's sequential FP64 sums on the parity path; then
+//           draws the MBS factor (MPC.cpp:287-289) and the rotation
+//           (MPC.cpp:244-257);
 //  apply  : rotate/scale, undo the shift, write the tile back in cell order.
-// A tile holding more than CAP particles processes the excess straight from
-// global memory in every phase (correct, slower).
+// A tile holding more than CAP particles reads the excess straight from
+// global memory (correct, slower).
 template <typename R, int NT, int CT, int CAP>
 __global__ void __launch_bounds__(NT) k_collide(
     const Tile* tiles, const RepInfo* reps, const RepDyn* dyn, const uint32_t* __restrict__ off,
@@ -713,10 +728,8 @@ __global__ void __launch_bounds__(NT) k_collide(
     const R* mpos, R* mvel, const uint2* mkey, const int* mimg, const double* inj_gamma,
     const double* inj_uphi, const double* inj_utheta, int rng, double rot_c, double rot_s,
     int strict, int mono_bin, ErrorState* err) {
-  typedef typename AccT<R>::type A;
   constexpr int GU = 4;
-  __shared__ A s_acc[CT * 4];
-  __shared__ A s_e[CT];
+  constexpr bool kFP64 = std::is_same<R, double>::value;
   __shared__ R s_cmv[CT * 3];
   __shared__ R s_rot[CT * 9];
   __shared__ R s_scale[CT];
@@ -744,10 +757,10 @@ __global__ void __launch_bounds__(NT) k_collide(
   const int nc = t.end - t.begin;
   C.nc = nc;
   C.err = err;
+  const R rc = static_cast<R>(rot_c), rs = static_cast<R>(rot_s);
+  const R kT = static_cast<R>(ri.kT);
 
   for (int i = threadIdx.x; i <= nc; i += NT) s_off[i] = off[t.begin + i];
-  for (int i = threadIdx.x; i < nc * 4; i += NT) s_acc[i] = A(0);
-  for (int i = threadIdx.x; i < nc; i += NT) s_e[i] = A(0);
   __syncthreads();
   const uint32_t p0 = s_off[0], p1 = s_off[nc];
   const int n = static_cast<int>(p1 - p0);
@@ -784,97 +797,75 @@ __global__ void __launch_bounds__(NT) k_collide(
   }
   __syncthreads();
 
-  // reduce: momentum and mass (MPC::calculateCMV, MPC.cpp:314-322)
-  for (int base = 0; base < nloc; base += NT) {
-    const int j = base + threadIdx.x;
-    Particle<R> P;
-    P.lc = -1;
-    if (j < nloc) {
-      P.v = s_v[j];
-      P.m = P.v.w;
-      P.lc = s_lc[j];
-    }
-    A val[4];
-    momentum_terms(P, val);
-    seg_reduce_to_smem<A, 4>(P.lc, val, s_acc);
-  }
-  for (int base = CAP; base < n; base += NT) {
-    Particle<R> P;
-    load_particle(P, p0 + base + threadIdx.x, p1, C);
-    A val[4];
-    momentum_terms(P, val);
-    seg_reduce_to_smem<A, 4>(P.lc, val, s_acc);
-  }
-  __syncthreads();
+  // cells: reductions and draws, one thread per cell
   for (int lc = threadIdx.x; lc < nc; lc += NT) {
+    const int j0 = static_cast<int>(s_off[lc] - p0), j1 = static_cast<int>(s_off[lc + 1] - p0);
     R cm[3];
-    if (std::is_same<R, double>::value) {
-      const R mt = static_cast<R>(s_acc[4 * lc + 3]);
-      for (int d = 0; d < 3; ++d) {
-        cm[d] = static_cast<R>(s_acc[4 * lc + d]);
-        if (mt > R(0)) cm[d] /= mt;
+    R ekin = R(0);
+    if (kFP64) {
+      R px = R(0), py = R(0), pz = R(0), mt = R(0);
+      for (int j = j0; j < j1; ++j) {
+        Particle<R> P;
+        tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
+        if (P.lc < 0) continue;
+        px += P.v.x * P.m;
+        py += P.v.y * P.m;
+        pz += P.v.z * P.m;
+        mt += P.m;
       }
+      cm[0] = px; cm[1] = py; cm[2] = pz;
+      if (mt > R(0)) {
+        cm[0] /= mt; cm[1] /= mt; cm[2] /= mt;
+      }
+      for (int j = j0; j < j1; ++j) {
+        Particle<R> P;
+        tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
+        if (P.lc < 0) continue;
+        const R d0 = P.v.x - cm[0], d1 = P.v.y - cm[1], d2 = P.v.z - cm[2];
+        ekin += P.m * ((d0 * d0 + d1 * d1) + d2 * d2);
+      }
+      ekin *= R(0.5);
     } else {
-      const float mt = acc_to_float(s_acc[4 * lc + 3]);
-      for (int d = 0; d < 3; ++d) {
-        const float pd = acc_to_float(s_acc[4 * lc + d]);
-        cm[d] = mt > 0.f ? static_cast<R>(pd / mt) : R(0);
+      long long px = 0, py = 0, pz = 0, e = 0;
+      int mq = 0;
+      for (int j = j0; j < j1; ++j) {
+        Particle<R> P;
+        tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
+        if (P.lc < 0) continue;
+        px += to_acc<R>(P.v.x * P.m);
+        py += to_acc<R>(P.v.y * P.m);
+        pz += to_acc<R>(P.v.z * P.m);
+        mq += mass_fix(static_cast<float>(P.m));
       }
+      const float mt = static_cast<float>(mq) * (1.0f / 65536.0f);
+      cm[0] = mt > 0.f ? acc_to_float(px) / mt : 0.f;
+      cm[1] = mt > 0.f ? acc_to_float(py) / mt : 0.f;
+      cm[2] = mt > 0.f ? acc_to_float(pz) / mt : 0.f;
+      for (int j = j0; j < j1; ++j) {
+        Particle<R> P;
+        tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
+        if (P.lc < 0) continue;
+        const R d0 = P.v.x - cm[0], d1 = P.v.y - cm[1], d2 = P.v.z - cm[2];
+        e += to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2));
+      }
+      ekin = acc_to_float(e) * 0.5f;
     }
-    s_cmv[3 * lc] = cm[0];
-    s_cmv[3 * lc + 1] = cm[1];
-    s_cmv[3 * lc + 2] = cm[2];
-  }
-  __syncthreads();
-
-  // reduce: kinetic energy about the cell velocity (MPC.cpp:277-280)
-  for (int base = 0; base < nloc; base += NT) {
-    const int j = base + threadIdx.x;
-    Particle<R> P;
-    P.lc = -1;
-    if (j < nloc) {
-      P.v = s_v[j];
-      P.m = P.v.w;
-      P.lc = s_lc[j];
-    }
-    A val[1] = {energy_term(P, s_cmv)};
-    seg_reduce_to_smem<A, 1>(P.lc, val, s_e);
-  }
-  for (int base = CAP; base < n; base += NT) {
-    Particle<R> P;
-    load_particle(P, p0 + base + threadIdx.x, p1, C);
-    A val[1] = {energy_term(P, s_cmv)};
-    seg_reduce_to_smem<A, 1>(P.lc, val, s_e);
-  }
-  __syncthreads();
-
-  // draw: MBS scaling (MPC.cpp:287-289) and rotation (MPC.cpp:244-257)
-  for (int lc = threadIdx.x; lc < nc; lc += NT) {
     const uint32_t cg = C.c0 + lc;
     const uint32_t cl = cg - C.cbase;
-    const uint32_t nn = s_off[lc + 1] - s_off[lc];
+    const uint32_t nn = static_cast<uint32_t>(j1 - j0);
     R scale = R(-1);
     if (nn >= 2u) {
-      R ekin;
-      if (std::is_same<R, double>::value) {
-        ekin = static_cast<R>(s_e[lc]);
-        ekin *= R(0.5);
-      } else {
-        ekin = static_cast<R>(acc_to_float(s_e[lc]) * 0.5f);
-      }
       R gv;
       if (rng == RNG_INJECT) {
         gv = static_cast<R>(inj_gamma[cg]);
       } else {
         bool ok = true;
         gv = philox_gamma<R>(ri.seed, cl, C.dn.step,
-                             static_cast<R>(1.5) * static_cast<R>(nn - 1u), &ok) *
-             static_cast<R>(ri.kT);
+                             static_cast<R>(1.5) * static_cast<R>(nn - 1u), &ok) * kT;
         if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
       }
       scale = (ekin > R(0)) ? r_sqrt(gv / ekin) : R(1);
     }
-    s_scale[lc] = scale;
     R uphi, uth;
     if (rng == RNG_INJECT) {
       uphi = static_cast<R>(inj_uphi[cg]);
@@ -891,28 +882,33 @@ __global__ void __launch_bounds__(NT) k_collide(
     R sphi, cphi;
     r_sincos(phi, &sphi, &cphi);
     const R a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
-    const R c = static_cast<R>(rot_c), s = static_cast<R>(rot_s);
-    R* M = s_rot + 9 * lc;
-    M[0] = a0 * a0 + (R(1) - a0 * a0) * c;
-    M[1] = a0 * a1 * (R(1) - c) - a2 * s;
-    M[2] = a0 * a2 * (R(1) - c) + a1 * s;
-    M[3] = a0 * a1 * (R(1) - c) + a2 * s;
-    M[4] = a1 * a1 + (R(1) - a1 * a1) * c;
-    M[5] = a1 * a2 * (R(1) - c) - a0 * s;
-    M[6] = a0 * a2 * (R(1) - c) - a1 * s;
-    M[7] = a1 * a2 * (R(1) - c) + a0 * s;
-    M[8] = a2 * a2 + (R(1) - a2 * a2) * c;
+    R M[9];
+    M[0] = a0 * a0 + (R(1) - a0 * a0) * rc;
+    M[1] = a0 * a1 * (R(1) - rc) - a2 * rs;
+    M[2] = a0 * a2 * (R(1) - rc) + a1 * rs;
+    M[3] = a0 * a1 * (R(1) - rc) + a2 * rs;
+    M[4] = a1 * a1 + (R(1) - a1 * a1) * rc;
+    M[5] = a1 * a2 * (R(1) - rc) - a0 * rs;
+    M[6] = a0 * a2 * (R(1) - rc) - a1 * rs;
+    M[7] = a1 * a2 * (R(1) - rc) + a0 * rs;
+    M[8] = a2 * a2 + (R(1) - a2 * a2) * rc;
+    if (!kFP64 && scale >= R(0)) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) M[q] *= scale;  // fast path: s R in one matrix
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) s_rot[9 * lc + q] = M[q];
+    s_cmv[3 * lc] = cm[0];
+    s_cmv[3 * lc + 1] = cm[1];
+    s_cmv[3 * lc + 2] = cm[2];
+    s_scale[lc] = kFP64 ? scale : R(-1);
   }
   __syncthreads();
 
   // apply
   for (int j = threadIdx.x; j < nloc; j += NT) {
     Particle<R> P;
-    P.x = s_x[j];
-    P.v = s_v[j];
-    P.m = P.v.w;
-    P.lc = s_lc[j];
-    P.src = unpack_src(P.x.w);  // solvent id (no MONO_BIT) or MONO_BIT | monomer
+    tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
     apply_collision(P, p0 + j, s_cmv, s_rot, s_scale, C, st_out, err);
   }
   for (int base = CAP; base < n; base += NT) {
