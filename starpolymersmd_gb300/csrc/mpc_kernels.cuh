@@ -210,6 +210,16 @@ __device__ __forceinline__ uint32_t cell_of(const Geo<R>& g, R x, R y, R z, bool
   return static_cast<uint32_t>(ix + g.Li[0] * (iy + g.Li[1] * iz));
 }
 
+// FP32 fast path (never strict): floor by directed-rounding add, clamped.
+__device__ __forceinline__ uint32_t cell_of(const Geo<float>& g, float x, float y, float z,
+                                            bool strict) {
+  if (strict) return cell_of<float>(g, x, y, z, true);
+  const int ix = min(f2i_floor_nonneg(fmaxf(r_add(x, g.half[0]), 0.0f)), g.Li[0] - 1);
+  const int iy = min(f2i_floor_nonneg(fmaxf(r_add(y, g.half[1]), 0.0f)), g.Li[1] - 1);
+  const int iz = min(f2i_floor_nonneg(fmaxf(r_add(z, g.half[2]), 0.0f)), g.Li[2] - 1);
+  return static_cast<uint32_t>(ix + g.Li[0] * (iy + g.Li[1] * iz));
+}
+
 __device__ __forceinline__ void raise_error(ErrorState* e, uint32_t bit, uint32_t a, uint32_t b) {
   const uint32_t old = atomicOr(&e->word, bit);
   if ((old & bit) == 0) {
@@ -524,31 +534,17 @@ struct AccT<float> {
   typedef long long type;  // 2^32 fixed point: exact, order-independent sums
 };
 
-constexpr float kFixScale = 4294967296.0f;  // 2^32
-constexpr float kFixInv = 2.3283064365386963e-10f;  // 2^-32
 
 template <typename R>
 __device__ __forceinline__ typename AccT<R>::type to_acc(R v);
 template <>
 __device__ __forceinline__ double to_acc<double>(double v) { return v; }
-// v * 2^32 rounded to an integer, built from two 32-bit conversions (the
-// 64-bit float<->int conversions run on the FP64 pipe, which is narrow on
-// GB300): hi = trunc(v * 2^16) is exact, the remainder v * 2^16 - hi is exact
-// in FP32, and its rounding at 2^-16 gives the low bits. Valid for |v| < 2^15.
 template <>
 __device__ __forceinline__ long long to_acc<float>(float v) {
-  const float a = v * 65536.0f;
-  const int hi = __float2int_rz(a);
-  const int lo = __float2int_rn((a - static_cast<float>(hi)) * 65536.0f);
-  return static_cast<long long>(hi) * 65536ll + lo;
+  return f2fix32(v);
 }
 
-// int64 2^32 fixed point back to float (two 32-bit conversions).
-__device__ __forceinline__ float acc_to_float(long long a) {
-  const int hi = static_cast<int>(a >> 32);
-  const unsigned lo = static_cast<unsigned>(a & 0xFFFFFFFFll);
-  return static_cast<float>(hi) + static_cast<float>(lo) * kFixInv;
-}
+__device__ __forceinline__ float acc_to_float(long long a) { return fix32_to_f(a); }
 
 // A particle of a collide tile in the collision frame.
 template <typename R>
@@ -704,8 +700,6 @@ __device__ __forceinline__ void tile_particle(Particle<R>& P, int j, int nloc, u
   }
 }
 
-// Mass in 2^16 fixed point (exact for masses on a 2^-16 grid, order-free).
-__device__ __forceinline__ int mass_fix(float m) { return __float2int_rn(m * 65536.0f); }
 
 // One CTA per tile of <= CT cells of one replica.
 //  stage  : gather the tile's particles (perm -> 32-byte records, GU loads in
@@ -797,14 +791,21 @@ __global__ void __launch_bounds__(NT) k_collide(
   }
   __syncthreads();
 
-  // cells: reductions and draws, one thread per cell
-  for (int lc = threadIdx.x; lc < nc; lc += NT) {
-    const int j0 = static_cast<int>(s_off[lc] - p0), j1 = static_cast<int>(s_off[lc + 1] - p0);
+  // cells: two lanes per cell (NT == 2 CT) each walk half of its particles;
+  // partial sums meet through one shuffle. Then lane 0 of the pair draws the
+  // gamma variate while lane 1 builds the rotation.
+  static_assert(NT == 2 * CT, "two threads per cell");
+  {
+    const int lc = threadIdx.x >> 1;
+    const int half = threadIdx.x & 1;
+    const bool live = lc < nc;
+    const int j0 = live ? static_cast<int>(s_off[lc] - p0) : 0;
+    const int j1 = live ? static_cast<int>(s_off[lc + 1] - p0) : 0;
     R cm[3];
     R ekin = R(0);
     if (kFP64) {
       R px = R(0), py = R(0), pz = R(0), mt = R(0);
-      for (int j = j0; j < j1; ++j) {
+      for (int j = j0 + half; j < j1; j += 2) {
         Particle<R> P;
         tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
         if (P.lc < 0) continue;
@@ -813,95 +814,121 @@ __global__ void __launch_bounds__(NT) k_collide(
         pz += P.v.z * P.m;
         mt += P.m;
       }
+      px += __shfl_xor_sync(0xFFFFFFFFu, px, 1);
+      py += __shfl_xor_sync(0xFFFFFFFFu, py, 1);
+      pz += __shfl_xor_sync(0xFFFFFFFFu, pz, 1);
+      mt += __shfl_xor_sync(0xFFFFFFFFu, mt, 1);
       cm[0] = px; cm[1] = py; cm[2] = pz;
       if (mt > R(0)) {
         cm[0] /= mt; cm[1] /= mt; cm[2] /= mt;
       }
-      for (int j = j0; j < j1; ++j) {
+      for (int j = j0 + half; j < j1; j += 2) {
         Particle<R> P;
         tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
         if (P.lc < 0) continue;
         const R d0 = P.v.x - cm[0], d1 = P.v.y - cm[1], d2 = P.v.z - cm[2];
         ekin += P.m * ((d0 * d0 + d1 * d1) + d2 * d2);
       }
+      ekin += __shfl_xor_sync(0xFFFFFFFFu, ekin, 1);
       ekin *= R(0.5);
     } else {
+      // int64 2^32 fixed point: exact and independent of particle order.
+      // Mass: solvent count times the solvent mass plus the monomers' masses.
       long long px = 0, py = 0, pz = 0, e = 0;
-      int mq = 0;
-      for (int j = j0; j < j1; ++j) {
+      int nsol = 0;
+      float mmono = 0.0f;
+      for (int j = j0 + half; j < j1; j += 2) {
         Particle<R> P;
         tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
         if (P.lc < 0) continue;
         px += to_acc<R>(P.v.x * P.m);
         py += to_acc<R>(P.v.y * P.m);
         pz += to_acc<R>(P.v.z * P.m);
-        mq += mass_fix(static_cast<float>(P.m));
+        if (P.src & MONO_BIT) {
+          mmono += static_cast<float>(P.m);
+        } else {
+          ++nsol;
+        }
       }
-      const float mt = static_cast<float>(mq) * (1.0f / 65536.0f);
-      cm[0] = mt > 0.f ? acc_to_float(px) / mt : 0.f;
-      cm[1] = mt > 0.f ? acc_to_float(py) / mt : 0.f;
-      cm[2] = mt > 0.f ? acc_to_float(pz) / mt : 0.f;
-      for (int j = j0; j < j1; ++j) {
+      px += __shfl_xor_sync(0xFFFFFFFFu, px, 1);
+      py += __shfl_xor_sync(0xFFFFFFFFu, py, 1);
+      pz += __shfl_xor_sync(0xFFFFFFFFu, pz, 1);
+      nsol += __shfl_xor_sync(0xFFFFFFFFu, nsol, 1);
+      mmono += __shfl_xor_sync(0xFFFFFFFFu, mmono, 1);
+      const float mt = fmaf(i2f_small(nsol), static_cast<float>(C.solvent_mass), mmono);
+      const float inv = mt > 0.f ? 1.0f / mt : 0.0f;
+      cm[0] = acc_to_float(px) * inv;
+      cm[1] = acc_to_float(py) * inv;
+      cm[2] = acc_to_float(pz) * inv;
+      for (int j = j0 + half; j < j1; j += 2) {
         Particle<R> P;
         tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
         if (P.lc < 0) continue;
         const R d0 = P.v.x - cm[0], d1 = P.v.y - cm[1], d2 = P.v.z - cm[2];
         e += to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2));
       }
+      e += __shfl_xor_sync(0xFFFFFFFFu, e, 1);
       ekin = acc_to_float(e) * 0.5f;
     }
     const uint32_t cg = C.c0 + lc;
     const uint32_t cl = cg - C.cbase;
     const uint32_t nn = static_cast<uint32_t>(j1 - j0);
     R scale = R(-1);
-    if (nn >= 2u) {
-      R gv;
-      if (rng == RNG_INJECT) {
-        gv = static_cast<R>(inj_gamma[cg]);
-      } else {
-        bool ok = true;
-        gv = philox_gamma<R>(ri.seed, cl, C.dn.step,
-                             static_cast<R>(1.5) * static_cast<R>(nn - 1u), &ok) * kT;
-        if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
-      }
-      scale = (ekin > R(0)) ? r_sqrt(gv / ekin) : R(1);
-    }
-    R uphi, uth;
-    if (rng == RNG_INJECT) {
-      uphi = static_cast<R>(inj_uphi[cg]);
-      uth = static_cast<R>(inj_utheta[cg]);
-    } else {
-      const Uniform2<R> u = philox_uniforms<R>(ri.seed, cl, C.dn.step, 0u);
-      uphi = u.a;
-      uth = u.b;
-    }
-    const R two_pi = R(6.283185307179586476925286766559);
-    const R phi = two_pi * uphi;
-    const R theta = R(2) * (uth - R(0.5));
-    const R stt = r_sqrt(R(1) - theta * theta);
-    R sphi, cphi;
-    r_sincos(phi, &sphi, &cphi);
-    const R a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
     R M[9];
-    M[0] = a0 * a0 + (R(1) - a0 * a0) * rc;
-    M[1] = a0 * a1 * (R(1) - rc) - a2 * rs;
-    M[2] = a0 * a2 * (R(1) - rc) + a1 * rs;
-    M[3] = a0 * a1 * (R(1) - rc) + a2 * rs;
-    M[4] = a1 * a1 + (R(1) - a1 * a1) * rc;
-    M[5] = a1 * a2 * (R(1) - rc) - a0 * rs;
-    M[6] = a0 * a2 * (R(1) - rc) - a1 * rs;
-    M[7] = a1 * a2 * (R(1) - rc) + a0 * rs;
-    M[8] = a2 * a2 + (R(1) - a2 * a2) * rc;
-    if (!kFP64 && scale >= R(0)) {
-#pragma unroll
-      for (int q = 0; q < 9; ++q) M[q] *= scale;  // fast path: s R in one matrix
+    if (half == 0) {
+      if (live && nn >= 2u) {
+        R gv;
+        if (rng == RNG_INJECT) {
+          gv = static_cast<R>(inj_gamma[cg]);
+        } else {
+          bool ok = true;
+          const R shape = kFP64 ? static_cast<R>(1.5) * static_cast<R>(nn - 1u)
+                                : static_cast<R>(1.5f * i2f_small(static_cast<int>(nn - 1u)));
+          gv = philox_gamma<R>(ri.seed, cl, C.dn.step, shape, &ok) * kT;
+          if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
+        }
+        scale = (ekin > R(0)) ? r_sqrt(gv / ekin) : R(1);
+      }
+    } else if (live) {
+      R uphi, uth;
+      if (rng == RNG_INJECT) {
+        uphi = static_cast<R>(inj_uphi[cg]);
+        uth = static_cast<R>(inj_utheta[cg]);
+      } else {
+        const Uniform2<R> u = philox_uniforms<R>(ri.seed, cl, C.dn.step, 0u);
+        uphi = u.a;
+        uth = u.b;
+      }
+      const R two_pi = R(6.283185307179586476925286766559);
+      const R phi = two_pi * uphi;
+      const R theta = R(2) * (uth - R(0.5));
+      const R stt = r_sqrt(R(1) - theta * theta);
+      R sphi, cphi;
+      r_sincos(phi, &sphi, &cphi);
+      const R a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
+      M[0] = a0 * a0 + (R(1) - a0 * a0) * rc;
+      M[1] = a0 * a1 * (R(1) - rc) - a2 * rs;
+      M[2] = a0 * a2 * (R(1) - rc) + a1 * rs;
+      M[3] = a0 * a1 * (R(1) - rc) + a2 * rs;
+      M[4] = a1 * a1 + (R(1) - a1 * a1) * rc;
+      M[5] = a1 * a2 * (R(1) - rc) - a0 * rs;
+      M[6] = a0 * a2 * (R(1) - rc) - a1 * rs;
+      M[7] = a1 * a2 * (R(1) - rc) + a0 * rs;
+      M[8] = a2 * a2 + (R(1) - a2 * a2) * rc;
     }
+    scale = __shfl_xor_sync(0xFFFFFFFFu, scale, 1);  // lane 1 gets lane 0's factor
+    if (half == 1 && live) {
+      if (!kFP64 && scale >= R(0)) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) s_rot[9 * lc + q] = M[q];
-    s_cmv[3 * lc] = cm[0];
-    s_cmv[3 * lc + 1] = cm[1];
-    s_cmv[3 * lc + 2] = cm[2];
-    s_scale[lc] = kFP64 ? scale : R(-1);
+        for (int q = 0; q < 9; ++q) M[q] *= scale;  // fast path: s R in one matrix
+      }
+#pragma unroll
+      for (int q = 0; q < 9; ++q) s_rot[9 * lc + q] = M[q];
+      s_cmv[3 * lc] = cm[0];
+      s_cmv[3 * lc + 1] = cm[1];
+      s_cmv[3 * lc + 2] = cm[2];
+      s_scale[lc] = kFP64 ? scale : R(-1);
+    }
   }
   __syncthreads();
 

@@ -9,7 +9,7 @@
 //                                                          s = collision counter
 //   double uniforms  uA = U53(w0, w1), uB = U53(w2, w3),
 //                    U53(lo, hi) = ((hi:lo) >> 11) * 2^-53 + 2^-54  in (0, 1)
-//   float uniforms   uA = (w1 >> 8) * 2^-24 + 2^-25, uB from w3: the same top bits
+//   float uniforms   uA = (w1 >> 9) * 2^-23 + 2^-24, uB from w3: the same top bits
 //   block k = 0            -> (u_phi, u_theta) of the rotation axis
 //   blocks 1+2i, 2+2i      -> iteration i of the gamma sampler (normal, acceptance)
 //   cell c = 0xFFFFFFFF    -> grid shift: block 0 gives x, y; block 1 gives z
@@ -60,9 +60,8 @@ __device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
   return __dadd_rn(__dmul_rn(static_cast<double>(bits), 0x1.0p-53), 0x1.0p-54);
 }
 
-__device__ __forceinline__ float u24(uint32_t hi) {
-  return static_cast<float>(hi >> 8) * 0x1.0p-24f + 0x1.0p-25f;
-}
+// top 23 bits of the high word, built without a conversion instruction
+__device__ __forceinline__ float u24(uint32_t hi) { return u23_open(hi); }
 
 template <typename R>
 __device__ __forceinline__ Uniform2<R> philox_uniforms(unsigned long long seed, uint32_t cell,
