@@ -1,5 +1,6 @@
 // FP32 fast-path instantiation: float4 state, int64 fixed-point cell sums.
 #define SMPC_REAL float
+#define SMPC_FAST_F32 1
 #define SMPC_COLLIDE_NT 256
 #define SMPC_COLLIDE_CT 128
 #define SMPC_COLLIDE_CAP 1408

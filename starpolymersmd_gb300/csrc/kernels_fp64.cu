@@ -1,6 +1,7 @@
 // FP64 reference-parity instantiation. Built with -fmad=false so every
 // multiply and add rounds separately, in the reference's order.
 #define SMPC_REAL double
+#define SMPC_FAST_F32 0
 #define SMPC_COLLIDE_NT 128
 #define SMPC_COLLIDE_CT 64
 #define SMPC_COLLIDE_CAP 768

@@ -3,6 +3,7 @@
 #pragma once
 #include "launch.h"
 #include "md_kernels.cuh"
+#include "mpc_fast.cuh"
 #include "mpc_kernels.cuh"
 
 namespace smpc {
@@ -36,16 +37,24 @@ void launch_init_solvent<Real>(const RepInfo* reps, int rep, int slot_cap, Real*
 template <>
 void launch_mono_prep<Real>(const RepInfo* reps, RepDyn* dyn, int n_rep, Real* mpos, Real* mvel,
                             uint2* mkey, int* mimg, uint32_t* count, ErrorState* err,
-                            int mono_bin, int strict, cudaStream_t st) {
+                            int mono_bin, int strict, FrameF* frames, double rot_c, double rot_s,
+                            cudaStream_t st) {
   k_mono_prep<Real, 256><<<n_rep, 256, 0, st>>>(reps, dyn, mpos, mvel, mkey, mimg, count, err,
-                                                mono_bin, strict);
+                                                mono_bin, strict, frames, rot_c, rot_s);
 }
 
 template <>
 void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
-                            const RepDyn* dyn, const Real* rec, uint2* keys, uint32_t* count,
-                            ErrorState* err, int strict, cudaStream_t st) {
+                            const RepDyn* dyn, const FrameF* frames, const Real* rec, uint2* keys,
+                            uint32_t* count, ErrorState* err, int strict, cudaStream_t st) {
   if (n_tiles == 0) return;
+#if SMPC_FAST_F32
+  if (!strict) {
+    k_fluid_bin_f32<SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, frames, rec, keys,
+                                                                  count);
+    return;
+  }
+#endif
   k_fluid_bin<Real, SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, dyn, rec, keys,
                                                                   count, err, strict);
 }
@@ -53,9 +62,24 @@ void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
 template <>
 void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
   if (a.n_tiles == 0) return;
+#if SMPC_FAST_F32
+  if (!a.strict) {
+    auto kern = k_collide_f32<SMPC_COLLIDE_NT, SMPC_COLLIDE_CT, SMPC_COLLIDE_CAP>;
+    const size_t dyn = collide_f32_dyn_smem(SMPC_COLLIDE_CAP);
+    static bool configured = false;  // the attribute is per function, set once
+    if (!configured) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn));
+      configured = true;
+    }
+    kern<<<a.n_tiles, SMPC_COLLIDE_NT, dyn, st>>>(
+        a.tiles, a.reps, a.frames, a.dyn, a.off, a.perm, a.st_in, a.st_out, a.mpos, a.mvel, a.mimg,
+        a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.mono_bin, a.err);
+    return;
+  }
+#endif
   auto kern = k_collide<Real, SMPC_COLLIDE_NT, SMPC_COLLIDE_CT, SMPC_COLLIDE_CAP>;
   const size_t dyn = collide_dyn_smem<Real>(SMPC_COLLIDE_CAP);
-  static bool configured = false;  // the attribute is per function, set once
+  static bool configured = false;
   if (!configured) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn));
     configured = true;

@@ -13,6 +13,7 @@ struct MdArgs;
 
 template <typename R>
 struct CollideArgs {
+  const FrameF* frames;  // float frames (FP32 path)
   const Tile* tiles;
   int n_tiles;
   const RepInfo* reps;
@@ -54,11 +55,11 @@ void launch_init_solvent(const RepInfo* reps, int rep, int slot_cap, R* rec,
 template <typename R>
 void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* mvel, uint2* mkey,
                       int* mimg, uint32_t* count, ErrorState* err, int mono_bin, int strict,
-                      cudaStream_t st);
+                      FrameF* frames, double rot_c, double rot_s, cudaStream_t st);
 template <typename R>
 void launch_fluid_bin(const Tile* tiles, int n_tiles, const RepInfo* reps, const RepDyn* dyn,
-                      const R* rec, uint2* keys, uint32_t* count, ErrorState* err, int strict,
-                      cudaStream_t st);
+                      const FrameF* frames, const R* rec, uint2* keys, uint32_t* count,
+                      ErrorState* err, int strict, cudaStream_t st);
 template <typename R>
 void launch_collide(const CollideArgs<R>& a, cudaStream_t st);
 template <typename R>

@@ -1,0 +1,414 @@
+// FP32 fast-path collision kernels (the FP64 reference-parity path keeps the
+// operation-by-operation kernels of mpc_kernels.cuh).
+//
+// Same physics as MPC::step (star-polymers/lib/Hydrodynamics/MPC.cpp:116-142),
+// arranged for throughput on GB300:
+//  * all per-replica constants come from a float frame written once per
+//    collision (no double->float conversion in any thread: those issue on the
+//    FP64 pipe, 2 lanes/clock/SM on this part);
+//  * the reference's three Lees-Edwards wraps (after streaming, after the
+//    grid shift, after the unshift, MPC.cpp:192-197, 301-311) are composed
+//    exactly: with X = x + v h (unwrapped) the collision frame is the image
+//    c_s = img(X_y + s_y) of the shifted point, the final position is the
+//    image c_t = img(X_y) of the unshifted one, and the velocity picks up the
+//    same total jump -(c_t) shear Ly, -(c_s) of it before the collision;
+//  * k_collide takes every particle's cell from the counting sort itself
+//    (sorted position -> cell range), so it never recomputes cell indices;
+//  * float<->int work uses exact FP32-pipe constructions (precision.cuh).
+#pragma once
+#include <stdint.h>
+
+#include "mpc_kernels.cuh"
+
+namespace smpc {
+
+// image index of y (-1, 0, +1) for |y| < 1.5 L; general rounding beyond
+__device__ __forceinline__ float img_f(float y, float L, float half) {
+  if (fabsf(y) < 1.5f * L) return y >= half ? 1.0f : (y < -half ? -1.0f : 0.0f);
+  return rintf(__fdiv_rn(y, L));
+}
+
+// periodic wrap into [-L/2, L/2) for |x| < 2.5 L; general rounding beyond
+__device__ __forceinline__ float wrap_f(float x, float L, float half) {
+  if (!(fabsf(x) < 2.5f * L)) x = __fsub_rn(x, __fmul_rn(L, rintf(__fdiv_rn(x, L))));
+  x = x >= half ? __fsub_rn(x, L) : (x < -half ? __fadd_rn(x, L) : x);
+  return x >= half ? __fsub_rn(x, L) : (x < -half ? __fadd_rn(x, L) : x);
+}
+
+// Recentre (MPC::check_bounds, MPC.cpp:183-188, incl. its LE wrap) and
+// stream (MPC.cpp:194): X = x + v h, unwrapped. Explicitly rounded so the
+// bin and collide kernels produce identical X.
+__device__ __forceinline__ void stream_f(const FrameF& f, float4& x, float4& v) {
+  if (f.recentre) {
+    x.x = __fsub_rn(x.x, f.com[0]);
+    x.y = __fsub_rn(x.y, f.com[1]);
+    x.z = __fsub_rn(x.z, f.com[2]);
+    v.x = __fsub_rn(v.x, f.comv[0]);
+    v.y = __fsub_rn(v.y, f.comv[1]);
+    v.z = __fsub_rn(v.z, f.comv[2]);
+    if (f.shear_on) {
+      const float c0 = img_f(x.y, f.L[1], f.half[1]);
+      x.y = __fsub_rn(x.y, __fmul_rn(c0, f.L[1]));
+      x.x = __fsub_rn(x.x, __fmul_rn(c0, f.delrx));
+      v.x = __fsub_rn(v.x, __fmul_rn(c0, f.shearLy));
+    }
+  }
+  x.x = __fadd_rn(x.x, __fmul_rn(v.x, f.h));
+  x.y = __fadd_rn(x.y, __fmul_rn(v.y, f.h));
+  x.z = __fadd_rn(x.z, __fmul_rn(v.z, f.h));
+}
+
+// Shifted collision-frame position and its y image index.
+__device__ __forceinline__ float shifted_f(const FrameF& f, const float4& X, float& xs, float& ys,
+                                           float& zs) {
+  ys = __fadd_rn(X.y, f.shift[1]);
+  const float cs = f.shear_on ? img_f(ys, f.L[1], f.half[1]) : 0.0f;
+  if (f.shear_on) {
+    ys = __fsub_rn(ys, __fmul_rn(cs, f.L[1]));
+    xs = wrap_f(__fsub_rn(__fadd_rn(X.x, f.shift[0]), __fmul_rn(cs, f.delrx)), f.L[0], f.half[0]);
+  } else {
+    ys = wrap_f(ys, f.L[1], f.half[1]);
+    xs = wrap_f(__fadd_rn(X.x, f.shift[0]), f.L[0], f.half[0]);
+  }
+  zs = wrap_f(__fadd_rn(X.z, f.shift[2]), f.L[2], f.half[2]);
+  return cs;
+}
+
+__device__ __forceinline__ uint32_t cell_f(const FrameF& f, float x, float y, float z) {
+  const int ix = min(f2i_floor_nonneg(fmaxf(__fadd_rn(x, f.half[0]), 0.0f)), f.Li[0] - 1);
+  const int iy = min(f2i_floor_nonneg(fmaxf(__fadd_rn(y, f.half[1]), 0.0f)), f.Li[1] - 1);
+  const int iz = min(f2i_floor_nonneg(fmaxf(__fadd_rn(z, f.half[2]), 0.0f)), f.Li[2] - 1);
+  return static_cast<uint32_t>(ix + f.Li[0] * (iy + f.Li[1] * iz));
+}
+
+__device__ __forceinline__ float4 ld_f4(const float* p, size_t i) {
+  return __ldg(reinterpret_cast<const float4*>(p) + i);
+}
+__device__ __forceinline__ void st_f4(float* p, size_t i, float4 v) {
+  reinterpret_cast<float4*>(p)[i] = v;
+}
+
+// --------------------------------------------------------------- binning
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_fluid_bin_f32(const Tile* tiles, const RepInfo* reps,
+                                                      const FrameF* frames,
+                                                      const float* __restrict__ st,
+                                                      uint2* __restrict__ keys, uint32_t* count) {
+  constexpr int U = 4;
+  const Tile t = tiles[blockIdx.x];
+  const FrameF f = frames[t.rep];
+  const uint32_t cbase = static_cast<uint32_t>(reps[t.rep].cell_base);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  for (int base = t.begin; base < t.end; base += NT * U) {
+    float4 x[U], v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = base + u * NT + threadIdx.x;
+      if (i < t.end) {
+        x[u] = ld_f4(st, 2 * static_cast<size_t>(i));
+        v[u] = ld_f4(st, 2 * static_cast<size_t>(i) + 1);
+      }
+    }
+    uint32_t key[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = base + u * NT + threadIdx.x;
+      key[u] = KEY_NONE;
+      if (i < t.end && __float_as_uint(x[u].w) != SLOT_EMPTY) {
+        stream_f(f, x[u], v[u]);
+        float xs, ys, zs;
+        shifted_f(f, x[u], xs, ys, zs);
+        key[u] = cbase + cell_f(f, xs, ys, zs);
+      }
+    }
+    unsigned peers[U];
+    uint32_t rbase[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) peers[u] = __match_any_sync(0xFFFFFFFFu, key[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      rbase[u] = 0u;
+      if (lane == static_cast<unsigned>(__ffs(peers[u]) - 1) && key[u] != KEY_NONE)
+        rbase[u] = atomicAdd(count + key[u], __popc(peers[u]));
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, rbase[u], __ffs(peers[u]) - 1);
+      const int i = base + u * NT + threadIdx.x;
+      if (i < t.end) keys[i] = make_uint2(key[u], b0 + __popc(peers[u] & below));
+    }
+  }
+}
+
+// --------------------------------------------------------------- collide
+
+constexpr size_t collide_f32_dyn_smem(int cap) {
+  return static_cast<size_t>(cap) * (2 * sizeof(float4) + sizeof(short));
+}
+
+// A staged particle: sx = (X unwrapped streamed position, id or MONO_BIT|m),
+// sv = (velocity in the collision frame, mass).
+struct FastP {
+  float4 x;
+  float4 v;
+};
+
+__device__ __forceinline__ void fetch_f(FastP& P, uint32_t src, const float* st,
+                                        const float* mpos, const float* mvel, const int* mimg,
+                                        const FrameF& f, int wrap_mono) {
+  if (src & MONO_BIT) {
+    const uint32_t m = src & ~MONO_BIT;
+    P.v = reinterpret_cast<const float4*>(mvel)[m];
+    P.v.w = reinterpret_cast<const float4*>(mpos)[m].w;
+    if (wrap_mono == MONOBIN_WRAPPED)
+      P.v.x = __fsub_rn(P.v.x, __fmul_rn(i2f_small(mimg[m]), f.shearLy));
+    P.x = make_float4(0.f, 0.f, 0.f, __uint_as_float(src));
+  } else {
+    P.x = ld_f4(st, 2 * static_cast<size_t>(src));
+    P.v = ld_f4(st, 2 * static_cast<size_t>(src) + 1);
+  }
+}
+
+// Solvent: stream (the unwrapped X replaces the position, the id stays in
+// .w) and move the velocity into the shifted collision frame (image c_s).
+// Monomers keep what fetch_f loaded.
+__device__ __forceinline__ void frame_f(FastP& P, const FrameF& f, float solvent_mass) {
+  if (__float_as_uint(P.x.w) & MONO_BIT) return;
+  stream_f(f, P.x, P.v);
+  if (f.shear_on) {
+    const float cs = img_f(__fadd_rn(P.x.y, f.shift[1]), f.L[1], f.half[1]);
+    P.v.x = __fsub_rn(P.v.x, __fmul_rn(cs, f.shearLy));
+  }
+  P.v.w = solvent_mass;
+}
+
+template <int NT, int CT, int CAP>
+__global__ void __launch_bounds__(NT) k_collide_f32(
+    const Tile* tiles, const RepInfo* reps, const FrameF* frames, const RepDyn* dyn,
+    const uint32_t* __restrict__ off, const uint32_t* __restrict__ perm,
+    const float* __restrict__ st_in, float* __restrict__ st_out, const float* mpos, float* mvel,
+    const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
+    int rng, int mono_bin, ErrorState* err) {
+  constexpr int GU = 4;
+  static_assert(NT == 2 * CT, "two threads per cell");
+  __shared__ float s_cmv[CT * 3];
+  __shared__ float s_rot[CT * 9];
+  __shared__ uint32_t s_off[CT + 1];
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  float4* s_x = reinterpret_cast<float4*>(s_dyn);
+  float4* s_v = s_x + CAP;
+  short* s_lc = reinterpret_cast<short*>(s_v + CAP);
+
+  const Tile t = tiles[blockIdx.x];
+  const FrameF f = frames[t.rep];
+  const RepInfo& ri = reps[t.rep];
+  const unsigned long long seed = ri.seed;
+  const unsigned long long step = dyn[t.rep].step;
+  const uint32_t cbase = static_cast<uint32_t>(ri.cell_base);
+  const int nc = t.end - t.begin;
+
+  for (int i = threadIdx.x; i <= nc; i += NT) s_off[i] = off[t.begin + i];
+  __syncthreads();
+  const uint32_t p0 = s_off[0], p1 = s_off[nc];
+  const int n = static_cast<int>(p1 - p0);
+  const int nloc = n < CAP ? n : CAP;
+
+  // stage: gather, stream, collision-frame velocity
+  for (int base = 0; base < nloc; base += NT * GU) {
+    uint32_t src[GU];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      src[u] = j < nloc ? perm[p0 + j] : 0u;
+    }
+    FastP P[GU];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      if (j < nloc) fetch_f(P[u], src[u], st_in, mpos, mvel, mimg, f, mono_bin);
+    }
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      if (j < nloc) {
+        frame_f(P[u], f, f.solvent_mass);
+        s_x[j] = P[u].x;
+        s_v[j] = P[u].v;
+      }
+    }
+  }
+  __syncthreads();
+
+  // cells: two lanes per cell; int64 2^32 fixed-point sums (exact, order-free)
+  {
+    const int lc = threadIdx.x >> 1;
+    const int half = threadIdx.x & 1;
+    const bool live = lc < nc;
+    const int j0 = live ? static_cast<int>(s_off[lc] - p0) : 0;
+    const int j1 = live ? static_cast<int>(s_off[lc + 1] - p0) : 0;
+    long long px = 0, py = 0, pz = 0, e = 0;
+    int nsol = 0;
+    float mmono = 0.0f;
+    for (int j = j0 + half; j < j1; j += 2) {
+      float4 v, x;
+      if (j < nloc) {
+        v = s_v[j];
+        x = s_x[j];
+        s_lc[j] = static_cast<short>(lc);
+      } else {  // past the staging capacity: straight from global memory
+        FastP P;
+        fetch_f(P, perm[p0 + j], st_in, mpos, mvel, mimg, f, mono_bin);
+        frame_f(P, f, f.solvent_mass);
+        v = P.v;
+        x = P.x;
+      }
+      px += f2fix32(v.x * v.w);
+      py += f2fix32(v.y * v.w);
+      pz += f2fix32(v.z * v.w);
+      if (__float_as_uint(x.w) & MONO_BIT) {
+        mmono += v.w;
+      } else {
+        ++nsol;
+      }
+    }
+    px += __shfl_xor_sync(0xFFFFFFFFu, px, 1);
+    py += __shfl_xor_sync(0xFFFFFFFFu, py, 1);
+    pz += __shfl_xor_sync(0xFFFFFFFFu, pz, 1);
+    nsol += __shfl_xor_sync(0xFFFFFFFFu, nsol, 1);
+    mmono += __shfl_xor_sync(0xFFFFFFFFu, mmono, 1);
+    const float mt = fmaf(i2f_small(nsol), f.solvent_mass, mmono);
+    const float inv = mt > 0.f ? 1.0f / mt : 0.0f;
+    const float cm0 = fix32_to_f(px) * inv, cm1 = fix32_to_f(py) * inv,
+                cm2 = fix32_to_f(pz) * inv;
+    for (int j = j0 + half; j < j1; j += 2) {
+      float4 v;
+      if (j < nloc) {
+        v = s_v[j];
+      } else {
+        FastP P;
+        fetch_f(P, perm[p0 + j], st_in, mpos, mvel, mimg, f, mono_bin);
+        frame_f(P, f, f.solvent_mass);
+        v = P.v;
+      }
+      const float d0 = v.x - cm0, d1 = v.y - cm1, d2 = v.z - cm2;
+      e += f2fix32(v.w * (d0 * d0 + d1 * d1 + d2 * d2));
+    }
+    e += __shfl_xor_sync(0xFFFFFFFFu, e, 1);
+    const float ekin = fix32_to_f(e) * 0.5f;
+    const uint32_t cg = static_cast<uint32_t>(t.begin + lc);
+    const uint32_t cl = cg - cbase;
+    const uint32_t nn = static_cast<uint32_t>(j1 - j0);
+    float scale = -1.0f;
+    float M[9];
+    if (half == 0) {
+      if (live && nn >= 2u) {
+        float gv;
+        if (rng == RNG_INJECT) {
+          gv = static_cast<float>(inj_gamma[cg]);
+        } else {
+          bool ok = true;
+          gv = philox_gamma<float>(seed, cl, step, 1.5f * i2f_small(static_cast<int>(nn - 1u)), &ok) *
+               f.kT;
+          if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
+        }
+        scale = ekin > 0.f ? sqrtf(gv / ekin) : 1.0f;
+      }
+    } else if (live) {
+      float uphi, uth;
+      if (rng == RNG_INJECT) {
+        uphi = static_cast<float>(inj_uphi[cg]);
+        uth = static_cast<float>(inj_utheta[cg]);
+      } else {
+        const Uniform2<float> u = philox_uniforms<float>(seed, cl, step, 0u);
+        uphi = u.a;
+        uth = u.b;
+      }
+      const float theta = 2.0f * (uth - 0.5f);
+      const float stt = sqrtf(1.0f - theta * theta);
+      float sphi, cphi;
+      sincosf(6.283185307179586f * uphi, &sphi, &cphi);
+      const float a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
+      const float c = f.rot_c, s = f.rot_s;
+      M[0] = a0 * a0 + (1.0f - a0 * a0) * c;
+      M[1] = a0 * a1 * (1.0f - c) - a2 * s;
+      M[2] = a0 * a2 * (1.0f - c) + a1 * s;
+      M[3] = a0 * a1 * (1.0f - c) + a2 * s;
+      M[4] = a1 * a1 + (1.0f - a1 * a1) * c;
+      M[5] = a1 * a2 * (1.0f - c) - a0 * s;
+      M[6] = a0 * a2 * (1.0f - c) - a1 * s;
+      M[7] = a1 * a2 * (1.0f - c) + a0 * s;
+      M[8] = a2 * a2 + (1.0f - a2 * a2) * c;
+    }
+    scale = __shfl_xor_sync(0xFFFFFFFFu, scale, 1);
+    if (half == 1 && live) {
+      const float sc = scale >= 0.0f ? scale : 1.0f;  // thermostat folded into R
+#pragma unroll
+      for (int q = 0; q < 9; ++q) s_rot[9 * lc + q] = M[q] * sc;
+      s_cmv[3 * lc] = cm0;
+      s_cmv[3 * lc + 1] = cm1;
+      s_cmv[3 * lc + 2] = cm2;
+    }
+  }
+  __syncthreads();
+
+  // apply: v' = cmv + sR (v - cmv), back to the primary box, write in cell order
+  for (int j = threadIdx.x; j < n; j += NT) {
+    float4 x, v;
+    int lc;
+    if (j < nloc) {
+      x = s_x[j];
+      v = s_v[j];
+      lc = s_lc[j];
+    } else {
+      FastP P;
+      fetch_f(P, perm[p0 + j], st_in, mpos, mvel, mimg, f, mono_bin);
+      frame_f(P, f, f.solvent_mass);
+      x = P.x;
+      v = P.v;
+      // cell of sorted position p0 + j: the range that contains it
+      lc = 0;
+      while (static_cast<int>(s_off[lc + 1] - p0) <= j) ++lc;
+    }
+    const float* cm = s_cmv + 3 * lc;
+    const float* M = s_rot + 9 * lc;
+    const float d0 = v.x - cm[0], d1 = v.y - cm[1], d2 = v.z - cm[2];
+    float vx = cm[0] + (M[0] * d0 + M[1] * d1 + M[2] * d2);
+    const float vy = cm[1] + (M[3] * d0 + M[4] * d1 + M[5] * d2);
+    const float vz = cm[2] + (M[6] * d0 + M[7] * d1 + M[8] * d2);
+    const uint32_t tag = __float_as_uint(x.w);
+    if (!(isfinite(vx) && isfinite(vy) && isfinite(vz))) raise_error(err, ERR_NONFINITE, p0 + j, tag);
+    const size_t p = static_cast<size_t>(p0) + j;
+    if (tag & MONO_BIT) {
+      const uint32_t m = tag & ~MONO_BIT;
+      if (mono_bin == MONOBIN_WRAPPED) vx = __fadd_rn(vx, __fmul_rn(i2f_small(mimg[m]), f.shearLy));
+      float4 mv = reinterpret_cast<float4*>(mvel)[m];
+      mv.x = vx;
+      mv.y = vy;
+      mv.z = vz;
+      reinterpret_cast<float4*>(mvel)[m] = mv;
+      st_f4(st_out, 2 * p, make_float4(0.f, 0.f, 0.f, __uint_as_float(SLOT_EMPTY)));
+      st_f4(st_out, 2 * p + 1, make_float4(0.f, 0.f, 0.f, 0.f));
+    } else {
+      // final image c_t of the streamed point; the velocity already carries -c_s
+      float ys = __fadd_rn(x.y, f.shift[1]);
+      const float cs = f.shear_on ? img_f(ys, f.L[1], f.half[1]) : 0.0f;
+      float X = x.x, Y = x.y, Z = x.z;
+      if (f.shear_on) {
+        const float ct = img_f(Y, f.L[1], f.half[1]);
+        Y = __fsub_rn(Y, __fmul_rn(ct, f.L[1]));
+        X = wrap_f(__fsub_rn(X, __fmul_rn(ct, f.delrx)), f.L[0], f.half[0]);
+        vx = __fsub_rn(vx, __fmul_rn(ct - cs, f.shearLy));
+      } else {
+        X = wrap_f(X, f.L[0], f.half[0]);
+        Y = wrap_f(Y, f.L[1], f.half[1]);
+      }
+      Z = wrap_f(Z, f.L[2], f.half[2]);
+      st_f4(st_out, 2 * p, make_float4(X, Y, Z, x.w));
+      st_f4(st_out, 2 * p + 1, make_float4(vx, vy, vz, 0.f));
+    }
+  }
+}
+
+}  // namespace smpc

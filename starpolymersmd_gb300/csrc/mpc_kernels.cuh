@@ -342,7 +342,8 @@ template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* dyn, R* mpos,
                                                   R* mvel, uint2* mkey, int* mimg,
                                                   uint32_t* count, ErrorState* err,
-                                                  int mono_bin, int strict) {
+                                                  int mono_bin, int strict, FrameF* frames,
+                                                  double rot_c, double rot_s) {
   const int r = blockIdx.x;
   const RepInfo ri = reps[r];
   __shared__ int s_out;
@@ -451,6 +452,29 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
       mkey[b + i] = make_uint2(key, rank);
       mimg[b + i] = img;
     }
+  }
+  if (frames != nullptr && threadIdx.x == 0) {
+    FrameF f;
+    for (int d = 0; d < 3; ++d) {
+      f.L[d] = static_cast<float>(ri.L[d]);
+      f.half[d] = 0.5f * static_cast<float>(ri.L[d]);
+      f.Li[d] = ri.L[d];
+      f.shift[d] = static_cast<float>(dn.shift[d]);
+      f.com[d] = static_cast<float>(dn.com[d]);
+      f.comv[d] = static_cast<float>(dn.comv[d]);
+    }
+    f.shear = static_cast<float>(ri.shear);
+    f.shearLy = static_cast<float>(ri.shear * ri.L[1]);
+    f.delrx = static_cast<float>(dn.delrx);
+    f.h = static_cast<float>(dn.h);
+    f.kT = static_cast<float>(ri.kT);
+    f.solvent_mass = static_cast<float>(ri.solvent_mass);
+    f.rot_c = static_cast<float>(rot_c);
+    f.rot_s = static_cast<float>(rot_s);
+    f.recentre = out;
+    f.shear_on = ri.shear != 0.0;
+    f.pad[0] = f.pad[1] = 0;
+    frames[r] = f;
   }
 }
 

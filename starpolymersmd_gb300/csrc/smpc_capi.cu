@@ -66,6 +66,7 @@ struct smpc_ctx {
 
   double* d_inj = nullptr;  // gamma | u_phi | u_theta, total_cells each
   ErrorState* d_err = nullptr;
+  smpc::FrameF* d_frames = nullptr;
   double rot_c = 0, rot_s = 0;
   int max_nb = 192;
   bool collided = false;
@@ -124,9 +125,11 @@ int launch_collision(smpc_ctx* ctx, int rng, int cur) {
   const R* rec_in = static_cast<const R*>(ctx->d_rec[cur]);
   smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
                             static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
-                            ctx->d_err, ctx->opt.mono_bin, strict, ctx->st);
-  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, rec_in,
-                            ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
+                            ctx->d_err, ctx->opt.mono_bin, strict, ctx->d_frames, ctx->rot_c,
+                            ctx->rot_s, ctx->st);
+  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
+                            ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
+                            ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
   smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
@@ -139,6 +142,7 @@ template <typename R>
 smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
   const int strict = ctx->opt.strict_cells;
   smpc::CollideArgs<R> a;
+  a.frames = ctx->d_frames;
   a.tiles = ctx->d_col_tiles;
   a.n_tiles = ctx->n_col_tiles;
   a.reps = ctx->d_reps;
@@ -200,10 +204,12 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
   cudaEventRecord(ev[1 + PH_BEGIN], ctx->st);
   smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
                             static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
-                            ctx->d_err, ctx->opt.mono_bin, strict, ctx->st);
+                            ctx->d_err, ctx->opt.mono_bin, strict, ctx->d_frames, ctx->rot_c,
+                            ctx->rot_s, ctx->st);
   cudaEventRecord(ev[1 + PH_MONO], ctx->st);
-  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn, rec_in,
-                            ctx->d_keys, ctx->d_count, ctx->d_err, strict, ctx->st);
+  smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
+                            ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
+                            ctx->st);
   cudaEventRecord(ev[1 + PH_BIN], ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
@@ -541,7 +547,7 @@ void free_all(smpc_ctx* ctx) {
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
                   ctx->d_mimg, ctx->d_bond_start, ctx->d_bonds, ctx->d_nlist, ctx->d_ncount,
-                  ctx->d_inj, ctx->d_err};
+                  ctx->d_inj, ctx->d_err, ctx->d_frames};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
@@ -641,7 +647,7 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
             dalloc(&ctx->d_col_tiles, col.size()) == cudaSuccess &&
             dalloc(&ctx->d_tmp_tiles, ctx->h_tmp_tiles.size()) == cudaSuccess &&
             dalloc(&ctx->d_tpart, ctx->h_tmp_tiles.size()) == cudaSuccess &&
-            dalloc(&ctx->d_err, 1) == cudaSuccess;
+            dalloc(&ctx->d_err, 1) == cudaSuccess && dalloc(&ctx->d_frames, n_rep) == cudaSuccess;
   if (!ok) return bail(SMPC_E_CUDA, "alloc");
   ok = cudaMemcpy(ctx->d_reps, ctx->reps.data(), n_rep * sizeof(RepInfo), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(ctx->d_dyn, ctx->dyn.data(), n_rep * sizeof(RepDyn), cudaMemcpyHostToDevice) == cudaSuccess &&

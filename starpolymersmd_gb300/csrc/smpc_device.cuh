@@ -80,6 +80,29 @@ struct RepDyn {
   int pad2;
 };
 
+// Single-precision constants of one replica for the current collision,
+// written once per collision by k_mono_prep (after recentring is known) so
+// the FP32 kernels' threads never convert from double.
+struct FrameF {
+  float L[3];
+  float half[3];
+  float shear;
+  float shearLy;        // shear * Ly: velocity jump across the y face
+  float delrx;
+  float shift[3];
+  float com[3];
+  float comv[3];
+  float h;
+  float kT;
+  float solvent_mass;
+  float rot_c;
+  float rot_s;
+  int Li[3];
+  int recentre;
+  int shear_on;
+  int pad[2];
+};
+
 // Work tiles: a contiguous range within one replica.
 struct Tile {
   int rep;
