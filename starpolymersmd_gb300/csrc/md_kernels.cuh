@@ -102,8 +102,22 @@ struct MdArgs {
   int n_steps;             // substeps in this launch; 0 = build lists + forces only
   int calc_epot;
   int force_rebuild;
+  int core_relative;       // fast path: displacements measured relative to the core's
   ErrorState* err;
 };
+
+// Cell key of a position on a grid of side rv: three 10-bit fields
+// (coordinates within +-512 cells of the origin) and a bucket hash.
+constexpr int MD_BUCKETS = 2048;
+__device__ __forceinline__ int md_cell_key(int cx, int cy, int cz) {
+  return ((cx + 512) & 1023) | (((cy + 512) & 1023) << 10) | (((cz + 512) & 1023) << 20);
+}
+__device__ __forceinline__ int md_bucket(int cx, int cy, int cz) {
+  return static_cast<int>((static_cast<unsigned>(cx) * 73856093u) ^
+                          (static_cast<unsigned>(cy) * 19349663u) ^
+                          (static_cast<unsigned>(cz) * 83492791u)) &
+         (MD_BUCKETS - 1);
+}
 
 template <typename R, int NT, int MPT>
 __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, R* mfrc,
@@ -111,6 +125,10 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
   constexpr int CAP = NT * MPT;
   __shared__ R sx[CAP], sy[CAP], sz[CAP];
   __shared__ unsigned char s_amphi[CAP];
+  __shared__ int s_head[MD_BUCKETS];
+  __shared__ int s_next[CAP];
+  __shared__ int s_ckey[CAP];
+  __shared__ R s_core_ref[3];
   __shared__ int s_rebuild;
   __shared__ double s_red[NT / 32];
   const int r = blockIdx.x;
@@ -143,7 +161,12 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
       sx[i] = p.x; sy[i] = p.y; sz[i] = p.z;
     }
   }
-  if (threadIdx.x == 0) s_rebuild = a.force_rebuild;
+  if (threadIdx.x == 0) {
+    s_rebuild = a.force_rebuild;
+    // the core's position at the last list build (its Verlet reference)
+    const R4<R> c = ld4_rw(mver, b);
+    s_core_ref[0] = c.x; s_core_ref[1] = c.y; s_core_ref[2] = c.z;
+  }
   __syncthreads();
   int rebuilds = 0;
   double epot = 0.0;
@@ -160,29 +183,72 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
             x[k][d] += v[k][d] * dt;
           }
           sx[i] = x[k][0]; sy[i] = x[k][1]; sz[i] = x[k][2];
-          const R d0 = x[k][0] - xv[k][0], d1 = x[k][1] - xv[k][1], d2 = x[k][2] - xv[k][2];
-          if (r_sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim) s_rebuild = 1;
+          if (!a.core_relative) {
+            // Box::check_VerletLists (Box.cpp:182-194)
+            const R d0 = x[k][0] - xv[k][0], d1 = x[k][1] - xv[k][1], d2 = x[k][2] - xv[k][2];
+            if (r_sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim) s_rebuild = 1;
+          }
+        }
+      }
+      if (a.core_relative) {
+        // Pair distances change by at most |dr_i - c| + |dr_j - c| for any
+        // common c; with c the core's displacement, a star carried by the
+        // flow does not trigger rebuilds.
+        __syncthreads();
+        const R c0 = sx[0] - s_core_ref[0], c1 = sy[0] - s_core_ref[1], c2 = sz[0] - s_core_ref[2];
+#pragma unroll
+        for (int k = 0; k < MPT; ++k) {
+          const int i = threadIdx.x + k * NT;
+          if (i < n) {
+            const R d0 = x[k][0] - xv[k][0] - c0, d1 = x[k][1] - xv[k][1] - c1,
+                    d2 = x[k][2] - xv[k][2] - c2;
+            if ((d0 * d0 + d1 * d1) + d2 * d2 > lim * lim) s_rebuild = 1;
+          }
         }
       }
     }
     __syncthreads();
     const int rebuild = s_rebuild;
     if (rebuild) {
-      // Verlet lists: every other bead within r_verlet (Box.cpp:146-179), all pairs
+      // Verlet lists: every other bead within r_verlet (Box.cpp:146-179), found
+      // through a hashed grid of side r_verlet in shared memory
       ++rebuilds;
+      const R inv_rv = R(1) / static_cast<R>(ri.r_verlet);
+      for (int q = threadIdx.x; q < MD_BUCKETS; q += NT) s_head[q] = -1;
+      __syncthreads();
+      int cx[MPT], cy[MPT], cz[MPT];
+#pragma unroll
+      for (int k = 0; k < MPT; ++k) {
+        const int i = threadIdx.x + k * NT;
+        if (i < n) {
+          cx[k] = static_cast<int>(floor(x[k][0] * inv_rv));
+          cy[k] = static_cast<int>(floor(x[k][1] * inv_rv));
+          cz[k] = static_cast<int>(floor(x[k][2] * inv_rv));
+          s_ckey[i] = md_cell_key(cx[k], cy[k], cz[k]);
+          s_next[i] = atomicExch(&s_head[md_bucket(cx[k], cy[k], cz[k])], i);
+        }
+      }
+      __syncthreads();
 #pragma unroll
       for (int k = 0; k < MPT; ++k) {
         const int i = threadIdx.x + k * NT;
         if (i < n) {
           int cnt = 0;
-          for (int j = 0; j < n; ++j) {
-            if (j == i) continue;
-            const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
-            if ((d0 * d0 + d1 * d1) + d2 * d2 <= rv2) {
-              if (cnt < a.max_nb) a.nlist[static_cast<size_t>(cnt) * a.n_mono_total + b + i] = b + j;
-              ++cnt;
-            }
-          }
+          for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+              for (int dx = -1; dx <= 1; ++dx) {
+                const int tx = cx[k] + dx, ty = cy[k] + dy, tz = cz[k] + dz;
+                const int want = md_cell_key(tx, ty, tz);
+                for (int j = s_head[md_bucket(tx, ty, tz)]; j >= 0; j = s_next[j]) {
+                  if (j == i || s_ckey[j] != want) continue;
+                  const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
+                  if ((d0 * d0 + d1 * d1) + d2 * d2 <= rv2) {
+                    if (cnt < a.max_nb)
+                      a.nlist[static_cast<size_t>(cnt) * a.n_mono_total + b + i] = b + j;
+                    ++cnt;
+                  }
+                }
+              }
           if (cnt > a.max_nb) {
             raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(b + i),
                         static_cast<uint32_t>(cnt));
@@ -191,6 +257,10 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
           a.ncount[b + i] = cnt;
           xv[k][0] = x[k][0]; xv[k][1] = x[k][1]; xv[k][2] = x[k][2];
         }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        s_core_ref[0] = sx[0]; s_core_ref[1] = sy[0]; s_core_ref[2] = sz[0];
       }
     }
     __syncthreads();

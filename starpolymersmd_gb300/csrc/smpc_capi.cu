@@ -182,6 +182,7 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   a.n_steps = n;
   a.calc_epot = calc_epot;
   a.force_rebuild = force_rebuild;
+  a.core_relative = ctx->opt.strict_cells ? 0 : 1;
   a.err = ctx->d_err;
   smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
                      static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->st);
