@@ -5,6 +5,6 @@
 #define SMPC_COLLIDE_CT 128
 #define SMPC_COLLIDE_CAP 1408
 #define SMPC_BIN_NT 256
-#define SMPC_MD_NT 512
-#define SMPC_MD_MPT 2
+#define SMPC_MD_NT 1024
+#define SMPC_MD_MPT 1
 #include "kernels_impl.cuh"

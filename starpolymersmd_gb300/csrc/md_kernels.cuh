@@ -274,16 +274,28 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
         R F0 = R(0), F1 = R(0), F2 = R(0);
         const bool ai = s_amphi[i] != 0;
         const int cnt = a.ncount[b + i];
-        for (int q = 0; q < cnt; ++q) {
-          const int j = a.nlist[static_cast<size_t>(q) * a.n_mono_total + b + i] - b;
-          const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
-          const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
-          const bool bb = ai && s_amphi[j] != 0;
-          const R fa = pair_force<R>(pot, bb, r2, lambda);
-          F0 -= d0 * fa;
-          F1 -= d1 * fa;
-          F2 -= d2 * fa;
-          if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
+        const int* nl = a.nlist + b + i;
+        const size_t stride = static_cast<size_t>(a.n_mono_total);
+        // neighbour indices come in groups of four independent loads, so the
+        // list walk is not a chain of dependent L2 round trips
+        constexpr int PF = 4;
+        for (int q0 = 0; q0 < cnt; q0 += PF) {
+          int js[PF];
+#pragma unroll
+          for (int u = 0; u < PF; ++u) js[u] = q0 + u < cnt ? nl[static_cast<size_t>(q0 + u) * stride] - b : -1;
+#pragma unroll
+          for (int u = 0; u < PF; ++u) {
+            const int j = js[u];
+            if (j < 0) continue;
+            const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
+            const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+            const bool bb = ai && s_amphi[j] != 0;
+            const R fa = pair_force<R>(pot, bb, r2, lambda);
+            F0 -= d0 * fa;
+            F1 -= d1 * fa;
+            F2 -= d2 * fa;
+            if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
+          }
         }
         for (int e = a.bond_start[b + i]; e < a.bond_start[b + i + 1]; ++e) {
           const int2 bd = a.bonds[e];
