@@ -132,6 +132,15 @@ int smpc_cycles(smpc_ctx* ctx, int n);
  * scan, perm, collide, cycle end; summed over the n cycles) and the total
  * elapsed time from the first to the last event. */
 int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, double* total_ms);
+/* Launch-shape variants of the FP32 fast-path kernels (solvent binning,
+ * collide, MD substeps); index 0 is the default. Changing them re-captures
+ * the cycle graph. */
+int smpc_set_variants(smpc_ctx* ctx, int bin, int collide, int md);
+int smpc_get_variants(const smpc_ctx* ctx, int* bin, int* collide, int* md);
+/* Times every variant of each fast-path kernel over `cycles` live cycles
+ * (CUDA events on the context stream), keeps the fastest and writes a JSON
+ * report (variant -> ms per cycle, chosen). Advances the simulation. */
+int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len);
 /* smpc_cycles bracketed by CUDA events on the context stream (ms). */
 int smpc_time_cycles(smpc_ctx* ctx, int n, double* total_ms);
 /* Solvent initial state generated on the device (MPC::initialize,

@@ -1,0 +1,56 @@
+"""Launch-shape autotuner front end with a JSON cache.
+
+smpc_autotune (C ABI) times every launch-shape variant of the fast-path
+solvent-binning, collide and MD kernels on the live workload with CUDA events
+and keeps the fastest. This module caches the choice per GPU model and
+workload signature, so later runs of the same workload start tuned.
+"""
+from __future__ import annotations
+
+import json
+import os
+from typing import Optional
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CACHE = os.path.join(HERE, "_tune", "autotune_cache.json")
+
+
+def gpu_name() -> str:
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.cuda.get_device_name(0)
+    except Exception:  # torch is optional here
+        pass
+    return "unknown-gpu"
+
+
+def signature(n_rep: int, particles: int, cells: int, monomers: int) -> str:
+    return f"{gpu_name()}|rep={n_rep}|particles={particles}|cells={cells}|monomers={monomers}"
+
+
+def _load(path: str) -> dict:
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def tune(ctx, key: str, cycles: int = 3, cache_path: Optional[str] = None,
+         force: bool = False) -> dict:
+    """Applies the cached variants for `key`, or measures and caches them."""
+    path = cache_path or CACHE
+    cache = _load(path)
+    if not force and key in cache:
+        ctx.set_variants(*cache[key]["index"])
+        return dict(cache[key], cached=True)
+    report = ctx.autotune(cycles)
+    entry = {"index": list(ctx.get_variants()), "report": report}
+    cache[key] = entry
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp%d" % os.getpid()
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+    return dict(entry, cached=False)

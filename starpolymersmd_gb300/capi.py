@@ -33,7 +33,8 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_cell_counts", "smpc_set_collision_counter", "smpc_verlet_rebuilds",
            "smpc_error_word", "smpc_synchronize", "smpc_cycles_profiled", "smpc_time_cycles",
            "smpc_init_solvent", "smpc_temperature_all", "smpc_set_monomer_state_all",
-           "smpc_get_monomer_state_all")
+           "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
+           "smpc_autotune")
 
 PHASES = ("md_substeps", "cycle_begin", "mono_prep", "fluid_bin", "scan", "build_perm",
           "collide", "cycle_end")
@@ -105,6 +106,9 @@ def load(path: Optional[str] = None):
         "smpc_temperature_all": ([P, P], I),
         "smpc_set_monomer_state_all": ([P, P, P], I),
         "smpc_get_monomer_state_all": ([P, P, P, P], I),
+        "smpc_set_variants": ([P, I, I, I], I),
+        "smpc_get_variants": ([P, C.POINTER(I), C.POINTER(I), C.POINTER(I)], I),
+        "smpc_autotune": ([P, I, C.c_char_p, I], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -250,6 +254,23 @@ class Context:
         self._check(self.lib.smpc_cycles_profiled(self.h, n, _p(ph), len(PHASES), C.byref(tot)),
                     "cycles_profiled")
         return dict(zip(PHASES, ph)), tot.value
+
+    def set_variants(self, bin, collide, md):
+        self._check(self.lib.smpc_set_variants(self.h, bin, collide, md), "set_variants")
+
+    def get_variants(self):
+        b, c, m = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.lib.smpc_get_variants(self.h, C.byref(b), C.byref(c), C.byref(m)),
+                    "get_variants")
+        return b.value, c.value, m.value
+
+    def autotune(self, cycles=3):
+        """Times each kernel's launch-shape variants on the live workload and
+        keeps the fastest; returns the report."""
+        import json
+        buf = C.create_string_buffer(8192)
+        self._check(self.lib.smpc_autotune(self.h, cycles, buf, 8192), "autotune")
+        return json.loads(buf.value.decode() or "{}")
 
     def time_cycles(self, n):
         tot = C.c_double()

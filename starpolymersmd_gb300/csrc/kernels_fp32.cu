@@ -8,3 +8,28 @@
 #define SMPC_MD_NT 1024
 #define SMPC_MD_MPT 1
 #include "kernels_impl.cuh"
+
+namespace smpc {
+// Variant tables (index 0 is the default shape). The names read
+// threads x cells-per-tile / staging capacity / gathers in flight.
+int bin_variant_count() { return 4; }
+int collide_variant_count() { return 5; }
+int md_variant_count() { return 2; }
+int collide_variant_cells(int v) {
+  switch (v) {
+    case 2: case 3: return 64;
+    case 4: return 256;
+    default: return 128;
+  }
+}
+const char* bin_variant_name(int v) {
+  static const char* n[] = {"256t x4", "256t x2", "256t x8", "128t x8"};
+  return v >= 0 && v < 4 ? n[v] : "?";
+}
+const char* collide_variant_name(int v) {
+  static const char* n[] = {"256t 128c cap1408 g4", "256t 128c cap1408 g8", "128t 64c cap704 g4",
+                            "128t 64c cap704 g8", "512t 256c cap2816 g4"};
+  return v >= 0 && v < 5 ? n[v] : "?";
+}
+const char* md_variant_name(int v) { return v == 1 ? "512t 2/thread" : "1024t 1/thread"; }
+}  // namespace smpc

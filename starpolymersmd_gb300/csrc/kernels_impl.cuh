@@ -43,18 +43,46 @@ void launch_mono_prep<Real>(const RepInfo* reps, RepDyn* dyn, int n_rep, Real* m
                                                 mono_bin, strict, frames, rot_c, rot_s);
 }
 
+#if SMPC_FAST_F32
+template <int NT, int U>
+void bin_f32(const Tile* tiles, int n_tiles, const RepInfo* reps, const FrameF* frames,
+             const float* rec, uint2* keys, uint32_t* count, cudaStream_t st) {
+  k_fluid_bin_f32<NT, U><<<n_tiles, NT, 0, st>>>(tiles, reps, frames, rec, keys, count);
+}
+
+template <int NT, int CT, int CAP, int GU>
+void collide_f32(const CollideArgs<float>& a, cudaStream_t st) {
+  auto kern = k_collide_f32<NT, CT, CAP, GU>;
+  const size_t dyn = collide_f32_dyn_smem(CAP);
+  static bool configured = false;  // the attribute is per function, set once
+  if (!configured) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn));
+    configured = true;
+  }
+  kern<<<a.n_tiles, NT, dyn, st>>>(a.tiles, a.reps, a.frames, a.dyn, a.off, a.perm, a.st_in,
+                                   a.st_out, a.mpos, a.mvel, a.mimg, a.inj_gamma, a.inj_uphi,
+                                   a.inj_utheta, a.rng, a.mono_bin, a.err);
+}
+#endif
+
 template <>
 void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
                             const RepDyn* dyn, const FrameF* frames, const Real* rec, uint2* keys,
-                            uint32_t* count, ErrorState* err, int strict, cudaStream_t st) {
+                            uint32_t* count, ErrorState* err, int strict, int variant,
+                            cudaStream_t st) {
   if (n_tiles == 0) return;
 #if SMPC_FAST_F32
   if (!strict) {
-    k_fluid_bin_f32<SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, frames, rec, keys,
-                                                                  count);
-    return;
+    switch (variant) {
+      case 1: bin_f32<256, 2>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
+      case 2: bin_f32<256, 8>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
+      case 3: bin_f32<128, 8>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
+      default: bin_f32<256, 4>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
+    }
   }
 #endif
+  (void)frames;
+  (void)variant;
   k_fluid_bin<Real, SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, dyn, rec, keys,
                                                                   count, err, strict);
 }
@@ -64,17 +92,13 @@ void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
   if (a.n_tiles == 0) return;
 #if SMPC_FAST_F32
   if (!a.strict) {
-    auto kern = k_collide_f32<SMPC_COLLIDE_NT, SMPC_COLLIDE_CT, SMPC_COLLIDE_CAP>;
-    const size_t dyn = collide_f32_dyn_smem(SMPC_COLLIDE_CAP);
-    static bool configured = false;  // the attribute is per function, set once
-    if (!configured) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn));
-      configured = true;
+    switch (a.variant) {
+      case 1: collide_f32<256, 128, 1408, 8>(a, st); return;
+      case 2: collide_f32<128, 64, 704, 4>(a, st); return;
+      case 3: collide_f32<128, 64, 704, 8>(a, st); return;
+      case 4: collide_f32<512, 256, 2816, 4>(a, st); return;
+      default: collide_f32<256, 128, 1408, 4>(a, st); return;
     }
-    kern<<<a.n_tiles, SMPC_COLLIDE_NT, dyn, st>>>(
-        a.tiles, a.reps, a.frames, a.dyn, a.off, a.perm, a.st_in, a.st_out, a.mpos, a.mvel, a.mimg,
-        a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.mono_bin, a.err);
-    return;
   }
 #endif
   auto kern = k_collide<Real, SMPC_COLLIDE_NT, SMPC_COLLIDE_CT, SMPC_COLLIDE_CAP>;
@@ -101,8 +125,15 @@ void launch_temperature<Real>(const Tile* tiles, int n_tiles, const RepInfo* rep
 
 template <>
 void launch_md<Real>(const MdArgs& a, int n_rep, Real* mpos, Real* mvel, Real* mfrc, Real* mver,
-                     cudaStream_t st) {
+                     int variant, cudaStream_t st) {
   if (n_rep == 0) return;
+#if SMPC_FAST_F32
+  if (variant == 1) {
+    k_md_substeps<Real, 512, 2><<<n_rep, 512, 0, st>>>(a, mpos, mvel, mfrc, mver);
+    return;
+  }
+#endif
+  (void)variant;
   k_md_substeps<Real, SMPC_MD_NT, SMPC_MD_MPT><<<n_rep, SMPC_MD_NT, 0, st>>>(a, mpos, mvel, mfrc,
                                                                           mver);
 }

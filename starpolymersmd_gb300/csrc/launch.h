@@ -11,8 +11,19 @@ namespace smpc {
 
 struct MdArgs;
 
+// Launch-shape variants of the FP32 fast-path kernels, chosen by the
+// autotuner (smpc_autotune). The FP64 parity kernels have one shape.
+int bin_variant_count();
+int collide_variant_count();
+int md_variant_count();
+int collide_variant_cells(int v);     // cells per collide tile of variant v
+const char* bin_variant_name(int v);
+const char* collide_variant_name(int v);
+const char* md_variant_name(int v);
+
 template <typename R>
 struct CollideArgs {
+  int variant;
   const FrameF* frames;  // float frames (FP32 path)
   const Tile* tiles;
   int n_tiles;
@@ -59,7 +70,7 @@ void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* m
 template <typename R>
 void launch_fluid_bin(const Tile* tiles, int n_tiles, const RepInfo* reps, const RepDyn* dyn,
                       const FrameF* frames, const R* rec, uint2* keys, uint32_t* count,
-                      ErrorState* err, int strict, cudaStream_t st);
+                      ErrorState* err, int strict, int variant, cudaStream_t st);
 template <typename R>
 void launch_collide(const CollideArgs<R>& a, cudaStream_t st);
 template <typename R>
@@ -67,7 +78,8 @@ void launch_temperature(const Tile* tiles, int n_tiles, const RepInfo* reps, con
                         const uint32_t* perm, const R* rec_cur, const R* mpos, const R* mvel,
                         const int* mimg, int mono_bin, TempPartial* partial, cudaStream_t st);
 template <typename R>
-void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, cudaStream_t st);
+void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, int variant,
+               cudaStream_t st);
 
 void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* grand, int n_cells,
                  cudaStream_t st);

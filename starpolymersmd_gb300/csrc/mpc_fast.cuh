@@ -90,12 +90,11 @@ __device__ __forceinline__ void st_f4(float* p, size_t i, float4 v) {
 
 // --------------------------------------------------------------- binning
 
-template <int NT>
+template <int NT, int U>
 __global__ void __launch_bounds__(NT) k_fluid_bin_f32(const Tile* tiles, const RepInfo* reps,
                                                       const FrameF* frames,
                                                       const float* __restrict__ st,
                                                       uint2* __restrict__ keys, uint32_t* count) {
-  constexpr int U = 4;
   const Tile t = tiles[blockIdx.x];
   const FrameF f = frames[t.rep];
   const uint32_t cbase = static_cast<uint32_t>(reps[t.rep].cell_base);
@@ -184,14 +183,13 @@ __device__ __forceinline__ void frame_f(FastP& P, const FrameF& f, float solvent
   P.v.w = solvent_mass;
 }
 
-template <int NT, int CT, int CAP>
+template <int NT, int CT, int CAP, int GU>
 __global__ void __launch_bounds__(NT) k_collide_f32(
     const Tile* tiles, const RepInfo* reps, const FrameF* frames, const RepDyn* dyn,
     const uint32_t* __restrict__ off, const uint32_t* __restrict__ perm,
     const float* __restrict__ st_in, float* __restrict__ st_out, const float* mpos, float* mvel,
     const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
     int rng, int mono_bin, ErrorState* err) {
-  constexpr int GU = 4;
   static_assert(NT == 2 * CT, "two threads per cell");
   __shared__ float s_cmv[CT * 3];
   __shared__ float s_rot[CT * 9];

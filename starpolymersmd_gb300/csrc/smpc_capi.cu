@@ -36,8 +36,12 @@ struct smpc_ctx {
   RepDyn* d_dyn = nullptr;
   Tile* d_bin_tiles = nullptr;
   int n_bin_tiles = 0;
-  Tile* d_col_tiles = nullptr;
+  Tile* d_col_tiles = nullptr;   // parity-path collide tiles
   int n_col_tiles = 0;
+  // fast path: collide tiles for each tile size the variants use (64/128/256 cells)
+  Tile* d_col_tiles_v[3] = {nullptr, nullptr, nullptr};
+  int n_col_tiles_v[3] = {0, 0, 0};
+  int var_bin = 0, var_col = 0, var_md = 0;
   std::vector<Tile> h_tmp_tiles;
   Tile* d_tmp_tiles = nullptr;
   TempPartial* d_tpart = nullptr;
@@ -81,6 +85,11 @@ struct smpc_ctx {
 };
 
 namespace {
+
+bool fast_path(const smpc_ctx* ctx) {
+  return ctx->opt.precision == SMPC_FP32 && !ctx->opt.strict_cells;
+}
+int tile_set(int cells) { return cells == 64 ? 0 : (cells == 128 ? 1 : 2); }
 
 int fail(smpc_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -129,7 +138,7 @@ int launch_collision(smpc_ctx* ctx, int rng, int cur) {
                             ctx->rot_s, ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
-                            ctx->st);
+                            ctx->var_bin, ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
   smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
@@ -142,9 +151,15 @@ template <typename R>
 smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
   const int strict = ctx->opt.strict_cells;
   smpc::CollideArgs<R> a;
+  a.variant = ctx->var_col;
   a.frames = ctx->d_frames;
   a.tiles = ctx->d_col_tiles;
   a.n_tiles = ctx->n_col_tiles;
+  if (fast_path(ctx)) {
+    const int k = tile_set(smpc::collide_variant_cells(ctx->var_col));
+    a.tiles = ctx->d_col_tiles_v[k];
+    a.n_tiles = ctx->n_col_tiles_v[k];
+  }
   a.reps = ctx->d_reps;
   a.dyn = ctx->d_dyn;
   a.off = ctx->d_off;
@@ -185,7 +200,8 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   a.core_relative = ctx->opt.strict_cells ? 0 : 1;
   a.err = ctx->d_err;
   smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
-                     static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->st);
+                     static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->var_md,
+                     ctx->st);
   return SMPC_OK;
 }
 
@@ -210,7 +226,7 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
   cudaEventRecord(ev[1 + PH_MONO], ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
-                            ctx->st);
+                            ctx->var_bin, ctx->st);
   cudaEventRecord(ev[1 + PH_BIN], ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
@@ -552,6 +568,8 @@ void free_all(smpc_ctx* ctx) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  for (int k = 0; k < 3; ++k)
+    if (ctx->d_col_tiles_v[k]) cudaFree(ctx->d_col_tiles_v[k]);
   if (ctx->st) cudaStreamDestroy(ctx->st);
 }
 
@@ -657,6 +675,17 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
        (ctx->h_tmp_tiles.empty() || cudaMemcpy(ctx->d_tmp_tiles, ctx->h_tmp_tiles.data(), ctx->h_tmp_tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice) == cudaSuccess) &&
        cudaMemset(ctx->d_err, 0, sizeof(ErrorState)) == cudaSuccess;
   if (!ok) return bail(SMPC_E_CUDA, "upload");
+  if (fast_path(ctx)) {
+    const int cells[3] = {64, 128, 256};
+    for (int k = 0; k < 3; ++k) {
+      std::vector<Tile> tv = make_tiles(ctx->reps, true, cells[k]);
+      ctx->n_col_tiles_v[k] = static_cast<int>(tv.size());
+      if (dalloc(&ctx->d_col_tiles_v[k], tv.size()) != cudaSuccess ||
+          cudaMemcpy(ctx->d_col_tiles_v[k], tv.data(), tv.size() * sizeof(Tile),
+                     cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(SMPC_E_CUDA, "tile tables");
+    }
+  }
   // empty solvent state until smpc_set_fluid: every slot a hole
   for (int r = 0; r < n_rep; ++r) {
     std::vector<double> z(3 * static_cast<size_t>(ctx->reps[r].n_fluid) + 3, 0.0);
@@ -829,11 +858,8 @@ int smpc_cycles(smpc_ctx* ctx, int n) {
   return SMPC_OK;
 }
 
-int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, double* total_ms) {
-  if (!ctx || n <= 0 || !phase_ms || n_phases < PH_COUNT || !total_ms) return SMPC_E_ARG;
-  if (ctx->opt.rng != SMPC_RNG_PHILOX) return fail(ctx, SMPC_E_STATE, "fused cycles need Philox draws");
-  if (ctx->total_mono > 0 && !ctx->md_ready) return fail(ctx, SMPC_E_STATE, "smpc_init_md not called");
-  cudaSetDevice(ctx->device);
+namespace {
+int run_profiled(smpc_ctx* ctx, int n, double* phase_ms, double* total_ms) {
   if (int rc = upload_host_dyn(ctx)) return rc;
   const double scale = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / ctx->opt.step_update : 1.0;
   std::vector<cudaEvent_t> ev(static_cast<size_t>(n) * (PH_COUNT + 1));
@@ -856,7 +882,7 @@ int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, d
     }
   }
   cudaError_t e = cudaStreamSynchronize(ctx->st);
-  for (int p = 0; p < n_phases; ++p) phase_ms[p] = 0.0;
+  for (int p = 0; p < PH_COUNT; ++p) phase_ms[p] = 0.0;
   *total_ms = 0.0;
   if (e == cudaSuccess) {
     for (int i = 0; i < n; ++i) {
@@ -873,6 +899,92 @@ int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, d
   }
   for (auto& x : ev) cudaEventDestroy(x);
   if (e != cudaSuccess) return fail(ctx, SMPC_E_CUDA, cudaGetErrorString(e));
+  return SMPC_OK;
+}
+
+void drop_graphs(smpc_ctx* ctx) {
+  for (int k = 0; k < 2; ++k)
+    if (ctx->graph[k]) {
+      cudaGraphExecDestroy(ctx->graph[k]);
+      ctx->graph[k] = nullptr;
+    }
+}
+}  // namespace
+
+int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, double* total_ms) {
+  if (!ctx || n <= 0 || !phase_ms || n_phases < PH_COUNT || !total_ms) return SMPC_E_ARG;
+  if (ctx->opt.rng != SMPC_RNG_PHILOX) return fail(ctx, SMPC_E_STATE, "fused cycles need Philox draws");
+  if (ctx->total_mono > 0 && !ctx->md_ready) return fail(ctx, SMPC_E_STATE, "smpc_init_md not called");
+  cudaSetDevice(ctx->device);
+  return run_profiled(ctx, n, phase_ms, total_ms);
+}
+
+int smpc_set_variants(smpc_ctx* ctx, int bin, int collide, int md) {
+  if (!ctx) return SMPC_E_ARG;
+  if (bin < 0 || bin >= smpc::bin_variant_count() || collide < 0 ||
+      collide >= smpc::collide_variant_count() || md < 0 || md >= smpc::md_variant_count())
+    return fail(ctx, SMPC_E_ARG, "variant index out of range");
+  if (bin != ctx->var_bin || collide != ctx->var_col || md != ctx->var_md) drop_graphs(ctx);
+  ctx->var_bin = bin;
+  ctx->var_col = collide;
+  ctx->var_md = md;
+  return SMPC_OK;
+}
+
+int smpc_get_variants(const smpc_ctx* ctx, int* bin, int* collide, int* md) {
+  if (!ctx) return SMPC_E_ARG;
+  if (bin) *bin = ctx->var_bin;
+  if (collide) *collide = ctx->var_col;
+  if (md) *md = ctx->var_md;
+  return SMPC_OK;
+}
+
+int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len) {
+  if (!ctx || cycles <= 0) return SMPC_E_ARG;
+  if (ctx->opt.rng != SMPC_RNG_PHILOX) return fail(ctx, SMPC_E_STATE, "autotuning runs Philox cycles");
+  if (ctx->total_mono > 0 && !ctx->md_ready) return fail(ctx, SMPC_E_STATE, "smpc_init_md not called");
+  cudaSetDevice(ctx->device);
+  std::string js = "{";
+  if (fast_path(ctx)) {
+    struct Cat {
+      const char* name;
+      int phase;
+      int count;
+      int* var;
+      const char* (*label)(int);
+    } cats[3] = {{"fluid_bin", PH_BIN, smpc::bin_variant_count(), &ctx->var_bin, smpc::bin_variant_name},
+                 {"collide", PH_COLLIDE, smpc::collide_variant_count(), &ctx->var_col,
+                  smpc::collide_variant_name},
+                 {"md_substeps", PH_MD, smpc::md_variant_count(), &ctx->var_md, smpc::md_variant_name}};
+    double ph[PH_COUNT], tot;
+    for (int c = 0; c < 3; ++c) {
+      int best = 0;
+      double best_ms = 1e300;
+      js += std::string(c ? ", " : "") + "\"" + cats[c].name + "\": {\"ms_per_cycle\": {";
+      for (int v = 0; v < cats[c].count; ++v) {
+        *cats[c].var = v;
+        drop_graphs(ctx);
+        if (int rc = run_profiled(ctx, cycles, ph, &tot)) return rc;
+        const double ms = ph[cats[c].phase] / cycles;
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "%s\"%s\": %.5f", v ? ", " : "", cats[c].label(v), ms);
+        js += buf;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = v;
+        }
+      }
+      *cats[c].var = best;
+      drop_graphs(ctx);
+      js += std::string("}, \"chosen\": \"") + cats[c].label(best) + "\", \"index\": " +
+            std::to_string(best) + "}";
+    }
+  }
+  js += "}";
+  if (report && report_len > 0) {
+    std::strncpy(report, js.c_str(), static_cast<size_t>(report_len) - 1);
+    report[report_len - 1] = 0;
+  }
   return SMPC_OK;
 }
 

@@ -279,3 +279,53 @@ def test_batched_fp32_tracks_fp64_oracle():
             bad = (dp > 1e-4 * s.L) | (dv > 1e-3 * vs)
             assert bad.mean() < 0.03, (k, bad.mean())
             assert abs(ctx.temperature(k) - o.temperature()) < 0.01
+
+
+def test_fp32_launch_variants_agree_bitwise():
+    # Every launch shape of the fast-path solvent kernels gives the same
+    # solvent state to the last bit: cell sums are int64 fixed point
+    # (independent of particle order) and each particle's update is a pure
+    # function of its cell's sums and draws.
+    from starpolymersmd_gb300 import system
+    rng = np.random.default_rng(8)
+    reps, states = [], []
+    for k, L in enumerate((11, 14)):
+        fp, fv = system.uniform_fluid((L, L, L), 10, 1.0, rng)
+        reps.append(dict(L=(L, L, L), n_fluid=len(fp), kT=1.0, shear=0.02 * (k + 1), h=0.1,
+                         seed=40 + k))
+        states.append((fp, fv))
+    finals = []
+    lib = capi.load()
+    n_bin, n_col = 4, 5
+    for vb, vc in [(0, 0)] + [(b, 0) for b in range(1, n_bin)] + [(0, c) for c in range(1, n_col)]:
+        with capi.Context(reps, precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=1,
+                          strict_cells=0) as ctx:
+            for k, (fp, fv) in enumerate(states):
+                ctx.set_fluid(k, fp, fv)
+            ctx.set_variants(vb, vc, 0)
+            ctx.cycles(3)
+            ctx.synchronize()
+            ctx.raise_on_device_error()
+            finals.append([ctx.get_fluid(k) for k in range(len(reps))])
+    for other in finals[1:]:
+        for (p0, v0), (p1, v1) in zip(finals[0], other):
+            np.testing.assert_array_equal(p0, p1)
+            np.testing.assert_array_equal(v0, v1)
+
+
+def test_autotune_reports_and_keeps_a_variant():
+    from starpolymersmd_gb300 import system
+    rng = np.random.default_rng(9)
+    fp, fv = system.uniform_fluid((12, 12, 12), 10, 1.0, rng)
+    rep = dict(L=(12, 12, 12), n_fluid=len(fp), kT=1.0, shear=0.05, h=0.1, seed=5)
+    with capi.Context([rep], precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=1,
+                      strict_cells=0) as ctx:
+        ctx.set_fluid(0, fp, fv)
+        report = ctx.autotune(2)
+        assert set(report) == {"fluid_bin", "collide", "md_substeps"}
+        chosen = ctx.get_variants()
+        assert chosen[0] == report["fluid_bin"]["index"]
+        assert chosen[1] == report["collide"]["index"]
+        ctx.cycles(2)
+        ctx.raise_on_device_error()
+        assert abs(ctx.temperature(0) - 1.0) < 0.2
