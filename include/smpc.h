@@ -123,6 +123,18 @@ int smpc_md_substeps(smpc_ctx* ctx, int n, int calc_epot);
  * call, a collision when t % step_update == 0. inj may be NULL only in
  * Philox mode. */
 int smpc_mpc_step(smpc_ctx* ctx, long t, double dt, const smpc_inject* inj);
+/* MPC::step in two phases, for drivers that draw the collision's random
+ * numbers themselves in the reference's order (grid shift before binning,
+ * then per cell gamma, phi, theta -- MPC.cpp:123, 244-245, 289), e.g. from
+ * the reference's own Rand stream:
+ *   smpc_mpc_bin: delrx advance; on a collision step (*collide_now = 1)
+ *     recentring, streaming, the grid shift (shift[3*n_rep], or NULL for the
+ *     Philox shift) and the counting sort; smpc_cell_counts then gives the
+ *     occupancies that decide which cells draw a gamma variate;
+ *   smpc_mpc_collide: the per-cell collisions with injected draws (inj) or
+ *     Philox draws (inj == NULL), and the unshift. */
+int smpc_mpc_bin(smpc_ctx* ctx, long t, double dt, const double* shift, int* collide_now);
+int smpc_mpc_collide(smpc_ctx* ctx, const smpc_inject* inj);
 /* n fused cycles of (step_update MD substeps + one collision) with Philox
  * draws, launched as a captured CUDA graph. */
 int smpc_cycles(smpc_ctx* ctx, int n);

@@ -34,7 +34,7 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_error_word", "smpc_synchronize", "smpc_cycles_profiled", "smpc_time_cycles",
            "smpc_init_solvent", "smpc_temperature_all", "smpc_set_monomer_state_all",
            "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
-           "smpc_autotune")
+           "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide")
 
 PHASES = ("md_substeps", "cycle_begin", "mono_prep", "fluid_bin", "scan", "build_perm",
           "collide", "cycle_end")
@@ -109,6 +109,8 @@ def load(path: Optional[str] = None):
         "smpc_set_variants": ([P, I, I, I], I),
         "smpc_get_variants": ([P, C.POINTER(I), C.POINTER(I), C.POINTER(I)], I),
         "smpc_autotune": ([P, I, C.c_char_p, I], I),
+        "smpc_mpc_bin": ([P, C.c_long, D, P, C.POINTER(I)], I),
+        "smpc_mpc_collide": ([P, C.POINTER(Inject)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -243,6 +245,23 @@ class Context:
             inj = Inject(*[a.ctypes.data for a in arrs])
         self._check(self.lib.smpc_mpc_step(self.h, t, dt, None if inj is None else C.byref(inj)),
                     "mpc_step")
+
+    def mpc_bin(self, t, dt, shift=None):
+        """First phase of MPC::step; returns True when this call binned a collision."""
+        arr = None if shift is None else _f64(shift).ravel()
+        self._keep_bin = arr
+        now = C.c_int()
+        self._check(self.lib.smpc_mpc_bin(self.h, t, dt, _p(arr), C.byref(now)), "mpc_bin")
+        return bool(now.value)
+
+    def mpc_collide(self, gamma=None, u_phi=None, u_theta=None):
+        inj = None
+        if gamma is not None:
+            arrs = [_f64(gamma).ravel(), _f64(u_phi).ravel(), _f64(u_theta).ravel()]
+            self._keep = arrs
+            inj = Inject(None, *[a.ctypes.data for a in arrs])
+        self._check(self.lib.smpc_mpc_collide(self.h, None if inj is None else C.byref(inj)),
+                    "mpc_collide")
 
     def cycles(self, n):
         self._check(self.lib.smpc_cycles(self.h, n), "cycles")

@@ -74,6 +74,8 @@ struct smpc_ctx {
   double rot_c = 0, rot_s = 0;
   int max_nb = 192;
   bool collided = false;
+  bool binned = false;      // smpc_mpc_bin done, collide pending
+  bool bin_philox = false;  // that binning drew its shift from Philox
   bool md_ready = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   std::string err;
@@ -129,7 +131,7 @@ template <typename R>
 smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur);
 
 template <typename R>
-int launch_collision(smpc_ctx* ctx, int rng, int cur) {
+int launch_binning(smpc_ctx* ctx, int cur) {
   const int strict = ctx->opt.strict_cells;
   const R* rec_in = static_cast<const R*>(ctx->d_rec[cur]);
   smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
@@ -143,6 +145,12 @@ int launch_collision(smpc_ctx* ctx, int rng, int cur) {
                     static_cast<int>(ctx->total_cells), ctx->st);
   smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
                           static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->st);
+  return SMPC_OK;
+}
+
+template <typename R>
+int launch_collision(smpc_ctx* ctx, int rng, int cur) {
+  launch_binning<R>(ctx, cur);
   smpc::launch_collide<R>(collide_args<R>(ctx, rng, cur), ctx->st);
   return SMPC_OK;
 }
@@ -819,6 +827,76 @@ int smpc_mpc_step(smpc_ctx* ctx, long t, double dt, const smpc_inject* inj) {
   return SMPC_OK;
 }
 
+int smpc_mpc_bin(smpc_ctx* ctx, long t, double dt, const double* shift, int* collide_now) {
+  if (!ctx || !collide_now) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  *collide_now = 0;
+  const int su = ctx->opt.step_update;
+  const double scale = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / su : 1.0;
+  for (int r = 0; r < ctx->n_rep; ++r) {  // MPC.cpp:117-118
+    RepDyn& dn = ctx->dyn[r];
+    const RepInfo& ri = ctx->reps[r];
+    dn.delrx += ri.shear * ri.L[1] * (dt * scale);
+    dn.delrx -= ri.L[0] * std::round(dn.delrx / ri.L[0]);
+    dn.h = dt;
+  }
+  if (t % su) return upload_host_dyn(ctx);
+  if (shift) {
+    for (int r = 0; r < ctx->n_rep; ++r)
+      for (int d = 0; d < 3; ++d) ctx->dyn[r].shift[d] = shift[3 * r + d];
+  } else if (ctx->opt.rng != SMPC_RNG_PHILOX) {
+    return fail(ctx, SMPC_E_ARG, "inject mode needs the grid shift");
+  }
+  if (int rc = upload_host_dyn(ctx)) return rc;
+  if (!shift) {
+    if (ctx->opt.precision == SMPC_FP64)
+      smpc::launch_cycle_begin<double>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, 0, 0.0, 1, ctx->st);
+    else
+      smpc::launch_cycle_begin<float>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, 0, 0.0, 1, ctx->st);
+  }
+  if (ctx->opt.precision == SMPC_FP64)
+    launch_binning<double>(ctx, ctx->cur);
+  else
+    launch_binning<float>(ctx, ctx->cur);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(ctx->st));
+  ctx->binned = true;
+  ctx->bin_philox = shift == nullptr;
+  *collide_now = 1;
+  return SMPC_OK;
+}
+
+int smpc_mpc_collide(smpc_ctx* ctx, const smpc_inject* inj) {
+  if (!ctx) return SMPC_E_ARG;
+  if (!ctx->binned) return fail(ctx, SMPC_E_STATE, "smpc_mpc_bin has not binned this collision");
+  cudaSetDevice(ctx->device);
+  const int rng = inj ? SMPC_RNG_INJECT : SMPC_RNG_PHILOX;
+  if (rng == SMPC_RNG_INJECT) {
+    if (!inj->gamma || !inj->u_phi || !inj->u_theta)
+      return fail(ctx, SMPC_E_ARG, "injected draws need gamma, u_phi and u_theta");
+    const size_t C = static_cast<size_t>(ctx->total_cells);
+    CU(cudaMemcpyAsync(ctx->d_inj, inj->gamma, C * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_inj + C, inj->u_phi, C * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_inj + 2 * C, inj->u_theta, C * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  }
+  if (ctx->opt.precision == SMPC_FP64)
+    smpc::launch_collide<double>(collide_args<double>(ctx, rng, ctx->cur), ctx->st);
+  else
+    smpc::launch_collide<float>(collide_args<float>(ctx, rng, ctx->cur), ctx->st);
+  if (ctx->bin_philox) {
+    if (ctx->opt.precision == SMPC_FP64)
+      smpc::launch_cycle_end<double>(ctx->d_dyn, ctx->n_rep, ctx->st);
+    else
+      smpc::launch_cycle_end<float>(ctx->d_dyn, ctx->n_rep, ctx->st);
+  }
+  CU(cudaGetLastError());
+  if (rng == SMPC_RNG_INJECT) CU(cudaStreamSynchronize(ctx->st));  // borrowed host buffers
+  ctx->cur ^= 1;
+  ctx->collided = true;
+  ctx->binned = false;
+  return SMPC_OK;
+}
+
 int smpc_cycles(smpc_ctx* ctx, int n) {
   if (!ctx || n < 0) return SMPC_E_ARG;
   if (ctx->opt.rng != SMPC_RNG_PHILOX) return fail(ctx, SMPC_E_STATE, "fused cycles need Philox draws");
@@ -1091,7 +1169,7 @@ int smpc_set_collision_counter(smpc_ctx* ctx, uint64_t counter) {
 
 int smpc_cell_counts(smpc_ctx* ctx, int rep, unsigned* total, unsigned* fluid) {
   if (int rc = check_rep(ctx, rep)) return rc;
-  if (!ctx->collided) return fail(ctx, SMPC_E_STATE, "no collision has run yet");
+  if (!ctx->collided && !ctx->binned) return fail(ctx, SMPC_E_STATE, "no collision has run yet");
   const RepInfo& ri = ctx->reps[rep];
   std::vector<uint32_t> off(ri.n_cell + 1);
   CU(cudaMemcpyAsync(off.data(), ctx->d_off + ri.cell_base, (ri.n_cell + 1) * sizeof(uint32_t),

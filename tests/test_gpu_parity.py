@@ -329,3 +329,30 @@ def test_autotune_reports_and_keeps_a_variant():
         ctx.cycles(2)
         ctx.raise_on_device_error()
         assert abs(ctx.temperature(0) - 1.0) < 0.2
+
+
+@pytest.mark.parametrize("name", ["star_mpc_L12", "mpc_shear_L6"])
+def test_two_phase_step_replays_reference(golden_dir, name):
+    # smpc_mpc_bin with the reference's grid shift, occupancies read back
+    # between the phases (what decides which cells draw a gamma variate), then
+    # smpc_mpc_collide with the reference's per-cell draws.
+    fx = gr.load(os.path.join(golden_dir, name + ".npz"))
+    coll = gr.collision_index(fx)
+    star = gr.has_star(fx)
+    with H.fixture_context(fx) as ctx:
+        for t in range(int(fx["n_loop"])):
+            if star and int(fx["with_md"]):
+                ctx.md_substeps(1)
+            k = coll.get(t)
+            binned = ctx.mpc_bin(t, float(fx["h"]), None if k is None else fx["shift"][k])
+            assert binned == (k is not None)
+            if binned:
+                tot, fl = ctx.cell_counts(0)
+                np.testing.assert_array_equal(tot, fx["count_total"][k])
+                np.testing.assert_array_equal(fl, fx["count_fluid"][k])
+                ctx.mpc_collide(np.nan_to_num(fx["gamma"][k]), fx["u_phi"][k], fx["u_theta"][k])
+                ctx.raise_on_device_error()
+                p, v = ctx.get_fluid(0)
+                H.close64(p, fx["fluid_pos"][k])
+                H.close64(v, fx["fluid_vel"][k])
+            assert ctx.delrx(0) == fx["delrx"][t]
