@@ -247,7 +247,7 @@ def run_ours(args, world, rank, local, dist):
     achieved = coll_bytes / (coll_ms / 1e3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and not args.replicas:
         with open(tpath) as f:
             tj = json.load(f)
         if args.workload in tj:
