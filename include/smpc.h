@@ -175,6 +175,14 @@ int smpc_set_delrx(smpc_ctx* ctx, int rep, double delrx);
 /* Cell occupancies of the last collision: MPCCellList sizes and
  * MPCCellListFluidParticles (MPC.h:40-41). */
 int smpc_cell_counts(smpc_ctx* ctx, int rep, unsigned* total, unsigned* fluid);
+/* Cell of every solvent particle (fluid_cell[n_fluid], by particle id) and of
+ * every monomer (mono_cell[n_mono], -1 if not binned) at the last collision:
+ * MPCParticle::CellIndex as MPC::sort set it (MPC.cpp:209, 224), from which a
+ * host-side driver rebuilds MPCCellList (MPC.h:40) for its per-cell getters
+ * (calculateFluidVelocity, calculateEkinInCell, print_fluid; MPC.cpp:335-418,
+ * 533-568). SMPC_E_STATE after a solvent upload or a binning without its
+ * collision. Either pointer may be NULL. */
+int smpc_cell_members(smpc_ctx* ctx, int rep, int* fluid_cell, int* mono_cell);
 int smpc_set_collision_counter(smpc_ctx* ctx, uint64_t counter);
 int smpc_verlet_rebuilds(smpc_ctx* ctx, int rep, int* out);
 

@@ -236,7 +236,8 @@ class RefSystem:
             "ref_get_fluid": [P, P, P], "ref_set_fluid": [P, P, P],
             "ref_get_monomers": [P, P, P, P, P, P, P], "ref_set_monomers": [P, P, P],
             "ref_propagate": [P, C.c_int], "ref_mpc_step": [P, C.c_long, C.c_double],
-            "ref_cell_counts": [P, P, P], "ref_set_delrx": [P, C.c_double],
+            "ref_cell_counts": [P, P, P], "ref_cell_index": [P, P, P],
+            "ref_set_delrx": [P, C.c_double],
             "ref_gyration": [P, P], "ref_run": [P, C.c_long, C.c_long, C.c_double, C.c_int],
             "ref_shift_arg_order": [P], "rand_tape_enable": [C.c_int], "rand_tape_clear": [],
             "rand_tape_copy": [P, P, C.c_long], "rand_tape_reseed": [C.c_ulonglong],
@@ -332,6 +333,13 @@ class RefSystem:
         fl = np.zeros(n, dtype=np.uint32)
         self.lib.ref_cell_counts(self.h, _p(tot), _p(fl))
         return tot, fl
+
+    def cell_index(self):
+        """CellIndex of every solvent particle and monomer at the last sort."""
+        fc = np.zeros(self.n_fluid, dtype=np.int32)
+        mc = np.zeros(self.n_mono, dtype=np.int32)
+        self.lib.ref_cell_index(self.h, _p(fc), _p(mc))
+        return fc, mc
 
     @property
     def delrx(self):

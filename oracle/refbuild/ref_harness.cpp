@@ -175,6 +175,19 @@ void ref_cell_counts(RefSys* s, unsigned* total, unsigned* fluid) {
   }
 }
 
+// MPCParticle::CellIndex of every solvent particle and monomer as the last
+// MPC::sort set it (MPC.cpp:209, 224).
+void ref_cell_index(RefSys* s, int* fluid_cell, int* mono_cell) {
+  if (fluid_cell)
+    for (size_t i = 0; i < s->mpc->Fluid.size(); ++i)
+      fluid_cell[i] = static_cast<int>(s->mpc->Fluid[i].CellIndex);
+  if (mono_cell) {
+    int k = 0;
+    for (auto& mol : s->box->Molecules)
+      for (auto& mono : mol.Monomers) mono_cell[k++] = static_cast<int>(mono.CellIndex);
+  }
+}
+
 double ref_delrx(RefSys* s) { return s->mpc->get_delrx(); }
 void ref_set_delrx(RefSys* s, double d) { s->mpc->set_delrx(d); }
 

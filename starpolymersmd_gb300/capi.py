@@ -30,7 +30,7 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_get_fluid", "smpc_set_monomers", "smpc_get_monomers", "smpc_set_bonds",
            "smpc_init_md", "smpc_md_substeps", "smpc_mpc_step", "smpc_cycles",
            "smpc_temperature", "smpc_epot", "smpc_delrx", "smpc_set_delrx",
-           "smpc_cell_counts", "smpc_set_collision_counter", "smpc_verlet_rebuilds",
+           "smpc_cell_counts", "smpc_cell_members", "smpc_set_collision_counter", "smpc_verlet_rebuilds",
            "smpc_error_word", "smpc_synchronize", "smpc_cycles_profiled", "smpc_time_cycles",
            "smpc_init_solvent", "smpc_temperature_all", "smpc_set_monomer_state_all",
            "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
@@ -96,6 +96,7 @@ def load(path: Optional[str] = None):
         "smpc_delrx": ([P, I, C.POINTER(D)], I),
         "smpc_set_delrx": ([P, I, D], I),
         "smpc_cell_counts": ([P, I, P, P], I),
+        "smpc_cell_members": ([P, I, P, P], I),
         "smpc_set_collision_counter": ([P, C.c_uint64], I),
         "smpc_verlet_rebuilds": ([P, I, C.POINTER(I)], I),
         "smpc_error_word": ([P, C.POINTER(C.c_uint), P], I),
@@ -341,6 +342,13 @@ class Context:
         fl = np.zeros(n, dtype=np.uint32)
         self._check(self.lib.smpc_cell_counts(self.h, rep, _p(tot), _p(fl)), "cell_counts")
         return tot, fl
+
+    def cell_members(self, rep=0):
+        """(cell of every solvent particle by id, cell of every monomer) at the last sort."""
+        fc = np.zeros(self.replicas[rep]["n_fluid"], dtype=np.int32)
+        mc = np.zeros(self.replicas[rep].get("n_mono", 0), dtype=np.int32)
+        self._check(self.lib.smpc_cell_members(self.h, rep, _p(fc), _p(mc)), "cell_members")
+        return fc, mc
 
     def set_collision_counter(self, c):
         self._check(self.lib.smpc_set_collision_counter(self.h, c), "set_collision_counter")

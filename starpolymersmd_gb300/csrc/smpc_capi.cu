@@ -75,6 +75,9 @@ struct smpc_ctx {
   int max_nb = 192;
   bool collided = false;
   bool binned = false;      // smpc_mpc_bin done, collide pending
+  // per replica: its solvent records sit in the last sort's cell order (set by
+  // a collision, cleared by a host upload or a new binning)
+  std::vector<uint8_t> sorted;
   bool bin_philox = false;  // that binning drew its shift from Philox
   bool md_ready = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -587,6 +590,7 @@ int dispatch_collision(smpc_ctx* ctx, int rng) {
   if (rng == SMPC_RNG_PHILOX) smpc::launch_cycle_end<R>(ctx->d_dyn, ctx->n_rep, ctx->st);
   ctx->cur ^= 1;
   ctx->collided = true;
+  std::fill(ctx->sorted.begin(), ctx->sorted.end(), 1);
   return SMPC_OK;
 }
 
@@ -603,6 +607,7 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
   if (ctx->opt.step_update <= 0) ctx->opt.step_update = 1;
   if (ctx->opt.max_neighbors > 0) ctx->max_nb = ctx->opt.max_neighbors;
   ctx->n_rep = n_rep;
+  ctx->sorted.assign(n_rep, 0);
   ctx->device = opt->device;
   ctx->real_size = opt->precision == SMPC_FP64 ? 8 : 4;
   ctx->rot_c = std::cos(130.0 * M_PI / 180.0);  // MPC.cpp:23-24
@@ -723,6 +728,7 @@ int smpc_n_cells(const smpc_ctx* ctx, int rep) {
 int smpc_set_fluid(smpc_ctx* ctx, int rep, const double* pos, const double* vel) {
   if (int rc = check_rep(ctx, rep)) return rc;
   if (!pos || !vel) return fail(ctx, SMPC_E_ARG, "null buffer");
+  ctx->sorted[rep] = 0;
   return ctx->opt.precision == SMPC_FP64 ? set_fluid_t<double>(ctx, rep, pos, vel)
                                          : set_fluid_t<float>(ctx, rep, pos, vel);
 }
@@ -862,6 +868,7 @@ int smpc_mpc_bin(smpc_ctx* ctx, long t, double dt, const double* shift, int* col
   CU(cudaStreamSynchronize(ctx->st));
   ctx->binned = true;
   ctx->bin_philox = shift == nullptr;
+  std::fill(ctx->sorted.begin(), ctx->sorted.end(), 0);
   *collide_now = 1;
   return SMPC_OK;
 }
@@ -894,6 +901,7 @@ int smpc_mpc_collide(smpc_ctx* ctx, const smpc_inject* inj) {
   ctx->cur ^= 1;
   ctx->collided = true;
   ctx->binned = false;
+  std::fill(ctx->sorted.begin(), ctx->sorted.end(), 1);
   return SMPC_OK;
 }
 
@@ -922,6 +930,7 @@ int smpc_cycles(smpc_ctx* ctx, int n) {
     CU(cudaGraphLaunch(ctx->graph[cur], ctx->st));
     ctx->cur ^= 1;
     ctx->collided = true;
+    std::fill(ctx->sorted.begin(), ctx->sorted.end(), 1);
     // mirror the device's delrx advance (k_cycle_begin), same FP64 operations
     for (int r = 0; r < ctx->n_rep; ++r) {
       const RepInfo& ri = ctx->reps[r];
@@ -949,6 +958,7 @@ int run_profiled(smpc_ctx* ctx, int n, double* phase_ms, double* total_ms) {
       profiled_cycle<float>(ctx, ctx->cur, ev.data() + static_cast<size_t>(i) * (PH_COUNT + 1));
     ctx->cur ^= 1;
     ctx->collided = true;
+    std::fill(ctx->sorted.begin(), ctx->sorted.end(), 1);
     for (int r = 0; r < ctx->n_rep; ++r) {
       const RepInfo& ri = ctx->reps[r];
       RepDyn& dn = ctx->dyn[r];
@@ -1090,6 +1100,7 @@ int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int reference_veloc
   if (int rc = check_rep(ctx, rep)) return rc;
   cudaSetDevice(ctx->device);
   const RepInfo& ri = ctx->reps[rep];
+  ctx->sorted[rep] = 0;
   if (ctx->opt.precision == SMPC_FP64)
     smpc::launch_init_solvent<double>(ctx->d_reps, rep, ri.slot_cap,
                                       static_cast<double*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
@@ -1187,6 +1198,58 @@ int smpc_cell_counts(smpc_ctx* ctx, int rep, unsigned* total, unsigned* fluid) {
     if (total) total[c] = tot;
     if (fluid) fluid[c] = tot - mono[c];
   }
+  return SMPC_OK;
+}
+
+int smpc_cell_members(smpc_ctx* ctx, int rep, int* fluid_cell, int* mono_cell) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (!ctx->sorted[rep])
+    return fail(ctx, SMPC_E_STATE, "no collision since the last binning or solvent upload");
+  const RepInfo& ri = ctx->reps[rep];
+  std::vector<uint32_t> off(ri.n_cell + 1);
+  CU(cudaMemcpyAsync(off.data(), ctx->d_off + ri.cell_base, (ri.n_cell + 1) * sizeof(uint32_t),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  std::vector<uint2> mk(ri.n_mono);
+  if (ri.n_mono && mono_cell)
+    CU(cudaMemcpyAsync(mk.data(), ctx->d_mkey + ri.mono_base, ri.n_mono * sizeof(uint2),
+                       cudaMemcpyDeviceToHost, ctx->st));
+  // the id word of every record: after a collision, slot p of the replica holds
+  // the particle at sorted position p, so p's cell is the one whose range
+  // [off[c], off[c+1]) contains it
+  const size_t rec_w = ctx->opt.precision == SMPC_FP64 ? sizeof(double) : sizeof(float);
+  std::vector<unsigned char> ids(static_cast<size_t>(ri.slot_cap) * rec_w);
+  if (fluid_cell && ri.slot_cap)
+    CU(cudaMemcpy2DAsync(ids.data(), rec_w,
+                         static_cast<const char*>(ctx->d_rec[ctx->cur]) +
+                             (8 * static_cast<size_t>(ri.slot_base) + 3) * rec_w,
+                         8 * rec_w, rec_w, ri.slot_cap, cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  if (mono_cell)
+    for (int m = 0; m < ri.n_mono; ++m)
+      mono_cell[m] = mk[m].x == smpc::KEY_NONE ? -1 : static_cast<int>(mk[m].x - ri.cell_base);
+  if (!fluid_cell) return SMPC_OK;
+  for (int i = 0; i < ri.n_fluid; ++i) fluid_cell[i] = -1;
+  int c = 0;
+  for (int i = 0; i < ri.slot_cap; ++i) {
+    const uint32_t p = static_cast<uint32_t>(ri.slot_base + i);
+    while (c < ri.n_cell && off[c + 1] <= p) ++c;
+    uint32_t id;
+    if (rec_w == sizeof(double)) {
+      double w;
+      std::memcpy(&w, ids.data() + i * rec_w, sizeof w);
+      id = id_of<double>(w);
+    } else {
+      float w;
+      std::memcpy(&w, ids.data() + i * rec_w, sizeof w);
+      id = id_of<float>(w);
+    }
+    if (id == smpc::SLOT_EMPTY) continue;
+    if (id >= static_cast<uint32_t>(ri.n_fluid) || c >= ri.n_cell || fluid_cell[id] != -1)
+      return fail(ctx, SMPC_E_STATE, "solvent records are not in cell order");
+    fluid_cell[id] = c;
+  }
+  for (int i = 0; i < ri.n_fluid; ++i)
+    if (fluid_cell[i] < 0) return fail(ctx, SMPC_E_DEVICE, "solvent particle missing from the records");
   return SMPC_OK;
 }
 

@@ -85,7 +85,7 @@ def run_scenario(name: str, sc: dict) -> dict:
         out.update(mono_pos0=m0["pos"], mono_vel0=m0["vel"], mono_force0=m0["force"],
                    mono_mass=m0["mass"], mono_amphi=m0["amphi"], mono_anchor=m0["anchor"])
     shifts, gammas, uphis, uths, tots, fls, steps = [], [], [], [], [], [], []
-    fl_pos, fl_vel, temps = [], [], []
+    fl_pos, fl_vel, temps, fl_cell, mo_cell = [], [], [], [], []
     m_pos, m_vel, m_frc, delrx, epots = [], [], [], [], []
     for t in range(sc["n_loop"]):
         if st and sc["with_md"]:
@@ -103,6 +103,8 @@ def run_scenario(name: str, sc: dict) -> dict:
                 p, v = ref.get_fluid()
                 fl_pos.append(p); fl_vel.append(v)
                 temps.append(ref.temperature())
+                fc, mc = ref.cell_index()
+                fl_cell.append(fc); mo_cell.append(mc)
         delrx.append(ref.delrx)
         if st:
             m = ref.get_monomers()
@@ -113,7 +115,8 @@ def run_scenario(name: str, sc: dict) -> dict:
         out.update(shift=np.array(shifts), gamma=np.array(gammas), u_phi=np.array(uphis),
                    u_theta=np.array(uths), count_total=np.array(tots), count_fluid=np.array(fls),
                    fluid_pos=np.array(fl_pos), fluid_vel=np.array(fl_vel),
-                   temperature=np.array(temps))
+                   temperature=np.array(temps), fluid_cell=np.array(fl_cell),
+                   mono_cell=np.array(mo_cell))
     if st:
         out.update(mono_pos=np.array(m_pos), mono_vel=np.array(m_vel), mono_force=np.array(m_frc),
                    gyration=ref.gyration())

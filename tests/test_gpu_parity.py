@@ -43,6 +43,9 @@ def test_fp64_replays_reference_fixture(path):
                     tot, fl = ctx.cell_counts(0)
                     np.testing.assert_array_equal(tot, fx["count_total"][k])
                     np.testing.assert_array_equal(fl, fx["count_fluid"][k])
+                    fc, mc = ctx.cell_members(0)
+                    np.testing.assert_array_equal(fc, fx["fluid_cell"][k])
+                    np.testing.assert_array_equal(mc, fx["mono_cell"][k])
                     p, v = ctx.get_fluid(0)
                     H.close64(p, fx["fluid_pos"][k])
                     H.close64(v, fx["fluid_vel"][k])
@@ -279,6 +282,13 @@ def test_batched_fp32_tracks_fp64_oracle():
             bad = (dp > 1e-4 * s.L) | (dv > 1e-3 * vs)
             assert bad.mean() < 0.03, (k, bad.mean())
             assert abs(ctx.temperature(k) - o.temperature()) < 0.01
+            # the fast path's cell-ordered records give the same membership as its counts
+            tot, fl = ctx.cell_counts(k)
+            fc, mc = ctx.cell_members(k)
+            n = len(tot)
+            np.testing.assert_array_equal(np.bincount(fc, minlength=n), fl)
+            np.testing.assert_array_equal(np.bincount(fc, minlength=n) +
+                                          np.bincount(mc[mc >= 0], minlength=n), tot)
 
 
 def test_fp32_launch_variants_agree_bitwise():
@@ -350,8 +360,13 @@ def test_two_phase_step_replays_reference(golden_dir, name):
                 tot, fl = ctx.cell_counts(0)
                 np.testing.assert_array_equal(tot, fx["count_total"][k])
                 np.testing.assert_array_equal(fl, fx["count_fluid"][k])
+                with pytest.raises(capi.SmpcError):
+                    ctx.cell_members(0)  # records are reordered only by the collision
                 ctx.mpc_collide(np.nan_to_num(fx["gamma"][k]), fx["u_phi"][k], fx["u_theta"][k])
                 ctx.raise_on_device_error()
+                fc, mc = ctx.cell_members(0)
+                np.testing.assert_array_equal(fc, fx["fluid_cell"][k])
+                np.testing.assert_array_equal(mc, fx["mono_cell"][k])
                 p, v = ctx.get_fluid(0)
                 H.close64(p, fx["fluid_pos"][k])
                 H.close64(v, fx["fluid_vel"][k])
