@@ -165,6 +165,16 @@ int smpc_temperature(smpc_ctx* ctx, int rep, double* out);   /* MPC.cpp:405-409 
 int smpc_epot(smpc_ctx* ctx, int rep, double* out);          /* sum of Molecule::Epot */
 /* Temperature of every replica (out[n_rep]) from one kernel launch. */
 int smpc_temperature_all(smpc_ctx* ctx, double* out);
+/* smpc_temperature_all without allocating anything, device or host (no
+ * counterpart in the reference, whose temperature is a host loop): the
+ * per-tile partial sums and per-replica results live in one static device
+ * array of 544 KB, at most 32768 temperature tiles (512 cells each, 16.7 M
+ * cells) and 4096 replicas per context; larger contexts get
+ * SMPC_E_UNSUPPORTED. For callers that cannot allocate mid-run. The first call
+ * on a device looks up the array's address (set-up); make it before any
+ * stream capture. The array is shared by every context of the process on that
+ * device: calls that overlap in time race on it. */
+int smpc_temperature_all_noalloc(smpc_ctx* ctx, double* out);
 /* Monomer positions/velocities of all replicas (concatenated, x,y,z
  * interleaved): the Box::Molecules state a host-side driver reads and writes
  * between steps (star-polymers.cpp:466-519). Masses and types are kept. */

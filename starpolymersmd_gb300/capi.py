@@ -32,7 +32,8 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_temperature", "smpc_epot", "smpc_delrx", "smpc_set_delrx",
            "smpc_cell_counts", "smpc_cell_members", "smpc_set_collision_counter", "smpc_verlet_rebuilds",
            "smpc_error_word", "smpc_synchronize", "smpc_cycles_profiled", "smpc_time_cycles",
-           "smpc_init_solvent", "smpc_temperature_all", "smpc_set_monomer_state_all",
+           "smpc_init_solvent", "smpc_temperature_all", "smpc_temperature_all_noalloc",
+           "smpc_set_monomer_state_all",
            "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
            "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide")
 
@@ -105,6 +106,7 @@ def load(path: Optional[str] = None):
         "smpc_time_cycles": ([P, I, C.POINTER(D)], I),
         "smpc_init_solvent": ([P, I, C.c_uint64, I], I),
         "smpc_temperature_all": ([P, P], I),
+        "smpc_temperature_all_noalloc": ([P, P], I),
         "smpc_set_monomer_state_all": ([P, P, P], I),
         "smpc_get_monomer_state_all": ([P, P, P, P], I),
         "smpc_set_variants": ([P, I, I, I], I),

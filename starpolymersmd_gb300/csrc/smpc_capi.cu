@@ -594,6 +594,80 @@ int dispatch_collision(smpc_ctx* ctx, int rng) {
   return SMPC_OK;
 }
 
+// ------------------------------------------------- allocation-free temperatures
+// smpc_temperature_all_noalloc: the same per-tile kernel as
+// smpc_temperature_all, with its partial sums and the per-replica results in
+// this file-scope device array instead of context buffers and host vectors,
+// and the per-replica sums done on the device. It is for callers that must
+// not allocate while a run is in flight: a driver that has handed the rest of
+// the GPU's memory to its own pool (a cudaMalloc can then fail mid-run), or
+// one that polls the temperature from a tight loop where cudaFree would
+// synchronise the device. Layout: kNoallocMaxTiles TempPartial, then
+// kNoallocMaxReps doubles. Every slot a call reads was written earlier in the
+// same call, so nothing has to start at zero. There is one array per device
+// (per process), shared by all contexts: calls that overlap in time, from two
+// threads or on two streams, race on it.
+constexpr int kNoallocMaxTiles = 32768;  // 16.7 M cells at 512 cells per tile
+constexpr int kNoallocMaxReps = 4096;
+constexpr size_t kNoallocScratchBytes =
+    kNoallocMaxTiles * sizeof(TempPartial) + kNoallocMaxReps * sizeof(double);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+constexpr int kNoallocMaxDevices = 64;
+void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the first call may load the module; it does not allocate).
+cudaError_t noalloc_scratch(int device, void** out) {
+  if (device < 0 || device >= kNoallocMaxDevices) return cudaErrorInvalidDevice;
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return cudaSuccess;
+}
+
+// One thread per replica: its tiles' partial sums in tile order, then
+// T = 2 E / (3 (N_solvent - filled cells)) (MPC.cpp:405-409), the same FP64
+// operations in the same order as the host sum of smpc_temperature_all.
+__global__ void k_temperature_finish(const Tile* tiles, int n_tiles, const RepInfo* reps,
+                                     int n_rep, const TempPartial* part, double* out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rep) return;
+  double e = 0.0;
+  unsigned filled = 0;
+  for (int t = 0; t < n_tiles; ++t)
+    if (tiles[t].rep == r) {
+      e += part[t].ekin;
+      filled += part[t].filled;
+    }
+  const unsigned nf = static_cast<unsigned>(reps[r].n_fluid);
+  out[r] = 2. * e / (3. * static_cast<unsigned>(nf - filled));
+}
+
+template <typename R>
+int temperature_all_noalloc_t(smpc_ctx* ctx, double* out) {
+  void* base = nullptr;
+  CU(noalloc_scratch(ctx->device, &base));
+  TempPartial* part = static_cast<TempPartial*>(base);
+  double* res = reinterpret_cast<double*>(static_cast<unsigned char*>(base) +
+                                          kNoallocMaxTiles * sizeof(TempPartial));
+  const int nt = static_cast<int>(ctx->h_tmp_tiles.size());
+  smpc::launch_temperature<R>(ctx->d_tmp_tiles, nt, ctx->d_reps, ctx->d_off, ctx->d_perm,
+                              static_cast<R*>(ctx->d_rec[ctx->cur]), static_cast<R*>(ctx->d_mpos),
+                              static_cast<R*>(ctx->d_mvel), ctx->d_mimg, ctx->opt.mono_bin, part,
+                              ctx->st);
+  k_temperature_finish<<<(ctx->n_rep + 127) / 128, 128, 0, ctx->st>>>(
+      ctx->d_tmp_tiles, nt, ctx->d_reps, ctx->n_rep, part, res);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out, res, ctx->n_rep * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1124,6 +1198,22 @@ int smpc_temperature_all(smpc_ctx* ctx, double* out) {
   if (!ctx || !out) return SMPC_E_ARG;
   return ctx->opt.precision == SMPC_FP64 ? temperature_all_t<double>(ctx, out)
                                          : temperature_all_t<float>(ctx, out);
+}
+
+int smpc_temperature_all_noalloc(smpc_ctx* ctx, double* out) {
+  if (!ctx || !out) return SMPC_E_ARG;
+  if (static_cast<long>(ctx->h_tmp_tiles.size()) > kNoallocMaxTiles ||
+      ctx->n_rep > kNoallocMaxReps)
+    return fail(ctx, SMPC_E_UNSUPPORTED,
+                "smpc_temperature_all_noalloc: context has " +
+                    std::to_string(ctx->h_tmp_tiles.size()) + " temperature tiles and " +
+                    std::to_string(ctx->n_rep) + " replicas; the static scratch holds at most " +
+                    std::to_string(kNoallocMaxTiles) + " tiles (512 cells each) and " +
+                    std::to_string(kNoallocMaxReps) + " replicas");
+  if (!ctx->collided) return fail(ctx, SMPC_E_STATE, "no collision has run yet (no cell lists)");
+  cudaSetDevice(ctx->device);
+  return ctx->opt.precision == SMPC_FP64 ? temperature_all_noalloc_t<double>(ctx, out)
+                                         : temperature_all_noalloc_t<float>(ctx, out);
 }
 
 int smpc_set_monomer_state_all(smpc_ctx* ctx, const double* pos, const double* vel) {
