@@ -11,6 +11,12 @@
 // computed per bead over its own Verlet list and its own undirected bond
 // list, so no atomics and no write conflicts; the reference's directed bond
 // (F_src -= f d, F_dst += f d) is the same force seen from both ends.
+//
+// With KMAX > 1 (one bead per thread, MPT = 1) a replica with n beads gives
+// each bead k = the largest power of two <= min(KMAX, NT / n) adjacent lanes:
+// all k hold the bead's state, each walks every k-th entry of its Verlet
+// list, and a butterfly over the k lanes sums the partial forces. Small
+// replicas then use the whole CTA instead of n of its threads.
 #pragma once
 #include <stdint.h>
 
@@ -104,6 +110,7 @@ struct MdArgs {
   int force_rebuild;
   int core_relative;       // fast path: displacements measured relative to the core's
   ErrorState* err;
+  const int* order;        // replica of each CTA (largest first), or null: CTA b = replica b
 };
 
 // Cell key of a position on a grid of side rv: three 10-bit fields
@@ -119,9 +126,10 @@ __device__ __forceinline__ int md_bucket(int cx, int cy, int cz) {
          (MD_BUCKETS - 1);
 }
 
-template <typename R, int NT, int MPT>
+template <typename R, int NT, int MPT, int KMAX = 1>
 __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, R* mfrc,
                                                     R* mver) {
+  static_assert(KMAX == 1 || MPT == 1, "lanes per bead > 1 needs one bead per thread");
   constexpr int CAP = NT * MPT;
   __shared__ R sx[CAP], sy[CAP], sz[CAP];
   __shared__ unsigned char s_amphi[CAP];
@@ -131,10 +139,16 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
   __shared__ R s_core_ref[3];
   __shared__ int s_rebuild;
   __shared__ double s_red[NT / 32];
-  const int r = blockIdx.x;
+  const int r = a.order ? a.order[blockIdx.x] : static_cast<int>(blockIdx.x);
   const RepInfo ri = a.reps[r];
   const int n = ri.n_mono;
   if (n == 0) return;
+  int lk = 0;  // log2 of the lanes per bead
+  if (KMAX > 1)
+    while ((2 << lk) <= KMAX && (n << (lk + 1)) <= NT) ++lk;
+  const int sub = static_cast<int>(threadIdx.x) & ((1 << lk) - 1);
+  const int slot = static_cast<int>(threadIdx.x) >> lk;  // bead of this lane (k = 0)
+  const bool lead = sub == 0;
   const int b = ri.mono_base;
   const R dt = static_cast<R>(ri.md_dt);
   const R dth = dt * R(0.50);
@@ -147,18 +161,20 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
   int anc[MPT];
 #pragma unroll
   for (int k = 0; k < MPT; ++k) {
-    const int i = threadIdx.x + k * NT;
+    const int i = slot + k * NT;
     if (i < n) {
       const R4<R> p = ld4_rw(mpos, b + i), vv = ld4_rw(mvel, b + i), ff = ld4_rw(mfrc, b + i),
                   pv = ld4_rw(mver, b + i);
       x[k][0] = p.x; x[k][1] = p.y; x[k][2] = p.z; m[k] = p.w;
       v[k][0] = vv.x; v[k][1] = vv.y; v[k][2] = vv.z;
       const int flags = static_cast<int>(vv.w);
-      s_amphi[i] = static_cast<unsigned char>(flags & 1);
       anc[k] = (flags >> 1) & 1;
       f[k][0] = ff.x; f[k][1] = ff.y; f[k][2] = ff.z;
       xv[k][0] = pv.x; xv[k][1] = pv.y; xv[k][2] = pv.z;
-      sx[i] = p.x; sy[i] = p.y; sz[i] = p.z;
+      if (lead) {
+        s_amphi[i] = static_cast<unsigned char>(flags & 1);
+        sx[i] = p.x; sy[i] = p.y; sz[i] = p.z;
+      }
     }
   }
   if (threadIdx.x == 0) {
@@ -176,13 +192,13 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
       // kick + drift (Thermostat_None.cpp:22-27)
 #pragma unroll
       for (int k = 0; k < MPT; ++k) {
-        const int i = threadIdx.x + k * NT;
+        const int i = slot + k * NT;
         if (i < n) {
           for (int d = 0; d < 3; ++d) {
             v[k][d] += (f[k][d] / m[k]) * dth;
             x[k][d] += v[k][d] * dt;
           }
-          sx[i] = x[k][0]; sy[i] = x[k][1]; sz[i] = x[k][2];
+          if (lead) { sx[i] = x[k][0]; sy[i] = x[k][1]; sz[i] = x[k][2]; }
           if (!a.core_relative) {
             // Box::check_VerletLists (Box.cpp:182-194)
             const R d0 = x[k][0] - xv[k][0], d1 = x[k][1] - xv[k][1], d2 = x[k][2] - xv[k][2];
@@ -198,7 +214,7 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
         const R c0 = sx[0] - s_core_ref[0], c1 = sy[0] - s_core_ref[1], c2 = sz[0] - s_core_ref[2];
 #pragma unroll
         for (int k = 0; k < MPT; ++k) {
-          const int i = threadIdx.x + k * NT;
+          const int i = slot + k * NT;
           if (i < n) {
             const R d0 = x[k][0] - xv[k][0] - c0, d1 = x[k][1] - xv[k][1] - c1,
                     d2 = x[k][2] - xv[k][2] - c2;
@@ -219,20 +235,22 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
       int cx[MPT], cy[MPT], cz[MPT];
 #pragma unroll
       for (int k = 0; k < MPT; ++k) {
-        const int i = threadIdx.x + k * NT;
+        const int i = slot + k * NT;
         if (i < n) {
           cx[k] = static_cast<int>(floor(x[k][0] * inv_rv));
           cy[k] = static_cast<int>(floor(x[k][1] * inv_rv));
           cz[k] = static_cast<int>(floor(x[k][2] * inv_rv));
-          s_ckey[i] = md_cell_key(cx[k], cy[k], cz[k]);
-          s_next[i] = atomicExch(&s_head[md_bucket(cx[k], cy[k], cz[k])], i);
+          if (lead) {
+            s_ckey[i] = md_cell_key(cx[k], cy[k], cz[k]);
+            s_next[i] = atomicExch(&s_head[md_bucket(cx[k], cy[k], cz[k])], i);
+          }
         }
       }
       __syncthreads();
 #pragma unroll
       for (int k = 0; k < MPT; ++k) {
-        const int i = threadIdx.x + k * NT;
-        if (i < n) {
+        const int i = slot + k * NT;
+        if (i < n && lead) {
           int cnt = 0;
           for (int dz = -1; dz <= 1; ++dz)
             for (int dy = -1; dy <= 1; ++dy)
@@ -255,8 +273,8 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
             cnt = a.max_nb;
           }
           a.ncount[b + i] = cnt;
-          xv[k][0] = x[k][0]; xv[k][1] = x[k][1]; xv[k][2] = x[k][2];
         }
+        if (i < n) { xv[k][0] = x[k][0]; xv[k][1] = x[k][1]; xv[k][2] = x[k][2]; }
       }
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -269,20 +287,24 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
     // forces (Box.cpp:243-286)
 #pragma unroll
     for (int k = 0; k < MPT; ++k) {
-      const int i = threadIdx.x + k * NT;
+      const int i = slot + k * NT;
+      R F0 = R(0), F1 = R(0), F2 = R(0);
       if (i < n) {
-        R F0 = R(0), F1 = R(0), F2 = R(0);
         const bool ai = s_amphi[i] != 0;
         const int cnt = a.ncount[b + i];
         const int* nl = a.nlist + b + i;
         const size_t stride = static_cast<size_t>(a.n_mono_total);
         // neighbour indices come in groups of four independent loads, so the
-        // list walk is not a chain of dependent L2 round trips
+        // list walk is not a chain of dependent L2 round trips; the lanes of
+        // a bead take every (1 << lk)-th entry
         constexpr int PF = 4;
-        for (int q0 = 0; q0 < cnt; q0 += PF) {
+        for (int q0 = sub; q0 < cnt; q0 += PF << lk) {
           int js[PF];
 #pragma unroll
-          for (int u = 0; u < PF; ++u) js[u] = q0 + u < cnt ? nl[static_cast<size_t>(q0 + u) * stride] - b : -1;
+          for (int u = 0; u < PF; ++u) {
+            const int q = q0 + (u << lk);
+            js[u] = q < cnt ? nl[static_cast<size_t>(q) * stride] - b : -1;
+          }
 #pragma unroll
           for (int u = 0; u < PF; ++u) {
             const int j = js[u];
@@ -297,7 +319,7 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
             if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
           }
         }
-        for (int e = a.bond_start[b + i]; e < a.bond_start[b + i + 1]; ++e) {
+        for (int e = lead ? a.bond_start[b + i] : 0; lead && e < a.bond_start[b + i + 1]; ++e) {
           const int2 bd = a.bonds[e];
           const int j = bd.x - b;
           const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
@@ -319,6 +341,14 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
           F2 -= d2 * fa;
           if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2f));
         }
+      }
+      // partial forces of a bead's lanes (every lane of the warp takes part)
+      for (int o = 1; KMAX > 1 && o < (1 << lk); o <<= 1) {
+        F0 += __shfl_xor_sync(0xFFFFFFFFu, F0, o);
+        F1 += __shfl_xor_sync(0xFFFFFFFFu, F1, o);
+        F2 += __shfl_xor_sync(0xFFFFFFFFu, F2, o);
+      }
+      if (i < n) {
         f[k][0] = F0; f[k][1] = F1; f[k][2] = F2;
         if (a.n_steps > 0)
           for (int d = 0; d < 3; ++d) v[k][d] += (f[k][d] / m[k]) * dth;  // second half-kick
@@ -329,8 +359,8 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
   // write back
 #pragma unroll
   for (int k = 0; k < MPT; ++k) {
-    const int i = threadIdx.x + k * NT;
-    if (i < n) {
+    const int i = slot + k * NT;
+    if (i < n && lead) {
       R4<R> p = ld4_rw(mpos, b + i);
       p.x = x[k][0]; p.y = x[k][1]; p.z = x[k][2];
       st4(mpos, b + i, p);

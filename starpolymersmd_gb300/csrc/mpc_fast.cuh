@@ -183,63 +183,46 @@ __device__ __forceinline__ void frame_f(FastP& P, const FrameF& f, float solvent
   P.v.w = solvent_mass;
 }
 
-template <int NT, int CT, int CAP, int GU>
-__global__ void __launch_bounds__(NT) k_collide_f32(
-    const Tile* tiles, const RepInfo* reps, const FrameF* frames, const RepDyn* dyn,
-    const uint32_t* __restrict__ off, const uint32_t* __restrict__ perm,
-    const float* __restrict__ st_in, float* __restrict__ st_out, const float* mpos, float* mvel,
-    const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
-    int rng, int mono_bin, ErrorState* err) {
-  static_assert(NT == 2 * CT, "two threads per cell");
-  __shared__ float s_cmv[CT * 3];
-  __shared__ float s_rot[CT * 9];
-  __shared__ uint32_t s_off[CT + 1];
-  extern __shared__ __align__(16) unsigned char s_dyn[];
-  float4* s_x = reinterpret_cast<float4*>(s_dyn);
-  float4* s_v = s_x + CAP;
-  short* s_lc = reinterpret_cast<short*>(s_v + CAP);
+// Per-tile work shared by the collide kernels. Staged particles sit in
+// s_x/s_v[0, nloc) in sorted order; sorted position p0 + j belongs to the
+// tile's local cell lc with s_off[lc] <= p0 + j < s_off[lc + 1]. Entries at
+// nloc and beyond (a tile fuller than the staging capacity) are read from
+// global memory again.
+struct CollideF32Args {
+  const float* st_in;
+  float* st_out;
+  const float* mpos;
+  float* mvel;
+  const int* mimg;
+  const uint32_t* perm;
+  const double* inj_gamma;
+  const double* inj_uphi;
+  const double* inj_utheta;
+  int rng;
+  int mono_bin;
+  ErrorState* err;
+};
 
-  const Tile t = tiles[blockIdx.x];
-  const FrameF f = frames[t.rep];
-  const RepInfo& ri = reps[t.rep];
-  const unsigned long long seed = ri.seed;
-  const unsigned long long step = dyn[t.rep].step;
-  const uint32_t cbase = static_cast<uint32_t>(ri.cell_base);
-  const int nc = t.end - t.begin;
-
-  for (int i = threadIdx.x; i <= nc; i += NT) s_off[i] = off[t.begin + i];
-  __syncthreads();
-  const uint32_t p0 = s_off[0], p1 = s_off[nc];
-  const int n = static_cast<int>(p1 - p0);
-  const int nloc = n < CAP ? n : CAP;
-
-  // stage: gather, stream, collision-frame velocity
-  for (int base = 0; base < nloc; base += NT * GU) {
-    uint32_t src[GU];
-#pragma unroll
-    for (int u = 0; u < GU; ++u) {
-      const int j = base + u * NT + threadIdx.x;
-      src[u] = j < nloc ? perm[p0 + j] : 0u;
-    }
-    FastP P[GU];
-#pragma unroll
-    for (int u = 0; u < GU; ++u) {
-      const int j = base + u * NT + threadIdx.x;
-      if (j < nloc) fetch_f(P[u], src[u], st_in, mpos, mvel, mimg, f, mono_bin);
-    }
-#pragma unroll
-    for (int u = 0; u < GU; ++u) {
-      const int j = base + u * NT + threadIdx.x;
-      if (j < nloc) {
-        frame_f(P[u], f, f.solvent_mass);
-        s_x[j] = P[u].x;
-        s_v[j] = P[u].v;
-      }
-    }
-  }
-  __syncthreads();
-
-  // cells: two lanes per cell; int64 2^32 fixed-point sums (exact, order-free)
+// cells: two lanes per cell; int64 2^32 fixed-point sums (exact, order-free),
+// then the thermostat scale and the rotation (folded together) per cell
+template <int NT>
+__device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const FrameF& f,
+                                                  const Tile& t, const uint32_t* s_off, int nc,
+                                                  uint32_t p0, int nloc, const float4* s_x,
+                                                  const float4* s_v, short* s_lc, float* s_cmv,
+                                                  float* s_rot, unsigned long long seed,
+                                                  unsigned long long step, uint32_t cbase) {
+  const float* st_in = A.st_in;
+  const float* mpos = A.mpos;
+  const float* mvel = A.mvel;
+  const int* mimg = A.mimg;
+  const uint32_t* perm = A.perm;
+  const int mono_bin = A.mono_bin;
+  const int rng = A.rng;
+  const double* inj_gamma = A.inj_gamma;
+  const double* inj_uphi = A.inj_uphi;
+  const double* inj_utheta = A.inj_utheta;
+  ErrorState* err = A.err;
   {
     const int lc = threadIdx.x >> 1;
     const int half = threadIdx.x & 1;
@@ -349,9 +332,23 @@ __global__ void __launch_bounds__(NT) k_collide_f32(
       s_cmv[3 * lc + 2] = cm2;
     }
   }
-  __syncthreads();
+}
 
-  // apply: v' = cmv + sR (v - cmv), back to the primary box, write in cell order
+// apply: v' = cmv + sR (v - cmv), back to the primary box, write in cell order
+template <int NT>
+__device__ __forceinline__ void collide_apply_f32(const CollideF32Args& A, const FrameF& f,
+                                                  const uint32_t* s_off, uint32_t p0, int n,
+                                                  int nloc, const float4* s_x, const float4* s_v,
+                                                  const short* s_lc, const float* s_cmv,
+                                                  const float* s_rot) {
+  const float* st_in = A.st_in;
+  float* st_out = A.st_out;
+  const float* mpos = A.mpos;
+  float* mvel = A.mvel;
+  const int* mimg = A.mimg;
+  const uint32_t* perm = A.perm;
+  const int mono_bin = A.mono_bin;
+  ErrorState* err = A.err;
   for (int j = threadIdx.x; j < n; j += NT) {
     float4 x, v;
     int lc;
@@ -406,6 +403,213 @@ __global__ void __launch_bounds__(NT) k_collide_f32(
       st_f4(st_out, 2 * p, make_float4(X, Y, Z, x.w));
       st_f4(st_out, 2 * p + 1, make_float4(vx, vy, vz, 0.f));
     }
+  }
+}
+
+template <int NT, int CT, int CAP, int GU>
+__global__ void __launch_bounds__(NT) k_collide_f32(
+    const Tile* tiles, const RepInfo* reps, const FrameF* frames, const RepDyn* dyn,
+    const uint32_t* __restrict__ off, const uint32_t* __restrict__ perm,
+    const float* __restrict__ st_in, float* __restrict__ st_out, const float* mpos, float* mvel,
+    const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
+    int rng, int mono_bin, ErrorState* err) {
+  static_assert(NT == 2 * CT, "two threads per cell");
+  __shared__ float s_cmv[CT * 3];
+  __shared__ float s_rot[CT * 9];
+  __shared__ uint32_t s_off[CT + 1];
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  float4* s_x = reinterpret_cast<float4*>(s_dyn);
+  float4* s_v = s_x + CAP;
+  short* s_lc = reinterpret_cast<short*>(s_v + CAP);
+
+  const Tile t = tiles[blockIdx.x];
+  const FrameF f = frames[t.rep];
+  const RepInfo& ri = reps[t.rep];
+  const unsigned long long seed = ri.seed;
+  const unsigned long long step = dyn[t.rep].step;
+  const uint32_t cbase = static_cast<uint32_t>(ri.cell_base);
+  const int nc = t.end - t.begin;
+
+  for (int i = threadIdx.x; i <= nc; i += NT) s_off[i] = off[t.begin + i];
+  __syncthreads();
+  const uint32_t p0 = s_off[0], p1 = s_off[nc];
+  const int n = static_cast<int>(p1 - p0);
+  const int nloc = n < CAP ? n : CAP;
+
+  // stage: gather, stream, collision-frame velocity
+  for (int base = 0; base < nloc; base += NT * GU) {
+    uint32_t src[GU];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      src[u] = j < nloc ? perm[p0 + j] : 0u;
+    }
+    FastP P[GU];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      if (j < nloc) fetch_f(P[u], src[u], st_in, mpos, mvel, mimg, f, mono_bin);
+    }
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int j = base + u * NT + threadIdx.x;
+      if (j < nloc) {
+        frame_f(P[u], f, f.solvent_mass);
+        s_x[j] = P[u].x;
+        s_v[j] = P[u].v;
+      }
+    }
+  }
+  __syncthreads();
+
+  const CollideF32Args A{st_in, st_out, mpos, mvel, mimg, perm, inj_gamma, inj_uphi, inj_utheta,
+                         rng, mono_bin, err};
+  collide_cells_f32<NT>(A, f, t, s_off, nc, p0, nloc, s_x, s_v, s_lc, s_cmv, s_rot, seed, step,
+                        cbase);
+  __syncthreads();
+  collide_apply_f32<NT>(A, f, s_off, p0, n, nloc, s_x, s_v, s_lc, s_cmv, s_rot);
+}
+
+// ------------------------------------------------- collide, pipelined
+// Persistent variant of k_collide_f32: each CTA walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... and gathers the particles of its next tile
+// with cp.async into the second of two shared-memory buffers while it
+// computes the current one, so the dependent loads (offsets -> sorted
+// slots -> records) of one tile overlap the arithmetic of the previous one.
+// The arithmetic is the same as k_collide_f32's, so both give identical bits.
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+constexpr size_t collide_f32_pipe_dyn_smem(int cap) {
+  return static_cast<size_t>(cap) * (4 * sizeof(float4) + sizeof(short));
+}
+
+template <int NT, int CT, int CAP>
+__global__ void __launch_bounds__(NT) k_collide_f32_pipe(
+    const Tile* tiles, int n_tiles, const RepInfo* reps, const FrameF* frames, const RepDyn* dyn,
+    const uint32_t* __restrict__ off, const uint32_t* __restrict__ perm,
+    const float* __restrict__ st_in, float* __restrict__ st_out, const float* mpos, float* mvel,
+    const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
+    int rng, int mono_bin, ErrorState* err) {
+  static_assert(NT == 2 * CT, "two threads per cell");
+  constexpr int J = (CAP + NT - 1) / NT;  // staged particles per thread
+  __shared__ float s_cmv[CT * 3];
+  __shared__ float s_rot[CT * 9];
+  __shared__ uint32_t s_off[3][CT + 1];  // ring: current, next, the one after
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  float4* s_buf = reinterpret_cast<float4*>(s_dyn);  // [2][x: CAP, v: CAP]
+  short* s_lc = reinterpret_cast<short*>(s_buf + 4 * CAP);
+  const CollideF32Args A{st_in, st_out, mpos, mvel, mimg, perm, inj_gamma, inj_uphi, inj_utheta,
+                         rng, mono_bin, err};
+
+  int t = blockIdx.x;
+  if (t >= n_tiles) return;
+
+  auto load_off = [&](int tile, uint32_t* dst) {
+    const Tile T = tiles[tile];
+    const int nc = T.end - T.begin;
+    for (int i = threadIdx.x; i <= nc; i += NT) dst[i] = off[T.begin + i];
+  };
+  // sorted slots of this thread's staged particles (loads in flight on return)
+  auto load_perm = [&](int tile, const uint32_t* so, uint32_t* src) {
+    const Tile T = tiles[tile];
+    const int nc = T.end - T.begin;
+    const uint32_t p0 = so[0];
+    const int n = static_cast<int>(so[nc] - p0);
+    const int nloc = n < CAP ? n : CAP;
+#pragma unroll
+    for (int u = 0; u < J; ++u) {
+      const int j = u * NT + threadIdx.x;
+      src[u] = j < nloc ? perm[p0 + j] : 0xFFFFFFFFu;
+    }
+  };
+  auto gather = [&](const uint32_t* src, float4* bx) {
+#pragma unroll
+    for (int u = 0; u < J; ++u) {
+      const int j = u * NT + threadIdx.x;
+      if (src[u] == 0xFFFFFFFFu) continue;
+      if (src[u] & MONO_BIT) {
+        const uint32_t m = src[u] & ~MONO_BIT;
+        cp_async16(bx + CAP + j, mvel + 4 * static_cast<size_t>(m));
+        bx[j] = make_float4(0.f, 0.f, 0.f, __uint_as_float(src[u]));
+      } else {
+        cp_async16(bx + j, st_in + 8 * static_cast<size_t>(src[u]));
+        cp_async16(bx + CAP + j, st_in + 8 * static_cast<size_t>(src[u]) + 4);
+      }
+    }
+    cp_async_commit();
+  };
+
+  // prologue: offsets and gather of the first tile, offsets of the second
+  load_off(t, s_off[0]);
+  __syncthreads();
+  {
+    uint32_t src[J];
+    load_perm(t, s_off[0], src);
+    gather(src, s_buf);
+  }
+  int tn = t + static_cast<int>(gridDim.x);
+  if (tn < n_tiles) load_off(tn, s_off[1]);
+  int cur = 0, oi = 0;
+  while (true) {
+    __syncthreads();  // s_off of the next tile is visible; the other buffer is free
+    const bool has_next = tn < n_tiles;
+    uint32_t src[J];
+    if (has_next) load_perm(tn, s_off[(oi + 1) % 3], src);
+    cp_async_wait_all();  // this tile's gather (issued one tile ago)
+    __syncthreads();
+
+    const Tile T = tiles[t];
+    const FrameF f = frames[T.rep];
+    const RepInfo& ri = reps[T.rep];
+    const uint32_t* so = s_off[oi];
+    const int nc = T.end - T.begin;
+    const uint32_t p0 = so[0];
+    const int n = static_cast<int>(so[nc] - p0);
+    const int nloc = n < CAP ? n : CAP;
+    float4* s_x = s_buf + 2 * CAP * cur;
+    float4* s_v = s_x + CAP;
+    // stream and move into the collision frame, in place (fetch_f + frame_f)
+    for (int j = threadIdx.x; j < nloc; j += NT) {
+      FastP P;
+      P.x = s_x[j];
+      P.v = s_v[j];
+      const uint32_t tag = __float_as_uint(P.x.w);
+      if (tag & MONO_BIT) {
+        const uint32_t m = tag & ~MONO_BIT;
+        P.v.w = reinterpret_cast<const float4*>(mpos)[m].w;
+        if (mono_bin == MONOBIN_WRAPPED)
+          P.v.x = __fsub_rn(P.v.x, __fmul_rn(i2f_small(mimg[m]), f.shearLy));
+      } else {
+        frame_f(P, f, f.solvent_mass);
+      }
+      s_x[j] = P.x;
+      s_v[j] = P.v;
+    }
+    if (has_next) gather(src, s_buf + 2 * CAP * (cur ^ 1));
+    const int tnn = tn + static_cast<int>(gridDim.x);
+    if (tnn < n_tiles) load_off(tnn, s_off[(oi + 2) % 3]);
+    __syncthreads();
+
+    collide_cells_f32<NT>(A, f, T, so, nc, p0, nloc, s_x, s_v, s_lc, s_cmv, s_rot, ri.seed,
+                          dyn[T.rep].step, static_cast<uint32_t>(ri.cell_base));
+    __syncthreads();
+    collide_apply_f32<NT>(A, f, so, p0, n, nloc, s_x, s_v, s_lc, s_cmv, s_rot);
+
+    if (!has_next) break;
+    t = tn;
+    tn = tnn;
+    cur ^= 1;
+    oi = (oi + 1) % 3;
   }
 }
 

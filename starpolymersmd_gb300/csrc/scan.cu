@@ -104,17 +104,36 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_add(uint32_t* __restrict__ off
   if (i == n) off[n] = *grand;
 }
 
-__global__ void k_build_perm(const uint2* __restrict__ keys, int n_slots,
-                             const uint2* __restrict__ mkey, int n_mono,
-                             const uint32_t* __restrict__ off, uint32_t* __restrict__ perm) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n_slots) {
-    const uint2 k = keys[i];
-    if (k.x != KEY_NONE) perm[off[k.x] + k.y] = static_cast<uint32_t>(i);
-  } else if (i < n_slots + n_mono) {
-    const int m = i - n_slots;
-    const uint2 k = mkey[m];
-    if (k.x != KEY_NONE) perm[off[k.x] + k.y] = MONO_BIT | static_cast<uint32_t>(m);
+// perm[off[cell] + rank] = source. Each thread takes PERM_U entries a block
+// apart and issues all key loads, then all offset gathers, then the stores,
+// so PERM_U independent gather chains are in flight per thread.
+constexpr int PERM_NT = 256;
+constexpr int PERM_U = 4;
+__global__ void __launch_bounds__(PERM_NT) k_build_perm(const uint2* __restrict__ keys, int n_slots,
+                                                        const uint2* __restrict__ mkey, int n_mono,
+                                                        const uint32_t* __restrict__ off,
+                                                        uint32_t* __restrict__ perm) {
+  const int n = n_slots + n_mono;
+  const int base = blockIdx.x * (PERM_NT * PERM_U) + threadIdx.x;
+  uint2 k[PERM_U];
+#pragma unroll
+  for (int u = 0; u < PERM_U; ++u) {
+    const int i = base + u * PERM_NT;
+    k[u] = make_uint2(KEY_NONE, 0u);
+    if (i < n_slots)
+      k[u] = keys[i];
+    else if (i < n)
+      k[u] = mkey[i - n_slots];
+  }
+  uint32_t o[PERM_U];
+#pragma unroll
+  for (int u = 0; u < PERM_U; ++u) o[u] = k[u].x != KEY_NONE ? off[k[u].x] : 0u;
+#pragma unroll
+  for (int u = 0; u < PERM_U; ++u) {
+    const int i = base + u * PERM_NT;
+    if (k[u].x == KEY_NONE) continue;
+    perm[o[u] + k[u].y] =
+        i < n_slots ? static_cast<uint32_t>(i) : (MONO_BIT | static_cast<uint32_t>(i - n_slots));
   }
 }
 
@@ -133,7 +152,8 @@ void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_
                        const uint32_t* off, uint32_t* perm, cudaStream_t st) {
   const int n = n_slots + n_mono;
   if (n == 0) return;
-  k_build_perm<<<(n + 255) / 256, 256, 0, st>>>(keys, n_slots, mkey, n_mono, off, perm);
+  k_build_perm<<<(n + PERM_NT * PERM_U - 1) / (PERM_NT * PERM_U), PERM_NT, 0, st>>>(
+      keys, n_slots, mkey, n_mono, off, perm);
 }
 
 }  // namespace smpc

@@ -4,6 +4,7 @@
 // uploaded); the step calls allocate nothing.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -65,6 +66,7 @@ struct smpc_ctx {
   int2* d_bonds = nullptr;
   int* d_nlist = nullptr;
   int* d_ncount = nullptr;
+  int* d_md_order = nullptr;  // replicas by decreasing monomer count (MD CTA order)
   std::vector<std::vector<int>> bsrc, bdst;
   std::vector<std::vector<int>> anchor;
 
@@ -210,6 +212,7 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   a.force_rebuild = force_rebuild;
   a.core_relative = ctx->opt.strict_cells ? 0 : 1;
   a.err = ctx->d_err;
+  a.order = ctx->d_md_order;
   smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
                      static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->var_md,
                      ctx->st);
@@ -525,6 +528,17 @@ int create_buffers(smpc_ctx* ctx) {
   CU(dalloc(&ctx->d_mimg, M));
   CU(dalloc(&ctx->d_ncount, M));
   CU(cudaMemset(ctx->d_ncount, 0, (M ? M : 1) * sizeof(int)));
+  {
+    // largest replicas first, so the MD kernel's last wave holds small ones
+    std::vector<int> order(ctx->n_rep);
+    for (int r = 0; r < ctx->n_rep; ++r) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](int p, int q) {
+      return ctx->reps[p].n_mono > ctx->reps[q].n_mono;
+    });
+    CU(dalloc(&ctx->d_md_order, order.size()));
+    CU(cudaMemcpy(ctx->d_md_order, order.data(), order.size() * sizeof(int),
+                  cudaMemcpyHostToDevice));
+  }
   CU(dalloc(&ctx->d_nlist, static_cast<size_t>(ctx->max_nb) * M));
   CU(dalloc(&ctx->d_bond_start, M + 1));
   CU(cudaMemset(ctx->d_bond_start, 0, (M + 1) * sizeof(int)));
@@ -575,7 +589,7 @@ void free_all(smpc_ctx* ctx) {
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
                   ctx->d_mimg, ctx->d_bond_start, ctx->d_bonds, ctx->d_nlist, ctx->d_ncount,
-                  ctx->d_inj, ctx->d_err, ctx->d_frames};
+                  ctx->d_md_order, ctx->d_inj, ctx->d_err, ctx->d_frames};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);

@@ -306,7 +306,7 @@ def test_fp32_launch_variants_agree_bitwise():
         states.append((fp, fv))
     finals = []
     lib = capi.load()
-    n_bin, n_col = 4, 5
+    n_bin, n_col = 4, 7
     for vb, vc in [(0, 0)] + [(b, 0) for b in range(1, n_bin)] + [(0, c) for c in range(1, n_col)]:
         with capi.Context(reps, precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=1,
                           strict_cells=0) as ctx:
@@ -321,6 +321,24 @@ def test_fp32_launch_variants_agree_bitwise():
         for (p0, v0), (p1, v1) in zip(finals[0], other):
             np.testing.assert_array_equal(p0, p1)
             np.testing.assert_array_equal(v0, v1)
+
+
+def test_fp32_collide_variants_agree_bitwise_with_stars():
+    # the same with monomers in the cells (staged from the monomer arrays,
+    # written back to them), MD substeps in between
+    finals = []
+    for vc in range(7):
+        ctx, _, specs = _batch_run(capi.FP32, cycles=0)
+        with ctx:
+            ctx.set_variants(0, vc, 0)
+            ctx.cycles(3)
+            ctx.synchronize()
+            ctx.raise_on_device_error()
+            finals.append([ctx.get_fluid(k) + ctx.get_monomers(k)[:2] for k in range(len(specs))])
+    for other in finals[1:]:
+        for a, b in zip(finals[0], other):
+            for x, y in zip(a, b):
+                np.testing.assert_array_equal(x, y)
 
 
 def test_autotune_reports_and_keeps_a_variant():
@@ -371,3 +389,48 @@ def test_two_phase_step_replays_reference(golden_dir, name):
                 H.close64(p, fx["fluid_pos"][k])
                 H.close64(v, fx["fluid_vel"][k])
             assert ctx.delrx(0) == fx["delrx"][t]
+
+
+@pytest.mark.parametrize("md_variant", [0, 1, 2])
+def test_fp32_md_variants_track_fp64_oracle(md_variant):
+    # MD only (no collisions): every FP32 launch shape of the substep kernel,
+    # including the one that splits a bead's Verlet list over several lanes,
+    # follows the FP64 oracle to FP32 round-off over 20 substeps.
+    from starpolymersmd_gb300 import system, workloads as W
+    specs = _batch_specs() + [system.ReplicaSpec(L=16, arms=6, n_arm=20, solvophobic_fraction=0.3,
+                                                 shear=0.05, seed=34)]
+    stars, descs = [], []
+    for s in specs:
+        st = system.make_star(s.arms, s.n_arm, s.solvophobic_fraction, s.mono_mass, s.kT,
+                              np.random.default_rng(600 + s.seed), bond=0.97)
+        stars.append(st)
+        descs.append(W.replica_desc(s, st))
+    n_sub = 20
+    with capi.Context(descs, precision=capi.FP32, rng=capi.RNG_PHILOX,
+                      mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL,
+                      step_update=W.N_SUB, max_neighbors=W.MAX_NB, strict_cells=0) as ctx:
+        ctx.set_variants(0, 0, md_variant)
+        for k, st in enumerate(stars):
+            ctx.set_monomers(k, st.pos, st.vel, np.zeros_like(st.pos), np.full(st.n, st.mass),
+                             st.amphi, st.anchor)
+            ctx.set_bonds(k, st.bond_src, st.bond_dst)
+        ctx.init_md()
+        ctx.md_substeps(n_sub)
+        ctx.raise_on_device_error()
+        for k, (s, st) in enumerate(zip(specs, stars)):
+            o = orc.OracleSystem((s.L,) * 3, s.kT, s.shear, W.N_SUB, 0, st.n, mol_start=[0, st.n],
+                                 lambda_=1.0, md_dt=W.MD_DT, r_cut=W.R_CUT_LJ,
+                                 r_verlet=W.R_CUT_LJ + W.SKIN, potential=orc.POT_LJ126,
+                                 delrx_dt_scale=1.0 / W.N_SUB, mono_wrap=1)
+            o.set_monomers(st.pos, st.vel, np.zeros_like(st.pos), np.full(st.n, st.mass),
+                           st.amphi, st.anchor)
+            o.set_bonds(st.bond_src, st.bond_dst)
+            o.init_md()
+            for _ in range(n_sub):
+                o.propagate(False)
+            assert o.error() == 0
+            mp, mv, mf = ctx.get_monomers(k)
+            op, ov, of = o.get_monomers()
+            np.testing.assert_allclose(mp, op, atol=1e-4)
+            np.testing.assert_allclose(mv, ov, atol=2e-3 * np.abs(ov).max())
+            np.testing.assert_allclose(mf, of, atol=2e-3 * np.abs(of).max())
