@@ -29,8 +29,7 @@ const char* bin_variant_name(int v) {
 const char* collide_variant_name(int v) {
   static const char* n[] = {"256t 128c cap1408 g4", "256t 128c cap1408 g8", "128t 64c cap704 g4",
                             "128t 64c cap704 g8", "512t 256c cap2816 g4",
-                            "128t 64c cap704 persistent cp.async x2",
-                            "256t 128c cap1408 persistent cp.async x2"};
+                            "128t 64c cap704 cp.async", "256t 128c cap1408 cp.async"};
   return v >= 0 && v < 7 ? n[v] : "?";
 }
 const char* md_variant_name(int v) {

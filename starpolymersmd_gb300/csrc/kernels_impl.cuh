@@ -65,22 +65,17 @@ void collide_f32(const CollideArgs<float>& a, cudaStream_t st) {
 }
 
 template <int NT, int CT, int CAP>
-void collide_f32_pipe(const CollideArgs<float>& a, cudaStream_t st) {
-  auto kern = k_collide_f32_pipe<NT, CT, CAP>;
-  const size_t dyn = collide_f32_pipe_dyn_smem(CAP);
-  static int grid_cap = 0;  // resident CTAs on the whole GPU, found once
-  if (grid_cap == 0) {
+void collide_f32_async(const CollideArgs<float>& a, cudaStream_t st) {
+  auto kern = k_collide_f32_async<NT, CT, CAP>;
+  const size_t dyn = collide_f32_dyn_smem(CAP);
+  static bool configured = false;
+  if (!configured) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn));
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, dyn);
-    grid_cap = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    configured = true;
   }
-  const int grid = a.n_tiles < grid_cap ? a.n_tiles : grid_cap;
-  kern<<<grid, NT, dyn, st>>>(a.tiles, a.n_tiles, a.reps, a.frames, a.dyn, a.off, a.perm, a.st_in,
-                              a.st_out, a.mpos, a.mvel, a.mimg, a.inj_gamma, a.inj_uphi,
-                              a.inj_utheta, a.rng, a.mono_bin, a.err);
+  kern<<<a.n_tiles, NT, dyn, st>>>(a.tiles, a.reps, a.frames, a.dyn, a.off, a.perm, a.st_in,
+                                   a.st_out, a.mpos, a.mvel, a.mimg, a.inj_gamma, a.inj_uphi,
+                                   a.inj_utheta, a.rng, a.mono_bin, a.err);
 }
 #endif
 
@@ -116,8 +111,8 @@ void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
       case 2: collide_f32<128, 64, 704, 4>(a, st); return;
       case 3: collide_f32<128, 64, 704, 8>(a, st); return;
       case 4: collide_f32<512, 256, 2816, 4>(a, st); return;
-      case 5: collide_f32_pipe<128, 64, 704>(a, st); return;
-      case 6: collide_f32_pipe<256, 128, 1408>(a, st); return;
+      case 5: collide_f32_async<128, 64, 704>(a, st); return;
+      case 6: collide_f32_async<256, 128, 1408>(a, st); return;
       default: collide_f32<256, 128, 1408, 4>(a, st); return;
     }
   }

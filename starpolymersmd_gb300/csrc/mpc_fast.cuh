@@ -470,32 +470,27 @@ __global__ void __launch_bounds__(NT) k_collide_f32(
   collide_apply_f32<NT>(A, f, s_off, p0, n, nloc, s_x, s_v, s_lc, s_cmv, s_rot);
 }
 
-// ------------------------------------------------- collide, pipelined
-// Persistent variant of k_collide_f32: each CTA walks tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ... and gathers the particles of its next tile
-// with cp.async into the second of two shared-memory buffers while it
-// computes the current one, so the dependent loads (offsets -> sorted
-// slots -> records) of one tile overlap the arithmetic of the previous one.
-// The arithmetic is the same as k_collide_f32's, so both give identical bits.
+// ------------------------------------------------- collide, cp.async staging
+// k_collide_f32 with the gather done by cp.async: every thread first loads
+// the sorted slots of all its staged particles, then issues all their 16-byte
+// record copies straight into shared memory (no registers hold data in
+// flight), then the streaming / collision-frame pass runs in place. A tile
+// costs three dependent load rounds (offsets, slots, records) whatever its
+// size, with the shared memory and register budget of k_collide_f32. The
+// arithmetic is the same as k_collide_f32's, so both give identical bits.
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
 __device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-constexpr size_t collide_f32_pipe_dyn_smem(int cap) {
-  return static_cast<size_t>(cap) * (4 * sizeof(float4) + sizeof(short));
-}
-
 template <int NT, int CT, int CAP>
-__global__ void __launch_bounds__(NT) k_collide_f32_pipe(
-    const Tile* tiles, int n_tiles, const RepInfo* reps, const FrameF* frames, const RepDyn* dyn,
+__global__ void __launch_bounds__(NT) k_collide_f32_async(
+    const Tile* tiles, const RepInfo* reps, const FrameF* frames, const RepDyn* dyn,
     const uint32_t* __restrict__ off, const uint32_t* __restrict__ perm,
     const float* __restrict__ st_in, float* __restrict__ st_out, const float* mpos, float* mvel,
     const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
@@ -504,113 +499,69 @@ __global__ void __launch_bounds__(NT) k_collide_f32_pipe(
   constexpr int J = (CAP + NT - 1) / NT;  // staged particles per thread
   __shared__ float s_cmv[CT * 3];
   __shared__ float s_rot[CT * 9];
-  __shared__ uint32_t s_off[3][CT + 1];  // ring: current, next, the one after
+  __shared__ uint32_t s_off[CT + 1];
   extern __shared__ __align__(16) unsigned char s_dyn[];
-  float4* s_buf = reinterpret_cast<float4*>(s_dyn);  // [2][x: CAP, v: CAP]
-  short* s_lc = reinterpret_cast<short*>(s_buf + 4 * CAP);
+  float4* s_x = reinterpret_cast<float4*>(s_dyn);
+  float4* s_v = s_x + CAP;
+  short* s_lc = reinterpret_cast<short*>(s_v + CAP);
+
+  const Tile t = tiles[blockIdx.x];
+  const int nc = t.end - t.begin;
+  for (int i = threadIdx.x; i <= nc; i += NT) s_off[i] = off[t.begin + i];
+  __syncthreads();
+  const uint32_t p0 = s_off[0];
+  const int n = static_cast<int>(s_off[nc] - p0);
+  const int nloc = n < CAP ? n : CAP;
+
+  uint32_t src[J];
+#pragma unroll
+  for (int u = 0; u < J; ++u) {
+    const int j = u * NT + threadIdx.x;
+    src[u] = j < nloc ? perm[p0 + j] : 0xFFFFFFFFu;
+  }
+#pragma unroll
+  for (int u = 0; u < J; ++u) {
+    const int j = u * NT + threadIdx.x;
+    if (src[u] == 0xFFFFFFFFu) continue;
+    if (src[u] & MONO_BIT) {
+      cp_async16(s_v + j, mvel + 4 * static_cast<size_t>(src[u] & ~MONO_BIT));
+      s_x[j] = make_float4(0.f, 0.f, 0.f, __uint_as_float(src[u]));
+    } else {
+      cp_async16(s_x + j, st_in + 8 * static_cast<size_t>(src[u]));
+      cp_async16(s_v + j, st_in + 8 * static_cast<size_t>(src[u]) + 4);
+    }
+  }
+  const FrameF f = frames[t.rep];
+  const RepInfo& ri = reps[t.rep];
+  cp_async_wait_all();
+  // each thread finishes the particles it copied: stream and move into the
+  // collision frame, in place (fetch_f + frame_f)
+#pragma unroll
+  for (int u = 0; u < J; ++u) {
+    const int j = u * NT + threadIdx.x;
+    if (src[u] == 0xFFFFFFFFu) continue;
+    FastP P;
+    P.x = s_x[j];
+    P.v = s_v[j];
+    if (src[u] & MONO_BIT) {
+      const uint32_t m = src[u] & ~MONO_BIT;
+      P.v.w = reinterpret_cast<const float4*>(mpos)[m].w;
+      if (mono_bin == MONOBIN_WRAPPED)
+        P.v.x = __fsub_rn(P.v.x, __fmul_rn(i2f_small(mimg[m]), f.shearLy));
+    } else {
+      frame_f(P, f, f.solvent_mass);
+    }
+    s_x[j] = P.x;
+    s_v[j] = P.v;
+  }
+  __syncthreads();
+
   const CollideF32Args A{st_in, st_out, mpos, mvel, mimg, perm, inj_gamma, inj_uphi, inj_utheta,
                          rng, mono_bin, err};
-
-  int t = blockIdx.x;
-  if (t >= n_tiles) return;
-
-  auto load_off = [&](int tile, uint32_t* dst) {
-    const Tile T = tiles[tile];
-    const int nc = T.end - T.begin;
-    for (int i = threadIdx.x; i <= nc; i += NT) dst[i] = off[T.begin + i];
-  };
-  // sorted slots of this thread's staged particles (loads in flight on return)
-  auto load_perm = [&](int tile, const uint32_t* so, uint32_t* src) {
-    const Tile T = tiles[tile];
-    const int nc = T.end - T.begin;
-    const uint32_t p0 = so[0];
-    const int n = static_cast<int>(so[nc] - p0);
-    const int nloc = n < CAP ? n : CAP;
-#pragma unroll
-    for (int u = 0; u < J; ++u) {
-      const int j = u * NT + threadIdx.x;
-      src[u] = j < nloc ? perm[p0 + j] : 0xFFFFFFFFu;
-    }
-  };
-  auto gather = [&](const uint32_t* src, float4* bx) {
-#pragma unroll
-    for (int u = 0; u < J; ++u) {
-      const int j = u * NT + threadIdx.x;
-      if (src[u] == 0xFFFFFFFFu) continue;
-      if (src[u] & MONO_BIT) {
-        const uint32_t m = src[u] & ~MONO_BIT;
-        cp_async16(bx + CAP + j, mvel + 4 * static_cast<size_t>(m));
-        bx[j] = make_float4(0.f, 0.f, 0.f, __uint_as_float(src[u]));
-      } else {
-        cp_async16(bx + j, st_in + 8 * static_cast<size_t>(src[u]));
-        cp_async16(bx + CAP + j, st_in + 8 * static_cast<size_t>(src[u]) + 4);
-      }
-    }
-    cp_async_commit();
-  };
-
-  // prologue: offsets and gather of the first tile, offsets of the second
-  load_off(t, s_off[0]);
+  collide_cells_f32<NT>(A, f, t, s_off, nc, p0, nloc, s_x, s_v, s_lc, s_cmv, s_rot, ri.seed,
+                        dyn[t.rep].step, static_cast<uint32_t>(ri.cell_base));
   __syncthreads();
-  {
-    uint32_t src[J];
-    load_perm(t, s_off[0], src);
-    gather(src, s_buf);
-  }
-  int tn = t + static_cast<int>(gridDim.x);
-  if (tn < n_tiles) load_off(tn, s_off[1]);
-  int cur = 0, oi = 0;
-  while (true) {
-    __syncthreads();  // s_off of the next tile is visible; the other buffer is free
-    const bool has_next = tn < n_tiles;
-    uint32_t src[J];
-    if (has_next) load_perm(tn, s_off[(oi + 1) % 3], src);
-    cp_async_wait_all();  // this tile's gather (issued one tile ago)
-    __syncthreads();
-
-    const Tile T = tiles[t];
-    const FrameF f = frames[T.rep];
-    const RepInfo& ri = reps[T.rep];
-    const uint32_t* so = s_off[oi];
-    const int nc = T.end - T.begin;
-    const uint32_t p0 = so[0];
-    const int n = static_cast<int>(so[nc] - p0);
-    const int nloc = n < CAP ? n : CAP;
-    float4* s_x = s_buf + 2 * CAP * cur;
-    float4* s_v = s_x + CAP;
-    // stream and move into the collision frame, in place (fetch_f + frame_f)
-    for (int j = threadIdx.x; j < nloc; j += NT) {
-      FastP P;
-      P.x = s_x[j];
-      P.v = s_v[j];
-      const uint32_t tag = __float_as_uint(P.x.w);
-      if (tag & MONO_BIT) {
-        const uint32_t m = tag & ~MONO_BIT;
-        P.v.w = reinterpret_cast<const float4*>(mpos)[m].w;
-        if (mono_bin == MONOBIN_WRAPPED)
-          P.v.x = __fsub_rn(P.v.x, __fmul_rn(i2f_small(mimg[m]), f.shearLy));
-      } else {
-        frame_f(P, f, f.solvent_mass);
-      }
-      s_x[j] = P.x;
-      s_v[j] = P.v;
-    }
-    if (has_next) gather(src, s_buf + 2 * CAP * (cur ^ 1));
-    const int tnn = tn + static_cast<int>(gridDim.x);
-    if (tnn < n_tiles) load_off(tnn, s_off[(oi + 2) % 3]);
-    __syncthreads();
-
-    collide_cells_f32<NT>(A, f, T, so, nc, p0, nloc, s_x, s_v, s_lc, s_cmv, s_rot, ri.seed,
-                          dyn[T.rep].step, static_cast<uint32_t>(ri.cell_base));
-    __syncthreads();
-    collide_apply_f32<NT>(A, f, so, p0, n, nloc, s_x, s_v, s_lc, s_cmv, s_rot);
-
-    if (!has_next) break;
-    t = tn;
-    tn = tnn;
-    cur ^= 1;
-    oi = (oi + 1) % 3;
-  }
+  collide_apply_f32<NT>(A, f, s_off, p0, n, nloc, s_x, s_v, s_lc, s_cmv, s_rot);
 }
 
 }  // namespace smpc
