@@ -194,6 +194,33 @@ int smpc_cell_counts(smpc_ctx* ctx, int rep, unsigned* total, unsigned* fluid);
  * collision. Either pointer may be NULL. */
 int smpc_cell_members(smpc_ctx* ctx, int rep, int* fluid_cell, int* mono_cell);
 int smpc_set_collision_counter(smpc_ctx* ctx, uint64_t counter);
+
+/* Molecules of a replica (Box::Molecules, Box.h:50): mol_start[n_mol + 1]
+ * monomer offsets within the replica, from 0 to n_mono, every molecule
+ * non-empty. Default: molecule 0 = the first mol0_size monomers, the rest one
+ * more molecule. Used by the observables below. */
+int smpc_set_molecules(smpc_ctx* ctx, int rep, int n_mol, const int* mol_start);
+/* Output-step observables of every replica from one launch, FP64
+ * (star-polymers.cpp:467-473), out[SMPC_OBS_PER_REP * n_rep]; per replica, in
+ * each molecule's centre-of-mass frame (Box::center_of_mass_reference_frame,
+ * Box.cpp:81-102): [0] R_g and [1..9] gyration tensor G (row-major), both
+ * averaged over molecules (Box::calculate_gyration_tensor, Box.cpp:330-353);
+ * [10..12] rotation frequency averaged over molecules
+ * (Box::calculate_rotation_frequency, Box.cpp:355-379); [13] kinetic energy
+ * (Box::calculate_ekin, Box.cpp:288-294); [14] the temperature
+ * 2 E / (3 (N - 1)) (Box::print_Ekin_and_Temperature, Box.cpp:635-646);
+ * [15] the number of molecules. */
+#define SMPC_OBS_PER_REP 16
+int smpc_molecule_observables_all(smpc_ctx* ctx, double* out);
+/* VelocityX once over a replica's solvent (Velocity_x.h:76-100, applied as
+ * star-polymers.cpp:483 does): velocity relative to molecule 0's mean
+ * velocity, binned by floor(p / width) of the Lees-Edwards-wrapped position
+ * relative to molecule 0's centre (MPC::wrap(pos, vel), MPC.cpp:492-495),
+ * along x (x_out) and along y (y_out). Bin k of an axis of length L sits at
+ * out[3 (k - floor(-L / (2 width)))] = (sum v_x, sum v_y, count); an axis needs
+ * floor(L / (2 width)) - floor(-L / (2 width)) + 1 bins (SMPC_E_ARG otherwise). */
+int smpc_velocity_profile(smpc_ctx* ctx, int rep, double width, double* x_out, int n_x,
+                          double* y_out, int n_y);
 int smpc_verlet_rebuilds(smpc_ctx* ctx, int rep, int* out);
 
 /* Device error word (0 = clean) and its first offender; clears it. */

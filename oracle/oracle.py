@@ -215,6 +215,12 @@ class OracleSystem:
         return self.lib.orc_verlet_rebuilds(self.h)
 
 
+def profile_bins(L, width):
+    """Bins k = floor(p / width) for p in [-L/2, L/2]: floor(L/2w) - floor(-L/2w) + 1."""
+    import math
+    return int(math.floor(L / (2.0 * width)) - math.floor(-L / (2.0 * width)) + 1)
+
+
 class RefSystem:
     """The reference's own classes (Box, MPC, Thermostat_None) via the harness."""
 
@@ -239,6 +245,8 @@ class RefSystem:
             "ref_cell_counts": [P, P, P], "ref_cell_index": [P, P, P],
             "ref_set_delrx": [P, C.c_double],
             "ref_gyration": [P, P], "ref_run": [P, C.c_long, C.c_long, C.c_double, C.c_int],
+            "ref_observables": [P, P],
+            "ref_velocity_profile": [P, C.c_double, P, C.c_int, P, C.c_int],
             "ref_shift_arg_order": [P], "rand_tape_enable": [C.c_int], "rand_tape_clear": [],
             "rand_tape_copy": [P, P, C.c_long], "rand_tape_reseed": [C.c_ulonglong],
         }.items():
@@ -333,6 +341,19 @@ class RefSystem:
         fl = np.zeros(n, dtype=np.uint32)
         self.lib.ref_cell_counts(self.h, _p(tot), _p(fl))
         return tot, fl
+
+    def observables(self):
+        """R_g, G (row-major), rotation frequency, kinetic energy, temperature, molecules."""
+        out = np.zeros(16)
+        self.lib.ref_observables(self.h, _p(out))
+        return out
+
+    def velocity_profile(self, width):
+        """VelocityX sums (v_x, v_y, count) per bin along x and along y."""
+        nx, ny = profile_bins(self.L[0], width), profile_bins(self.L[1], width)
+        xo, yo = np.zeros((nx, 3)), np.zeros((ny, 3))
+        self.lib.ref_velocity_profile(self.h, width, _p(xo), nx, _p(yo), ny)
+        return xo, yo
 
     def cell_index(self):
         """CellIndex of every solvent particle and monomer at the last sort."""

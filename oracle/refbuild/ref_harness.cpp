@@ -5,12 +5,15 @@
 // star-polymers/src/star-polymers.cpp:352-404 do, run the driver loop body
 // (star-polymers.cpp:466,530,534: propagate, then MPC::step), and read or
 // overwrite the state, the cell occupancies and the recorded random draws.
+#include <cmath>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "Box.h"
 #include "MPC.h"
 #include "Thermostat_None.h"
+#include "Velocity_x.h"
 #include "rand_tape.h"
 
 namespace {
@@ -207,6 +210,65 @@ void ref_gyration(RefSys* s, double* out) {
   out[0] = std::get<0>(g);
   const Matrix3d& m = std::get<1>(g);
   for (int i = 0; i < 9; ++i) out[1 + i] = m.data()[i];
+}
+
+// Output-step observables of the star-polymers.cpp loop (:467-473) after
+// Box::center_of_mass_reference_frame: out[0] = R_g, out[1..9] = G
+// (row-major), out[10..12] = rotation frequency (Box.cpp:330-379),
+// out[13] = kinetic energy (Box::calculate_ekin, Box.cpp:288-294), out[14] =
+// the temperature Box::print_Ekin_and_Temperature prints (Box.cpp:635-646),
+// out[15] = number of molecules.
+void ref_observables(RefSys* s, double* out) {
+  Box& b = *s->box;
+  b.center_of_mass_reference_frame();
+  auto g = b.calculate_gyration_tensor();
+  out[0] = std::get<0>(g);
+  const Matrix3d& m = std::get<1>(g);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) out[1 + 3 * i + j] = m(i, j);
+  const Vector3d w = b.calculate_rotation_frequency();
+  for (int i = 0; i < 3; ++i) out[10 + i] = w(i);
+  unsigned n = 0;
+  for (auto& mol : b.Molecules) n += mol.NumberOfMonomers;
+  out[13] = b.calculate_ekin();
+  out[14] = out[13] * 2. / (3. * (n - 1));
+  out[15] = static_cast<double>(b.Molecules.size());
+}
+
+// VelocityX (Velocity_x.h:76-100) applied to the solvent once, the way
+// star-polymers.cpp:468,483 does (centre-of-mass frame first): per bin k of
+// floor(p / width) along x and along y, (sum v_x, sum v_y, count) at
+// out[3 * (k - k0)] with k0 = floor(-L / (2 width)) of the axis.
+class HarnessVelocityX : public VelocityX {
+ public:
+  using VelocityX::VelocityX;
+  void dump(double width, const std::map<double, vel_xy>& sums,
+            const std::map<double, double>& counts, int L, double* out, int n) const {
+    const long k0 = static_cast<long>(std::floor(-L / (2.0 * width)));
+    for (int i = 0; i < 3 * n; ++i) out[i] = 0.0;
+    for (const auto& kv : sums) {
+      const long k = std::lround(kv.first / width) - k0;
+      if (k < 0 || k >= n) continue;
+      out[3 * k] = kv.second.vel_x;
+      out[3 * k + 1] = kv.second.vel_y;
+      out[3 * k + 2] = counts.at(kv.first);
+    }
+  }
+  void dump_x(double w, int L, double* out, int n) const {
+    dump(w, vel_x_average, vel_x_average_count, L, out, n);
+  }
+  void dump_y(double w, int L, double* out, int n) const {
+    dump(w, vel_y_average, vel_y_average_count, L, out, n);
+  }
+};
+
+void ref_velocity_profile(RefSys* s, double width, double* x_out, int n_x, double* y_out,
+                          int n_y) {
+  s->box->center_of_mass_reference_frame();
+  HarnessVelocityX vx(*s->box, *s->mpc, width);
+  (*s->mpc)(vx);
+  vx.dump_x(width, s->box->BoxSize[0], x_out, n_x);
+  vx.dump_y(width, s->box->BoxSize[1], y_out, n_y);
 }
 
 // Runs the star-polymers.cpp loop body (lines 466/530 then 534) for

@@ -35,10 +35,20 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_init_solvent", "smpc_temperature_all", "smpc_temperature_all_noalloc",
            "smpc_set_monomer_state_all",
            "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
-           "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide")
+           "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide", "smpc_set_molecules",
+           "smpc_molecule_observables_all", "smpc_velocity_profile")
 
 PHASES = ("md_substeps", "cycle_begin", "mono_prep", "fluid_bin", "scan", "build_perm",
           "collide", "cycle_end")
+
+
+OBS_PER_REP = 16
+
+
+def profile_bins(L, width):
+    """Bins k = floor(p / width) for p in [-L/2, L/2]: floor(L/2w) - floor(-L/2w) + 1."""
+    import math
+    return int(math.floor(L / (2.0 * width)) - math.floor(-L / (2.0 * width)) + 1)
 
 
 class SmpcError(RuntimeError):
@@ -114,6 +124,9 @@ def load(path: Optional[str] = None):
         "smpc_autotune": ([P, I, C.c_char_p, I], I),
         "smpc_mpc_bin": ([P, C.c_long, D, P, C.POINTER(I)], I),
         "smpc_mpc_collide": ([P, C.POINTER(Inject)], I),
+        "smpc_set_molecules": ([P, I, I, P], I),
+        "smpc_molecule_observables_all": ([P, P], I),
+        "smpc_velocity_profile": ([P, I, D, P, I, P, I], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -344,6 +357,26 @@ class Context:
         fl = np.zeros(n, dtype=np.uint32)
         self._check(self.lib.smpc_cell_counts(self.h, rep, _p(tot), _p(fl)), "cell_counts")
         return tot, fl
+
+    def set_molecules(self, rep, mol_start):
+        ms = np.ascontiguousarray(mol_start, dtype=np.int32)
+        self._check(self.lib.smpc_set_molecules(self.h, rep, len(ms) - 1, _p(ms)), "set_molecules")
+
+    def molecule_observables_all(self):
+        """Per replica: R_g, G (3x3), rotation frequency, kinetic energy, temperature, molecules."""
+        out = np.zeros((self.n_rep, OBS_PER_REP))
+        self._check(self.lib.smpc_molecule_observables_all(self.h, _p(out)),
+                    "molecule_observables_all")
+        return out
+
+    def velocity_profile(self, rep, width):
+        """VelocityX sums (v_x, v_y, count) per bin along x and along y."""
+        L = self.replicas[rep]["L"]
+        nx, ny = profile_bins(int(L[0]), width), profile_bins(int(L[1]), width)
+        xo, yo = np.zeros((nx, 3)), np.zeros((ny, 3))
+        self._check(self.lib.smpc_velocity_profile(self.h, rep, width, _p(xo), nx, _p(yo), ny),
+                    "velocity_profile")
+        return xo, yo
 
     def cell_members(self, rep=0):
         """(cell of every solvent particle by id, cell of every monomer) at the last sort."""

@@ -5,6 +5,7 @@
 #include "md_kernels.cuh"
 #include "mpc_fast.cuh"
 #include "mpc_kernels.cuh"
+#include "observables.cuh"
 
 namespace smpc {
 
@@ -137,6 +138,26 @@ void launch_temperature<Real>(const Tile* tiles, int n_tiles, const RepInfo* rep
   if (n_tiles == 0) return;
   k_temperature<Real, 128><<<n_tiles, 128, 0, st>>>(tiles, reps, off, perm, rec_cur, mpos, mvel,
                                                     mimg, mono_bin, partial);
+}
+
+template <>
+void launch_mol_observables<Real>(const int2* rep_mols, const int2* mols, int n_rep,
+                                  const Real* mpos, const Real* mvel, double* out,
+                                  cudaStream_t st) {
+  if (n_rep == 0) return;
+  k_mol_observables<Real, 256><<<n_rep, 256, 0, st>>>(rep_mols, mols, mpos, mvel, out);
+}
+
+template <>
+void launch_velocity_profile<Real>(const RepInfo* reps, const int2* rep_mols, const int2* mols,
+                                   int rep, int slot_cap, const Real* rec, const Real* mpos,
+                                   const Real* mvel, double delrx, double width, long long kx0,
+                                   int nx, long long ky0, int ny, double* c6, double* bins,
+                                   cudaStream_t st) {
+  k_profile_centre<Real><<<1, 1, 0, st>>>(rep_mols, mols, mpos, mvel, rep, c6);
+  if (slot_cap == 0) return;
+  k_velocity_profile<Real><<<(slot_cap + 255) / 256, 256, 0, st>>>(
+      reps, rep, rec, delrx, width, kx0, nx, ky0, ny, c6, bins);
 }
 
 template <>

@@ -81,6 +81,15 @@ template <typename R>
 void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, int variant,
                cudaStream_t st);
 
+template <typename R>
+void launch_mol_observables(const int2* rep_mols, const int2* mols, int n_rep, const R* mpos,
+                            const R* mvel, double* out, cudaStream_t st);
+template <typename R>
+void launch_velocity_profile(const RepInfo* reps, const int2* rep_mols, const int2* mols, int rep,
+                             int slot_cap, const R* rec, const R* mpos, const R* mvel,
+                             double delrx, double width, long long kx0, int nx, long long ky0,
+                             int ny, double* c6, double* bins, cudaStream_t st);
+
 void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* grand, int n_cells,
                  cudaStream_t st);
 int scan_tile_count(int n_cells);

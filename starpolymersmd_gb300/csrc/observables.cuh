@@ -1,0 +1,198 @@
+// Output-step observables on the device, FP64 (star-polymers.cpp:466-483):
+//   k_mol_observables  per replica: radius of gyration and gyration tensor
+//                      (Box::calculate_gyration_tensor, Box.cpp:330-353),
+//                      rotation frequency (Box::calculate_rotation_frequency,
+//                      Box.cpp:355-379), kinetic energy and temperature
+//                      (Box::calculate_ekin / print_Ekin_and_Temperature,
+//                      Box.cpp:288-294, 635-646), all in each molecule's
+//                      centre-of-mass frame (Box::center_of_mass_reference_frame,
+//                      Box.cpp:81-102);
+//   k_velocity_profile VelocityX (Velocity_x.h:76-100): solvent velocity
+//                      relative to molecule 0's centre-of-mass velocity, binned
+//                      by the Lees-Edwards-wrapped position relative to its
+//                      centre of mass, along x and along y.
+// Centres of mass are summed by one thread in monomer order, like the
+// reference, so every position relative to them is the reference's to the
+// last bit; the tensor, momentum and energy sums are block reductions.
+#pragma once
+#include <stdint.h>
+
+#include "mpc_kernels.cuh"
+#include "smpc_device.cuh"
+
+namespace smpc {
+
+constexpr int OBS_PER_REP = 16;
+
+// centre of molecule [b, e): unweighted mean position and velocity
+template <typename R>
+__device__ __forceinline__ void molecule_centre(const R* mpos, const R* mvel, int b, int e,
+                                                double* c) {
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = b; i < e; ++i) {
+    const R4<R> p = ld4_rw(mpos, i), v = ld4_rw(mvel, i);
+    s[0] += static_cast<double>(p.x);
+    s[1] += static_cast<double>(p.y);
+    s[2] += static_cast<double>(p.z);
+    s[3] += static_cast<double>(v.x);
+    s[4] += static_cast<double>(v.y);
+    s[5] += static_cast<double>(v.z);
+  }
+  const double n = static_cast<double>(e - b);
+  for (int k = 0; k < 6; ++k) c[k] = s[k] / n;
+}
+
+// x = A^-1 b for a symmetric positive-definite 3x3 A (LDL^T, no pivoting)
+__device__ __forceinline__ void solve_sym3(const double A[3][3], const double b[3], double x[3]) {
+  double L10 = 0, L20 = 0, L21 = 0, D0, D1, D2;
+  D0 = A[0][0];
+  L10 = A[1][0] / D0;
+  L20 = A[2][0] / D0;
+  D1 = A[1][1] - L10 * L10 * D0;
+  L21 = (A[2][1] - L20 * L10 * D0) / D1;
+  D2 = A[2][2] - L20 * L20 * D0 - L21 * L21 * D1;
+  const double y0 = b[0];
+  const double y1 = b[1] - L10 * y0;
+  const double y2 = b[2] - L20 * y0 - L21 * y1;
+  x[2] = y2 / D2;
+  x[1] = y1 / D1 - L21 * x[2];
+  x[0] = y0 / D0 - L10 * x[1] - L20 * x[2];
+}
+
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* s_red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < NT / 32; ++w) t += s_red[w];
+  return t;  // valid in thread 0
+}
+
+// One CTA per replica. rep_mols[r] = (first molecule, count); mols[m] =
+// global monomer range [x, y). out[OBS_PER_REP * r + ...]: R_g, G (row-major,
+// 9), rotation frequency (3), kinetic energy, temperature, molecules.
+template <typename R, int NT>
+__global__ void __launch_bounds__(NT) k_mol_observables(const int2* rep_mols, const int2* mols,
+                                                        const R* mpos, const R* mvel,
+                                                        double* out) {
+  __shared__ double s_c[6];
+  __shared__ double s_red[NT / 32];
+  const int r = blockIdx.x;
+  const int2 rm = rep_mols[r];
+  double rg = 0, G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, w[3] = {0, 0, 0}, ekin = 0;
+  long long n_total = 0;
+  for (int mi = rm.x; mi < rm.x + rm.y; ++mi) {
+    const int2 mb = mols[mi];
+    const int n = mb.y - mb.x;
+    if (threadIdx.x == 0) molecule_centre<R>(mpos, mvel, mb.x, mb.y, s_c);
+    __syncthreads();
+    // S = sum r r^T (6), angular momentum (3), sum m |u|^2
+    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = mb.x + threadIdx.x; i < mb.y; i += NT) {
+      const R4<R> p = ld4_rw(mpos, i), v = ld4_rw(mvel, i);
+      const double x0 = static_cast<double>(p.x) - s_c[0], x1 = static_cast<double>(p.y) - s_c[1],
+                   x2 = static_cast<double>(p.z) - s_c[2];
+      const double u0 = static_cast<double>(v.x) - s_c[3], u1 = static_cast<double>(v.y) - s_c[4],
+                   u2 = static_cast<double>(v.z) - s_c[5];
+      acc[0] += x0 * x0;
+      acc[1] += x0 * x1;
+      acc[2] += x0 * x2;
+      acc[3] += x1 * x1;
+      acc[4] += x1 * x2;
+      acc[5] += x2 * x2;
+      acc[6] += x1 * u2 - x2 * u1;
+      acc[7] += x2 * u0 - x0 * u2;
+      acc[8] += x0 * u1 - x1 * u0;
+      acc[9] += static_cast<double>(p.w) * ((u0 * u0 + u1 * u1) + u2 * u2);
+    }
+    double tot[10];
+    for (int k = 0; k < 10; ++k) tot[k] = block_sum<NT>(acc[k], s_red);
+    if (threadIdx.x == 0 && n > 0) {
+      const double dn = static_cast<double>(n);
+      const double g[9] = {tot[0] / dn, tot[1] / dn, tot[2] / dn, tot[1] / dn, tot[3] / dn,
+                           tot[4] / dn, tot[2] / dn, tot[4] / dn, tot[5] / dn};
+      for (int k = 0; k < 9; ++k) G[k] += g[k];
+      rg += sqrt(g[0] + g[4] + g[8]);
+      const double tr = tot[0] + tot[3] + tot[5];
+      const double I[3][3] = {{tr - tot[0], -tot[1], -tot[2]},
+                              {-tot[1], tr - tot[3], -tot[4]},
+                              {-tot[2], -tot[4], tr - tot[5]}};
+      const double Lm[3] = {tot[6], tot[7], tot[8]};
+      double om[3];
+      solve_sym3(I, Lm, om);
+      for (int k = 0; k < 3; ++k) w[k] += om[k];
+      ekin += tot[9] * 0.5;
+      n_total += n;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double nm = rm.y > 0 ? static_cast<double>(rm.y) : 1.0;
+    double* o = out + static_cast<size_t>(OBS_PER_REP) * r;
+    o[0] = rg / nm;
+    for (int k = 0; k < 9; ++k) o[1 + k] = G[k] / nm;
+    for (int k = 0; k < 3; ++k) o[10 + k] = w[k] / nm;
+    o[13] = ekin;
+    o[14] = n_total > 1 ? ekin * 2. / (3. * static_cast<double>(n_total - 1)) : 0.0;
+    o[15] = static_cast<double>(rm.y);
+  }
+}
+
+template <typename R>
+__global__ void k_profile_centre(const int2* rep_mols, const int2* mols, const R* mpos,
+                                 const R* mvel, int rep, double* c6) {
+  const int2 rm = rep_mols[rep];
+  if (rm.y == 0) {
+    for (int k = 0; k < 6; ++k) c6[k] = 0.0;
+    return;
+  }
+  const int2 mb = mols[rm.x];
+  molecule_centre<R>(mpos, mvel, mb.x, mb.y, c6);
+}
+
+// bins: x then y, 3 doubles per bin (sum v_x, sum v_y, count), zeroed by the host
+template <typename R>
+__global__ void k_velocity_profile(const RepInfo* reps, int rep, const R* rec, double delrx,
+                                   double width, long long kx0, int nx, long long ky0, int ny,
+                                   const double* c6, double* bins) {
+  const RepInfo& ri = reps[rep];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ri.slot_cap) return;
+  const size_t s = static_cast<size_t>(ri.slot_base) + i;
+  const R* p = rec + 8 * s;
+  if (slot_id(p[3]) == SLOT_EMPTY) return;
+  double x0 = static_cast<double>(p[0]) - c6[0], x1 = static_cast<double>(p[1]) - c6[1],
+         x2 = static_cast<double>(p[2]) - c6[2];
+  double v0 = static_cast<double>(p[4]) - c6[3], v1 = static_cast<double>(p[5]) - c6[4];
+  const double Lx = ri.L[0], Ly = ri.L[1], Lz = ri.L[2];
+  if (ri.shear != 0.0) {  // MPC::LEBC(pos, vel) (MPC.cpp:431-439)
+    const double cy = round(x1 / Ly);
+    x0 -= Lx * round(x0 / Lx);
+    x0 -= cy * delrx;
+    x0 -= Lx * round(x0 / Lx);
+    x1 -= Ly * cy;
+    x2 -= Lz * round(x2 / Lz);
+    v0 -= cy * ri.shear * Ly;
+  } else {  // MPC::wrap(pos) (MPC.cpp:473-478)
+    x0 -= round(x0 / Lx) * Lx;
+    x1 -= round(x1 / Ly) * Ly;
+  }
+  const long long kx = static_cast<long long>(floor(x0 / width)) - kx0;
+  const long long ky = static_cast<long long>(floor(x1 / width)) - ky0;
+  if (kx >= 0 && kx < nx) {
+    atomicAdd(bins + 3 * kx, v0);
+    atomicAdd(bins + 3 * kx + 1, v1);
+    atomicAdd(bins + 3 * kx + 2, 1.0);
+  }
+  if (ky >= 0 && ky < ny) {
+    double* b = bins + 3 * static_cast<size_t>(nx);
+    atomicAdd(b + 3 * ky, v0);
+    atomicAdd(b + 3 * ky + 1, v1);
+    atomicAdd(b + 3 * ky + 2, 1.0);
+  }
+}
+
+}  // namespace smpc

@@ -14,6 +14,7 @@
 #include "../../include/smpc.h"
 #include "launch.h"
 #include "md_kernels.cuh"
+#include "observables.cuh"
 #include "smpc_device.cuh"
 
 using smpc::ErrorState;
@@ -73,6 +74,14 @@ struct smpc_ctx {
   double* d_inj = nullptr;  // gamma | u_phi | u_theta, total_cells each
   ErrorState* d_err = nullptr;
   smpc::FrameF* d_frames = nullptr;
+  // molecules per replica (local monomer offsets) and their device tables
+  std::vector<std::vector<int>> mol_start;
+  int2* d_rep_mols = nullptr;  // per replica: first molecule, count
+  int2* d_mols = nullptr;      // per molecule: global monomer range
+  double* d_obs = nullptr;     // OBS_PER_REP per replica
+  double* d_prof = nullptr;    // velocity-profile bins, grown on demand
+  size_t prof_cap = 0;
+  double* d_c6 = nullptr;      // centre of molecule 0 (position, velocity)
   double rot_c = 0, rot_s = 0;
   int max_nb = 192;
   bool collided = false;
@@ -589,7 +598,8 @@ void free_all(smpc_ctx* ctx) {
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
                   ctx->d_mimg, ctx->d_bond_start, ctx->d_bonds, ctx->d_nlist, ctx->d_ncount,
-                  ctx->d_md_order, ctx->d_inj, ctx->d_err, ctx->d_frames};
+                  ctx->d_md_order, ctx->d_inj, ctx->d_err, ctx->d_frames, ctx->d_rep_mols,
+                  ctx->d_mols, ctx->d_obs, ctx->d_prof, ctx->d_c6};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
@@ -679,6 +689,27 @@ int temperature_all_noalloc_t(smpc_ctx* ctx, double* out) {
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(out, res, ctx->n_rep * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
   CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+int upload_molecules(smpc_ctx* ctx) {
+  std::vector<int2> rep_mols(ctx->n_rep), mols;
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    const std::vector<int>& ms = ctx->mol_start[r];
+    const int base = ctx->reps[r].mono_base;
+    rep_mols[r] = make_int2(static_cast<int>(mols.size()), static_cast<int>(ms.size()) - 1);
+    for (size_t k = 0; k + 1 < ms.size(); ++k) mols.push_back(make_int2(base + ms[k], base + ms[k + 1]));
+  }
+  if (ctx->d_rep_mols) cudaFree(ctx->d_rep_mols);
+  if (ctx->d_mols) cudaFree(ctx->d_mols);
+  ctx->d_rep_mols = nullptr;
+  ctx->d_mols = nullptr;
+  CU(dalloc(&ctx->d_rep_mols, rep_mols.size()));
+  CU(dalloc(&ctx->d_mols, mols.size()));
+  CU(cudaMemcpy(ctx->d_rep_mols, rep_mols.data(), rep_mols.size() * sizeof(int2),
+                cudaMemcpyHostToDevice));
+  if (!mols.empty())
+    CU(cudaMemcpy(ctx->d_mols, mols.data(), mols.size() * sizeof(int2), cudaMemcpyHostToDevice));
   return SMPC_OK;
 }
 
@@ -787,6 +818,21 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
         return bail(SMPC_E_CUDA, "tile tables");
     }
   }
+  // molecules: molecule 0 = the first mol0_size monomers (the recentring
+  // reference, MPC.cpp:175-176), the rest one more molecule
+  ctx->mol_start.resize(n_rep);
+  for (int r = 0; r < n_rep; ++r) {
+    const int nm = ctx->reps[r].n_mono, m0 = ctx->reps[r].mol0_size;
+    std::vector<int>& ms = ctx->mol_start[r];
+    ms.push_back(0);
+    if (nm > 0) {
+      if (m0 > 0 && m0 < nm) ms.push_back(m0);
+      ms.push_back(nm);
+    }
+  }
+  if (upload_molecules(ctx) != SMPC_OK || dalloc(&ctx->d_obs, static_cast<size_t>(n_rep) * smpc::OBS_PER_REP) != cudaSuccess ||
+      dalloc(&ctx->d_c6, 6) != cudaSuccess)
+    return bail(SMPC_E_CUDA, "molecule tables");
   // empty solvent state until smpc_set_fluid: every slot a hole
   for (int r = 0; r < n_rep; ++r) {
     std::vector<double> z(3 * static_cast<size_t>(ctx->reps[r].n_fluid) + 3, 0.0);
@@ -1354,6 +1400,84 @@ int smpc_cell_members(smpc_ctx* ctx, int rep, int* fluid_cell, int* mono_cell) {
   }
   for (int i = 0; i < ri.n_fluid; ++i)
     if (fluid_cell[i] < 0) return fail(ctx, SMPC_E_DEVICE, "solvent particle missing from the records");
+  return SMPC_OK;
+}
+
+int smpc_set_molecules(smpc_ctx* ctx, int rep, int n_mol, const int* mol_start) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  const int nm = ctx->reps[rep].n_mono;
+  if (n_mol < 0 || (n_mol > 0 && !mol_start)) return fail(ctx, SMPC_E_ARG, "molecule table");
+  if (n_mol == 0 ? nm != 0 : (mol_start[0] != 0 || mol_start[n_mol] != nm))
+    return fail(ctx, SMPC_E_ARG, "molecules must cover the replica's monomers exactly");
+  for (int k = 0; k < n_mol; ++k)
+    if (mol_start[k + 1] <= mol_start[k]) return fail(ctx, SMPC_E_ARG, "empty or unordered molecule");
+  ctx->mol_start[rep].assign(mol_start, mol_start + n_mol + 1);
+  if (n_mol == 0) ctx->mol_start[rep].assign(1, 0);
+  cudaSetDevice(ctx->device);
+  CU(cudaStreamSynchronize(ctx->st));
+  return upload_molecules(ctx);
+}
+
+int smpc_molecule_observables_all(smpc_ctx* ctx, double* out) {
+  if (!ctx || !out) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->opt.precision == SMPC_FP64)
+    smpc::launch_mol_observables<double>(ctx->d_rep_mols, ctx->d_mols, ctx->n_rep,
+                                         static_cast<const double*>(ctx->d_mpos),
+                                         static_cast<const double*>(ctx->d_mvel), ctx->d_obs, ctx->st);
+  else
+    smpc::launch_mol_observables<float>(ctx->d_rep_mols, ctx->d_mols, ctx->n_rep,
+                                        static_cast<const float*>(ctx->d_mpos),
+                                        static_cast<const float*>(ctx->d_mvel), ctx->d_obs, ctx->st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out, ctx->d_obs, static_cast<size_t>(ctx->n_rep) * smpc::OBS_PER_REP * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+int smpc_velocity_profile(smpc_ctx* ctx, int rep, double width, double* x_out, int n_x,
+                          double* y_out, int n_y) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (!(width > 0) || !x_out || !y_out) return fail(ctx, SMPC_E_ARG, "profile width or buffers");
+  const RepInfo& ri = ctx->reps[rep];
+  const long long kx0 = static_cast<long long>(std::floor(-ri.L[0] / (2.0 * width)));
+  const long long ky0 = static_cast<long long>(std::floor(-ri.L[1] / (2.0 * width)));
+  const long long need_x = static_cast<long long>(std::floor(ri.L[0] / (2.0 * width))) - kx0 + 1;
+  const long long need_y = static_cast<long long>(std::floor(ri.L[1] / (2.0 * width))) - ky0 + 1;
+  if (n_x < need_x || n_y < need_y)
+    return fail(ctx, SMPC_E_ARG, "profile needs " + std::to_string(need_x) + " x bins and " +
+                                     std::to_string(need_y) + " y bins");
+  cudaSetDevice(ctx->device);
+  const size_t nb = 3 * static_cast<size_t>(n_x + n_y);
+  if (nb > ctx->prof_cap) {
+    CU(cudaStreamSynchronize(ctx->st));
+    if (ctx->d_prof) cudaFree(ctx->d_prof);
+    ctx->d_prof = nullptr;
+    ctx->prof_cap = 0;
+    CU(dalloc(&ctx->d_prof, nb));
+    ctx->prof_cap = nb;
+  }
+  CU(cudaMemsetAsync(ctx->d_prof, 0, nb * sizeof(double), ctx->st));
+  const double delrx = ctx->dyn[rep].delrx;
+  if (ctx->opt.precision == SMPC_FP64)
+    smpc::launch_velocity_profile<double>(
+        ctx->d_reps, ctx->d_rep_mols, ctx->d_mols, rep, ri.slot_cap,
+        static_cast<const double*>(ctx->d_rec[ctx->cur]), static_cast<const double*>(ctx->d_mpos),
+        static_cast<const double*>(ctx->d_mvel), delrx, width, kx0, n_x, ky0, n_y, ctx->d_c6,
+        ctx->d_prof, ctx->st);
+  else
+    smpc::launch_velocity_profile<float>(
+        ctx->d_reps, ctx->d_rep_mols, ctx->d_mols, rep, ri.slot_cap,
+        static_cast<const float*>(ctx->d_rec[ctx->cur]), static_cast<const float*>(ctx->d_mpos),
+        static_cast<const float*>(ctx->d_mvel), delrx, width, kx0, n_x, ky0, n_y, ctx->d_c6,
+        ctx->d_prof, ctx->st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(x_out, ctx->d_prof, 3 * static_cast<size_t>(n_x) * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaMemcpyAsync(y_out, ctx->d_prof + 3 * static_cast<size_t>(n_x),
+                     3 * static_cast<size_t>(n_y) * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
   return SMPC_OK;
 }
 

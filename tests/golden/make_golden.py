@@ -31,6 +31,7 @@ from oracle import oracle as orc  # noqa: E402
 from starpolymersmd_gb300 import system  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
+PROFILE_WIDTH = 0.2  # VelocityX bin width of star-polymers.cpp:355
 
 SCENARIOS = {
     # pure solvent with Lees-Edwards shear, like mpc_test.cpp (step_update = 1)
@@ -86,6 +87,7 @@ def run_scenario(name: str, sc: dict) -> dict:
                    mono_mass=m0["mass"], mono_amphi=m0["amphi"], mono_anchor=m0["anchor"])
     shifts, gammas, uphis, uths, tots, fls, steps = [], [], [], [], [], [], []
     fl_pos, fl_vel, temps, fl_cell, mo_cell = [], [], [], [], []
+    obs, prof_x, prof_y = [], [], []
     m_pos, m_vel, m_frc, delrx, epots = [], [], [], [], []
     for t in range(sc["n_loop"]):
         if st and sc["with_md"]:
@@ -105,6 +107,11 @@ def run_scenario(name: str, sc: dict) -> dict:
                 temps.append(ref.temperature())
                 fc, mc = ref.cell_index()
                 fl_cell.append(fc); mo_cell.append(mc)
+                if st:
+                    # output-step observables (star-polymers.cpp:467-473, 483)
+                    obs.append(ref.observables())
+                    px, py = ref.velocity_profile(PROFILE_WIDTH)
+                    prof_x.append(px); prof_y.append(py)
         delrx.append(ref.delrx)
         if st:
             m = ref.get_monomers()
@@ -117,6 +124,9 @@ def run_scenario(name: str, sc: dict) -> dict:
                    fluid_pos=np.array(fl_pos), fluid_vel=np.array(fl_vel),
                    temperature=np.array(temps), fluid_cell=np.array(fl_cell),
                    mono_cell=np.array(mo_cell))
+        if obs:
+            out.update(observables=np.array(obs), profile_x=np.array(prof_x),
+                       profile_y=np.array(prof_y), profile_width=PROFILE_WIDTH)
     if st:
         out.update(mono_pos=np.array(m_pos), mono_vel=np.array(m_vel), mono_force=np.array(m_frc),
                    gyration=ref.gyration())

@@ -50,6 +50,13 @@ def test_fp64_replays_reference_fixture(path):
                     H.close64(p, fx["fluid_pos"][k])
                     H.close64(v, fx["fluid_vel"][k])
                     H.close64(ctx.temperature(0), fx["temperature"][k])
+                    if "observables" in fx:
+                        # output-step observables and the VelocityX profile
+                        H.close64(ctx.molecule_observables_all()[0], fx["observables"][k])
+                        px, py = ctx.velocity_profile(0, float(fx["profile_width"]))
+                        for got, want in ((px, fx["profile_x"][k]), (py, fx["profile_y"][k])):
+                            np.testing.assert_array_equal(got[:, 2], want[:, 2])
+                            H.close64(got[:, :2], want[:, :2])
                 else:
                     ctx.mpc_step(t, float(fx["h"]))
             assert ctx.delrx(0) == fx["delrx"][t]
@@ -434,3 +441,83 @@ def test_fp32_md_variants_track_fp64_oracle(md_variant):
             np.testing.assert_allclose(mp, op, atol=1e-4)
             np.testing.assert_allclose(mv, ov, atol=2e-3 * np.abs(ov).max())
             np.testing.assert_allclose(mf, of, atol=2e-3 * np.abs(of).max())
+
+
+def _numpy_observables(pos, vel, mass, mol_start):
+    """The reference's output-step observables (Box.cpp:81-102, 288-294,
+    330-379, 635-646) restated in numpy for one replica."""
+    rg, G, w, ekin = 0.0, np.zeros((3, 3)), np.zeros(3), 0.0
+    for a, b in zip(mol_start[:-1], mol_start[1:]):
+        r = pos[a:b] - pos[a:b].mean(axis=0)
+        u = vel[a:b] - vel[a:b].mean(axis=0)
+        g = r.T @ r / (b - a)
+        G += g
+        rg += np.sqrt(np.trace(g))
+        S = r.T @ r
+        w += np.linalg.solve(np.trace(S) * np.eye(3) - S, np.cross(r, u).sum(axis=0))
+        ekin += 0.5 * (mass[a:b] * (u * u).sum(axis=1)).sum()
+    nm = len(mol_start) - 1
+    n = mol_start[-1]
+    return np.concatenate([[rg / nm], (G / nm).ravel(), w / nm, [ekin, ekin * 2 / (3 * (n - 1)), nm]])
+
+
+def _numpy_profile(fpos, fvel, c_pos, c_vel, L, shear, delrx, width):
+    p = fpos - c_pos
+    v = fvel - c_vel
+    cy = np.round(p[:, 1] / L[1]) if shear != 0 else np.zeros(len(p))
+    if shear != 0:
+        p[:, 0] -= L[0] * np.round(p[:, 0] / L[0])
+        p[:, 0] -= cy * delrx
+        p[:, 0] -= L[0] * np.round(p[:, 0] / L[0])
+        p[:, 1] -= L[1] * cy
+        v[:, 0] -= cy * shear * L[1]
+    else:
+        p[:, 0] -= np.round(p[:, 0] / L[0]) * L[0]
+        p[:, 1] -= np.round(p[:, 1] / L[1]) * L[1]
+    out = []
+    for ax in (0, 1):
+        k0 = np.floor(-L[ax] / (2 * width))
+        k = (np.floor(p[:, ax] / width) - k0).astype(int)
+        n = capi.profile_bins(L[ax], width)
+        prof = np.zeros((n, 3))
+        np.add.at(prof[:, 0], k, v[:, 0])
+        np.add.at(prof[:, 1], k, v[:, 1])
+        np.add.at(prof[:, 2], k, 1.0)
+        out.append(prof)
+    return out
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.FP32])
+def test_observables_of_every_replica_match_numpy(precision):
+    # batched layout (monomer offsets per replica), molecules set by the
+    # caller, both precisions: the device observables against a numpy
+    # restatement of the reference's definitions on the same state
+    ctx, _, specs = _batch_run(precision, cycles=1)
+    with ctx:
+        n1 = None
+        for k, s in enumerate(specs):
+            if k == 1:  # split replica 1's star into two molecules
+                n = ctx.replicas[k]["n_mono"]
+                n1 = n // 3
+                ctx.set_molecules(k, [0, n1, n])
+        obs = ctx.molecule_observables_all()
+        width = 0.2
+        for k, s in enumerate(specs):
+            pos, vel, _ = ctx.get_monomers(k)
+            mass = np.full(len(pos), s.mono_mass)
+            n = len(pos)
+            ms = [0, n1, n] if k == 1 else [0, n]
+            want = _numpy_observables(pos, vel, mass, ms)
+            tol = 1e-9 if precision == capi.FP64 else 1e-5
+            np.testing.assert_allclose(obs[k], want, rtol=tol, atol=tol * np.abs(want).max())
+            fp, fv = ctx.get_fluid(k)
+            L = (s.L,) * 3
+            px, py = ctx.velocity_profile(k, width)
+            c_pos, c_vel = pos[:ms[1]].mean(axis=0), vel[:ms[1]].mean(axis=0)
+            wx, wy = _numpy_profile(fp, fv, c_pos, c_vel, L, s.shear, ctx.delrx(k), width)
+            for got, want_p in ((px, wx), (py, wy)):
+                # a particle within rounding of a bin face may fall on either side
+                assert np.abs(got[:, 2] - want_p[:, 2]).sum() <= 4
+                assert abs(got[:, 2].sum() - len(fp)) == 0
+                np.testing.assert_allclose(got[:, :2].sum(axis=0), want_p[:, :2].sum(axis=0),
+                                           rtol=1e-6, atol=1e-6 * len(fp))
