@@ -35,6 +35,18 @@ __device__ __forceinline__ float wrap_f(float x, float L, float half) {
   return x >= half ? __fsub_rn(x, L) : (x < -half ? __fadd_rn(x, L) : x);
 }
 
+// The same two functions without their general-rounding branches, as
+// selects: img_sel is img_f for |y| < 1.5 L, wrap_sel is wrap_f for
+// |x| < 2.5 L, bit for bit (x - c L with c in {-1, 0, 1} is exact or one
+// correctly rounded add either way).
+__device__ __forceinline__ float img_sel(float y, float half) {
+  return y >= half ? 1.0f : (y < -half ? -1.0f : 0.0f);
+}
+__device__ __forceinline__ float wrap_sel(float x, float L, float half) {
+  x = fmaf(-img_sel(x, half), L, x);
+  return fmaf(-img_sel(x, half), L, x);
+}
+
 // Recentre (MPC::check_bounds, MPC.cpp:183-188, incl. its LE wrap) and
 // stream (MPC.cpp:194): X = x + v h, unwrapped. Explicitly rounded so the
 // bin and collide kernels produce identical X.
@@ -209,8 +221,8 @@ template <int NT>
 __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const FrameF& f,
                                                   const Tile& t, const uint32_t* s_off, int nc,
                                                   uint32_t p0, int nloc, const float4* s_x,
-                                                  const float4* s_v, short* s_lc, float* s_cmv,
-                                                  float* s_rot, unsigned long long seed,
+                                                  const float4* s_v, short* s_lc, float4* s_rc,
+                                                  unsigned long long seed,
                                                   unsigned long long step, uint32_t cbase) {
   const float* st_in = A.st_in;
   const float* mpos = A.mpos;
@@ -229,6 +241,12 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
     const bool live = lc < nc;
     const int j0 = live ? static_cast<int>(s_off[lc] - p0) : 0;
     const int j1 = live ? static_cast<int>(s_off[lc + 1] - p0) : 0;
+    // One pass: P = sum m v and S = sum m |v|^2, both int64 fixed point (exact
+    // and independent of the particles' order), then c = P / M and
+    // E = (S - |P|^2 / M) / 2. S is kept at 2^24 fixed point (the m |v|^2
+    // terms are pre-scaled by 2^-8) so fast shear flows stay in range; the
+    // one float subtraction costs ~1e-5 relative in E at a cell velocity of
+    // ten thermal speeds.
     long long px = 0, py = 0, pz = 0, e = 0;
     int nsol = 0;
     float mmono = 0.0f;
@@ -248,6 +266,7 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
       px += f2fix32(v.x * v.w);
       py += f2fix32(v.y * v.w);
       pz += f2fix32(v.z * v.w);
+      e += f2fix32((v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z));
       if (__float_as_uint(x.w) & MONO_BIT) {
         mmono += v.w;
       } else {
@@ -257,60 +276,91 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
     px += __shfl_xor_sync(0xFFFFFFFFu, px, 1);
     py += __shfl_xor_sync(0xFFFFFFFFu, py, 1);
     pz += __shfl_xor_sync(0xFFFFFFFFu, pz, 1);
+    e += __shfl_xor_sync(0xFFFFFFFFu, e, 1);
     nsol += __shfl_xor_sync(0xFFFFFFFFu, nsol, 1);
     mmono += __shfl_xor_sync(0xFFFFFFFFu, mmono, 1);
     const float mt = fmaf(i2f_small(nsol), f.solvent_mass, mmono);
     const float inv = mt > 0.f ? 1.0f / mt : 0.0f;
-    const float cm0 = fix32_to_f(px) * inv, cm1 = fix32_to_f(py) * inv,
-                cm2 = fix32_to_f(pz) * inv;
-    for (int j = j0 + half; j < j1; j += 2) {
-      float4 v;
-      if (j < nloc) {
-        v = s_v[j];
-      } else {
-        FastP P;
-        fetch_f(P, perm[p0 + j], st_in, mpos, mvel, mimg, f, mono_bin);
-        frame_f(P, f, f.solvent_mass);
-        v = P.v;
-      }
-      const float d0 = v.x - cm0, d1 = v.y - cm1, d2 = v.z - cm2;
-      e += f2fix32(v.w * (d0 * d0 + d1 * d1 + d2 * d2));
-    }
-    e += __shfl_xor_sync(0xFFFFFFFFu, e, 1);
-    const float ekin = fix32_to_f(e) * 0.5f;
+    const float q0 = fix32_to_f(px), q1 = fix32_to_f(py), q2 = fix32_to_f(pz);
+    const float cm0 = q0 * inv, cm1 = q1 * inv, cm2 = q2 * inv;
+    const float ekin =
+        fmaxf(0.5f * (fix32_to_f(e) * 256.0f - (q0 * q0 + q1 * q1 + q2 * q2) * inv), 0.0f);
     const uint32_t cg = static_cast<uint32_t>(t.begin + lc);
     const uint32_t cl = cg - cbase;
     const uint32_t nn = static_cast<uint32_t>(j1 - j0);
     float scale = -1.0f;
-    float M[9];
-    if (half == 0) {
-      if (live && nn >= 2u) {
-        float gv;
-        if (rng == RNG_INJECT) {
-          gv = static_cast<float>(inj_gamma[cg]);
-        } else {
-          bool ok = true;
-          gv = philox_gamma<float>(seed, cl, step, 1.5f * i2f_small(static_cast<int>(nn - 1u)), &ok) *
-               f.kT;
-          if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // rotation axis (lane 1)
+    if (rng == RNG_INJECT) {
+      if (half == 0) {
+        if (live && nn >= 2u) {
+          const float gv = static_cast<float>(inj_gamma[cg]);
+          scale = ekin > 0.f ? sqrtf(gv / ekin) : 1.0f;
         }
-        scale = ekin > 0.f ? sqrtf(gv / ekin) : 1.0f;
+      } else if (live) {
+        const float uphi = static_cast<float>(inj_uphi[cg]);
+        const float theta = 2.0f * (static_cast<float>(inj_utheta[cg]) - 0.5f);
+        const float stt = sqrtf(1.0f - theta * theta);
+        float sphi, cphi;
+        sincosf(6.283185307179586f * uphi, &sphi, &cphi);
+        a0 = stt * cphi;
+        a1 = stt * sphi;
+        a2 = theta;
       }
-    } else if (live) {
-      float uphi, uth;
-      if (rng == RNG_INJECT) {
-        uphi = static_cast<float>(inj_uphi[cg]);
-        uth = static_cast<float>(inj_utheta[cg]);
+    } else {
+      // Both lanes of a cell draw at once: lane 1 the axis block (k = 0),
+      // lane 0 the first normal pair of the gamma sampler (k = 1); then one
+      // r = sqrt(t), sincos(2 pi w) serves both (lane 0: t = -2 ln u_a,
+      // w = u_b, normal r cos; lane 1: t = 1 - theta^2, w = u_phi, axis
+      // (r cos, r sin, theta)). Same stream and formulas as philox_gamma /
+      // philox_uniforms.
+      const Philox4 b = philox4x32_10(cl, static_cast<uint32_t>(step),
+                                      static_cast<uint32_t>(step >> 32), half ? 0u : 1u,
+                                      static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+      const float ua = u24(b.w[1]), ub = u24(b.w[3]);
+      const float theta = 2.0f * (ub - 0.5f);
+      const float lg = logf(half ? 1.0f : ua);
+      const float r = sqrtf(half ? 1.0f - theta * theta : -2.0f * lg);
+      float sn, cs;
+      sincosf(6.283185307179586f * (half ? ua : ub), &sn, &cs);
+      if (half == 0) {
+        if (live && nn >= 2u) {
+          // Marsaglia-Tsang, iteration 0 with the normal above, further
+          // iterations (rare) exactly as philox_gamma
+          const float shape = 1.5f * i2f_small(static_cast<int>(nn - 1u));
+          const float d = shape - 1.0f / 3.0f;
+          const float c9 = 1.0f / sqrtf(9.0f * d);
+          float x = r * cs;
+          float gv = -1.0f;
+          for (uint32_t it = 0; it < 64u; ++it) {
+            if (it > 0) {
+              const Uniform2<float> n2 = philox_uniforms<float>(seed, cl, step, 1u + 2u * it);
+              x = sqrtf(-2.0f * logf(n2.a)) * cosf(6.283185307179586f * n2.b);
+            }
+            float v = 1.0f + c9 * x;
+            if (v <= 0.0f) continue;
+            v = v * v * v;
+            const float u = philox_uniforms<float>(seed, cl, step, 2u + 2u * it).a;
+            const float x2 = x * x;
+            if (u < 1.0f - 0.0331f * (x2 * x2) || logf(u) < 0.5f * x2 + d * (1.0f - v + logf(v))) {
+              gv = d * v;
+              break;
+            }
+          }
+          if (gv < 0.0f) {
+            raise_error(err, ERR_GAMMA_ITERS, cg, nn);
+            gv = d;
+          }
+          gv *= f.kT;
+          scale = ekin > 0.f ? sqrtf(gv / ekin) : 1.0f;
+        }
       } else {
-        const Uniform2<float> u = philox_uniforms<float>(seed, cl, step, 0u);
-        uphi = u.a;
-        uth = u.b;
+        a0 = r * cs;
+        a1 = r * sn;
+        a2 = theta;
       }
-      const float theta = 2.0f * (uth - 0.5f);
-      const float stt = sqrtf(1.0f - theta * theta);
-      float sphi, cphi;
-      sincosf(6.283185307179586f * uphi, &sphi, &cphi);
-      const float a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
+    }
+    float M[9];
+    if (half == 1) {
       const float c = f.rot_c, s = f.rot_s;
       M[0] = a0 * a0 + (1.0f - a0 * a0) * c;
       M[1] = a0 * a1 * (1.0f - c) - a2 * s;
@@ -325,11 +375,10 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
     scale = __shfl_xor_sync(0xFFFFFFFFu, scale, 1);
     if (half == 1 && live) {
       const float sc = scale >= 0.0f ? scale : 1.0f;  // thermostat folded into R
-#pragma unroll
-      for (int q = 0; q < 9; ++q) s_rot[9 * lc + q] = M[q] * sc;
-      s_cmv[3 * lc] = cm0;
-      s_cmv[3 * lc + 1] = cm1;
-      s_cmv[3 * lc + 2] = cm2;
+      // row q of sR with component q of the cell's velocity in .w
+      s_rc[3 * lc] = make_float4(M[0] * sc, M[1] * sc, M[2] * sc, cm0);
+      s_rc[3 * lc + 1] = make_float4(M[3] * sc, M[4] * sc, M[5] * sc, cm1);
+      s_rc[3 * lc + 2] = make_float4(M[6] * sc, M[7] * sc, M[8] * sc, cm2);
     }
   }
 }
@@ -339,8 +388,7 @@ template <int NT>
 __device__ __forceinline__ void collide_apply_f32(const CollideF32Args& A, const FrameF& f,
                                                   const uint32_t* s_off, uint32_t p0, int n,
                                                   int nloc, const float4* s_x, const float4* s_v,
-                                                  const short* s_lc, const float* s_cmv,
-                                                  const float* s_rot) {
+                                                  const short* s_lc, const float4* s_rc) {
   const float* st_in = A.st_in;
   float* st_out = A.st_out;
   const float* mpos = A.mpos;
@@ -366,12 +414,11 @@ __device__ __forceinline__ void collide_apply_f32(const CollideF32Args& A, const
       lc = 0;
       while (static_cast<int>(s_off[lc + 1] - p0) <= j) ++lc;
     }
-    const float* cm = s_cmv + 3 * lc;
-    const float* M = s_rot + 9 * lc;
-    const float d0 = v.x - cm[0], d1 = v.y - cm[1], d2 = v.z - cm[2];
-    float vx = cm[0] + (M[0] * d0 + M[1] * d1 + M[2] * d2);
-    const float vy = cm[1] + (M[3] * d0 + M[4] * d1 + M[5] * d2);
-    const float vz = cm[2] + (M[6] * d0 + M[7] * d1 + M[8] * d2);
+    const float4 r0 = s_rc[3 * lc], r1 = s_rc[3 * lc + 1], r2 = s_rc[3 * lc + 2];
+    const float d0 = v.x - r0.w, d1 = v.y - r1.w, d2 = v.z - r2.w;
+    float vx = r0.w + (r0.x * d0 + r0.y * d1 + r0.z * d2);
+    const float vy = r1.w + (r1.x * d0 + r1.y * d1 + r1.z * d2);
+    const float vz = r2.w + (r2.x * d0 + r2.y * d1 + r2.z * d2);
     const uint32_t tag = __float_as_uint(x.w);
     if (!(isfinite(vx) && isfinite(vy) && isfinite(vz))) raise_error(err, ERR_NONFINITE, p0 + j, tag);
     const size_t p = static_cast<size_t>(p0) + j;
@@ -388,8 +435,26 @@ __device__ __forceinline__ void collide_apply_f32(const CollideF32Args& A, const
     } else {
       // final image c_t of the streamed point; the velocity already carries -c_s
       float ys = __fadd_rn(x.y, f.shift[1]);
-      const float cs = f.shear_on ? img_f(ys, f.L[1], f.half[1]) : 0.0f;
       float X = x.x, Y = x.y, Z = x.z;
+      if (fabsf(X) < 1.5f * f.L[0] && fabsf(ys) < 1.5f * f.L[1] && fabsf(Y) < 1.5f * f.L[1] &&
+          fabsf(Z) < 1.5f * f.L[2]) {
+        // every streamed point in practice: selects only
+        if (f.shear_on) {
+          const float cs = img_sel(ys, f.half[1]);
+          const float ct = img_sel(Y, f.half[1]);
+          Y = fmaf(-ct, f.L[1], Y);
+          X = wrap_sel(fmaf(-ct, f.delrx, X), f.L[0], f.half[0]);
+          vx = fmaf(-(ct - cs), f.shearLy, vx);
+        } else {
+          X = wrap_sel(X, f.L[0], f.half[0]);
+          Y = wrap_sel(Y, f.L[1], f.half[1]);
+        }
+        Z = wrap_sel(Z, f.L[2], f.half[2]);
+        st_f4(st_out, 2 * p, make_float4(X, Y, Z, x.w));
+        st_f4(st_out, 2 * p + 1, make_float4(vx, vy, vz, 0.f));
+        continue;
+      }
+      const float cs = f.shear_on ? img_f(ys, f.L[1], f.half[1]) : 0.0f;
       if (f.shear_on) {
         const float ct = img_f(Y, f.L[1], f.half[1]);
         Y = __fsub_rn(Y, __fmul_rn(ct, f.L[1]));
@@ -414,8 +479,7 @@ __global__ void __launch_bounds__(NT) k_collide_f32(
     const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
     int rng, int mono_bin, ErrorState* err) {
   static_assert(NT == 2 * CT, "two threads per cell");
-  __shared__ float s_cmv[CT * 3];
-  __shared__ float s_rot[CT * 9];
+  __shared__ float4 s_rc[CT * 3];  // per cell: rows of sR, cell velocity in .w
   __shared__ uint32_t s_off[CT + 1];
   extern __shared__ __align__(16) unsigned char s_dyn[];
   float4* s_x = reinterpret_cast<float4*>(s_dyn);
@@ -464,10 +528,10 @@ __global__ void __launch_bounds__(NT) k_collide_f32(
 
   const CollideF32Args A{st_in, st_out, mpos, mvel, mimg, perm, inj_gamma, inj_uphi, inj_utheta,
                          rng, mono_bin, err};
-  collide_cells_f32<NT>(A, f, t, s_off, nc, p0, nloc, s_x, s_v, s_lc, s_cmv, s_rot, seed, step,
+  collide_cells_f32<NT>(A, f, t, s_off, nc, p0, nloc, s_x, s_v, s_lc, s_rc, seed, step,
                         cbase);
   __syncthreads();
-  collide_apply_f32<NT>(A, f, s_off, p0, n, nloc, s_x, s_v, s_lc, s_cmv, s_rot);
+  collide_apply_f32<NT>(A, f, s_off, p0, n, nloc, s_x, s_v, s_lc, s_rc);
 }
 
 // ------------------------------------------------- collide, cp.async staging
@@ -497,8 +561,7 @@ __global__ void __launch_bounds__(NT) k_collide_f32_async(
     int rng, int mono_bin, ErrorState* err) {
   static_assert(NT == 2 * CT, "two threads per cell");
   constexpr int J = (CAP + NT - 1) / NT;  // staged particles per thread
-  __shared__ float s_cmv[CT * 3];
-  __shared__ float s_rot[CT * 9];
+  __shared__ float4 s_rc[CT * 3];  // per cell: rows of sR, cell velocity in .w
   __shared__ uint32_t s_off[CT + 1];
   extern __shared__ __align__(16) unsigned char s_dyn[];
   float4* s_x = reinterpret_cast<float4*>(s_dyn);
@@ -522,13 +585,14 @@ __global__ void __launch_bounds__(NT) k_collide_f32_async(
 #pragma unroll
   for (int u = 0; u < J; ++u) {
     const int j = u * NT + threadIdx.x;
-    if (src[u] == 0xFFFFFFFFu) continue;
-    if (src[u] & MONO_BIT) {
-      cp_async16(s_v + j, mvel + 4 * static_cast<size_t>(src[u] & ~MONO_BIT));
-      s_x[j] = make_float4(0.f, 0.f, 0.f, __uint_as_float(src[u]));
-    } else {
-      cp_async16(s_x + j, st_in + 8 * static_cast<size_t>(src[u]));
-      cp_async16(s_v + j, st_in + 8 * static_cast<size_t>(src[u]) + 4);
+    if (src[u] != 0xFFFFFFFFu) {
+      if (src[u] & MONO_BIT) {
+        cp_async16(s_v + j, mvel + 4 * static_cast<size_t>(src[u] & ~MONO_BIT));
+        s_x[j] = make_float4(0.f, 0.f, 0.f, __uint_as_float(src[u]));
+      } else {
+        cp_async16(s_x + j, st_in + 8 * static_cast<size_t>(src[u]));
+        cp_async16(s_v + j, st_in + 8 * static_cast<size_t>(src[u]) + 4);
+      }
     }
   }
   const FrameF f = frames[t.rep];
@@ -539,7 +603,7 @@ __global__ void __launch_bounds__(NT) k_collide_f32_async(
 #pragma unroll
   for (int u = 0; u < J; ++u) {
     const int j = u * NT + threadIdx.x;
-    if (src[u] == 0xFFFFFFFFu) continue;
+    if (src[u] == 0xFFFFFFFFu) break;  // this thread's remaining slots are past nloc too
     FastP P;
     P.x = s_x[j];
     P.v = s_v[j];
@@ -558,10 +622,10 @@ __global__ void __launch_bounds__(NT) k_collide_f32_async(
 
   const CollideF32Args A{st_in, st_out, mpos, mvel, mimg, perm, inj_gamma, inj_uphi, inj_utheta,
                          rng, mono_bin, err};
-  collide_cells_f32<NT>(A, f, t, s_off, nc, p0, nloc, s_x, s_v, s_lc, s_cmv, s_rot, ri.seed,
+  collide_cells_f32<NT>(A, f, t, s_off, nc, p0, nloc, s_x, s_v, s_lc, s_rc, ri.seed,
                         dyn[t.rep].step, static_cast<uint32_t>(ri.cell_base));
   __syncthreads();
-  collide_apply_f32<NT>(A, f, s_off, p0, n, nloc, s_x, s_v, s_lc, s_cmv, s_rot);
+  collide_apply_f32<NT>(A, f, s_off, p0, n, nloc, s_x, s_v, s_lc, s_rc);
 }
 
 }  // namespace smpc
