@@ -23,7 +23,6 @@ import concurrent.futures as cf
 import csv
 import io
 import json
-import math
 import os
 import subprocess
 import sys
@@ -321,12 +320,13 @@ def fp64_plain_ratio(workload, built, batched_rep_steps):
 def e2e_measure(ctx, built, K):
     """Through the C ABI with host buffers: per cycle, upload every monomer's
     position and velocity from pinned host memory, run the cycle, read the
-    monomer state and every replica's temperature back."""
+    monomer state and every replica's output-step observables back (gyration
+    tensor, rotation frequency, polymer kinetic energy and temperature: what
+    the reference driver reads after a step, star-polymers.cpp:466-473)."""
     import torch
     n = int(sum(built.n_mono))
     pos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     vel = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
-    temps = np.zeros(built.n_rep)
     ctx.get_monomer_state_all(pos, vel)
     k = max(3, min(K, 50))
     ctx.synchronize()
@@ -335,17 +335,17 @@ def e2e_measure(ctx, built, K):
         ctx.set_monomer_state_all(pos, vel)
         ctx.cycles(1)
         ctx.get_monomer_state_all(pos, vel)
-        ctx.temperature_all(temps)
+        obs = ctx.molecule_observables_all()
     dt = time.perf_counter() - t0
     ctx.raise_on_device_error()
-    if not np.all(np.isfinite(temps)):
-        raise RuntimeError("non-finite temperature")
+    if not np.all(np.isfinite(obs)):
+        raise RuntimeError("non-finite observables")
     h2d = n * 2 * 16  # float4 positions + velocities
-    n_tiles = sum(math.ceil(s.L ** 3 / 512) for s in built.specs)
-    d2h = n * 2 * 16 + n_tiles * 16
+    d2h = n * 2 * 16 + built.n_rep * 16 * 8
     return {"value": built.particles * k / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": k,
-            "what": "per cycle: monomer state up, cycle, monomer state + temperatures down"}
+            "what": "per cycle: monomer state up, cycle, monomer state + per-replica "
+                    "gyration tensor / rotation frequency / polymer temperature down"}
 
 
 # ---------------------------------------------------------- reference arm

@@ -160,6 +160,58 @@ void launch_velocity_profile<Real>(const RepInfo* reps, const int2* rep_mols, co
       reps, rep, rec, delrx, width, kx0, nx, ky0, ny, c6, bins);
 }
 
+template <typename R>
+__global__ void k_unpack_monomers(const double* __restrict__ stage, int n, R* mpos, R* mvel) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* p = stage + 3 * static_cast<size_t>(i);
+  const double* v = stage + 3 * (static_cast<size_t>(n) + i);
+  R4<R> x = ld4_rw(mpos, i), u = ld4_rw(mvel, i);
+  x.x = static_cast<R>(p[0]);
+  x.y = static_cast<R>(p[1]);
+  x.z = static_cast<R>(p[2]);
+  u.x = static_cast<R>(v[0]);
+  u.y = static_cast<R>(v[1]);
+  u.z = static_cast<R>(v[2]);
+  st4(mpos, i, x);
+  st4(mvel, i, u);
+}
+
+template <typename R>
+__global__ void k_pack_monomers(const R* mpos, const R* mvel, const R* mfrc, int n,
+                                double* __restrict__ stage) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const R4<R> x = ld4_rw(mpos, i), u = ld4_rw(mvel, i);
+  double* p = stage + 3 * static_cast<size_t>(i);
+  double* v = stage + 3 * (static_cast<size_t>(n) + i);
+  p[0] = static_cast<double>(x.x);
+  p[1] = static_cast<double>(x.y);
+  p[2] = static_cast<double>(x.z);
+  v[0] = static_cast<double>(u.x);
+  v[1] = static_cast<double>(u.y);
+  v[2] = static_cast<double>(u.z);
+  if (mfrc) {
+    const R4<R> fr = ld4_rw(mfrc, i);
+    double* q = stage + 3 * (2 * static_cast<size_t>(n) + i);
+    q[0] = static_cast<double>(fr.x);
+    q[1] = static_cast<double>(fr.y);
+    q[2] = static_cast<double>(fr.z);
+  }
+}
+
+template <>
+void launch_unpack_monomers<Real>(const double* stage, int n, Real* mpos, Real* mvel,
+                                  cudaStream_t st) {
+  if (n > 0) k_unpack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(stage, n, mpos, mvel);
+}
+
+template <>
+void launch_pack_monomers<Real>(const Real* mpos, const Real* mvel, const Real* mfrc, int n,
+                                double* stage, cudaStream_t st) {
+  if (n > 0) k_pack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(mpos, mvel, mfrc, n, stage);
+}
+
 template <>
 void launch_md<Real>(const MdArgs& a, int n_rep, Real* mpos, Real* mvel, Real* mfrc, Real* mver,
                      int variant, cudaStream_t st) {

@@ -90,6 +90,14 @@ void launch_velocity_profile(const RepInfo* reps, const int2* rep_mols, const in
                              double delrx, double width, long long kx0, int nx, long long ky0,
                              int ny, double* c6, double* bins, cudaStream_t st);
 
+// Monomer state between the C ABI's x,y,z-interleaved doubles and the device
+// records (pos.w / vel.w keep mass and type): stage = pos[3M] | vel[3M] | force[3M]
+template <typename R>
+void launch_unpack_monomers(const double* stage, int n, R* mpos, R* mvel, cudaStream_t st);
+template <typename R>
+void launch_pack_monomers(const R* mpos, const R* mvel, const R* mfrc, int n, double* stage,
+                          cudaStream_t st);
+
 void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* grand, int n_cells,
                  cudaStream_t st);
 int scan_tile_count(int n_cells);

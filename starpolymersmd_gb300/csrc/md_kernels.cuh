@@ -56,6 +56,30 @@ __device__ __forceinline__ R pair_force(int pot, bool bb, R r2, R lambda) {
   return R(0);
 }
 
+// FP32: 1/r2 as the correctly rounded reciprocal (the same bits as the
+// division, without its general path)
+template <>
+__device__ __forceinline__ float pair_force<float>(int pot, bool bb, float r2, float lambda) {
+  if (pot == POT_REF4824) {
+    if (r2 < 1.0594631f || (bb && r2 < 2.25f)) {
+      const float rm2 = __frcp_rn(r2);
+      float rm24 = rm2 * rm2 * rm2;
+      rm24 *= rm24;
+      rm24 *= rm24;
+      const float f = 192.0f * rm2 * rm24 * (rm24 - 0.5f);
+      return r2 < 1.0594631f ? f : lambda * f;
+    }
+    return 0.0f;
+  }
+  if (r2 < 1.2599210498948732f || (bb && r2 < 6.25f)) {
+    const float rm2 = __frcp_rn(r2);
+    const float rm6 = rm2 * rm2 * rm2;
+    const float f = 48.0f * rm2 * rm6 * (rm6 - 0.5f);
+    return r2 < 1.2599210498948732f ? f : lambda * f;
+  }
+  return 0.0f;
+}
+
 template <typename R>
 __device__ __forceinline__ R pair_pot(int pot, bool bb, R r2, R lambda) {
   if (pot == POT_REF4824) {
@@ -89,6 +113,10 @@ __device__ __forceinline__ R pair_pot(int pot, bool bb, R r2, R lambda) {
 template <typename R>
 __device__ __forceinline__ R fene_force(bool anchor, R r2) {
   return anchor ? R(-30.0) / (R(1.0) - (r2 / R(20.25))) : R(-30.0) / (R(1.0) - (r2 / R(2.25)));
+}
+template <>
+__device__ __forceinline__ float fene_force<float>(bool anchor, float r2) {
+  return -30.0f * __frcp_rn(1.0f - r2 * (anchor ? 1.0f / 20.25f : 1.0f / 2.25f));
 }
 template <typename R>
 __device__ __forceinline__ R fene_pot(bool anchor, R r2) {

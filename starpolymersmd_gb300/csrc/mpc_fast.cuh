@@ -250,27 +250,59 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
     long long px = 0, py = 0, pz = 0, e = 0;
     int nsol = 0;
     float mmono = 0.0f;
-    for (int j = j0 + half; j < j1; j += 2) {
-      float4 v, x;
-      if (j < nloc) {
-        v = s_v[j];
-        x = s_x[j];
-        s_lc[j] = static_cast<short>(lc);
-      } else {  // past the staging capacity: straight from global memory
-        FastP P;
-        fetch_f(P, perm[p0 + j], st_in, mpos, mvel, mimg, f, mono_bin);
-        frame_f(P, f, f.solvent_mass);
-        v = P.v;
-        x = P.x;
+    if (j1 - j0 <= 1024) {
+      // at most 512 terms per lane: int32 split accumulators
+      int xh = 0, xl = 0, yh = 0, yl = 0, zh = 0, zl = 0, eh = 0, el = 0;
+      for (int j = j0 + half; j < j1; j += 2) {
+        float4 v, x;
+        if (j < nloc) {
+          v = s_v[j];
+          x = s_x[j];
+          s_lc[j] = static_cast<short>(lc);
+        } else {  // past the staging capacity: straight from global memory
+          FastP P;
+          fetch_f(P, perm[p0 + j], st_in, mpos, mvel, mimg, f, mono_bin);
+          frame_f(P, f, f.solvent_mass);
+          v = P.v;
+          x = P.x;
+        }
+        fix32_add(v.x * v.w, xh, xl);
+        fix32_add(v.y * v.w, yh, yl);
+        fix32_add(v.z * v.w, zh, zl);
+        fix32_add((v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z), eh, el);
+        if (__float_as_uint(x.w) & MONO_BIT) {
+          mmono += v.w;
+        } else {
+          ++nsol;
+        }
       }
-      px += f2fix32(v.x * v.w);
-      py += f2fix32(v.y * v.w);
-      pz += f2fix32(v.z * v.w);
-      e += f2fix32((v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z));
-      if (__float_as_uint(x.w) & MONO_BIT) {
-        mmono += v.w;
-      } else {
-        ++nsol;
+      px = fix32_join(xh, xl);
+      py = fix32_join(yh, yl);
+      pz = fix32_join(zh, zl);
+      e = fix32_join(eh, el);
+    } else {
+      for (int j = j0 + half; j < j1; j += 2) {
+        float4 v, x;
+        if (j < nloc) {
+          v = s_v[j];
+          x = s_x[j];
+          s_lc[j] = static_cast<short>(lc);
+        } else {
+          FastP P;
+          fetch_f(P, perm[p0 + j], st_in, mpos, mvel, mimg, f, mono_bin);
+          frame_f(P, f, f.solvent_mass);
+          v = P.v;
+          x = P.x;
+        }
+        px += f2fix32(v.x * v.w);
+        py += f2fix32(v.y * v.w);
+        pz += f2fix32(v.z * v.w);
+        e += f2fix32((v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z));
+        if (__float_as_uint(x.w) & MONO_BIT) {
+          mmono += v.w;
+        } else {
+          ++nsol;
+        }
       }
     }
     px += __shfl_xor_sync(0xFFFFFFFFu, px, 1);

@@ -59,6 +59,22 @@ __device__ __forceinline__ long long f2fix32(float v) {
   return static_cast<long long>(hi) * 4194304ll + lo;
 }
 
+// The same value as f2fix32, added to split accumulators: hi (units of 2^-10)
+// and lo (units of 2^-32), each a plain int32 add; the sum is
+// hi * 2^22 + lo. |hi| < 2^22 and |lo| <= 2^21 per term, so 512 terms cannot
+// overflow either part.
+__device__ __forceinline__ void fix32_add(float v, int& hi_acc, int& lo_acc) {
+  v = fminf(fmaxf(v, -4095.0f), 4095.0f);
+  const float a = v * 1024.0f;
+  const float m = __fadd_rn(a, 12582912.0f);  // rn(a) in the low mantissa bits
+  const float r = __fsub_rn(a, __fsub_rn(m, 12582912.0f));  // a - rn(a), exact
+  hi_acc += __float_as_int(m) - 0x4B400000;
+  lo_acc += f2i_rn_small(r * 4194304.0f);
+}
+__device__ __forceinline__ long long fix32_join(int hi, int lo) {
+  return static_cast<long long>(hi) * 4194304ll + lo;
+}
+
 // int64 2^32 fixed point to float (three exact 21-bit pieces, one rounding).
 __device__ __forceinline__ float fix32_to_f(long long a) {
   const int a0 = static_cast<int>(a & 0x1FFFFFll);

@@ -94,7 +94,7 @@ struct smpc_ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   std::string err;
   // host staging reused across calls
-  void* h_stage = nullptr;          // pinned: 3 x 4 x total_mono Reals
+  double* d_dstage = nullptr;       // monomer state as the C ABI lays it out (9 x total_mono)
   std::vector<double> h_mass;       // per monomer (pos.w)
   std::vector<double> h_flags;      // amphi + 2*anchor (vel.w)
   std::vector<TempPartial> stage_t;
@@ -417,39 +417,37 @@ int get_monomers_t(smpc_ctx* ctx, int rep, double* pos, double* vel, double* for
 // All replicas' monomers in one transfer each way (replicas concatenated),
 // through pinned staging buffers allocated at creation. Masses and type flags
 // (the .w lanes) come from the host copy kept by smpc_set_monomers.
+// Every replica's monomers at once: the host arrays are copied as they are
+// (DMA at full speed when they are pinned) and converted on the device.
 template <typename R>
 int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, double* pos_out,
                    double* vel_out, double* force_out) {
   const size_t n = static_cast<size_t>(ctx->total_mono);
   if (n == 0) return SMPC_OK;
-  R* p = static_cast<R*>(ctx->h_stage);
-  R* v = p + 4 * n;
-  R* f = v + 4 * n;
+  const int ni = static_cast<int>(n);
   if (pos_in) {
-    for (size_t i = 0; i < n; ++i) {
-      for (int d = 0; d < 3; ++d) {
-        p[4 * i + d] = static_cast<R>(pos_in[3 * i + d]);
-        v[4 * i + d] = static_cast<R>(vel_in[3 * i + d]);
-      }
-      p[4 * i + 3] = static_cast<R>(ctx->h_mass[i]);
-      v[4 * i + 3] = static_cast<R>(ctx->h_flags[i]);
-    }
-    CU(cudaMemcpyAsync(ctx->d_mpos, p, 4 * n * sizeof(R), cudaMemcpyHostToDevice, ctx->st));
-    CU(cudaMemcpyAsync(ctx->d_mvel, v, 4 * n * sizeof(R), cudaMemcpyHostToDevice, ctx->st));
-    CU(cudaStreamSynchronize(ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_dstage, pos_in, 3 * n * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_dstage + 3 * n, vel_in, 3 * n * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->st));
+    smpc::launch_unpack_monomers<R>(ctx->d_dstage, ni, static_cast<R*>(ctx->d_mpos),
+                                    static_cast<R*>(ctx->d_mvel), ctx->st);
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(ctx->st));  // the host arrays are borrowed for the call only
     return SMPC_OK;
   }
-  CU(cudaMemcpyAsync(p, ctx->d_mpos, 4 * n * sizeof(R), cudaMemcpyDeviceToHost, ctx->st));
-  CU(cudaMemcpyAsync(v, ctx->d_mvel, 4 * n * sizeof(R), cudaMemcpyDeviceToHost, ctx->st));
+  smpc::launch_pack_monomers<R>(static_cast<const R*>(ctx->d_mpos), static_cast<const R*>(ctx->d_mvel),
+                                force_out ? static_cast<const R*>(ctx->d_mfrc) : nullptr, ni,
+                                ctx->d_dstage, ctx->st);
+  CU(cudaGetLastError());
+  if (pos_out)
+    CU(cudaMemcpyAsync(pos_out, ctx->d_dstage, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  if (vel_out)
+    CU(cudaMemcpyAsync(vel_out, ctx->d_dstage + 3 * n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->st));
   if (force_out)
-    CU(cudaMemcpyAsync(f, ctx->d_mfrc, 4 * n * sizeof(R), cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaMemcpyAsync(force_out, ctx->d_dstage + 6 * n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->st));
   CU(cudaStreamSynchronize(ctx->st));
-  for (size_t i = 0; i < n; ++i)
-    for (int d = 0; d < 3; ++d) {
-      if (pos_out) pos_out[3 * i + d] = static_cast<double>(p[4 * i + d]);
-      if (vel_out) vel_out[3 * i + d] = static_cast<double>(v[4 * i + d]);
-      if (force_out) force_out[3 * i + d] = static_cast<double>(f[4 * i + d]);
-    }
   return SMPC_OK;
 }
 
@@ -553,7 +551,7 @@ int create_buffers(smpc_ctx* ctx) {
   CU(cudaMemset(ctx->d_bond_start, 0, (M + 1) * sizeof(int)));
   CU(dalloc(&ctx->d_inj, 3 * C));
   CU(cudaMemset(ctx->d_inj, 0, 3 * C * sizeof(double)));
-  CU(cudaMallocHost(&ctx->h_stage, (12 * M + 4) * sizeof(R)));
+  CU(dalloc(&ctx->d_dstage, 9 * M));
   ctx->h_mass.assign(M, 1.0);
   ctx->h_flags.assign(M, 0.0);
   return SMPC_OK;
@@ -599,10 +597,9 @@ void free_all(smpc_ctx* ctx) {
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
                   ctx->d_mimg, ctx->d_bond_start, ctx->d_bonds, ctx->d_nlist, ctx->d_ncount,
                   ctx->d_md_order, ctx->d_inj, ctx->d_err, ctx->d_frames, ctx->d_rep_mols,
-                  ctx->d_mols, ctx->d_obs, ctx->d_prof, ctx->d_c6};
+                  ctx->d_mols, ctx->d_obs, ctx->d_prof, ctx->d_c6, ctx->d_dstage};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   for (int k = 0; k < 3; ++k)
     if (ctx->d_col_tiles_v[k]) cudaFree(ctx->d_col_tiles_v[k]);
   if (ctx->st) cudaStreamDestroy(ctx->st);
