@@ -47,6 +47,15 @@ enum { SMPC_RNG_INJECT = 0, SMPC_RNG_PHILOX = 1 };
 enum { SMPC_POT_REF4824 = 0, SMPC_POT_LJ126 = 1 };
 enum { SMPC_MONOBIN_REFERENCE = 0, SMPC_MONOBIN_WRAPPED = 1 };
 enum { SMPC_DELRX_REFERENCE = 0, SMPC_DELRX_PHYSICAL = 1 };
+/* Replica flags. SMPC_REPLICA_PERIODIC_MD: the box's monomers (any number of
+ * stars) interact through the Lees-Edwards minimum image and are kept in the
+ * primary box, with Verlet lists on a periodic cell grid and a rebuild
+ * criterion that includes the change of delrx; no recentring (mol0_size only
+ * names the default molecule 0). MD substep k of a call (k = 0, 1, ...) uses
+ * the delrx that k + 1 further MPC::step(t, h) calls will give (MPC.cpp:117-118).
+ * Needs mono_bin = SMPC_MONOBIN_WRAPPED and every L >= 3 r_verlet. The
+ * reference integrates one star without periodic images (Box.cpp:105-180). */
+enum { SMPC_REPLICA_PERIODIC_MD = 1 };
 
 /* One independent box (MPC + Box + Thermostat_None of the reference). */
 typedef struct {
@@ -64,7 +73,7 @@ typedef struct {
   double solvent_mass;    /* 1.0 in the reference (MPC.cpp:30) */
   uint64_t seed;          /* Philox key of this box */
   int potential;          /* SMPC_POT_* */
-  int pad;
+  int flags;              /* SMPC_REPLICA_* bits */
 } smpc_replica_desc;
 
 typedef struct {

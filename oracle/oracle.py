@@ -74,6 +74,7 @@ def _oracle_lib():
             "orc_mpc_step": [P, C.c_long, C.c_double], "orc_propagate": [P, C.c_int],
             "orc_run": [P, C.c_long, C.c_long, C.c_double, C.c_int],
             "orc_cell_counts": [P, P, P], "orc_philox4x32_10": [P, P, P],
+            "orc_set_periodic_md": [P, C.c_double],
         }.items():
             getattr(lib, name).argtypes = args
             getattr(lib, name).restype = None
@@ -163,6 +164,10 @@ class OracleSystem:
         src = np.ascontiguousarray(src, dtype=np.int32)
         dst = np.ascontiguousarray(dst, dtype=np.int32)
         self.lib.orc_set_bonds(self.h, len(src), _p(src), _p(dst))
+
+    def set_periodic_md(self, h):
+        """Periodic many-molecule MD (before init_md; needs mono_wrap=1)."""
+        self.lib.orc_set_periodic_md(self.h, float(h))
 
     def init_md(self):
         self.lib.orc_init_md(self.h)

@@ -86,6 +86,13 @@ struct smpc_orc {
   uint64_t seed;
   uint64_t step_ctr;
 
+  /* periodic MD of many molecules (orc_set_periodic_md) */
+  int periodic;
+  double pmd_h;       /* MPC step the per-substep delrx is extrapolated with */
+  int* adj_start;     /* undirected bond lists, per monomer: [n_m + 1] */
+  int* adj_idx;
+  unsigned char* adj_anchor;
+
   int err;
 };
 
@@ -307,6 +314,7 @@ void orc_destroy(smpc_orc* o) {
   free(o->vcell_head); free(o->vcell_next); free(o->c_tot); free(o->c_fl); free(o->c_start);
   free(o->c_mem);
   free(o->m_img);
+  free(o->adj_start); free(o->adj_idx); free(o->adj_anchor);
   free(o);
 }
 
@@ -558,13 +566,25 @@ static void forces_verlet(smpc_orc* o, int calc_epot) {
   }
 }
 
+static void pmd_init(smpc_orc* o);
+
 void orc_init_md(smpc_orc* o) {
+  if (o->periodic) {
+    pmd_init(o);
+    return;
+  }
   update_verlet(o);
   forces_verlet(o, 0);
 }
 
 /* Thermostat_None::propagate (Thermostat_None.cpp:21-38). */
+static void pmd_propagate(smpc_orc* o, int calc_epot);
+
 void orc_propagate(smpc_orc* o, int calc_epot) {
+  if (o->periodic) {
+    pmd_propagate(o, calc_epot);
+    return;
+  }
   const double dt = o->p.md_dt;
   const double dth = dt * 0.50;
   for (int i = 0; i < o->n_m; ++i) {
@@ -609,6 +629,7 @@ static inline void wrap_particle(const smpc_orc* o, double* x, double* v) {
 
 /* MPC::check_bounds (MPC.cpp:160-190). */
 static void check_bounds(smpc_orc* o) {
+  if (o->periodic) return; /* no recentring in a periodic box */
   int out = 0;
   for (int i = 0; i < o->n_m && !out; ++i)
     for (int d = 0; d < 3; ++d)
@@ -904,4 +925,139 @@ void orc_cell_counts(const smpc_orc* o, unsigned* total, unsigned* fluid) {
     if (total) total[c] = o->c_tot[c];
     if (fluid) fluid[c] = o->c_fl[c];
   }
+}
+
+/* ------------------------------------------------------------ periodic MD
+ * Many molecules in one periodic Lees-Edwards box. The reference integrates
+ * one star without periodic images; this mode restates the GPU's periodic
+ * form with the reference's own pieces: Thermostat_None::propagate
+ * (Thermostat_None.cpp:21-38), MPC::LEBC for keeping monomers in the primary
+ * box (MPC.cpp:421-429), MPC::relative_position for every pair and bond
+ * distance (MPC.cpp:456-465) and the potentials of Potentials.h. Pairs are
+ * summed over all other monomers in index order (no Verlet list: only pairs
+ * inside the potentials' ranges contribute), then each monomer's undirected
+ * bonds in bond order, the order the GPU keeps. */
+
+void orc_set_periodic_md(smpc_orc* o, double h) {
+  o->periodic = 1;
+  o->pmd_h = h;
+}
+
+/* delrx one MD step ahead (MPC.cpp:117-118) */
+static double pmd_next_delrx(const smpc_orc* o) {
+  double d = o->delrx;
+  d += o->p.shear * o->p.L[1] * (o->pmd_h * o->p.delrx_dt_scale);
+  d -= o->p.L[0] * round(d / o->p.L[0]);
+  return d;
+}
+
+static inline void pmd_wrap(const smpc_orc* o, double dl, double* x, double* v) {
+  const double Lx = o->p.L[0], Ly = o->p.L[1], Lz = o->p.L[2];
+  double cy = round(x[1] / Ly);
+  x[0] -= Lx * round(x[0] / Lx);
+  x[0] -= cy * dl;
+  x[0] -= Lx * round(x[0] / Lx);
+  x[1] -= Ly * cy;
+  x[2] -= Lz * round(x[2] / Lz);
+  v[0] -= cy * o->p.shear * Ly;
+}
+
+static inline void pmd_min_image(const smpc_orc* o, double dl, double* d) {
+  const double Lx = o->p.L[0], Ly = o->p.L[1], Lz = o->p.L[2];
+  double cy = round(d[1] / Ly);
+  d[0] -= Lx * round(d[0] / Lx);
+  d[0] -= cy * dl;
+  d[0] -= Lx * round(d[0] / Lx);
+  d[1] -= Ly * cy;
+  d[2] -= Lz * round(d[2] / Lz);
+}
+
+static void pmd_adjacency(smpc_orc* o) {
+  const int n = o->n_m;
+  free(o->adj_start); free(o->adj_idx); free(o->adj_anchor);
+  o->adj_start = (int*)calloc((size_t)n + 2, sizeof(int));
+  o->adj_idx = (int*)malloc(sizeof(int) * (size_t)(2 * o->n_bond + 1));
+  o->adj_anchor = (unsigned char*)malloc((size_t)(2 * o->n_bond + 1));
+  int* fill = (int*)calloc((size_t)n + 1, sizeof(int));
+  for (int b = 0; b < o->n_bond; ++b) {
+    o->adj_start[o->bsrc[b] + 1]++;
+    o->adj_start[o->bdst[b] + 1]++;
+  }
+  for (int i = 0; i < n; ++i) o->adj_start[i + 1] += o->adj_start[i];
+  for (int b = 0; b < o->n_bond; ++b) {
+    const int s = o->bsrc[b], d = o->bdst[b];
+    int k = o->adj_start[s] + fill[s]++;
+    o->adj_idx[k] = d;
+    o->adj_anchor[k] = o->anchor[s];
+    k = o->adj_start[d] + fill[d]++;
+    o->adj_idx[k] = s;
+    o->adj_anchor[k] = o->anchor[s];
+  }
+  free(fill);
+}
+
+static void pmd_forces(smpc_orc* o, double dl, int calc_epot) {
+  const int n = o->n_m, pot = o->p.potential;
+  const double lambda = o->p.lambda;
+  for (int m = 0; m < o->n_mol; ++m) o->epot_mol[m] = 0.0;
+  int mol = 0;
+  for (int i = 0; i < n; ++i) {
+    while (mol + 1 < o->n_mol && i >= o->mol_start[mol + 1]) ++mol;
+    const double* xi = o->mx + 3 * i;
+    double F0 = 0.0, F1 = 0.0, F2 = 0.0, ep = 0.0;
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      double d[3] = {o->mx[3 * j] - xi[0], o->mx[3 * j + 1] - xi[1], o->mx[3 * j + 2] - xi[2]};
+      pmd_min_image(o, dl, d);
+      const double r2 = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+      const int bb = (o->amphi[i] == 1 && o->amphi[j] == 1);
+      const double fa = pair_force(pot, bb, r2, lambda);
+      F0 -= d[0] * fa;
+      F1 -= d[1] * fa;
+      F2 -= d[2] * fa;
+      if (calc_epot) ep += 0.5 * pair_pot(pot, bb, r2, lambda);
+    }
+    for (int k = o->adj_start[i]; k < o->adj_start[i + 1]; ++k) {
+      const int j = o->adj_idx[k];
+      const int anch = o->adj_anchor[k];
+      double d[3] = {o->mx[3 * j] - xi[0], o->mx[3 * j + 1] - xi[1], o->mx[3 * j + 2] - xi[2]};
+      pmd_min_image(o, dl, d);
+      double r2 = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+      if (pot != ORC_POT_REF4824) {
+        const double cap = (anch ? 20.25 : 2.25) * 0.98;
+        if (r2 > cap) r2 = cap;
+      }
+      const double fa = anch ? fene_anchor_force(r2) : fene_force(r2);
+      F0 -= d[0] * fa;
+      F1 -= d[1] * fa;
+      F2 -= d[2] * fa;
+      if (calc_epot) ep += 0.5 * (anch ? fene_anchor_pot(r2) : fene_pot(r2));
+    }
+    o->mf[3 * i] = F0;
+    o->mf[3 * i + 1] = F1;
+    o->mf[3 * i + 2] = F2;
+    if (o->n_mol > 0) o->epot_mol[mol] += ep;
+  }
+}
+
+static void pmd_init(smpc_orc* o) {
+  pmd_adjacency(o);
+  for (int i = 0; i < o->n_m; ++i) pmd_wrap(o, o->delrx, o->mx + 3 * i, o->mv + 3 * i);
+  pmd_forces(o, o->delrx, 0);
+}
+
+static void pmd_propagate(smpc_orc* o, int calc_epot) {
+  const double dt = o->p.md_dt;
+  const double dth = dt * 0.50;
+  const double dl = pmd_next_delrx(o);
+  for (int i = 0; i < o->n_m; ++i) {
+    for (int d = 0; d < 3; ++d) {
+      o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
+      o->mx[3 * i + d] += o->mv[3 * i + d] * dt;
+    }
+    pmd_wrap(o, dl, o->mx + 3 * i, o->mv + 3 * i);
+  }
+  pmd_forces(o, dl, calc_epot);
+  for (int i = 0; i < o->n_m; ++i)
+    for (int d = 0; d < 3; ++d) o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
 }

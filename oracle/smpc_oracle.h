@@ -79,6 +79,11 @@ void orc_get_monomers(const smpc_orc* o, double* pos, double* vel, double* force
 void orc_set_bonds(smpc_orc* o, int n_bond, const int* src, const int* dst);
 /* Thermostat_None constructor: Verlet lists + forces (Thermostat_None.cpp:5-12). */
 void orc_init_md(smpc_orc* o);
+/* Periodic MD of many molecules (call before orc_init_md; needs mono_wrap = 1):
+ * every pair and bond distance is the Lees-Edwards minimum image, monomers are
+ * wrapped into the primary box with the v_x jump, no recentring; MD step t uses
+ * the delrx the next MPC::step(t, h) call gives. */
+void orc_set_periodic_md(smpc_orc* o, double h);
 
 double orc_delrx(const smpc_orc* o);
 void orc_set_delrx(smpc_orc* o, double d);

@@ -20,6 +20,7 @@ RNG_INJECT, RNG_PHILOX = 0, 1
 POT_REF4824, POT_LJ126 = 0, 1
 MONOBIN_REFERENCE, MONOBIN_WRAPPED = 0, 1
 DELRX_REFERENCE, DELRX_PHYSICAL = 0, 1
+REPLICA_PERIODIC_MD = 1  # smpc_replica_desc.flags
 
 ERR_BITS = {1: "solvent cell out of range", 2: "monomer cell out of range",
             4: "Verlet list overflow", 8: "non-finite velocity", 32: "gamma iteration limit",
@@ -60,7 +61,7 @@ class ReplicaDesc(C.Structure):
                 ("mol0_size", C.c_int), ("kT", C.c_double), ("shear", C.c_double),
                 ("h", C.c_double), ("md_dt", C.c_double), ("lambda_", C.c_double),
                 ("r_cut", C.c_double), ("r_verlet", C.c_double), ("solvent_mass", C.c_double),
-                ("seed", C.c_uint64), ("potential", C.c_int), ("pad", C.c_int)]
+                ("seed", C.c_uint64), ("potential", C.c_int), ("flags", C.c_int)]
 
 
 class Options(C.Structure):
@@ -174,6 +175,7 @@ class Context:
             d.solvent_mass = float(r.get("solvent_mass", 1.0))
             d.seed = int(r.get("seed", 1))
             d.potential = int(r.get("potential", POT_REF4824))
+            d.flags = int(r.get("flags", 0))
             self.replicas.append(dict(r))
         opt = Options(precision, rng, mono_bin, delrx_mode, step_update, max_neighbors,
                       int(precision == FP64 if strict_cells is None else strict_cells), device)

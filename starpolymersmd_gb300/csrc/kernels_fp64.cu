@@ -14,4 +14,5 @@ namespace smpc {
 int fluid_slots_per_tile() { return 4096; }
 int temperature_cells_per_tile() { return 512; }
 int md_max_monomers() { return SMPC_MD_NT * SMPC_MD_MPT; }
+int pmd_block_count(int n_beads) { return (n_beads + PMD_NT - 1) / PMD_NT; }
 }  // namespace smpc

@@ -6,6 +6,7 @@
 #include "mpc_fast.cuh"
 #include "mpc_kernels.cuh"
 #include "observables.cuh"
+#include "pmd_kernels.cuh"
 
 namespace smpc {
 
@@ -146,6 +147,31 @@ void launch_mol_observables<Real>(const int2* rep_mols, const int2* mols, int n_
                                   cudaStream_t st) {
   if (n_rep == 0) return;
   k_mol_observables<Real, 256><<<n_rep, 256, 0, st>>>(rep_mols, mols, mpos, mvel, out);
+}
+
+template <>
+void launch_unwrap_molecules<Real>(const RepInfo* reps, const RepDyn* dyn, const int2* rep_mols,
+                                   const int2* mols, int n_rep, const int* bond_start,
+                                   const int2* bonds, const Real* mpos, const Real* mvel,
+                                   Real* upos, Real* uvel, cudaStream_t st) {
+  if (n_rep == 0) return;
+  k_unwrap_molecules<Real><<<n_rep, 128, 0, st>>>(reps, dyn, rep_mols, mols, bond_start, bonds,
+                                                  mpos, mvel, upos, uvel);
+}
+
+template <>
+void launch_pmd_substep<Real>(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, Real* mpos,
+                              Real* mvel, Real* mfrc, Real* mdisp, int adv_k, double adv_scale,
+                              int drift, int calc_epot, cudaStream_t st) {
+  if (a.n == 0) return;
+  const int nb = a.n_blocks;
+  k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, adv_k,
+                                           adv_scale, drift);
+  k_pmd_bin<Real><<<nb, PMD_NT, 0, st>>>(a, reps, mpos);
+  k_pmd_nlist<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mdisp, adv_k, adv_scale);
+  k_pmd_forces<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, adv_k, adv_scale,
+                                            drift, calc_epot);
+  k_pmd_finish<Real><<<1, 32, 0, st>>>(a, reps, dyn, adv_k, adv_scale, calc_epot);
 }
 
 template <>

@@ -10,6 +10,7 @@
 namespace smpc {
 
 struct MdArgs;
+struct PmdArgs;
 
 // Launch-shape variants of the FP32 fast-path kernels, chosen by the
 // autotuner (smpc_autotune). The FP64 parity kernels have one shape.
@@ -80,6 +81,21 @@ void launch_temperature(const Tile* tiles, int n_tiles, const RepInfo* reps, con
 template <typename R>
 void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, int variant,
                cudaStream_t st);
+
+// One MD substep of one periodic box (pmd_kernels.cuh): substep k of a call
+// passes adv_k = k + 1; drift = 0 builds lists and forces only (set-up).
+template <typename R>
+void launch_pmd_substep(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, R* mpos, R* mvel,
+                        R* mfrc, R* mdisp, int adv_k, double adv_scale, int drift, int calc_epot,
+                        cudaStream_t st);
+int pmd_block_count(int n_beads);
+
+// Molecules of periodic boxes made whole (observables.cuh); other boxes copied.
+template <typename R>
+void launch_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* rep_mols,
+                             const int2* mols, int n_rep, const int* bond_start,
+                             const int2* bonds, const R* mpos, const R* mvel, R* upos, R* uvel,
+                             cudaStream_t st);
 
 template <typename R>
 void launch_mol_observables(const int2* rep_mols, const int2* mols, int n_rep, const R* mpos,

@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
   const int r = a.order ? a.order[blockIdx.x] : static_cast<int>(blockIdx.x);
   const RepInfo ri = a.reps[r];
   const int n = ri.n_mono;
-  if (n == 0) return;
+  if (n == 0 || (ri.flags & REP_PERIODIC_MD)) return;  // periodic boxes: pmd_kernels.cuh
   int lk = 0;  // log2 of the lanes per bead
   if (KMAX > 1)
     while ((2 << lk) <= KMAX && (n << (lk + 1)) <= NT) ++lk;

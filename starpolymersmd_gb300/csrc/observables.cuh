@@ -141,6 +141,65 @@ __global__ void __launch_bounds__(NT) k_mol_observables(const int2* rep_mols, co
   }
 }
 
+// Molecules of periodic boxes made whole for the observables: bead i is placed
+// at the Lees-Edwards minimum image (MPC.cpp:456-465, current delrx) next to
+// its lowest-indexed bonded partner in the molecule, which comes earlier and is
+// already placed, or next to the molecule's first bead when it has none (stars
+// and chains numbered outward from the core always have one). Its v_x gets the
+// shear velocity of the image it moved to (MPC.cpp:428). Other boxes are
+// copied as they are. One block per box; one thread per molecule of a periodic
+// box walks its beads in order.
+template <typename R>
+__global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* rep_mols,
+                                   const int2* mols, const int* bond_start, const int2* bonds,
+                                   const R* mpos, const R* mvel, R* upos, R* uvel) {
+  const int r = blockIdx.x;
+  const RepInfo& ri = reps[r];
+  if (!(ri.flags & REP_PERIODIC_MD)) {
+    for (int i = ri.mono_base + threadIdx.x; i < ri.mono_base + ri.n_mono; i += blockDim.x) {
+      st4(upos, i, ld4_rw(mpos, i));
+      st4(uvel, i, ld4_rw(mvel, i));
+    }
+    return;
+  }
+  const double L[3] = {static_cast<double>(ri.L[0]), static_cast<double>(ri.L[1]),
+                       static_cast<double>(ri.L[2])};
+  const double delrx = dyn[r].delrx;
+  const int2 rm = rep_mols[r];
+  for (int m = rm.x + threadIdx.x; m < rm.x + rm.y; m += blockDim.x) {
+    const int2 mb = mols[m];
+    for (int i = mb.x; i < mb.y; ++i) {
+      int p = -1;
+      for (int e = bond_start[i]; e < bond_start[i + 1]; ++e) {
+        const int j = bonds[e].x;
+        if (j >= mb.x && j < i && (p < 0 || j < p)) p = j;
+      }
+      if (p < 0) p = mb.x;
+      R4<R> x = ld4_rw(mpos, i), v = ld4_rw(mvel, i);
+      if (i != mb.x) {
+        const R4<R> xp = ld4_rw(mpos, p), up = ld4_rw(upos, p);
+        double d0 = static_cast<double>(x.x) - static_cast<double>(xp.x);
+        double d1 = static_cast<double>(x.y) - static_cast<double>(xp.y);
+        double d2 = static_cast<double>(x.z) - static_cast<double>(xp.z);
+        const double cy = round(d1 / L[1]);
+        d0 -= L[0] * round(d0 / L[0]);
+        d0 -= cy * delrx;
+        d0 -= L[0] * round(d0 / L[0]);
+        d1 -= L[1] * cy;
+        d2 -= L[2] * round(d2 / L[2]);
+        const double uy = static_cast<double>(up.y) + d1;
+        const double ny = round((uy - static_cast<double>(x.y)) / L[1]);
+        x.x = static_cast<R>(static_cast<double>(up.x) + d0);
+        x.y = static_cast<R>(uy);
+        x.z = static_cast<R>(static_cast<double>(up.z) + d2);
+        v.x = static_cast<R>(static_cast<double>(v.x) + ny * ri.shear * L[1]);
+      }
+      st4(upos, i, x);
+      st4(uvel, i, v);
+    }
+  }
+}
+
 template <typename R>
 __global__ void k_profile_centre(const int2* rep_mols, const int2* mols, const R* mpos,
                                  const R* mvel, int rep, double* c6) {

@@ -9,6 +9,8 @@ namespace smpc {
 
 __device__ __forceinline__ float r_round(float x) { return roundf(x); }
 __device__ __forceinline__ double r_round(double x) { return ::round(x); }
+__device__ __forceinline__ float r_floor(float x) { return floorf(x); }
+__device__ __forceinline__ double r_floor(double x) { return ::floor(x); }
 __device__ __forceinline__ float r_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double r_sqrt(double x) { return ::sqrt(x); }
 __device__ __forceinline__ float r_log(float x) { return logf(x); }

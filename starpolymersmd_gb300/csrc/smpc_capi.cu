@@ -15,6 +15,7 @@
 #include "launch.h"
 #include "md_kernels.cuh"
 #include "observables.cuh"
+#include "pmd_kernels.cuh"
 #include "smpc_device.cuh"
 
 using smpc::ErrorState;
@@ -68,6 +69,13 @@ struct smpc_ctx {
   int* d_nlist = nullptr;
   int* d_ncount = nullptr;
   int* d_md_order = nullptr;  // replicas by decreasing monomer count (MD CTA order)
+  bool any_local_md = false;  // a non-periodic replica has monomers
+  // periodic boxes (SMPC_REPLICA_PERIODIC_MD): launch arguments with their grid
+  // buffers, and molecules made whole for the observables
+  std::vector<smpc::PmdArgs> pmd;
+  std::vector<void*> pmd_mem;
+  void* d_upos = nullptr;
+  void* d_uvel = nullptr;
   std::vector<std::vector<int>> bsrc, bdst;
   std::vector<std::vector<int>> anchor;
 
@@ -207,6 +215,22 @@ smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
 template <typename R>
 int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   if (ctx->total_mono == 0) return SMPC_OK;
+  const double adv = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / ctx->opt.step_update : 1.0;
+  for (const smpc::PmdArgs& p : ctx->pmd) {
+    R* mpos = static_cast<R*>(ctx->d_mpos);
+    R* mvel = static_cast<R*>(ctx->d_mvel);
+    R* mfrc = static_cast<R*>(ctx->d_mfrc);
+    R* mdisp = static_cast<R*>(ctx->d_mver);
+    if (n == 0) {
+      smpc::launch_pmd_substep<R>(p, ctx->d_reps, ctx->d_dyn, mpos, mvel, mfrc, mdisp, 0, adv, 0,
+                                  calc_epot, ctx->st);
+    } else {
+      for (int k = 0; k < n; ++k)
+        smpc::launch_pmd_substep<R>(p, ctx->d_reps, ctx->d_dyn, mpos, mvel, mfrc, mdisp, k + 1,
+                                    adv, 1, calc_epot && k == n - 1, ctx->st);
+    }
+  }
+  if (!ctx->any_local_md) return SMPC_OK;
   smpc::MdArgs a;
   a.reps = ctx->d_reps;
   a.dyn = ctx->d_dyn;
@@ -584,6 +608,7 @@ int upload_bonds(smpc_ctx* ctx) {
   if (!flat.empty())
     CU(cudaMemcpy(ctx->d_bonds, flat.data(), flat.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_bond_start, start.data(), (M + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  for (smpc::PmdArgs& p : ctx->pmd) p.bonds = ctx->d_bonds;
   return SMPC_OK;
 }
 
@@ -592,6 +617,12 @@ void free_all(smpc_ctx* ctx) {
     if (ctx->graph[k]) cudaGraphExecDestroy(ctx->graph[k]);
     cudaFree(ctx->d_rec[k]);
   }
+  for (void* q : ctx->pmd_mem)
+    if (q) cudaFree(q);
+  ctx->pmd_mem.clear();
+  ctx->pmd.clear();
+  if (ctx->d_upos) cudaFree(ctx->d_upos);
+  if (ctx->d_uvel) cudaFree(ctx->d_uvel);
   void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
@@ -710,6 +741,60 @@ int upload_molecules(smpc_ctx* ctx) {
   return SMPC_OK;
 }
 
+// Grid buffers and launch arguments of every periodic box: cells of side
+// >= r_verlet (Box.cpp:20-25 sizes its grid the same way), PMD_CELL_CAP beads
+// each.
+int create_periodic_md(smpc_ctx* ctx) {
+  const size_t M = static_cast<size_t>(ctx->total_mono);
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    const RepInfo& ri = ctx->reps[r];
+    if (!(ri.flags & smpc::REP_PERIODIC_MD) || ri.n_mono == 0) continue;
+    smpc::PmdArgs a{};
+    a.rep = r;
+    a.base = ri.mono_base;
+    a.n = ri.n_mono;
+    a.ncell = 1;
+    for (int k = 0; k < 3; ++k) {
+      a.nc[k] = static_cast<int>(std::floor(ri.L[k] / ri.r_verlet));
+      a.ncell *= a.nc[k];
+    }
+    a.n_blocks = smpc::pmd_block_count(a.n);
+    const size_t cells = static_cast<size_t>(a.ncell);
+    void *cnt = nullptr, *items = nullptr, *flag = nullptr, *db = nullptr, *ep = nullptr;
+    CU(cudaMalloc(&cnt, cells * sizeof(uint32_t)));
+    ctx->pmd_mem.push_back(cnt);
+    CU(cudaMalloc(&items, cells * smpc::PMD_CELL_CAP * sizeof(int)));
+    ctx->pmd_mem.push_back(items);
+    CU(cudaMalloc(&flag, sizeof(int)));
+    ctx->pmd_mem.push_back(flag);
+    CU(cudaMalloc(&db, sizeof(double)));
+    ctx->pmd_mem.push_back(db);
+    CU(cudaMalloc(&ep, static_cast<size_t>(a.n_blocks) * sizeof(double)));
+    ctx->pmd_mem.push_back(ep);
+    CU(cudaMemset(cnt, 0, cells * sizeof(uint32_t)));
+    CU(cudaMemset(flag, 0, sizeof(int)));
+    CU(cudaMemset(db, 0, sizeof(double)));
+    a.cnt = static_cast<uint32_t*>(cnt);
+    a.items = static_cast<int*>(items);
+    a.flag = static_cast<int*>(flag);
+    a.delrx_build = static_cast<double*>(db);
+    a.epot_part = static_cast<double*>(ep);
+    a.nlist = ctx->d_nlist;
+    a.ncount = ctx->d_ncount;
+    a.n_mono_total = static_cast<int>(M);
+    a.max_nb = ctx->max_nb;
+    a.bond_start = ctx->d_bond_start;
+    a.bonds = ctx->d_bonds;
+    a.err = ctx->d_err;
+    ctx->pmd.push_back(a);
+  }
+  if (!ctx->pmd.empty()) {
+    CU(cudaMalloc(&ctx->d_upos, 4 * M * ctx->real_size));
+    CU(cudaMalloc(&ctx->d_uvel, 4 * M * ctx->real_size));
+  }
+  return SMPC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -742,7 +827,17 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
     const smpc_replica_desc& d = descs[r];
     if (d.L[0] <= 0 || d.L[1] <= 0 || d.L[2] <= 0 || d.n_fluid < 0 || d.n_mono < 0)
       return bail(SMPC_E_ARG, "replica geometry");
-    if (d.n_mono > smpc::md_max_monomers()) return bail(SMPC_E_UNSUPPORTED, "too many monomers");
+    if (d.flags & ~SMPC_REPLICA_PERIODIC_MD) return bail(SMPC_E_ARG, "replica flags");
+    const bool periodic = (d.flags & SMPC_REPLICA_PERIODIC_MD) != 0;
+    if (!periodic && d.n_mono > smpc::md_max_monomers())
+      return bail(SMPC_E_UNSUPPORTED, "too many monomers");
+    if (periodic) {
+      if (opt->mono_bin != SMPC_MONOBIN_WRAPPED)
+        return bail(SMPC_E_ARG, "periodic MD needs wrapped monomer binning");
+      for (int k = 0; k < 3; ++k)
+        if (!(d.r_verlet > 0) || d.L[k] < 3.0 * d.r_verlet)
+          return bail(SMPC_E_UNSUPPORTED, "periodic MD needs every box edge >= 3 r_verlet");
+    }
     RepInfo ri{};
     for (int k = 0; k < 3; ++k) ri.L[k] = d.L[k];
     ri.n_cell = d.L[0] * d.L[1] * d.L[2];
@@ -752,7 +847,9 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
     ri.n_fluid = d.n_fluid;
     ri.mono_base = static_cast<int>(mono);
     ri.n_mono = d.n_mono;
-    ri.mol0_size = d.mol0_size;
+    ri.mol0_size = periodic ? 0 : d.mol0_size;  // no recentring in a periodic box
+    ri.flags = periodic ? smpc::REP_PERIODIC_MD : 0;
+    if (!periodic && d.n_mono > 0) ctx->any_local_md = true;
     ri.shear = d.shear;
     ri.kT = d.kT;
     ri.h = d.h;
@@ -819,7 +916,7 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
   // reference, MPC.cpp:175-176), the rest one more molecule
   ctx->mol_start.resize(n_rep);
   for (int r = 0; r < n_rep; ++r) {
-    const int nm = ctx->reps[r].n_mono, m0 = ctx->reps[r].mol0_size;
+    const int nm = ctx->reps[r].n_mono, m0 = descs[r].mol0_size;
     std::vector<int>& ms = ctx->mol_start[r];
     ms.push_back(0);
     if (nm > 0) {
@@ -830,6 +927,7 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
   if (upload_molecules(ctx) != SMPC_OK || dalloc(&ctx->d_obs, static_cast<size_t>(n_rep) * smpc::OBS_PER_REP) != cudaSuccess ||
       dalloc(&ctx->d_c6, 6) != cudaSuccess)
     return bail(SMPC_E_CUDA, "molecule tables");
+  if (int rc2 = create_periodic_md(ctx)) return bail(rc2, ctx->err);
   // empty solvent state until smpc_set_fluid: every slot a hole
   for (int r = 0; r < n_rep; ++r) {
     std::vector<double> z(3 * static_cast<size_t>(ctx->reps[r].n_fluid) + 3, 0.0);
@@ -903,6 +1001,13 @@ int smpc_set_bonds(smpc_ctx* ctx, int rep, int n_bond, const int* src, const int
 int smpc_init_md(smpc_ctx* ctx) {
   if (!ctx) return SMPC_E_ARG;
   cudaSetDevice(ctx->device);
+  // captured cycles hold the bond table's address, which is about to change
+  CU(cudaStreamSynchronize(ctx->st));
+  for (int k = 0; k < 2; ++k)
+    if (ctx->graph[k]) {
+      cudaGraphExecDestroy(ctx->graph[k]);
+      ctx->graph[k] = nullptr;
+    }
   if (int rc = upload_bonds(ctx)) return rc;
   int rc = ctx->opt.precision == SMPC_FP64 ? launch_md_steps<double>(ctx, 0, 0, 1)
                                            : launch_md_steps<float>(ctx, 0, 0, 1);
@@ -1415,17 +1520,56 @@ int smpc_set_molecules(smpc_ctx* ctx, int rep, int n_mol, const int* mol_start) 
   return upload_molecules(ctx);
 }
 
+}  // extern "C"
+
+namespace {
+// Monomer state the observables read: the device arrays, or for contexts with
+// periodic boxes their copy with every molecule made whole.
+template <typename R>
+void observed_monomers(smpc_ctx* ctx, const R** pos, const R** vel) {
+  *pos = static_cast<const R*>(ctx->d_mpos);
+  *vel = static_cast<const R*>(ctx->d_mvel);
+  if (ctx->pmd.empty()) return;
+  smpc::launch_unwrap_molecules<R>(ctx->d_reps, ctx->d_dyn, ctx->d_rep_mols, ctx->d_mols,
+                                   ctx->n_rep, ctx->d_bond_start, ctx->d_bonds, *pos, *vel,
+                                   static_cast<R*>(ctx->d_upos), static_cast<R*>(ctx->d_uvel),
+                                   ctx->st);
+  *pos = static_cast<const R*>(ctx->d_upos);
+  *vel = static_cast<const R*>(ctx->d_uvel);
+}
+
+template <typename R>
+void mol_observables_t(smpc_ctx* ctx) {
+  const R *p, *v;
+  observed_monomers<R>(ctx, &p, &v);
+  smpc::launch_mol_observables<R>(ctx->d_rep_mols, ctx->d_mols, ctx->n_rep, p, v, ctx->d_obs,
+                                  ctx->st);
+}
+
+template <typename R>
+void velocity_profile_t(smpc_ctx* ctx, int rep, double width, long long kx0, int n_x,
+                        long long ky0, int n_y) {
+  const R *p, *v;
+  observed_monomers<R>(ctx, &p, &v);
+  smpc::launch_velocity_profile<R>(ctx->d_reps, ctx->d_rep_mols, ctx->d_mols, rep,
+                                   ctx->reps[rep].slot_cap,
+                                   static_cast<const R*>(ctx->d_rec[ctx->cur]), p, v,
+                                   ctx->dyn[rep].delrx, width, kx0, n_x, ky0, n_y, ctx->d_c6,
+                                   ctx->d_prof, ctx->st);
+}
+}  // namespace
+
+extern "C" {
+
 int smpc_molecule_observables_all(smpc_ctx* ctx, double* out) {
   if (!ctx || !out) return SMPC_E_ARG;
   cudaSetDevice(ctx->device);
+  if (ctx->total_mono > 0 && !ctx->md_ready && !ctx->pmd.empty())
+    return fail(ctx, SMPC_E_STATE, "smpc_init_md not called (bonds make periodic molecules whole)");
   if (ctx->opt.precision == SMPC_FP64)
-    smpc::launch_mol_observables<double>(ctx->d_rep_mols, ctx->d_mols, ctx->n_rep,
-                                         static_cast<const double*>(ctx->d_mpos),
-                                         static_cast<const double*>(ctx->d_mvel), ctx->d_obs, ctx->st);
+    mol_observables_t<double>(ctx);
   else
-    smpc::launch_mol_observables<float>(ctx->d_rep_mols, ctx->d_mols, ctx->n_rep,
-                                        static_cast<const float*>(ctx->d_mpos),
-                                        static_cast<const float*>(ctx->d_mvel), ctx->d_obs, ctx->st);
+    mol_observables_t<float>(ctx);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(out, ctx->d_obs, static_cast<size_t>(ctx->n_rep) * smpc::OBS_PER_REP * sizeof(double),
                      cudaMemcpyDeviceToHost, ctx->st));
@@ -1456,19 +1600,12 @@ int smpc_velocity_profile(smpc_ctx* ctx, int rep, double width, double* x_out, i
     ctx->prof_cap = nb;
   }
   CU(cudaMemsetAsync(ctx->d_prof, 0, nb * sizeof(double), ctx->st));
-  const double delrx = ctx->dyn[rep].delrx;
+  if (ctx->total_mono > 0 && !ctx->md_ready && !ctx->pmd.empty())
+    return fail(ctx, SMPC_E_STATE, "smpc_init_md not called (bonds make periodic molecules whole)");
   if (ctx->opt.precision == SMPC_FP64)
-    smpc::launch_velocity_profile<double>(
-        ctx->d_reps, ctx->d_rep_mols, ctx->d_mols, rep, ri.slot_cap,
-        static_cast<const double*>(ctx->d_rec[ctx->cur]), static_cast<const double*>(ctx->d_mpos),
-        static_cast<const double*>(ctx->d_mvel), delrx, width, kx0, n_x, ky0, n_y, ctx->d_c6,
-        ctx->d_prof, ctx->st);
+    velocity_profile_t<double>(ctx, rep, width, kx0, n_x, ky0, n_y);
   else
-    smpc::launch_velocity_profile<float>(
-        ctx->d_reps, ctx->d_rep_mols, ctx->d_mols, rep, ri.slot_cap,
-        static_cast<const float*>(ctx->d_rec[ctx->cur]), static_cast<const float*>(ctx->d_mpos),
-        static_cast<const float*>(ctx->d_mvel), delrx, width, kx0, n_x, ky0, n_y, ctx->d_c6,
-        ctx->d_prof, ctx->st);
+    velocity_profile_t<float>(ctx, rep, width, kx0, n_x, ky0, n_y);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(x_out, ctx->d_prof, 3 * static_cast<size_t>(n_x) * sizeof(double),
                      cudaMemcpyDeviceToHost, ctx->st));

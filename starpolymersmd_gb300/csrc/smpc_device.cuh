@@ -37,6 +37,7 @@ enum : uint32_t {
 enum : int { POT_REF4824 = 0, POT_LJ126 = 1 };
 enum : int { MONOBIN_REFERENCE = 0, MONOBIN_WRAPPED = 1 };
 enum : int { RNG_INJECT = 0, RNG_PHILOX = 1 };
+enum : int { REP_PERIODIC_MD = 1 };  // smpc.h SMPC_REPLICA_PERIODIC_MD
 
 // Static per-replica description (uploaded once).
 struct RepInfo {
@@ -49,7 +50,7 @@ struct RepInfo {
   int mono_base;
   int n_mono;
   int mol0_size;       // monomers of molecule 0 (recentring reference)
-  int pad0;
+  int flags;           // REP_* bits
   double shear;
   double kT;
   double h;            // collision step (streaming time)

@@ -196,3 +196,160 @@ def batched_replica_table(n: int = 256, seed: int = 1) -> List[ReplicaSpec]:
 
 def replica_table_json(specs: Sequence[ReplicaSpec]) -> str:
     return json.dumps([dataclasses.asdict(s) for s in specs], indent=0)
+
+
+@dataclasses.dataclass
+class StarSolution:
+    """Several stars in one periodic box, concatenated star by star (each in
+    the reference's star layout); positions are unwrapped (every star
+    contiguous) and may reach outside the primary box."""
+    stars: List[Star]
+    L: tuple
+
+    @property
+    def n(self) -> int:
+        return sum(s.n for s in self.stars)
+
+    @property
+    def mol_start(self) -> np.ndarray:
+        return np.concatenate([[0], np.cumsum([s.n for s in self.stars])]).astype(np.int32)
+
+    def _cat(self, name):
+        return np.concatenate([getattr(s, name) for s in self.stars])
+
+    @property
+    def pos(self) -> np.ndarray:
+        return self._cat("pos")
+
+    @property
+    def vel(self) -> np.ndarray:
+        return self._cat("vel")
+
+    @property
+    def amphi(self) -> np.ndarray:
+        return self._cat("amphi")
+
+    @property
+    def anchor(self) -> np.ndarray:
+        return self._cat("anchor")
+
+    @property
+    def mass(self) -> np.ndarray:
+        return np.concatenate([np.full(s.n, s.mass) for s in self.stars])
+
+    @property
+    def bond_src(self) -> np.ndarray:
+        off = self.mol_start
+        return np.concatenate([s.bond_src + off[k] for k, s in enumerate(self.stars)]).astype(np.int32)
+
+    @property
+    def bond_dst(self) -> np.ndarray:
+        off = self.mol_start
+        return np.concatenate([s.bond_dst + off[k] for k, s in enumerate(self.stars)]).astype(np.int32)
+
+
+class _PeriodicOccupancy:
+    """Placed beads of a periodic box on a hash grid of unit cells, for
+    self-avoidance checks under the minimum image (no shear offset: set-up
+    happens at delrx = 0)."""
+
+    def __init__(self, L, cell: float = 1.0):
+        self.L = np.asarray(L, dtype=np.float64)
+        self.n = np.maximum(1, np.floor(self.L / cell)).astype(int)
+        self.side = self.L / self.n
+        self.cells = {}
+
+    def _key(self, x):
+        return tuple((np.floor((x + 0.5 * self.L) / self.side).astype(int) % self.n).tolist())
+
+    def add(self, idx: int, x) -> None:
+        self.cells.setdefault(self._key(x), []).append((idx, np.array(x, dtype=np.float64)))
+
+    def free(self, x, r_min: float, skip: int = -1) -> bool:
+        k = np.array(self._key(x))
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    c = tuple(((k + (dx, dy, dz)) % self.n).tolist())
+                    for idx, p in self.cells.get(c, ()):
+                        if idx == skip:
+                            continue
+                        d = p - x
+                        d -= self.L * np.round(d / self.L)
+                        if float(d @ d) <= r_min * r_min:
+                            return False
+        return True
+
+
+def star_solution(n_stars: int, arms: int, n_arm: int, solvophobic_fraction: float,
+                  mass: float, kT: float, L: Sequence[int], rng: np.random.Generator,
+                  bond: float = 1.0, anchor_bond: float = 2.0, r_min: float = 1.0,
+                  outward_bias: float = 0.5, jitter: float = 0.25,
+                  max_tries: int = 400) -> StarSolution:
+    """``n_stars`` self-avoiding stars (no bead within ``r_min`` of another,
+    across stars and periodic images) with their cores on a randomised cubic
+    lattice: the first ``n_stars`` sites of a ceil(n^(1/3))-per-axis lattice,
+    in random order, each core moved by up to ``jitter`` of the spacing along
+    every axis. Arms grow round-robin as in ``saw_star``."""
+    Lv = np.asarray(L, dtype=np.float64)
+    m = int(math.ceil(n_stars ** (1.0 / 3.0) - 1e-9))
+    sites = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)])
+    sites = sites[rng.permutation(len(sites))[:n_stars]]
+    spacing = Lv / m
+    centres = -0.5 * Lv + (sites + 0.5) * spacing
+    centres += rng.uniform(-jitter, jitter, size=centres.shape) * spacing
+    occ = _PeriodicOccupancy(Lv)
+    B = int(round(solvophobic_fraction * n_arm))
+    A = n_arm - B
+    amphi, anch, src, dst = star_topology(arms, A, B)
+    golden = math.pi * (3.0 - math.sqrt(5.0))
+    stars = []
+    base = 0
+    for c in centres:
+        n = 1 + arms * n_arm
+        for _attempt in range(50):
+            q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+            roots = []
+            for a in range(arms):
+                z = 1.0 - 2.0 * (a + 0.5) / arms
+                r = math.sqrt(max(0.0, 1.0 - z * z))
+                roots.append(c + (q @ np.array([r * math.cos(golden * a),
+                                                r * math.sin(golden * a), z])) * anchor_bond)
+            if occ.free(c, r_min) and all(occ.free(p, r_min) for p in roots):
+                break
+        else:
+            raise RuntimeError("no free place for a star core")
+        occ.add(base, c)
+        arm_beads = [[p] for p in roots]
+        last = []
+        for a, p in enumerate(roots):
+            occ.add(base + 1 + a * n_arm, p)
+            last.append(base + 1 + a * n_arm)
+        for k in range(1, n_arm):
+            for a in range(arms):
+                prev = arm_beads[a][-1]
+                radial = prev - c
+                radial /= max(np.linalg.norm(radial), 1e-12)
+                for _t in range(max_tries):
+                    s = rng.normal(size=3)
+                    s /= np.linalg.norm(s)
+                    s = s + outward_bias * radial
+                    s /= np.linalg.norm(s)
+                    x = prev + s * bond
+                    if occ.free(x, r_min, skip=last[a]):
+                        break
+                else:
+                    raise RuntimeError("self-avoiding walk got stuck")
+                idx = base + 1 + a * n_arm + k
+                occ.add(idx, x)
+                last[a] = idx
+                arm_beads[a].append(x)
+        pos = np.zeros((n, 3))
+        pos[0] = c
+        for a in range(arms):
+            pos[1 + a * n_arm: 1 + (a + 1) * n_arm] = np.asarray(arm_beads[a])
+        vel = thermal_velocities(n, mass, kT, rng)
+        stars.append(Star(arms, A, B, mass, pos, vel, amphi.copy(), anch.copy(), src.copy(),
+                          dst.copy()))
+        base += n
+    return StarSolution(stars, tuple(int(x) for x in L))

@@ -25,15 +25,20 @@ def wrapped_diff(a, b, L):
     return d - Lv * np.round(d / Lv)
 
 
-def fixture_context(fx, precision=capi.FP64):
+def fixture_context(fx, precision=capi.FP64, periodic=False):
+    """Context replaying a reference fixture; with ``periodic`` the box runs
+    the periodic many-molecule MD (wrapped monomer binning), which for one
+    star away from the faces is the reference's MD."""
     n_f = len(fx["fluid_pos0"])
     star = gr.has_star(fx)
     n_m = len(fx["mono_pos0"]) if star else 0
     rep = dict(L=fx["L"], n_fluid=n_f, n_mono=n_m, mol0_size=n_m, kT=float(fx["kT"]),
                shear=float(fx["shear"]), h=float(fx["h"]), md_dt=float(fx["md_dt"]),
+               flags=capi.REPLICA_PERIODIC_MD if periodic else 0,
                **{"lambda": float(fx["lam"])})
     ctx = capi.Context([rep], precision=precision, rng=capi.RNG_INJECT,
-                       step_update=int(fx["step_update"]))
+                       step_update=int(fx["step_update"]),
+                       mono_bin=capi.MONOBIN_WRAPPED if periodic else capi.MONOBIN_REFERENCE)
     ctx.set_fluid(0, fx["fluid_pos0"], fx["fluid_vel0"])
     if star:
         ctx.set_monomers(0, fx["mono_pos0"], fx["mono_vel0"], fx["mono_force0"], fx["mono_mass"],
