@@ -37,6 +37,7 @@ import numpy as np  # noqa: E402
 METRIC = "MPC particle-updates/s"
 UNIT = "particle-updates/s"
 PHASE_LAUNCHES = 10  # kernels per cycle: md, begin, mono_prep, fluid_bin, 3x scan, perm, collide, end
+PMD_LAUNCHES = 2     # kernels per MD substep of a periodic box (nlist, forces), plus 2 per cycle
 
 
 def parse_args():
@@ -143,7 +144,9 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
     from oracle import oracle as orc
     from starpolymersmd_gb300 import system, workloads as W
 
-    if workload == "batched_256":
+    if workload in W.SOLUTIONS:
+        pick = [W.semidilute_spec() if workload == "semidilute_100" else W.large_box_spec()]
+    elif workload == "batched_256":
         specs = system.batched_replica_table(256)
         pick = specs[:: max(1, len(specs) // n_threads)][:n_threads]
     elif workload == "single_star_50":
@@ -157,17 +160,26 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
 
     def make(spec):
         rng = np.random.default_rng(2000 + spec.seed)
-        st = W.compact_star(spec)
+        st = W.make_solution(spec) if workload in W.SOLUTIONS else W.compact_star(spec)
+        mol_start = st.mol_start if workload in W.SOLUTIONS else [0, st.n]
+        mass = st.mass if workload in W.SOLUTIONS else np.full(st.n, st.mass)
         L = spec.L
         fpos, fvel = system.uniform_fluid((L, L, L), spec.n_c, spec.kT, rng)
         o = orc.OracleSystem((L, L, L), spec.kT, spec.shear, W.N_SUB, len(fpos), st.n,
-                             mol_start=[0, st.n], lambda_=1.0, md_dt=W.MD_DT,
+                             mol_start=mol_start, lambda_=1.0, md_dt=W.MD_DT,
                              r_cut=W.R_CUT_LJ, r_verlet=W.R_CUT_LJ + W.SKIN,
                              potential=orc.POT_LJ126, delrx_dt_scale=1.0 / W.N_SUB, mono_wrap=1)
+        mvel = st.vel
+        if workload in W.SOLUTIONS:  # the steady shear flow, as the GPU workload starts
+            fvel[:, 0] += spec.shear * fpos[:, 1]
+            mvel = st.vel.copy()
+            mvel[:, 0] += spec.shear * st.pos[:, 1]
         o.set_fluid(fpos, fvel)
-        o.set_monomers(st.pos, st.vel, np.zeros_like(st.pos), np.full(st.n, st.mass), st.amphi,
-                       st.anchor)
+        del fpos, fvel
+        o.set_monomers(st.pos, mvel, np.zeros_like(st.pos), mass, st.amphi, st.anchor)
         o.set_bonds(st.bond_src, st.bond_dst)
+        if workload in W.SOLUTIONS:
+            o.set_periodic_md(W.H)
         o.init_md()
         o.set_philox(spec.seed, 0)
         return o, len(fpos) + st.n
@@ -191,7 +203,8 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
 
 def cpu_cycles_for(workload, n_threads):
     # about 10-30 s of CPU work in total
-    return {"batched_256": 20, "single_star_50": 5, "single_star_20": 40}.get(workload, 5)
+    return {"batched_256": 20, "single_star_50": 5, "single_star_20": 40, "semidilute_100": 3,
+            "large_box_200": 1}.get(workload, 5)
 
 
 # --------------------------------------------------------------- our arm
@@ -262,6 +275,8 @@ def run_ours(args, world, rank, local, dist):
              "frac": round(cycle_alg_bytes / (ms / K / 1e3) / 1e9 / peak, 4),
              "alg_bytes_per_cycle": cycle_alg_bytes}
 
+    launches_per_cycle = (PHASE_LAUNCHES - 1 + PMD_LAUNCHES * W.N_SUB + 2
+                          if args.workload in W.SOLUTIONS else PHASE_LAUNCHES)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
            "warmup": Wm, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32",
@@ -274,7 +289,7 @@ def run_ours(args, world, rank, local, dist):
                       "precision": "fp32 state, int64 fixed-point cell sums, fp64 delrx",
                       "l2": "state of %.1f GB per copy, inputs larger than L2" % (units * 32 / 1e9),
                       "parallelism": "replicas only" if world == 1 else f"replicas x{world}"},
-           "replica_steps_per_s": rep_steps, "gpu_launches": PHASE_LAUNCHES * K,
+           "replica_steps_per_s": rep_steps, "gpu_launches": launches_per_cycle * K,
            "autotune": {"chosen": {k: v.get("chosen") for k, v in tuned["report"].items()},
                         "cached": tuned["cached"]},
            "roofline": roofline, "cycle_roofline": whole, "phase_share": phase_share,
@@ -305,7 +320,8 @@ def fp64_plain_ratio(workload, built, batched_rep_steps):
     cyc = 3
     t_sum = 0.0
     for s in sample:
-        b = W.build([s], precision=capi.FP64)
+        b = (W.build_solution(s, precision=capi.FP64) if workload in W.SOLUTIONS
+             else W.build([s], precision=capi.FP64))
         b.ctx.cycles(2)
         t_sum += b.ctx.time_cycles(cyc) / 1e3
         b.ctx.raise_on_device_error()

@@ -166,8 +166,11 @@ int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len);
 int smpc_time_cycles(smpc_ctx* ctx, int n, double* total_ms);
 /* Solvent initial state generated on the device (MPC::initialize,
  * MPC.cpp:34-55): positions uniform in the box; velocities uniform in
- * [-1/2, 1/2) when reference_velocities != 0, else Maxwell-Boltzmann at kT. */
-int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int reference_velocities);
+ * [-1/2, 1/2) with SMPC_INIT_REFERENCE_VELOCITIES, else Maxwell-Boltzmann at
+ * kT; SMPC_INIT_SHEAR_PROFILE adds the steady Lees-Edwards flow shear * y to
+ * v_x (a long sheared run's state, instead of a fluid at rest). */
+enum { SMPC_INIT_REFERENCE_VELOCITIES = 1, SMPC_INIT_SHEAR_PROFILE = 2 };
+int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int flags);
 
 /* Observables. */
 int smpc_temperature(smpc_ctx* ctx, int rep, double* out);   /* MPC.cpp:405-409 */

@@ -74,7 +74,7 @@ def _oracle_lib():
             "orc_mpc_step": [P, C.c_long, C.c_double], "orc_propagate": [P, C.c_int],
             "orc_run": [P, C.c_long, C.c_long, C.c_double, C.c_int],
             "orc_cell_counts": [P, P, P], "orc_philox4x32_10": [P, P, P],
-            "orc_set_periodic_md": [P, C.c_double],
+            "orc_set_periodic_md": [P, C.c_double], "orc_periodic_forces": [P, C.c_int, P],
         }.items():
             getattr(lib, name).argtypes = args
             getattr(lib, name).restype = None
@@ -168,6 +168,11 @@ class OracleSystem:
     def set_periodic_md(self, h):
         """Periodic many-molecule MD (before init_md; needs mono_wrap=1)."""
         self.lib.orc_set_periodic_md(self.h, float(h))
+
+    def periodic_forces(self, grid):
+        out = np.zeros((self.n_mono, 3))
+        self.lib.orc_periodic_forces(self.h, int(grid), _p(out))
+        return out
 
     def init_md(self):
         self.lib.orc_init_md(self.h)

@@ -92,6 +92,7 @@ struct smpc_orc {
   int* adj_start;     /* undirected bond lists, per monomer: [n_m + 1] */
   int* adj_idx;
   unsigned char* adj_anchor;
+  int pmd_force_grid; /* test hook: take the grid path whatever the size */
 
   int err;
 };
@@ -900,6 +901,17 @@ void orc_run(smpc_orc* o, long t0, long n, double mpc_dt, int with_md) {
 double orc_temperature(smpc_orc* o) {
   double ekin_tot = 0.0;
   unsigned filled = 0;
+  /* monomers binned at a Lees-Edwards image count with that image's velocity,
+   * as in the collision (orc_mpc_step) */
+  double* vx_saved = NULL;
+  if (o->p.mono_wrap && o->n_m > 0) {
+    const double sLy = o->p.shear * o->p.L[1];
+    vx_saved = (double*)malloc(sizeof(double) * (size_t)o->n_m);
+    for (int m = 0; m < o->n_m; ++m) {
+      vx_saved[m] = o->mv[3 * m];
+      o->mv[3 * m] -= o->m_img[m] * sLy;
+    }
+  }
   for (unsigned c = 0; c < o->n_cell; ++c) {
     double cmv[3];
     cell_cmv(o, c, cmv);
@@ -914,6 +926,10 @@ double orc_temperature(smpc_orc* o) {
     ekin *= 0.5;
     ekin_tot += ekin;
     if (nfl > 0) filled++;
+  }
+  if (vx_saved) {
+    for (int m = 0; m < o->n_m; ++m) o->mv[3 * m] = vx_saved[m];
+    free(vx_saved);
   }
   return 2. * ekin_tot / (3. * (unsigned)((unsigned)o->n_f - filled));
 }
@@ -996,16 +1012,88 @@ static void pmd_adjacency(smpc_orc* o) {
   free(fill);
 }
 
+static int pmd_cell_axis(double x, double L, int nc) {
+  int c = (int)floor((x + 0.5 * L) * (nc / L));
+  return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+static int cmp_int(const void* a, const void* b) {
+  const int x = *(const int*)a, y = *(const int*)b;
+  return (x > y) - (x < y);
+}
+
+/* Large boxes: the partners of monomer i come from a periodic grid of cells
+ * of side >= r_verlet (the rows beyond a y face looked up at x -/+ delrx),
+ * sorted by index, so the sums below see the same non-zero terms in the same
+ * order as the loop over all monomers. */
+typedef struct {
+  int nc[3];
+  int* head;
+  int* next;
+} pmd_grid;
+
+static int pmd_grid_build(const smpc_orc* o, pmd_grid* g) {
+  for (int d = 0; d < 3; ++d) {
+    g->nc[d] = (int)floor(o->p.L[d] / o->p.r_verlet);
+    if (g->nc[d] < 3) return 0;
+  }
+  const long ncell = (long)g->nc[0] * g->nc[1] * g->nc[2];
+  g->head = (int*)malloc(sizeof(int) * (size_t)ncell);
+  g->next = (int*)malloc(sizeof(int) * (size_t)(o->n_m + 1));
+  for (long c = 0; c < ncell; ++c) g->head[c] = -1;
+  for (int i = o->n_m - 1; i >= 0; --i) {
+    const double* x = o->mx + 3 * i;
+    const long c = pmd_cell_axis(x[0], o->p.L[0], g->nc[0]) +
+                   (long)g->nc[0] * (pmd_cell_axis(x[1], o->p.L[1], g->nc[1]) +
+                                     (long)g->nc[1] * pmd_cell_axis(x[2], o->p.L[2], g->nc[2]));
+    g->next[i] = g->head[c];
+    g->head[c] = i;
+  }
+  return 1;
+}
+
+static int pmd_grid_partners(const smpc_orc* o, const pmd_grid* g, double dl, int i, int* out) {
+  const double* x = o->mx + 3 * i;
+  const int nx = g->nc[0], ny = g->nc[1], nz = g->nc[2];
+  const double Lx = o->p.L[0];
+  const int cy = pmd_cell_axis(x[1], o->p.L[1], ny), cz = pmd_cell_axis(x[2], o->p.L[2], nz);
+  int cnt = 0;
+  for (int oz = -1; oz <= 1; ++oz) {
+    const int zz = (cz + oz + nz) % nz;
+    for (int oy = -1; oy <= 1; ++oy) {
+      const int yr = cy + oy, yy = (yr + ny) % ny;
+      double xc = x[0];
+      if (yr >= ny) xc -= dl;
+      if (yr < 0) xc += dl;
+      xc -= Lx * round(xc / Lx);
+      const int cx = pmd_cell_axis(xc, Lx, nx);
+      for (int ox = -1; ox <= 1; ++ox) {
+        const long c = (cx + ox + nx) % nx + (long)nx * (yy + (long)ny * zz);
+        for (int j = g->head[c]; j >= 0; j = g->next[j])
+          if (j != i) out[cnt++] = j;
+      }
+    }
+  }
+  qsort(out, (size_t)cnt, sizeof(int), cmp_int);
+  return cnt;
+}
+
 static void pmd_forces(smpc_orc* o, double dl, int calc_epot) {
   const int n = o->n_m, pot = o->p.potential;
   const double lambda = o->p.lambda;
   for (int m = 0; m < o->n_mol; ++m) o->epot_mol[m] = 0.0;
+  pmd_grid grid = {{0, 0, 0}, NULL, NULL};
+  const int use_grid = (n > 2048 || o->pmd_force_grid) && pmd_grid_build(o, &grid);
+  int* part = (int*)malloc(sizeof(int) * (size_t)(n + 1));
   int mol = 0;
   for (int i = 0; i < n; ++i) {
     while (mol + 1 < o->n_mol && i >= o->mol_start[mol + 1]) ++mol;
     const double* xi = o->mx + 3 * i;
     double F0 = 0.0, F1 = 0.0, F2 = 0.0, ep = 0.0;
-    for (int j = 0; j < n; ++j) {
+    int np = n;
+    if (use_grid) np = pmd_grid_partners(o, &grid, dl, i, part);
+    for (int q = 0; q < np; ++q) {
+      const int j = use_grid ? part[q] : q;
       if (j == i) continue;
       double d[3] = {o->mx[3 * j] - xi[0], o->mx[3 * j + 1] - xi[1], o->mx[3 * j + 2] - xi[2]};
       pmd_min_image(o, dl, d);
@@ -1038,6 +1126,23 @@ static void pmd_forces(smpc_orc* o, double dl, int calc_epot) {
     o->mf[3 * i + 2] = F2;
     if (o->n_mol > 0) o->epot_mol[mol] += ep;
   }
+  free(part);
+  free(grid.head);
+  free(grid.next);
+}
+
+/* Test hook: forces at the current positions by the grid (force_grid = 1) or
+ * by the loop over all monomers (0), for checking that both agree. */
+void orc_periodic_forces(smpc_orc* o, int force_grid, double* out) {
+  const int n = o->n_m;
+  double* saved = (double*)malloc(sizeof(double) * (size_t)(3 * n + 3));
+  memcpy(saved, o->mf, sizeof(double) * (size_t)(3 * n));
+  o->pmd_force_grid = force_grid; /* the size threshold lifted (grids need L >= 3 r_verlet) */
+  pmd_forces(o, o->delrx, 0);
+  o->pmd_force_grid = 0;
+  memcpy(out, o->mf, sizeof(double) * (size_t)(3 * n));
+  memcpy(o->mf, saved, sizeof(double) * (size_t)(3 * n));
+  free(saved);
 }
 
 static void pmd_init(smpc_orc* o) {

@@ -314,9 +314,9 @@ class Context:
         self._check(self.lib.smpc_time_cycles(self.h, n, C.byref(tot)), "time_cycles")
         return tot.value
 
-    def init_solvent(self, rep, seed, reference_velocities=False):
-        self._check(self.lib.smpc_init_solvent(self.h, rep, seed, int(reference_velocities)),
-                    "init_solvent")
+    def init_solvent(self, rep, seed, reference_velocities=False, shear_profile=False):
+        flags = (1 if reference_velocities else 0) | (2 if shear_profile else 0)
+        self._check(self.lib.smpc_init_solvent(self.h, rep, seed, flags), "init_solvent")
 
     def synchronize(self):
         self._check(self.lib.smpc_synchronize(self.h), "synchronize")

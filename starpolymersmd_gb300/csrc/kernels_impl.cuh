@@ -1,6 +1,7 @@
 // Launch wrappers shared by kernels_fp64.cu and kernels_fp32.cu; each of
 // those defines SMPC_REAL and the tile constants and includes this file once.
 #pragma once
+#include <algorithm>
 #include "launch.h"
 #include "md_kernels.cuh"
 #include "mpc_fast.cuh"
@@ -40,9 +41,10 @@ template <>
 void launch_mono_prep<Real>(const RepInfo* reps, RepDyn* dyn, int n_rep, Real* mpos, Real* mvel,
                             uint2* mkey, int* mimg, uint32_t* count, ErrorState* err,
                             int mono_bin, int strict, FrameF* frames, double rot_c, double rot_s,
-                            cudaStream_t st) {
-  k_mono_prep<Real, 256><<<n_rep, 256, 0, st>>>(reps, dyn, mpos, mvel, mkey, mimg, count, err,
-                                                mono_bin, strict, frames, rot_c, rot_s);
+                            int chunks, cudaStream_t st) {
+  const dim3 grid(n_rep, chunks > 0 ? chunks : 1);
+  k_mono_prep<Real, 256><<<grid, 256, 0, st>>>(reps, dyn, mpos, mvel, mkey, mimg, count, err,
+                                               mono_bin, strict, frames, rot_c, rot_s);
 }
 
 #if SMPC_FAST_F32
@@ -160,18 +162,31 @@ void launch_unwrap_molecules<Real>(const RepInfo* reps, const RepDyn* dyn, const
 }
 
 template <>
-void launch_pmd_substep<Real>(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, Real* mpos,
-                              Real* mvel, Real* mfrc, Real* mdisp, int adv_k, double adv_scale,
-                              int drift, int calc_epot, cudaStream_t st) {
+void launch_pmd_call<Real>(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, Real* mpos,
+                           Real* mnext, Real* mvel, Real* mfrc, Real* mdisp, int n,
+                           double adv_scale, int calc_epot, cudaStream_t st) {
   if (a.n == 0) return;
   const int nb = a.n_blocks;
-  k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, adv_k,
-                                           adv_scale, drift);
-  k_pmd_bin<Real><<<nb, PMD_NT, 0, st>>>(a, reps, mpos);
-  k_pmd_nlist<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mdisp, adv_k, adv_scale);
-  k_pmd_forces<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, adv_k, adv_scale,
-                                            drift, calc_epot);
-  k_pmd_finish<Real><<<1, 32, 0, st>>>(a, reps, dyn, adv_k, adv_scale, calc_epot);
+  // k_pmd_nlist: warps stride over the beads; at most 8 blocks per SM of GB300
+  const int nb_list = std::min((a.n + PMD_NT / 32 - 1) / (PMD_NT / 32), 152 * 8);
+  const int nb_force = pmd_force_block_count<Real>(a.n);
+  if (n == 0) {
+    k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, 0, adv_scale, 0);
+    k_pmd_nlist<Real><<<nb_list, PMD_NT, 0, st>>>(a, reps, mpos, mdisp, 0, adv_scale);
+    k_pmd_forces<Real><<<nb_force, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mnext, mvel, mfrc, mdisp,
+                                                    0, adv_scale, 0, 0, calc_epot);
+    return;
+  }
+  k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, 1, adv_scale, 1);
+  for (int k = 1; k <= n; ++k) {
+    Real* pin = (k & 1) ? mpos : mnext;  // substep k's positions: buffer (k - 1) & 1
+    Real* pout = (k & 1) ? mnext : mpos;
+    k_pmd_nlist<Real><<<nb_list, PMD_NT, 0, st>>>(a, reps, pin, mdisp, k, adv_scale);
+    k_pmd_forces<Real><<<nb_force, PMD_NT, 0, st>>>(a, reps, dyn, pin, pout, mvel, mfrc, mdisp,
+                                                    k, adv_scale, 1, k < n,
+                                                    calc_epot && k == n);
+  }
+  if ((n & 1) == 0) k_pmd_copy<Real><<<nb, PMD_NT, 0, st>>>(a, mnext, mpos);
 }
 
 template <>

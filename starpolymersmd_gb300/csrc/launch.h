@@ -67,7 +67,7 @@ void launch_init_solvent(const RepInfo* reps, int rep, int slot_cap, R* rec,
 template <typename R>
 void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* mvel, uint2* mkey,
                       int* mimg, uint32_t* count, ErrorState* err, int mono_bin, int strict,
-                      FrameF* frames, double rot_c, double rot_s, cudaStream_t st);
+                      FrameF* frames, double rot_c, double rot_s, int chunks, cudaStream_t st);
 template <typename R>
 void launch_fluid_bin(const Tile* tiles, int n_tiles, const RepInfo* reps, const RepDyn* dyn,
                       const FrameF* frames, const R* rec, uint2* keys, uint32_t* count,
@@ -82,12 +82,12 @@ template <typename R>
 void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, int variant,
                cudaStream_t st);
 
-// One MD substep of one periodic box (pmd_kernels.cuh): substep k of a call
-// passes adv_k = k + 1; drift = 0 builds lists and forces only (set-up).
+// n MD substeps of one periodic box (pmd_kernels.cuh); n = 0 builds lists
+// and forces only (set-up). mnext: second position buffer of the box.
 template <typename R>
-void launch_pmd_substep(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, R* mpos, R* mvel,
-                        R* mfrc, R* mdisp, int adv_k, double adv_scale, int drift, int calc_epot,
-                        cudaStream_t st);
+void launch_pmd_call(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, R* mpos, R* mnext,
+                     R* mvel, R* mfrc, R* mdisp, int n, double adv_scale, int calc_epot,
+                     cudaStream_t st);
 int pmd_block_count(int n_beads);
 
 // Molecules of periodic boxes made whole (observables.cuh); other boxes copied.

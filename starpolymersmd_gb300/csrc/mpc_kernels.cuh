@@ -308,7 +308,8 @@ __global__ void k_cycle_end(RepDyn* dyn, int n_rep) {
 // same values. Slots past n_fluid become holes.
 template <typename R>
 __global__ void k_init_solvent(const RepInfo* reps, int rep, R* st, unsigned long long seed,
-                               double kT, int ref_vel) {
+                               double kT, int flags) {
+  const int ref_vel = flags & 1;  // smpc.h SMPC_INIT_REFERENCE_VELOCITIES
   const RepInfo ri = reps[rep];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ri.slot_cap) return;
@@ -334,10 +335,14 @@ __global__ void k_init_solvent(const RepInfo* reps, int rep, R* st, unsigned lon
     v = R4<R>{static_cast<R>(sd * r1 * cos(t1)), static_cast<R>(sd * r1 * sin(t1)),
               static_cast<R>(sd * r2 * cos(t2)), R(0)};
   }
+  if (flags & 2)  // SMPC_INIT_SHEAR_PROFILE: the steady flow shear * y
+    v.x = static_cast<R>(static_cast<double>(v.x) + ri.shear * static_cast<double>(x.y));
   st_rec(st, slot, x, v);
 }
 
 // One CTA per replica: MPC::check_bounds, then shift and bin the monomers.
+// A replica that cannot recentre (mol0_size == 0, e.g. a periodic box) has
+// independent monomers: it is split over the gridDim.y CTAs of its row.
 template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* dyn, R* mpos,
                                                   R* mvel, uint2* mkey, int* mimg,
@@ -346,12 +351,16 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
                                                   double rot_c, double rot_s) {
   const int r = blockIdx.x;
   const RepInfo ri = reps[r];
+  const bool split = ri.mol0_size == 0;
+  if (blockIdx.y > 0 && !split) return;
   __shared__ int s_out;
   if (threadIdx.x == 0) s_out = 0;
   __syncthreads();
-  const int b = ri.mono_base, n = ri.n_mono;
+  const int per = split ? (ri.n_mono + gridDim.y - 1) / gridDim.y : ri.n_mono;
+  const int b = ri.mono_base + static_cast<int>(blockIdx.y) * per;
+  const int n = max(0, min(per, ri.n_mono - static_cast<int>(blockIdx.y) * per));
   // MPC.cpp:166: any monomer with |x_d| >= L_d/2 - 0.5 triggers recentring
-  for (int i = threadIdx.x; i < n; i += NT) {
+  for (int i = threadIdx.x; i < n && !split; i += NT) {
     const R4<R> x = ld4_rw(mpos, b + i);
     const R xs[3] = {x.x, x.y, x.z};
     for (int d = 0; d < 3; ++d)
@@ -386,7 +395,7 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
         dn.comv[d] = s_c[3 + d] / nm;
       }
     }
-  } else if (threadIdx.x == 0) {
+  } else if (threadIdx.x == 0 && blockIdx.y == 0) {
     dn.recentre = out;
     if (out) {
       // Molecule::calculate_center_of_mass[_velocity] (Molecule.cpp:139-155):
@@ -439,7 +448,8 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
       }
       const uint32_t c = cell_of(g, wx, wy, wz, strict != 0);
       if (c >= static_cast<uint32_t>(ri.n_cell)) {
-        raise_error(err, ERR_MONO_CELL, static_cast<uint32_t>(r), static_cast<uint32_t>(i));
+        raise_error(err, ERR_MONO_CELL, static_cast<uint32_t>(r),
+                    static_cast<uint32_t>(b - ri.mono_base + i));
       } else {
         key = static_cast<uint32_t>(ri.cell_base) + c;
       }
@@ -453,7 +463,7 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
       mimg[b + i] = img;
     }
   }
-  if (frames != nullptr && threadIdx.x == 0) {
+  if (frames != nullptr && threadIdx.x == 0 && blockIdx.y == 0) {
     FrameF f;
     for (int d = 0; d < 3; ++d) {
       f.L[d] = static_cast<float>(ri.L[d]);

@@ -9,25 +9,46 @@
 // periodic images (Box.cpp:105-180); several interacting stars in one box
 // need this form.
 //
-// One substep of one periodic box is five launches over its beads:
-//   k_pmd_drift   half kick and drift, Lees-Edwards wrap, displacement since
-//                 the last list build, rebuild request
-//   k_pmd_bin     (rebuild only) beads into fixed-capacity grid cells
-//   k_pmd_nlist   (rebuild only) Verlet lists from the 27 neighbour cells;
-//                 across a y face the neighbour rows are looked up at x -/+
-//                 delrx. Each list is kept in bead-index order, so the force
-//                 sums do not depend on the order the atomics binned in.
-//   k_pmd_forces  forces and the second half kick; empties the grid after a
-//                 rebuild
-//   k_pmd_finish  records the new lists' delrx, clears the request, sums the
-//                 potential energy of the blocks in a fixed order
-// A rebuild is requested when a bead has moved more than half of what is left
-// of the skin after the change of delrx since the last build: pairs across the
-// y faces see that change as a relative displacement. For periodic boxes the
-// Verlet-reference array holds that displacement (summed v dt), which wrapping
-// does not disturb.
+// A call of n substeps (k = 1..n) is 2n + 1 launches, plus a copy when n is
+// even:
+//   k_pmd_drift   substep 1: half kick and drift, Lees-Edwards wrap, peculiar
+//                 displacement, binning into the grid of substep 1, rebuild
+//                 request; block 0 records the substep's delrx
+//   k_pmd_nlist   records delrx and the rebuild threshold of the next
+//                 substep; then (rebuild only) one warp per bead: the lanes
+//                 test the beads of the 27 neighbour cells (across a y face
+//                 the neighbour rows are looked up at x -/+ delrx) and the
+//                 list is written in bead-index order, so the force sums do
+//                 not depend on the order the binning atomics filled the
+//                 cells in. Lists are rows of max_nb entries per bead.
+//   k_pmd_forces  LANES lanes per bead split its Verlet list, a butterfly sums
+//                 them; second half kick; then, for k < n, substep k+1's half
+//                 kick, drift, wrap and binning, writing the positions into
+//                 the other of two position buffers (other beads still read
+//                 substep k's); the last block to finish records the new
+//                 lists' delrx, clears the request and sums the potential
+//                 energy of the blocks in a fixed order
+// Substep k's positions live in buffer (k - 1) & 1 (0 = the monomer array),
+// its grid, rebuild request and delrx in slots k & 1. The set-up call (n = 0)
+// wraps, bins and builds lists and forces at the current positions.
+//
+// Rebuild criterion. The Verlet-reference array of a periodic box holds each
+// bead's peculiar displacement since the last build, u = sum (v - shear y e_x)
+// dt with y the bead's height at the start of the drift (continuous across a
+// y face, where y and v_x jump together). Lees-Edwards images move with the
+// affine flow, so over a time t the minimum-image separation of any two beads
+// changes by u_j - u_i plus shear * t times their image-frame height
+// difference, which is at most r_verlet + skin for every pair that can come
+// within r_cut. A pair outside the lists then stays outside r_cut while
+//   2 max|u| + shear t (r_verlet + skin) + |delrx drift| <= skin,
+// where the delrx drift is the part of the change of delrx since the build
+// that the flow does not explain (zero in the physical delrx mode, up to
+// round-off; the reference mode advances delrx faster than the flow). Beads
+// carried by the shear flow therefore trigger no rebuilds.
 #pragma once
 #include <stdint.h>
+
+#include <type_traits>
 
 #include "md_kernels.cuh"
 #include "observables.cuh"
@@ -36,6 +57,19 @@ namespace smpc {
 
 constexpr int PMD_CELL_CAP = 128;  // beads per grid cell
 constexpr int PMD_NT = 256;        // threads per block of every periodic-MD kernel
+constexpr int PMD_NL_CAP = 256;    // Verlet-list entries one warp of k_pmd_nlist collects
+
+// Lanes per bead in k_pmd_forces: FP64 keeps one (the oracle's order of the
+// sums), FP32 splits each list over eight.
+template <typename R>
+constexpr int pmd_force_lanes() {
+  return std::is_same<R, float>::value ? 8 : 1;
+}
+
+template <typename R>
+inline int pmd_force_block_count(int n_beads) {
+  return (n_beads * pmd_force_lanes<R>() + PMD_NT - 1) / PMD_NT;
+}
 
 struct PmdArgs {
   int rep;
@@ -43,14 +77,17 @@ struct PmdArgs {
   int n;               // beads
   int nc[3];           // grid cells per axis (>= 3, side >= r_verlet)
   int ncell;
-  int n_blocks;        // blocks of the per-bead launches
-  uint32_t* cnt;       // beads per grid cell; zero between rebuilds
-  int* items;          // ncell x PMD_CELL_CAP bead indices (box-local)
-  int* flag;           // rebuild requested
+  int n_blocks;        // blocks of the one-thread-per-bead launches
+  uint32_t* cnt[2];    // beads per grid cell, grids of even / odd substeps
+  int* items[2];       // ncell x PMD_CELL_CAP bead indices (box-local)
+  int* flag;           // [0], [1] rebuild requested (even / odd substep),
+                       // [2] blocks done, [3] substeps since the last build
   double* delrx_build; // delrx of the current lists
+  double* dl_slot;     // substep k: delrx at [k & 1], rebuild threshold at [2 + (k & 1)]
   double* epot_part;   // per block of k_pmd_forces
-  int* nlist;          // [max_nb][n_mono_total] global indices, as md_kernels.cuh
-  int* ncount;
+  int* nlist;          // [n][max_nb] global indices of each bead's Verlet list
+  int* ncount;         // per global monomer
+  const uint8_t* amphi;  // per global monomer: 1 = solvophobic
   int n_mono_total;
   int max_nb;
   const int* bond_start;
@@ -58,16 +95,13 @@ struct PmdArgs {
   ErrorState* err;
 };
 
-// delrx after k more MD steps: k_cycle_begin's operations (MPC.cpp:117-118)
-__device__ __forceinline__ double pmd_delrx(const RepInfo& ri, double d, int k,
-                                            double adv_scale) {
+// delrx one MD step later: one iteration of k_cycle_begin's loop
+// (MPC.cpp:117-118), so substep k of a call sees k of them
+__device__ __forceinline__ double pmd_advance(const RepInfo& ri, double d, double adv_scale) {
   const double Lx = static_cast<double>(ri.L[0]);
   const double adv_dt = __dmul_rn(ri.h, adv_scale);
-  for (int s = 0; s < k; ++s) {
-    d = __dadd_rn(d, __dmul_rn(__dmul_rn(ri.shear, static_cast<double>(ri.L[1])), adv_dt));
-    d = __dsub_rn(d, __dmul_rn(Lx, round(__ddiv_rn(d, Lx))));
-  }
-  return d;
+  d = __dadd_rn(d, __dmul_rn(__dmul_rn(ri.shear, static_cast<double>(ri.L[1])), adv_dt));
+  return __dsub_rn(d, __dmul_rn(Lx, round(__ddiv_rn(d, Lx))));
 }
 
 // q / L: a division in FP64 (the reference's operation), the reciprocal
@@ -110,50 +144,46 @@ __device__ __forceinline__ int pmd_cell_axis(R x, R L, int nc) {
   return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
-// delrx of this launch's substep, computed once per block
-__device__ __forceinline__ double pmd_block_delrx(const RepInfo& ri, const RepDyn* dyn, int rep,
-                                                  int adv_k, double adv_scale) {
-  __shared__ double s_dl;
-  if (threadIdx.x == 0) s_dl = pmd_delrx(ri, dyn[rep].delrx, adv_k, adv_scale);
-  __syncthreads();
-  return s_dl;
+template <typename R>
+__device__ __forceinline__ int pmd_cell(const PmdArgs& a, const PmdBox<R>& b, const R4<R>& x) {
+  return pmd_cell_axis(x.x, b.L[0], a.nc[0]) +
+         a.nc[0] * (pmd_cell_axis(x.y, b.L[1], a.nc[1]) +
+                    a.nc[1] * pmd_cell_axis(x.z, b.L[2], a.nc[2]));
+}
+
+// Rebuild threshold of a substep whose drift ends `tb` after the last build
+// at delrx `db`, at delrx `dl` (criterion in the header comment).
+template <typename R>
+__device__ __forceinline__ R pmd_threshold(const RepInfo& ri, double dl, double db, R tb) {
+  const R Lx = static_cast<R>(ri.L[0]);
+  const R shear = static_cast<R>(ri.shear);
+  const R skin = static_cast<R>(ri.r_verlet) - static_cast<R>(ri.r_cut);
+  R ddl = static_cast<R>(dl - db) - shear * static_cast<R>(ri.L[1]) * tb;
+  ddl -= Lx * r_round(ddl / Lx);
+  return R(0.5) * (skin - r_fabs(shear) * tb * (static_cast<R>(ri.r_verlet) + skin) - r_fabs(ddl));
+}
+
+// One bead's half kick (with the force f), drift, Lees-Edwards wrap and
+// peculiar displacement (Thermostat_None.cpp:22-27, MPC.cpp:421-429).
+template <typename R>
+__device__ __forceinline__ void pmd_drift_bead(const RepInfo& ri, const PmdBox<R>& b, R4<R>& x,
+                                               R4<R>& v, R4<R>& u, R f0, R f1, R f2) {
+  const R dt = static_cast<R>(ri.md_dt), dth = dt * R(0.50);
+  const R y0 = x.y;
+  v.x += (f0 / x.w) * dth;
+  x.x += v.x * dt;
+  u.x += (v.x - static_cast<R>(ri.shear) * y0) * dt;
+  v.y += (f1 / x.w) * dth;
+  x.y += v.y * dt;
+  u.y += v.y * dt;
+  v.z += (f2 / x.w) * dth;
+  x.z += v.z * dt;
+  u.z += v.z * dt;
 }
 
 template <typename R>
-__global__ void __launch_bounds__(PMD_NT)
-    k_pmd_drift(PmdArgs a, const RepInfo* reps, const RepDyn* dyn, R* mpos, R* mvel,
-                const R* mfrc, R* mdisp, int adv_k, double adv_scale, int drift) {
-  const RepInfo& ri = reps[a.rep];
-  const double dl = pmd_block_delrx(ri, dyn, a.rep, adv_k, adv_scale);
-  __shared__ R s_thr;
-  if (threadIdx.x == 0) {
-    const double Lx = static_cast<double>(ri.L[0]);
-    double ddl = dl - *a.delrx_build;
-    ddl -= Lx * round(ddl / Lx);
-    s_thr = static_cast<R>(0.5 * ((ri.r_verlet - ri.r_cut) - fabs(ddl)));
-  }
-  __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const PmdBox<R> b = pmd_box<R>(ri, dl);
-  const size_t g = static_cast<size_t>(a.base) + i;
-  R4<R> x = ld4_rw(mpos, g), v = ld4_rw(mvel, g), u = ld4_rw(mdisp, g);
-  if (drift) {
-    const R4<R> f = ld4_rw(mfrc, g);
-    const R dt = static_cast<R>(ri.md_dt), dth = dt * R(0.50);
-    // kick + drift (Thermostat_None.cpp:22-27)
-    v.x += (f.x / x.w) * dth;
-    x.x += v.x * dt;
-    u.x += v.x * dt;
-    v.y += (f.y / x.w) * dth;
-    x.y += v.y * dt;
-    u.y += v.y * dt;
-    v.z += (f.z / x.w) * dth;
-    x.z += v.z * dt;
-    u.z += v.z * dt;
-  }
-  // back into the primary box (MPC::LEBC); the set-up call (drift = 0) only
-  // wraps what the caller placed outside
+__device__ __forceinline__ void pmd_wrap(const RepInfo& ri, const PmdBox<R>& b, R4<R>& x,
+                                         R4<R>& v) {
   const R cy = r_round(pmd_ratio(x.y, b.L[1], b.inv[1]));
   x.x -= b.L[0] * r_round(pmd_ratio(x.x, b.L[0], b.inv[0]));
   x.x -= cy * b.delrx;
@@ -161,133 +191,217 @@ __global__ void __launch_bounds__(PMD_NT)
   x.y -= b.L[1] * cy;
   x.z -= b.L[2] * r_round(pmd_ratio(x.z, b.L[2], b.inv[2]));
   v.x -= cy * static_cast<R>(ri.shear) * b.L[1];
-  st4(mpos, g, x);
-  st4(mvel, g, v);
-  if (!drift) {  // set-up: lists and forces from the current positions
-    if (i == 0) *a.flag = 1;
-    return;
-  }
-  st4(mdisp, g, u);
-  const R thr = s_thr;
-  if (thr <= R(0) || (u.x * u.x + u.y * u.y) + u.z * u.z > thr * thr) *a.flag = 1;
 }
 
+// bead i (box-local) into grid s
 template <typename R>
-__global__ void __launch_bounds__(PMD_NT) k_pmd_bin(PmdArgs a, const RepInfo* reps, const R* mpos) {
-  if (*a.flag == 0) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const RepInfo& ri = reps[a.rep];
-  const R4<R> x = ld4_rw(mpos, static_cast<size_t>(a.base) + i);
-  const int cx = pmd_cell_axis(x.x, static_cast<R>(ri.L[0]), a.nc[0]);
-  const int cy = pmd_cell_axis(x.y, static_cast<R>(ri.L[1]), a.nc[1]);
-  const int cz = pmd_cell_axis(x.z, static_cast<R>(ri.L[2]), a.nc[2]);
-  const int c = cx + a.nc[0] * (cy + a.nc[1] * cz);
-  const uint32_t k = atomicAdd(a.cnt + c, 1u);
+__device__ __forceinline__ void pmd_bin(const PmdArgs& a, int s, const PmdBox<R>& b,
+                                        const R4<R>& x, int i) {
+  const int c = pmd_cell(a, b, x);
+  const uint32_t k = atomicAdd(a.cnt[s] + c, 1u);
   if (k < static_cast<uint32_t>(PMD_CELL_CAP))
-    a.items[static_cast<size_t>(c) * PMD_CELL_CAP + k] = i;
+    a.items[s][static_cast<size_t>(c) * PMD_CELL_CAP + k] = i;
   else
     raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(a.base + i), k);
 }
 
+// Substep 1 of a call (adv_k = 1, drift = 1) or the set-up (adv_k = 0,
+// drift = 0: wrap what the caller placed outside, request the first build).
 template <typename R>
 __global__ void __launch_bounds__(PMD_NT)
-    k_pmd_nlist(PmdArgs a, const RepInfo* reps, const RepDyn* dyn, const R* mpos, R* mdisp,
-                int adv_k, double adv_scale) {
-  if (*a.flag == 0) return;
+    k_pmd_drift(PmdArgs a, const RepInfo* reps, const RepDyn* dyn, R* mpos, R* mvel,
+                const R* mfrc, R* mdisp, int adv_k, double adv_scale, int drift) {
   const RepInfo& ri = reps[a.rep];
-  const PmdBox<R> b = pmd_box<R>(ri, pmd_block_delrx(ri, dyn, a.rep, adv_k, adv_scale));
+  __shared__ double s_dl;
+  __shared__ R s_thr;
+  if (threadIdx.x == 0) {
+    const double base = dyn[a.rep].delrx;
+    const double dl = adv_k == 0 ? base : pmd_advance(ri, base, adv_scale);
+    if (blockIdx.x == 0) a.dl_slot[adv_k & 1] = dl;
+    s_dl = dl;
+    s_thr = pmd_threshold<R>(ri, dl, *a.delrx_build,
+                             static_cast<R>(a.flag[3] + 1) * static_cast<R>(ri.md_dt));
+  }
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const R rv2 = static_cast<R>(ri.r_verlet) * static_cast<R>(ri.r_verlet);
+  const PmdBox<R> b = pmd_box<R>(ri, s_dl);
   const size_t g = static_cast<size_t>(a.base) + i;
-  const R4<R> x = ld4_rw(mpos, g);
-  const int nx = a.nc[0], ny = a.nc[1], nz = a.nc[2];
-  const int cy = pmd_cell_axis(x.y, b.L[1], ny);
-  const int cz = pmd_cell_axis(x.z, b.L[2], nz);
-  const size_t stride = static_cast<size_t>(a.n_mono_total);
-  int* nl = a.nlist + g;
-  int cnt = 0;
-  for (int oz = -1; oz <= 1; ++oz) {
-    const int zz = (cz + oz + nz) % nz;
-    for (int oy = -1; oy <= 1; ++oy) {
-      const int yr = cy + oy;
-      const int yy = (yr + ny) % ny;
-      // the row beyond a y face is the image shifted by delrx along x
-      R xc = x.x;
-      if (yr >= ny) xc -= b.delrx;
-      if (yr < 0) xc += b.delrx;
-      xc -= b.L[0] * r_round(pmd_ratio(xc, b.L[0], b.inv[0]));
-      const int cx = pmd_cell_axis(xc, b.L[0], nx);
-      for (int ox = -1; ox <= 1; ++ox) {
-        const int c = (cx + ox + nx) % nx + nx * (yy + ny * zz);
-        const int m = min(static_cast<int>(a.cnt[c]), PMD_CELL_CAP);
-        for (int q = 0; q < m; ++q) {
-          const int j = a.items[static_cast<size_t>(c) * PMD_CELL_CAP + q];
-          if (j == i) continue;
-          const R4<R> y = ld4_rw(mpos, static_cast<size_t>(a.base) + j);
-          R d0 = y.x - x.x, d1 = y.y - x.y, d2 = y.z - x.z;
-          pmd_min_image(d0, d1, d2, b);
-          if ((d0 * d0 + d1 * d1) + d2 * d2 <= rv2) {
-            if (cnt < a.max_nb) {  // insertion in index order
-              int p = cnt;
-              while (p > 0 && nl[static_cast<size_t>(p - 1) * stride] > a.base + j) {
-                nl[static_cast<size_t>(p) * stride] = nl[static_cast<size_t>(p - 1) * stride];
-                --p;
-              }
-              nl[static_cast<size_t>(p) * stride] = a.base + j;
-            }
-            ++cnt;
-          }
-        }
-      }
-    }
+  R4<R> x = ld4_rw(mpos, g), v = ld4_rw(mvel, g), u = ld4_rw(mdisp, g);
+  if (drift) {
+    const R4<R> f = ld4_rw(mfrc, g);
+    pmd_drift_bead(ri, b, x, v, u, f.x, f.y, f.z);
   }
-  if (cnt > a.max_nb) {
-    raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(g), static_cast<uint32_t>(cnt));
-    cnt = a.max_nb;
+  pmd_wrap(ri, b, x, v);
+  st4(mpos, g, x);
+  st4(mvel, g, v);
+  pmd_bin(a, adv_k & 1, b, x, i);
+  if (!drift) {
+    if (i == 0) a.flag[0] = 1;
+    return;
   }
-  a.ncount[g] = cnt;
-  st4(mdisp, g, R4<R>{R(0), R(0), R(0), R(0)});
+  st4(mdisp, g, u);
+  const R thr = s_thr;
+  if (thr <= R(0) || (u.x * u.x + u.y * u.y) + u.z * u.z > thr * thr) a.flag[adv_k & 1] = 1;
 }
 
+// Verlet list of bead i (box-local) by the 32 lanes of one warp; buf holds
+// PMD_NL_CAP entries.
+template <typename R>
+__device__ __forceinline__ void pmd_list_bead(const PmdArgs& a, int s, const PmdBox<R>& b, R rv2,
+                                              const R* pos, R* mdisp, int i, int lane, int* buf) {
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  const size_t g = static_cast<size_t>(a.base) + i;
+  const R4<R> x = ld4_rw(pos, g);
+  const int nx = a.nc[0], ny = a.nc[1], nz = a.nc[2];
+  const uint32_t* cnt = a.cnt[s];
+  const int* items = a.items[s];
+  // lanes 0..26: one neighbour cell each (row-major over dz, dy, dx)
+  int c_l = 0, m_l = 0;
+  if (lane < 27) {
+    const int oz = lane / 9 - 1, oy = (lane / 3) % 3 - 1, ox = lane % 3 - 1;
+    const int zz = (pmd_cell_axis(x.z, b.L[2], nz) + oz + nz) % nz;
+    const int yr = pmd_cell_axis(x.y, b.L[1], ny) + oy;
+    const int yy = (yr + ny) % ny;
+    // the row beyond a y face is the image shifted by delrx along x
+    R xc = x.x;
+    if (yr >= ny) xc -= b.delrx;
+    if (yr < 0) xc += b.delrx;
+    xc -= b.L[0] * r_round(pmd_ratio(xc, b.L[0], b.inv[0]));
+    const int cx = pmd_cell_axis(xc, b.L[0], nx);
+    c_l = (cx + ox + nx) % nx + nx * (yy + ny * zz);
+    m_l = min(static_cast<int>(cnt[c_l]), PMD_CELL_CAP);
+  }
+  int incl = m_l;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int excl = incl - m_l;
+  const int total = __shfl_sync(FULL, incl, 31);
+  // the candidates of all 27 cells, 32 at a time: lane k takes candidate k0 + k
+  int n_acc = 0;
+  for (int k0 = 0; k0 < total; k0 += 32) {
+    const int k = k0 + lane;
+    int L = 0;  // the cell lane whose range [excl, incl) holds k
+    for (int st = 16; st > 0; st >>= 1) {
+      const int e = __shfl_sync(FULL, excl, L + st);
+      if (L + st < 27 && e <= k) L += st;
+    }
+    const int cell = __shfl_sync(FULL, c_l, L);
+    const int q = k - __shfl_sync(FULL, excl, L);
+    bool ok = false;
+    int j = -1;
+    if (k < total) {
+      j = items[static_cast<size_t>(cell) * PMD_CELL_CAP + q];
+      if (j != i) {
+        const R4<R> y = ld4_rw(pos, static_cast<size_t>(a.base) + j);
+        R d0 = y.x - x.x, d1 = y.y - x.y, d2 = y.z - x.z;
+        pmd_min_image(d0, d1, d2, b);
+        ok = (d0 * d0 + d1 * d1) + d2 * d2 <= rv2;
+      }
+    }
+    const unsigned ball = __ballot_sync(FULL, ok);
+    const int at = n_acc + __popc(ball & ((1u << lane) - 1u));
+    if (ok && at < PMD_NL_CAP) buf[at] = j;
+    n_acc += __popc(ball);
+  }
+  __syncwarp();
+  const int cap = min(a.max_nb, PMD_NL_CAP);
+  if (n_acc > cap) {
+    if (lane == 0)
+      raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(g), static_cast<uint32_t>(n_acc));
+    n_acc = cap;
+  }
+  // entry e goes to the place of its rank among the collected indices
+  int* row = a.nlist + static_cast<size_t>(i) * a.max_nb;
+  for (int e = lane; e < n_acc; e += 32) {
+    const int je = buf[e];
+    int r = 0;
+    for (int f = 0; f < n_acc; ++f) r += buf[f] < je ? 1 : 0;
+    row[r] = a.base + je;
+  }
+  if (lane == 0) {
+    a.ncount[g] = n_acc;
+    st4(mdisp, g, R4<R>{R(0), R(0), R(0), R(0)});
+  }
+}
+
+// One warp per bead, the warps striding over the beads.
 template <typename R>
 __global__ void __launch_bounds__(PMD_NT)
-    k_pmd_forces(PmdArgs a, const RepInfo* reps, const RepDyn* dyn, const R* mpos, R* mvel,
-                 R* mfrc, int adv_k, double adv_scale, int kick, int calc_epot) {
+    k_pmd_nlist(PmdArgs a, const RepInfo* reps, const R* pos, R* mdisp, int adv_k,
+                double adv_scale) {
+  const int s = adv_k & 1;
   const RepInfo& ri = reps[a.rep];
-  const PmdBox<R> b = pmd_box<R>(ri, pmd_block_delrx(ri, dyn, a.rep, adv_k, adv_scale));
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // the next substep's delrx and threshold, for the drift in k_pmd_forces:
+    // its lists are this substep's if it rebuilds them, else the older ones
+    const double dl = a.dl_slot[s];
+    const int rebuilt = a.flag[s];
+    const double dl1 = pmd_advance(ri, dl, adv_scale);
+    const double db = rebuilt ? dl : *a.delrx_build;
+    const int since = rebuilt ? 0 : a.flag[3] + 1;
+    a.dl_slot[s ^ 1] = dl1;
+    a.dl_slot[2 + (s ^ 1)] = static_cast<double>(
+        pmd_threshold<R>(ri, dl1, db, static_cast<R>(since + 1) * static_cast<R>(ri.md_dt)));
+  }
+  if (a.flag[s] == 0) return;
+  __shared__ int s_buf[PMD_NT / 32][PMD_NL_CAP];
+  const int warp = static_cast<int>(threadIdx.x) >> 5, lane = static_cast<int>(threadIdx.x) & 31;
+  const PmdBox<R> b = pmd_box<R>(ri, a.dl_slot[s]);
+  const R rv2 = static_cast<R>(ri.r_verlet) * static_cast<R>(ri.r_verlet);
+  for (int i = static_cast<int>(blockIdx.x) * (PMD_NT / 32) + warp; i < a.n;
+       i += static_cast<int>(gridDim.x) * (PMD_NT / 32)) {
+    pmd_list_bead(a, s, b, rv2, pos, mdisp, i, lane, s_buf[warp]);
+    __syncwarp();  // the buffer is refilled by the warp's next bead
+  }
+}
+
+// Substep k: forces at positions pin, second half kick; with drift_next,
+// substep k+1's kick, drift, wrap and binning into pout.
+template <typename R>
+__global__ void __launch_bounds__(PMD_NT)
+    k_pmd_forces(PmdArgs a, const RepInfo* reps, RepDyn* dyn, const R* pin, R* pout, R* mvel,
+                 R* mfrc, R* mdisp, int adv_k, double adv_scale, int kick, int drift_next,
+                 int calc_epot) {
+  constexpr int LANES = pmd_force_lanes<R>();
+  const RepInfo& ri = reps[a.rep];
+  const int s = adv_k & 1;
+  const PmdBox<R> b = pmd_box<R>(ri, a.dl_slot[s]);
+  const int t = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+  const int i = t / LANES, sub = t % LANES;
   double ep = 0.0;
+  R F0 = R(0), F1 = R(0), F2 = R(0);
+  size_t g = 0;
+  R4<R> x{}, v{};
   if (i < a.n) {
     const R lambda = static_cast<R>(ri.lambda);
     const int pot = ri.potential;
-    const size_t g = static_cast<size_t>(a.base) + i;
-    const R4<R> x = ld4_rw(mpos, g);
-    R4<R> v = ld4_rw(mvel, g);
-    const bool ai = (static_cast<int>(v.w) & 1) != 0;
-    const size_t stride = static_cast<size_t>(a.n_mono_total);
-    R F0 = R(0), F1 = R(0), F2 = R(0);
+    g = static_cast<size_t>(a.base) + i;
+    x = ld4_rw(pin, g);
+    const bool ai = a.amphi[g] != 0;
     const int cnt = a.ncount[g];
-    const int* nl = a.nlist + g;
-    // (Box.cpp:243-286) pairs in index order, then the bead's bonds; the
-    // neighbour indices come four at a time, as independent loads
+    const int* nl = a.nlist + static_cast<size_t>(i) * a.max_nb;
+    // (Box.cpp:243-286) pairs in index order (every LANES-th to each lane),
+    // four independent neighbour loads at a time; then the bead's bonds
     constexpr int PF = 4;
-    for (int q0 = 0; q0 < cnt; q0 += PF) {
+    for (int q0 = sub; q0 < cnt; q0 += PF * LANES) {
       int js[PF];
 #pragma unroll
-      for (int u = 0; u < PF; ++u)
-        js[u] = q0 + u < cnt ? nl[static_cast<size_t>(q0 + u) * stride] : -1;
+      for (int u = 0; u < PF; ++u) {
+        const int q = q0 + u * LANES;
+        js[u] = q < cnt ? nl[q] : -1;
+      }
 #pragma unroll
       for (int u = 0; u < PF; ++u) {
         const int j = js[u];
         if (j < 0) continue;
-        const R4<R> y = ld4_rw(mpos, static_cast<size_t>(j));
-        const R wy = mvel[4 * static_cast<size_t>(j) + 3];
+        const R4<R> y = ld4_rw(pin, static_cast<size_t>(j));
         R d0 = y.x - x.x, d1 = y.y - x.y, d2 = y.z - x.z;
         pmd_min_image(d0, d1, d2, b);
         const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
-        const bool bb = ai && (static_cast<int>(wy) & 1) != 0;
+        const bool bb = ai && a.amphi[j] != 0;
         const R fa = pair_force<R>(pot, bb, r2, lambda);
         F0 -= d0 * fa;
         F1 -= d1 * fa;
@@ -295,9 +409,9 @@ __global__ void __launch_bounds__(PMD_NT)
         if (calc_epot) ep += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
       }
     }
-    for (int e = a.bond_start[g]; e < a.bond_start[g + 1]; ++e) {
+    for (int e = a.bond_start[g] + sub; e < a.bond_start[g + 1]; e += LANES) {
       const int2 bd = a.bonds[e];
-      const R4<R> y = ld4_rw(mpos, static_cast<size_t>(bd.x));
+      const R4<R> y = ld4_rw(pin, static_cast<size_t>(bd.x));
       R d0 = y.x - x.x, d1 = y.y - x.y, d2 = y.z - x.z;
       pmd_min_image(d0, d1, d2, b);
       const bool anch = bd.y != 0;
@@ -316,41 +430,75 @@ __global__ void __launch_bounds__(PMD_NT)
       F2 -= d2 * fa;
       if (calc_epot) ep += 0.5 * static_cast<double>(fene_pot<R>(anch, r2));
     }
+  }
+  // the lanes of a bead are adjacent within one warp (LANES divides 32)
+  for (int o = 1; o < LANES; o <<= 1) {
+    F0 += __shfl_xor_sync(0xFFFFFFFFu, F0, o);
+    F1 += __shfl_xor_sync(0xFFFFFFFFu, F1, o);
+    F2 += __shfl_xor_sync(0xFFFFFFFFu, F2, o);
+  }
+  if (i < a.n && sub == 0) {
     st4(mfrc, g, R4<R>{F0, F1, F2, R(0)});
+    // this substep's grid is empty again: its beads' cells back to zero
+    a.cnt[s][pmd_cell(a, b, x)] = 0u;
+    v = ld4_rw(mvel, g);
     if (kick) {  // second half kick (Thermostat_None.cpp:33-37)
       const R dth = static_cast<R>(ri.md_dt) * R(0.50);
       v.x += (F0 / x.w) * dth;
       v.y += (F1 / x.w) * dth;
       v.z += (F2 / x.w) * dth;
-      st4(mvel, g, v);
     }
+    if (drift_next) {
+      const PmdBox<R> b1 = pmd_box<R>(ri, a.dl_slot[s ^ 1]);
+      R4<R> u = ld4_rw(mdisp, g);
+      pmd_drift_bead(ri, b1, x, v, u, F0, F1, F2);
+      pmd_wrap(ri, b1, x, v);
+      st4(pout, g, x);
+      st4(mdisp, g, u);
+      pmd_bin(a, s ^ 1, b1, x, i);
+      const R thr = static_cast<R>(a.dl_slot[2 + (s ^ 1)]);
+      if (thr <= R(0) || (u.x * u.x + u.y * u.y) + u.z * u.z > thr * thr) a.flag[s ^ 1] = 1;
+    }
+    if (kick || drift_next) st4(mvel, g, v);
   }
   if (calc_epot) {
     __shared__ double s_red[PMD_NT / 32];
-    const double t = block_sum<PMD_NT>(ep, s_red);
-    if (threadIdx.x == 0) a.epot_part[blockIdx.x] = t;
+    const double tot = block_sum<PMD_NT>(ep, s_red);
+    if (threadIdx.x == 0) a.epot_part[blockIdx.x] = tot;
   }
-  if (*a.flag != 0) {  // the grid is empty again for the next rebuild
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell; c += gridDim.x * blockDim.x)
-      a.cnt[c] = 0u;
+  // the last block to get here closes the substep (no block waits for another)
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(reinterpret_cast<unsigned*>(a.flag + 2), 1u) == gridDim.x - 1;
   }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  RepDyn& dn = dyn[a.rep];
+  if (a.flag[s] != 0) {
+    *a.delrx_build = a.dl_slot[s];
+    a.flag[3] = 0;
+    dn.verlet_rebuilds += 1;
+  } else {
+    a.flag[3] += 1;
+  }
+  a.flag[s] = 0;
+  if (calc_epot) {
+    double tot = 0.0;
+    for (int k = 0; k < static_cast<int>(gridDim.x); ++k) tot += a.epot_part[k];
+    dn.epot = tot;
+  }
+  a.flag[2] = 0;
 }
 
 template <typename R>
-__global__ void k_pmd_finish(PmdArgs a, const RepInfo* reps, RepDyn* dyn, int adv_k,
-                             double adv_scale, int calc_epot) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  RepDyn& dn = dyn[a.rep];
-  if (*a.flag != 0) {
-    *a.delrx_build = pmd_delrx(reps[a.rep], dn.delrx, adv_k, adv_scale);
-    *a.flag = 0;
-    dn.verlet_rebuilds += 1;
-  }
-  if (calc_epot) {
-    double s = 0.0;
-    for (int k = 0; k < a.n_blocks; ++k) s += a.epot_part[k];
-    dn.epot = s;
-  }
+__global__ void __launch_bounds__(PMD_NT) k_pmd_copy(PmdArgs a, const R* src, R* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const size_t g = static_cast<size_t>(a.base) + i;
+  st4(dst, g, ld4_rw(src, g));
 }
 
 }  // namespace smpc

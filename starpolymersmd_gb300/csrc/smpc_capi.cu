@@ -70,12 +70,15 @@ struct smpc_ctx {
   int* d_ncount = nullptr;
   int* d_md_order = nullptr;  // replicas by decreasing monomer count (MD CTA order)
   bool any_local_md = false;  // a non-periodic replica has monomers
+  int mono_chunks = 1;        // CTAs per replica of k_mono_prep (replicas that cannot recentre)
   // periodic boxes (SMPC_REPLICA_PERIODIC_MD): launch arguments with their grid
   // buffers, and molecules made whole for the observables
   std::vector<smpc::PmdArgs> pmd;
   std::vector<void*> pmd_mem;
   void* d_upos = nullptr;
   void* d_uvel = nullptr;
+  void* d_mnext = nullptr;    // second monomer position buffer of the periodic MD
+  uint8_t* d_pamphi = nullptr;  // solvophobic flag per monomer (periodic MD)
   std::vector<std::vector<int>> bsrc, bdst;
   std::vector<std::vector<int>> anchor;
 
@@ -159,7 +162,7 @@ int launch_binning(smpc_ctx* ctx, int cur) {
   smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
                             static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
                             ctx->d_err, ctx->opt.mono_bin, strict, ctx->d_frames, ctx->rot_c,
-                            ctx->rot_s, ctx->st);
+                            ctx->rot_s, ctx->mono_chunks, ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
                             ctx->var_bin, ctx->st);
@@ -216,20 +219,11 @@ template <typename R>
 int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   if (ctx->total_mono == 0) return SMPC_OK;
   const double adv = ctx->opt.delrx_mode == SMPC_DELRX_PHYSICAL ? 1.0 / ctx->opt.step_update : 1.0;
-  for (const smpc::PmdArgs& p : ctx->pmd) {
-    R* mpos = static_cast<R*>(ctx->d_mpos);
-    R* mvel = static_cast<R*>(ctx->d_mvel);
-    R* mfrc = static_cast<R*>(ctx->d_mfrc);
-    R* mdisp = static_cast<R*>(ctx->d_mver);
-    if (n == 0) {
-      smpc::launch_pmd_substep<R>(p, ctx->d_reps, ctx->d_dyn, mpos, mvel, mfrc, mdisp, 0, adv, 0,
-                                  calc_epot, ctx->st);
-    } else {
-      for (int k = 0; k < n; ++k)
-        smpc::launch_pmd_substep<R>(p, ctx->d_reps, ctx->d_dyn, mpos, mvel, mfrc, mdisp, k + 1,
-                                    adv, 1, calc_epot && k == n - 1, ctx->st);
-    }
-  }
+  for (const smpc::PmdArgs& p : ctx->pmd)
+    smpc::launch_pmd_call<R>(p, ctx->d_reps, ctx->d_dyn, static_cast<R*>(ctx->d_mpos),
+                             static_cast<R*>(ctx->d_mnext), static_cast<R*>(ctx->d_mvel),
+                             static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), n, adv,
+                             calc_epot, ctx->st);
   if (!ctx->any_local_md) return SMPC_OK;
   smpc::MdArgs a;
   a.reps = ctx->d_reps;
@@ -269,7 +263,7 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
   smpc::launch_mono_prep<R>(ctx->d_reps, ctx->d_dyn, ctx->n_rep, static_cast<R*>(ctx->d_mpos),
                             static_cast<R*>(ctx->d_mvel), ctx->d_mkey, ctx->d_mimg, ctx->d_count,
                             ctx->d_err, ctx->opt.mono_bin, strict, ctx->d_frames, ctx->rot_c,
-                            ctx->rot_s, ctx->st);
+                            ctx->rot_s, ctx->mono_chunks, ctx->st);
   cudaEventRecord(ev[1 + PH_MONO], ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
@@ -609,6 +603,11 @@ int upload_bonds(smpc_ctx* ctx) {
     CU(cudaMemcpy(ctx->d_bonds, flat.data(), flat.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(ctx->d_bond_start, start.data(), (M + 1) * sizeof(int), cudaMemcpyHostToDevice));
   for (smpc::PmdArgs& p : ctx->pmd) p.bonds = ctx->d_bonds;
+  if (ctx->d_pamphi) {  // solvophobic flags (vel.w bit 0) for the periodic force loop
+    std::vector<uint8_t> am(M);
+    for (size_t i = 0; i < M; ++i) am[i] = static_cast<uint8_t>(static_cast<int>(ctx->h_flags[i]) & 1);
+    CU(cudaMemcpy(ctx->d_pamphi, am.data(), M, cudaMemcpyHostToDevice));
+  }
   return SMPC_OK;
 }
 
@@ -623,6 +622,8 @@ void free_all(smpc_ctx* ctx) {
   ctx->pmd.clear();
   if (ctx->d_upos) cudaFree(ctx->d_upos);
   if (ctx->d_uvel) cudaFree(ctx->d_uvel);
+  if (ctx->d_mnext) cudaFree(ctx->d_mnext);
+  if (ctx->d_pamphi) cudaFree(ctx->d_pamphi);
   void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
@@ -760,26 +761,39 @@ int create_periodic_md(smpc_ctx* ctx) {
     }
     a.n_blocks = smpc::pmd_block_count(a.n);
     const size_t cells = static_cast<size_t>(a.ncell);
-    void *cnt = nullptr, *items = nullptr, *flag = nullptr, *db = nullptr, *ep = nullptr;
-    CU(cudaMalloc(&cnt, cells * sizeof(uint32_t)));
-    ctx->pmd_mem.push_back(cnt);
-    CU(cudaMalloc(&items, cells * smpc::PMD_CELL_CAP * sizeof(int)));
-    ctx->pmd_mem.push_back(items);
-    CU(cudaMalloc(&flag, sizeof(int)));
+    void *flag = nullptr, *db = nullptr, *ep = nullptr, *slot = nullptr;
+    for (int s = 0; s < 2; ++s) {  // grids of even and odd substeps
+      void *cnt = nullptr, *items = nullptr;
+      CU(cudaMalloc(&cnt, cells * sizeof(uint32_t)));
+      ctx->pmd_mem.push_back(cnt);
+      CU(cudaMalloc(&items, cells * smpc::PMD_CELL_CAP * sizeof(int)));
+      ctx->pmd_mem.push_back(items);
+      CU(cudaMemset(cnt, 0, cells * sizeof(uint32_t)));
+      a.cnt[s] = static_cast<uint32_t*>(cnt);
+      a.items[s] = static_cast<int*>(items);
+    }
+    CU(cudaMalloc(&flag, 4 * sizeof(int)));
     ctx->pmd_mem.push_back(flag);
     CU(cudaMalloc(&db, sizeof(double)));
     ctx->pmd_mem.push_back(db);
-    CU(cudaMalloc(&ep, static_cast<size_t>(a.n_blocks) * sizeof(double)));
+    // per block of k_pmd_forces, whose lanes per bead depend on the precision
+    const int force_blocks = std::max(smpc::pmd_force_block_count<float>(a.n),
+                                      smpc::pmd_force_block_count<double>(a.n));
+    CU(cudaMalloc(&ep, static_cast<size_t>(force_blocks) * sizeof(double)));
     ctx->pmd_mem.push_back(ep);
-    CU(cudaMemset(cnt, 0, cells * sizeof(uint32_t)));
-    CU(cudaMemset(flag, 0, sizeof(int)));
+    CU(cudaMalloc(&slot, 4 * sizeof(double)));
+    ctx->pmd_mem.push_back(slot);
+    CU(cudaMemset(slot, 0, 4 * sizeof(double)));
+    void* rows = nullptr;  // the box's Verlet lists, one row of max_nb per bead
+    CU(cudaMalloc(&rows, static_cast<size_t>(a.n) * ctx->max_nb * sizeof(int)));
+    ctx->pmd_mem.push_back(rows);
+    CU(cudaMemset(flag, 0, 4 * sizeof(int)));
     CU(cudaMemset(db, 0, sizeof(double)));
-    a.cnt = static_cast<uint32_t*>(cnt);
-    a.items = static_cast<int*>(items);
     a.flag = static_cast<int*>(flag);
     a.delrx_build = static_cast<double*>(db);
     a.epot_part = static_cast<double*>(ep);
-    a.nlist = ctx->d_nlist;
+    a.dl_slot = static_cast<double*>(slot);
+    a.nlist = static_cast<int*>(rows);
     a.ncount = ctx->d_ncount;
     a.n_mono_total = static_cast<int>(M);
     a.max_nb = ctx->max_nb;
@@ -789,8 +803,12 @@ int create_periodic_md(smpc_ctx* ctx) {
     ctx->pmd.push_back(a);
   }
   if (!ctx->pmd.empty()) {
+    CU(cudaMalloc(&ctx->d_pamphi, M));
+    CU(cudaMemset(ctx->d_pamphi, 0, M));
+    for (smpc::PmdArgs& p : ctx->pmd) p.amphi = ctx->d_pamphi;
     CU(cudaMalloc(&ctx->d_upos, 4 * M * ctx->real_size));
     CU(cudaMalloc(&ctx->d_uvel, 4 * M * ctx->real_size));
+    CU(cudaMalloc(&ctx->d_mnext, 4 * M * ctx->real_size));
   }
   return SMPC_OK;
 }
@@ -850,6 +868,8 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
     ri.mol0_size = periodic ? 0 : d.mol0_size;  // no recentring in a periodic box
     ri.flags = periodic ? smpc::REP_PERIODIC_MD : 0;
     if (!periodic && d.n_mono > 0) ctx->any_local_md = true;
+    if (ri.mol0_size == 0)
+      ctx->mono_chunks = std::max(ctx->mono_chunks, std::min(1024, (d.n_mono + 1023) / 1024));
     ri.shear = d.shear;
     ri.kT = d.kT;
     ri.h = d.h;
@@ -1332,7 +1352,7 @@ int smpc_time_cycles(smpc_ctx* ctx, int n, double* total_ms) {
   return SMPC_OK;
 }
 
-int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int reference_velocities) {
+int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int flags) {
   if (int rc = check_rep(ctx, rep)) return rc;
   cudaSetDevice(ctx->device);
   const RepInfo& ri = ctx->reps[rep];
@@ -1340,11 +1360,11 @@ int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int reference_veloc
   if (ctx->opt.precision == SMPC_FP64)
     smpc::launch_init_solvent<double>(ctx->d_reps, rep, ri.slot_cap,
                                       static_cast<double*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
-                                      reference_velocities, ctx->st);
+                                      flags, ctx->st);
   else
     smpc::launch_init_solvent<float>(ctx->d_reps, rep, ri.slot_cap,
                                      static_cast<float*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
-                                     reference_velocities, ctx->st);
+                                     flags, ctx->st);
   CU(cudaGetLastError());
   return SMPC_OK;
 }

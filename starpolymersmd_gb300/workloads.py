@@ -8,11 +8,17 @@ Named by what they are:
                    log-uniform in [1e-3, 0.5], seeds 1..256 (system.batched_replica_table)
   single_star_20   one star f=6, N_arm=20, 20^3 cells (80k solvent), the
                    CPU-runnable case
+  semidilute_100   64 stars f=8, N_arm=40 (20,544 beads) on a randomised
+                   lattice in one periodic 100^3 box (10M solvent), shear 0.1
+  large_box_200    16 stars f=12, N_arm=30 (5,776 beads) in one periodic
+                   200^3 box (80M solvent), shear 0.05
 All use h = 0.1, MD dt = 0.01 (10 substeps per collision), kT = 1, solvent
 mass 1 and the 12-6 pair preset (WCA core, LJ attraction to 2.5 between
 solvophobic beads) with Verlet skin 0.3. Solvent initial states are drawn on
 the device (uniform positions, Maxwell-Boltzmann velocities); stars are
-self-avoiding walks from the box centre.
+self-avoiding walks from the box centre; in the two star solutions they
+interact through the Lees-Edwards minimum image (periodic MD), 50%
+solvophobic, and solvent and beads start in the steady linear shear flow.
 """
 from __future__ import annotations
 
@@ -96,6 +102,63 @@ def build(specs: Sequence[system.ReplicaSpec], precision=capi.FP32, rng_mode=cap
     return Built(ctx, list(specs), stars, [d["n_fluid"] for d in descs], [st.n for st in stars])
 
 
+def solution_desc(spec: system.ReplicaSpec, sol: system.StarSolution) -> dict:
+    L = spec.L
+    return dict(L=(L, L, L), n_fluid=spec.n_c * L ** 3, n_mono=sol.n, mol0_size=sol.stars[0].n,
+                kT=spec.kT, shear=spec.shear, h=H, md_dt=MD_DT, seed=spec.seed,
+                potential=capi.POT_LJ126, r_cut=R_CUT_LJ, r_verlet=R_CUT_LJ + SKIN,
+                flags=capi.REPLICA_PERIODIC_MD, **{"lambda": 1.0})
+
+
+def make_solution(spec: system.ReplicaSpec) -> system.StarSolution:
+    return system.star_solution(spec.n_stars, spec.arms, spec.n_arm, spec.solvophobic_fraction,
+                                spec.mono_mass, spec.kT, (spec.L,) * 3,
+                                np.random.default_rng(3000 + spec.seed), bond=0.97,
+                                outward_bias=0.15)
+
+
+def build_solution(spec: system.ReplicaSpec, precision=capi.FP32, rng_mode=capi.RNG_PHILOX,
+                   delrx_mode=capi.DELRX_PHYSICAL) -> Built:
+    """One periodic box holding ``spec.n_stars`` interacting stars."""
+    sol = make_solution(spec)
+    desc = solution_desc(spec, sol)
+    ctx = capi.Context([desc], precision=precision, rng=rng_mode, mono_bin=capi.MONOBIN_WRAPPED,
+                       delrx_mode=delrx_mode, step_update=N_SUB, max_neighbors=MAX_NB,
+                       strict_cells=0)
+    # start in the steady shear flow a long run reaches (v_x += shear * y for
+    # solvent and beads), not from rest
+    ctx.init_solvent(0, seed=spec.seed, shear_profile=True)
+    vel = sol.vel.copy()
+    vel[:, 0] += spec.shear * sol.pos[:, 1]
+    ctx.set_monomers(0, sol.pos, vel, np.zeros_like(sol.pos), sol.mass, sol.amphi, sol.anchor)
+    ctx.set_bonds(0, sol.bond_src, sol.bond_dst)
+    ctx.set_molecules(0, sol.mol_start)
+    ctx.init_md()
+    ctx.synchronize()
+    return Built(ctx, [spec], sol.stars, [desc["n_fluid"]], [sol.n])
+
+
+def semidilute_spec(shear=0.1) -> system.ReplicaSpec:
+    return system.ReplicaSpec(L=100, arms=8, n_arm=40, solvophobic_fraction=0.5, shear=shear,
+                              seed=1, n_stars=64)
+
+
+def large_box_spec(shear=0.05) -> system.ReplicaSpec:
+    return system.ReplicaSpec(L=200, arms=12, n_arm=30, solvophobic_fraction=0.5, shear=shear,
+                              seed=1, n_stars=16)
+
+
+def semidilute_100(precision=capi.FP32, shear=0.1, **kw) -> Built:
+    return build_solution(semidilute_spec(shear), precision=precision, **kw)
+
+
+def large_box_200(precision=capi.FP32, shear=0.05, **kw) -> Built:
+    return build_solution(large_box_spec(shear), precision=precision, **kw)
+
+
+SOLUTIONS = ("semidilute_100", "large_box_200")
+
+
 def single_star_50(precision=capi.FP32, shear=0.05, **kw) -> Built:
     spec = system.ReplicaSpec(L=50, arms=10, n_arm=40, solvophobic_fraction=0.5, shear=shear,
                               seed=1)
@@ -114,4 +177,5 @@ def batched_256(precision=capi.FP32, n=256, **kw) -> Built:
 
 
 WORKLOADS = {"batched_256": batched_256, "single_star_50": single_star_50,
-             "single_star_20": single_star_20}
+             "single_star_20": single_star_20, "semidilute_100": semidilute_100,
+             "large_box_200": large_box_200}

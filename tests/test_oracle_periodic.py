@@ -118,3 +118,15 @@ def test_star_solution_is_self_avoiding_across_images():
     ms = sol.mol_start
     mol = np.searchsorted(ms, np.arange(sol.n), side="right") - 1
     np.testing.assert_array_equal(mol[sol.bond_src], mol[sol.bond_dst])
+
+
+@pytest.mark.parametrize("shear", [0.0, 1.5])
+def test_periodic_grid_partners_match_all_pairs(shear):
+    # the cell-grid partner search of large boxes gives the loop over all
+    # monomers to the last bit, Lees-Edwards rows included
+    sol, o = _solution_oracle(shear, 0.002, L=12, seed=6)
+    for t in range(1, 301):
+        o.propagate(False)
+        o.mpc_step(t, 0.1)
+    assert o.delrx != 0.0 or shear == 0.0
+    np.testing.assert_array_equal(o.periodic_forces(True), o.periodic_forces(False))
