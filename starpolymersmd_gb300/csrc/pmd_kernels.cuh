@@ -127,15 +127,26 @@ __device__ __forceinline__ PmdBox<R> pmd_box(const RepInfo& ri, double dl) {
   return b;
 }
 
-// Lees-Edwards minimum image of d = x_j - x_i (MPC::relative_position)
-template <typename R>
-__device__ __forceinline__ void pmd_min_image(R& dx, R& dy, R& dz, const PmdBox<R>& b) {
-  const R cy = r_round(pmd_ratio(dy, b.L[1], b.inv[1]));
-  dx -= b.L[0] * r_round(pmd_ratio(dx, b.L[0], b.inv[0]));
+// Lees-Edwards minimum image of d = x_j - x_i: FP64 with the operations of
+// MPC::relative_position (MPC.cpp:456-465); FP32 with one wrap of x after the
+// shift and rint (the same image, away from exact half-box separations,
+// which no Verlet pair has)
+__device__ __forceinline__ void pmd_min_image(double& dx, double& dy, double& dz,
+                                              const PmdBox<double>& b) {
+  const double cy = round(dy / b.L[1]);
+  dx -= b.L[0] * round(dx / b.L[0]);
   dx -= cy * b.delrx;
-  dx -= b.L[0] * r_round(pmd_ratio(dx, b.L[0], b.inv[0]));
+  dx -= b.L[0] * round(dx / b.L[0]);
   dy -= b.L[1] * cy;
-  dz -= b.L[2] * r_round(pmd_ratio(dz, b.L[2], b.inv[2]));
+  dz -= b.L[2] * round(dz / b.L[2]);
+}
+__device__ __forceinline__ void pmd_min_image(float& dx, float& dy, float& dz,
+                                              const PmdBox<float>& b) {
+  const float cy = rintf(dy * b.inv[1]);
+  dx -= cy * b.delrx;
+  dx -= b.L[0] * rintf(dx * b.inv[0]);
+  dy -= b.L[1] * cy;
+  dz -= b.L[2] * rintf(dz * b.inv[2]);
 }
 
 template <typename R>
