@@ -175,6 +175,7 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
             mvel = st.vel.copy()
             mvel[:, 0] += spec.shear * st.pos[:, 1]
         o.set_fluid(fpos, fvel)
+        n_f = len(fpos)
         del fpos, fvel
         o.set_monomers(st.pos, mvel, np.zeros_like(st.pos), mass, st.amphi, st.anchor)
         o.set_bonds(st.bond_src, st.bond_dst)
@@ -182,7 +183,7 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
             o.set_periodic_md(W.H)
         o.init_md()
         o.set_philox(spec.seed, 0)
-        return o, len(fpos) + st.n
+        return o, n_f + st.n
 
     systems = [make(s) for s in pick]
 

@@ -239,6 +239,25 @@ int smpc_verlet_rebuilds(smpc_ctx* ctx, int rep, int* out);
 int smpc_error_word(smpc_ctx* ctx, unsigned* word, unsigned* info3);
 int smpc_synchronize(smpc_ctx* ctx);
 
+/* Checkpoint / restart. Replaces the reference's restart files -- the fluid
+ * as "%f" text (MPC::print_fluid_complete, MPC.cpp:570-579, read back by
+ * MPC::initialize(filename, Box_old), MPC.cpp:57-113) and the stars as PDB
+ * with velocities at %7.3f (Box::print_PDB_with_velocity, Box.cpp:563-602,
+ * read back by Molecule::star_from_file, Molecule.cpp:178-224), after which
+ * the reference re-seeds its random stream. A checkpoint here holds the
+ * context's full state at its own precision: solvent records, monomer state
+ * with forces and Verlet lists, every replica's delrx and Philox collision
+ * counter, bonds, molecules and the periodic-MD bookkeeping. Loading it into
+ * a context created with the same replicas and options continues the run bit
+ * for bit. Call between steps (not between smpc_mpc_bin and
+ * smpc_mpc_collide). A load that fails validation (other replicas, options or
+ * format) leaves the context unchanged; a truncated stream leaves it undefined. */
+int smpc_checkpoint_size(smpc_ctx* ctx, uint64_t* bytes);
+int smpc_checkpoint_save(smpc_ctx* ctx, void* buf, uint64_t capacity);
+int smpc_checkpoint_load(smpc_ctx* ctx, const void* buf, uint64_t length);
+int smpc_checkpoint_write(smpc_ctx* ctx, const char* path);
+int smpc_checkpoint_read(smpc_ctx* ctx, const char* path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -269,6 +269,15 @@ class RefSystem:
             getattr(lib, name).restype = rt
         lib.ref_get_bonds.argtypes = [P, P, P]
         lib.ref_get_bonds.restype = C.c_int
+        for name, args in {"ref_print_fluid_complete": [P, C.c_char_p],
+                           "ref_print_pdb_with_velocity": [P, C.c_char_p, C.c_int]}.items():
+            getattr(lib, name).argtypes = args
+            getattr(lib, name).restype = C.c_int
+        lib.ref_mpc_initialize_from_file.argtypes = [P, C.c_char_p, C.c_int, C.c_int, C.c_int]
+        lib.ref_mpc_initialize_from_file.restype = None
+        lib.ref_star_from_file.argtypes = [P, C.c_int, C.c_char_p, C.c_uint, C.c_uint, C.c_uint,
+                                           C.c_int]
+        lib.ref_star_from_file.restype = None
         lib.rand_tape_size.argtypes = []
         lib.rand_tape_size.restype = C.c_long
         self.lib = lib
@@ -297,6 +306,21 @@ class RefSystem:
 
     def add_star(self, A, B, arms, mass):
         self.lib.ref_add_star(self.h, A, B, arms, mass)
+
+    # the reference's restart files, through its own writers and readers
+    def print_fluid_complete(self, path):
+        if self.lib.ref_print_fluid_complete(self.h, os.fsencode(path)):
+            raise OSError(path)
+
+    def initialize_fluid_from_file(self, path, L_old):
+        self.lib.ref_mpc_initialize_from_file(self.h, os.fsencode(path), *[int(x) for x in L_old])
+
+    def print_pdb_with_velocity(self, path, step):
+        if self.lib.ref_print_pdb_with_velocity(self.h, os.fsencode(path), int(step)):
+            raise OSError(path)
+
+    def star_from_file(self, mol, path, A, B, arms, set_zero=False):
+        self.lib.ref_star_from_file(self.h, int(mol), os.fsencode(path), A, B, arms, int(set_zero))
 
     def make_thermostat(self, dt):
         self.lib.ref_make_thermostat(self.h, dt)

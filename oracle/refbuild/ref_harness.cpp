@@ -5,7 +5,9 @@
 // star-polymers/src/star-polymers.cpp:352-404 do, run the driver loop body
 // (star-polymers.cpp:466,530,534: propagate, then MPC::step), and read or
 // overwrite the state, the cell occupancies and the recorded random draws.
+#include <array>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -278,6 +280,36 @@ void ref_run(RefSys* s, long t0, long n, double mpc_dt, int with_md) {
     if (with_md) s->thermo->propagate(false);
     s->mpc->step(t, mpc_dt);
   }
+}
+
+// The reference's restart files, written and read by its own code:
+// MPC::print_fluid_complete (MPC.cpp:570-579), MPC::initialize(filename,
+// Box_old) (MPC.cpp:57-113), Box::print_PDB_with_velocity (Box.cpp:563-602)
+// and Molecule::star_from_file (Molecule.cpp:178-224) on molecule `mol`.
+int ref_print_fluid_complete(RefSys* s, const char* path) {
+  FILE* f = std::fopen(path, "w");
+  if (!f) return 1;
+  s->mpc->print_fluid_complete(f);
+  std::fclose(f);
+  return 0;
+}
+
+void ref_mpc_initialize_from_file(RefSys* s, const char* path, int Lx_old, int Ly_old,
+                                  int Lz_old) {
+  s->mpc->initialize(path, std::array<int, 3>{Lx_old, Ly_old, Lz_old});
+}
+
+int ref_print_pdb_with_velocity(RefSys* s, const char* path, int step) {
+  FILE* f = std::fopen(path, "w");
+  if (!f) return 1;
+  s->box->print_PDB_with_velocity(f, step);
+  std::fclose(f);
+  return 0;
+}
+
+void ref_star_from_file(RefSys* s, int mol, const char* path, unsigned A, unsigned B,
+                        unsigned arms, int set_zero) {
+  s->box->Molecules[mol].star_from_file(path, A, B, arms, set_zero != 0);
 }
 
 // Reports which draw of "Vector3d(f() - 0.5, f() - 0.5, f() - 0.5)" lands in

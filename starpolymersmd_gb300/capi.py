@@ -37,7 +37,9 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_set_monomer_state_all",
            "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
            "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide", "smpc_set_molecules",
-           "smpc_molecule_observables_all", "smpc_velocity_profile")
+           "smpc_molecule_observables_all", "smpc_velocity_profile", "smpc_checkpoint_size",
+           "smpc_checkpoint_save", "smpc_checkpoint_load", "smpc_checkpoint_write",
+           "smpc_checkpoint_read")
 
 PHASES = ("md_substeps", "cycle_begin", "mono_prep", "fluid_bin", "scan", "build_perm",
           "collide", "cycle_end")
@@ -128,6 +130,11 @@ def load(path: Optional[str] = None):
         "smpc_set_molecules": ([P, I, I, P], I),
         "smpc_molecule_observables_all": ([P, P], I),
         "smpc_velocity_profile": ([P, I, D, P, I, P, I], I),
+        "smpc_checkpoint_size": ([P, C.POINTER(C.c_uint64)], I),
+        "smpc_checkpoint_save": ([P, P, C.c_uint64], I),
+        "smpc_checkpoint_load": ([P, P, C.c_uint64], I),
+        "smpc_checkpoint_write": ([P, C.c_char_p], I),
+        "smpc_checkpoint_read": ([P, C.c_char_p], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -386,6 +393,24 @@ class Context:
         mc = np.zeros(self.replicas[rep].get("n_mono", 0), dtype=np.int32)
         self._check(self.lib.smpc_cell_members(self.h, rep, _p(fc), _p(mc)), "cell_members")
         return fc, mc
+
+    def checkpoint(self) -> bytes:
+        """The context's full state (smpc_checkpoint_save)."""
+        n = C.c_uint64()
+        self._check(self.lib.smpc_checkpoint_size(self.h, C.byref(n)), "checkpoint_size")
+        buf = np.empty(n.value, dtype=np.uint8)
+        self._check(self.lib.smpc_checkpoint_save(self.h, _p(buf), n.value), "checkpoint_save")
+        return buf.tobytes()
+
+    def restore(self, blob: bytes):
+        buf = np.frombuffer(blob, dtype=np.uint8)
+        self._check(self.lib.smpc_checkpoint_load(self.h, _p(buf), len(buf)), "checkpoint_load")
+
+    def checkpoint_write(self, path: str):
+        self._check(self.lib.smpc_checkpoint_write(self.h, os.fsencode(path)), "checkpoint_write")
+
+    def checkpoint_read(self, path: str):
+        self._check(self.lib.smpc_checkpoint_read(self.h, os.fsencode(path)), "checkpoint_read")
 
     def set_collision_counter(self, c):
         self._check(self.lib.smpc_set_collision_counter(self.h, c), "set_collision_counter")

@@ -1654,3 +1654,345 @@ int smpc_synchronize(smpc_ctx* ctx) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------- checkpoints
+// One blob holds everything a context needs to continue a run exactly where it
+// was saved: the host mirror and device copy of every replica's dynamic record
+// (delrx, grid shift, Philox collision counter, rebuild counter, ...), the
+// solvent records in their cell order, the monomer state with its forces,
+// Verlet lists and their references, the last collision's cell lists (for
+// the observables), bonds, molecules, and the periodic-MD bookkeeping. Every
+// section is the context's own bytes (FP32 or FP64), so a restored context
+// continues bit for bit. The reference writes lossy text (%f, %7.3f) and draws
+// a new random stream on restart (MPC.cpp:57-113, 570-579; Box.cpp:563-602).
+namespace {
+
+constexpr char kCkptMagic[8] = {'S', 'M', 'P', 'C', 'C', 'K', 'P', '1'};
+constexpr uint32_t kCkptVersion = 1;
+
+struct CkptHeader {
+  char magic[8];
+  uint32_t version;
+  uint32_t precision;
+  uint32_t n_rep;
+  uint32_t step_update;
+  uint32_t mono_bin;
+  uint32_t delrx_mode;
+  uint32_t strict;
+  uint32_t max_nb;
+  uint32_t cur;
+  uint32_t collided;
+  uint64_t total_slots;
+  uint64_t total_mono;
+  uint64_t total_cells;
+  uint64_t n_pmd;
+};
+
+// Byte stream to a buffer, a file, or nowhere (size count).
+struct CkptIo {
+  unsigned char* buf = nullptr;      // save into memory
+  const unsigned char* in = nullptr; // load from memory
+  uint64_t cap = 0;
+  uint64_t pos = 0;
+  FILE* f = nullptr;
+  bool ok = true;
+};
+
+void ck_put(CkptIo& io, const void* p, uint64_t n) {
+  if (!io.ok || n == 0) {
+    io.pos += io.ok ? n : 0;
+    return;
+  }
+  if (io.f) {
+    io.ok = std::fwrite(p, 1, n, io.f) == n;
+  } else if (io.buf) {
+    if (io.pos + n > io.cap) {
+      io.ok = false;
+      return;
+    }
+    std::memcpy(io.buf + io.pos, p, n);
+  }
+  io.pos += n;
+}
+
+void ck_get(CkptIo& io, void* p, uint64_t n) {
+  if (!io.ok || n == 0) return;
+  if (io.f) {
+    io.ok = std::fread(p, 1, n, io.f) == n;
+  } else {
+    if (io.pos + n > io.cap) {
+      io.ok = false;
+      return;
+    }
+    std::memcpy(p, io.in + io.pos, n);
+  }
+  io.pos += n;
+}
+
+// device bytes through a bounded host staging buffer
+constexpr uint64_t kCkptChunk = 64ull << 20;
+
+int ck_put_dev(smpc_ctx* ctx, CkptIo& io, const void* d, uint64_t n) {
+  if (!io.ok || n == 0 || (!io.f && !io.buf)) {
+    io.pos += io.ok ? n : 0;
+    return SMPC_OK;
+  }
+  if (io.buf) {  // straight into the caller's buffer
+    if (io.pos + n > io.cap) {
+      io.ok = false;
+      return SMPC_OK;
+    }
+    CU(cudaMemcpy(io.buf + io.pos, d, n, cudaMemcpyDeviceToHost));
+    io.pos += n;
+    return SMPC_OK;
+  }
+  std::vector<unsigned char> stage(std::min(n, kCkptChunk));
+  for (uint64_t o = 0; o < n; o += kCkptChunk) {
+    const uint64_t k = std::min(kCkptChunk, n - o);
+    CU(cudaMemcpy(stage.data(), static_cast<const unsigned char*>(d) + o, k, cudaMemcpyDeviceToHost));
+    ck_put(io, stage.data(), k);
+  }
+  return SMPC_OK;
+}
+
+int ck_get_dev(smpc_ctx* ctx, CkptIo& io, void* d, uint64_t n) {
+  if (!io.ok || n == 0) return SMPC_OK;
+  if (!io.f) {
+    if (io.pos + n > io.cap) {
+      io.ok = false;
+      return SMPC_OK;
+    }
+    CU(cudaMemcpy(d, io.in + io.pos, n, cudaMemcpyHostToDevice));
+    io.pos += n;
+    return SMPC_OK;
+  }
+  std::vector<unsigned char> stage(std::min(n, kCkptChunk));
+  for (uint64_t o = 0; o < n && io.ok; o += kCkptChunk) {
+    const uint64_t k = std::min(kCkptChunk, n - o);
+    ck_get(io, stage.data(), k);
+    if (io.ok) CU(cudaMemcpy(static_cast<unsigned char*>(d) + o, stage.data(), k, cudaMemcpyHostToDevice));
+  }
+  return SMPC_OK;
+}
+
+template <typename T>
+void ck_put_vec(CkptIo& io, const std::vector<T>& v) {
+  const uint64_t n = v.size();
+  ck_put(io, &n, sizeof n);
+  ck_put(io, v.data(), n * sizeof(T));
+}
+
+template <typename T>
+void ck_get_vec(CkptIo& io, std::vector<T>& v, uint64_t limit) {
+  uint64_t n = 0;
+  ck_get(io, &n, sizeof n);
+  if (!io.ok || n > limit) {
+    io.ok = false;
+    return;
+  }
+  v.resize(n);
+  ck_get(io, v.data(), n * sizeof(T));
+}
+
+CkptHeader ck_header(const smpc_ctx* ctx) {
+  CkptHeader h{};
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = kCkptVersion;
+  h.precision = static_cast<uint32_t>(ctx->opt.precision);
+  h.n_rep = static_cast<uint32_t>(ctx->n_rep);
+  h.step_update = static_cast<uint32_t>(ctx->opt.step_update);
+  h.mono_bin = static_cast<uint32_t>(ctx->opt.mono_bin);
+  h.delrx_mode = static_cast<uint32_t>(ctx->opt.delrx_mode);
+  h.strict = static_cast<uint32_t>(ctx->opt.strict_cells);
+  h.max_nb = static_cast<uint32_t>(ctx->max_nb);
+  h.cur = static_cast<uint32_t>(ctx->cur);
+  h.collided = ctx->collided ? 1u : 0u;
+  h.total_slots = static_cast<uint64_t>(ctx->total_slots);
+  h.total_mono = static_cast<uint64_t>(ctx->total_mono);
+  h.total_cells = static_cast<uint64_t>(ctx->total_cells);
+  h.n_pmd = ctx->pmd.size();
+  return h;
+}
+
+// The device arrays of a checkpoint, in order, with their sizes.
+struct CkptArray {
+  void* d;
+  uint64_t bytes;
+};
+
+std::vector<CkptArray> ck_arrays(smpc_ctx* ctx) {
+  const uint64_t S = static_cast<uint64_t>(ctx->total_slots), M = static_cast<uint64_t>(ctx->total_mono),
+                 C = static_cast<uint64_t>(ctx->total_cells), rs = ctx->real_size;
+  std::vector<CkptArray> a = {
+      {ctx->d_dyn, ctx->n_rep * sizeof(RepDyn)},
+      {ctx->d_rec[ctx->cur], 8 * S * rs},
+      {ctx->d_mpos, 4 * M * rs},
+      {ctx->d_mvel, 4 * M * rs},
+      {ctx->d_mfrc, 4 * M * rs},
+      {ctx->d_mver, 4 * M * rs},
+      {ctx->d_nlist, static_cast<uint64_t>(ctx->max_nb) * M * sizeof(int)},
+      {ctx->d_ncount, M * sizeof(int)},
+      {ctx->d_off, (C + 1) * sizeof(uint32_t)},
+      {ctx->d_perm, (S + M) * sizeof(uint32_t)},
+      {ctx->d_mkey, M * sizeof(uint2)},
+      {ctx->d_mimg, M * sizeof(int)},
+  };
+  for (const smpc::PmdArgs& p : ctx->pmd) {
+    a.push_back({p.flag, 4 * sizeof(int)});
+    a.push_back({p.delrx_build, sizeof(double)});
+    a.push_back({p.dl_slot, 4 * sizeof(double)});
+    a.push_back({p.nlist, static_cast<uint64_t>(p.n) * ctx->max_nb * sizeof(int)});
+  }
+  return a;
+}
+
+int ck_save(smpc_ctx* ctx, CkptIo& io) {
+  if (ctx->binned) return fail(ctx, SMPC_E_STATE, "a collision is binned but not collided");
+  CU(cudaStreamSynchronize(ctx->st));
+  const CkptHeader h = ck_header(ctx);
+  ck_put(io, &h, sizeof h);
+  ck_put(io, ctx->reps.data(), ctx->n_rep * sizeof(RepInfo));
+  ck_put(io, ctx->dyn.data(), ctx->n_rep * sizeof(RepDyn));
+  ck_put(io, ctx->sorted.data(), ctx->sorted.size());
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    ck_put_vec(io, ctx->bsrc[r]);
+    ck_put_vec(io, ctx->bdst[r]);
+    ck_put_vec(io, ctx->anchor[r]);
+    ck_put_vec(io, ctx->mol_start[r]);
+  }
+  ck_put_vec(io, ctx->h_mass);
+  ck_put_vec(io, ctx->h_flags);
+  const uint8_t md = ctx->md_ready ? 1 : 0;
+  ck_put(io, &md, 1);
+  for (const CkptArray& a : ck_arrays(ctx))
+    if (int rc = ck_put_dev(ctx, io, a.d, a.bytes)) return rc;
+  if (!io.ok) return fail(ctx, SMPC_E_ARG, "checkpoint buffer too small or write failed");
+  return SMPC_OK;
+}
+
+int ck_load(smpc_ctx* ctx, CkptIo& io) {
+  if (ctx->binned) return fail(ctx, SMPC_E_STATE, "a collision is binned but not collided");
+  CU(cudaStreamSynchronize(ctx->st));
+  CkptHeader h{};
+  ck_get(io, &h, sizeof h);
+  if (!io.ok || std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != kCkptVersion)
+    return fail(ctx, SMPC_E_ARG, "not a checkpoint of this format");
+  CkptHeader mine = ck_header(ctx);
+  mine.cur = h.cur;
+  mine.collided = h.collided;
+  if (std::memcmp(&h, &mine, sizeof h) != 0 || h.cur > 1)
+    return fail(ctx, SMPC_E_ARG, "checkpoint of a context with other replicas or options");
+  std::vector<RepInfo> reps(ctx->n_rep);
+  ck_get(io, reps.data(), reps.size() * sizeof(RepInfo));
+  if (!io.ok || std::memcmp(reps.data(), ctx->reps.data(), reps.size() * sizeof(RepInfo)) != 0)
+    return fail(ctx, SMPC_E_ARG, "checkpoint of a context with other replicas");
+  std::vector<RepDyn> dyn(ctx->n_rep);
+  std::vector<uint8_t> sorted(ctx->n_rep);
+  ck_get(io, dyn.data(), dyn.size() * sizeof(RepDyn));
+  ck_get(io, sorted.data(), sorted.size());
+  std::vector<std::vector<int>> bsrc(ctx->n_rep), bdst(ctx->n_rep), anchor(ctx->n_rep),
+      mol(ctx->n_rep);
+  const uint64_t M = static_cast<uint64_t>(ctx->total_mono);
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    const uint64_t n = static_cast<uint64_t>(ctx->reps[r].n_mono);
+    ck_get_vec(io, bsrc[r], 4 * n + 16);
+    ck_get_vec(io, bdst[r], 4 * n + 16);
+    ck_get_vec(io, anchor[r], n);
+    ck_get_vec(io, mol[r], n + 1);
+    for (size_t k = 0; io.ok && k < bsrc[r].size(); ++k)
+      if (k >= bdst[r].size() || bsrc[r][k] < 0 || static_cast<uint64_t>(bsrc[r][k]) >= n ||
+          bdst[r][k] < 0 || static_cast<uint64_t>(bdst[r][k]) >= n)
+        io.ok = false;
+    if (io.ok && (mol[r].empty() || mol[r].front() != 0 ||
+                  (n > 0 && static_cast<uint64_t>(mol[r].back()) != n)))
+      io.ok = false;
+  }
+  std::vector<double> mass, flags;
+  ck_get_vec(io, mass, M);
+  ck_get_vec(io, flags, M);
+  uint8_t md = 0;
+  ck_get(io, &md, 1);
+  if (!io.ok || mass.size() != M || flags.size() != M)
+    return fail(ctx, SMPC_E_ARG, "truncated or inconsistent checkpoint");
+  // from here the context's state is replaced
+  for (int k = 0; k < 2; ++k)
+    if (ctx->graph[k]) {
+      cudaGraphExecDestroy(ctx->graph[k]);
+      ctx->graph[k] = nullptr;
+    }
+  ctx->cur = static_cast<int>(h.cur);
+  for (const CkptArray& a : ck_arrays(ctx))
+    if (int rc = ck_get_dev(ctx, io, a.d, a.bytes)) return rc;
+  if (!io.ok) return fail(ctx, SMPC_E_ARG, "truncated checkpoint (context state undefined)");
+  ctx->collided = h.collided != 0;
+  ctx->binned = false;
+  ctx->dyn = dyn;
+  ctx->sorted = sorted;
+  ctx->bsrc = bsrc;
+  ctx->bdst = bdst;
+  ctx->anchor = anchor;
+  ctx->mol_start = mol;
+  ctx->h_mass = mass;
+  ctx->h_flags = flags;
+  if (int rc = upload_molecules(ctx)) return rc;
+  if (int rc = upload_bonds(ctx)) return rc;
+  ctx->md_ready = md != 0;
+  return SMPC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int smpc_checkpoint_size(smpc_ctx* ctx, uint64_t* bytes) {
+  if (!ctx || !bytes) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  CkptIo io;  // counts only
+  if (int rc = ck_save(ctx, io)) return rc;
+  *bytes = io.pos;
+  return SMPC_OK;
+}
+
+int smpc_checkpoint_save(smpc_ctx* ctx, void* buf, uint64_t cap) {
+  if (!ctx || !buf) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  CkptIo io;
+  io.buf = static_cast<unsigned char*>(buf);
+  io.cap = cap;
+  return ck_save(ctx, io);
+}
+
+int smpc_checkpoint_load(smpc_ctx* ctx, const void* buf, uint64_t len) {
+  if (!ctx || !buf) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  CkptIo io;
+  io.in = static_cast<const unsigned char*>(buf);
+  io.cap = len;
+  return ck_load(ctx, io);
+}
+
+int smpc_checkpoint_write(smpc_ctx* ctx, const char* path) {
+  if (!ctx || !path) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(ctx, SMPC_E_ARG, std::string("cannot open ") + path + " for writing");
+  CkptIo io;
+  io.f = f;
+  int rc = ck_save(ctx, io);
+  if (std::fclose(f) != 0 && rc == SMPC_OK) rc = fail(ctx, SMPC_E_ARG, "checkpoint write failed");
+  return rc;
+}
+
+int smpc_checkpoint_read(smpc_ctx* ctx, const char* path) {
+  if (!ctx || !path) return SMPC_E_ARG;
+  cudaSetDevice(ctx->device);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(ctx, SMPC_E_ARG, std::string("cannot open ") + path);
+  CkptIo io;
+  io.f = f;
+  const int rc = ck_load(ctx, io);
+  std::fclose(f);
+  return rc;
+}
+
+}  // extern "C"

@@ -525,11 +525,10 @@ def test_observables_of_every_replica_match_numpy(precision):
 
 @pytest.mark.parametrize("offset", [0.0, 2.6])
 def test_fp32_graph_cycles_match_stepwise(offset):
-    # FP32 fast path: graph cycles bin the next collision's solvent inside the
-    # collide kernel; cycles issued call by call bin it in the binning pass.
-    # Both give the same state to the last bit. With the star moved next to
-    # the box face, check_bounds recentres it, which the graph path handles by
-    # rebinning that replica.
+    # FP32 fast path: graph cycles (delrx and grid shift advanced on the
+    # device) against the same cycles issued call by call (host delrx): the
+    # same state to the last bit. With the star moved next to the box face,
+    # check_bounds recentres it inside the cycles.
     L, su, h = 10, 10, 0.1
     star, fpos, fvel = H.small_star_system(L=L, shear=0.1, seed=5)
     star.pos[:] += offset
@@ -550,8 +549,8 @@ def test_fp32_graph_cycles_match_stepwise(offset):
         np.testing.assert_array_equal(vb, va)
         for x, y in zip(b.get_monomers(0), a.get_monomers(0)):
             np.testing.assert_array_equal(x, y)
-        # a call-by-call cycle between graph cycles: the keys binned ahead by
-        # the last graph cycle are dropped, the next graph cycle bins again
+        # call-by-call cycles between graph cycles: the host's delrx mirror
+        # and the device state stay in step
         for t in range(4 * su + 1, 6 * su + 1):
             a.md_substeps(1)
             a.mpc_step(t, h)
