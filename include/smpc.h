@@ -85,6 +85,8 @@ typedef struct {
   int max_neighbors;      /* Verlet list capacity per monomer (0: default 192) */
   int strict_cells;       /* 1: reference cell formula + range error; 0: clamp into the box */
   int device;             /* CUDA device ordinal */
+  int angular_momentum;   /* 1: angular-momentum-conserving collision in cells of more than two
+                             particles (MPC.cpp:260-269, 324-374; MPC(..., angular_mom)) */
 } smpc_options;
 
 /* Draws injected for one collision of every replica (reference parity):
@@ -238,6 +240,21 @@ int smpc_verlet_rebuilds(smpc_ctx* ctx, int rep, int* out);
 /* Device error word (0 = clean) and its first offender; clears it. */
 int smpc_error_word(smpc_ctx* ctx, unsigned* word, unsigned* info3);
 int smpc_synchronize(smpc_ctx* ctx);
+
+/* Solvent analyses (the reference's Analysis functors, sums on the device).
+ * smpc_fourier_modes: Fourier_Autocorr::operator() (Fourier_Autocorr.h) for one
+ *   sample: for k = (2 pi / box_length) e_j, j = x, y, z, the transverse mode
+ *   sum_i v_i exp(i k . r_i) / N with its j component removed; out18 =
+ *   3 modes x 3 components x (re, im).
+ * smpc_vacf_*: Vel_Autocorr_Fluid (Vel_Autocorr_Fluid.h) over solvent
+ *   particles 0..n_particles-1 of one replica: a window of `entries`
+ *   velocity samples (one per smpc_vacf_sample); once it is full, every
+ *   sample adds sum_i v_i(oldest) . v_i(oldest + j) to lag_sums[j]. The
+ *   reference's average is lag_sums[j] / calculations / n_particles. */
+int smpc_fourier_modes(smpc_ctx* ctx, int rep, double box_length, double* out18);
+int smpc_vacf_start(smpc_ctx* ctx, int rep, int n_particles, int entries);
+int smpc_vacf_sample(smpc_ctx* ctx);
+int smpc_vacf_result(smpc_ctx* ctx, double* lag_sums, uint64_t* calculations);
 
 /* Checkpoint / restart. Replaces the reference's restart files -- the fluid
  * as "%f" text (MPC::print_fluid_complete, MPC.cpp:570-579, read back by

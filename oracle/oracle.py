@@ -112,13 +112,13 @@ class OracleSystem:
 
     def __init__(self, L, kT, shear, step_update, n_fluid, n_mono=0, mol_start=(0,),
                  lambda_=1.0, md_dt=0.01, r_cut=1.5, r_verlet=2.0, potential=POT_REF4824,
-                 delrx_dt_scale=1.0, mono_wrap=0):
+                 delrx_dt_scale=1.0, mono_wrap=0, angular_momentum=0):
         self.lib = _oracle_lib()
         p = OrcParams()
         for d in range(3):
             p.L[d] = int(L[d])
         p.kT, p.shear, p.step_update = kT, shear, step_update
-        p.angular_momentum = 0
+        p.angular_momentum = int(angular_momentum)
         p.lambda_, p.md_dt, p.r_cut, p.r_verlet = lambda_, md_dt, r_cut, r_verlet
         p.potential, p.delrx_dt_scale = potential, delrx_dt_scale
         p.mono_wrap = int(mono_wrap)

@@ -785,7 +785,101 @@ static void cell_thermostat(smpc_orc* o, unsigned c, const double* cmv) {
   }
 }
 
-/* MPC::collide (MPC.cpp:239-270), angular-momentum variant off. */
+/* Position of a cell member in the collision frame: the solvent's stored
+ * (shifted, wrapped) position; a monomer's shifted position, at its
+ * Lees-Edwards image when monomers are binned wrapped. */
+static void ppos(const smpc_orc* o, long id, double* x) {
+  if (id >= 0) {
+    for (int d = 0; d < 3; ++d) x[d] = o->fx[3 * id + d];
+    return;
+  }
+  const int m = (int)(-id - 1);
+  for (int d = 0; d < 3; ++d) x[d] = o->mx[3 * m + d];
+  if (o->p.mono_wrap) {
+    double dv = 0.0;
+    wrap_particle(o, x, &dv);
+  }
+}
+
+/* x = A^-1 b for symmetric positive-definite A by the Cholesky factor
+ * A = L L^T, column by column, then forward and back substitution. */
+static void llt_solve3(const double A[3][3], const double b[3], double x[3]) {
+  double l[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, y[3];
+  for (int j = 0; j < 3; ++j) {
+    double s = A[j][j];
+    for (int k = 0; k < j; ++k) s -= l[j][k] * l[j][k];
+    l[j][j] = sqrt(s);
+    for (int i = j + 1; i < 3; ++i) {
+      double t = A[i][j];
+      for (int k = 0; k < j; ++k) t -= l[i][k] * l[j][k];
+      l[i][j] = t / l[j][j];
+    }
+  }
+  for (int i = 0; i < 3; ++i) {
+    double s = b[i];
+    for (int k = 0; k < i; ++k) s -= l[i][k] * y[k];
+    y[i] = s / l[i][i];
+  }
+  for (int i = 2; i >= 0; --i) {
+    double s = y[i];
+    for (int k = i + 1; k < 3; ++k) s -= l[k][i] * x[k];
+    x[i] = s / l[i][i];
+  }
+}
+
+/* MPC::calculateCMP and MPC::calculateAngular (MPC.cpp:324-374): the cell's
+ * centre of mass and the angular velocity that restores its angular momentum
+ * after the rotation R, in the reference's operation order. */
+static void cell_angular(smpc_orc* o, unsigned c, const double* cmv, double R[3][3],
+                         double* cmp, double* ang) {
+  double tm = 0.0;
+  cmp[0] = cmp[1] = cmp[2] = 0.0;
+  for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
+    const long id = o->c_mem[k];
+    double x[3];
+    ppos(o, id, x);
+    const double m = pmass(o, id);
+    cmp[0] += x[0] * m;
+    cmp[1] += x[1] * m;
+    cmp[2] += x[2] * m;
+    tm += m;
+  }
+  if (tm > 0) {
+    cmp[0] /= tm;
+    cmp[1] /= tm;
+    cmp[2] /= tm;
+  }
+  double cv[3] = {0, 0, 0}, I[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
+    const long id = o->c_mem[k];
+    double x[3];
+    ppos(o, id, x);
+    const double* v = pvel(o, id);
+    const double m = pmass(o, id);
+    const double q[3] = {x[0] - cmp[0], x[1] - cmp[1], x[2] - cmp[2]};
+    const double u[3] = {v[0] - cmv[0], v[1] - cmv[1], v[2] - cmv[2]};
+    double w[3];
+    for (int i = 0; i < 3; ++i) w[i] = u[i] - ((R[i][0] * u[0] + R[i][1] * u[1]) + R[i][2] * u[2]);
+    const double cr[3] = {q[1] * w[2] - q[2] * w[1], q[2] * w[0] - q[0] * w[2],
+                          q[0] * w[1] - q[1] * w[0]};
+    cv[0] += m * cr[0];
+    cv[1] += m * cr[1];
+    cv[2] += m * cr[2];
+    I[0][0] += m * (q[1] * q[1] + q[2] * q[2]);
+    I[1][1] += m * (q[0] * q[0] + q[2] * q[2]);
+    I[2][2] += m * (q[1] * q[1] + q[0] * q[0]);
+    I[0][1] -= m * q[0] * q[1];
+    I[0][2] -= m * q[0] * q[2];
+    I[1][2] -= m * q[1] * q[2];
+  }
+  I[1][0] = I[0][1];
+  I[2][0] = I[0][2];
+  I[2][1] = I[1][2];
+  llt_solve3(I, cv, ang);
+}
+
+/* MPC::collide (MPC.cpp:239-270), with the angular-momentum correction in
+ * cells of more than two particles when p.angular_momentum is set. */
 static void cell_collide(smpc_orc* o, unsigned c, const double* cmv) {
   double uphi, uth;
   if (o->rng_mode == ORC_RNG_INJECT) {
@@ -811,6 +905,9 @@ static void cell_collide(smpc_orc* o, unsigned c, const double* cmv) {
   R[2][0] = a[0] * a[2] * (1 - cc) - a[1] * ss;
   R[2][1] = a[1] * a[2] * (1 - cc) + a[0] * ss;
   R[2][2] = a[2] * a[2] + (1 - a[2] * a[2]) * cc;
+  const int amc = o->p.angular_momentum && (o->c_start[c + 1] - o->c_start[c]) > 2;
+  double cmp[3] = {0, 0, 0}, ang[3] = {0, 0, 0};
+  if (amc) cell_angular(o, c, cmv, R, cmp, ang);
   for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
     double* v = pvel(o, o->c_mem[k]);
     double d0 = v[0] - cmv[0], d1 = v[1] - cmv[1], d2 = v[2] - cmv[2];
@@ -820,6 +917,14 @@ static void cell_collide(smpc_orc* o, unsigned c, const double* cmv) {
     v[0] = cmv[0] + r0;
     v[1] = cmv[1] + r1;
     v[2] = cmv[2] + r2;
+    if (amc) {
+      double x[3];
+      ppos(o, o->c_mem[k], x);
+      const double q[3] = {x[0] - cmp[0], x[1] - cmp[1], x[2] - cmp[2]};
+      v[0] += ang[1] * q[2] - ang[2] * q[1];
+      v[1] += ang[2] * q[0] - ang[0] * q[2];
+      v[2] += ang[0] * q[1] - ang[1] * q[0];
+    }
   }
 }
 

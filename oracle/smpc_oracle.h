@@ -49,7 +49,7 @@ typedef struct {
   double kT;             /* MPC temperature (MPC.cpp:12) */
   double shear;          /* Lees-Edwards shear rate (MPC.cpp:13) */
   unsigned step_update;  /* collide when t % step_update == 0 (MPC.cpp:119) */
-  int angular_momentum;  /* MPC.cpp:15; only 0 is supported by this oracle */
+  int angular_momentum;  /* MPC.cpp:15: angular-momentum-conserving collision */
   double lambda;         /* BB attraction depth (Box.cpp:7) */
   double md_dt;          /* velocity-Verlet step (Thermostat.cpp:3) */
   double r_cut;          /* Verlet cut-off (Box.cpp:8, 1.5) */

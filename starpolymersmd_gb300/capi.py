@@ -69,7 +69,7 @@ class ReplicaDesc(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("rng", C.c_int), ("mono_bin", C.c_int),
                 ("delrx_mode", C.c_int), ("step_update", C.c_int), ("max_neighbors", C.c_int),
-                ("strict_cells", C.c_int), ("device", C.c_int)]
+                ("strict_cells", C.c_int), ("device", C.c_int), ("angular_momentum", C.c_int)]
 
 
 class Inject(C.Structure):
@@ -160,7 +160,7 @@ class Context:
 
     def __init__(self, replicas: Sequence[dict], precision=FP64, rng=RNG_INJECT,
                  mono_bin=MONOBIN_REFERENCE, delrx_mode=DELRX_REFERENCE, step_update=1,
-                 max_neighbors=0, strict_cells=None, device=0):
+                 max_neighbors=0, strict_cells=None, device=0, angular_momentum=False):
         self.lib = load()
         n = len(replicas)
         descs = (ReplicaDesc * n)()
@@ -185,7 +185,8 @@ class Context:
             d.flags = int(r.get("flags", 0))
             self.replicas.append(dict(r))
         opt = Options(precision, rng, mono_bin, delrx_mode, step_update, max_neighbors,
-                      int(precision == FP64 if strict_cells is None else strict_cells), device)
+                      int(precision == FP64 if strict_cells is None else strict_cells), device,
+                      int(bool(angular_momentum)))
         h = C.c_void_p()
         rc = self.lib.smpc_create(descs, n, C.byref(opt), C.byref(h))
         if rc != 0:

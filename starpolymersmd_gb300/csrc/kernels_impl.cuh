@@ -8,6 +8,7 @@
 #include "mpc_kernels.cuh"
 #include "observables.cuh"
 #include "pmd_kernels.cuh"
+#include "analysis.cuh"
 
 namespace smpc {
 
@@ -90,7 +91,7 @@ void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
                             cudaStream_t st) {
   if (n_tiles == 0) return;
 #if SMPC_FAST_F32
-  if (!strict) {
+  if (!strict && variant >= 0) {  // variant < 0: the generic kernel (what k_collide recomputes)
     switch (variant) {
       case 1: bin_f32<256, 2>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
       case 2: bin_f32<256, 8>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
@@ -109,7 +110,7 @@ template <>
 void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
   if (a.n_tiles == 0) return;
 #if SMPC_FAST_F32
-  if (!a.strict) {
+  if (!a.strict && !a.amc) {
     switch (a.variant) {
       case 1: collide_f32<256, 128, 1408, 8>(a, st); return;
       case 2: collide_f32<128, 64, 704, 4>(a, st); return;
@@ -130,7 +131,8 @@ void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
   }
   kern<<<a.n_tiles, SMPC_COLLIDE_NT, dyn, st>>>(
       a.tiles, a.reps, a.dyn, a.off, a.perm, a.st_in, a.st_out, a.mpos, a.mvel, a.mkey, a.mimg,
-      a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.rot_c, a.rot_s, a.strict, a.mono_bin, a.err);
+      a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.rot_c, a.rot_s, a.strict, a.mono_bin, a.amc,
+      a.err);
 }
 
 template <>
@@ -144,21 +146,46 @@ void launch_temperature<Real>(const Tile* tiles, int n_tiles, const RepInfo* rep
 }
 
 template <>
-void launch_mol_observables<Real>(const int2* rep_mols, const int2* mols, int n_rep,
-                                  const Real* mpos, const Real* mvel, double* out,
-                                  cudaStream_t st) {
+void launch_mol_observables<Real>(const int2* rep_mols, const int2* mols, int n_rep, int n_mols,
+                                  const Real* mpos, const Real* mvel, double* mol_out,
+                                  double* out, cudaStream_t st) {
   if (n_rep == 0) return;
-  k_mol_observables<Real, 256><<<n_rep, 256, 0, st>>>(rep_mols, mols, mpos, mvel, out);
+  if (n_mols > 0) k_mol_observables<Real, 256><<<n_mols, 256, 0, st>>>(mols, mpos, mvel, mol_out);
+  k_obs_reduce<Real><<<(n_rep + 127) / 128, 128, 0, st>>>(rep_mols, mol_out, n_rep, out);
 }
 
 template <>
-void launch_unwrap_molecules<Real>(const RepInfo* reps, const RepDyn* dyn, const int2* rep_mols,
-                                   const int2* mols, int n_rep, const int* bond_start,
-                                   const int2* bonds, const Real* mpos, const Real* mvel,
-                                   Real* upos, Real* uvel, cudaStream_t st) {
-  if (n_rep == 0) return;
-  k_unwrap_molecules<Real><<<n_rep, 128, 0, st>>>(reps, dyn, rep_mols, mols, bond_start, bonds,
-                                                  mpos, mvel, upos, uvel);
+void launch_unwrap_molecules<Real>(const RepInfo* reps, const RepDyn* dyn, const int2* mols,
+                                   const int* mol_rep, int n_mols, int n_mono,
+                                   const int* bond_start, const int2* bonds, const Real* mpos,
+                                   const Real* mvel, Real* upos, Real* uvel, cudaStream_t st) {
+  if (n_mono == 0) return;
+  k_copy_monomers<Real><<<std::min((n_mono + 255) / 256, 152 * 8), 256, 0, st>>>(n_mono, mpos, mvel,
+                                                                              upos, uvel);
+  if (n_mols > 0)
+    k_unwrap_molecules<Real><<<(n_mols + 7) / 8, 256, 0, st>>>(reps, dyn, mols, mol_rep, n_mols,
+                                                               bond_start, bonds, mpos, mvel,
+                                                               upos, uvel);
+}
+
+template <>
+void launch_fourier_modes<Real>(const RepInfo* reps, int rep, const Real* rec, double kwave,
+                                double* part, int n_blocks, cudaStream_t st) {
+  k_fourier_modes<Real><<<n_blocks, ANA_NT, 0, st>>>(reps, rep, rec, kwave, part);
+}
+
+template <>
+void launch_vacf_sample<Real>(const RepInfo* reps, int rep, int slot_cap, const Real* rec,
+                              int n_p, int slot, double* ring, cudaStream_t st) {
+  if (slot_cap == 0) return;
+  k_vacf_sample<Real><<<std::min((slot_cap + ANA_NT - 1) / ANA_NT, 152 * 8), ANA_NT, 0, st>>>(
+      reps, rep, rec, n_p, slot, ring);
+}
+
+template <>
+void launch_vacf_lags<Real>(const double* ring, int n_p, int entries, int first, double* part,
+                            int n_blocks, cudaStream_t st) {
+  k_vacf_lags<Real><<<dim3(n_blocks, entries), ANA_NT, 0, st>>>(ring, n_p, entries, first, part);
 }
 
 template <>

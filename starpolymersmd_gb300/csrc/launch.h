@@ -46,6 +46,7 @@ struct CollideArgs {
   double rot_s;
   int strict;
   int mono_bin;
+  int amc;  // angular-momentum-conserving collision (generic kernel only)
   ErrorState* err;
 };
 
@@ -92,19 +93,33 @@ int pmd_block_count(int n_beads);
 
 // Molecules of periodic boxes made whole (observables.cuh); other boxes copied.
 template <typename R>
-void launch_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* rep_mols,
-                             const int2* mols, int n_rep, const int* bond_start,
+void launch_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* mols,
+                             const int* mol_rep, int n_mols, int n_mono, const int* bond_start,
                              const int2* bonds, const R* mpos, const R* mvel, R* upos, R* uvel,
                              cudaStream_t st);
 
+// Output-step observables: per molecule into mol_out (OBS_PER_REP each), then
+// per replica into out.
 template <typename R>
-void launch_mol_observables(const int2* rep_mols, const int2* mols, int n_rep, const R* mpos,
-                            const R* mvel, double* out, cudaStream_t st);
+void launch_mol_observables(const int2* rep_mols, const int2* mols, int n_rep, int n_mols,
+                            const R* mpos, const R* mvel, double* mol_out, double* out,
+                            cudaStream_t st);
 template <typename R>
 void launch_velocity_profile(const RepInfo* reps, const int2* rep_mols, const int2* mols, int rep,
                              int slot_cap, const R* rec, const R* mpos, const R* mvel,
                              double delrx, double width, long long kx0, int nx, long long ky0,
                              int ny, double* c6, double* bins, cudaStream_t st);
+
+// Solvent analyses (analysis.cuh); part: per-block partial sums.
+template <typename R>
+void launch_fourier_modes(const RepInfo* reps, int rep, const R* rec, double kwave, double* part,
+                          int n_blocks, cudaStream_t st);
+template <typename R>
+void launch_vacf_sample(const RepInfo* reps, int rep, int slot_cap, const R* rec, int n_p,
+                        int slot, double* ring, cudaStream_t st);
+template <typename R>
+void launch_vacf_lags(const double* ring, int n_p, int entries, int first, double* part,
+                      int n_blocks, cudaStream_t st);
 
 // Monomer state between the C ABI's x,y,z-interleaved doubles and the device
 // records (pos.w / vel.w keep mass and type): stage = pos[3M] | vel[3M] | force[3M]

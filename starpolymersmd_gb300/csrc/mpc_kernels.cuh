@@ -610,6 +610,7 @@ struct CollideCtx {
   uint32_t c0;
   int nc;
   bool strict;
+  bool amc;  // angular-momentum-conserving collision: monomers need positions
   ErrorState* err;
 };
 
@@ -621,6 +622,18 @@ __device__ __forceinline__ void finish_particle(Particle<R>& P, uint32_t p, cons
     const uint32_t m = P.src & ~MONO_BIT;
     if (C.g.wrap_mono == MONOBIN_WRAPPED)
       P.v.x = r_sub(P.v.x, r_mul(r_mul(static_cast<R>(C.mimg[m]), C.g.shear), C.g.L[1]));
+    if (C.amc) {
+      // the monomer where k_mono_prep binned it: shifted, at its image when
+      // monomers are binned wrapped
+      const R4<R> x = ld4_rw(C.mpos, m);
+      P.x.x = x.x + C.g.shift[0];
+      P.x.y = x.y + C.g.shift[1];
+      P.x.z = x.z + C.g.shift[2];
+      if (C.g.wrap_mono == MONOBIN_WRAPPED) {
+        R dvx = R(0);
+        le_wrap(C.g, P.x.x, P.x.y, P.x.z, dvx);
+      }
+    }
     P.lc = static_cast<int>(C.mkey[m].x - C.c0);
   } else {
     fluid_to_collision_frame(C.g, P.x, P.v);
@@ -660,6 +673,7 @@ __device__ __forceinline__ void load_particle(Particle<R>& P, uint32_t p, uint32
 template <typename R>
 __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, const R* s_cmv,
                                                 const R* s_rot, const R* s_scale,
+                                                const R* s_ang, const R* s_cmp,
                                                 const CollideCtx<R>& C, R* st_out,
                                                 ErrorState* err) {
   if (P.lc < 0) return;
@@ -687,6 +701,14 @@ __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, cons
   vx = cm[0] + ((M[0] * d0 + M[1] * d1) + M[2] * d2);
   vy = cm[1] + ((M[3] * d0 + M[4] * d1) + M[5] * d2);
   vz = cm[2] + ((M[6] * d0 + M[7] * d1) + M[8] * d2);
+  if (C.amc) {  // + Angular x (r - CMP) (MPC.cpp:268); zero outside AMC cells
+    const R* w = s_ang + 3 * P.lc;
+    const R* c = s_cmp + 3 * P.lc;
+    const R q0 = P.x.x - c[0], q1 = P.x.y - c[1], q2 = P.x.z - c[2];
+    vx += w[1] * q2 - w[2] * q1;
+    vy += w[2] * q0 - w[0] * q2;
+    vz += w[0] * q1 - w[1] * q0;
+  }
   if (!(r_isfinite(vx) && r_isfinite(vy) && r_isfinite(vz)))
     raise_error(err, ERR_NONFINITE, p, P.src);
   if (P.src & MONO_BIT) {
@@ -735,6 +757,51 @@ __device__ __forceinline__ void tile_particle(Particle<R>& P, int j, int nloc, u
 }
 
 
+template <typename R>
+__device__ __forceinline__ R acc_to_r(typename AccT<R>::type a);
+template <>
+__device__ __forceinline__ double acc_to_r<double>(double a) { return a; }
+template <>
+__device__ __forceinline__ float acc_to_r<float>(long long a) { return fix32_to_f(a); }
+
+__device__ __forceinline__ long long shfl_pair(long long v) {
+  return __shfl_xor_sync(0xFFFFFFFFu, v, 1);
+}
+__device__ __forceinline__ double shfl_pair(double v) {
+  return __shfl_xor_sync(0xFFFFFFFFu, v, 1);
+}
+
+// x = A^-1 b for a symmetric positive-definite 3x3 A: the Cholesky factor
+// A = L L^T column by column, forward then back substitution (the LLT solve
+// MPC::calculateAngular calls, MPC.cpp:373).
+template <typename R>
+__device__ __forceinline__ void llt_solve3(const R A[3][3], const R b[3], R x[3]) {
+  R l[3][3] = {{R(0), R(0), R(0)}, {R(0), R(0), R(0)}, {R(0), R(0), R(0)}}, y[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    R s = A[j][j];
+    for (int k = 0; k < j; ++k) s -= l[j][k] * l[j][k];
+    l[j][j] = r_sqrt(s);
+    for (int i = j + 1; i < 3; ++i) {
+      R t = A[i][j];
+      for (int k = 0; k < j; ++k) t -= l[i][k] * l[j][k];
+      l[i][j] = t / l[j][j];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    R s = b[i];
+    for (int k = 0; k < i; ++k) s -= l[i][k] * y[k];
+    y[i] = s / l[i][i];
+  }
+#pragma unroll
+  for (int i = 2; i >= 0; --i) {
+    R s = y[i];
+    for (int k = i + 1; k < 3; ++k) s -= l[k][i] * x[k];
+    x[i] = s / l[i][i];
+  }
+}
+
 // One CTA per tile of <= CT cells of one replica.
 //  stage  : gather the tile's particles (perm -> 32-byte records, GU loads in
 //           flight per thread), recompute their collision-frame state, keep
@@ -746,7 +813,13 @@ __device__ __forceinline__ void tile_particle(Particle<R>& P, int j, int nloc, u
 //           the reference's sequential FP64 sums on the parity path; then
 //           draws the MBS factor (MPC.cpp:287-289) and the rotation
 //           (MPC.cpp:244-257);
-//  apply  : rotate/scale, undo the shift, write the tile back in cell order.
+//  amc    : (angular-momentum-conserving collision, cells of more than two
+//           particles) the cell's centre of mass, the angular momentum the
+//           rotation removed and the inertia tensor, summed by the same two
+//           lanes about the cell's corner (FP32: fixed point), and the
+//           angular velocity that puts it back (MPC.cpp:260-269, 324-374);
+//  apply  : rotate/scale (+ angular term), undo the shift, write the tile
+//           back in cell order.
 // A tile holding more than CAP particles reads the excess straight from
 // global memory (correct, slower).
 template <typename R, int NT, int CT, int CAP>
@@ -755,12 +828,15 @@ __global__ void __launch_bounds__(NT) k_collide(
     const uint32_t* __restrict__ perm, const R* __restrict__ st_in, R* __restrict__ st_out,
     const R* mpos, R* mvel, const uint2* mkey, const int* mimg, const double* inj_gamma,
     const double* inj_uphi, const double* inj_utheta, int rng, double rot_c, double rot_s,
-    int strict, int mono_bin, ErrorState* err) {
+    int strict, int mono_bin, int amc, ErrorState* err) {
   constexpr int GU = 4;
   constexpr bool kFP64 = std::is_same<R, double>::value;
+  typedef typename AccT<R>::type Acc;
   __shared__ R s_cmv[CT * 3];
   __shared__ R s_rot[CT * 9];
   __shared__ R s_scale[CT];
+  __shared__ R s_ang[CT * 3];
+  __shared__ R s_cmp[CT * 3];
   __shared__ uint32_t s_off[CT + 1];
   extern __shared__ __align__(16) unsigned char s_dyn[];
   R4<R>* s_x = reinterpret_cast<R4<R>*>(s_dyn);
@@ -782,6 +858,7 @@ __global__ void __launch_bounds__(NT) k_collide(
   C.cbase = static_cast<uint32_t>(ri.cell_base);
   C.c0 = static_cast<uint32_t>(t.begin);
   C.strict = strict != 0;
+  C.amc = amc != 0;
   const int nc = t.end - t.begin;
   C.nc = nc;
   C.err = err;
@@ -950,7 +1027,95 @@ __global__ void __launch_bounds__(NT) k_collide(
       M[7] = a1 * a2 * (R(1) - rc) + a0 * rs;
       M[8] = a2 * a2 + (R(1) - a2 * a2) * rc;
     }
-    scale = __shfl_xor_sync(0xFFFFFFFFu, scale, 1);  // lane 1 gets lane 0's factor
+    {  // both lanes get lane 0's factor
+      const R other = __shfl_xor_sync(0xFFFFFFFFu, scale, 1);
+      if (half == 1) scale = other;
+    }
+    R ang[3] = {R(0), R(0), R(0)}, cmp[3] = {R(0), R(0), R(0)};
+    if (amc) {  // uniform over the CTA
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {  // lane 0 takes lane 1's rotation
+        const R o = __shfl_xor_sync(0xFFFFFFFFu, M[q], 1);
+        if (half == 0) M[q] = o;
+      }
+      const bool cell_amc = live && nn > 2u;
+      // the cell's corner in the collision frame (cell index = floor(x + L/2))
+      const int Lx = ri.L[0], Ly = ri.L[1];
+      const int ix = static_cast<int>(cl % static_cast<uint32_t>(Lx));
+      const int iy = static_cast<int>((cl / static_cast<uint32_t>(Lx)) % static_cast<uint32_t>(Ly));
+      const int iz = static_cast<int>(cl / static_cast<uint32_t>(Lx * Ly));
+      const R k0 = static_cast<R>(ix) - C.g.half[0], k1 = static_cast<R>(iy) - C.g.half[1],
+              k2 = static_cast<R>(iz) - C.g.half[2];
+      Acc s0 = 0, s1 = 0, s2 = 0, sm = 0;
+      for (int j = j0 + half; cell_amc && j < j1; j += 2) {
+        Particle<R> P;
+        tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
+        if (P.lc < 0) continue;
+        s0 += to_acc<R>((P.x.x - k0) * P.m);
+        s1 += to_acc<R>((P.x.y - k1) * P.m);
+        s2 += to_acc<R>((P.x.z - k2) * P.m);
+        sm += to_acc<R>(P.m);
+      }
+      s0 += shfl_pair(s0);
+      s1 += shfl_pair(s1);
+      s2 += shfl_pair(s2);
+      sm += shfl_pair(sm);
+      const R mt = acc_to_r<R>(sm);
+      const R c0 = mt > R(0) ? acc_to_r<R>(s0) / mt : R(0);
+      const R c1 = mt > R(0) ? acc_to_r<R>(s1) / mt : R(0);
+      const R c2 = mt > R(0) ? acc_to_r<R>(s2) / mt : R(0);
+      // angular momentum the rotation removes, and the inertia tensor
+      Acc a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      const R f = scale >= R(0) ? scale : R(1);
+      for (int j = j0 + half; cell_amc && j < j1; j += 2) {
+        Particle<R> P;
+        tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
+        if (P.lc < 0) continue;
+        const R q0 = (P.x.x - k0) - c0, q1 = (P.x.y - k1) - c1, q2 = (P.x.z - k2) - c2;
+        R u0, u1, u2;
+        if (kFP64 && scale >= R(0)) {  // the thermostatted velocity (MPC.cpp:291)
+          u0 = (scale * P.v.x + (R(1) - scale) * cm[0]) - cm[0];
+          u1 = (scale * P.v.y + (R(1) - scale) * cm[1]) - cm[1];
+          u2 = (scale * P.v.z + (R(1) - scale) * cm[2]) - cm[2];
+        } else {
+          u0 = (P.v.x - cm[0]) * f;
+          u1 = (P.v.y - cm[1]) * f;
+          u2 = (P.v.z - cm[2]) * f;
+        }
+        const R w0 = u0 - ((M[0] * u0 + M[1] * u1) + M[2] * u2);
+        const R w1 = u1 - ((M[3] * u0 + M[4] * u1) + M[5] * u2);
+        const R w2 = u2 - ((M[6] * u0 + M[7] * u1) + M[8] * u2);
+        a[0] += to_acc<R>(P.m * (q1 * w2 - q2 * w1));
+        a[1] += to_acc<R>(P.m * (q2 * w0 - q0 * w2));
+        a[2] += to_acc<R>(P.m * (q0 * w1 - q1 * w0));
+        a[3] += to_acc<R>(P.m * (q1 * q1 + q2 * q2));
+        a[4] += to_acc<R>(P.m * (q0 * q0 + q2 * q2));
+        a[5] += to_acc<R>(P.m * (q1 * q1 + q0 * q0));
+        a[6] += to_acc<R>(P.m * q0 * q1);
+        a[7] += to_acc<R>(P.m * q0 * q2);
+        a[8] += to_acc<R>(P.m * q1 * q2);
+      }
+#pragma unroll
+      for (int q = 0; q < 9; ++q) a[q] += shfl_pair(a[q]);
+      if (cell_amc) {
+        const R I[3][3] = {{acc_to_r<R>(a[3]), -acc_to_r<R>(a[6]), -acc_to_r<R>(a[7])},
+                           {-acc_to_r<R>(a[6]), acc_to_r<R>(a[4]), -acc_to_r<R>(a[8])},
+                           {-acc_to_r<R>(a[7]), -acc_to_r<R>(a[8]), acc_to_r<R>(a[5])}};
+        const R cv[3] = {acc_to_r<R>(a[0]), acc_to_r<R>(a[1]), acc_to_r<R>(a[2])};
+        llt_solve3<R>(I, cv, ang);
+        cmp[0] = k0 + c0;
+        cmp[1] = k1 + c1;
+        cmp[2] = k2 + c2;
+      }
+    }
+    if (half == 1 && live) {
+      s_ang[3 * lc] = ang[0];
+      s_ang[3 * lc + 1] = ang[1];
+      s_ang[3 * lc + 2] = ang[2];
+      s_cmp[3 * lc] = cmp[0];
+      s_cmp[3 * lc + 1] = cmp[1];
+      s_cmp[3 * lc + 2] = cmp[2];
+    }
     if (half == 1 && live) {
       if (!kFP64 && scale >= R(0)) {
 #pragma unroll
@@ -970,12 +1135,13 @@ __global__ void __launch_bounds__(NT) k_collide(
   for (int j = threadIdx.x; j < nloc; j += NT) {
     Particle<R> P;
     tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
-    apply_collision(P, p0 + j, s_cmv, s_rot, s_scale, C, st_out, err);
+    apply_collision(P, p0 + j, s_cmv, s_rot, s_scale, s_ang, s_cmp, C, st_out, err);
   }
   for (int base = CAP; base < n; base += NT) {
     Particle<R> P;
     load_particle(P, p0 + base + threadIdx.x, p1, C);
-    apply_collision(P, p0 + base + threadIdx.x, s_cmv, s_rot, s_scale, C, st_out, err);
+    apply_collision(P, p0 + base + threadIdx.x, s_cmv, s_rot, s_scale, s_ang, s_cmp, C, st_out,
+                    err);
   }
 }
 

@@ -17,6 +17,8 @@
 #pragma once
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "mpc_kernels.cuh"
 #include "smpc_device.cuh"
 
@@ -71,132 +73,227 @@ __device__ __forceinline__ double block_sum(double v, double* s_red) {
   return t;  // valid in thread 0
 }
 
-// One CTA per replica. rep_mols[r] = (first molecule, count); mols[m] =
-// global monomer range [x, y). out[OBS_PER_REP * r + ...]: R_g, G (row-major,
-// 9), rotation frequency (3), kinetic energy, temperature, molecules.
+// One CTA per molecule; mols[m] = global monomer range [x, y). mol_out[16 m
+// + ...]: R_g of the molecule, G (row-major, 9), rotation frequency (3),
+// kinetic energy, monomers. FP64 sums the centre in monomer order (the
+// reference's order, so the relative positions are the reference's to the
+// last bit); FP32 sums it as a block reduction.
 template <typename R, int NT>
-__global__ void __launch_bounds__(NT) k_mol_observables(const int2* rep_mols, const int2* mols,
-                                                        const R* mpos, const R* mvel,
-                                                        double* out) {
+__global__ void __launch_bounds__(NT) k_mol_observables(const int2* mols, const R* mpos,
+                                                        const R* mvel, double* mol_out) {
   __shared__ double s_c[6];
   __shared__ double s_red[NT / 32];
-  const int r = blockIdx.x;
+  const int2 mb = mols[blockIdx.x];
+  const int n = mb.y - mb.x;
+  if (std::is_same<R, double>::value) {
+    if (threadIdx.x == 0) molecule_centre<R>(mpos, mvel, mb.x, mb.y, s_c);
+  } else {
+    double c[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = mb.x + threadIdx.x; i < mb.y; i += NT) {
+      const R4<R> p = ld4_rw(mpos, i), v = ld4_rw(mvel, i);
+      c[0] += static_cast<double>(p.x);
+      c[1] += static_cast<double>(p.y);
+      c[2] += static_cast<double>(p.z);
+      c[3] += static_cast<double>(v.x);
+      c[4] += static_cast<double>(v.y);
+      c[5] += static_cast<double>(v.z);
+    }
+    for (int k = 0; k < 6; ++k) {
+      const double t = block_sum<NT>(c[k], s_red);
+      if (threadIdx.x == 0) s_c[k] = t / static_cast<double>(n);
+    }
+  }
+  __syncthreads();
+  // S = sum r r^T (6), angular momentum (3), sum m |u|^2
+  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = mb.x + threadIdx.x; i < mb.y; i += NT) {
+    const R4<R> p = ld4_rw(mpos, i), v = ld4_rw(mvel, i);
+    const double x0 = static_cast<double>(p.x) - s_c[0], x1 = static_cast<double>(p.y) - s_c[1],
+                 x2 = static_cast<double>(p.z) - s_c[2];
+    const double u0 = static_cast<double>(v.x) - s_c[3], u1 = static_cast<double>(v.y) - s_c[4],
+                 u2 = static_cast<double>(v.z) - s_c[5];
+    acc[0] += x0 * x0;
+    acc[1] += x0 * x1;
+    acc[2] += x0 * x2;
+    acc[3] += x1 * x1;
+    acc[4] += x1 * x2;
+    acc[5] += x2 * x2;
+    acc[6] += x1 * u2 - x2 * u1;
+    acc[7] += x2 * u0 - x0 * u2;
+    acc[8] += x0 * u1 - x1 * u0;
+    acc[9] += static_cast<double>(p.w) * ((u0 * u0 + u1 * u1) + u2 * u2);
+  }
+  double tot[10];
+  for (int k = 0; k < 10; ++k) tot[k] = block_sum<NT>(acc[k], s_red);
+  if (threadIdx.x != 0) return;
+  double* o = mol_out + static_cast<size_t>(OBS_PER_REP) * blockIdx.x;
+  for (int k = 0; k < OBS_PER_REP; ++k) o[k] = 0.0;
+  if (n <= 0) return;
+  const double dn = static_cast<double>(n);
+  const double g[9] = {tot[0] / dn, tot[1] / dn, tot[2] / dn, tot[1] / dn, tot[3] / dn,
+                       tot[4] / dn, tot[2] / dn, tot[4] / dn, tot[5] / dn};
+  for (int k = 0; k < 9; ++k) o[1 + k] = g[k];
+  o[0] = sqrt(g[0] + g[4] + g[8]);
+  const double tr = tot[0] + tot[3] + tot[5];
+  const double I[3][3] = {{tr - tot[0], -tot[1], -tot[2]},
+                          {-tot[1], tr - tot[3], -tot[4]},
+                          {-tot[2], -tot[4], tr - tot[5]}};
+  const double Lm[3] = {tot[6], tot[7], tot[8]};
+  double om[3];
+  solve_sym3(I, Lm, om);
+  for (int k = 0; k < 3; ++k) o[10 + k] = om[k];
+  o[13] = tot[9] * 0.5;
+  o[14] = dn;
+}
+
+// One thread per replica: its molecules' values in molecule order. out[16 r
+// + ...]: mean R_g, mean G (row-major, 9), mean rotation frequency (3),
+// kinetic energy, temperature 2 E / (3 (N - 1)), molecules.
+template <typename R>  // R: the precision of the instantiating unit (one copy per unit)
+__global__ void k_obs_reduce(const int2* rep_mols, const double* mol_out, int n_rep, double* out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rep) return;
   const int2 rm = rep_mols[r];
   double rg = 0, G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, w[3] = {0, 0, 0}, ekin = 0;
   long long n_total = 0;
-  for (int mi = rm.x; mi < rm.x + rm.y; ++mi) {
-    const int2 mb = mols[mi];
-    const int n = mb.y - mb.x;
-    if (threadIdx.x == 0) molecule_centre<R>(mpos, mvel, mb.x, mb.y, s_c);
-    __syncthreads();
-    // S = sum r r^T (6), angular momentum (3), sum m |u|^2
-    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int i = mb.x + threadIdx.x; i < mb.y; i += NT) {
-      const R4<R> p = ld4_rw(mpos, i), v = ld4_rw(mvel, i);
-      const double x0 = static_cast<double>(p.x) - s_c[0], x1 = static_cast<double>(p.y) - s_c[1],
-                   x2 = static_cast<double>(p.z) - s_c[2];
-      const double u0 = static_cast<double>(v.x) - s_c[3], u1 = static_cast<double>(v.y) - s_c[4],
-                   u2 = static_cast<double>(v.z) - s_c[5];
-      acc[0] += x0 * x0;
-      acc[1] += x0 * x1;
-      acc[2] += x0 * x2;
-      acc[3] += x1 * x1;
-      acc[4] += x1 * x2;
-      acc[5] += x2 * x2;
-      acc[6] += x1 * u2 - x2 * u1;
-      acc[7] += x2 * u0 - x0 * u2;
-      acc[8] += x0 * u1 - x1 * u0;
-      acc[9] += static_cast<double>(p.w) * ((u0 * u0 + u1 * u1) + u2 * u2);
-    }
-    double tot[10];
-    for (int k = 0; k < 10; ++k) tot[k] = block_sum<NT>(acc[k], s_red);
-    if (threadIdx.x == 0 && n > 0) {
-      const double dn = static_cast<double>(n);
-      const double g[9] = {tot[0] / dn, tot[1] / dn, tot[2] / dn, tot[1] / dn, tot[3] / dn,
-                           tot[4] / dn, tot[2] / dn, tot[4] / dn, tot[5] / dn};
-      for (int k = 0; k < 9; ++k) G[k] += g[k];
-      rg += sqrt(g[0] + g[4] + g[8]);
-      const double tr = tot[0] + tot[3] + tot[5];
-      const double I[3][3] = {{tr - tot[0], -tot[1], -tot[2]},
-                              {-tot[1], tr - tot[3], -tot[4]},
-                              {-tot[2], -tot[4], tr - tot[5]}};
-      const double Lm[3] = {tot[6], tot[7], tot[8]};
-      double om[3];
-      solve_sym3(I, Lm, om);
-      for (int k = 0; k < 3; ++k) w[k] += om[k];
-      ekin += tot[9] * 0.5;
-      n_total += n;
-    }
-    __syncthreads();
+  for (int m = rm.x; m < rm.x + rm.y; ++m) {
+    const double* o = mol_out + static_cast<size_t>(OBS_PER_REP) * m;
+    if (o[14] <= 0.0) continue;
+    for (int k = 0; k < 9; ++k) G[k] += o[1 + k];
+    rg += o[0];
+    for (int k = 0; k < 3; ++k) w[k] += o[10 + k];
+    ekin += o[13];
+    n_total += static_cast<long long>(o[14]);
   }
-  if (threadIdx.x == 0) {
-    const double nm = rm.y > 0 ? static_cast<double>(rm.y) : 1.0;
-    double* o = out + static_cast<size_t>(OBS_PER_REP) * r;
-    o[0] = rg / nm;
-    for (int k = 0; k < 9; ++k) o[1 + k] = G[k] / nm;
-    for (int k = 0; k < 3; ++k) o[10 + k] = w[k] / nm;
-    o[13] = ekin;
-    o[14] = n_total > 1 ? ekin * 2. / (3. * static_cast<double>(n_total - 1)) : 0.0;
-    o[15] = static_cast<double>(rm.y);
-  }
+  const double nm = rm.y > 0 ? static_cast<double>(rm.y) : 1.0;
+  double* o = out + static_cast<size_t>(OBS_PER_REP) * r;
+  o[0] = rg / nm;
+  for (int k = 0; k < 9; ++k) o[1 + k] = G[k] / nm;
+  for (int k = 0; k < 3; ++k) o[10 + k] = w[k] / nm;
+  o[13] = ekin;
+  o[14] = n_total > 1 ? ekin * 2. / (3. * static_cast<double>(n_total - 1)) : 0.0;
+  o[15] = static_cast<double>(rm.y);
 }
 
 // Molecules of periodic boxes made whole for the observables: bead i is placed
 // at the Lees-Edwards minimum image (MPC.cpp:456-465, current delrx) next to
 // its lowest-indexed bonded partner in the molecule, which comes earlier and is
-// already placed, or next to the molecule's first bead when it has none (stars
-// and chains numbered outward from the core always have one). Its v_x gets the
-// shear velocity of the image it moved to (MPC.cpp:428). Other boxes are
-// copied as they are. One block per box; one thread per molecule of a periodic
-// box walks its beads in order.
+// already placed, or next to the molecule's first bead when it has none. Its
+// v_x gets the shear velocity of the image it moved to (MPC.cpp:428).
+// k_copy_monomers copies every monomer first; k_unwrap_molecules then runs one
+// warp per molecule of a periodic box over chunks of 32 beads: when every
+// bead of a chunk has its partner either before the chunk (placed) or right
+// before itself (stars and chains numbered outward from the core), the chunk
+// is one segmented prefix sum of the bond vectors; otherwise lane 0 walks it.
 template <typename R>
-__global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* rep_mols,
-                                   const int2* mols, const int* bond_start, const int2* bonds,
-                                   const R* mpos, const R* mvel, R* upos, R* uvel) {
-  const int r = blockIdx.x;
-  const RepInfo& ri = reps[r];
-  if (!(ri.flags & REP_PERIODIC_MD)) {
-    for (int i = ri.mono_base + threadIdx.x; i < ri.mono_base + ri.n_mono; i += blockDim.x) {
-      st4(upos, i, ld4_rw(mpos, i));
-      st4(uvel, i, ld4_rw(mvel, i));
-    }
-    return;
+__global__ void k_copy_monomers(int n, const R* mpos, const R* mvel, R* upos, R* uvel) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    st4(upos, i, ld4_rw(mpos, i));
+    st4(uvel, i, ld4_rw(mvel, i));
   }
+}
+
+__device__ __forceinline__ void unwrap_bond(const double L[3], double delrx, double& d0,
+                                            double& d1, double& d2) {
+  const double cy = round(d1 / L[1]);
+  d0 -= L[0] * round(d0 / L[0]);
+  d0 -= cy * delrx;
+  d0 -= L[0] * round(d0 / L[0]);
+  d1 -= L[1] * cy;
+  d2 -= L[2] * round(d2 / L[2]);
+}
+
+template <typename R>
+__global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* mols,
+                                   const int* mol_rep, int n_mols, const int* bond_start,
+                                   const int2* bonds, const R* mpos, const R* mvel, R* upos,
+                                   R* uvel) {
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (m >= n_mols) return;  // whole warps
+  const RepInfo& ri = reps[mol_rep[m]];
+  if (!(ri.flags & REP_PERIODIC_MD)) return;
   const double L[3] = {static_cast<double>(ri.L[0]), static_cast<double>(ri.L[1]),
                        static_cast<double>(ri.L[2])};
-  const double delrx = dyn[r].delrx;
-  const int2 rm = rep_mols[r];
-  for (int m = rm.x + threadIdx.x; m < rm.x + rm.y; m += blockDim.x) {
-    const int2 mb = mols[m];
-    for (int i = mb.x; i < mb.y; ++i) {
-      int p = -1;
+  const double delrx = dyn[mol_rep[m]].delrx;
+  const double sLy = ri.shear * L[1];
+  const int2 mb = mols[m];
+  for (int c0 = mb.x + 1; c0 < mb.y; c0 += 32) {
+    const int i = c0 + lane;
+    const bool active = i < mb.y;
+    int p = -1;
+    double d0 = 0, d1 = 0, d2 = 0;
+    if (active) {
       for (int e = bond_start[i]; e < bond_start[i + 1]; ++e) {
         const int j = bonds[e].x;
         if (j >= mb.x && j < i && (p < 0 || j < p)) p = j;
       }
       if (p < 0) p = mb.x;
-      R4<R> x = ld4_rw(mpos, i), v = ld4_rw(mvel, i);
-      if (i != mb.x) {
-        const R4<R> xp = ld4_rw(mpos, p), up = ld4_rw(upos, p);
-        double d0 = static_cast<double>(x.x) - static_cast<double>(xp.x);
-        double d1 = static_cast<double>(x.y) - static_cast<double>(xp.y);
-        double d2 = static_cast<double>(x.z) - static_cast<double>(xp.z);
-        const double cy = round(d1 / L[1]);
-        d0 -= L[0] * round(d0 / L[0]);
-        d0 -= cy * delrx;
-        d0 -= L[0] * round(d0 / L[0]);
-        d1 -= L[1] * cy;
-        d2 -= L[2] * round(d2 / L[2]);
-        const double uy = static_cast<double>(up.y) + d1;
-        const double ny = round((uy - static_cast<double>(x.y)) / L[1]);
-        x.x = static_cast<R>(static_cast<double>(up.x) + d0);
-        x.y = static_cast<R>(uy);
-        x.z = static_cast<R>(static_cast<double>(up.z) + d2);
-        v.x = static_cast<R>(static_cast<double>(v.x) + ny * ri.shear * L[1]);
+      const R4<R> x = ld4_rw(mpos, i), xp = ld4_rw(mpos, p);
+      d0 = static_cast<double>(x.x) - static_cast<double>(xp.x);
+      d1 = static_cast<double>(x.y) - static_cast<double>(xp.y);
+      d2 = static_cast<double>(x.z) - static_cast<double>(xp.z);
+      unwrap_bond(L, delrx, d0, d1, d2);
+    }
+    const bool chained = active && p == i - 1 && p >= c0;
+    if (__any_sync(FULL, active && p >= c0 && !chained)) {
+      // a partner inside the chunk that is not the previous bead: one by one
+      for (int k = 0; k < 32; ++k) {
+        const int q = __shfl_sync(FULL, p, k);
+        const double e0 = __shfl_sync(FULL, d0, k), e1 = __shfl_sync(FULL, d1, k),
+                     e2 = __shfl_sync(FULL, d2, k);
+        if (lane == 0 && c0 + k < mb.y) {
+          const R4<R> up = ld4_rw(upos, q);
+          R4<R> u = ld4_rw(upos, c0 + k);
+          u.x = static_cast<R>(static_cast<double>(up.x) + e0);
+          u.y = static_cast<R>(static_cast<double>(up.y) + e1);
+          u.z = static_cast<R>(static_cast<double>(up.z) + e2);
+          st4(upos, c0 + k, u);
+        }
+        __syncwarp();
       }
-      st4(upos, i, x);
+    } else {
+      // segment heads take their placed partner's image; the scan adds the
+      // bond vectors down each segment
+      double a0 = d0, a1 = d1, a2 = d2;
+      if (active && !chained) {
+        const R4<R> up = ld4_rw(upos, p);
+        a0 += static_cast<double>(up.x);
+        a1 += static_cast<double>(up.y);
+        a2 += static_cast<double>(up.z);
+      }
+      int head = chained ? -1 : lane;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int h = __shfl_up_sync(FULL, head, o);
+        if (lane >= o && h > head) head = h;
+      }
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t0 = __shfl_up_sync(FULL, a0, o), t1 = __shfl_up_sync(FULL, a1, o),
+                     t2 = __shfl_up_sync(FULL, a2, o);
+        if (lane - o >= head) {
+          a0 += t0;
+          a1 += t1;
+          a2 += t2;
+        }
+      }
+      if (active) {
+        R4<R> u = ld4_rw(upos, i);
+        u.x = static_cast<R>(a0);
+        u.y = static_cast<R>(a1);
+        u.z = static_cast<R>(a2);
+        st4(upos, i, u);
+      }
+    }
+    __syncwarp();
+    if (active) {  // the image's shear velocity
+      const R4<R> x = ld4_rw(mpos, i), u = ld4_rw(upos, i);
+      const double ny = round((static_cast<double>(u.y) - static_cast<double>(x.y)) / L[1]);
+      R4<R> v = ld4_rw(uvel, i);
+      v.x = static_cast<R>(static_cast<double>(v.x) + ny * sLy);
       st4(uvel, i, v);
     }
+    __syncwarp();
   }
 }
 

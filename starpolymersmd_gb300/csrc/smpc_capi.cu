@@ -79,6 +79,13 @@ struct smpc_ctx {
   void* d_uvel = nullptr;
   void* d_mnext = nullptr;    // second monomer position buffer of the periodic MD
   uint8_t* d_pamphi = nullptr;  // solvophobic flag per monomer (periodic MD)
+  // solvent analyses: per-block partials, and the velocity-autocorrelation ring
+  double* d_ana_part = nullptr;
+  size_t ana_part_cap = 0;
+  double* d_vacf_ring = nullptr;
+  int vacf_rep = -1, vacf_np = 0, vacf_entries = 0;
+  uint64_t vacf_samples = 0, vacf_calcs = 0;
+  std::vector<double> vacf_sum;
   std::vector<std::vector<int>> bsrc, bdst;
   std::vector<std::vector<int>> anchor;
 
@@ -90,6 +97,9 @@ struct smpc_ctx {
   int2* d_rep_mols = nullptr;  // per replica: first molecule, count
   int2* d_mols = nullptr;      // per molecule: global monomer range
   double* d_obs = nullptr;     // OBS_PER_REP per replica
+  double* d_mol_obs = nullptr; // OBS_PER_REP per molecule
+  int* d_mol_rep = nullptr;    // replica of each molecule
+  int n_mols = 0;
   double* d_prof = nullptr;    // velocity-profile bins, grown on demand
   size_t prof_cap = 0;
   double* d_c6 = nullptr;      // centre of molecule 0 (position, velocity)
@@ -114,7 +124,7 @@ struct smpc_ctx {
 namespace {
 
 bool fast_path(const smpc_ctx* ctx) {
-  return ctx->opt.precision == SMPC_FP32 && !ctx->opt.strict_cells;
+  return ctx->opt.precision == SMPC_FP32 && !ctx->opt.strict_cells && !ctx->opt.angular_momentum;
 }
 int tile_set(int cells) { return cells == 64 ? 0 : (cells == 128 ? 1 : 2); }
 
@@ -165,7 +175,7 @@ int launch_binning(smpc_ctx* ctx, int cur) {
                             ctx->rot_s, ctx->mono_chunks, ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
-                            ctx->var_bin, ctx->st);
+                            ctx->opt.angular_momentum ? -1 : ctx->var_bin, ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
   smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
@@ -211,6 +221,7 @@ smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
   a.rot_s = ctx->rot_s;
   a.strict = strict;
   a.mono_bin = ctx->opt.mono_bin;
+  a.amc = ctx->opt.angular_momentum ? 1 : 0;
   a.err = ctx->d_err;
   return a;
 }
@@ -267,7 +278,7 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
   cudaEventRecord(ev[1 + PH_MONO], ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
-                            ctx->var_bin, ctx->st);
+                            ctx->opt.angular_momentum ? -1 : ctx->var_bin, ctx->st);
   cudaEventRecord(ev[1 + PH_BIN], ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
@@ -623,13 +634,16 @@ void free_all(smpc_ctx* ctx) {
   if (ctx->d_upos) cudaFree(ctx->d_upos);
   if (ctx->d_uvel) cudaFree(ctx->d_uvel);
   if (ctx->d_mnext) cudaFree(ctx->d_mnext);
+  if (ctx->d_ana_part) cudaFree(ctx->d_ana_part);
+  if (ctx->d_vacf_ring) cudaFree(ctx->d_vacf_ring);
   if (ctx->d_pamphi) cudaFree(ctx->d_pamphi);
   void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
                   ctx->d_mimg, ctx->d_bond_start, ctx->d_bonds, ctx->d_nlist, ctx->d_ncount,
                   ctx->d_md_order, ctx->d_inj, ctx->d_err, ctx->d_frames, ctx->d_rep_mols,
-                  ctx->d_mols, ctx->d_obs, ctx->d_prof, ctx->d_c6, ctx->d_dstage};
+                  ctx->d_mols, ctx->d_obs, ctx->d_prof, ctx->d_c6, ctx->d_dstage, ctx->d_mol_obs,
+                  ctx->d_mol_rep};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < 3; ++k)
@@ -723,16 +737,29 @@ int temperature_all_noalloc_t(smpc_ctx* ctx, double* out) {
 
 int upload_molecules(smpc_ctx* ctx) {
   std::vector<int2> rep_mols(ctx->n_rep), mols;
+  std::vector<int> mol_rep;
   for (int r = 0; r < ctx->n_rep; ++r) {
     const std::vector<int>& ms = ctx->mol_start[r];
     const int base = ctx->reps[r].mono_base;
     rep_mols[r] = make_int2(static_cast<int>(mols.size()), static_cast<int>(ms.size()) - 1);
-    for (size_t k = 0; k + 1 < ms.size(); ++k) mols.push_back(make_int2(base + ms[k], base + ms[k + 1]));
+    for (size_t k = 0; k + 1 < ms.size(); ++k) {
+      mols.push_back(make_int2(base + ms[k], base + ms[k + 1]));
+      mol_rep.push_back(r);
+    }
   }
-  if (ctx->d_rep_mols) cudaFree(ctx->d_rep_mols);
-  if (ctx->d_mols) cudaFree(ctx->d_mols);
+  for (void* q : {static_cast<void*>(ctx->d_rep_mols), static_cast<void*>(ctx->d_mols),
+                  static_cast<void*>(ctx->d_mol_obs), static_cast<void*>(ctx->d_mol_rep)})
+    if (q) cudaFree(q);
   ctx->d_rep_mols = nullptr;
   ctx->d_mols = nullptr;
+  ctx->d_mol_obs = nullptr;
+  ctx->d_mol_rep = nullptr;
+  ctx->n_mols = static_cast<int>(mols.size());
+  CU(dalloc(&ctx->d_mol_obs, static_cast<size_t>(smpc::OBS_PER_REP) * mols.size()));
+  CU(dalloc(&ctx->d_mol_rep, mol_rep.size()));
+  if (!mol_rep.empty())
+    CU(cudaMemcpy(ctx->d_mol_rep, mol_rep.data(), mol_rep.size() * sizeof(int),
+                  cudaMemcpyHostToDevice));
   CU(dalloc(&ctx->d_rep_mols, rep_mols.size()));
   CU(dalloc(&ctx->d_mols, mols.size()));
   CU(cudaMemcpy(ctx->d_rep_mols, rep_mols.data(), rep_mols.size() * sizeof(int2),
@@ -1550,8 +1577,9 @@ void observed_monomers(smpc_ctx* ctx, const R** pos, const R** vel) {
   *pos = static_cast<const R*>(ctx->d_mpos);
   *vel = static_cast<const R*>(ctx->d_mvel);
   if (ctx->pmd.empty()) return;
-  smpc::launch_unwrap_molecules<R>(ctx->d_reps, ctx->d_dyn, ctx->d_rep_mols, ctx->d_mols,
-                                   ctx->n_rep, ctx->d_bond_start, ctx->d_bonds, *pos, *vel,
+  smpc::launch_unwrap_molecules<R>(ctx->d_reps, ctx->d_dyn, ctx->d_mols, ctx->d_mol_rep,
+                                   ctx->n_mols, static_cast<int>(ctx->total_mono),
+                                   ctx->d_bond_start, ctx->d_bonds, *pos, *vel,
                                    static_cast<R*>(ctx->d_upos), static_cast<R*>(ctx->d_uvel),
                                    ctx->st);
   *pos = static_cast<const R*>(ctx->d_upos);
@@ -1562,8 +1590,8 @@ template <typename R>
 void mol_observables_t(smpc_ctx* ctx) {
   const R *p, *v;
   observed_monomers<R>(ctx, &p, &v);
-  smpc::launch_mol_observables<R>(ctx->d_rep_mols, ctx->d_mols, ctx->n_rep, p, v, ctx->d_obs,
-                                  ctx->st);
+  smpc::launch_mol_observables<R>(ctx->d_rep_mols, ctx->d_mols, ctx->n_rep, ctx->n_mols, p, v,
+                                  ctx->d_mol_obs, ctx->d_obs, ctx->st);
 }
 
 template <typename R>
@@ -1650,6 +1678,121 @@ int smpc_error_word(smpc_ctx* ctx, unsigned* word, unsigned* info3) {
 int smpc_synchronize(smpc_ctx* ctx) {
   if (!ctx) return SMPC_E_ARG;
   CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- solvent analyses
+namespace {
+constexpr int kAnaBlocks = 152 * 4;  // partial sums per analysis pass
+
+int ana_partials(smpc_ctx* ctx, size_t n) {
+  if (n <= ctx->ana_part_cap) return SMPC_OK;
+  CU(cudaStreamSynchronize(ctx->st));
+  if (ctx->d_ana_part) cudaFree(ctx->d_ana_part);
+  ctx->d_ana_part = nullptr;
+  ctx->ana_part_cap = 0;
+  CU(dalloc(&ctx->d_ana_part, n));
+  ctx->ana_part_cap = n;
+  return SMPC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int smpc_fourier_modes(smpc_ctx* ctx, int rep, double box_length, double* out18) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (!out18 || !(box_length > 0)) return fail(ctx, SMPC_E_ARG, "fourier modes: buffer or length");
+  cudaSetDevice(ctx->device);
+  if (int rc = ana_partials(ctx, 18 * static_cast<size_t>(kAnaBlocks))) return rc;
+  const double kwave = 2 * M_PI / box_length;
+  if (ctx->opt.precision == SMPC_FP64)
+    smpc::launch_fourier_modes<double>(ctx->d_reps, rep, static_cast<const double*>(ctx->d_rec[ctx->cur]),
+                                       kwave, ctx->d_ana_part, kAnaBlocks, ctx->st);
+  else
+    smpc::launch_fourier_modes<float>(ctx->d_reps, rep, static_cast<const float*>(ctx->d_rec[ctx->cur]),
+                                      kwave, ctx->d_ana_part, kAnaBlocks, ctx->st);
+  CU(cudaGetLastError());
+  std::vector<double> part(18 * static_cast<size_t>(kAnaBlocks));
+  CU(cudaMemcpyAsync(part.data(), ctx->d_ana_part, part.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  // Fourier_Autocorr: divided by the particle count, component along k removed
+  const double n = static_cast<double>(ctx->reps[rep].n_fluid);
+  for (int q = 0; q < 18; ++q) {
+    double s = 0.0;
+    for (int b = 0; b < kAnaBlocks; ++b) s += part[18 * static_cast<size_t>(b) + q];
+    out18[q] = n > 0 ? s / n : 0.0;
+  }
+  for (int j = 0; j < 3; ++j) out18[6 * j + 2 * j] = out18[6 * j + 2 * j + 1] = 0.0;
+  return SMPC_OK;
+}
+
+int smpc_vacf_start(smpc_ctx* ctx, int rep, int n_particles, int entries) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (n_particles <= 0 || n_particles > ctx->reps[rep].n_fluid || entries <= 0)
+    return fail(ctx, SMPC_E_ARG, "vacf: particle count or entries");
+  cudaSetDevice(ctx->device);
+  CU(cudaStreamSynchronize(ctx->st));
+  if (ctx->d_vacf_ring) cudaFree(ctx->d_vacf_ring);
+  ctx->d_vacf_ring = nullptr;
+  CU(dalloc(&ctx->d_vacf_ring, 3 * static_cast<size_t>(n_particles) * entries));
+  if (int rc = ana_partials(ctx, static_cast<size_t>(kAnaBlocks) * entries)) return rc;
+  ctx->vacf_rep = rep;
+  ctx->vacf_np = n_particles;
+  ctx->vacf_entries = entries;
+  ctx->vacf_samples = 0;
+  ctx->vacf_calcs = 0;
+  ctx->vacf_sum.assign(entries, 0.0);
+  return SMPC_OK;
+}
+
+int smpc_vacf_sample(smpc_ctx* ctx) {
+  if (!ctx) return SMPC_E_ARG;
+  if (ctx->vacf_rep < 0) return fail(ctx, SMPC_E_STATE, "smpc_vacf_start not called");
+  cudaSetDevice(ctx->device);
+  const int rep = ctx->vacf_rep, E = ctx->vacf_entries, np = ctx->vacf_np;
+  const int slot = static_cast<int>(ctx->vacf_samples % static_cast<uint64_t>(E));
+  if (ctx->opt.precision == SMPC_FP64)
+    smpc::launch_vacf_sample<double>(ctx->d_reps, rep, ctx->reps[rep].slot_cap,
+                                     static_cast<const double*>(ctx->d_rec[ctx->cur]), np, slot,
+                                     ctx->d_vacf_ring, ctx->st);
+  else
+    smpc::launch_vacf_sample<float>(ctx->d_reps, rep, ctx->reps[rep].slot_cap,
+                                    static_cast<const float*>(ctx->d_rec[ctx->cur]), np, slot,
+                                    ctx->d_vacf_ring, ctx->st);
+  ctx->vacf_samples += 1;
+  if (ctx->vacf_samples < static_cast<uint64_t>(E)) {
+    CU(cudaGetLastError());
+    return SMPC_OK;
+  }
+  // the window is full: Vel_Autocorr_Fluid::calculate() over its samples
+  const int first = static_cast<int>((ctx->vacf_samples - E) % static_cast<uint64_t>(E));
+  const int nb = std::min(kAnaBlocks, (np + 255) / 256);
+  if (ctx->opt.precision == SMPC_FP64)
+    smpc::launch_vacf_lags<double>(ctx->d_vacf_ring, np, E, first, ctx->d_ana_part, nb, ctx->st);
+  else
+    smpc::launch_vacf_lags<float>(ctx->d_vacf_ring, np, E, first, ctx->d_ana_part, nb, ctx->st);
+  CU(cudaGetLastError());
+  std::vector<double> part(static_cast<size_t>(nb) * E);
+  CU(cudaMemcpyAsync(part.data(), ctx->d_ana_part, part.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  for (int j = 0; j < E; ++j) {
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += part[static_cast<size_t>(j) * nb + b];
+    ctx->vacf_sum[j] += s;
+  }
+  ctx->vacf_calcs += 1;
+  return SMPC_OK;
+}
+
+int smpc_vacf_result(smpc_ctx* ctx, double* lag_sums, uint64_t* calculations) {
+  if (!ctx || !lag_sums || !calculations) return SMPC_E_ARG;
+  if (ctx->vacf_rep < 0) return fail(ctx, SMPC_E_STATE, "smpc_vacf_start not called");
+  for (int j = 0; j < ctx->vacf_entries; ++j) lag_sums[j] = ctx->vacf_sum[j];
+  *calculations = ctx->vacf_calcs;
   return SMPC_OK;
 }
 

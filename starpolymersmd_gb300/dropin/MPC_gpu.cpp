@@ -73,6 +73,7 @@ MPC::MPC(Box& box, double aTemperature, int N_c, double aShear, unsigned step, b
   bc.shear = Shear;
   bc.step_update = step_update;
   bc.n_fluid = NumberOfMPCParticles;
+  bc.angular_momentum = angular_momentum;
 }
 
 MPC::~MPC() { smpc_dropin::detach(SimBox); }
@@ -144,12 +145,6 @@ void MPC::step(const long int& t, const double& dt) {
   delrx += Shear * BoxSize[1] * dt;
   delrx -= BoxSize[0] * round(delrx / BoxSize[0]);
   if (t % step_update) return;
-  if (angular_momentum) {
-    std::fprintf(stderr,
-                 "MPC::step: the angular-momentum-conserving collision (MPC.cpp:260-269) is not "
-                 "implemented on the GPU\n");
-    std::abort();
-  }
   smpc_dropin::BoxContext& bc = smpc_dropin::find(SimBox);
   smpc_ctx* ctx = smpc_dropin::ensure(SimBox);
   if (fluid_dirty) {

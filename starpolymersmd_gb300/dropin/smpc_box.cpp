@@ -143,6 +143,7 @@ smpc_ctx* ensure(Box& box) {
   o.max_neighbors = 0;
   o.strict_cells = 1;
   o.device = device_ordinal();
+  o.angular_momentum = bc.angular_momentum ? 1 : 0;
   smpc_ctx* ctx = nullptr;
   int rc = smpc_create(&d, 1, &o, &ctx);
   if (rc != SMPC_OK) fail(ctx, "smpc_create", rc);

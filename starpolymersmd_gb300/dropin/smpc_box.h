@@ -34,6 +34,7 @@ struct BoxContext {
   double shear = 0.0;
   unsigned step_update = 1;
   unsigned n_fluid = 0;
+  bool angular_momentum = false;  // MPC(..., angular_mom)
   // integrator, registered by the Thermostat_GPU constructor
   bool has_md = false;
   double md_dt = 0.01;

@@ -48,6 +48,12 @@ SCENARIOS = {
     "recentre_L12": dict(L=(12, 12, 12), n_c=3, kT=1.0, shear=0.05, step_update=1, h=0.1,
                          md_dt=0.01, lam=1.0, star=dict(A=2, B=2, arms=3, mass=5.0),
                          n_loop=3, with_md=True, star_offset=(3.5, -1.0, 0.5)),
+    # the angular-momentum-conserving collision (MPC.cpp:260-269, 324-374)
+    "amc_mpc_L6": dict(L=(6, 6, 6), n_c=6, kT=1.0, shear=0.1, step_update=1, h=0.1,
+                       star=None, n_loop=3, with_md=False, amc=True),
+    "amc_star_L12": dict(L=(12, 12, 12), n_c=3, kT=1.0, shear=0.05, step_update=5, h=0.1,
+                         md_dt=0.01, lam=1.0, star=dict(A=2, B=2, arms=3, mass=5.0),
+                         n_loop=11, with_md=True, amc=True),
     # larger self-avoiding star, MD only with a strong BB attraction
     "md_saw_L16": dict(L=(16, 16, 16), n_c=1, kT=1.0, shear=0.0, step_update=1, h=0.1,
                        md_dt=0.01, lam=1.5, star=dict(A=5, B=5, arms=6, mass=5.0),
@@ -57,7 +63,7 @@ SCENARIOS = {
 
 def run_scenario(name: str, sc: dict) -> dict:
     ref = orc.RefSystem(sc["L"], sc["kT"], sc.get("lam", 1.0), sc["n_c"], sc["shear"],
-                        sc["step_update"])
+                        sc["step_update"], amc=sc.get("amc", False))
     ref.reseed(1)
     order = ref.shift_order()
     st = sc.get("star")
@@ -81,6 +87,7 @@ def run_scenario(name: str, sc: dict) -> dict:
                step_update=sc["step_update"], h=sc["h"], md_dt=sc.get("md_dt", 0.0),
                lam=sc.get("lam", 1.0), n_loop=sc["n_loop"], with_md=int(sc["with_md"]),
                md_only=int(bool(sc.get("md_only"))), shift_order=order,
+               amc=int(bool(sc.get("amc"))),
                fluid_pos0=fpos0, fluid_vel0=fvel0, bond_src=src, bond_dst=dst)
     if st:
         out.update(mono_pos0=m0["pos"], mono_vel0=m0["vel"], mono_force0=m0["force"],

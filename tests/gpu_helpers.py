@@ -38,7 +38,8 @@ def fixture_context(fx, precision=capi.FP64, periodic=False):
                **{"lambda": float(fx["lam"])})
     ctx = capi.Context([rep], precision=precision, rng=capi.RNG_INJECT,
                        step_update=int(fx["step_update"]),
-                       mono_bin=capi.MONOBIN_WRAPPED if periodic else capi.MONOBIN_REFERENCE)
+                       mono_bin=capi.MONOBIN_WRAPPED if periodic else capi.MONOBIN_REFERENCE,
+                       angular_momentum=bool(int(fx.get("amc", 0))))
     ctx.set_fluid(0, fx["fluid_pos0"], fx["fluid_vel0"])
     if star:
         ctx.set_monomers(0, fx["mono_pos0"], fx["mono_vel0"], fx["mono_force0"], fx["mono_mass"],

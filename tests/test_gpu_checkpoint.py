@@ -62,8 +62,9 @@ def test_batched_restart_continues_the_run(precision):
         a.ctx.raise_on_device_error()
         b.ctx.raise_on_device_error()
         _assert_same(_state(a.ctx), _state(b.ctx), precision)
+        # FP64 reductions whose order follows the binning ranks: to round-off
         _assert_same([a.ctx.temperature_all(), a.ctx.molecule_observables_all()],
-                     [b.ctx.temperature_all(), b.ctx.molecule_observables_all()], precision)
+                     [b.ctx.temperature_all(), b.ctx.molecule_observables_all()], capi.FP64)
     finally:
         a.close()
         b.close()

@@ -129,8 +129,9 @@ def test_fp64_graph_cycles_match_stepwise():
         assert a.delrx(0) == b.delrx(0)
 
 
-def test_fp32_matches_fp64_oracle_on_injected_draws(golden_dir):
-    fx = gr.load(os.path.join(golden_dir, "star_mpc_L12.npz"))
+@pytest.mark.parametrize("name", ["star_mpc_L12", "amc_star_L12"])
+def test_fp32_matches_fp64_oracle_on_injected_draws(golden_dir, name):
+    fx = gr.load(os.path.join(golden_dir, name + ".npz"))
     coll = gr.collision_index(fx)
     L = fx["L"]
     with H.fixture_context(fx, precision=capi.FP32) as ctx:

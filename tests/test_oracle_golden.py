@@ -23,7 +23,7 @@ def make_oracle(fx):
     n_m = len(fx["mono_pos0"]) if gr.has_star(fx) else 0
     o = orc.OracleSystem(fx["L"], float(fx["kT"]), float(fx["shear"]), int(fx["step_update"]),
                          n_f, n_m, mol_start=[0, n_m] if n_m else [0], lambda_=float(fx["lam"]),
-                         md_dt=float(fx["md_dt"]))
+                         md_dt=float(fx["md_dt"]), angular_momentum=int(fx.get("amc", 0)))
     o.set_fluid(fx["fluid_pos0"], fx["fluid_vel0"])
     if n_m:
         o.set_monomers(fx["mono_pos0"], fx["mono_vel0"], fx["mono_force0"], fx["mono_mass"],
