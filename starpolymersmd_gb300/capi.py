@@ -39,7 +39,8 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide", "smpc_set_molecules",
            "smpc_molecule_observables_all", "smpc_velocity_profile", "smpc_checkpoint_size",
            "smpc_checkpoint_save", "smpc_checkpoint_load", "smpc_checkpoint_write",
-           "smpc_checkpoint_read")
+           "smpc_checkpoint_read", "smpc_fourier_modes", "smpc_vacf_start", "smpc_vacf_sample",
+           "smpc_vacf_result")
 
 PHASES = ("md_substeps", "cycle_begin", "mono_prep", "fluid_bin", "scan", "build_perm",
           "collide", "cycle_end")
@@ -135,6 +136,10 @@ def load(path: Optional[str] = None):
         "smpc_checkpoint_load": ([P, P, C.c_uint64], I),
         "smpc_checkpoint_write": ([P, C.c_char_p], I),
         "smpc_checkpoint_read": ([P, C.c_char_p], I),
+        "smpc_fourier_modes": ([P, I, D, P], I),
+        "smpc_vacf_start": ([P, I, I, I], I),
+        "smpc_vacf_sample": ([P], I),
+        "smpc_vacf_result": ([P, P, C.POINTER(C.c_uint64)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -394,6 +399,29 @@ class Context:
         mc = np.zeros(self.replicas[rep].get("n_mono", 0), dtype=np.int32)
         self._check(self.lib.smpc_cell_members(self.h, rep, _p(fc), _p(mc)), "cell_members")
         return fc, mc
+
+    def fourier_modes(self, rep, box_length):
+        """The three transverse solvent modes of Fourier_Autocorr (complex, 3 x 3:
+        mode along x, y, z by velocity component)."""
+        out = np.zeros(18)
+        self._check(self.lib.smpc_fourier_modes(self.h, rep, float(box_length), _p(out)),
+                    "fourier_modes")
+        return (out[0::2] + 1j * out[1::2]).reshape(3, 3)
+
+    def vacf_start(self, rep, n_particles, entries):
+        self._vacf_entries = int(entries)
+        self._check(self.lib.smpc_vacf_start(self.h, rep, int(n_particles), int(entries)),
+                    "vacf_start")
+
+    def vacf_sample(self):
+        self._check(self.lib.smpc_vacf_sample(self.h), "vacf_sample")
+
+    def vacf_result(self):
+        """(lag sums over particles and calculations, number of calculations)."""
+        out = np.zeros(self._vacf_entries)
+        n = C.c_uint64()
+        self._check(self.lib.smpc_vacf_result(self.h, _p(out), C.byref(n)), "vacf_result")
+        return out, n.value
 
     def checkpoint(self) -> bytes:
         """The context's full state (smpc_checkpoint_save)."""

@@ -1,0 +1,73 @@
+"""Solvent analyses on the device against numpy restatements of the
+reference's functors (Fourier_Autocorr.h, Vel_Autocorr_Fluid.h) on the same
+states."""
+import numpy as np
+import pytest
+
+from starpolymersmd_gb300 import analysis, capi
+from tests import gpu_helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _solvent_context(precision, L=6, n_c=5, shear=0.2):
+    star, fpos, fvel = H.small_star_system(L=L, n_c=n_c, shear=shear, seed=7)
+    return H.context_for(None, fpos, fvel, L, 1.0, shear, 1, precision=precision,
+                         rng=capi.RNG_PHILOX, seed=3)
+
+
+def _numpy_modes(pos, vel, L):
+    k = 2 * np.pi / L
+    out = np.zeros((3, 3), dtype=np.complex128)
+    for j in range(3):
+        e = np.exp(1j * k * pos[:, j])
+        out[j] = (vel * e[:, None]).sum(axis=0) / len(pos)
+        out[j, j] = 0.0
+    return out
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.FP32])
+def test_fourier_modes_match_numpy(precision):
+    L = 6
+    with _solvent_context(precision, L) as ctx:
+        fa = analysis.FourierAutocorr(3, 0.1)
+        fb = analysis.FourierAutocorr(3, 0.1)
+        for t in range(5):
+            ctx.mpc_step(t, 0.1)
+            p, v = ctx.get_fluid(0)
+            got = ctx.fourier_modes(0, L)
+            want = _numpy_modes(p, v, L)
+            tol = 1e-12 if precision == capi.FP64 else 1e-6
+            np.testing.assert_allclose(got, want, rtol=0, atol=tol * np.abs(v).max())
+            assert np.all(np.diag(got) == 0)
+            fa.push(got)
+            fb.push(want)
+        ta, aa = fa.result()
+        tb, ab = fb.result()
+        assert fa.counter == 3
+        np.testing.assert_allclose(aa, ab, rtol=1e-5, atol=1e-9)
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.FP32])
+def test_velocity_autocorrelation_matches_numpy(precision):
+    n_p, entries = 150, 4
+    with _solvent_context(precision) as ctx:
+        ctx.vacf_start(0, n_p, entries)
+        window, sums, calcs = [], np.zeros(entries), 0
+        for t in range(9):
+            ctx.mpc_step(t, 0.1)
+            ctx.vacf_sample()
+            _, v = ctx.get_fluid(0)
+            window.append(v[:n_p].copy())
+            window = window[-entries:]
+            if len(window) == entries:
+                for j in range(entries):
+                    sums[j] += np.sum(window[0] * window[j])
+                calcs += 1
+        got, n = ctx.vacf_result()
+        assert n == calcs == 6
+        np.testing.assert_allclose(got, sums, rtol=1e-12)
+        avg = analysis.vacf_average(got, n, n_p)
+        assert avg[0] > 0
+        assert analysis.vacf_diffusion(avg, 1.0, n) == pytest.approx(
+            np.sum(sums / n / n_p * 1.0 / n) / 3.0)
