@@ -252,6 +252,12 @@ int smpc_synchronize(smpc_ctx* ctx);
  *   sample adds sum_i v_i(oldest) . v_i(oldest + j) to lag_sums[j]. The
  *   reference's average is lag_sums[j] / calculations / n_particles. */
 int smpc_fourier_modes(smpc_ctx* ctx, int rep, double box_length, double* out18);
+/* Pressure tensor of every replica (no reference counterpart): out[12 r + k],
+ * k = 0..5 the kinetic part (1/V) sum m u u^T over solvent and monomers with
+ * the peculiar velocity u = v - shear y e_x, k = 6..11 the monomers' pair and
+ * FENE virial (1/V) sum over pairs r_ij F_ij^T; components xx yy zz xy xz yz.
+ * The SRD collision's momentum transfer is not included. */
+int smpc_pressure_tensor_all(smpc_ctx* ctx, double* out);
 int smpc_vacf_start(smpc_ctx* ctx, int rep, int n_particles, int entries);
 int smpc_vacf_sample(smpc_ctx* ctx);
 int smpc_vacf_result(smpc_ctx* ctx, double* lag_sums, uint64_t* calculations);

@@ -40,7 +40,7 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_molecule_observables_all", "smpc_velocity_profile", "smpc_checkpoint_size",
            "smpc_checkpoint_save", "smpc_checkpoint_load", "smpc_checkpoint_write",
            "smpc_checkpoint_read", "smpc_fourier_modes", "smpc_vacf_start", "smpc_vacf_sample",
-           "smpc_vacf_result")
+           "smpc_vacf_result", "smpc_pressure_tensor_all")
 
 PHASES = ("md_substeps", "cycle_begin", "mono_prep", "fluid_bin", "scan", "build_perm",
           "collide", "cycle_end")
@@ -140,6 +140,7 @@ def load(path: Optional[str] = None):
         "smpc_vacf_start": ([P, I, I, I], I),
         "smpc_vacf_sample": ([P], I),
         "smpc_vacf_result": ([P, P, C.POINTER(C.c_uint64)], I),
+        "smpc_pressure_tensor_all": ([P, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -407,6 +408,12 @@ class Context:
         self._check(self.lib.smpc_fourier_modes(self.h, rep, float(box_length), _p(out)),
                     "fourier_modes")
         return (out[0::2] + 1j * out[1::2]).reshape(3, 3)
+
+    def pressure_tensor_all(self):
+        """(kinetic, virial): (n_rep, 6) each, components xx yy zz xy xz yz."""
+        out = np.zeros((self.n_rep, 12))
+        self._check(self.lib.smpc_pressure_tensor_all(self.h, _p(out)), "pressure_tensor_all")
+        return out[:, :6], out[:, 6:]
 
     def vacf_start(self, rep, n_particles, entries):
         self._vacf_entries = int(entries)

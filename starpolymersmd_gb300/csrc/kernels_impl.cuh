@@ -189,13 +189,33 @@ void launch_vacf_lags<Real>(const double* ring, int n_p, int entries, int first,
 }
 
 template <>
+void launch_kinetic_tensor<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
+                                 const Real* rec, double* part, cudaStream_t st) {
+  if (n_tiles == 0) return;
+  k_kinetic_tensor<Real><<<n_tiles, ANA_NT, 0, st>>>(tiles, reps, rec, part);
+}
+
+template <>
+void launch_mono_stress<Real>(const RepInfo* reps, const RepDyn* dyn, int n_rep, const Real* mpos,
+                              const Real* mvel, const int* nlist_t, const int* ncount,
+                              int n_mono_total, int* const* rows, int max_nb,
+                              const int* bond_start, const int2* bonds, double* out,
+                              cudaStream_t st) {
+  if (n_rep == 0) return;
+  k_mono_stress<Real><<<n_rep, ANA_NT, 0, st>>>(reps, dyn, mpos, mvel, nlist_t, ncount,
+                                                n_mono_total, rows, max_nb, bond_start, bonds,
+                                                out);
+}
+
+template <>
 void launch_pmd_call<Real>(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, Real* mpos,
                            Real* mnext, Real* mvel, Real* mfrc, Real* mdisp, int n,
                            double adv_scale, int calc_epot, cudaStream_t st) {
   if (a.n == 0) return;
   const int nb = a.n_blocks;
-  // k_pmd_nlist: warps stride over the beads; at most 8 blocks per SM of GB300
-  const int nb_list = std::min((a.n + PMD_NT / 32 - 1) / (PMD_NT / 32), 152 * 8);
+  // k_pmd_nlist: warps stride over the beads, four blocks per SM of GB300 (a
+  // launch without a rebuild request returns at once and stays short)
+  const int nb_list = std::min((a.n + PMD_NT / 32 - 1) / (PMD_NT / 32), 152 * 4);
   const int nb_force = pmd_force_block_count<Real>(a.n);
   if (n == 0) {
     k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, 0, adv_scale, 0);

@@ -121,6 +121,17 @@ template <typename R>
 void launch_vacf_lags(const double* ring, int n_p, int entries, int first, double* part,
                       int n_blocks, cudaStream_t st);
 
+// Pressure tensor parts (analysis.cuh): solvent kinetic per slot tile
+// (part[6 * tile]), monomer kinetic + virial per replica (out[12 * r]).
+template <typename R>
+void launch_kinetic_tensor(const Tile* tiles, int n_tiles, const RepInfo* reps, const R* rec,
+                           double* part, cudaStream_t st);
+template <typename R>
+void launch_mono_stress(const RepInfo* reps, const RepDyn* dyn, int n_rep, const R* mpos,
+                        const R* mvel, const int* nlist_t, const int* ncount, int n_mono_total,
+                        int* const* rows, int max_nb, const int* bond_start, const int2* bonds,
+                        double* out, cudaStream_t st);
+
 // Monomer state between the C ABI's x,y,z-interleaved doubles and the device
 // records (pos.w / vel.w keep mass and type): stage = pos[3M] | vel[3M] | force[3M]
 template <typename R>

@@ -14,8 +14,7 @@
 //   k_pmd_drift   substep 1: half kick and drift, Lees-Edwards wrap, peculiar
 //                 displacement, binning into the grid of substep 1, rebuild
 //                 request; block 0 records the substep's delrx
-//   k_pmd_nlist   records delrx and the rebuild threshold of the next
-//                 substep; then (rebuild only) one warp per bead: the lanes
+//   k_pmd_nlist   (rebuild only, else it returns at once) one warp per bead: the lanes
 //                 test the beads of the 27 neighbour cells (across a y face
 //                 the neighbour rows are looked up at x -/+ delrx) and the
 //                 list is written in bead-index order, so the force sums do
@@ -26,8 +25,10 @@
 //                 kick, drift, wrap and binning, writing the positions into
 //                 the other of two position buffers (other beads still read
 //                 substep k's); the last block to finish records the new
-//                 lists' delrx, clears the request and sums the potential
-//                 energy of the blocks in a fixed order
+//                 lists' delrx, clears the request, sums the potential
+//                 energy of the blocks in a fixed order, and records delrx
+//                 and the rebuild threshold of substep k + 2 (the drift
+//                 kernel's last block those of substep 2)
 // Substep k's positions live in buffer (k - 1) & 1 (0 = the monomer array),
 // its grid, rebuild request and delrx in slots k & 1. The set-up call (n = 0)
 // wraps, bins and builds lists and forces at the current positions.
@@ -174,6 +175,38 @@ __device__ __forceinline__ R pmd_threshold(const RepInfo& ri, double dl, double 
   return R(0.5) * (skin - r_fabs(shear) * tb * (static_cast<R>(ri.r_verlet) + skin) - r_fabs(ddl));
 }
 
+// Records delrx and the rebuild threshold of the substep after substep k
+// (slot s = k & 1), once k's rebuild request is final: its lists will be k's
+// if k rebuilds them, else the older ones.
+template <typename R>
+__device__ __forceinline__ void pmd_next_constants(const PmdArgs& a, const RepInfo& ri, int s,
+                                                   double adv_scale) {
+  const double dl = a.dl_slot[s];
+  const int rebuilt = a.flag[s];
+  const double dl1 = pmd_advance(ri, dl, adv_scale);
+  const double db = rebuilt ? dl : *a.delrx_build;
+  const int since = rebuilt ? 0 : a.flag[3] + 1;
+  a.dl_slot[s ^ 1] = dl1;
+  a.dl_slot[2 + (s ^ 1)] = static_cast<double>(
+      pmd_threshold<R>(ri, dl1, db, static_cast<R>(since + 1) * static_cast<R>(ri.md_dt)));
+}
+
+// True in one thread of the last block of the grid to get here; the blocks
+// count themselves in flag[2], which that thread resets (no block waits).
+__device__ __forceinline__ bool pmd_last_block(const PmdArgs& a) {
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(reinterpret_cast<unsigned*>(a.flag + 2), 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return false;
+  __threadfence();
+  a.flag[2] = 0;
+  return true;
+}
+
 // One bead's half kick (with the force f), drift, Lees-Edwards wrap and
 // peculiar displacement (Thermostat_None.cpp:22-27, MPC.cpp:421-429).
 template <typename R>
@@ -235,25 +268,28 @@ __global__ void __launch_bounds__(PMD_NT)
   }
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const PmdBox<R> b = pmd_box<R>(ri, s_dl);
-  const size_t g = static_cast<size_t>(a.base) + i;
-  R4<R> x = ld4_rw(mpos, g), v = ld4_rw(mvel, g), u = ld4_rw(mdisp, g);
-  if (drift) {
-    const R4<R> f = ld4_rw(mfrc, g);
-    pmd_drift_bead(ri, b, x, v, u, f.x, f.y, f.z);
+  if (i < a.n) {
+    const PmdBox<R> b = pmd_box<R>(ri, s_dl);
+    const size_t g = static_cast<size_t>(a.base) + i;
+    R4<R> x = ld4_rw(mpos, g), v = ld4_rw(mvel, g), u = ld4_rw(mdisp, g);
+    if (drift) {
+      const R4<R> f = ld4_rw(mfrc, g);
+      pmd_drift_bead(ri, b, x, v, u, f.x, f.y, f.z);
+    }
+    pmd_wrap(ri, b, x, v);
+    st4(mpos, g, x);
+    st4(mvel, g, v);
+    pmd_bin(a, adv_k & 1, b, x, i);
+    if (!drift) {
+      if (i == 0) a.flag[0] = 1;
+    } else {
+      st4(mdisp, g, u);
+      const R thr = s_thr;
+      if (thr <= R(0) || (u.x * u.x + u.y * u.y) + u.z * u.z > thr * thr) a.flag[adv_k & 1] = 1;
+    }
   }
-  pmd_wrap(ri, b, x, v);
-  st4(mpos, g, x);
-  st4(mvel, g, v);
-  pmd_bin(a, adv_k & 1, b, x, i);
-  if (!drift) {
-    if (i == 0) a.flag[0] = 1;
-    return;
-  }
-  st4(mdisp, g, u);
-  const R thr = s_thr;
-  if (thr <= R(0) || (u.x * u.x + u.y * u.y) + u.z * u.z > thr * thr) a.flag[adv_k & 1] = 1;
+  // this substep's request is final: the next substep's constants
+  if (pmd_last_block(a)) pmd_next_constants<R>(a, ri, adv_k & 1, adv_scale);
 }
 
 // Verlet list of bead i (box-local) by the 32 lanes of one warp; buf holds
@@ -345,18 +381,6 @@ __global__ void __launch_bounds__(PMD_NT)
                 double adv_scale) {
   const int s = adv_k & 1;
   const RepInfo& ri = reps[a.rep];
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    // the next substep's delrx and threshold, for the drift in k_pmd_forces:
-    // its lists are this substep's if it rebuilds them, else the older ones
-    const double dl = a.dl_slot[s];
-    const int rebuilt = a.flag[s];
-    const double dl1 = pmd_advance(ri, dl, adv_scale);
-    const double db = rebuilt ? dl : *a.delrx_build;
-    const int since = rebuilt ? 0 : a.flag[3] + 1;
-    a.dl_slot[s ^ 1] = dl1;
-    a.dl_slot[2 + (s ^ 1)] = static_cast<double>(
-        pmd_threshold<R>(ri, dl1, db, static_cast<R>(since + 1) * static_cast<R>(ri.md_dt)));
-  }
   if (a.flag[s] == 0) return;
   __shared__ int s_buf[PMD_NT / 32][PMD_NL_CAP];
   const int warp = static_cast<int>(threadIdx.x) >> 5, lane = static_cast<int>(threadIdx.x) & 31;
@@ -478,15 +502,7 @@ __global__ void __launch_bounds__(PMD_NT)
     if (threadIdx.x == 0) a.epot_part[blockIdx.x] = tot;
   }
   // the last block to get here closes the substep (no block waits for another)
-  __shared__ bool s_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(reinterpret_cast<unsigned*>(a.flag + 2), 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!s_last || threadIdx.x != 0) return;
-  __threadfence();
+  if (!pmd_last_block(a)) return;
   RepDyn& dn = dyn[a.rep];
   if (a.flag[s] != 0) {
     *a.delrx_build = a.dl_slot[s];
@@ -501,7 +517,8 @@ __global__ void __launch_bounds__(PMD_NT)
     for (int k = 0; k < static_cast<int>(gridDim.x); ++k) tot += a.epot_part[k];
     dn.epot = tot;
   }
-  a.flag[2] = 0;
+  // the next substep's request is final too: the constants of the one after
+  pmd_next_constants<R>(a, ri, s ^ 1, adv_scale);
 }
 
 template <typename R>

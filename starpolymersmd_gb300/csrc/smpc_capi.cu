@@ -39,6 +39,7 @@ struct smpc_ctx {
   RepDyn* d_dyn = nullptr;
   Tile* d_bin_tiles = nullptr;
   int n_bin_tiles = 0;
+  std::vector<int> bin_tile_rep;  // replica of each binning tile
   Tile* d_col_tiles = nullptr;   // parity-path collide tiles
   int n_col_tiles = 0;
   // fast path: collide tiles for each tile size the variants use (64/128/256 cells)
@@ -83,6 +84,8 @@ struct smpc_ctx {
   double* d_ana_part = nullptr;
   size_t ana_part_cap = 0;
   double* d_vacf_ring = nullptr;
+  int** d_rows_by_rep = nullptr;  // each replica's periodic Verlet rows, or null
+  double* d_stress = nullptr;     // 12 per replica
   int vacf_rep = -1, vacf_np = 0, vacf_entries = 0;
   uint64_t vacf_samples = 0, vacf_calcs = 0;
   std::vector<double> vacf_sum;
@@ -636,6 +639,8 @@ void free_all(smpc_ctx* ctx) {
   if (ctx->d_mnext) cudaFree(ctx->d_mnext);
   if (ctx->d_ana_part) cudaFree(ctx->d_ana_part);
   if (ctx->d_vacf_ring) cudaFree(ctx->d_vacf_ring);
+  if (ctx->d_rows_by_rep) cudaFree(ctx->d_rows_by_rep);
+  if (ctx->d_stress) cudaFree(ctx->d_stress);
   if (ctx->d_pamphi) cudaFree(ctx->d_pamphi);
   void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
@@ -829,6 +834,14 @@ int create_periodic_md(smpc_ctx* ctx) {
     a.err = ctx->d_err;
     ctx->pmd.push_back(a);
   }
+  {
+    std::vector<int*> rows(ctx->n_rep, nullptr);
+    for (const smpc::PmdArgs& p : ctx->pmd) rows[p.rep] = p.nlist;
+    CU(dalloc(&ctx->d_rows_by_rep, rows.size()));
+    CU(cudaMemcpy(ctx->d_rows_by_rep, rows.data(), rows.size() * sizeof(int*),
+                  cudaMemcpyHostToDevice));
+    CU(dalloc(&ctx->d_stress, 12 * static_cast<size_t>(ctx->n_rep)));
+  }
   if (!ctx->pmd.empty()) {
     CU(cudaMalloc(&ctx->d_pamphi, M));
     CU(cudaMemset(ctx->d_pamphi, 0, M));
@@ -933,6 +946,7 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
   std::vector<Tile> col = make_tiles(ctx->reps, true, ct);
   ctx->h_tmp_tiles = make_tiles(ctx->reps, true, smpc::temperature_cells_per_tile());
   ctx->n_bin_tiles = static_cast<int>(bin.size());
+  for (const Tile& t : bin) ctx->bin_tile_rep.push_back(t.rep);
   ctx->n_col_tiles = static_cast<int>(col.size());
   bool ok = dalloc(&ctx->d_reps, n_rep) == cudaSuccess && dalloc(&ctx->d_dyn, n_rep) == cudaSuccess &&
             dalloc(&ctx->d_bin_tiles, bin.size()) == cudaSuccess &&
@@ -1726,6 +1740,58 @@ int smpc_fourier_modes(smpc_ctx* ctx, int rep, double box_length, double* out18)
     out18[q] = n > 0 ? s / n : 0.0;
   }
   for (int j = 0; j < 3; ++j) out18[6 * j + 2 * j] = out18[6 * j + 2 * j + 1] = 0.0;
+  return SMPC_OK;
+}
+
+int smpc_pressure_tensor_all(smpc_ctx* ctx, double* out) {
+  if (!ctx || !out) return SMPC_E_ARG;
+  if (ctx->total_mono > 0 && !ctx->md_ready)
+    return fail(ctx, SMPC_E_STATE, "smpc_init_md not called (the virial walks the Verlet lists)");
+  cudaSetDevice(ctx->device);
+  if (int rc = ana_partials(ctx, 6 * static_cast<size_t>(std::max(ctx->n_bin_tiles, 1)))) return rc;
+  if (ctx->opt.precision == SMPC_FP64) {
+    smpc::launch_kinetic_tensor<double>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps,
+                                        static_cast<const double*>(ctx->d_rec[ctx->cur]),
+                                        ctx->d_ana_part, ctx->st);
+    smpc::launch_mono_stress<double>(ctx->d_reps, ctx->d_dyn, ctx->n_rep,
+                                     static_cast<const double*>(ctx->d_mpos),
+                                     static_cast<const double*>(ctx->d_mvel), ctx->d_nlist,
+                                     ctx->d_ncount, static_cast<int>(ctx->total_mono),
+                                     ctx->d_rows_by_rep, ctx->max_nb, ctx->d_bond_start,
+                                     ctx->d_bonds, ctx->d_stress, ctx->st);
+  } else {
+    smpc::launch_kinetic_tensor<float>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps,
+                                       static_cast<const float*>(ctx->d_rec[ctx->cur]),
+                                       ctx->d_ana_part, ctx->st);
+    smpc::launch_mono_stress<float>(ctx->d_reps, ctx->d_dyn, ctx->n_rep,
+                                    static_cast<const float*>(ctx->d_mpos),
+                                    static_cast<const float*>(ctx->d_mvel), ctx->d_nlist,
+                                    ctx->d_ncount, static_cast<int>(ctx->total_mono),
+                                    ctx->d_rows_by_rep, ctx->max_nb, ctx->d_bond_start,
+                                    ctx->d_bonds, ctx->d_stress, ctx->st);
+  }
+  CU(cudaGetLastError());
+  std::vector<double> part(6 * static_cast<size_t>(ctx->n_bin_tiles));
+  std::vector<double> mono(12 * static_cast<size_t>(ctx->n_rep));
+  if (!part.empty())
+    CU(cudaMemcpyAsync(part.data(), ctx->d_ana_part, part.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaMemcpyAsync(mono.data(), ctx->d_stress, mono.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CU(cudaStreamSynchronize(ctx->st));
+  // the slot tiles' partial sums, tile by tile into their replicas
+  std::vector<double> kin(6 * static_cast<size_t>(ctx->n_rep), 0.0);
+  for (int t = 0; t < ctx->n_bin_tiles; ++t)
+    for (int k = 0; k < 6; ++k)
+      kin[6 * ctx->bin_tile_rep[t] + k] += part[6 * static_cast<size_t>(t) + k];
+  for (int q = 0; q < ctx->n_rep; ++q) {
+    const RepInfo& ri = ctx->reps[q];
+    const double V = static_cast<double>(ri.L[0]) * ri.L[1] * ri.L[2];
+    for (int k = 0; k < 6; ++k) {
+      out[12 * q + k] = (kin[6 * q + k] + mono[12 * q + k]) / V;
+      out[12 * q + 6 + k] = mono[12 * q + 6 + k] / V;
+    }
+  }
   return SMPC_OK;
 }
 

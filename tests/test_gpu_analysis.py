@@ -4,14 +4,14 @@ states."""
 import numpy as np
 import pytest
 
-from starpolymersmd_gb300 import analysis, capi
+from starpolymersmd_gb300 import analysis, capi, system
 from tests import gpu_helpers as H
 
 pytestmark = pytest.mark.gpu
 
 
 def _solvent_context(precision, L=6, n_c=5, shear=0.2):
-    star, fpos, fvel = H.small_star_system(L=L, n_c=n_c, shear=shear, seed=7)
+    fpos, fvel = system.uniform_fluid((L, L, L), n_c, 1.0, np.random.default_rng(7))
     return H.context_for(None, fpos, fvel, L, 1.0, shear, 1, precision=precision,
                          rng=capi.RNG_PHILOX, seed=3)
 
