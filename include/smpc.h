@@ -47,6 +47,12 @@ enum { SMPC_RNG_INJECT = 0, SMPC_RNG_PHILOX = 1 };
 enum { SMPC_POT_REF4824 = 0, SMPC_POT_LJ126 = 1 };
 enum { SMPC_MONOBIN_REFERENCE = 0, SMPC_MONOBIN_WRAPPED = 1 };
 enum { SMPC_DELRX_REFERENCE = 0, SMPC_DELRX_PHYSICAL = 1 };
+/* MD thermostats. NONE: Thermostat_None (Thermostat_None.cpp:21-38), the
+ * integrator of MPC runs. ANDERSEN: AndersenStochastic (Andersen_stochastic.cpp:
+ * 30-59): after each substep every bead, with probability andersen_nu * md_dt,
+ * gets new velocity components from N(0, sqrt(kT / m)); draws from Philox on
+ * the replica's seed (the reference draws from its global Rand stream). */
+enum { SMPC_MDTHERMO_NONE = 0, SMPC_MDTHERMO_ANDERSEN = 1 };
 /* Replica flags. SMPC_REPLICA_PERIODIC_MD: the box's monomers (any number of
  * stars) interact through the Lees-Edwards minimum image and are kept in the
  * primary box, with Verlet lists on a periodic cell grid and a rebuild
@@ -87,6 +93,8 @@ typedef struct {
   int device;             /* CUDA device ordinal */
   int angular_momentum;   /* 1: angular-momentum-conserving collision in cells of more than two
                              particles (MPC.cpp:260-269, 324-374; MPC(..., angular_mom)) */
+  int md_thermostat;      /* SMPC_MDTHERMO_*: thermostat of the MD substeps (MPC-off runs) */
+  double andersen_nu;     /* collision frequency of SMPC_MDTHERMO_ANDERSEN */
 } smpc_options;
 
 /* Draws injected for one collision of every replica (reference parity):

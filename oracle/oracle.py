@@ -75,6 +75,7 @@ def _oracle_lib():
             "orc_run": [P, C.c_long, C.c_long, C.c_double, C.c_int],
             "orc_cell_counts": [P, P, P], "orc_philox4x32_10": [P, P, P],
             "orc_set_periodic_md": [P, C.c_double], "orc_periodic_forces": [P, C.c_int, P],
+            "orc_set_andersen": [P, C.c_double, C.c_uint64],
         }.items():
             getattr(lib, name).argtypes = args
             getattr(lib, name).restype = None
@@ -168,6 +169,10 @@ class OracleSystem:
     def set_periodic_md(self, h):
         """Periodic many-molecule MD (before init_md; needs mono_wrap=1)."""
         self.lib.orc_set_periodic_md(self.h, float(h))
+
+    def set_andersen(self, nu, seed):
+        """Andersen stochastic thermostat after every MD step."""
+        self.lib.orc_set_andersen(self.h, float(nu), int(seed))
 
     def periodic_forces(self, grid):
         out = np.zeros((self.n_mono, 3))

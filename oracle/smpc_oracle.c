@@ -94,6 +94,12 @@ struct smpc_orc {
   unsigned char* adj_anchor;
   int pmd_force_grid; /* test hook: take the grid path whatever the size */
 
+  /* Andersen stochastic thermostat (orc_set_andersen) */
+  int andersen;
+  double andersen_nu;
+  uint64_t andersen_seed;
+  uint64_t md_step;
+
   int err;
 };
 
@@ -579,6 +585,41 @@ void orc_init_md(smpc_orc* o) {
 }
 
 /* Thermostat_None::propagate (Thermostat_None.cpp:21-38). */
+/* AndersenStochastic::propagate (Andersen_stochastic.cpp:30-59): the kick is
+ * grouped as F (dt/2 / m); after the second kick each monomer, with
+ * probability nu dt, gets every velocity component from N(0, sqrt(kT / m)).
+ * Draws restated from the GPU's layout: Philox on the seed, counter
+ * (0x80000000 | monomer, MD step, k); k = 0: trigger, u1; k = 1: u2, u3;
+ * k = 2: u4; Box-Muller (u1, u2) -> x, y and (u3, u4) -> z. */
+void orc_set_andersen(smpc_orc* o, double nu, uint64_t seed) {
+  o->andersen = 1;
+  o->andersen_nu = nu;
+  o->andersen_seed = seed;
+}
+
+static inline double md_kick(const smpc_orc* o, double f, double m, double dth) {
+  return o->andersen ? f * (dth / m) : (f / m) * dth;
+}
+
+static void andersen_step(smpc_orc* o) {
+  const double p = o->andersen_nu * o->p.md_dt;
+  const double sigma = sqrt(o->p.kT);
+  for (int i = 0; i < o->n_m; ++i) {
+    const uint32_t c = 0x80000000u | (uint32_t)i;
+    double t, u1, u2, u3, u4;
+    philox_block(o->andersen_seed, c, o->md_step, 0u, &t, &u1);
+    if (!(t < p)) continue;
+    philox_block(o->andersen_seed, c, o->md_step, 1u, &u2, &u3);
+    philox_block(o->andersen_seed, c, o->md_step, 2u, &u4, NULL);
+    const double s = sigma / sqrt(o->mm[i]);
+    const double r1 = sqrt(-2.0 * log(u1)), r2 = sqrt(-2.0 * log(u3));
+    const double two_pi = 6.283185307179586476925286766559;
+    o->mv[3 * i] = s * (r1 * cos(two_pi * u2));
+    o->mv[3 * i + 1] = s * (r1 * sin(two_pi * u2));
+    o->mv[3 * i + 2] = s * (r2 * cos(two_pi * u4));
+  }
+}
+
 static void pmd_propagate(smpc_orc* o, int calc_epot);
 
 void orc_propagate(smpc_orc* o, int calc_epot) {
@@ -590,14 +631,16 @@ void orc_propagate(smpc_orc* o, int calc_epot) {
   const double dth = dt * 0.50;
   for (int i = 0; i < o->n_m; ++i) {
     for (int d = 0; d < 3; ++d) {
-      o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
+      o->mv[3 * i + d] += md_kick(o, o->mf[3 * i + d], o->mm[i], dth);
       o->mx[3 * i + d] += o->mv[3 * i + d] * dt;
     }
   }
   check_verlet(o);
   forces_verlet(o, calc_epot);
   for (int i = 0; i < o->n_m; ++i)
-    for (int d = 0; d < 3; ++d) o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
+    for (int d = 0; d < 3; ++d) o->mv[3 * i + d] += md_kick(o, o->mf[3 * i + d], o->mm[i], dth);
+  if (o->andersen) andersen_step(o);
+  o->md_step++;
 }
 
 double orc_epot(const smpc_orc* o) {
@@ -1262,12 +1305,14 @@ static void pmd_propagate(smpc_orc* o, int calc_epot) {
   const double dl = pmd_next_delrx(o);
   for (int i = 0; i < o->n_m; ++i) {
     for (int d = 0; d < 3; ++d) {
-      o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
+      o->mv[3 * i + d] += md_kick(o, o->mf[3 * i + d], o->mm[i], dth);
       o->mx[3 * i + d] += o->mv[3 * i + d] * dt;
     }
     pmd_wrap(o, dl, o->mx + 3 * i, o->mv + 3 * i);
   }
   pmd_forces(o, dl, calc_epot);
   for (int i = 0; i < o->n_m; ++i)
-    for (int d = 0; d < 3; ++d) o->mv[3 * i + d] += (o->mf[3 * i + d] / o->mm[i]) * dth;
+    for (int d = 0; d < 3; ++d) o->mv[3 * i + d] += md_kick(o, o->mf[3 * i + d], o->mm[i], dth);
+  if (o->andersen) andersen_step(o);
+  o->md_step++;
 }

@@ -84,6 +84,8 @@ void orc_init_md(smpc_orc* o);
  * wrapped into the primary box with the v_x jump, no recentring; MD step t uses
  * the delrx the next MPC::step(t, h) call gives. */
 void orc_set_periodic_md(smpc_orc* o, double h);
+/* Andersen stochastic thermostat after every MD step (MPC-off runs). */
+void orc_set_andersen(smpc_orc* o, double nu, uint64_t seed);
 /* Periodic forces at the current positions and delrx into out[3 n_mono]: by
  * the cell grid that large boxes use (force_grid = 1) or by the loop over all
  * monomers (0). The state is not changed. */

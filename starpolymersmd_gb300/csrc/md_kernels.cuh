@@ -109,6 +109,35 @@ __device__ __forceinline__ R pair_pot(int pot, bool bb, R r2, R lambda) {
   return R(0);
 }
 
+// Andersen stochastic thermostat of the MPC-off runs
+// (AndersenStochastic::propagate, Thermostats/Andersen_stochastic.cpp:30-59):
+// after the second half kick each bead, with probability nu dt, gets every
+// velocity component drawn from N(0, sqrt(kT / m)). Draws: Philox on the
+// replica's seed, counter (ANDERSEN_STREAM | bead, MD substep, k): k = 0 gives
+// the trigger uniform and u1, k = 1 u2 and u3, k = 2 u4; Box-Muller pairs
+// (u1, u2) -> x, y and (u3, u4) -> z.
+constexpr uint32_t ANDERSEN_STREAM = 0x80000000u;
+
+template <typename R>
+__device__ __forceinline__ void andersen_draw(unsigned long long seed, int bead,
+                                              unsigned long long md_step, R p, R sigma, R m,
+                                              R* v) {
+  const uint32_t c = ANDERSEN_STREAM | static_cast<uint32_t>(bead);
+  const Uniform2<R> a = philox_uniforms<R>(seed, c, md_step, 0u);
+  if (!(a.a < p)) return;
+  const Uniform2<R> b = philox_uniforms<R>(seed, c, md_step, 1u);
+  const Uniform2<R> d = philox_uniforms<R>(seed, c, md_step, 2u);
+  const R two_pi = R(6.283185307179586476925286766559);
+  const R s = sigma / r_sqrt(m);
+  const R r1 = r_sqrt(R(-2) * r_log(a.b)), r2 = r_sqrt(R(-2) * r_log(b.b));
+  R s1, c1, s2, c2;
+  r_sincos(two_pi * b.a, &s1, &c1);
+  r_sincos(two_pi * d.a, &s2, &c2);
+  v[0] = s * (r1 * c1);
+  v[1] = s * (r1 * s1);
+  v[2] = s * (r2 * c2);
+}
+
 // FENE (Potentials.h:24-55): anchor bonds (core) use R0^2 = 20.25.
 template <typename R>
 __device__ __forceinline__ R fene_force(bool anchor, R r2) {
@@ -139,6 +168,8 @@ struct MdArgs {
   int core_relative;       // fast path: displacements measured relative to the core's
   ErrorState* err;
   const int* order;        // replica of each CTA (largest first), or null: CTA b = replica b
+  int andersen;            // Andersen stochastic thermostat (MPC-off runs)
+  double andersen_nu;      // its collision frequency
 };
 
 // Cell key of a position on a grid of side rv: three 10-bit fields
@@ -184,6 +215,7 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
   const R rv2 = static_cast<R>(ri.r_verlet) * static_cast<R>(ri.r_verlet);
   const R lim = (static_cast<R>(ri.r_verlet) - static_cast<R>(ri.r_cut)) * R(0.5);
   const int pot = ri.potential;
+  const unsigned long long md_step0 = a.dyn[r].md_step;  // thread 0 adds n_steps at the end
 
   R x[MPT][3], v[MPT][3], f[MPT][3], xv[MPT][3], m[MPT];
   int anc[MPT];
@@ -223,7 +255,7 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
         const int i = slot + k * NT;
         if (i < n) {
           for (int d = 0; d < 3; ++d) {
-            v[k][d] += (f[k][d] / m[k]) * dth;
+            v[k][d] += a.andersen ? f[k][d] * (dth / m[k]) : (f[k][d] / m[k]) * dth;
             x[k][d] += v[k][d] * dt;
           }
           if (lead) { sx[i] = x[k][0]; sy[i] = x[k][1]; sz[i] = x[k][2]; }
@@ -378,8 +410,14 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
       }
       if (i < n) {
         f[k][0] = F0; f[k][1] = F1; f[k][2] = F2;
-        if (a.n_steps > 0)
-          for (int d = 0; d < 3; ++d) v[k][d] += (f[k][d] / m[k]) * dth;  // second half-kick
+        if (a.n_steps > 0) {
+          for (int d = 0; d < 3; ++d)  // second half-kick
+            v[k][d] += a.andersen ? f[k][d] * (dth / m[k]) : (f[k][d] / m[k]) * dth;
+          if (a.andersen)
+            andersen_draw<R>(ri.seed, i, md_step0 + static_cast<unsigned long long>(step),
+                             static_cast<R>(a.andersen_nu * ri.md_dt),
+                             r_sqrt(static_cast<R>(ri.kT)), m[k], v[k]);
+        }
       }
     }
     __syncthreads();  // positions are rewritten by the next drift
@@ -409,7 +447,10 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
       a.dyn[r].epot = s;
     }
   }
-  if (threadIdx.x == 0) a.dyn[r].verlet_rebuilds += rebuilds;
+  if (threadIdx.x == 0) {
+    a.dyn[r].verlet_rebuilds += rebuilds;
+    if (a.n_steps > 0) a.dyn[r].md_step = md_step0 + static_cast<unsigned long long>(a.n_steps);
+  }
 }
 
 }  // namespace smpc

@@ -94,6 +94,8 @@ struct PmdArgs {
   const int* bond_start;
   const int2* bonds;
   ErrorState* err;
+  int andersen;        // Andersen stochastic thermostat (MPC-off runs), md_kernels.cuh
+  double andersen_nu;
 };
 
 // delrx one MD step later: one iteration of k_cycle_begin's loop
@@ -210,17 +212,24 @@ __device__ __forceinline__ bool pmd_last_block(const PmdArgs& a) {
 // One bead's half kick (with the force f), drift, Lees-Edwards wrap and
 // peculiar displacement (Thermostat_None.cpp:22-27, MPC.cpp:421-429).
 template <typename R>
+__device__ __forceinline__ R pmd_kick(R f, R m, R dth, int andersen) {
+  // Thermostat_None.cpp:24; Andersen_stochastic.cpp:33 groups it as f (dt/2 / m)
+  return andersen ? f * (dth / m) : (f / m) * dth;
+}
+
+template <typename R>
 __device__ __forceinline__ void pmd_drift_bead(const RepInfo& ri, const PmdBox<R>& b, R4<R>& x,
-                                               R4<R>& v, R4<R>& u, R f0, R f1, R f2) {
+                                               R4<R>& v, R4<R>& u, R f0, R f1, R f2,
+                                               int andersen) {
   const R dt = static_cast<R>(ri.md_dt), dth = dt * R(0.50);
   const R y0 = x.y;
-  v.x += (f0 / x.w) * dth;
+  v.x += pmd_kick(f0, x.w, dth, andersen);
   x.x += v.x * dt;
   u.x += (v.x - static_cast<R>(ri.shear) * y0) * dt;
-  v.y += (f1 / x.w) * dth;
+  v.y += pmd_kick(f1, x.w, dth, andersen);
   x.y += v.y * dt;
   u.y += v.y * dt;
-  v.z += (f2 / x.w) * dth;
+  v.z += pmd_kick(f2, x.w, dth, andersen);
   x.z += v.z * dt;
   u.z += v.z * dt;
 }
@@ -274,7 +283,7 @@ __global__ void __launch_bounds__(PMD_NT)
     R4<R> x = ld4_rw(mpos, g), v = ld4_rw(mvel, g), u = ld4_rw(mdisp, g);
     if (drift) {
       const R4<R> f = ld4_rw(mfrc, g);
-      pmd_drift_bead(ri, b, x, v, u, f.x, f.y, f.z);
+      pmd_drift_bead(ri, b, x, v, u, f.x, f.y, f.z, a.andersen);
     }
     pmd_wrap(ri, b, x, v);
     st4(mpos, g, x);
@@ -479,14 +488,22 @@ __global__ void __launch_bounds__(PMD_NT)
     v = ld4_rw(mvel, g);
     if (kick) {  // second half kick (Thermostat_None.cpp:33-37)
       const R dth = static_cast<R>(ri.md_dt) * R(0.50);
-      v.x += (F0 / x.w) * dth;
-      v.y += (F1 / x.w) * dth;
-      v.z += (F2 / x.w) * dth;
+      v.x += pmd_kick(F0, x.w, dth, a.andersen);
+      v.y += pmd_kick(F1, x.w, dth, a.andersen);
+      v.z += pmd_kick(F2, x.w, dth, a.andersen);
+      if (a.andersen) {
+        R w[3] = {v.x, v.y, v.z};
+        andersen_draw<R>(ri.seed, i, dyn[a.rep].md_step, static_cast<R>(a.andersen_nu * ri.md_dt),
+                         r_sqrt(static_cast<R>(ri.kT)), x.w, w);
+        v.x = w[0];
+        v.y = w[1];
+        v.z = w[2];
+      }
     }
     if (drift_next) {
       const PmdBox<R> b1 = pmd_box<R>(ri, a.dl_slot[s ^ 1]);
       R4<R> u = ld4_rw(mdisp, g);
-      pmd_drift_bead(ri, b1, x, v, u, F0, F1, F2);
+      pmd_drift_bead(ri, b1, x, v, u, F0, F1, F2, a.andersen);
       pmd_wrap(ri, b1, x, v);
       st4(pout, g, x);
       st4(mdisp, g, u);
@@ -504,6 +521,7 @@ __global__ void __launch_bounds__(PMD_NT)
   // the last block to get here closes the substep (no block waits for another)
   if (!pmd_last_block(a)) return;
   RepDyn& dn = dyn[a.rep];
+  if (kick) dn.md_step += 1;  // the thermostat's draws of this substep are done
   if (a.flag[s] != 0) {
     *a.delrx_build = a.dl_slot[s];
     a.flag[3] = 0;

@@ -254,6 +254,8 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   a.core_relative = ctx->opt.strict_cells ? 0 : 1;
   a.err = ctx->d_err;
   a.order = ctx->d_md_order;
+  a.andersen = ctx->opt.md_thermostat == SMPC_MDTHERMO_ANDERSEN ? 1 : 0;
+  a.andersen_nu = ctx->opt.andersen_nu;
   smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
                      static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->var_md,
                      ctx->st);
@@ -832,6 +834,8 @@ int create_periodic_md(smpc_ctx* ctx) {
     a.bond_start = ctx->d_bond_start;
     a.bonds = ctx->d_bonds;
     a.err = ctx->d_err;
+    a.andersen = ctx->opt.md_thermostat == SMPC_MDTHERMO_ANDERSEN ? 1 : 0;
+    a.andersen_nu = ctx->opt.andersen_nu;
     ctx->pmd.push_back(a);
   }
   {
@@ -879,6 +883,9 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
     return code;
   };
   if (opt->precision != SMPC_FP64 && opt->precision != SMPC_FP32) return bail(SMPC_E_ARG, "precision");
+  if (opt->md_thermostat != SMPC_MDTHERMO_NONE &&
+      (opt->md_thermostat != SMPC_MDTHERMO_ANDERSEN || !(opt->andersen_nu >= 0)))
+    return bail(SMPC_E_ARG, "md thermostat");
   if (cudaSetDevice(ctx->device) != cudaSuccess) return bail(SMPC_E_CUDA, "cudaSetDevice");
   long long cells = 0, slots = 0, mono = 0;
   for (int r = 0; r < n_rep; ++r) {

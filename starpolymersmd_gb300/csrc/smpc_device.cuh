@@ -79,6 +79,7 @@ struct RepDyn {
   double epot;           // last potential energy (calc_epot substeps)
   int verlet_rebuilds;
   int pad2;
+  unsigned long long md_step;    // MD substeps so far (Philox counter of the MD thermostat)
 };
 
 // Single-precision constants of one replica for the current collision,

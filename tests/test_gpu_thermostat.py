@@ -1,0 +1,104 @@
+"""Andersen stochastic thermostat of MPC-off runs (SMPC_MDTHERMO_ANDERSEN)
+against the oracle's restatement of AndersenStochastic::propagate
+(Andersen_stochastic.cpp:30-59) on the same Philox draws, for one star and
+for a periodic many-star box, and its temperature on a long FP32 run."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from starpolymersmd_gb300 import capi, system
+from tests import gpu_helpers as H
+from tests.test_gpu_periodic import _solution
+
+pytestmark = pytest.mark.gpu
+
+NU, SEED = 5.0, 41
+
+
+def test_fp64_andersen_one_star_matches_oracle():
+    L = 12
+    star, fpos, fvel = H.small_star_system(L=L, seed=6)
+    fpos = fvel = np.zeros((0, 3))
+    n = star.n
+    o = orc.OracleSystem((L, L, L), 1.0, 0.0, 1000, 0, n, mol_start=[0, n])
+    o.set_monomers(star.pos, star.vel, np.zeros_like(star.pos), np.full(n, star.mass),
+                   star.amphi, star.anchor)
+    o.set_bonds(star.bond_src, star.bond_dst)
+    o.set_andersen(NU, SEED)
+    o.init_md()
+    rep = dict(L=(L, L, L), n_fluid=0, n_mono=n, mol0_size=n, kT=1.0, shear=0.0, h=0.1,
+               md_dt=0.01, seed=SEED, **{"lambda": 1.0})
+    with capi.Context([rep], precision=capi.FP64, rng=capi.RNG_PHILOX, step_update=1000,
+                      md_thermostat=capi.MDTHERMO_ANDERSEN, andersen_nu=NU) as ctx:
+        ctx.set_monomers(0, star.pos, star.vel, np.zeros_like(star.pos), np.full(n, star.mass),
+                         star.amphi, star.anchor)
+        ctx.set_bonds(0, star.bond_src, star.bond_dst)
+        ctx.init_md()
+        before = ctx.get_monomers(0)[1].copy()
+        for _ in range(40):
+            o.propagate(False)
+        ctx.md_substeps(25)
+        ctx.md_substeps(15)  # the draws follow the MD step counter across calls
+        ctx.raise_on_device_error()
+        mp, mv, mf = ctx.get_monomers(0)
+        op, ov, of = o.get_monomers()
+        H.close64(mp, op, rtol=1e-11)
+        H.close64(mv, ov, rtol=1e-11)
+        H.close64(mf, of, rtol=1e-11)
+        # with nu dt = 0.05 most beads were redrawn at least once
+        assert np.mean(np.any(mv != before, axis=1)) > 0.5
+
+
+def test_fp64_andersen_periodic_box_matches_oracle():
+    L = 12
+    sol = _solution(seed=8)
+    fpos = np.zeros((0, 3))
+    su, md_dt = 1000, 0.005
+    o = orc.OracleSystem((L, L, L), 1.0, 0.3, su, 0, sol.n, mol_start=sol.mol_start, md_dt=md_dt,
+                         r_verlet=1.8, delrx_dt_scale=1.0 / su, mono_wrap=1)
+    o.set_monomers(sol.pos, sol.vel, np.zeros_like(sol.pos), sol.mass, sol.amphi, sol.anchor)
+    o.set_bonds(sol.bond_src, sol.bond_dst)
+    o.set_periodic_md(su * md_dt)
+    o.set_andersen(NU, SEED)
+    o.init_md()
+    rep = dict(L=(L, L, L), n_fluid=0, n_mono=sol.n, mol0_size=sol.stars[0].n, kT=1.0,
+               shear=0.3, h=su * md_dt, md_dt=md_dt, seed=SEED, r_verlet=1.8,
+               flags=capi.REPLICA_PERIODIC_MD, **{"lambda": 1.0})
+    with capi.Context([rep], precision=capi.FP64, rng=capi.RNG_PHILOX, step_update=su,
+                      mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL,
+                      md_thermostat=capi.MDTHERMO_ANDERSEN, andersen_nu=NU) as ctx:
+        ctx.set_monomers(0, sol.pos, sol.vel, np.zeros_like(sol.pos), sol.mass, sol.amphi,
+                         sol.anchor)
+        ctx.set_bonds(0, sol.bond_src, sol.bond_dst)
+        ctx.init_md()
+        for t in range(1, 61):
+            o.propagate(False)
+            o.mpc_step(t, su * md_dt)  # delrx advance only
+        ctx.md_substeps(60)
+        ctx.raise_on_device_error()
+        for x, y in zip(ctx.get_monomers(0), o.get_monomers()):
+            H.close64(x, y, rtol=1e-11)
+
+
+def test_fp32_andersen_holds_the_temperature():
+    L, kT = 16, 1.5
+    sol = system.star_solution(6, 4, 8, 0.5, 5.0, 0.2, (L, L, L), np.random.default_rng(12))
+    rep = dict(L=(L, L, L), n_fluid=0, n_mono=sol.n, mol0_size=sol.stars[0].n, kT=kT, shear=0.0,
+               h=10.0, md_dt=0.01, seed=SEED, potential=capi.POT_LJ126, r_cut=2.5,
+               r_verlet=2.8, flags=capi.REPLICA_PERIODIC_MD, **{"lambda": 1.0})
+    with capi.Context([rep], precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=1000,
+                      mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL,
+                      strict_cells=0, md_thermostat=capi.MDTHERMO_ANDERSEN,
+                      andersen_nu=2.0) as ctx:
+        ctx.set_monomers(0, sol.pos, sol.vel, np.zeros_like(sol.pos), sol.mass, sol.amphi,
+                         sol.anchor)
+        ctx.set_bonds(0, sol.bond_src, sol.bond_dst)
+        ctx.init_md()
+        ctx.md_substeps(1000)
+        temps = []
+        for _ in range(20):
+            ctx.md_substeps(50)
+            _, v, _ = ctx.get_monomers(0)
+            temps.append((sol.mass[:, None] * v * v).sum() / (3 * sol.n))
+        ctx.raise_on_device_error()
+        assert abs(np.mean(temps) / kT - 1.0) < 0.05
