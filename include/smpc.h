@@ -51,7 +51,8 @@ enum { SMPC_DELRX_REFERENCE = 0, SMPC_DELRX_PHYSICAL = 1 };
  * integrator of MPC runs. ANDERSEN: AndersenStochastic (Andersen_stochastic.cpp:
  * 30-59): after each substep every bead, with probability andersen_nu * md_dt,
  * gets new velocity components from N(0, sqrt(kT / m)); draws from Philox on
- * the replica's seed (the reference draws from its global Rand stream). */
+ * the replica's seed (the reference draws from its global Rand stream), or the
+ * resets come from the host (smpc_stage_andersen). */
 enum { SMPC_MDTHERMO_NONE = 0, SMPC_MDTHERMO_ANDERSEN = 1 };
 /* Replica flags. SMPC_REPLICA_PERIODIC_MD: the box's monomers (any number of
  * stars) interact through the Lees-Edwards minimum image and are kept in the
@@ -138,6 +139,18 @@ int smpc_init_md(smpc_ctx* ctx);
  * (Thermostat_None.cpp:21-38); the potential energy of the last substep is
  * kept when calc_epot != 0 (Box::print_Epot, Box.cpp:605-613). */
 int smpc_md_substeps(smpc_ctx* ctx, int n, int calc_epot);
+/* The Andersen resets of replica rep's next n_steps MD substeps, given by the
+ * host in place of the device's draws: in substep s (0-based) of the next
+ * smpc_md_substeps call (which must have n == n_steps), replica-local monomer
+ * mono[e] gets the velocity vel[3e .. 3e+2] after the second half kick, for
+ * e in [step_start[s], step_start[s + 1]). The reference's loop of
+ * AndersenStochastic::propagate (Andersen_stochastic.cpp:49-58: one
+ * Rand::real_uniform() per monomer, three Rand::real_normal(0, sigma) when it
+ * is below nu * dt) runs on the host, so a drop-in replays the reference's
+ * global Rand stream exactly. Needs SMPC_MDTHERMO_ANDERSEN; not for periodic
+ * replicas (SMPC_E_UNSUPPORTED). Replicas without staged resets draw. */
+int smpc_stage_andersen(smpc_ctx* ctx, int rep, int n_steps, const int* step_start,
+                        const int* mono, const double* vel);
 /* MPC::step(t, dt) for every replica (MPC.cpp:116-142): delrx advance on every
  * call, a collision when t % step_update == 0. inj may be NULL only in
  * Philox mode. */

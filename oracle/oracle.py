@@ -76,6 +76,7 @@ def _oracle_lib():
             "orc_cell_counts": [P, P, P], "orc_philox4x32_10": [P, P, P],
             "orc_set_periodic_md": [P, C.c_double], "orc_periodic_forces": [P, C.c_int, P],
             "orc_set_andersen": [P, C.c_double, C.c_uint64],
+            "orc_stage_andersen": [P, C.c_int, P, P],
         }.items():
             getattr(lib, name).argtypes = args
             getattr(lib, name).restype = None
@@ -174,6 +175,14 @@ class OracleSystem:
         """Andersen stochastic thermostat after every MD step."""
         self.lib.orc_set_andersen(self.h, float(nu), int(seed))
 
+    def stage_andersen(self, mono, vel):
+        """Velocity resets of the next MD step in place of the Philox draws:
+        monomer ``mono[k]`` gets ``vel[k]`` after the second half kick."""
+        mono = np.ascontiguousarray(mono, dtype=np.int32)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        self._keep_andersen = (mono, vel)
+        self.lib.orc_stage_andersen(self.h, len(mono), _p(mono), _p(vel))
+
     def periodic_forces(self, grid):
         out = np.zeros((self.n_mono, 3))
         self.lib.orc_periodic_forces(self.h, int(grid), _p(out))
@@ -254,6 +263,7 @@ class RefSystem:
             "ref_destroy": [P], "ref_box_size": [P, P],
             "ref_add_star": [P, C.c_uint, C.c_uint, C.c_uint, C.c_double],
             "ref_make_thermostat": [P, C.c_double], "ref_mpc_initialize": [P],
+            "ref_make_andersen": [P, C.c_double, C.c_double, C.c_double],
             "ref_get_fluid": [P, P, P], "ref_set_fluid": [P, P, P],
             "ref_get_monomers": [P, P, P, P, P, P, P], "ref_set_monomers": [P, P, P],
             "ref_propagate": [P, C.c_int], "ref_mpc_step": [P, C.c_long, C.c_double],
@@ -329,6 +339,10 @@ class RefSystem:
 
     def make_thermostat(self, dt):
         self.lib.ref_make_thermostat(self.h, dt)
+
+    def make_andersen(self, dt, T, nu):
+        """AndersenStochastic{box, dt, T, nu} as the propagating thermostat."""
+        self.lib.ref_make_andersen(self.h, dt, T, nu)
 
     def mpc_initialize(self):
         self.lib.ref_mpc_initialize(self.h)
@@ -431,6 +445,31 @@ class RefSystem:
 
     def reseed(self, seed):
         self.lib.rand_tape_reseed(seed)
+
+
+def decode_andersen_tape(vals, kinds, masses, nu_dt, sigma):
+    """Velocity resets of one AndersenStochastic::propagate from its draws.
+
+    Draw order of Andersen_stochastic.cpp:49-58: for every monomer in
+    molecule order one uniform; when it is below nu * dt, three normals
+    N(0, sigma) (mass 1) or N(0, sigma / sqrt(m)) for x, y, z, each formed as
+    Rand::real_normal(mean, std) does (Rand.cpp:16-18: z * std + mean).
+    Returns (monomer indices, velocities[n, 3]).
+    """
+    idx, vel = [], []
+    k = 0
+    for i, m in enumerate(masses):
+        assert kinds[k] == 1, "expected the trigger uniform"
+        u = vals[k]
+        k += 1
+        if u < nu_dt:
+            assert all(kinds[k + d] == 3 for d in range(3)), "expected three normals"
+            std = sigma if m == 1.0 else sigma / np.sqrt(m)
+            vel.append([vals[k + d] * std + 0.0 for d in range(3)])
+            idx.append(i)
+            k += 3
+    assert k == len(vals), (k, len(vals))
+    return np.array(idx, dtype=np.int32), np.array(vel, dtype=np.float64).reshape(-1, 3)
 
 
 def decode_collision_tape(vals, kinds, counts, shift_order):

@@ -14,6 +14,7 @@
 
 #include "Box.h"
 #include "MPC.h"
+#include "Andersen_stochastic.h"
 #include "Thermostat_None.h"
 #include "Velocity_x.h"
 #include "rand_tape.h"
@@ -35,6 +36,8 @@ struct RefSys {
   Box* box = nullptr;
   HarnessMPC* mpc = nullptr;
   Thermostat_None* thermo = nullptr;
+  AndersenStochastic* andersen = nullptr;
+  Thermostat* active = nullptr;  // the one propagate() drives
 };
 
 int g_probe_counter = 0;
@@ -54,6 +57,7 @@ RefSys* ref_create(int Lx, int Ly, int Lz, double T, double lambda, int Nc, doub
 
 void ref_destroy(RefSys* s) {
   delete s->thermo;
+  delete s->andersen;
   delete s->mpc;
   delete s->box;
   delete s;
@@ -70,6 +74,15 @@ void ref_add_star(RefSys* s, unsigned A, unsigned B, unsigned arms, double mass)
 void ref_make_thermostat(RefSys* s, double dt) {
   delete s->thermo;
   s->thermo = new Thermostat_None{*s->box, dt};
+  s->active = s->thermo;
+}
+
+// The MPC-off integrator of star-polymers.cpp:387 (AndersenStochastic{box,
+// StepSize, Temperature, 0.1}) with its temperature and frequency free.
+void ref_make_andersen(RefSys* s, double dt, double T, double nu) {
+  delete s->andersen;
+  s->andersen = new AndersenStochastic{*s->box, dt, T, nu};
+  s->active = s->andersen;
 }
 
 void ref_mpc_initialize(RefSys* s) { s->mpc->initialize(); }
@@ -166,7 +179,7 @@ int ref_get_bonds(RefSys* s, int* src, int* dst) {
   return nb;
 }
 
-void ref_propagate(RefSys* s, int calc_epot) { s->thermo->propagate(calc_epot != 0); }
+void ref_propagate(RefSys* s, int calc_epot) { s->active->propagate(calc_epot != 0); }
 
 void ref_mpc_step(RefSys* s, long t, double dt) { s->mpc->step(t, dt); }
 
@@ -277,7 +290,7 @@ void ref_velocity_profile(RefSys* s, double width, double* x_out, int n_x, doubl
 // t = t0 .. t0+n-1 without output; used to time the reference.
 void ref_run(RefSys* s, long t0, long n, double mpc_dt, int with_md) {
   for (long t = t0; t < t0 + n; ++t) {
-    if (with_md) s->thermo->propagate(false);
+    if (with_md) s->active->propagate(false);
     s->mpc->step(t, mpc_dt);
   }
 }

@@ -99,6 +99,10 @@ struct smpc_orc {
   double andersen_nu;
   uint64_t andersen_seed;
   uint64_t md_step;
+  int and_staged;     /* orc_stage_andersen: resets of the next step */
+  int and_n;
+  int* and_idx;
+  double* and_vel;
 
   int err;
 };
@@ -322,6 +326,7 @@ void orc_destroy(smpc_orc* o) {
   free(o->c_mem);
   free(o->m_img);
   free(o->adj_start); free(o->adj_idx); free(o->adj_anchor);
+  free(o->and_idx); free(o->and_vel);
   free(o);
 }
 
@@ -597,11 +602,32 @@ void orc_set_andersen(smpc_orc* o, double nu, uint64_t seed) {
   o->andersen_seed = seed;
 }
 
+/* Injected resets (the reference's own Rand draws, decoded on the host:
+ * Andersen_stochastic.cpp:49-58) replace the Philox draws of the next step. */
+void orc_stage_andersen(smpc_orc* o, int n, const int* idx, const double* vel) {
+  free(o->and_idx);
+  free(o->and_vel);
+  o->and_idx = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+  o->and_vel = (double*)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
+  for (int k = 0; k < n; ++k) {
+    o->and_idx[k] = idx[k];
+    for (int d = 0; d < 3; ++d) o->and_vel[3 * k + d] = vel[3 * k + d];
+  }
+  o->and_n = n;
+  o->and_staged = 1;
+}
+
 static inline double md_kick(const smpc_orc* o, double f, double m, double dth) {
   return o->andersen ? f * (dth / m) : (f / m) * dth;
 }
 
 static void andersen_step(smpc_orc* o) {
+  if (o->and_staged) {
+    for (int k = 0; k < o->and_n; ++k)
+      for (int d = 0; d < 3; ++d) o->mv[3 * o->and_idx[k] + d] = o->and_vel[3 * k + d];
+    o->and_staged = 0;
+    return;
+  }
   const double p = o->andersen_nu * o->p.md_dt;
   const double sigma = sqrt(o->p.kT);
   for (int i = 0; i < o->n_m; ++i) {

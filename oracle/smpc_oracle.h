@@ -86,6 +86,9 @@ void orc_init_md(smpc_orc* o);
 void orc_set_periodic_md(smpc_orc* o, double h);
 /* Andersen stochastic thermostat after every MD step (MPC-off runs). */
 void orc_set_andersen(smpc_orc* o, double nu, uint64_t seed);
+/* The next MD step's Andersen resets given explicitly (monomer idx[k] gets
+ * vel[3k..3k+2] after the second half kick) instead of drawn. */
+void orc_stage_andersen(smpc_orc* o, int n, const int* idx, const double* vel);
 /* Periodic forces at the current positions and delrx into out[3 n_mono]: by
  * the cell grid that large boxes use (force_grid = 1) or by the loop over all
  * monomers (0). The state is not changed. */

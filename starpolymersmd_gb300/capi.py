@@ -30,7 +30,8 @@ ERR_BITS = {1: "solvent cell out of range", 2: "monomer cell out of range",
 # Every entry point declared in include/smpc.h.
 EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "smpc_set_fluid",
            "smpc_get_fluid", "smpc_set_monomers", "smpc_get_monomers", "smpc_set_bonds",
-           "smpc_init_md", "smpc_md_substeps", "smpc_mpc_step", "smpc_cycles",
+           "smpc_init_md", "smpc_md_substeps", "smpc_stage_andersen", "smpc_mpc_step",
+           "smpc_cycles",
            "smpc_temperature", "smpc_epot", "smpc_delrx", "smpc_set_delrx",
            "smpc_cell_counts", "smpc_cell_members", "smpc_set_collision_counter", "smpc_verlet_rebuilds",
            "smpc_error_word", "smpc_synchronize", "smpc_cycles_profiled", "smpc_time_cycles",
@@ -106,6 +107,7 @@ def load(path: Optional[str] = None):
         "smpc_set_bonds": ([P, I, I, P, P], I),
         "smpc_init_md": ([P], I),
         "smpc_md_substeps": ([P, I, I], I),
+        "smpc_stage_andersen": ([P, I, I, P, P, P], I),
         "smpc_mpc_step": ([P, C.c_long, D, C.POINTER(Inject)], I),
         "smpc_cycles": ([P, I], I),
         "smpc_temperature": ([P, I, C.POINTER(D)], I),
@@ -270,6 +272,16 @@ class Context:
     # stepping ------------------------------------------------------------------
     def md_substeps(self, n=1, calc_epot=False):
         self._check(self.lib.smpc_md_substeps(self.h, n, int(calc_epot)), "md_substeps")
+
+    def stage_andersen(self, rep, step_start, mono, vel):
+        """Andersen resets of the next ``len(step_start) - 1`` substeps from the
+        host (replica-local monomer ``mono[e]`` gets ``vel[e]`` in substep s for
+        e in [step_start[s], step_start[s + 1])), in place of device draws."""
+        st = np.ascontiguousarray(step_start, dtype=np.int32)
+        mo = np.ascontiguousarray(mono, dtype=np.int32)
+        ve = _f64(np.asarray(vel, dtype=np.float64).reshape(-1, 3))
+        self._check(self.lib.smpc_stage_andersen(self.h, rep, len(st) - 1, _p(st), _p(mo),
+                                                 _p(ve)), "stage_andersen")
 
     def mpc_step(self, t, dt, shift=None, gamma=None, u_phi=None, u_theta=None):
         inj = None

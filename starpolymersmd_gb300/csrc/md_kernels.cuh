@@ -170,6 +170,13 @@ struct MdArgs {
   const int* order;        // replica of each CTA (largest first), or null: CTA b = replica b
   int andersen;            // Andersen stochastic thermostat (MPC-off runs)
   double andersen_nu;      // its collision frequency
+  // Staged Andersen resets (smpc_stage_andersen), or null: replica r's
+  // substep s resets beads and_mono[e] (replica-local) to and_vel[3 e ..] for
+  // e in [and_start[r (n_steps + 1) + s], ... + s + 1); and_start[r (n_steps + 1)]
+  // < 0 marks a replica that draws from Philox instead.
+  const int* and_start;
+  const int* and_mono;
+  const double* and_vel;
 };
 
 // Cell key of a position on a grid of side rv: three 10-bit fields
@@ -413,10 +420,19 @@ __global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, 
         if (a.n_steps > 0) {
           for (int d = 0; d < 3; ++d)  // second half-kick
             v[k][d] += a.andersen ? f[k][d] * (dth / m[k]) : (f[k][d] / m[k]) * dth;
-          if (a.andersen)
-            andersen_draw<R>(ri.seed, i, md_step0 + static_cast<unsigned long long>(step),
-                             static_cast<R>(a.andersen_nu * ri.md_dt),
-                             r_sqrt(static_cast<R>(ri.kT)), m[k], v[k]);
+          if (a.andersen) {
+            const int* as = a.and_start ? a.and_start + static_cast<size_t>(r) * (a.n_steps + 1)
+                                        : nullptr;
+            if (as && as[0] >= 0) {
+              for (int e = as[step]; e < as[step + 1]; ++e)
+                if (a.and_mono[e] == i)
+                  for (int d = 0; d < 3; ++d) v[k][d] = static_cast<R>(a.and_vel[3 * e + d]);
+            } else {
+              andersen_draw<R>(ri.seed, i, md_step0 + static_cast<unsigned long long>(step),
+                               static_cast<R>(a.andersen_nu * ri.md_dt),
+                               r_sqrt(static_cast<R>(ri.kT)), m[k], v[k]);
+            }
+          }
         }
       }
     }

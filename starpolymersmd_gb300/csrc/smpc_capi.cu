@@ -71,6 +71,19 @@ struct smpc_ctx {
   int* d_ncount = nullptr;
   int* d_md_order = nullptr;  // replicas by decreasing monomer count (MD CTA order)
   bool any_local_md = false;  // a non-periodic replica has monomers
+  // Andersen resets staged for the next smpc_md_substeps (smpc_stage_andersen):
+  // per replica the staged substep count (-1: none) and the host tables; the
+  // device copy (starts, then monomers) lives in d_and_i / d_and_v while a
+  // staged call's MD launch is issued
+  std::vector<int> and_steps;
+  std::vector<std::vector<int>> and_start_h, and_mono_h;
+  std::vector<std::vector<double>> and_vel_h;
+  int* d_and_i = nullptr;
+  double* d_and_v = nullptr;
+  size_t and_i_cap = 0, and_v_cap = 0;
+  const int* and_start_dev = nullptr;  // set only while a staged launch is issued
+  const int* and_mono_dev = nullptr;
+  const double* and_vel_dev = nullptr;
   int mono_chunks = 1;        // CTAs per replica of k_mono_prep (replicas that cannot recentre)
   // periodic boxes (SMPC_REPLICA_PERIODIC_MD): launch arguments with their grid
   // buffers, and molecules made whole for the observables
@@ -256,6 +269,9 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   a.order = ctx->d_md_order;
   a.andersen = ctx->opt.md_thermostat == SMPC_MDTHERMO_ANDERSEN ? 1 : 0;
   a.andersen_nu = ctx->opt.andersen_nu;
+  a.and_start = ctx->and_start_dev;
+  a.and_mono = ctx->and_mono_dev;
+  a.and_vel = ctx->and_vel_dev;
   smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
                      static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->var_md,
                      ctx->st);
@@ -644,6 +660,8 @@ void free_all(smpc_ctx* ctx) {
   if (ctx->d_rows_by_rep) cudaFree(ctx->d_rows_by_rep);
   if (ctx->d_stress) cudaFree(ctx->d_stress);
   if (ctx->d_pamphi) cudaFree(ctx->d_pamphi);
+  if (ctx->d_and_i) cudaFree(ctx->d_and_i);
+  if (ctx->d_and_v) cudaFree(ctx->d_and_v);
   void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
                   ctx->d_tpart, ctx->d_keys, ctx->d_perm, ctx->d_count, ctx->d_off, ctx->d_tsum,
                   ctx->d_grand, ctx->d_mpos, ctx->d_mvel, ctx->d_mfrc, ctx->d_mver, ctx->d_mkey,
@@ -1085,12 +1103,94 @@ int smpc_init_md(smpc_ctx* ctx) {
   return SMPC_OK;
 }
 
+int smpc_stage_andersen(smpc_ctx* ctx, int rep, int n_steps, const int* step_start,
+                        const int* mono, const double* vel) {
+  if (int rc = check_rep(ctx, rep)) return rc;
+  if (ctx->opt.md_thermostat != SMPC_MDTHERMO_ANDERSEN)
+    return fail(ctx, SMPC_E_STATE, "Andersen resets staged without the Andersen thermostat");
+  if (ctx->reps[rep].flags & smpc::REP_PERIODIC_MD)
+    return fail(ctx, SMPC_E_UNSUPPORTED, "staged Andersen resets on a periodic replica");
+  if (n_steps < 1 || !step_start) return fail(ctx, SMPC_E_ARG, "n_steps < 1 or null step_start");
+  const int n_mono = ctx->reps[rep].n_mono;
+  if (step_start[0] != 0) return fail(ctx, SMPC_E_ARG, "step_start[0] != 0");
+  for (int s = 0; s < n_steps; ++s)
+    if (step_start[s + 1] < step_start[s])
+      return fail(ctx, SMPC_E_ARG, "step_start not non-decreasing");
+  const int total = step_start[n_steps];
+  if (total > 0 && (!mono || !vel)) return fail(ctx, SMPC_E_ARG, "null reset buffer");
+  for (int e = 0; e < total; ++e)
+    if (mono[e] < 0 || mono[e] >= n_mono) return fail(ctx, SMPC_E_ARG, "reset monomer out of range");
+  if (ctx->and_steps.empty()) {
+    ctx->and_steps.assign(ctx->n_rep, -1);
+    ctx->and_start_h.resize(ctx->n_rep);
+    ctx->and_mono_h.resize(ctx->n_rep);
+    ctx->and_vel_h.resize(ctx->n_rep);
+  }
+  ctx->and_steps[rep] = n_steps;
+  ctx->and_start_h[rep].assign(step_start, step_start + n_steps + 1);
+  ctx->and_mono_h[rep].assign(mono, mono + total);
+  ctx->and_vel_h[rep].assign(vel, vel + 3 * static_cast<size_t>(total));
+  return SMPC_OK;
+}
+
+// Device table of the staged resets for an n-substep call (layout in
+// md_kernels.cuh, MdArgs::and_start); the staged entries are consumed.
+static int upload_staged_andersen(smpc_ctx* ctx, int n) {
+  std::vector<int> starts(static_cast<size_t>(ctx->n_rep) * (n + 1), -1), monos;
+  std::vector<double> vels;
+  for (int r = 0; r < ctx->n_rep; ++r) {
+    if (ctx->and_steps[r] < 0) continue;
+    if (ctx->and_steps[r] != n)
+      return fail(ctx, SMPC_E_ARG, "staged Andersen resets cover a different substep count");
+    const int base = static_cast<int>(monos.size());
+    for (int s = 0; s <= n; ++s)
+      starts[static_cast<size_t>(r) * (n + 1) + s] = base + ctx->and_start_h[r][s];
+    monos.insert(monos.end(), ctx->and_mono_h[r].begin(), ctx->and_mono_h[r].end());
+    vels.insert(vels.end(), ctx->and_vel_h[r].begin(), ctx->and_vel_h[r].end());
+    ctx->and_steps[r] = -1;
+  }
+  const size_t ni = starts.size() + monos.size(), nv = vels.size() > 0 ? vels.size() : 1;
+  if (ni > ctx->and_i_cap) {
+    if (ctx->d_and_i) CU(cudaFree(ctx->d_and_i));
+    ctx->d_and_i = nullptr;
+    CU(cudaMalloc(&ctx->d_and_i, ni * sizeof(int)));
+    ctx->and_i_cap = ni;
+  }
+  if (nv > ctx->and_v_cap) {
+    if (ctx->d_and_v) CU(cudaFree(ctx->d_and_v));
+    ctx->d_and_v = nullptr;
+    CU(cudaMalloc(&ctx->d_and_v, nv * sizeof(double)));
+    ctx->and_v_cap = nv;
+  }
+  CU(cudaMemcpyAsync(ctx->d_and_i, starts.data(), starts.size() * sizeof(int),
+                     cudaMemcpyHostToDevice, ctx->st));
+  if (!monos.empty())
+    CU(cudaMemcpyAsync(ctx->d_and_i + starts.size(), monos.data(), monos.size() * sizeof(int),
+                       cudaMemcpyHostToDevice, ctx->st));
+  if (!vels.empty())
+    CU(cudaMemcpyAsync(ctx->d_and_v, vels.data(), vels.size() * sizeof(double),
+                       cudaMemcpyHostToDevice, ctx->st));
+  // the host tables are locals: wait for the copies before they go
+  CU(cudaStreamSynchronize(ctx->st));
+  ctx->and_start_dev = ctx->d_and_i;
+  ctx->and_mono_dev = ctx->d_and_i + starts.size();
+  ctx->and_vel_dev = ctx->d_and_v;
+  return SMPC_OK;
+}
+
 int smpc_md_substeps(smpc_ctx* ctx, int n, int calc_epot) {
   if (!ctx || n < 0) return SMPC_E_ARG;
   if (ctx->total_mono > 0 && !ctx->md_ready) return fail(ctx, SMPC_E_STATE, "smpc_init_md not called");
   if (n == 0) return SMPC_OK;
+  bool staged = false;
+  for (int k : ctx->and_steps) staged = staged || k >= 0;
+  if (staged)
+    if (int rc = upload_staged_andersen(ctx, n)) return rc;
   int rc = ctx->opt.precision == SMPC_FP64 ? launch_md_steps<double>(ctx, n, calc_epot, 0)
                                            : launch_md_steps<float>(ctx, n, calc_epot, 0);
+  ctx->and_start_dev = nullptr;
+  ctx->and_mono_dev = nullptr;
+  ctx->and_vel_dev = nullptr;
   if (rc) return rc;
   CU(cudaGetLastError());
   return SMPC_OK;

@@ -47,26 +47,7 @@ void Thermostat_GPU::dtime(double& dt) {
 
 // Thermostat_None.cpp:21-38 on the device: half kick, drift, Verlet check and
 // rebuild, forces (with the potential energy when calc_epot), half kick.
-void Thermostat_GPU::propagate(bool calc_epot) {
-  smpc_dropin::BoxContext& bc = smpc_dropin::find(SimBox);
-  smpc_ctx* ctx = smpc_dropin::ensure(SimBox);
-  if (!bc.md_ready) {
-    if (!bc.mono_on_device) smpc_dropin::upload_monomer_state(SimBox);
-    smpc_dropin::check(ctx, "smpc_init_md", smpc_init_md(ctx));
-    bc.md_ready = true;
-    bc.mono_on_device = true;
-  }
-  smpc_dropin::check(ctx, "smpc_md_substeps", smpc_md_substeps(ctx, 1, calc_epot ? 1 : 0));
-  if (!calc_epot) return;
-  smpc_dropin::check_device(ctx, "Thermostat_GPU::propagate");
-  smpc_dropin::download_monomer_state(SimBox, true);
-  double epot = 0.;
-  smpc_dropin::check(ctx, "smpc_epot", smpc_epot(ctx, 0, &epot));
-  // the device sums the potential energy over all molecules; Box::print_Epot
-  // (Box.cpp:605-613) reads the sum over Molecules
-  for (auto& mol : SimBox.Molecules) mol.Epot = 0.0;
-  if (!SimBox.Molecules.empty()) SimBox.Molecules[0].Epot = epot;
-}
+void Thermostat_GPU::propagate(bool calc_epot) { smpc_dropin::md_step(SimBox, calc_epot); }
 
 void Thermostat_GPU::propagate_gaussian(bool) {
   std::fprintf(stderr, "Thermostat_GPU::propagate_gaussian is not implemented on the GPU\n");

@@ -144,6 +144,8 @@ smpc_ctx* ensure(Box& box) {
   o.strict_cells = 1;
   o.device = device_ordinal();
   o.angular_momentum = bc.angular_momentum ? 1 : 0;
+  o.md_thermostat = bc.md_thermostat;
+  o.andersen_nu = bc.andersen_nu;
   smpc_ctx* ctx = nullptr;
   int rc = smpc_create(&d, 1, &o, &ctx);
   if (rc != SMPC_OK) fail(ctx, "smpc_create", rc);
@@ -207,6 +209,27 @@ void download_monomer_state(Box& box, bool with_force) {
       }
       ++k;
     }
+}
+
+void md_step(Box& box, bool calc_epot) {
+  BoxContext& bc = find(box);
+  smpc_ctx* ctx = ensure(box);
+  if (!bc.md_ready) {
+    if (!bc.mono_on_device) upload_monomer_state(box);
+    check(ctx, "smpc_init_md", smpc_init_md(ctx));
+    bc.md_ready = true;
+    bc.mono_on_device = true;
+  }
+  check(ctx, "smpc_md_substeps", smpc_md_substeps(ctx, 1, calc_epot ? 1 : 0));
+  if (!calc_epot) return;
+  check_device(ctx, "md_step");
+  download_monomer_state(box, true);
+  double epot = 0.;
+  check(ctx, "smpc_epot", smpc_epot(ctx, 0, &epot));
+  // the device sums the potential energy over all molecules; Box::print_Epot
+  // (Box.cpp:605-613) reads the sum over Molecules
+  for (auto& mol : box.Molecules) mol.Epot = 0.0;
+  if (!box.Molecules.empty()) box.Molecules[0].Epot = epot;
 }
 
 }  // namespace smpc_dropin

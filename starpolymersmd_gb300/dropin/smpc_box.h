@@ -35,9 +35,12 @@ struct BoxContext {
   unsigned step_update = 1;
   unsigned n_fluid = 0;
   bool angular_momentum = false;  // MPC(..., angular_mom)
-  // integrator, registered by the Thermostat_GPU constructor
+  // integrator, registered by the Thermostat_GPU or AndersenStochastic
+  // constructor (SMPC_MDTHERMO_ANDERSEN for the latter, with its frequency)
   bool has_md = false;
   double md_dt = 0.01;
+  int md_thermostat = SMPC_MDTHERMO_NONE;
+  double andersen_nu = 0.0;
   // device holds the newer monomer state than Box::Molecules
   bool mono_on_device = false;
   bool md_ready = false;
@@ -51,6 +54,12 @@ BoxContext& find(Box& box);
 // Creates the context (first call) and uploads the molecules and their bonds;
 // the solvent is uploaded by its owner (MPC::step).
 smpc_ctx* ensure(Box& box);
+
+// One velocity-Verlet step of every monomer on the device (the device
+// context is created and the MD initialised at the first call); with
+// calc_epot the box's monomers, forces and Molecules[0].Epot (the sum over
+// all molecules, which Box::print_Epot adds up) are refreshed on the host.
+void md_step(Box& box, bool calc_epot);
 
 // Host <-> device copies of the monomer positions and velocities, in
 // Box::Molecules order (molecule by molecule, monomer by monomer).

@@ -19,6 +19,7 @@ The fixtures are plain .npz files; tests read them without the reference.
 from __future__ import annotations
 
 import argparse
+import math
 import os
 import sys
 
@@ -58,6 +59,15 @@ SCENARIOS = {
     "md_saw_L16": dict(L=(16, 16, 16), n_c=1, kT=1.0, shear=0.0, step_update=1, h=0.1,
                        md_dt=0.01, lam=1.5, star=dict(A=5, B=5, arms=6, mass=5.0),
                        saw_seed=7, n_loop=60, with_md=True, md_only=True),
+    # MPC off: the driver's AndersenStochastic integrator (star-polymers.cpp:387),
+    # heavy monomers (N(0, sqrt(T / m)) resets) and unit-mass ones (N(0, sqrt(T)))
+    "andersen_saw_L16": dict(L=(16, 16, 16), n_c=1, kT=1.0, shear=0.0, step_update=1, h=0.1,
+                             md_dt=0.01, lam=1.5, star=dict(A=5, B=5, arms=6, mass=5.0),
+                             saw_seed=11, n_loop=60, with_md=True, md_only=True,
+                             andersen_nu=2.0),
+    "andersen_m1_L12": dict(L=(12, 12, 12), n_c=1, kT=0.8, shear=0.0, step_update=1, h=0.1,
+                            md_dt=0.005, lam=1.0, star=dict(A=2, B=2, arms=3, mass=1.0),
+                            n_loop=40, with_md=True, md_only=True, andersen_nu=5.0),
 }
 
 
@@ -77,7 +87,10 @@ def run_scenario(name: str, sc: dict) -> dict:
             ref.set_monomers(pos, mono["vel"])
         if "star_offset" in sc:
             ref.set_monomers(mono["pos"] + np.asarray(sc["star_offset"]), mono["vel"])
-        ref.make_thermostat(sc["md_dt"])
+        if "andersen_nu" in sc:
+            ref.make_andersen(sc["md_dt"], sc["kT"], sc["andersen_nu"])
+        else:
+            ref.make_thermostat(sc["md_dt"])
     if not sc.get("md_only"):
         ref.mpc_initialize()
     fpos0, fvel0 = ref.get_fluid()
@@ -96,9 +109,19 @@ def run_scenario(name: str, sc: dict) -> dict:
     fl_pos, fl_vel, temps, fl_cell, mo_cell = [], [], [], [], []
     obs, prof_x, prof_y = [], [], []
     m_pos, m_vel, m_frc, delrx, epots = [], [], [], [], []
+    and_start, and_idx, and_vel = [0], [], []
     for t in range(sc["n_loop"]):
         if st and sc["with_md"]:
+            if "andersen_nu" in sc:
+                ref.tape_start()
             ref.propagate(True)
+            if "andersen_nu" in sc:
+                vals, kinds = ref.tape_take()
+                ix, vv = orc.decode_andersen_tape(vals, kinds, m0["mass"],
+                                                  sc["andersen_nu"] * sc["md_dt"],
+                                                  math.sqrt(sc["kT"]))
+                and_idx.append(ix); and_vel.append(vv)
+                and_start.append(and_start[-1] + len(ix))
             epots.append(ref.epot())
         if not sc.get("md_only"):
             ref.tape_start()
@@ -125,6 +148,13 @@ def run_scenario(name: str, sc: dict) -> dict:
             m_pos.append(m["pos"]); m_vel.append(m["vel"]); m_frc.append(m["force"])
     out.update(coll_steps=np.array(steps, dtype=np.int64), delrx=np.array(delrx),
                epot=np.array(epots))
+    if "andersen_nu" in sc:
+        # per driver-loop step t: monomers and_idx[and_start[t]:and_start[t + 1]]
+        # got the velocities and_vel[...] from the reference's draws
+        out.update(andersen_nu=sc["andersen_nu"],
+                   andersen_start=np.array(and_start, dtype=np.int32),
+                   andersen_idx=np.concatenate(and_idx).astype(np.int32),
+                   andersen_vel=np.concatenate(and_vel).reshape(-1, 3))
     if steps:
         out.update(shift=np.array(shifts), gamma=np.array(gammas), u_phi=np.array(uphis),
                    u_theta=np.array(uths), count_total=np.array(tots), count_fluid=np.array(fls),

@@ -17,3 +17,14 @@ def has_star(fx):
 
 def collision_index(fx):
     return {int(t): k for k, t in enumerate(fx["coll_steps"])}
+
+
+def is_andersen(fx):
+    """MPC-off fixture driven by the reference's AndersenStochastic."""
+    return "andersen_nu" in fx
+
+
+def andersen_resets(fx, t):
+    """(monomer indices, velocities) the reference's draws reset in loop step t."""
+    a, b = int(fx["andersen_start"][t]), int(fx["andersen_start"][t + 1])
+    return fx["andersen_idx"][a:b], fx["andersen_vel"][a:b]

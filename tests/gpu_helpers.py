@@ -39,7 +39,10 @@ def fixture_context(fx, precision=capi.FP64, periodic=False):
     ctx = capi.Context([rep], precision=precision, rng=capi.RNG_INJECT,
                        step_update=int(fx["step_update"]),
                        mono_bin=capi.MONOBIN_WRAPPED if periodic else capi.MONOBIN_REFERENCE,
-                       angular_momentum=bool(int(fx.get("amc", 0))))
+                       angular_momentum=bool(int(fx.get("amc", 0))),
+                       md_thermostat=(capi.MDTHERMO_ANDERSEN if gr.is_andersen(fx)
+                                      else capi.MDTHERMO_NONE),
+                       andersen_nu=float(fx.get("andersen_nu", 0.0)))
     ctx.set_fluid(0, fx["fluid_pos0"], fx["fluid_vel0"])
     if star:
         ctx.set_monomers(0, fx["mono_pos0"], fx["mono_vel0"], fx["mono_force0"], fx["mono_mass"],

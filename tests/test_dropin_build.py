@@ -45,6 +45,10 @@ def test_reference_drivers_build_against_dropins(tmp_path):
         for sym in ("smpc_create", "smpc_mpc_bin", "smpc_mpc_collide", "smpc_cell_counts",
                     "smpc_get_fluid", "smpc_cell_members", "smpc_temperature"):
             assert sym in und, (exe, sym)
+        if exe == "star-polymers":
+            # the MPC-off integrator (AndersenStochastic) steps on the device
+            for sym in ("smpc_stage_andersen", "smpc_md_substeps"):
+                assert sym in und, (exe, sym)
         # ... and resolve them from the in-tree libsmpc
         ldd = subprocess.run(["ldd", str(path)], capture_output=True, text=True).stdout
         assert os.path.realpath(lib) in ldd or os.path.basename(lib) in ldd

@@ -32,6 +32,9 @@ def test_fp64_replays_reference_fixture(path):
             H.close64(f0, fx["mono_force0"])
         for t in range(int(fx["n_loop"])):
             if star and int(fx["with_md"]):
+                if gr.is_andersen(fx):
+                    idx, vel = gr.andersen_resets(fx, t)
+                    ctx.stage_andersen(0, [0, len(idx)], idx, vel)
                 ctx.md_substeps(1, calc_epot=True)
                 H.close64(ctx.epot(0), fx["epot"][t])
             if not int(fx["md_only"]):

@@ -102,3 +102,67 @@ def test_fp32_andersen_holds_the_temperature():
             temps.append((sol.mass[:, None] * v * v).sum() / (3 * sol.n))
         ctx.raise_on_device_error()
         assert abs(np.mean(temps) / kT - 1.0) < 0.05
+
+
+def test_staged_resets_over_several_substeps_and_replicas(golden_dir):
+    # the reference fixture's resets staged four substeps at a time into
+    # replica 0, while replica 1 (same star) draws from Philox like the oracle
+    import os
+    from tests import golden_replay as gr
+    fx = gr.load(os.path.join(golden_dir, "andersen_m1_L12.npz"))
+    n = len(fx["mono_pos0"])
+    L = tuple(int(x) for x in fx["L"])
+    rep = dict(L=L, n_fluid=0, n_mono=n, mol0_size=n, kT=float(fx["kT"]), shear=0.0, h=0.1,
+               md_dt=float(fx["md_dt"]), seed=SEED, **{"lambda": float(fx["lam"])})
+    nu = float(fx["andersen_nu"])
+    o = orc.OracleSystem(L, float(fx["kT"]), 0.0, 1000, 0, n, mol_start=[0, n],
+                         lambda_=float(fx["lam"]), md_dt=float(fx["md_dt"]))
+    o.set_monomers(fx["mono_pos0"], fx["mono_vel0"], fx["mono_force0"], fx["mono_mass"],
+                   fx["mono_amphi"], fx["mono_anchor"])
+    o.set_bonds(fx["bond_src"], fx["bond_dst"])
+    o.set_andersen(nu, SEED)
+    o.init_md()
+    with capi.Context([rep, rep], precision=capi.FP64, rng=capi.RNG_PHILOX, step_update=1000,
+                      md_thermostat=capi.MDTHERMO_ANDERSEN, andersen_nu=nu) as ctx:
+        for r in range(2):
+            ctx.set_monomers(r, fx["mono_pos0"], fx["mono_vel0"], fx["mono_force0"],
+                             fx["mono_mass"], fx["mono_amphi"], fx["mono_anchor"])
+            ctx.set_bonds(r, fx["bond_src"], fx["bond_dst"])
+        ctx.init_md()
+        # a staged count that differs from the call's is refused, nothing runs
+        ctx.stage_andersen(0, [0, 0, 0], [], np.zeros((0, 3)))
+        with pytest.raises(capi.SmpcError):
+            ctx.md_substeps(3)
+        for t0 in range(0, 40, 4):
+            starts, idx, vel = [0], [], []
+            for t in range(t0, t0 + 4):
+                i, v = gr.andersen_resets(fx, t)
+                idx.append(i); vel.append(v)
+                starts.append(starts[-1] + len(i))
+                o.propagate(False)
+            ctx.stage_andersen(0, starts, np.concatenate(idx), np.concatenate(vel))
+            ctx.md_substeps(4)
+        ctx.raise_on_device_error()
+        p0, v0, _ = ctx.get_monomers(0)
+        H.close64(p0, fx["mono_pos"][39])
+        H.close64(v0, fx["mono_vel"][39])
+        p1, v1, _ = ctx.get_monomers(1)
+        op, ov, _ = o.get_monomers()
+        H.close64(p1, op, rtol=1e-11)
+        H.close64(v1, ov, rtol=1e-11)
+        # out-of-range monomer, bad starts
+        with pytest.raises(capi.SmpcError):
+            ctx.stage_andersen(0, [0, 1], [n], np.zeros((1, 3)))
+        with pytest.raises(capi.SmpcError):
+            ctx.stage_andersen(0, [1, 1], [0], np.zeros((1, 3)))
+
+
+def test_staging_needs_the_andersen_thermostat():
+    L = 12
+    star, _, _ = H.small_star_system(L=L, seed=6)
+    n = star.n
+    rep = dict(L=(L, L, L), n_fluid=0, n_mono=n, mol0_size=n, kT=1.0, shear=0.0, h=0.1,
+               md_dt=0.01, **{"lambda": 1.0})
+    with capi.Context([rep], precision=capi.FP64, rng=capi.RNG_PHILOX, step_update=1000) as ctx:
+        with pytest.raises(capi.SmpcError):
+            ctx.stage_andersen(0, [0, 0], [], np.zeros((0, 3)))

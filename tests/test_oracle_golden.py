@@ -29,6 +29,8 @@ def make_oracle(fx):
         o.set_monomers(fx["mono_pos0"], fx["mono_vel0"], fx["mono_force0"], fx["mono_mass"],
                        fx["mono_amphi"], fx["mono_anchor"])
         o.set_bonds(fx["bond_src"], fx["bond_dst"])
+        if gr.is_andersen(fx):
+            o.set_andersen(float(fx["andersen_nu"]), 0)
         o.init_md()
     return o
 
@@ -43,6 +45,8 @@ def test_oracle_matches_reference_bitwise(path):
     coll = gr.collision_index(fx)
     for t in range(int(fx["n_loop"])):
         if gr.has_star(fx) and int(fx["with_md"]):
+            if gr.is_andersen(fx):
+                o.stage_andersen(*gr.andersen_resets(fx, t))
             o.propagate(True)
             assert o.epot() == fx["epot"][t]
         if not int(fx["md_only"]):
