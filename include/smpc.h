@@ -212,7 +212,11 @@ int smpc_temperature_all(smpc_ctx* ctx, double* out);
 int smpc_temperature_all_noalloc(smpc_ctx* ctx, double* out);
 /* Monomer positions/velocities of all replicas (concatenated, x,y,z
  * interleaved): the Box::Molecules state a host-side driver reads and writes
- * between steps (star-polymers.cpp:466-519). Masses and types are kept. */
+ * between steps (star-polymers.cpp:466-519). Masses and types are kept. The
+ * stored forces are kept too (velocity Verlet carries them into the next
+ * substep's first half kick, Thermostat_None.cpp:21-27): after placing a
+ * different configuration, smpc_init_md recomputes them. Periodic replicas
+ * rebuild their Verlet lists at the next substep. */
 int smpc_set_monomer_state_all(smpc_ctx* ctx, const double* pos, const double* vel);
 int smpc_get_monomer_state_all(smpc_ctx* ctx, double* pos, double* vel, double* force);
 int smpc_delrx(smpc_ctx* ctx, int rep, double* out);

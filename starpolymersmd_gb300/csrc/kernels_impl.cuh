@@ -151,7 +151,7 @@ void launch_mol_observables<Real>(const int2* rep_mols, const int2* mols, int n_
                                   double* out, cudaStream_t st) {
   if (n_rep == 0) return;
   if (n_mols > 0) k_mol_observables<Real, 256><<<n_mols, 256, 0, st>>>(mols, mpos, mvel, mol_out);
-  k_obs_reduce<Real><<<(n_rep + 127) / 128, 128, 0, st>>>(rep_mols, mol_out, n_rep, out);
+  k_obs_reduce<Real><<<(n_rep + 3) / 4, 128, 0, st>>>(rep_mols, mol_out, n_rep, out);
 }
 
 template <>

@@ -73,6 +73,28 @@ __device__ __forceinline__ double block_sum(double v, double* s_red) {
   return t;  // valid in thread 0
 }
 
+// K block sums at once, each with block_sum's order (so the same bits): one
+// shuffle pass over all K values, one exchange, thread k < K adds the warps'
+// partials of value k into out[k] (shared; valid in every thread on return).
+// s_red holds K * NT / 32 doubles.
+template <int NT, int K>
+__device__ __forceinline__ void block_sum_n(double (&v)[K], double* s_red, double* out) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] += __shfl_down_sync(0xFFFFFFFFu, v[k], o);
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) s_red[k * (NT / 32) + (threadIdx.x >> 5)] = v[k];
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double t = 0.0;
+    for (int w = 0; w < NT / 32; ++w) t += s_red[threadIdx.x * (NT / 32) + w];
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
 // One CTA per molecule; mols[m] = global monomer range [x, y). mol_out[16 m
 // + ...]: R_g of the molecule, G (row-major, 9), rotation frequency (3),
 // kinetic energy, monomers. FP64 sums the centre in monomer order (the
@@ -82,7 +104,8 @@ template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_mol_observables(const int2* mols, const R* mpos,
                                                         const R* mvel, double* mol_out) {
   __shared__ double s_c[6];
-  __shared__ double s_red[NT / 32];
+  __shared__ double s_red[10 * (NT / 32)];
+  __shared__ double s_tot[10];
   const int2 mb = mols[blockIdx.x];
   const int n = mb.y - mb.x;
   if (std::is_same<R, double>::value) {
@@ -98,10 +121,8 @@ __global__ void __launch_bounds__(NT) k_mol_observables(const int2* mols, const 
       c[4] += static_cast<double>(v.y);
       c[5] += static_cast<double>(v.z);
     }
-    for (int k = 0; k < 6; ++k) {
-      const double t = block_sum<NT>(c[k], s_red);
-      if (threadIdx.x == 0) s_c[k] = t / static_cast<double>(n);
-    }
+    block_sum_n<NT, 6>(c, s_red, s_tot);
+    if (threadIdx.x < 6) s_c[threadIdx.x] = s_tot[threadIdx.x] / static_cast<double>(n);
   }
   __syncthreads();
   // S = sum r r^T (6), angular momentum (3), sum m |u|^2
@@ -123,9 +144,10 @@ __global__ void __launch_bounds__(NT) k_mol_observables(const int2* mols, const 
     acc[8] += x0 * u1 - x1 * u0;
     acc[9] += static_cast<double>(p.w) * ((u0 * u0 + u1 * u1) + u2 * u2);
   }
-  double tot[10];
-  for (int k = 0; k < 10; ++k) tot[k] = block_sum<NT>(acc[k], s_red);
+  block_sum_n<NT, 10>(acc, s_red, s_tot);
   if (threadIdx.x != 0) return;
+  double tot[10];
+  for (int k = 0; k < 10; ++k) tot[k] = s_tot[k];
   double* o = mol_out + static_cast<size_t>(OBS_PER_REP) * blockIdx.x;
   for (int k = 0; k < OBS_PER_REP; ++k) o[k] = 0.0;
   if (n <= 0) return;
@@ -151,27 +173,42 @@ __global__ void __launch_bounds__(NT) k_mol_observables(const int2* mols, const 
 // kinetic energy, temperature 2 E / (3 (N - 1)), molecules.
 template <typename R>  // R: the precision of the instantiating unit (one copy per unit)
 __global__ void k_obs_reduce(const int2* rep_mols, const double* mol_out, int n_rep, double* out) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rep) return;
+  // one warp per replica: lane l sums molecules l, l + 32, ... in order, then
+  // a fixed xor butterfly joins the lanes (every lane ends with the same bits;
+  // a replica of one molecule gets its values unchanged)
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n_rep) return;  // whole warps
   const int2 rm = rep_mols[r];
-  double rg = 0, G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, w[3] = {0, 0, 0}, ekin = 0;
+  double acc[14];  // R_g, G (9), rotation frequency (3), kinetic energy
+#pragma unroll
+  for (int k = 0; k < 14; ++k) acc[k] = 0.0;
   long long n_total = 0;
-  for (int m = rm.x; m < rm.x + rm.y; ++m) {
+  for (int m = rm.x + lane; m < rm.x + rm.y; m += 32) {
     const double* o = mol_out + static_cast<size_t>(OBS_PER_REP) * m;
-    if (o[14] <= 0.0) continue;
-    for (int k = 0; k < 9; ++k) G[k] += o[1 + k];
-    rg += o[0];
-    for (int k = 0; k < 3; ++k) w[k] += o[10 + k];
-    ekin += o[13];
-    n_total += static_cast<long long>(o[14]);
+    double v[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) v[k] = o[k];
+    if (v[14] <= 0.0) continue;
+#pragma unroll
+    for (int k = 0; k < 14; ++k) acc[k] += v[k];
+    n_total += static_cast<long long>(v[14]);
   }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 14; ++k) acc[k] += __shfl_xor_sync(FULL, acc[k], off);
+    n_total += __shfl_xor_sync(FULL, n_total, off);
+  }
+  if (lane != 0) return;
   const double nm = rm.y > 0 ? static_cast<double>(rm.y) : 1.0;
   double* o = out + static_cast<size_t>(OBS_PER_REP) * r;
-  o[0] = rg / nm;
-  for (int k = 0; k < 9; ++k) o[1 + k] = G[k] / nm;
-  for (int k = 0; k < 3; ++k) o[10 + k] = w[k] / nm;
-  o[13] = ekin;
-  o[14] = n_total > 1 ? ekin * 2. / (3. * static_cast<double>(n_total - 1)) : 0.0;
+  o[0] = acc[0] / nm;
+  for (int k = 0; k < 9; ++k) o[1 + k] = acc[1 + k] / nm;
+  for (int k = 0; k < 3; ++k) o[10 + k] = acc[10 + k] / nm;
+  o[13] = acc[13];
+  o[14] = n_total > 1 ? acc[13] * 2. / (3. * static_cast<double>(n_total - 1)) : 0.0;
   o[15] = static_cast<double>(rm.y);
 }
 
@@ -193,14 +230,17 @@ __global__ void k_copy_monomers(int n, const R* mpos, const R* mvel, R* upos, R*
   }
 }
 
-__device__ __forceinline__ void unwrap_bond(const double L[3], double delrx, double& d0,
-                                            double& d1, double& d2) {
-  const double cy = round(d1 / L[1]);
-  d0 -= L[0] * round(d0 / L[0]);
+// Lees-Edwards minimum image of a bond vector. The image counts come from
+// products with 1 / L: a bond is far shorter than half the box, so d / L is
+// never near a half-integer and the count is the one the division gives.
+__device__ __forceinline__ void unwrap_bond(const double L[3], const double invL[3], double delrx,
+                                            double& d0, double& d1, double& d2) {
+  const double cy = round(d1 * invL[1]);
+  d0 -= L[0] * round(d0 * invL[0]);
   d0 -= cy * delrx;
-  d0 -= L[0] * round(d0 / L[0]);
+  d0 -= L[0] * round(d0 * invL[0]);
   d1 -= L[1] * cy;
-  d2 -= L[2] * round(d2 / L[2]);
+  d2 -= L[2] * round(d2 * invL[2]);
 }
 
 template <typename R>
@@ -216,6 +256,7 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
   if (!(ri.flags & REP_PERIODIC_MD)) return;
   const double L[3] = {static_cast<double>(ri.L[0]), static_cast<double>(ri.L[1]),
                        static_cast<double>(ri.L[2])};
+  const double invL[3] = {1.0 / L[0], 1.0 / L[1], 1.0 / L[2]};
   const double delrx = dyn[mol_rep[m]].delrx;
   const double sLy = ri.shear * L[1];
   const int2 mb = mols[m];
@@ -223,7 +264,7 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
     const int i = c0 + lane;
     const bool active = i < mb.y;
     int p = -1;
-    double d0 = 0, d1 = 0, d2 = 0;
+    double d0 = 0, d1 = 0, d2 = 0, xy = 0, uy = 0;
     if (active) {
       for (int e = bond_start[i]; e < bond_start[i + 1]; ++e) {
         const int j = bonds[e].x;
@@ -231,10 +272,11 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
       }
       if (p < 0) p = mb.x;
       const R4<R> x = ld4_rw(mpos, i), xp = ld4_rw(mpos, p);
+      xy = static_cast<double>(x.y);
       d0 = static_cast<double>(x.x) - static_cast<double>(xp.x);
-      d1 = static_cast<double>(x.y) - static_cast<double>(xp.y);
+      d1 = xy - static_cast<double>(xp.y);
       d2 = static_cast<double>(x.z) - static_cast<double>(xp.z);
-      unwrap_bond(L, delrx, d0, d1, d2);
+      unwrap_bond(L, invL, delrx, d0, d1, d2);
     }
     const bool chained = active && p == i - 1 && p >= c0;
     if (__any_sync(FULL, active && p >= c0 && !chained)) {
@@ -253,6 +295,7 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
         }
         __syncwarp();
       }
+      if (active) uy = static_cast<double>(ld4_rw(upos, i).y);
     } else {
       // segment heads take their placed partner's image; the scan adds the
       // bond vectors down each segment
@@ -283,12 +326,11 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
         u.y = static_cast<R>(a1);
         u.z = static_cast<R>(a2);
         st4(upos, i, u);
+        uy = static_cast<double>(u.y);
       }
     }
-    __syncwarp();
     if (active) {  // the image's shear velocity
-      const R4<R> x = ld4_rw(mpos, i), u = ld4_rw(upos, i);
-      const double ny = round((static_cast<double>(u.y) - static_cast<double>(x.y)) / L[1]);
+      const double ny = round((uy - xy) * invL[1]);
       R4<R> v = ld4_rw(uvel, i);
       v.x = static_cast<R>(static_cast<double>(v.x) + ny * sLy);
       st4(uvel, i, v);

@@ -482,6 +482,12 @@ int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, do
     smpc::launch_unpack_monomers<R>(ctx->d_dstage, ni, static_cast<R*>(ctx->d_mpos),
                                     static_cast<R*>(ctx->d_mvel), ctx->st);
     CU(cudaGetLastError());
+    // Periodic boxes decide list rebuilds from the integrated peculiar
+    // displacement, which does not see positions set from outside: request a
+    // rebuild at substep 1 (parity 1) of the next call.
+    const int one = 1;
+    for (const smpc::PmdArgs& a : ctx->pmd)
+      CU(cudaMemcpyAsync(a.flag + 1, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
     CU(cudaStreamSynchronize(ctx->st));  // the host arrays are borrowed for the call only
     return SMPC_OK;
   }

@@ -292,3 +292,42 @@ def test_periodic_observables_use_whole_molecules(precision):
         # whole stars stay compact: no bond of the unwrapped copy spans a face
         d = up[sol.bond_dst] - up[sol.bond_src]
         assert np.sqrt((d * d).sum(axis=1)).max() < 4.5
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.FP32])
+def test_state_set_from_outside_rebuilds_the_lists(precision):
+    # The periodic rebuild criterion integrates the peculiar displacement, so
+    # it cannot see positions placed by smpc_set_monomer_state_all: the upload
+    # requests a list rebuild at the next substep. The stored forces stay those
+    # of the old positions (velocity Verlet carries them between calls), so a
+    # rewind to an earlier configuration calls smpc_init_md, and must then
+    # replay the same trajectory bit for bit.
+    sol = _solution(seed=3)
+    empty = np.zeros((0, 3))
+    # 12-6 preset (capped FENE): stable without a thermostat
+    with _context(sol, empty, empty, 0.2, 1000, 2.8, precision=precision,
+                  potential=capi.POT_LJ126, r_cut=2.5, md_dt=0.005) as ctx:
+        n = sol.n
+        state = lambda: (np.zeros((n, 3)), np.zeros((n, 3)))
+        ctx.md_substeps(10)
+        p0, v0 = state()
+        ctx.get_monomer_state_all(p0, v0)
+        ctx.md_substeps(400)
+        p1, v1 = state()
+        ctx.get_monomer_state_all(p1, v1)
+        assert np.all(np.isfinite(p1)) and np.all(np.isfinite(v1))
+        assert np.abs(H.wrapped_diff(p1, p0, (L, L, L))).max() > 0.3  # the beads did move
+        # the upload alone: a rebuild at the next substep
+        r0 = ctx.verlet_rebuilds(0)
+        ctx.set_monomer_state_all(p1, v1)
+        ctx.md_substeps(1)
+        assert ctx.verlet_rebuilds(0) == r0 + 1
+        # rewind: positions, velocities and (init_md) their forces
+        ctx.set_monomer_state_all(p0, v0)
+        ctx.init_md()
+        ctx.md_substeps(400)
+        p2, v2 = state()
+        ctx.get_monomer_state_all(p2, v2)
+        ctx.raise_on_device_error()
+        np.testing.assert_array_equal(p2, p1)
+        np.testing.assert_array_equal(v2, v1)
