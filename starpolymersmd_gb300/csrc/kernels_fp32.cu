@@ -14,7 +14,7 @@ namespace smpc {
 // threads x cells-per-tile / staging capacity / gathers in flight.
 int bin_variant_count() { return 4; }
 int collide_variant_count() { return 7; }
-int md_variant_count() { return 3; }
+int md_variant_count() { return 4; }
 int collide_variant_cells(int v) {
   switch (v) {
     case 2: case 3: case 5: return 64;
@@ -33,7 +33,8 @@ const char* collide_variant_name(int v) {
   return v >= 0 && v < 7 ? n[v] : "?";
 }
 const char* md_variant_name(int v) {
-  static const char* n[] = {"1024t 1/thread", "512t 2/thread", "1024t lanes/bead, largest first"};
-  return v >= 0 && v < 3 ? n[v] : "?";
+  static const char* n[] = {"1024t 1/thread", "512t 2/thread", "1024t lanes/bead, largest first",
+                            "1024t big + 512t small side by side, lanes/bead"};
+  return v >= 0 && v < 4 ? n[v] : "?";
 }
 }  // namespace smpc

@@ -302,11 +302,23 @@ void launch_pack_monomers<Real>(const Real* mpos, const Real* mvel, const Real* 
 
 template <>
 void launch_md<Real>(const MdArgs& a, int n_rep, Real* mpos, Real* mvel, Real* mfrc, Real* mver,
-                     int variant, cudaStream_t st) {
+                     int variant, cudaStream_t st, const MdSplit& split) {
   if (n_rep == 0) return;
   MdArgs b = a;
 #if SMPC_FAST_F32
-  if (variant == 2) {
+  if (variant == 3 && split.n_big > 0 && split.n_big < n_rep && a.order) {
+    // big replicas on the forked stream, small ones here; joined before return
+    cudaEventRecord(split.fork, st);
+    cudaStreamWaitEvent(split.st2, split.fork, 0);
+    k_md_substeps<Real, 1024, 1, 8><<<split.n_big, 1024, 0, split.st2>>>(b, mpos, mvel, mfrc, mver);
+    MdArgs c = a;
+    c.order = a.order + split.n_big;
+    k_md_substeps<Real, 512, 1, 8><<<n_rep - split.n_big, 512, 0, st>>>(c, mpos, mvel, mfrc, mver);
+    cudaEventRecord(split.join, split.st2);
+    cudaStreamWaitEvent(st, split.join, 0);
+    return;
+  }
+  if (variant == 2 || variant == 3) {
     k_md_substeps<Real, 1024, 1, 8><<<n_rep, 1024, 0, st>>>(b, mpos, mvel, mfrc, mver);
     return;
   }

@@ -79,9 +79,18 @@ template <typename R>
 void launch_temperature(const Tile* tiles, int n_tiles, const RepInfo* reps, const uint32_t* off,
                         const uint32_t* perm, const R* rec_cur, const R* mpos, const R* mvel,
                         const int* mimg, int mono_bin, TempPartial* partial, cudaStream_t st);
+// A second stream with fork / join events for the MD launch shape that runs
+// two kernels side by side (variant 3): replicas order[0, n_big) of the MD
+// order (more than 512 monomers) on 1024-thread blocks, the rest on
+// 512-thread blocks, two of which fit one SM.
+struct MdSplit {
+  cudaStream_t st2;
+  cudaEvent_t fork, join;
+  int n_big;
+};
 template <typename R>
 void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, int variant,
-               cudaStream_t st);
+               cudaStream_t st, const MdSplit& split);
 
 // n MD substeps of one periodic box (pmd_kernels.cuh); n = 0 builds lists
 // and forces only (set-up). mnext: second position buffer of the box.

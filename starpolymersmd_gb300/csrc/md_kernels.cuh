@@ -192,9 +192,11 @@ __device__ __forceinline__ int md_bucket(int cx, int cy, int cz) {
          (MD_BUCKETS - 1);
 }
 
+// The 512-thread lanes-per-bead shape is held to 64 registers so that two of
+// its blocks share an SM (the side-by-side MD launch shape).
 template <typename R, int NT, int MPT, int KMAX = 1>
-__global__ void __launch_bounds__(NT) k_md_substeps(MdArgs a, R* mpos, R* mvel, R* mfrc,
-                                                    R* mver) {
+__global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
+    k_md_substeps(MdArgs a, R* mpos, R* mvel, R* mfrc, R* mver) {
   static_assert(KMAX == 1 || MPT == 1, "lanes per bead > 1 needs one bead per thread");
   constexpr int CAP = NT * MPT;
   __shared__ R sx[CAP], sy[CAP], sz[CAP];

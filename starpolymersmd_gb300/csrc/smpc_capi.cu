@@ -70,6 +70,7 @@ struct smpc_ctx {
   int* d_nlist = nullptr;
   int* d_ncount = nullptr;
   int* d_md_order = nullptr;  // replicas by decreasing monomer count (MD CTA order)
+  smpc::MdSplit md_split{};   // side-by-side MD launch shape: second stream, events, split
   bool any_local_md = false;  // a non-periodic replica has monomers
   // Andersen resets staged for the next smpc_md_substeps (smpc_stage_andersen):
   // per replica the staged substep count (-1: none) and the host tables; the
@@ -274,7 +275,7 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   a.and_vel = ctx->and_vel_dev;
   smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
                      static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->var_md,
-                     ctx->st);
+                     ctx->st, ctx->md_split);
   return SMPC_OK;
 }
 
@@ -679,6 +680,9 @@ void free_all(smpc_ctx* ctx) {
     if (p) cudaFree(p);
   for (int k = 0; k < 3; ++k)
     if (ctx->d_col_tiles_v[k]) cudaFree(ctx->d_col_tiles_v[k]);
+  if (ctx->md_split.fork) cudaEventDestroy(ctx->md_split.fork);
+  if (ctx->md_split.join) cudaEventDestroy(ctx->md_split.join);
+  if (ctx->md_split.st2) cudaStreamDestroy(ctx->md_split.st2);
   if (ctx->st) cudaStreamDestroy(ctx->st);
 }
 
@@ -967,8 +971,14 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
   ctx->bsrc.resize(n_rep);
   ctx->bdst.resize(n_rep);
   ctx->anchor.resize(n_rep);
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->md_split.st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->md_split.fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->md_split.join, cudaEventDisableTiming) != cudaSuccess)
     return bail(SMPC_E_CUDA, "stream");
+  // replicas above 512 monomers lead the MD order (it sorts by size)
+  for (int r = 0; r < n_rep; ++r)
+    if (ctx->reps[r].n_mono > 512) ++ctx->md_split.n_big;
   int rc = opt->precision == SMPC_FP64 ? create_buffers<double>(ctx) : create_buffers<float>(ctx);
   if (rc) return bail(rc, ctx->err);
   const int ct = opt->precision == SMPC_FP64 ? smpc::collide_cells_per_tile<double>()

@@ -402,14 +402,18 @@ def test_two_phase_step_replays_reference(golden_dir, name):
             assert ctx.delrx(0) == fx["delrx"][t]
 
 
-@pytest.mark.parametrize("md_variant", [0, 1, 2])
+@pytest.mark.parametrize("md_variant", [0, 1, 2, 3])
 def test_fp32_md_variants_track_fp64_oracle(md_variant):
     # MD only (no collisions): every FP32 launch shape of the substep kernel,
-    # including the one that splits a bead's Verlet list over several lanes,
-    # follows the FP64 oracle to FP32 round-off over 20 substeps.
+    # including the one that splits a bead's Verlet list over several lanes
+    # and the one that runs stars above 512 beads in a second kernel beside
+    # the rest, follows the FP64 oracle to FP32 round-off over 20 substeps.
     from starpolymersmd_gb300 import system, workloads as W
     specs = _batch_specs() + [system.ReplicaSpec(L=16, arms=6, n_arm=20, solvophobic_fraction=0.3,
-                                                 shear=0.05, seed=34)]
+                                                 shear=0.05, seed=34),
+                              system.ReplicaSpec(L=28, arms=12, n_arm=45,
+                                                 solvophobic_fraction=0.5, shear=0.02, seed=35)]
+    assert max(s.arms * s.n_arm + 1 for s in specs) > 512
     stars, descs = [], []
     for s in specs:
         st = system.make_star(s.arms, s.n_arm, s.solvophobic_fraction, s.mono_mass, s.kT,
@@ -565,3 +569,39 @@ def test_fp32_graph_cycles_match_stepwise(offset):
         b.synchronize()
         for x, y in zip(b.get_fluid(0), a.get_fluid(0)):
             np.testing.assert_array_equal(x, y)
+
+
+def test_fp32_side_by_side_md_in_graph_cycles():
+    # The side-by-side MD shape (stars above 512 beads on a forked stream,
+    # joined before the collision) inside captured cycles, against the
+    # single-kernel lanes-per-bead shape. The FP32 MD sums forces in the order
+    # its shared-memory cell lists come out, so runs agree to FP32 round-off,
+    # not bit for bit: every box, big, mid-sized and small, must follow.
+    from starpolymersmd_gb300 import system, workloads as W
+    specs = [system.ReplicaSpec(L=28, arms=12, n_arm=45, solvophobic_fraction=0.5, shear=0.02,
+                                seed=41),
+             system.ReplicaSpec(L=16, arms=8, n_arm=20, solvophobic_fraction=0.4, shear=0.05,
+                                seed=42),
+             system.ReplicaSpec(L=10, arms=4, n_arm=10, solvophobic_fraction=0.5, shear=0.1,
+                                seed=43)]
+    sizes = [s.arms * s.n_arm + 1 for s in specs]
+    assert sizes[0] > 512 and 64 < sizes[1] <= 512 and sizes[2] <= 64
+    a, b = W.build(specs), W.build(specs)
+    try:
+        a.ctx.set_variants(0, 5, 2)
+        b.ctx.set_variants(0, 5, 3)
+        for x in (a, b):
+            x.ctx.cycles(3)
+            x.ctx.synchronize()
+            x.ctx.raise_on_device_error()
+        for k, s in enumerate(specs):
+            L = (s.L,) * 3
+            (pa, va, _), (pb, vb, _) = a.ctx.get_monomers(k), b.ctx.get_monomers(k)
+            assert np.abs(H.wrapped_diff(pa, pb, L)).max() < 1e-3
+            assert np.abs(va - vb).max() < 1e-2 * np.abs(va).max()
+            (fpa, fva), (fpb, fvb) = a.ctx.get_fluid(k), b.ctx.get_fluid(k)
+            assert np.abs(H.wrapped_diff(fpa, fpb, L)).max() < 1e-3
+            assert np.abs(fva - fvb).max() < 1e-2 * np.abs(fva).max()
+    finally:
+        a.close()
+        b.close()
