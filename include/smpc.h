@@ -53,7 +53,15 @@ enum { SMPC_DELRX_REFERENCE = 0, SMPC_DELRX_PHYSICAL = 1 };
  * gets new velocity components from N(0, sqrt(kT / m)); draws from Philox on
  * the replica's seed (the reference draws from its global Rand stream), or the
  * resets come from the host (smpc_stage_andersen). */
-enum { SMPC_MDTHERMO_NONE = 0, SMPC_MDTHERMO_ANDERSEN = 1 };
+/* LOWE_ANDERSEN: Lowe_Andersen (Lowe_Andersen.cpp:46-88; the reference's
+ * class declares propagate_gaussian without defining it, so its drivers cannot
+ * construct it): after the forces of each substep, every Verlet-list pair
+ * closer than lowe_radius (at most r_cut) collides with probability
+ * nu dt exp(-nu dt) / 2 (nu = andersen_nu), exchanging momentum along its
+ * axis with a relative velocity drawn from N(0, sqrt(kT / mu)); collisions in
+ * the order beads ascending, partners ascending, with Philox draws; one-star
+ * replicas only (SMPC_E_UNSUPPORTED for periodic ones). */
+enum { SMPC_MDTHERMO_NONE = 0, SMPC_MDTHERMO_ANDERSEN = 1, SMPC_MDTHERMO_LOWE_ANDERSEN = 2 };
 /* Replica flags. SMPC_REPLICA_PERIODIC_MD: the box's monomers (any number of
  * stars) interact through the Lees-Edwards minimum image and are kept in the
  * primary box, with Verlet lists on a periodic cell grid and a rebuild
@@ -95,7 +103,8 @@ typedef struct {
   int angular_momentum;   /* 1: angular-momentum-conserving collision in cells of more than two
                              particles (MPC.cpp:260-269, 324-374; MPC(..., angular_mom)) */
   int md_thermostat;      /* SMPC_MDTHERMO_*: thermostat of the MD substeps (MPC-off runs) */
-  double andersen_nu;     /* collision frequency of SMPC_MDTHERMO_ANDERSEN */
+  double andersen_nu;     /* collision frequency of SMPC_MDTHERMO_ANDERSEN and _LOWE_ANDERSEN */
+  double lowe_radius;     /* interaction radius of SMPC_MDTHERMO_LOWE_ANDERSEN */
 } smpc_options;
 
 /* Draws injected for one collision of every replica (reference parity):

@@ -77,6 +77,7 @@ def _oracle_lib():
             "orc_set_periodic_md": [P, C.c_double], "orc_periodic_forces": [P, C.c_int, P],
             "orc_set_andersen": [P, C.c_double, C.c_uint64],
             "orc_stage_andersen": [P, C.c_int, P, P],
+            "orc_set_lowe_andersen": [P, C.c_double, C.c_double, C.c_uint64],
         }.items():
             getattr(lib, name).argtypes = args
             getattr(lib, name).restype = None
@@ -174,6 +175,10 @@ class OracleSystem:
     def set_andersen(self, nu, seed):
         """Andersen stochastic thermostat after every MD step."""
         self.lib.orc_set_andersen(self.h, float(nu), int(seed))
+
+    def set_lowe_andersen(self, nu, radius, seed):
+        """Lowe-Andersen pair thermostat after the forces of every MD step."""
+        self.lib.orc_set_lowe_andersen(self.h, float(nu), float(radius), int(seed))
 
     def stage_andersen(self, mono, vel):
         """Velocity resets of the next MD step in place of the Philox draws:

@@ -99,6 +99,8 @@ struct smpc_orc {
   double andersen_nu;
   uint64_t andersen_seed;
   uint64_t md_step;
+  int lowe;          /* Lowe-Andersen pair thermostat (orc_set_lowe_andersen) */
+  double lowe_radius;
   int and_staged;     /* orc_stage_andersen: resets of the next step */
   int and_n;
   int* and_idx;
@@ -646,6 +648,73 @@ static void andersen_step(smpc_orc* o) {
   }
 }
 
+/* Lowe-Andersen (Lowe_Andersen.cpp:46-88): after the forces, every Verlet-list
+ * candidate (i, j) closer than the radius collides with probability
+ * nu dt exp(-nu dt) / 2; collisions one after another on the updated
+ * velocities, beads i ascending and partners j ascending. Draws restated from
+ * the GPU's layout: Philox on the seed, counter (0x40000000 | i, MD step,
+ * 2 j + k); k = 0: trigger, u1; k = 1: u2; z = sqrt(-2 ln u1) cos(2 pi u2).
+ * The pair arithmetic is Lowe_Andersen::collide (Lowe_Andersen.cpp:28-41). */
+void orc_set_lowe_andersen(smpc_orc* o, double nu, double radius, uint64_t seed) {
+  o->lowe = 1;
+  o->andersen_nu = nu;
+  o->lowe_radius = radius;
+  o->andersen_seed = seed;
+}
+
+static int lowe_cmp_int(const void* a, const void* b) {
+  const int x = *(const int*)a, y = *(const int*)b;
+  return (x > y) - (x < y);
+}
+
+static void lowe_step(smpc_orc* o) {
+  const double nudt = o->andersen_nu * o->p.md_dt * exp(-o->p.md_dt * o->andersen_nu);
+  const double half = nudt * 0.5;
+  const double two_pi = 6.283185307179586476925286766559;
+  int cap = 0;
+  int* js = NULL;
+  for (int i = 0; i < o->n_m; ++i) {
+    const int a = o->vl_start[i], b = o->vl_start[i + 1];
+    if (b - a > cap) {
+      cap = b - a;
+      js = (int*)realloc(js, sizeof(int) * (size_t)cap);
+    }
+    for (int t = a; t < b; ++t) js[t - a] = o->vl_idx[t];
+    qsort(js, (size_t)(b - a), sizeof(int), lowe_cmp_int);
+    const uint32_t c = 0x40000000u | (uint32_t)i;
+    for (int q = 0; q < b - a; ++q) {
+      const int j = js[q];
+      double tr, u1, u2;
+      philox_block(o->andersen_seed, c, o->md_step, 2u * (uint32_t)j, &tr, &u1);
+      if (half < tr) continue;
+      const double* xi = o->mx + 3 * i;
+      const double* xj = o->mx + 3 * j;
+      const double d0 = xj[0] - xi[0], d1 = xj[1] - xi[1], d2 = xj[2] - xi[2];
+      const double dist = sqrt((d0 * d0 + d1 * d1) + d2 * d2);
+      if (!(dist < o->lowe_radius)) continue;
+      philox_block(o->andersen_seed, c, o->md_step, 2u * (uint32_t)j + 1u, &u2, NULL);
+      const double mi = o->mm[i], mj = o->mm[j];
+      const double mu = mi == mj ? 0.5 * mi : mi * mj / (mi + mj);
+      const double sigma = sqrt(o->p.kT / mu);
+      const double z = sqrt(-2.0 * log(u1)) * cos(two_pi * u2);
+      const double e0 = d0 / dist, e1 = d1 / dist, e2 = d2 / dist;
+      const double tv = sigma * z, ci = mu / mi, cj = mu / mj;
+      double* vi = o->mv + 3 * i;
+      double* vj = o->mv + 3 * j;
+      const double w0 = vj[0] - vi[0], w1 = vj[1] - vi[1], w2 = vj[2] - vi[2];
+      const double sc = tv + ((w0 * e0 + w1 * e1) + w2 * e2);
+      const double dv0 = e0 * sc, dv1 = e1 * sc, dv2 = e2 * sc;
+      vi[0] += dv0 * ci;
+      vi[1] += dv1 * ci;
+      vi[2] += dv2 * ci;
+      vj[0] -= dv0 * cj;
+      vj[1] -= dv1 * cj;
+      vj[2] -= dv2 * cj;
+    }
+  }
+  free(js);
+}
+
 static void pmd_propagate(smpc_orc* o, int calc_epot);
 
 void orc_propagate(smpc_orc* o, int calc_epot) {
@@ -663,6 +732,7 @@ void orc_propagate(smpc_orc* o, int calc_epot) {
   }
   check_verlet(o);
   forces_verlet(o, calc_epot);
+  if (o->lowe) lowe_step(o);
   for (int i = 0; i < o->n_m; ++i)
     for (int d = 0; d < 3; ++d) o->mv[3 * i + d] += md_kick(o, o->mf[3 * i + d], o->mm[i], dth);
   if (o->andersen) andersen_step(o);

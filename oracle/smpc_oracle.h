@@ -86,6 +86,9 @@ void orc_init_md(smpc_orc* o);
 void orc_set_periodic_md(smpc_orc* o, double h);
 /* Andersen stochastic thermostat after every MD step (MPC-off runs). */
 void orc_set_andersen(smpc_orc* o, double nu, uint64_t seed);
+/* Lowe-Andersen pair thermostat after the forces of every MD step (MPC-off
+ * runs; non-periodic boxes). */
+void orc_set_lowe_andersen(smpc_orc* o, double nu, double radius, uint64_t seed);
 /* The next MD step's Andersen resets given explicitly (monomer idx[k] gets
  * vel[3k..3k+2] after the second half kick) instead of drawn. */
 void orc_stage_andersen(smpc_orc* o, int n, const int* idx, const double* vel);

@@ -20,7 +20,7 @@ RNG_INJECT, RNG_PHILOX = 0, 1
 POT_REF4824, POT_LJ126 = 0, 1
 MONOBIN_REFERENCE, MONOBIN_WRAPPED = 0, 1
 DELRX_REFERENCE, DELRX_PHYSICAL = 0, 1
-MDTHERMO_NONE, MDTHERMO_ANDERSEN = 0, 1
+MDTHERMO_NONE, MDTHERMO_ANDERSEN, MDTHERMO_LOWE_ANDERSEN = 0, 1, 2
 REPLICA_PERIODIC_MD = 1  # smpc_replica_desc.flags
 
 ERR_BITS = {1: "solvent cell out of range", 2: "monomer cell out of range",
@@ -73,7 +73,8 @@ class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("rng", C.c_int), ("mono_bin", C.c_int),
                 ("delrx_mode", C.c_int), ("step_update", C.c_int), ("max_neighbors", C.c_int),
                 ("strict_cells", C.c_int), ("device", C.c_int), ("angular_momentum", C.c_int),
-                ("md_thermostat", C.c_int), ("andersen_nu", C.c_double)]
+                ("md_thermostat", C.c_int), ("andersen_nu", C.c_double),
+                ("lowe_radius", C.c_double)]
 
 
 class Inject(C.Structure):
@@ -171,7 +172,7 @@ class Context:
     def __init__(self, replicas: Sequence[dict], precision=FP64, rng=RNG_INJECT,
                  mono_bin=MONOBIN_REFERENCE, delrx_mode=DELRX_REFERENCE, step_update=1,
                  max_neighbors=0, strict_cells=None, device=0, angular_momentum=False,
-                 md_thermostat=MDTHERMO_NONE, andersen_nu=0.0):
+                 md_thermostat=MDTHERMO_NONE, andersen_nu=0.0, lowe_radius=0.0):
         self.lib = load()
         n = len(replicas)
         descs = (ReplicaDesc * n)()
@@ -197,7 +198,8 @@ class Context:
             self.replicas.append(dict(r))
         opt = Options(precision, rng, mono_bin, delrx_mode, step_update, max_neighbors,
                       int(precision == FP64 if strict_cells is None else strict_cells), device,
-                      int(bool(angular_momentum)), int(md_thermostat), float(andersen_nu))
+                      int(bool(angular_momentum)), int(md_thermostat), float(andersen_nu),
+                      float(lowe_radius))
         h = C.c_void_p()
         rc = self.lib.smpc_create(descs, n, C.byref(opt), C.byref(h))
         if rc != 0:

@@ -177,7 +177,169 @@ struct MdArgs {
   const int* and_start;
   const int* and_mono;
   const double* and_vel;
+  // Lowe-Andersen pair thermostat (MPC-off runs): collision frequency in
+  // andersen_nu, interaction radius, scratch of LOWE_MAX LoweEntry<R> per
+  // monomer (null when off)
+  int lowe;
+  double lowe_radius;
+  void* lowe_buf;
 };
+
+// Lowe-Andersen thermostat (Lowe_Andersen::propagate, Thermostats/
+// Lowe_Andersen.cpp:46-88): after the forces of a substep and before its
+// second half kick, every Verlet-list entry (i, j) is a collision candidate
+// with probability NuDt / 2, NuDt = nu dt exp(-nu dt); a candidate closer than
+// the interaction radius exchanges momentum along the pair axis e:
+//   dv = e (sqrt(kT / mu) z + (v_j - v_i) . e),  v_i += dv mu / m_i,  v_j -= dv mu / m_j,
+// mu the reduced mass (m / 2 for equal masses), z a standard normal.
+// Collisions act one after another on the updated velocities, so their order
+// is part of the result: here it is canonical, beads i ascending and each
+// bead's partners j ascending (the reference walks its lists in the order its
+// cell lists produce). Draws: Philox on the replica's seed, counter
+// (LOWE_STREAM | i, MD substep, 2 j + k): k = 0 gives the trigger uniform and
+// u1, k = 1 gives u2; z = sqrt(-2 ln u1) cos(2 pi u2).
+constexpr uint32_t LOWE_STREAM = 0x40000000u;
+constexpr int LOWE_MAX = 16;  // accepted collisions per bead and substep (an error beyond)
+
+template <typename R>
+struct LoweEntry {
+  int i, j;
+  R e0, e1, e2;  // unit pair axis, from i to j
+  R tv;          // sqrt(kT / mu) z
+  R ci, cj;      // mu / m_i, mu / m_j
+};
+
+// One substep's collisions of the replica at monomer base b (n beads), run by
+// the whole CTA: candidates by each bead's lead lane, offsets by warp 0, the
+// velocity updates in canonical order by thread 0 on velocities staged in
+// sx/sy/sz (the positions there are not needed again before the next drift
+// rewrites them). v[k] of every lane comes back updated.
+template <typename R, int NT, int MPT>
+__device__ void lowe_andersen_pass(const MdArgs& a, const RepInfo& ri, int b, int n, int slot,
+                                   bool lead, unsigned long long md_step, const R (&x)[MPT][3],
+                                   R (&v)[MPT][3], const R (&m)[MPT], const R* mpos, R* sx, R* sy,
+                                   R* sz, int* s_cnt, int* s_off, int* s_total) {
+  LoweEntry<R>* buf = static_cast<LoweEntry<R>*>(a.lowe_buf) + static_cast<size_t>(b) * LOWE_MAX;
+  const double nudt = a.andersen_nu * ri.md_dt * exp(-ri.md_dt * a.andersen_nu);
+  const R half = static_cast<R>(nudt * 0.5);
+  const R radius = static_cast<R>(a.lowe_radius);
+  const R kT = static_cast<R>(ri.kT);
+  const size_t stride = static_cast<size_t>(a.n_mono_total);
+  int acc[MPT][LOWE_MAX];
+  int na[MPT];
+  __syncthreads();  // the forces are done with sx/sy/sz
+#pragma unroll
+  for (int k = 0; k < MPT; ++k) {
+    const int i = slot + k * NT;
+    na[k] = 0;
+    if (i >= n || !lead) continue;
+    const int cnt = a.ncount[b + i];
+    for (int q = 0; q < cnt; ++q) {
+      const int j = a.nlist[static_cast<size_t>(q) * stride + b + i] - b;
+      const Uniform2<R> t = philox_uniforms<R>(ri.seed, LOWE_STREAM | static_cast<uint32_t>(i),
+                                               md_step, 2u * static_cast<uint32_t>(j));
+      if (half < t.a) continue;  // Lowe_Andersen.cpp:71
+      const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
+      if (!(r_sqrt((d0 * d0 + d1 * d1) + d2 * d2) < radius)) continue;  // Lowe_Andersen.cpp:31
+      if (na[k] < LOWE_MAX) {
+        int p = na[k];
+        while (p > 0 && acc[k][p - 1] > j) {
+          acc[k][p] = acc[k][p - 1];
+          --p;
+        }
+        acc[k][p] = j;
+      } else {
+        raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(b + i), LOWE_MAX + 1u);
+      }
+      ++na[k];
+    }
+    if (na[k] > LOWE_MAX) na[k] = LOWE_MAX;
+    s_cnt[i] = na[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {  // exclusive offsets of the beads' collisions
+    const int lane = threadIdx.x;
+    int carry = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int i = base + lane;
+      const int c = i < n ? s_cnt[i] : 0;
+      int incl = c;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (i < n) s_off[i] = carry + incl - c;
+      carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    if (lane == 0) *s_total = carry;
+  }
+  __syncthreads();
+  const R two_pi = R(6.283185307179586476925286766559);
+#pragma unroll
+  for (int k = 0; k < MPT; ++k) {
+    const int i = slot + k * NT;
+    if (i >= n || !lead) continue;
+    for (int q = 0; q < na[k]; ++q) {
+      const int j = acc[k][q];
+      const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
+      const R dist = r_sqrt((d0 * d0 + d1 * d1) + d2 * d2);
+      const R mi = m[k], mj = mpos[4 * static_cast<size_t>(b + j) + 3];
+      const R mu = mi == mj ? R(0.5) * mi : mi * mj / (mi + mj);
+      const R sigma = r_sqrt(kT / mu);
+      const uint32_t c = LOWE_STREAM | static_cast<uint32_t>(i);
+      const Uniform2<R> t0 = philox_uniforms<R>(ri.seed, c, md_step, 2u * static_cast<uint32_t>(j));
+      const Uniform2<R> t1 =
+          philox_uniforms<R>(ri.seed, c, md_step, 2u * static_cast<uint32_t>(j) + 1u);
+      const R z = r_sqrt(R(-2) * r_log(t0.b)) * r_cos(two_pi * t1.a);
+      LoweEntry<R> e;
+      e.i = i;
+      e.j = j;
+      e.e0 = d0 / dist;
+      e.e1 = d1 / dist;
+      e.e2 = d2 / dist;
+      e.tv = sigma * z;
+      e.ci = mu / mi;
+      e.cj = mu / mj;
+      buf[s_off[i] + q] = e;
+    }
+  }
+  __syncthreads();  // entries written, positions no longer read
+#pragma unroll
+  for (int k = 0; k < MPT; ++k) {
+    const int i = slot + k * NT;
+    if (i < n && lead) {
+      sx[i] = v[k][0];
+      sy[i] = v[k][1];
+      sz[i] = v[k][2];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int total = *s_total;
+    for (int q = 0; q < total; ++q) {
+      const LoweEntry<R> e = buf[q];
+      const R w0 = sx[e.j] - sx[e.i], w1 = sy[e.j] - sy[e.i], w2 = sz[e.j] - sz[e.i];
+      const R sc = e.tv + ((w0 * e.e0 + w1 * e.e1) + w2 * e.e2);
+      const R dv0 = e.e0 * sc, dv1 = e.e1 * sc, dv2 = e.e2 * sc;
+      sx[e.i] += dv0 * e.ci;
+      sy[e.i] += dv1 * e.ci;
+      sz[e.i] += dv2 * e.ci;
+      sx[e.j] -= dv0 * e.cj;
+      sy[e.j] -= dv1 * e.cj;
+      sz[e.j] -= dv2 * e.cj;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < MPT; ++k) {
+    const int i = slot + k * NT;
+    if (i < n) {
+      v[k][0] = sx[i];
+      v[k][1] = sy[i];
+      v[k][2] = sz[i];
+    }
+  }
+}
 
 // Cell key of a position on a grid of side rv: three 10-bit fields
 // (coordinates within +-512 cells of the origin) and a bucket hash.
@@ -206,6 +368,7 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
   __shared__ int s_ckey[CAP];
   __shared__ R s_core_ref[3];
   __shared__ int s_rebuild;
+  __shared__ int s_lowe_total;
   __shared__ double s_red[NT / 32];
   const int r = a.order ? a.order[blockIdx.x] : static_cast<int>(blockIdx.x);
   const RepInfo ri = a.reps[r];
@@ -419,7 +582,7 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
       }
       if (i < n) {
         f[k][0] = F0; f[k][1] = F1; f[k][2] = F2;
-        if (a.n_steps > 0) {
+        if (a.n_steps > 0 && !a.lowe) {
           for (int d = 0; d < 3; ++d)  // second half-kick
             v[k][d] += a.andersen ? f[k][d] * (dth / m[k]) : (f[k][d] / m[k]) * dth;
           if (a.andersen) {
@@ -436,6 +599,18 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
             }
           }
         }
+      }
+    }
+    if (a.lowe && a.n_steps > 0) {
+      // pair collisions between the forces and the second half kick
+      lowe_andersen_pass<R, NT, MPT>(a, ri, b, n, slot, lead,
+                                     md_step0 + static_cast<unsigned long long>(step), x, v, m,
+                                     mpos, sx, sy, sz, s_next, s_ckey, &s_lowe_total);
+#pragma unroll
+      for (int k = 0; k < MPT; ++k) {
+        const int i = slot + k * NT;
+        if (i < n)
+          for (int d = 0; d < 3; ++d) v[k][d] += (f[k][d] / m[k]) * dth;
       }
     }
     __syncthreads();  // positions are rewritten by the next drift

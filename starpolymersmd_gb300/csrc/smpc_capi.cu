@@ -71,6 +71,7 @@ struct smpc_ctx {
   int* d_ncount = nullptr;
   int* d_md_order = nullptr;  // replicas by decreasing monomer count (MD CTA order)
   smpc::MdSplit md_split{};   // side-by-side MD launch shape: second stream, events, split
+  void* d_lowe = nullptr;     // Lowe-Andersen collision entries, LOWE_MAX per monomer
   bool any_local_md = false;  // a non-periodic replica has monomers
   // Andersen resets staged for the next smpc_md_substeps (smpc_stage_andersen):
   // per replica the staged substep count (-1: none) and the host tables; the
@@ -273,6 +274,9 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
   a.and_start = ctx->and_start_dev;
   a.and_mono = ctx->and_mono_dev;
   a.and_vel = ctx->and_vel_dev;
+  a.lowe = ctx->opt.md_thermostat == SMPC_MDTHERMO_LOWE_ANDERSEN ? 1 : 0;
+  a.lowe_radius = ctx->opt.lowe_radius;
+  a.lowe_buf = ctx->d_lowe;
   smpc::launch_md<R>(a, ctx->n_rep, static_cast<R*>(ctx->d_mpos), static_cast<R*>(ctx->d_mvel),
                      static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), ctx->var_md,
                      ctx->st, ctx->md_split);
@@ -591,6 +595,8 @@ int create_buffers(smpc_ctx* ctx) {
   CU(dalloc(&ctx->d_mkey, M));
   CU(dalloc(&ctx->d_mimg, M));
   CU(dalloc(&ctx->d_ncount, M));
+  if (ctx->opt.md_thermostat == SMPC_MDTHERMO_LOWE_ANDERSEN && M > 0)
+    CU(cudaMalloc(&ctx->d_lowe, M * smpc::LOWE_MAX * sizeof(smpc::LoweEntry<R>)));
   CU(cudaMemset(ctx->d_ncount, 0, (M ? M : 1) * sizeof(int)));
   {
     // largest replicas first, so the MD kernel's last wave holds small ones
@@ -667,6 +673,7 @@ void free_all(smpc_ctx* ctx) {
   if (ctx->d_rows_by_rep) cudaFree(ctx->d_rows_by_rep);
   if (ctx->d_stress) cudaFree(ctx->d_stress);
   if (ctx->d_pamphi) cudaFree(ctx->d_pamphi);
+  if (ctx->d_lowe) cudaFree(ctx->d_lowe);
   if (ctx->d_and_i) cudaFree(ctx->d_and_i);
   if (ctx->d_and_v) cudaFree(ctx->d_and_v);
   void* ptrs[] = {ctx->d_reps, ctx->d_dyn, ctx->d_bin_tiles, ctx->d_col_tiles, ctx->d_tmp_tiles,
@@ -911,9 +918,13 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
     return code;
   };
   if (opt->precision != SMPC_FP64 && opt->precision != SMPC_FP32) return bail(SMPC_E_ARG, "precision");
-  if (opt->md_thermostat != SMPC_MDTHERMO_NONE &&
-      (opt->md_thermostat != SMPC_MDTHERMO_ANDERSEN || !(opt->andersen_nu >= 0)))
+  if (opt->md_thermostat != SMPC_MDTHERMO_NONE && opt->md_thermostat != SMPC_MDTHERMO_ANDERSEN &&
+      opt->md_thermostat != SMPC_MDTHERMO_LOWE_ANDERSEN)
     return bail(SMPC_E_ARG, "md thermostat");
+  if (opt->md_thermostat != SMPC_MDTHERMO_NONE && !(opt->andersen_nu >= 0))
+    return bail(SMPC_E_ARG, "md thermostat frequency");
+  const bool lowe = opt->md_thermostat == SMPC_MDTHERMO_LOWE_ANDERSEN;
+  if (lowe && !(opt->lowe_radius > 0)) return bail(SMPC_E_ARG, "Lowe-Andersen radius");
   if (cudaSetDevice(ctx->device) != cudaSuccess) return bail(SMPC_E_CUDA, "cudaSetDevice");
   long long cells = 0, slots = 0, mono = 0;
   for (int r = 0; r < n_rep; ++r) {
@@ -924,6 +935,12 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
     const bool periodic = (d.flags & SMPC_REPLICA_PERIODIC_MD) != 0;
     if (!periodic && d.n_mono > smpc::md_max_monomers())
       return bail(SMPC_E_UNSUPPORTED, "too many monomers");
+    if (lowe && periodic && d.n_mono > 0)
+      return bail(SMPC_E_UNSUPPORTED, "Lowe-Andersen on a periodic box");
+    // pairs inside the radius must be in the Verlet lists, which hold every
+    // pair inside r_cut at any substep
+    if (lowe && d.n_mono > 0 && opt->lowe_radius > d.r_cut)
+      return bail(SMPC_E_ARG, "Lowe-Andersen radius above r_cut");
     if (periodic) {
       if (opt->mono_bin != SMPC_MONOBIN_WRAPPED)
         return bail(SMPC_E_ARG, "periodic MD needs wrapped monomer binning");

@@ -166,3 +166,79 @@ def test_staging_needs_the_andersen_thermostat():
     with capi.Context([rep], precision=capi.FP64, rng=capi.RNG_PHILOX, step_update=1000) as ctx:
         with pytest.raises(capi.SmpcError):
             ctx.stage_andersen(0, [0, 0], [], np.zeros((0, 3)))
+
+
+LOWE_NU, LOWE_R = 20.0, 1.5
+
+
+def _lowe_pair(precision, seed=7, n_arm=8, arms=6, L=16):
+    star, _, _ = H.small_star_system(L=L, n_c=1, arms=arms, n_arm=n_arm, seed=seed)
+    n = star.n
+    o = orc.OracleSystem((L, L, L), 1.0, 0.0, 1000, 0, n, mol_start=[0, n])
+    o.set_monomers(star.pos, star.vel, np.zeros_like(star.pos), np.full(n, star.mass),
+                   star.amphi, star.anchor)
+    o.set_bonds(star.bond_src, star.bond_dst)
+    o.set_lowe_andersen(LOWE_NU, LOWE_R, SEED)
+    o.init_md()
+    rep = dict(L=(L, L, L), n_fluid=0, n_mono=n, mol0_size=n, kT=1.0, shear=0.0, h=0.1,
+               md_dt=0.01, seed=SEED, **{"lambda": 1.0})
+    ctx = capi.Context([rep], precision=precision, rng=capi.RNG_PHILOX, step_update=1000,
+                       md_thermostat=capi.MDTHERMO_LOWE_ANDERSEN, andersen_nu=LOWE_NU,
+                       lowe_radius=LOWE_R)
+    ctx.set_monomers(0, star.pos, star.vel, np.zeros_like(star.pos), np.full(n, star.mass),
+                     star.amphi, star.anchor)
+    ctx.set_bonds(0, star.bond_src, star.bond_dst)
+    ctx.init_md()
+    return star, o, ctx
+
+
+def test_fp64_lowe_andersen_matches_oracle():
+    # the pair collisions in canonical order (beads ascending, partners
+    # ascending) on the same Philox draws as the oracle's restatement of
+    # Lowe_Andersen::propagate (Lowe_Andersen.cpp:46-88)
+    star, o, ctx = _lowe_pair(capi.FP64)
+    with ctx:
+        before = ctx.get_monomers(0)[1].copy()
+        for _ in range(40):
+            o.propagate(False)
+        ctx.md_substeps(25)
+        ctx.md_substeps(15)
+        ctx.raise_on_device_error()
+        mp, mv, mf = ctx.get_monomers(0)
+        op, ov, of = o.get_monomers()
+        H.close64(mp, op, rtol=1e-11)
+        H.close64(mv, ov, rtol=1e-11)
+        H.close64(mf, of, rtol=1e-11)
+        assert np.abs(mv - before).max() > 0.1  # the thermostat did act
+
+
+def test_fp32_lowe_andersen_conserves_momentum_and_holds_kT():
+    star, o, ctx = _lowe_pair(capi.FP32, seed=9, n_arm=12, arms=8)
+    with ctx:
+        m = star.mass
+        p0 = m * ctx.get_monomers(0)[1].sum(axis=0)
+        temps = []
+        for _ in range(30):
+            ctx.md_substeps(100)
+            v = ctx.get_monomers(0)[1]
+            u = v - v.mean(axis=0)
+            temps.append(m * (u * u).sum() / (3 * (len(v) - 1)))
+        ctx.raise_on_device_error()
+        p1 = m * ctx.get_monomers(0)[1].sum(axis=0)
+        scale = m * np.sqrt(len(v)) * 1.0 / np.sqrt(m)
+        assert np.abs(p1 - p0).max() < 1e-3 * scale  # pairwise exchanges conserve momentum
+        assert abs(np.mean(temps[5:]) - 1.0) < 0.12
+
+
+def test_lowe_andersen_limits():
+    # radius above r_cut, or a periodic box: refused at creation
+    rep = dict(L=(12, 12, 12), n_fluid=0, n_mono=10, mol0_size=10, kT=1.0, md_dt=0.01,
+               r_cut=1.5, r_verlet=2.0)
+    with pytest.raises(capi.SmpcError):
+        capi.Context([rep], precision=capi.FP64, rng=capi.RNG_PHILOX,
+                     md_thermostat=capi.MDTHERMO_LOWE_ANDERSEN, andersen_nu=1.0, lowe_radius=1.8)
+    per = dict(rep, flags=capi.REPLICA_PERIODIC_MD)
+    with pytest.raises(capi.SmpcError):
+        capi.Context([per], precision=capi.FP64, rng=capi.RNG_PHILOX,
+                     mono_bin=capi.MONOBIN_WRAPPED,
+                     md_thermostat=capi.MDTHERMO_LOWE_ANDERSEN, andersen_nu=1.0, lowe_radius=1.0)
