@@ -43,6 +43,7 @@ AndersenStochastic::AndersenStochastic(Box& box, double dt, double T, double nu,
   bc.md_dt = dt;
   bc.md_thermostat = SMPC_MDTHERMO_ANDERSEN;
   bc.andersen_nu = nu;
+  bc.md_kT = T;
   update_temp();
   dtime(dt);
   SimBox.update_VerletLists();

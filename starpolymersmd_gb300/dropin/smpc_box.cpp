@@ -123,7 +123,7 @@ smpc_ctx* ensure(Box& box) {
   d.n_fluid = bc.has_solvent ? static_cast<int>(bc.n_fluid) : 0;
   d.n_mono = static_cast<int>(n_mono);
   d.mol0_size = box.Molecules.empty() ? 0 : static_cast<int>(box.Molecules[0].Monomers.size());
-  d.kT = bc.has_solvent ? bc.kT : box.Temperature;
+  d.kT = bc.has_solvent ? bc.kT : (bc.md_kT > 0 ? bc.md_kT : box.Temperature);
   d.shear = bc.shear;
   d.h = 0.1;  // replaced by the dt of every MPC::step
   d.md_dt = bc.md_dt;
@@ -146,6 +146,7 @@ smpc_ctx* ensure(Box& box) {
   o.angular_momentum = bc.angular_momentum ? 1 : 0;
   o.md_thermostat = bc.md_thermostat;
   o.andersen_nu = bc.andersen_nu;
+  o.lowe_radius = bc.lowe_radius;
   smpc_ctx* ctx = nullptr;
   int rc = smpc_create(&d, 1, &o, &ctx);
   if (rc != SMPC_OK) fail(ctx, "smpc_create", rc);

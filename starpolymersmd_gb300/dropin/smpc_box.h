@@ -35,12 +35,15 @@ struct BoxContext {
   unsigned step_update = 1;
   unsigned n_fluid = 0;
   bool angular_momentum = false;  // MPC(..., angular_mom)
-  // integrator, registered by the Thermostat_GPU or AndersenStochastic
-  // constructor (SMPC_MDTHERMO_ANDERSEN for the latter, with its frequency)
+  // integrator, registered by the Thermostat_GPU, AndersenStochastic or
+  // Lowe_Andersen constructor (the thermostat kind, its frequency, radius
+  // and temperature)
   bool has_md = false;
   double md_dt = 0.01;
   int md_thermostat = SMPC_MDTHERMO_NONE;
   double andersen_nu = 0.0;
+  double lowe_radius = 0.0;
+  double md_kT = 0.0;  // the thermostat's temperature (> 0), used when there is no solvent
   // device holds the newer monomer state than Box::Molecules
   bool mono_on_device = false;
   bool md_ready = false;
