@@ -111,3 +111,16 @@ def test_pressure_tensor_of_one_star():
         np.testing.assert_allclose(vir[0], wv, rtol=1e-10, atol=1e-10 * np.abs(wv).max())
         # the solvent alone, at rest on average in the flow frame: kT on the diagonal
         assert np.all(np.abs(kin[0][:3] * L ** 3 / len(fp) - 1.0) < 0.3)
+
+
+def test_precision_report_runs_both_paths():
+    # the FP32-versus-FP64 report on a small workload: both runs sample, the
+    # momentum along y and z is conserved, the kinetic temperature is near kT
+    from starpolymersmd_gb300 import precision_report as P
+    r = P.report("single_star_20", cycles=6, every=2)
+    assert set(r["momentum_yz_drift_per_particle"]) == {"fp32", "fp64"}
+    assert r["momentum_yz_drift_per_particle"]["fp64"] < 1e-12
+    assert r["momentum_yz_drift_per_particle"]["fp32"] < 1e-6
+    for name in ("fp32", "fp64"):
+        assert abs(r["temperature_kinetic"][name] - 1.0) < 0.05
+    assert len(r["gyration"]["fp32"]) == 9
