@@ -56,6 +56,9 @@ def parse_args():
 # ----------------------------------------------------------------- helpers
 
 def dist_setup(args):
+    """One process per GPU under torchrun (RANK, LOCAL_RANK, WORLD_SIZE, MASTER_*).
+    NCCL on GPU machines; gloo where no GPU is visible (host-side tests) or when
+    SMPC_DIST_BACKEND names it."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -63,8 +66,11 @@ def dist_setup(args):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        backend = os.environ.get("SMPC_DIST_BACKEND") or (
+            "nccl" if torch.cuda.is_available() else "gloo")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local, dist
 
 
@@ -77,9 +83,16 @@ def max_over_ranks(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_value(units, steps, world, ms_max):
+    """Whole-job throughput: every rank processes `units` per step (replicas
+    only, weak scaling), timed by the slowest rank."""
+    return units * steps * world / (ms_max / 1e3)
 
 
 def measured_peaks():
@@ -247,7 +260,7 @@ def run_ours(args, world, rank, local, dist):
     ctx.raise_on_device_error()
     ms = max_over_ranks(dist, ms)
     barrier(dist)
-    value = units * K * world / (ms / 1e3)
+    value = job_value(units, K, world, ms)
     rep_steps = built.n_rep * K * world / (ms / 1e3)
 
     # per-kernel device times over a second timed region (events on the stream)
