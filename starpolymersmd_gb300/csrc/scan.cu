@@ -43,28 +43,52 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
   return before;
 }
 
+// One tile of SCAN_TILE cells per CTA. Warp w owns the tile's w-th run of
+// 32 * SCAN_IPT consecutive cells, read as SCAN_IPT rows of 32 (every load and
+// store of a warp is one contiguous 128-byte row); each row is a warp scan
+// carried into the next, then the warps' totals give each warp's base.
 __global__ void __launch_bounds__(SCAN_NT) k_scan_tiles(uint32_t* __restrict__ count,
                                                         uint32_t* __restrict__ off,
                                                         uint32_t* __restrict__ tile_sum, int n) {
-  const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
-  uint32_t c[SCAN_IPT];
-  uint32_t s = 0;
+  __shared__ uint32_t warp_tot[SCAN_NT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int seg = blockIdx.x * SCAN_TILE + w * (32 * SCAN_IPT);
+  uint32_t c[SCAN_IPT], pre[SCAN_IPT];
 #pragma unroll
   for (int k = 0; k < SCAN_IPT; ++k) {
-    const int i = base + k;
+    const int i = seg + 32 * k + lane;
     c[k] = i < n ? count[i] : 0u;
-    s += c[k];
   }
 #pragma unroll
-  for (int k = 0; k < SCAN_IPT; ++k)
-    if (base + k < n) count[base + k] = 0u;
-  uint32_t total;
-  uint32_t run = block_exclusive_scan(s, &total);
+  for (int k = 0; k < SCAN_IPT; ++k) {
+    const int i = seg + 32 * k + lane;
+    if (i < n) count[i] = 0u;  // re-zeroed for the next collision
+  }
+  uint32_t carry = 0;
 #pragma unroll
   for (int k = 0; k < SCAN_IPT; ++k) {
-    const int i = base + k;
-    if (i < n) off[i] = run;
-    run += c[k];
+    uint32_t x = c[k];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= o) x += y;
+    }
+    pre[k] = carry + x - c[k];
+    carry += __shfl_sync(0xFFFFFFFFu, x, 31);
+  }
+  if (lane == 0) warp_tot[w] = carry;
+  __syncthreads();
+  uint32_t wbase = 0, total = 0;
+#pragma unroll
+  for (int q = 0; q < SCAN_NT / 32; ++q) {
+    const uint32_t t = warp_tot[q];
+    if (q < w) wbase += t;
+    total += t;
+  }
+#pragma unroll
+  for (int k = 0; k < SCAN_IPT; ++k) {
+    const int i = seg + 32 * k + lane;
+    if (i < n) off[i] = wbase + pre[k];
   }
   if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
 }
@@ -96,12 +120,24 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_tile_sums(uint32_t* __restrict
   if (threadIdx.x == 0) *grand = carry;
 }
 
+// SCAN_ADD_U cells per thread, a block apart (coalesced, independent loads)
+constexpr int SCAN_ADD_U = 4;
 __global__ void __launch_bounds__(SCAN_NT) k_scan_add(uint32_t* __restrict__ off,
                                                       const uint32_t* __restrict__ tile_base,
                                                       const uint32_t* __restrict__ grand, int n) {
-  const int i = blockIdx.x * SCAN_NT + threadIdx.x;
-  if (i < n) off[i] += tile_base[i / SCAN_TILE];
-  if (i == n) off[n] = *grand;
+  const int base = blockIdx.x * (SCAN_NT * SCAN_ADD_U) + threadIdx.x;
+  uint32_t v[SCAN_ADD_U];
+#pragma unroll
+  for (int u = 0; u < SCAN_ADD_U; ++u) {
+    const int i = base + u * SCAN_NT;
+    v[u] = i < n ? off[i] + tile_base[i / SCAN_TILE] : 0u;
+  }
+#pragma unroll
+  for (int u = 0; u < SCAN_ADD_U; ++u) {
+    const int i = base + u * SCAN_NT;
+    if (i < n) off[i] = v[u];
+    if (i == n) off[n] = *grand;
+  }
 }
 
 // perm[off[cell] + rank] = source. Each thread takes PERM_U entries a block
@@ -144,8 +180,9 @@ void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* g
   const int tiles = scan_tile_count(n_cells);
   k_scan_tiles<<<tiles, SCAN_NT, 0, st>>>(count, off, tile_sum, n_cells);
   k_scan_tile_sums<<<1, SCAN_NT, 0, st>>>(tile_sum, tiles, grand);
-  k_scan_add<<<(n_cells + 1 + SCAN_NT - 1) / SCAN_NT, SCAN_NT, 0, st>>>(off, tile_sum, grand,
-                                                                       n_cells);
+  const int per_block = SCAN_NT * SCAN_ADD_U;
+  k_scan_add<<<(n_cells + 1 + per_block - 1) / per_block, SCAN_NT, 0, st>>>(off, tile_sum, grand,
+                                                                           n_cells);
 }
 
 void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_mono,
