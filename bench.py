@@ -355,30 +355,31 @@ def e2e_measure(ctx, built, K):
     position and velocity from pinned host memory, run the cycle, read the
     monomer state and every replica's output-step observables back (gyration
     tensor, rotation frequency, polymer kinetic energy and temperature: what
-    the reference driver reads after a step, star-polymers.cpp:466-473)."""
+    the reference driver reads after a step, star-polymers.cpp:466-473), all
+    in one smpc_cycles_io call with one synchronisation."""
     import torch
+    from starpolymersmd_gb300 import capi
     n = int(sum(built.n_mono))
     pos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     vel = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    obs = torch.empty((built.n_rep, capi.OBS_PER_REP), dtype=torch.float64,
+                      pin_memory=True).numpy()
     ctx.get_monomer_state_all(pos, vel)
     k = max(3, min(K, 50))
     ctx.synchronize()
     t0 = time.perf_counter()
     for _ in range(k):
-        ctx.set_monomer_state_all(pos, vel)
-        ctx.cycles(1)
-        ctx.get_monomer_state_all(pos, vel)
-        obs = ctx.molecule_observables_all()
+        ctx.cycles_io(1, pos, vel, pos, vel, obs)
     dt = time.perf_counter() - t0
     ctx.raise_on_device_error()
     if not np.all(np.isfinite(obs)):
         raise RuntimeError("non-finite observables")
-    h2d = n * 2 * 16  # float4 positions + velocities
-    d2h = n * 2 * 16 + built.n_rep * 16 * 8
+    h2d = n * 6 * 8  # positions + velocities, 3 doubles each
+    d2h = n * 6 * 8 + built.n_rep * capi.OBS_PER_REP * 8
     return {"value": built.particles * k / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": k,
-            "what": "per cycle: monomer state up, cycle, monomer state + per-replica "
-                    "gyration tensor / rotation frequency / polymer temperature down"}
+            "what": "per cycle, one smpc_cycles_io call: monomer state up, cycle, monomer state "
+                    "+ per-replica gyration tensor / rotation frequency / polymer temperature down"}
 
 
 # ---------------------------------------------------------- reference arm

@@ -228,6 +228,15 @@ int smpc_temperature_all_noalloc(smpc_ctx* ctx, double* out);
  * rebuild their Verlet lists at the next substep. */
 int smpc_set_monomer_state_all(smpc_ctx* ctx, const double* pos, const double* vel);
 int smpc_get_monomer_state_all(smpc_ctx* ctx, double* pos, double* vel, double* force);
+/* One call per output step of a host-side driver (star-polymers.cpp:466-534):
+ * smpc_set_monomer_state_all(pos_in, vel_in) when pos_in is given, n fused
+ * cycles (smpc_cycles), smpc_get_monomer_state_all(pos_out, vel_out) when
+ * pos_out is given and smpc_molecule_observables_all(obs_out) when obs_out is
+ * given, queued on the context's stream with one synchronisation at the end
+ * (copies from and to pinned buffers overlap nothing else but skip the host
+ * round trips between the parts). pos_in and pos_out may be the same array. */
+int smpc_cycles_io(smpc_ctx* ctx, int n, const double* pos_in, const double* vel_in,
+                   double* pos_out, double* vel_out, double* obs_out);
 int smpc_delrx(smpc_ctx* ctx, int rep, double* out);
 int smpc_set_delrx(smpc_ctx* ctx, int rep, double delrx);
 /* Cell occupancies of the last collision: MPCCellList sizes and

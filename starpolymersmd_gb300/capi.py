@@ -36,7 +36,7 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_cell_counts", "smpc_cell_members", "smpc_set_collision_counter", "smpc_verlet_rebuilds",
            "smpc_error_word", "smpc_synchronize", "smpc_cycles_profiled", "smpc_time_cycles",
            "smpc_init_solvent", "smpc_temperature_all", "smpc_temperature_all_noalloc",
-           "smpc_set_monomer_state_all",
+           "smpc_set_monomer_state_all", "smpc_cycles_io",
            "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
            "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide", "smpc_set_molecules",
            "smpc_molecule_observables_all", "smpc_velocity_profile", "smpc_checkpoint_size",
@@ -108,6 +108,7 @@ def load(path: Optional[str] = None):
         "smpc_set_bonds": ([P, I, I, P, P], I),
         "smpc_init_md": ([P], I),
         "smpc_md_substeps": ([P, I, I], I),
+        "smpc_cycles_io": ([P, I, P, P, P, P, P], I),
         "smpc_stage_andersen": ([P, I, I, P, P, P], I),
         "smpc_mpc_step": ([P, C.c_long, D, C.POINTER(Inject)], I),
         "smpc_cycles": ([P, I], I),
@@ -366,6 +367,12 @@ class Context:
     def set_monomer_state_all(self, pos, vel):
         self._check(self.lib.smpc_set_monomer_state_all(self.h, _p(pos), _p(vel)),
                     "set_monomer_state_all")
+
+    def cycles_io(self, n, pos_in=None, vel_in=None, pos_out=None, vel_out=None, obs_out=None):
+        """Monomer state in, n fused cycles, monomer state and observables out,
+        with one synchronisation (smpc_cycles_io)."""
+        self._check(self.lib.smpc_cycles_io(self.h, n, _p(pos_in), _p(vel_in), _p(pos_out),
+                                            _p(vel_out), _p(obs_out)), "cycles_io")
 
     def get_monomer_state_all(self, pos, vel, force=None):
         self._check(self.lib.smpc_get_monomer_state_all(self.h, _p(pos), _p(vel), _p(force)),

@@ -476,7 +476,7 @@ int get_monomers_t(smpc_ctx* ctx, int rep, double* pos, double* vel, double* for
 // (DMA at full speed when they are pinned) and converted on the device.
 template <typename R>
 int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, double* pos_out,
-                   double* vel_out, double* force_out) {
+                   double* vel_out, double* force_out, bool sync = true) {
   const size_t n = static_cast<size_t>(ctx->total_mono);
   if (n == 0) return SMPC_OK;
   const int ni = static_cast<int>(n);
@@ -493,7 +493,7 @@ int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, do
     const int one = 1;
     for (const smpc::PmdArgs& a : ctx->pmd)
       CU(cudaMemcpyAsync(a.flag + 1, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
-    CU(cudaStreamSynchronize(ctx->st));  // the host arrays are borrowed for the call only
+    if (sync) CU(cudaStreamSynchronize(ctx->st));  // the host arrays are borrowed for the call only
     return SMPC_OK;
   }
   smpc::launch_pack_monomers<R>(static_cast<const R*>(ctx->d_mpos), static_cast<const R*>(ctx->d_mvel),
@@ -508,7 +508,7 @@ int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, do
   if (force_out)
     CU(cudaMemcpyAsync(force_out, ctx->d_dstage + 6 * n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
                        ctx->st));
-  CU(cudaStreamSynchronize(ctx->st));
+  if (sync) CU(cudaStreamSynchronize(ctx->st));
   return SMPC_OK;
 }
 
@@ -1776,6 +1776,38 @@ int smpc_molecule_observables_all(smpc_ctx* ctx, double* out) {
   CU(cudaMemcpyAsync(out, ctx->d_obs, static_cast<size_t>(ctx->n_rep) * smpc::OBS_PER_REP * sizeof(double),
                      cudaMemcpyDeviceToHost, ctx->st));
   CU(cudaStreamSynchronize(ctx->st));
+  return SMPC_OK;
+}
+
+int smpc_cycles_io(smpc_ctx* ctx, int n, const double* pos_in, const double* vel_in,
+                   double* pos_out, double* vel_out, double* obs_out) {
+  if (!ctx || n < 0) return SMPC_E_ARG;
+  if ((pos_in == nullptr) != (vel_in == nullptr) || (pos_out == nullptr) != (vel_out == nullptr))
+    return fail(ctx, SMPC_E_ARG, "positions and velocities go together");
+  cudaSetDevice(ctx->device);
+  const bool fp64 = ctx->opt.precision == SMPC_FP64;
+  if (pos_in) {
+    int rc = fp64 ? monomers_all_t<double>(ctx, pos_in, vel_in, nullptr, nullptr, nullptr, false)
+                  : monomers_all_t<float>(ctx, pos_in, vel_in, nullptr, nullptr, nullptr, false);
+    if (rc) return rc;
+  }
+  if (int rc = smpc_cycles(ctx, n)) return rc;
+  if (pos_out) {
+    int rc = fp64 ? monomers_all_t<double>(ctx, nullptr, nullptr, pos_out, vel_out, nullptr, false)
+                  : monomers_all_t<float>(ctx, nullptr, nullptr, pos_out, vel_out, nullptr, false);
+    if (rc) return rc;
+  }
+  if (obs_out) {
+    if (fp64)
+      mol_observables_t<double>(ctx);
+    else
+      mol_observables_t<float>(ctx);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(obs_out, ctx->d_obs,
+                       static_cast<size_t>(ctx->n_rep) * smpc::OBS_PER_REP * sizeof(double),
+                       cudaMemcpyDeviceToHost, ctx->st));
+  }
+  CU(cudaStreamSynchronize(ctx->st));  // the host buffers are borrowed for the call only
   return SMPC_OK;
 }
 

@@ -605,3 +605,40 @@ def test_fp32_side_by_side_md_in_graph_cycles():
     finally:
         a.close()
         b.close()
+
+
+def test_cycles_io_is_the_separate_calls():
+    # smpc_cycles_io = set state, cycles, get state, observables with one
+    # synchronisation: two contexts from the same inputs, one through the
+    # separate calls and one through the fused call (FP64: the MD sums are
+    # in a fixed order, so the runs agree bit for bit up to the atomics of
+    # the cell sort, which only permute particles inside a cell)
+    from starpolymersmd_gb300 import workloads as W
+    specs = _batch_specs()
+    a, b = W.build(specs, precision=capi.FP64), W.build(specs, precision=capi.FP64)
+    try:
+        n = int(sum(a.n_mono))
+        pa, va = np.zeros((n, 3)), np.zeros((n, 3))
+        a.ctx.get_monomer_state_all(pa, va)
+        va *= 0.9  # a state change the upload must carry
+        pb, vb = pa.copy(), va.copy()
+        a.ctx.set_monomer_state_all(pa, va)
+        a.ctx.cycles(2)
+        a.ctx.get_monomer_state_all(pa, va)
+        obs_a = a.ctx.molecule_observables_all()
+        obs_b = np.zeros_like(obs_a)
+        b.ctx.cycles_io(2, pb, vb, pb, vb, obs_b)
+        for x in (a, b):
+            x.ctx.raise_on_device_error()
+        H.close64(pb, pa)
+        H.close64(vb, va)
+        H.close64(obs_b, obs_a)
+        # outputs only, and inputs only
+        p2, v2 = np.zeros((n, 3)), np.zeros((n, 3))
+        b.ctx.cycles_io(0, None, None, p2, v2, None)
+        np.testing.assert_array_equal(p2, pb)
+        with pytest.raises(capi.SmpcError):
+            b.ctx.cycles_io(1, pb, None, None, None, None)
+    finally:
+        a.close()
+        b.close()
