@@ -163,9 +163,9 @@ void launch_unwrap_molecules<Real>(const RepInfo* reps, const RepDyn* dyn, const
   k_copy_monomers<Real><<<std::min((n_mono + 255) / 256, 152 * 8), 256, 0, st>>>(n_mono, mpos, mvel,
                                                                               upos, uvel);
   if (n_mols > 0)
-    k_unwrap_molecules<Real><<<(n_mols + 7) / 8, 256, 0, st>>>(reps, dyn, mols, mol_rep, n_mols,
-                                                               bond_start, bonds, mpos, mvel,
-                                                               upos, uvel);
+    k_unwrap_molecules<Real><<<n_mols, UNWRAP_NT, 0, st>>>(reps, dyn, mols, mol_rep, n_mols,
+                                                           bond_start, bonds, mpos, mvel, upos,
+                                                           uvel);
 }
 
 template <>

@@ -25,6 +25,7 @@
 namespace smpc {
 
 constexpr int OBS_PER_REP = 16;
+constexpr int UNWRAP_NT = 256;  // threads (and beads per chunk) of k_unwrap_molecules
 
 // centre of molecule [b, e): unweighted mean position and velocity
 template <typename R>
@@ -218,10 +219,11 @@ __global__ void k_obs_reduce(const int2* rep_mols, const double* mol_out, int n_
 // already placed, or next to the molecule's first bead when it has none. Its
 // v_x gets the shear velocity of the image it moved to (MPC.cpp:428).
 // k_copy_monomers copies every monomer first; k_unwrap_molecules then runs one
-// warp per molecule of a periodic box over chunks of 32 beads: when every
-// bead of a chunk has its partner either before the chunk (placed) or right
-// before itself (stars and chains numbered outward from the core), the chunk
-// is one segmented prefix sum of the bond vectors; otherwise lane 0 walks it.
+// CTA per molecule of a periodic box over chunks of UNWRAP_NT beads: when
+// every bead of a chunk has its partner either before the chunk (placed) or
+// right before itself (stars and chains numbered outward from the core), the
+// chunk is one segmented prefix sum of the bond vectors (warp scans joined in
+// warp order); otherwise thread 0 walks it.
 template <typename R>
 __global__ void k_copy_monomers(int n, const R* mpos, const R* mvel, R* upos, R* uvel) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -244,27 +246,34 @@ __device__ __forceinline__ void unwrap_bond(const double L[3], const double invL
 }
 
 template <typename R>
-__global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* mols,
-                                   const int* mol_rep, int n_mols, const int* bond_start,
-                                   const int2* bonds, const R* mpos, const R* mvel, R* upos,
-                                   R* uvel) {
+__global__ void __launch_bounds__(UNWRAP_NT)
+    k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const int2* mols,
+                       const int* mol_rep, int n_mols, const int* bond_start, const int2* bonds,
+                       const R* mpos, const R* mvel, R* upos, R* uvel) {
   constexpr unsigned FULL = 0xFFFFFFFFu;
-  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (m >= n_mols) return;  // whole warps
+  constexpr int NW = UNWRAP_NT / 32;
+  __shared__ double s_wsum[3][NW];  // per warp: the scan value of its last lane
+  __shared__ int s_whead[NW];       // per warp: it holds a segment head
+  __shared__ double s_carry[3][NW];  // per warp: what its leading (headless) lanes add
+  __shared__ int s_walk;            // the chunk needs the one-by-one walk
+  __shared__ int s_p[UNWRAP_NT];
+  __shared__ double s_d[3][UNWRAP_NT];
+  const int m = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const RepInfo& ri = reps[mol_rep[m]];
-  if (!(ri.flags & REP_PERIODIC_MD)) return;
+  if (!(ri.flags & REP_PERIODIC_MD)) return;  // whole block
   const double L[3] = {static_cast<double>(ri.L[0]), static_cast<double>(ri.L[1]),
                        static_cast<double>(ri.L[2])};
   const double invL[3] = {1.0 / L[0], 1.0 / L[1], 1.0 / L[2]};
   const double delrx = dyn[mol_rep[m]].delrx;
   const double sLy = ri.shear * L[1];
   const int2 mb = mols[m];
-  for (int c0 = mb.x + 1; c0 < mb.y; c0 += 32) {
-    const int i = c0 + lane;
+  for (int c0 = mb.x + 1; c0 < mb.y; c0 += UNWRAP_NT) {
+    const int i = c0 + tid;
     const bool active = i < mb.y;
     int p = -1;
     double d0 = 0, d1 = 0, d2 = 0, xy = 0, uy = 0;
+    if (tid == 0) s_walk = 0;
     if (active) {
       for (int e = bond_start[i]; e < bond_start[i + 1]; ++e) {
         const int j = bonds[e].x;
@@ -279,26 +288,30 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
       unwrap_bond(L, invL, delrx, d0, d1, d2);
     }
     const bool chained = active && p == i - 1 && p >= c0;
-    if (__any_sync(FULL, active && p >= c0 && !chained)) {
+    __syncthreads();
+    if (active && p >= c0 && !chained) s_walk = 1;
+    __syncthreads();
+    if (s_walk) {
       // a partner inside the chunk that is not the previous bead: one by one
-      for (int k = 0; k < 32; ++k) {
-        const int q = __shfl_sync(FULL, p, k);
-        const double e0 = __shfl_sync(FULL, d0, k), e1 = __shfl_sync(FULL, d1, k),
-                     e2 = __shfl_sync(FULL, d2, k);
-        if (lane == 0 && c0 + k < mb.y) {
-          const R4<R> up = ld4_rw(upos, q);
+      s_p[tid] = p;
+      s_d[0][tid] = d0;
+      s_d[1][tid] = d1;
+      s_d[2][tid] = d2;
+      __syncthreads();
+      if (tid == 0)
+        for (int k = 0; k < UNWRAP_NT && c0 + k < mb.y; ++k) {
+          const R4<R> up = ld4_rw(upos, s_p[k]);
           R4<R> u = ld4_rw(upos, c0 + k);
-          u.x = static_cast<R>(static_cast<double>(up.x) + e0);
-          u.y = static_cast<R>(static_cast<double>(up.y) + e1);
-          u.z = static_cast<R>(static_cast<double>(up.z) + e2);
+          u.x = static_cast<R>(static_cast<double>(up.x) + s_d[0][k]);
+          u.y = static_cast<R>(static_cast<double>(up.y) + s_d[1][k]);
+          u.z = static_cast<R>(static_cast<double>(up.z) + s_d[2][k]);
           st4(upos, c0 + k, u);
         }
-        __syncwarp();
-      }
+      __syncthreads();
       if (active) uy = static_cast<double>(ld4_rw(upos, i).y);
     } else {
-      // segment heads take their placed partner's image; the scan adds the
-      // bond vectors down each segment
+      // segment heads take their placed partner's image; a segmented scan
+      // over the block adds the bond vectors down each segment
       double a0 = d0, a1 = d1, a2 = d2;
       if (active && !chained) {
         const R4<R> up = ld4_rw(upos, p);
@@ -306,7 +319,7 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
         a1 += static_cast<double>(up.y);
         a2 += static_cast<double>(up.z);
       }
-      int head = chained ? -1 : lane;
+      int head = chained ? -1 : lane;  // inactive lanes head themselves
       for (int o = 1; o < 32; o <<= 1) {
         const int h = __shfl_up_sync(FULL, head, o);
         if (lane >= o && h > head) head = h;
@@ -314,11 +327,31 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
       for (int o = 1; o < 32; o <<= 1) {
         const double t0 = __shfl_up_sync(FULL, a0, o), t1 = __shfl_up_sync(FULL, a1, o),
                      t2 = __shfl_up_sync(FULL, a2, o);
-        if (lane - o >= head) {
+        if (lane >= o && lane - o >= head) {  // head < 0: the segment began before the warp
           a0 += t0;
           a1 += t1;
           a2 += t2;
         }
+      }
+      if (lane == 31) {
+        s_wsum[0][w] = a0;
+        s_wsum[1][w] = a1;
+        s_wsum[2][w] = a2;
+        s_whead[w] = head >= 0;
+      }
+      __syncthreads();
+      if (tid == 0) {  // carry into each warp's leading lanes, warps in order
+        double c[3] = {0.0, 0.0, 0.0};
+        for (int q = 0; q < NW; ++q) {
+          for (int k = 0; k < 3; ++k) s_carry[k][q] = c[k];
+          for (int k = 0; k < 3; ++k) c[k] = s_whead[q] ? s_wsum[k][q] : c[k] + s_wsum[k][q];
+        }
+      }
+      __syncthreads();
+      if (head < 0) {  // this lane's segment began in an earlier warp
+        a0 += s_carry[0][w];
+        a1 += s_carry[1][w];
+        a2 += s_carry[2][w];
       }
       if (active) {
         R4<R> u = ld4_rw(upos, i);
@@ -335,7 +368,7 @@ __global__ void k_unwrap_molecules(const RepInfo* reps, const RepDyn* dyn, const
       v.x = static_cast<R>(static_cast<double>(v.x) + ny * sLy);
       st4(uvel, i, v);
     }
-    __syncwarp();
+    __syncthreads();  // this chunk's images are placed before the next chunk reads them
   }
 }
 

@@ -331,3 +331,68 @@ def test_state_set_from_outside_rebuilds_the_lists(precision):
         ctx.raise_on_device_error()
         np.testing.assert_array_equal(p2, p1)
         np.testing.assert_array_equal(v2, v1)
+
+
+@pytest.mark.parametrize("interleave", [False, True])
+def test_unwrap_of_long_and_interleaved_molecules(interleave):
+    # Molecules made whole by the device against numpy: stars of 8 x 40 beads
+    # span several 256-bead chunks (the block scan carries segments across
+    # warps and chunks); with the arms numbered round-robin every partner sits
+    # 8 beads back inside the chunk, which takes the one-by-one walk.
+    from tests.test_gpu_parity import _numpy_observables
+    rng = np.random.default_rng(21)
+    Lb = 40
+    sol = system.star_solution(3, 8, 40, 0.5, 5.0, 1.0, (Lb, Lb, Lb), rng, bond=0.97)
+    pos, vel, mass = sol.pos.copy(), sol.vel.copy(), np.asarray(sol.mass).copy()
+    amphi, anchor = np.asarray(sol.amphi).copy(), np.asarray(sol.anchor).copy()
+    src, dst = np.asarray(sol.bond_src).copy(), np.asarray(sol.bond_dst).copy()
+    ms = list(sol.mol_start)
+    if interleave:
+        perm = np.arange(len(pos))  # new index -> old index
+        for a, b in zip(ms[:-1], ms[1:]):
+            arms, n_arm = 8, 40
+            old = [a] + [a + 1 + arm * n_arm + k for k in range(n_arm) for arm in range(arms)]
+            perm[a:b] = old
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(len(perm))
+        pos, vel, mass, amphi, anchor = pos[perm], vel[perm], mass[perm], amphi[perm], anchor[perm]
+        src, dst = inv[src], inv[dst]
+    desc = dict(L=(Lb, Lb, Lb), n_fluid=0, n_mono=len(pos), mol0_size=ms[1], kT=1.0, shear=0.2,
+                h=0.1, md_dt=0.005, seed=5, potential=capi.POT_LJ126, r_cut=2.5, r_verlet=2.8,
+                flags=capi.REPLICA_PERIODIC_MD)
+    with capi.Context([desc], precision=capi.FP64, rng=capi.RNG_PHILOX, step_update=10,
+                      mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL) as ctx:
+        ctx.set_monomers(0, pos, vel, np.zeros_like(pos), mass, amphi, anchor)
+        ctx.set_bonds(0, src, dst)
+        ctx.set_molecules(0, ms)
+        ctx.init_md()
+        ctx.md_substeps(20)
+        ctx.raise_on_device_error()
+        p, v, _ = ctx.get_monomers(0)
+        up, uv = _numpy_unwrap_L(p, v, src, dst, ms, ctx.delrx(0), 0.2, Lb)
+        want = _numpy_observables(up, uv, mass, ms)
+        got = ctx.molecule_observables_all()[0]
+        np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-9 * np.abs(want).max())
+
+
+def _numpy_unwrap_L(pos, vel, src, dst, mol_start, delrx, shear, Lb):
+    n = len(pos)
+    nb = [[] for _ in range(n)]
+    for s, d in zip(src, dst):
+        nb[s].append(d)
+        nb[d].append(s)
+    up, uv = pos.copy(), vel.copy()
+    for a, b in zip(mol_start[:-1], mol_start[1:]):
+        for i in range(a + 1, b):
+            cands = [j for j in nb[i] if a <= j < i]
+            p = min(cands) if cands else a
+            d = pos[i] - pos[p]
+            cy = np.round(d[1] / Lb)
+            d[0] -= Lb * np.round(d[0] / Lb)
+            d[0] -= cy * delrx
+            d[0] -= Lb * np.round(d[0] / Lb)
+            d[1] -= Lb * cy
+            d[2] -= Lb * np.round(d[2] / Lb)
+            up[i] = up[p] + d
+            uv[i, 0] = vel[i, 0] + np.round((up[i, 1] - pos[i, 1]) / Lb) * shear * Lb
+    return up, uv
