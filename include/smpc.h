@@ -8,7 +8,9 @@
  *
  * A context holds one or many independent replicas (boxes). The reference
  * interfaces each entry point replaces are cited per function; the reference
- * binds them through its C++ classes, see INTEGRATION.md for the adapter.
+ * binds them through its C++ classes; the adapter classes (MPC,
+ * AndersenStochastic, Lowe_Andersen, Thermostat_GPU over this ABI) are in
+ * starpolymersmd_gb300/dropin/.
  */
 #ifndef SMPC_H
 #define SMPC_H

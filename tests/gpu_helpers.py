@@ -6,7 +6,7 @@ from oracle import oracle as orc
 from starpolymersmd_gb300 import capi, system
 from tests import golden_replay as gr
 
-# Tolerances stated by the tests (see DESIGN.md "Parity"):
+# Tolerances stated by the tests:
 FP64_RTOL = 1e-12          # FP64 path vs reference / oracle, relative to the array's scale
 FP32_POS_ATOL = 2e-5       # FP32 path: absolute position error per unit of box edge
 FP32_VEL_RTOL = 2e-5       # FP32 path: velocity error relative to the velocity scale
