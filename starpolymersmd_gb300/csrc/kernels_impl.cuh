@@ -225,15 +225,36 @@ void launch_pmd_call<Real>(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, R
     return;
   }
   k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, 1, adv_scale, 1);
+  // the kernels after the drift follow their predecessor programmatically
+  // (pmd_wait_previous): their launch overlaps its last blocks
+  cudaLaunchAttribute pdl[1];
+  pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  pdl[0].val.programmaticStreamSerializationAllowed = 1;
+  auto cfg = [&](int blocks) {
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3(blocks);
+    c.blockDim = dim3(PMD_NT);
+    c.dynamicSmemBytes = 0;
+    c.stream = st;
+    c.attrs = pdl;
+    c.numAttrs = 1;
+    return c;
+  };
   for (int k = 1; k <= n; ++k) {
     Real* pin = (k & 1) ? mpos : mnext;  // substep k's positions: buffer (k - 1) & 1
     Real* pout = (k & 1) ? mnext : mpos;
-    k_pmd_nlist<Real><<<nb_list, PMD_NT, 0, st>>>(a, reps, pin, mdisp, k, adv_scale);
-    k_pmd_forces<Real><<<nb_force, PMD_NT, 0, st>>>(a, reps, dyn, pin, pout, mvel, mfrc, mdisp,
-                                                    k, adv_scale, 1, k < n,
-                                                    calc_epot && k == n);
+    const cudaLaunchConfig_t cl = cfg(nb_list);
+    cudaLaunchKernelEx(&cl, k_pmd_nlist<Real>, a, reps, static_cast<const Real*>(pin), mdisp, k,
+                       adv_scale);
+    const cudaLaunchConfig_t cf = cfg(nb_force);
+    cudaLaunchKernelEx(&cf, k_pmd_forces<Real>, a, reps, dyn, static_cast<const Real*>(pin), pout,
+                       mvel, mfrc, mdisp, k, adv_scale, 1, static_cast<int>(k < n),
+                       static_cast<int>(calc_epot && k == n));
   }
-  if ((n & 1) == 0) k_pmd_copy<Real><<<nb, PMD_NT, 0, st>>>(a, mnext, mpos);
+  if ((n & 1) == 0) {
+    const cudaLaunchConfig_t cc = cfg(nb);
+    cudaLaunchKernelEx(&cc, k_pmd_copy<Real>, a, static_cast<const Real*>(mnext), mpos);
+  }
 }
 
 template <>

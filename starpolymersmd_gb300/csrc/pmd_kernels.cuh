@@ -258,6 +258,15 @@ __device__ __forceinline__ void pmd_bin(const PmdArgs& a, int s, const PmdBox<R>
     raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(a.base + i), k);
 }
 
+// Programmatic dependent launch: the substep kernels after the first are
+// launched with cudaLaunchAttributeProgrammaticStreamSerialization, so their
+// blocks are scheduled while the previous kernel drains; each waits here,
+// before its first read, until that kernel has completed and its writes are
+// visible (griddepcontrol.wait; it returns at once for an ordinary launch).
+__device__ __forceinline__ void pmd_wait_previous() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Substep 1 of a call (adv_k = 1, drift = 1) or the set-up (adv_k = 0,
 // drift = 0: wrap what the caller placed outside, request the first build).
 template <typename R>
@@ -388,6 +397,7 @@ template <typename R>
 __global__ void __launch_bounds__(PMD_NT)
     k_pmd_nlist(PmdArgs a, const RepInfo* reps, const R* pos, R* mdisp, int adv_k,
                 double adv_scale) {
+  pmd_wait_previous();
   const int s = adv_k & 1;
   const RepInfo& ri = reps[a.rep];
   if (a.flag[s] == 0) return;
@@ -409,6 +419,7 @@ __global__ void __launch_bounds__(PMD_NT)
     k_pmd_forces(PmdArgs a, const RepInfo* reps, RepDyn* dyn, const R* pin, R* pout, R* mvel,
                  R* mfrc, R* mdisp, int adv_k, double adv_scale, int kick, int drift_next,
                  int calc_epot) {
+  pmd_wait_previous();
   constexpr int LANES = pmd_force_lanes<R>();
   const RepInfo& ri = reps[a.rep];
   const int s = adv_k & 1;
@@ -541,6 +552,7 @@ __global__ void __launch_bounds__(PMD_NT)
 
 template <typename R>
 __global__ void __launch_bounds__(PMD_NT) k_pmd_copy(PmdArgs a, const R* src, R* dst) {
+  pmd_wait_previous();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const size_t g = static_cast<size_t>(a.base) + i;
