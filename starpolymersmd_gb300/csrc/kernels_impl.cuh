@@ -269,12 +269,16 @@ void launch_velocity_profile<Real>(const RepInfo* reps, const int2* rep_mols, co
       reps, rep, rec, delrx, width, kx0, nx, ky0, ny, c6, bins);
 }
 
+// Monomer state between the device's R4 records and x,y,z-interleaved double
+// arrays: a device staging buffer, or the caller's pinned host arrays read and
+// written in place over the C2C link (the host pointer is the device pointer).
 template <typename R>
-__global__ void k_unpack_monomers(const double* __restrict__ stage, int n, R* mpos, R* mvel) {
+__global__ void k_unpack_monomers(const double* __restrict__ pos, const double* __restrict__ vel,
+                                  int n, R* mpos, R* mvel) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double* p = stage + 3 * static_cast<size_t>(i);
-  const double* v = stage + 3 * (static_cast<size_t>(n) + i);
+  const double* p = pos + 3 * static_cast<size_t>(i);
+  const double* v = vel + 3 * static_cast<size_t>(i);
   R4<R> x = ld4_rw(mpos, i), u = ld4_rw(mvel, i);
   x.x = static_cast<R>(p[0]);
   x.y = static_cast<R>(p[1]);
@@ -288,21 +292,22 @@ __global__ void k_unpack_monomers(const double* __restrict__ stage, int n, R* mp
 
 template <typename R>
 __global__ void k_pack_monomers(const R* mpos, const R* mvel, const R* mfrc, int n,
-                                double* __restrict__ stage) {
+                                double* __restrict__ pos, double* __restrict__ vel,
+                                double* __restrict__ frc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const R4<R> x = ld4_rw(mpos, i), u = ld4_rw(mvel, i);
-  double* p = stage + 3 * static_cast<size_t>(i);
-  double* v = stage + 3 * (static_cast<size_t>(n) + i);
+  double* p = pos + 3 * static_cast<size_t>(i);
+  double* v = vel + 3 * static_cast<size_t>(i);
   p[0] = static_cast<double>(x.x);
   p[1] = static_cast<double>(x.y);
   p[2] = static_cast<double>(x.z);
   v[0] = static_cast<double>(u.x);
   v[1] = static_cast<double>(u.y);
   v[2] = static_cast<double>(u.z);
-  if (mfrc) {
+  if (mfrc && frc) {
     const R4<R> fr = ld4_rw(mfrc, i);
-    double* q = stage + 3 * (2 * static_cast<size_t>(n) + i);
+    double* q = frc + 3 * static_cast<size_t>(i);
     q[0] = static_cast<double>(fr.x);
     q[1] = static_cast<double>(fr.y);
     q[2] = static_cast<double>(fr.z);
@@ -310,15 +315,16 @@ __global__ void k_pack_monomers(const R* mpos, const R* mvel, const R* mfrc, int
 }
 
 template <>
-void launch_unpack_monomers<Real>(const double* stage, int n, Real* mpos, Real* mvel,
-                                  cudaStream_t st) {
-  if (n > 0) k_unpack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(stage, n, mpos, mvel);
+void launch_unpack_monomers<Real>(const double* pos, const double* vel, int n, Real* mpos,
+                                  Real* mvel, cudaStream_t st) {
+  if (n > 0) k_unpack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(pos, vel, n, mpos, mvel);
 }
 
 template <>
 void launch_pack_monomers<Real>(const Real* mpos, const Real* mvel, const Real* mfrc, int n,
-                                double* stage, cudaStream_t st) {
-  if (n > 0) k_pack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(mpos, mvel, mfrc, n, stage);
+                                double* pos, double* vel, double* frc, cudaStream_t st) {
+  if (n > 0)
+    k_pack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(mpos, mvel, mfrc, n, pos, vel, frc);
 }
 
 template <>

@@ -142,12 +142,14 @@ void launch_mono_stress(const RepInfo* reps, const RepDyn* dyn, int n_rep, const
                         double* out, cudaStream_t st);
 
 // Monomer state between the C ABI's x,y,z-interleaved doubles and the device
-// records (pos.w / vel.w keep mass and type): stage = pos[3M] | vel[3M] | force[3M]
+// records (pos.w / vel.w keep mass and type): pos, vel, frc each 3M doubles, in
+// the device staging buffer or in pinned host memory the device maps
 template <typename R>
-void launch_unpack_monomers(const double* stage, int n, R* mpos, R* mvel, cudaStream_t st);
+void launch_unpack_monomers(const double* pos, const double* vel, int n, R* mpos, R* mvel,
+                            cudaStream_t st);
 template <typename R>
-void launch_pack_monomers(const R* mpos, const R* mvel, const R* mfrc, int n, double* stage,
-                          cudaStream_t st);
+void launch_pack_monomers(const R* mpos, const R* mvel, const R* mfrc, int n, double* pos,
+                          double* vel, double* frc, cudaStream_t st);
 
 void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* grand, int n_cells,
                  cudaStream_t st);

@@ -153,8 +153,17 @@ __global__ void __launch_bounds__(NT) k_mol_observables(const int2* mols, const 
   for (int k = 0; k < OBS_PER_REP; ++k) o[k] = 0.0;
   if (n <= 0) return;
   const double dn = static_cast<double>(n);
-  const double g[9] = {tot[0] / dn, tot[1] / dn, tot[2] / dn, tot[1] / dn, tot[3] / dn,
-                       tot[4] / dn, tot[2] / dn, tot[4] / dn, tot[5] / dn};
+  double g[9];
+  if (std::is_same<R, double>::value) {  // the reference's divisions (Box.cpp:330-379)
+    const double gg[9] = {tot[0] / dn, tot[1] / dn, tot[2] / dn, tot[1] / dn, tot[3] / dn,
+                          tot[4] / dn, tot[2] / dn, tot[4] / dn, tot[5] / dn};
+    for (int k = 0; k < 9; ++k) g[k] = gg[k];
+  } else {  // FP32 path: one division
+    const double inv = 1.0 / dn;
+    const double gg[9] = {tot[0] * inv, tot[1] * inv, tot[2] * inv, tot[1] * inv, tot[3] * inv,
+                          tot[4] * inv, tot[2] * inv, tot[4] * inv, tot[5] * inv};
+    for (int k = 0; k < 9; ++k) g[k] = gg[k];
+  }
   for (int k = 0; k < 9; ++k) o[1 + k] = g[k];
   o[0] = sqrt(g[0] + g[4] + g[8]);
   const double tr = tot[0] + tot[3] + tot[5];
@@ -203,11 +212,12 @@ __global__ void k_obs_reduce(const int2* rep_mols, const double* mol_out, int n_
     n_total += __shfl_xor_sync(FULL, n_total, off);
   }
   if (lane != 0) return;
-  const double nm = rm.y > 0 ? static_cast<double>(rm.y) : 1.0;
+  // one division (FP64 divisions are slow on this part); exact for one molecule
+  const double inv = 1.0 / (rm.y > 0 ? static_cast<double>(rm.y) : 1.0);
   double* o = out + static_cast<size_t>(OBS_PER_REP) * r;
-  o[0] = acc[0] / nm;
-  for (int k = 0; k < 9; ++k) o[1 + k] = acc[1 + k] / nm;
-  for (int k = 0; k < 3; ++k) o[10 + k] = acc[10 + k] / nm;
+  o[0] = acc[0] * inv;
+  for (int k = 0; k < 9; ++k) o[1 + k] = acc[1 + k] * inv;
+  for (int k = 0; k < 3; ++k) o[10 + k] = acc[10 + k] * inv;
   o[13] = acc[13];
   o[14] = n_total > 1 ? acc[13] * 2. / (3. * static_cast<double>(n_total - 1)) : 0.0;
   o[15] = static_cast<double>(rm.y);
