@@ -13,11 +13,11 @@ namespace smpc {
 // Variant tables (index 0 is the default shape). The names read
 // threads x cells-per-tile / staging capacity / gathers in flight.
 int bin_variant_count() { return 4; }
-int collide_variant_count() { return 7; }
+int collide_variant_count() { return 9; }
 int md_variant_count() { return 4; }
 int collide_variant_cells(int v) {
   switch (v) {
-    case 2: case 3: case 5: return 64;
+    case 2: case 3: case 5: case 7: case 8: return 64;
     case 4: return 256;
     default: return 128;
   }
@@ -29,8 +29,9 @@ const char* bin_variant_name(int v) {
 const char* collide_variant_name(int v) {
   static const char* n[] = {"256t 128c cap1408 g4", "256t 128c cap1408 g8", "128t 64c cap704 g4",
                             "128t 64c cap704 g8", "512t 256c cap2816 g4",
-                            "128t 64c cap704 cp.async", "256t 128c cap1408 cp.async"};
-  return v >= 0 && v < 7 ? n[v] : "?";
+                            "128t 64c cap704 cp.async", "256t 128c cap1408 cp.async",
+                            "128t 64c cap736 cp.async", "128t 64c cap768 cp.async"};
+  return v >= 0 && v < 9 ? n[v] : "?";
 }
 const char* md_variant_name(int v) {
   static const char* n[] = {"1024t 1/thread", "512t 2/thread", "1024t lanes/bead, largest first",

@@ -118,6 +118,8 @@ void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
       case 4: collide_f32<512, 256, 2816, 4>(a, st); return;
       case 5: collide_f32_async<128, 64, 704>(a, st); return;
       case 6: collide_f32_async<256, 128, 1408>(a, st); return;
+      case 7: collide_f32_async<128, 64, 736>(a, st); return;
+      case 8: collide_f32_async<128, 64, 768>(a, st); return;
       default: collide_f32<256, 128, 1408, 4>(a, st); return;
     }
   }
