@@ -212,9 +212,13 @@ def test_fp64_lowe_andersen_matches_oracle():
         assert np.abs(mv - before).max() > 0.1  # the thermostat did act
 
 
-def test_fp32_lowe_andersen_conserves_momentum_and_holds_kT():
+@pytest.mark.parametrize("md_variant", [0, 2])
+def test_fp32_lowe_andersen_conserves_momentum_and_holds_kT(md_variant):
+    # md_variant 2 gives each bead several lanes (the candidates are still
+    # taken by the bead's lead lane)
     star, o, ctx = _lowe_pair(capi.FP32, seed=9, n_arm=12, arms=8)
     with ctx:
+        ctx.set_variants(0, 0, md_variant)
         m = star.mass
         p0 = m * ctx.get_monomers(0)[1].sum(axis=0)
         temps = []
