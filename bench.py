@@ -158,7 +158,7 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
     from starpolymersmd_gb300 import system, workloads as W
 
     if workload in W.SOLUTIONS:
-        pick = [W.semidilute_spec() if workload == "semidilute_100" else W.large_box_spec()]
+        pick = [W.SOLUTION_SPECS[workload]()]
     elif workload == "batched_256":
         specs = system.batched_replica_table(256)
         pick = specs[:: max(1, len(specs) // n_threads)][:n_threads]
@@ -218,7 +218,7 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
 def cpu_cycles_for(workload, n_threads):
     # about 10-30 s of CPU work in total
     return {"batched_256": 20, "single_star_50": 5, "single_star_20": 40, "semidilute_100": 3,
-            "large_box_200": 1}.get(workload, 5)
+            "large_box_200": 1, "single_star_50_periodic": 5}.get(workload, 5)
 
 
 # --------------------------------------------------------------- our arm

@@ -156,7 +156,21 @@ def large_box_200(precision=capi.FP32, shear=0.05, **kw) -> Built:
     return build_solution(large_box_spec(shear), precision=precision, **kw)
 
 
-SOLUTIONS = ("semidilute_100", "large_box_200")
+def single_star_periodic_spec(shear=0.05) -> system.ReplicaSpec:
+    return system.ReplicaSpec(L=50, arms=10, n_arm=40, solvophobic_fraction=0.5, shear=shear,
+                              seed=1, n_stars=1)
+
+
+def single_star_50_periodic(precision=capi.FP32, shear=0.05, **kw) -> Built:
+    """The single-star system of single_star_50 through the periodic MD path:
+    the star's MD spread over many CTAs (Lees-Edwards images, no recentring)
+    instead of one CTA per replica."""
+    return build_solution(single_star_periodic_spec(shear), precision=precision, **kw)
+
+
+SOLUTIONS = ("semidilute_100", "large_box_200", "single_star_50_periodic")
+SOLUTION_SPECS = {"semidilute_100": semidilute_spec, "large_box_200": large_box_spec,
+                  "single_star_50_periodic": single_star_periodic_spec}
 
 
 def single_star_50(precision=capi.FP32, shear=0.05, **kw) -> Built:
@@ -178,4 +192,4 @@ def batched_256(precision=capi.FP32, n=256, **kw) -> Built:
 
 WORKLOADS = {"batched_256": batched_256, "single_star_50": single_star_50,
              "single_star_20": single_star_20, "semidilute_100": semidilute_100,
-             "large_box_200": large_box_200}
+             "large_box_200": large_box_200, "single_star_50_periodic": single_star_50_periodic}
