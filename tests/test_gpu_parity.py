@@ -642,3 +642,34 @@ def test_cycles_io_is_the_separate_calls():
     finally:
         a.close()
         b.close()
+
+
+def test_cycles_io_pinned_input_is_read_in_place():
+    # pinned host arrays are read by the unpack kernel over the C2C link; the
+    # result must equal the staged upload of the same (pageable) arrays
+    torch = pytest.importorskip("torch")
+    from starpolymersmd_gb300 import workloads as W
+    specs = _batch_specs()
+    a, b = W.build(specs, precision=capi.FP64), W.build(specs, precision=capi.FP64)
+    try:
+        n = int(sum(a.n_mono))
+        p, v = np.zeros((n, 3)), np.zeros((n, 3))
+        a.ctx.get_monomer_state_all(p, v)
+        v *= 1.1
+        pp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        vp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        pp[:], vp[:] = p, v
+        a.ctx.cycles_io(0, p, v, None, None, None)       # pageable: staged copy
+        b.ctx.cycles_io(0, pp, vp, None, None, None)     # pinned: read in place
+        for x in (a, b):
+            x.ctx.raise_on_device_error()
+        qa, wa = np.zeros((n, 3)), np.zeros((n, 3))
+        qb, wb = np.zeros((n, 3)), np.zeros((n, 3))
+        a.ctx.get_monomer_state_all(qa, wa)
+        b.ctx.get_monomer_state_all(qb, wb)
+        np.testing.assert_array_equal(qa, qb)
+        np.testing.assert_array_equal(wa, wb)
+        np.testing.assert_array_equal(wa, v)  # FP64 state: the upload is exact
+    finally:
+        a.close()
+        b.close()
