@@ -162,7 +162,9 @@ def cpu_sample(workload, n_threads, cycles, max_replicas=None):
     elif workload == "batched_256":
         specs = system.batched_replica_table(256)
         pick = specs[:: max(1, len(specs) // n_threads)][:n_threads]
-    elif workload == "single_star_50":
+    elif workload in ("single_star_50", "single_star_50_periodic"):
+        # the reference's one-star model (the periodic variant's MD is the
+        # same physics while the star has no self-image, see star_extent)
         pick = [system.ReplicaSpec(L=50, arms=10, n_arm=40, solvophobic_fraction=0.5,
                                    shear=0.05, seed=1)]
     else:
@@ -290,7 +292,7 @@ def run_ours(args, world, rank, local, dist):
              "alg_bytes_per_cycle": cycle_alg_bytes}
 
     launches_per_cycle = (PHASE_LAUNCHES - 1 + PMD_LAUNCHES * W.N_SUB + 2
-                          if args.workload in W.SOLUTIONS else PHASE_LAUNCHES)
+                          if args.workload in W.PERIODIC else PHASE_LAUNCHES)
     big = sum(1 for n in built.n_mono if n > 512)
     if ctx.get_variants()[2] == 3 and 0 < big < built.n_rep:
         launches_per_cycle += 1  # the side-by-side MD shape runs two MD kernels
@@ -313,6 +315,14 @@ def run_ours(args, world, rank, local, dist):
            "build_s": round(build_s, 1)}
     if clocks:
         out["clocks"] = clocks
+    if args.workload == "single_star_50_periodic":
+        # no bead may meet another bead's periodic image: the star's extent
+        # along every axis stays below L - r_cut (then this is single_star_50's
+        # physics through the periodic MD kernels)
+        ext = W.star_extent(built)
+        L = float(built.specs[0].L)
+        out["config"]["star_extent_after_run"] = [round(float(e), 2) for e in ext]
+        out["config"]["self_image_free"] = bool(float(ext.max()) < L - W.R_CUT_LJ)
 
     if not args.no_extras:
         out["fp64_plain"] = fp64_plain_ratio(args.workload, built, rep_steps)
@@ -337,8 +347,12 @@ def fp64_plain_ratio(workload, built, batched_rep_steps):
     cyc = 3
     t_sum = 0.0
     for s in sample:
-        b = (W.build_solution(s, precision=capi.FP64) if workload in W.SOLUTIONS
-             else W.build([s], precision=capi.FP64))
+        if workload in W.SOLUTIONS:
+            b = W.build_solution(s, precision=capi.FP64)
+        elif workload in W.PERIODIC:
+            b = W.build([s], precision=capi.FP64, flags=capi.REPLICA_PERIODIC_MD)
+        else:
+            b = W.build([s], precision=capi.FP64)
         b.ctx.cycles(2)
         t_sum += b.ctx.time_cycles(cyc) / 1e3
         b.ctx.raise_on_device_error()

@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 ORACLE_SO = os.path.join(BUILD_DIR, "libsmpc_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsmpc_ref.so")
-REF_SRC_DEFAULT = "/root/reference"
+# a reference checkout beside the repository, unless SMPC_REFERENCE names one
+REF_SRC_SIBLING = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 RNG_INJECT, RNG_PHILOX = 0, 1
 POT_REF4824, POT_LJ126 = 0, 1
@@ -39,7 +40,7 @@ def build_oracle(force: bool = False) -> str:
 
 def build_reference(ref_root: str | None = None) -> str | None:
     """Compiles the reference's own sources into _ref/ when they are present."""
-    ref_root = ref_root or os.environ.get("SMPC_REFERENCE", REF_SRC_DEFAULT)
+    ref_root = ref_root or os.environ.get("SMPC_REFERENCE") or REF_SRC_SIBLING
     if not os.path.isdir(os.path.join(ref_root, "star-polymers", "lib")):
         return None
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "refbuild"), "REF=" + ref_root])

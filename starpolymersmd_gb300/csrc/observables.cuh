@@ -212,12 +212,21 @@ __global__ void k_obs_reduce(const int2* rep_mols, const double* mol_out, int n_
     n_total += __shfl_xor_sync(FULL, n_total, off);
   }
   if (lane != 0) return;
-  // one division (FP64 divisions are slow on this part); exact for one molecule
-  const double inv = 1.0 / (rm.y > 0 ? static_cast<double>(rm.y) : 1.0);
+  const double nm = rm.y > 0 ? static_cast<double>(rm.y) : 1.0;
   double* o = out + static_cast<size_t>(OBS_PER_REP) * r;
-  o[0] = acc[0] * inv;
-  for (int k = 0; k < 9; ++k) o[1 + k] = acc[1 + k] * inv;
-  for (int k = 0; k < 3; ++k) o[10 + k] = acc[10 + k] * inv;
+  if (std::is_same<R, double>::value) {
+    // the reference's divisions by Molecules.size() (Box.cpp:350-351, 378)
+    o[0] = acc[0] / nm;
+    for (int k = 0; k < 9; ++k) o[1 + k] = acc[1 + k] / nm;
+    for (int k = 0; k < 3; ++k) o[10 + k] = acc[10 + k] / nm;
+  } else {
+    // FP32 path: one division (FP64 divisions are slow on this part); exact
+    // for one molecule
+    const double inv = 1.0 / nm;
+    o[0] = acc[0] * inv;
+    for (int k = 0; k < 9; ++k) o[1 + k] = acc[1 + k] * inv;
+    for (int k = 0; k < 3; ++k) o[10 + k] = acc[10 + k] * inv;
+  }
   o[13] = acc[13];
   o[14] = n_total > 1 ? acc[13] * 2. / (3. * static_cast<double>(n_total - 1)) : 0.0;
   o[15] = static_cast<double>(rm.y);

@@ -489,13 +489,23 @@ int get_monomers_t(smpc_ctx* ctx, int rep, double* pos, double* vel, double* for
 // pageable memory: the unpack kernel then reads the caller's arrays over the
 // C2C link instead of staging them through a copy (65 -> 15 us per upload of
 // 70 k monomers).
-static void* mapped_host(const void* p) {
+// The mapping is used only when this context's device can reach it: the
+// allocation was made with that device current, or it is portable (mapped
+// into every device's address space). Otherwise the staged copy is taken.
+static void* mapped_host(const void* p, int device) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();  // clear the query's error state
     return nullptr;
   }
-  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+  if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+  if (at.device == device) return at.devicePointer;
+  unsigned flags = 0;
+  if (cudaHostGetFlags(&flags, const_cast<void*>(p)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (flags & cudaHostAllocPortable) ? at.devicePointer : nullptr;
 }
 
 // All replicas' monomers in one transfer each way (replicas concatenated),
@@ -510,8 +520,8 @@ int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, do
   if (n == 0) return SMPC_OK;
   const int ni = static_cast<int>(n);
   if (pos_in) {
-    const double* dp = static_cast<const double*>(mapped_host(pos_in));
-    const double* dv = static_cast<const double*>(mapped_host(vel_in));
+    const double* dp = static_cast<const double*>(mapped_host(pos_in, ctx->device));
+    const double* dv = static_cast<const double*>(mapped_host(vel_in, ctx->device));
     if (!dp || !dv) {  // pageable arrays: through the staging buffer
       CU(cudaMemcpyAsync(ctx->d_dstage, pos_in, 3 * n * sizeof(double), cudaMemcpyHostToDevice,
                          ctx->st));
@@ -535,20 +545,16 @@ int monomers_all_t(smpc_ctx* ctx, const double* pos_in, const double* vel_in, do
   // outputs go through the staging buffer and the copy engine even when they
   // are pinned: the pack kernel's 8-byte stores straight into host memory made
   // the download slower (83 against 48 us for 70 k monomers), unlike the reads
-  double* mp = nullptr;
-  double* mv = nullptr;
-  double* mf = nullptr;
   smpc::launch_pack_monomers<R>(static_cast<const R*>(ctx->d_mpos), static_cast<const R*>(ctx->d_mvel),
                                 force_out ? static_cast<const R*>(ctx->d_mfrc) : nullptr, ni,
-                                mp ? mp : ctx->d_dstage, mv ? mv : ctx->d_dstage + 3 * n,
-                                mf ? mf : ctx->d_dstage + 6 * n, ctx->st);
+                                ctx->d_dstage, ctx->d_dstage + 3 * n, ctx->d_dstage + 6 * n, ctx->st);
   CU(cudaGetLastError());
-  if (pos_out && !mp)
+  if (pos_out)
     CU(cudaMemcpyAsync(pos_out, ctx->d_dstage, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-  if (vel_out && !mv)
+  if (vel_out)
     CU(cudaMemcpyAsync(vel_out, ctx->d_dstage + 3 * n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
                        ctx->st));
-  if (force_out && !mf)
+  if (force_out)
     CU(cudaMemcpyAsync(force_out, ctx->d_dstage + 6 * n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost,
                        ctx->st));
   if (sync) CU(cudaStreamSynchronize(ctx->st));
@@ -786,18 +792,25 @@ cudaError_t noalloc_scratch(int device, void** out) {
 
 // One thread per replica: its tiles' partial sums in tile order, then
 // T = 2 E / (3 (N_solvent - filled cells)) (MPC.cpp:405-409), the same FP64
-// operations in the same order as the host sum of smpc_temperature_all.
+// operations in the same order as the host sum of smpc_temperature_all. The
+// tiles are sorted by replica with each replica's tiles contiguous, so the
+// first one is found by binary search and only that range is summed.
 __global__ void k_temperature_finish(const Tile* tiles, int n_tiles, const RepInfo* reps,
                                      int n_rep, const TempPartial* part, double* out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rep) return;
+  int lo = 0, hi = n_tiles;  // first tile with rep >= r
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (tiles[mid].rep < r) lo = mid + 1;
+    else hi = mid;
+  }
   double e = 0.0;
   unsigned filled = 0;
-  for (int t = 0; t < n_tiles; ++t)
-    if (tiles[t].rep == r) {
-      e += part[t].ekin;
-      filled += part[t].filled;
-    }
+  for (int t = lo; t < n_tiles && tiles[t].rep == r; ++t) {
+    e += part[t].ekin;
+    filled += part[t].filled;
+  }
   const unsigned nf = static_cast<unsigned>(reps[r].n_fluid);
   out[r] = 2. * e / (3. * static_cast<unsigned>(nf - filled));
 }
@@ -1828,12 +1841,10 @@ int smpc_molecule_observables_all(smpc_ctx* ctx, double* out) {
   return SMPC_OK;
 }
 
-int smpc_cycles_io(smpc_ctx* ctx, int n, const double* pos_in, const double* vel_in,
-                   double* pos_out, double* vel_out, double* obs_out) {
-  if (!ctx || n < 0) return SMPC_E_ARG;
-  if ((pos_in == nullptr) != (vel_in == nullptr) || (pos_out == nullptr) != (vel_out == nullptr))
-    return fail(ctx, SMPC_E_ARG, "positions and velocities go together");
-  cudaSetDevice(ctx->device);
+// The queued part of smpc_cycles_io; returns at the first failure with the
+// work queued so far still in flight.
+static int cycles_io_queue(smpc_ctx* ctx, int n, const double* pos_in, const double* vel_in,
+                           double* pos_out, double* vel_out, double* obs_out) {
   const bool fp64 = ctx->opt.precision == SMPC_FP64;
   if (pos_in) {
     int rc = fp64 ? monomers_all_t<double>(ctx, pos_in, vel_in, nullptr, nullptr, nullptr, false)
@@ -1856,7 +1867,23 @@ int smpc_cycles_io(smpc_ctx* ctx, int n, const double* pos_in, const double* vel
                        static_cast<size_t>(ctx->n_rep) * smpc::OBS_PER_REP * sizeof(double),
                        cudaMemcpyDeviceToHost, ctx->st));
   }
-  CU(cudaStreamSynchronize(ctx->st));  // the host buffers are borrowed for the call only
+  return SMPC_OK;
+}
+
+int smpc_cycles_io(smpc_ctx* ctx, int n, const double* pos_in, const double* vel_in,
+                   double* pos_out, double* vel_out, double* obs_out) {
+  if (!ctx || n < 0) return SMPC_E_ARG;
+  if ((pos_in == nullptr) != (vel_in == nullptr) || (pos_out == nullptr) != (vel_out == nullptr))
+    return fail(ctx, SMPC_E_ARG, "positions and velocities go together");
+  cudaSetDevice(ctx->device);
+  const int rc = cycles_io_queue(ctx, n, pos_in, vel_in, pos_out, vel_out, obs_out);
+  // Every exit, the failing ones included, waits for what was queued: the
+  // pinned input arrays are read in place and the outputs written by queued
+  // copies, and the host buffers are borrowed for the call only.
+  const cudaError_t e = cudaStreamSynchronize(ctx->st);
+  if (rc) return rc;  // the first failure is the one reported
+  if (e != cudaSuccess)
+    return fail(ctx, SMPC_E_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
   return SMPC_OK;
 }
 

@@ -86,9 +86,9 @@ def replica_desc(spec: system.ReplicaSpec, star: system.Star) -> dict:
 
 
 def build(specs: Sequence[system.ReplicaSpec], precision=capi.FP32, rng_mode=capi.RNG_PHILOX,
-          mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL) -> Built:
+          mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL, flags=0) -> Built:
     stars = [compact_star(spec) for spec in specs]
-    descs = [replica_desc(s, st) for s, st in zip(specs, stars)]
+    descs = [dict(replica_desc(s, st), flags=flags) for s, st in zip(specs, stars)]
     ctx = capi.Context(descs, precision=precision, rng=rng_mode, mono_bin=mono_bin,
                        delrx_mode=delrx_mode, step_update=N_SUB, max_neighbors=MAX_NB,
                        strict_cells=0)
@@ -162,15 +162,44 @@ def single_star_periodic_spec(shear=0.05) -> system.ReplicaSpec:
 
 
 def single_star_50_periodic(precision=capi.FP32, shear=0.05, **kw) -> Built:
-    """The single-star system of single_star_50 through the periodic MD path:
-    the star's MD spread over many CTAs (Lees-Edwards images, no recentring)
-    instead of one CTA per replica."""
-    return build_solution(single_star_periodic_spec(shear), precision=precision, **kw)
+    """single_star_50 (the same star, solvent and initial velocities, built by
+    ``build``) with its MD through the periodic path: the star's beads spread
+    over many CTAs, kept in the primary box and interacting through the
+    Lees-Edwards minimum image, with no recentring. That is the reference's
+    one-star model (no periodic images, Box.cpp:105-180) as long as no two
+    beads of the star are further apart than L - r_cut along an axis, so that
+    no bead meets another one's image; ``star_extent`` measures it."""
+    spec = system.ReplicaSpec(L=50, arms=10, n_arm=40, solvophobic_fraction=0.5, shear=shear,
+                              seed=1)
+    return build([spec], precision=precision, flags=capi.REPLICA_PERIODIC_MD, **kw)
 
 
-SOLUTIONS = ("semidilute_100", "large_box_200", "single_star_50_periodic")
-SOLUTION_SPECS = {"semidilute_100": semidilute_spec, "large_box_200": large_box_spec,
-                  "single_star_50_periodic": single_star_periodic_spec}
+def star_extent(built: Built, rep: int = 0) -> np.ndarray:
+    """Largest separation along x, y and z between two beads of the replica's
+    first molecule after making it whole: every bond (outward from the core,
+    bonds in topology order) is placed at its Lees-Edwards minimum image
+    (MPC.cpp:456-465) with the current delrx."""
+    spec, star = built.specs[rep], built.stars[rep]
+    L = float(spec.L)
+    pos, _, _ = built.ctx.get_monomers(rep)
+    pos = np.array(pos[:star.n], dtype=np.float64)
+    delrx = built.ctx.delrx(rep)
+    whole = pos.copy()
+    for a, b in zip(star.bond_src, star.bond_dst):
+        d = pos[b] - whole[a]
+        cy = np.round(d[1] / L)
+        d[1] -= cy * L
+        d[0] -= cy * delrx
+        d[0] -= L * np.round(d[0] / L)
+        d[2] -= L * np.round(d[2] / L)
+        whole[b] = whole[a] + d
+    return whole.max(axis=0) - whole.min(axis=0)
+
+
+SOLUTIONS = ("semidilute_100", "large_box_200")
+SOLUTION_SPECS = {"semidilute_100": semidilute_spec, "large_box_200": large_box_spec}
+# workloads whose MD runs through the periodic path
+PERIODIC = SOLUTIONS + ("single_star_50_periodic",)
 
 
 def single_star_50(precision=capi.FP32, shear=0.05, **kw) -> Built:
