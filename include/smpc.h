@@ -41,7 +41,9 @@ enum {
   SMPC_ERR_NONFINITE = 8,     /* non-finite velocity after a collision */
   SMPC_ERR_GAMMA_ITERS = 32,  /* gamma sampler iteration limit */
   SMPC_ERR_FENE = 64,         /* FENE bond at or beyond R0 (Potentials.h:29,50) */
-  SMPC_ERR_KEY_MISMATCH = 128 /* internal consistency check of the collide kernel */
+  SMPC_ERR_KEY_MISMATCH = 128, /* internal consistency check of the collide kernel */
+  SMPC_ERR_FIXPOINT = 256      /* FP32 path: a particle's m v (or m |v|^2 / 256) reached the
+                                  range of the exact fixed-point cell sums, |.| < 4095 */
 };
 
 enum { SMPC_FP64 = 0, SMPC_FP32 = 1 };
@@ -201,8 +203,9 @@ int smpc_time_cycles(smpc_ctx* ctx, int n, double* total_ms);
 /* Solvent initial state generated on the device (MPC::initialize,
  * MPC.cpp:34-55): positions uniform in the box; velocities uniform in
  * [-1/2, 1/2) with SMPC_INIT_REFERENCE_VELOCITIES, else Maxwell-Boltzmann at
- * kT; SMPC_INIT_SHEAR_PROFILE adds the steady Lees-Edwards flow shear * y to
- * v_x (a long sheared run's state, instead of a fluid at rest). */
+ * kT, minus their mean, so the solvent's total momentum is zero as in the
+ * reference; SMPC_INIT_SHEAR_PROFILE then adds the steady Lees-Edwards flow
+ * shear * y to v_x (a long sheared run's state, instead of a fluid at rest). */
 enum { SMPC_INIT_REFERENCE_VELOCITIES = 1, SMPC_INIT_SHEAR_PROFILE = 2 };
 int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int flags);
 

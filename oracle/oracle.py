@@ -79,6 +79,7 @@ def _oracle_lib():
             "orc_set_andersen": [P, C.c_double, C.c_uint64],
             "orc_stage_andersen": [P, C.c_int, P, P],
             "orc_set_lowe_andersen": [P, C.c_double, C.c_double, C.c_uint64],
+            "orc_set_f32_uniforms": [P, C.c_int], "orc_cell_members": [P, P, P],
         }.items():
             getattr(lib, name).argtypes = args
             getattr(lib, name).restype = None
@@ -217,6 +218,14 @@ class OracleSystem:
     def set_philox(self, seed, counter=0):
         self.lib.orc_set_philox(self.h, seed, counter)
 
+    def set_f32_uniforms(self, on=True):
+        """Collision draws from the FP32 path's 23-bit uniforms."""
+        self.lib.orc_set_f32_uniforms(self.h, int(on))
+
+    @property
+    def collision_counter(self):
+        return self.lib.orc_collision_counter(self.h)
+
     # stepping --------------------------------------------------------------
     def mpc_step(self, t, dt):
         self.lib.orc_mpc_step(self.h, t, dt)
@@ -243,6 +252,13 @@ class OracleSystem:
 
     def verlet_rebuilds(self):
         return self.lib.orc_verlet_rebuilds(self.h)
+
+    def cell_members(self):
+        """(fluid_cell[n_fluid], mono_cell[n_mono]) of the last collision, -1: not binned."""
+        fc = np.zeros(self.n_fluid, dtype=np.int32)
+        mc = np.zeros(max(self.n_mono, 1), dtype=np.int32)
+        self.lib.orc_cell_members(self.h, _p(fc), _p(mc))
+        return fc, mc[:self.n_mono]
 
 
 def profile_bins(L, width):

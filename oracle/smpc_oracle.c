@@ -79,6 +79,7 @@ struct smpc_orc {
   int* m_img;  /* Lees-Edwards image index of each monomer when binned wrapped */
 
   int rng_mode;
+  int f32_uniforms; /* orc_set_f32_uniforms: collision draws from 23-bit uniforms */
   const double* inj_shift;
   const double* inj_gamma;
   const double* inj_uphi;
@@ -148,6 +149,41 @@ static void philox_block(uint64_t seed, uint32_t cell, uint64_t step, uint32_t k
   orc_philox4x32_10(ctr, key, w);
   *uA = u53(w[0], w[1]);
   if (uB) *uB = u53(w[2], w[3]);
+}
+
+/* The FP32 path's uniforms: the top 23 bits of the high word of each pair,
+ * (w >> 9) 2^-23 + 2^-24, exact in a float and in a double. */
+static inline double u23(uint32_t hi) { return (double)(hi >> 9) * 0x1.0p-23 + 0x1.0p-24; }
+
+static void philox_block23(uint64_t seed, uint32_t cell, uint64_t step, uint32_t k, double* uA,
+                           double* uB) {
+  uint32_t ctr[4] = {cell, (uint32_t)step, (uint32_t)(step >> 32), k};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t w[4];
+  orc_philox4x32_10(ctr, key, w);
+  *uA = u23(w[1]);
+  if (uB) *uB = u23(w[3]);
+}
+
+static double philox_gamma_mode(uint64_t seed, uint64_t step, uint32_t cell, double shape,
+                                int f32u) {
+  const double d = shape - 1.0 / 3.0;
+  const double c = 1.0 / sqrt(9.0 * d);
+  void (*block)(uint64_t, uint32_t, uint64_t, uint32_t, double*, double*) =
+      f32u ? philox_block23 : philox_block;
+  for (uint32_t it = 0; it < 64; ++it) {
+    double a, b, u;
+    block(seed, cell, step, 1u + 2u * it, &a, &b);
+    const double x = sqrt(-2.0 * log(a)) * cos(2.0 * M_PI * b);
+    double v = 1.0 + c * x;
+    if (v <= 0.0) continue;
+    v = v * v * v;
+    block(seed, cell, step, 2u + 2u * it, &u, NULL);
+    const double x2 = x * x;
+    if (u < 1.0 - 0.0331 * (x2 * x2)) return d * v;
+    if (log(u) < 0.5 * x2 + d * (1.0 - v + log(v))) return d * v;
+  }
+  return d;
 }
 
 double orc_philox_gamma(uint64_t seed, uint64_t step, uint32_t cell, double shape) {
@@ -398,6 +434,7 @@ void orc_set_philox(smpc_orc* o, uint64_t seed, uint64_t collision_counter) {
   o->step_ctr = collision_counter;
 }
 uint64_t orc_collision_counter(const smpc_orc* o) { return o->step_ctr; }
+void orc_set_f32_uniforms(smpc_orc* o, int on) { o->f32_uniforms = on != 0; }
 
 /* -------------------------------------------------------- Box: Verlet/MD */
 
@@ -915,7 +952,7 @@ static void cell_thermostat(smpc_orc* o, unsigned c, const double* cmv) {
     g = o->inj_gamma ? o->inj_gamma[c] * 1.0 : 0.0;
     /* injected values are Gamma(1.5(n-1), kT) variates as drawn */
   } else {
-    g = orc_philox_gamma(o->seed, o->step_ctr, c, 1.5 * (count - 1)) * o->p.kT;
+    g = philox_gamma_mode(o->seed, o->step_ctr, c, 1.5 * (count - 1), o->f32_uniforms) * o->p.kT;
   }
   double scaling = sqrt(g / ekin);
   for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
@@ -1024,6 +1061,8 @@ static void cell_collide(smpc_orc* o, unsigned c, const double* cmv) {
   if (o->rng_mode == ORC_RNG_INJECT) {
     uphi = o->inj_uphi[c];
     uth = o->inj_utheta[c];
+  } else if (o->f32_uniforms) {
+    philox_block23(o->seed, c, o->step_ctr, 0u, &uphi, &uth);
   } else {
     philox_block(o->seed, c, o->step_ctr, 0u, &uphi, &uth);
   }
@@ -1179,6 +1218,25 @@ double orc_temperature(smpc_orc* o) {
 }
 
 unsigned orc_n_cells(const smpc_orc* o) { return o->n_cell; }
+
+/* Cell of every solvent particle and monomer in the last collision's cell
+ * lists (MPCParticle::CellIndex, MPC.cpp:209,224); -1 for one that was not
+ * binned. */
+void orc_cell_members(const smpc_orc* o, int* fluid_cell, int* mono_cell) {
+  if (fluid_cell)
+    for (long i = 0; i < o->n_f; ++i) fluid_cell[i] = -1;
+  if (mono_cell)
+    for (int m = 0; m < o->n_m; ++m) mono_cell[m] = -1;
+  for (unsigned c = 0; c < o->n_cell; ++c)
+    for (unsigned k = o->c_start[c]; k < o->c_start[c + 1]; ++k) {
+      const long id = o->c_mem[k];
+      if (id >= 0) {
+        if (fluid_cell) fluid_cell[id] = (int)c;
+      } else if (mono_cell) {
+        mono_cell[-id - 1] = (int)c;
+      }
+    }
+}
 
 void orc_cell_counts(const smpc_orc* o, unsigned* total, unsigned* fluid) {
   for (unsigned c = 0; c < o->n_cell; ++c) {

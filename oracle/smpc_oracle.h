@@ -124,6 +124,13 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 /* The project's gamma sampler on the Philox stream (shape a >= 1, scale 1). */
 double orc_philox_gamma(uint64_t seed, uint64_t step, uint32_t cell, double shape);
 
+/* Collision draws (rotation axis and gamma sampler, not the grid shift) from
+ * the FP32 path's 23-bit uniforms (w >> 9) 2^-23 + 2^-24 of the same Philox
+ * words, so the oracle consumes exactly the values the FP32 kernels do. */
+void orc_set_f32_uniforms(smpc_orc* o, int on);
+/* Cells of the last collision per solvent particle and monomer (-1: none). */
+void orc_cell_members(const smpc_orc* o, int* fluid_cell, int* mono_cell);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,8 @@ REPLICA_PERIODIC_MD = 1  # smpc_replica_desc.flags
 
 ERR_BITS = {1: "solvent cell out of range", 2: "monomer cell out of range",
             4: "Verlet list overflow", 8: "non-finite velocity", 32: "gamma iteration limit",
-            64: "FENE bond beyond R0", 128: "collide/bin cell mismatch"}
+            64: "FENE bond beyond R0", 128: "collide/bin cell mismatch",
+            256: "fixed-point cell sum out of range"}
 
 # Every entry point declared in include/smpc.h.
 EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "smpc_set_fluid",

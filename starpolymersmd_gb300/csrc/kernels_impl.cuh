@@ -33,9 +33,13 @@ void launch_cycle_end<Real>(RepDyn* dyn, int n_rep, cudaStream_t st) {
 
 template <>
 void launch_init_solvent<Real>(const RepInfo* reps, int rep, int slot_cap, Real* rec,
-                               unsigned long long seed, double kT, int ref_vel, cudaStream_t st) {
+                               unsigned long long seed, double kT, int flags, double* part,
+                               cudaStream_t st) {
+  static_assert(INIT_PART_DOUBLES == 3 * INIT_SUM_BLOCKS, "partials buffer size");
   if (slot_cap == 0) return;
-  k_init_solvent<Real><<<(slot_cap + 255) / 256, 256, 0, st>>>(reps, rep, rec, seed, kT, ref_vel);
+  k_init_solvent<Real><<<(slot_cap + 255) / 256, 256, 0, st>>>(reps, rep, rec, seed, kT, flags);
+  k_init_velocity_sum<Real><<<INIT_SUM_BLOCKS, INIT_SUM_THREADS, 0, st>>>(reps, rep, rec, part);
+  k_init_velocity_finish<Real><<<INIT_SUM_BLOCKS, 256, 0, st>>>(reps, rep, rec, part, flags);
 }
 
 template <>

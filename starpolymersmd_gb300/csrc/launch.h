@@ -64,7 +64,9 @@ template <typename R>
 void launch_cycle_end(RepDyn* dyn, int n_rep, cudaStream_t st);
 template <typename R>
 void launch_init_solvent(const RepInfo* reps, int rep, int slot_cap, R* rec,
-                         unsigned long long seed, double kT, int ref_vel, cudaStream_t st);
+                         unsigned long long seed, double kT, int flags, double* part,
+                         cudaStream_t st);
+constexpr int INIT_PART_DOUBLES = 3 * 256;  // k_init_velocity_sum partials (INIT_SUM_BLOCKS)
 template <typename R>
 void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* mvel, uint2* mkey,
                       int* mimg, uint32_t* count, ErrorState* err, int mono_bin, int strict,

@@ -250,6 +250,7 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
     long long px = 0, py = 0, pz = 0, e = 0;
     int nsol = 0;
     float mmono = 0.0f;
+    float big = 0.0f;  // largest fixed-point term (range check)
     if (j1 - j0 <= 1024) {
       // at most 512 terms per lane: int32 split accumulators
       int xh = 0, xl = 0, yh = 0, yl = 0, zh = 0, zl = 0, eh = 0, el = 0;
@@ -266,10 +267,13 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
           v = P.v;
           x = P.x;
         }
-        fix32_add(v.x * v.w, xh, xl);
-        fix32_add(v.y * v.w, yh, yl);
-        fix32_add(v.z * v.w, zh, zl);
-        fix32_add((v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z), eh, el);
+        const float mx = v.x * v.w, my = v.y * v.w, mz = v.z * v.w;
+        const float et = (v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z);
+        big = fmaxf(big, fmaxf(fmaxf(fabsf(mx), fabsf(my)), fmaxf(fabsf(mz), et)));
+        fix32_add(mx, xh, xl);
+        fix32_add(my, yh, yl);
+        fix32_add(mz, zh, zl);
+        fix32_add(et, eh, el);
         if (__float_as_uint(x.w) & MONO_BIT) {
           mmono += v.w;
         } else {
@@ -294,10 +298,13 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
           v = P.v;
           x = P.x;
         }
-        px += f2fix32(v.x * v.w);
-        py += f2fix32(v.y * v.w);
-        pz += f2fix32(v.z * v.w);
-        e += f2fix32((v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z));
+        const float mx = v.x * v.w, my = v.y * v.w, mz = v.z * v.w;
+        const float et = (v.w * 0.00390625f) * (v.x * v.x + v.y * v.y + v.z * v.z);
+        big = fmaxf(big, fmaxf(fmaxf(fabsf(mx), fabsf(my)), fmaxf(fabsf(mz), et)));
+        px += f2fix32(mx);
+        py += f2fix32(my);
+        pz += f2fix32(mz);
+        e += f2fix32(et);
         if (__float_as_uint(x.w) & MONO_BIT) {
           mmono += v.w;
         } else {
@@ -320,6 +327,7 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
     const uint32_t cg = static_cast<uint32_t>(t.begin + lc);
     const uint32_t cl = cg - cbase;
     const uint32_t nn = static_cast<uint32_t>(j1 - j0);
+    if (big >= FIX32_LIMIT) raise_error(err, ERR_FIXPOINT, cg, __float_as_uint(big));
     float scale = -1.0f;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // rotation axis (lane 1)
     if (rng == RNG_INJECT) {

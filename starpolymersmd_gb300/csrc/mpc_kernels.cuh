@@ -335,9 +335,74 @@ __global__ void k_init_solvent(const RepInfo* reps, int rep, R* st, unsigned lon
     v = R4<R>{static_cast<R>(sd * r1 * cos(t1)), static_cast<R>(sd * r1 * sin(t1)),
               static_cast<R>(sd * r2 * cos(t2)), R(0)};
   }
-  if (flags & 2)  // SMPC_INIT_SHEAR_PROFILE: the steady flow shear * y
-    v.x = static_cast<R>(static_cast<double>(v.x) + ri.shear * static_cast<double>(x.y));
   st_rec(st, slot, x, v);
+}
+
+// MPC::initialize removes the mean of the drawn velocities (MPC.cpp:42-48).
+// k_init_velocity_sum: per-block FP64 sums over the replica's solvent with a
+// fixed grid (grid-stride, warp butterflies, warps joined in order), so the
+// mean does not depend on scheduling. k_init_velocity_finish: every thread
+// sums the block partials in order, subtracts the mean, then adds the steady
+// flow shear * y to v_x for SMPC_INIT_SHEAR_PROFILE.
+constexpr int INIT_SUM_BLOCKS = 256;
+constexpr int INIT_SUM_THREADS = 256;
+
+template <typename R>
+__global__ void __launch_bounds__(INIT_SUM_THREADS)
+    k_init_velocity_sum(const RepInfo* reps, int rep, const R* st, double* part) {
+  const RepInfo ri = reps[rep];
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * INIT_SUM_THREADS + threadIdx.x; i < ri.n_fluid;
+       i += INIT_SUM_BLOCKS * INIT_SUM_THREADS) {
+    const R4<R> v = ld_vel(st, static_cast<size_t>(ri.slot_base) + i);
+    s0 += static_cast<double>(v.x);
+    s1 += static_cast<double>(v.y);
+    s2 += static_cast<double>(v.z);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xFFFFFFFFu, s0, o);
+    s1 += __shfl_xor_sync(0xFFFFFFFFu, s1, o);
+    s2 += __shfl_xor_sync(0xFFFFFFFFu, s2, o);
+  }
+  __shared__ double w[INIT_SUM_THREADS / 32][3];
+  if ((threadIdx.x & 31) == 0) {
+    w[threadIdx.x >> 5][0] = s0;
+    w[threadIdx.x >> 5][1] = s1;
+    w[threadIdx.x >> 5][2] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int k = 0; k < INIT_SUM_THREADS / 32; ++k) t += w[k][threadIdx.x];
+    part[3 * blockIdx.x + threadIdx.x] = t;
+  }
+}
+
+template <typename R>
+__global__ void k_init_velocity_finish(const RepInfo* reps, int rep, R* st, const double* part,
+                                       int flags) {
+  const RepInfo ri = reps[rep];
+  __shared__ double s_mean[3];
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int b = 0; b < INIT_SUM_BLOCKS; ++b) t += part[3 * b + threadIdx.x];
+    s_mean[threadIdx.x] = ri.n_fluid > 0 ? t / static_cast<double>(ri.n_fluid) : 0.0;
+  }
+  __syncthreads();
+  const double m0 = s_mean[0], m1 = s_mean[1], m2 = s_mean[2];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ri.n_fluid;
+       i += gridDim.x * blockDim.x) {
+    const size_t slot = static_cast<size_t>(ri.slot_base) + i;
+    const R4<R> x = ld_pos(st, slot);
+    R4<R> v = ld_vel(st, slot);
+    double vx = static_cast<double>(v.x) - m0;
+    if (flags & 2)  // SMPC_INIT_SHEAR_PROFILE: the steady flow shear * y
+      vx += ri.shear * static_cast<double>(x.y);
+    v.x = static_cast<R>(vx);
+    v.y = static_cast<R>(static_cast<double>(v.y) - m1);
+    v.z = static_cast<R>(static_cast<double>(v.z) - m2);
+    st4(st, 2 * slot + 1, v);
+  }
 }
 
 // One CTA per replica: MPC::check_bounds, then shift and bin the monomers.
@@ -569,12 +634,15 @@ struct AccT<float> {
 };
 
 
+// One term of a cell sum; the FP32 form also keeps the largest |v| converted
+// in `big` (fixed-point range check, precision.cuh).
 template <typename R>
-__device__ __forceinline__ typename AccT<R>::type to_acc(R v);
+__device__ __forceinline__ typename AccT<R>::type to_acc(R v, float& big);
 template <>
-__device__ __forceinline__ double to_acc<double>(double v) { return v; }
+__device__ __forceinline__ double to_acc<double>(double v, float&) { return v; }
 template <>
-__device__ __forceinline__ long long to_acc<float>(float v) {
+__device__ __forceinline__ long long to_acc<float>(float v, float& big) {
+  big = fmaxf(big, fabsf(v));
   return f2fix32(v);
 }
 
@@ -914,6 +982,7 @@ __global__ void __launch_bounds__(NT) k_collide(
     const int j1 = live ? static_cast<int>(s_off[lc + 1] - p0) : 0;
     R cm[3];
     R ekin = R(0);
+    float fix_big = 0.0f;  // FP32: largest fixed-point term (range check)
     if (kFP64) {
       R px = R(0), py = R(0), pz = R(0), mt = R(0);
       for (int j = j0 + half; j < j1; j += 2) {
@@ -952,9 +1021,9 @@ __global__ void __launch_bounds__(NT) k_collide(
         Particle<R> P;
         tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
         if (P.lc < 0) continue;
-        px += to_acc<R>(P.v.x * P.m);
-        py += to_acc<R>(P.v.y * P.m);
-        pz += to_acc<R>(P.v.z * P.m);
+        px += to_acc<R>(P.v.x * P.m, fix_big);
+        py += to_acc<R>(P.v.y * P.m, fix_big);
+        pz += to_acc<R>(P.v.z * P.m, fix_big);
         if (P.src & MONO_BIT) {
           mmono += static_cast<float>(P.m);
         } else {
@@ -976,7 +1045,7 @@ __global__ void __launch_bounds__(NT) k_collide(
         tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
         if (P.lc < 0) continue;
         const R d0 = P.v.x - cm[0], d1 = P.v.y - cm[1], d2 = P.v.z - cm[2];
-        e += to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2));
+        e += to_acc<R>(P.m * ((d0 * d0 + d1 * d1) + d2 * d2), fix_big);
       }
       e += __shfl_xor_sync(0xFFFFFFFFu, e, 1);
       ekin = acc_to_float(e) * 0.5f;
@@ -1051,10 +1120,10 @@ __global__ void __launch_bounds__(NT) k_collide(
         Particle<R> P;
         tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);
         if (P.lc < 0) continue;
-        s0 += to_acc<R>((P.x.x - k0) * P.m);
-        s1 += to_acc<R>((P.x.y - k1) * P.m);
-        s2 += to_acc<R>((P.x.z - k2) * P.m);
-        sm += to_acc<R>(P.m);
+        s0 += to_acc<R>((P.x.x - k0) * P.m, fix_big);
+        s1 += to_acc<R>((P.x.y - k1) * P.m, fix_big);
+        s2 += to_acc<R>((P.x.z - k2) * P.m, fix_big);
+        sm += to_acc<R>(P.m, fix_big);
       }
       s0 += shfl_pair(s0);
       s1 += shfl_pair(s1);
@@ -1085,15 +1154,15 @@ __global__ void __launch_bounds__(NT) k_collide(
         const R w0 = u0 - ((M[0] * u0 + M[1] * u1) + M[2] * u2);
         const R w1 = u1 - ((M[3] * u0 + M[4] * u1) + M[5] * u2);
         const R w2 = u2 - ((M[6] * u0 + M[7] * u1) + M[8] * u2);
-        a[0] += to_acc<R>(P.m * (q1 * w2 - q2 * w1));
-        a[1] += to_acc<R>(P.m * (q2 * w0 - q0 * w2));
-        a[2] += to_acc<R>(P.m * (q0 * w1 - q1 * w0));
-        a[3] += to_acc<R>(P.m * (q1 * q1 + q2 * q2));
-        a[4] += to_acc<R>(P.m * (q0 * q0 + q2 * q2));
-        a[5] += to_acc<R>(P.m * (q1 * q1 + q0 * q0));
-        a[6] += to_acc<R>(P.m * q0 * q1);
-        a[7] += to_acc<R>(P.m * q0 * q2);
-        a[8] += to_acc<R>(P.m * q1 * q2);
+        a[0] += to_acc<R>(P.m * (q1 * w2 - q2 * w1), fix_big);
+        a[1] += to_acc<R>(P.m * (q2 * w0 - q0 * w2), fix_big);
+        a[2] += to_acc<R>(P.m * (q0 * w1 - q1 * w0), fix_big);
+        a[3] += to_acc<R>(P.m * (q1 * q1 + q2 * q2), fix_big);
+        a[4] += to_acc<R>(P.m * (q0 * q0 + q2 * q2), fix_big);
+        a[5] += to_acc<R>(P.m * (q1 * q1 + q0 * q0), fix_big);
+        a[6] += to_acc<R>(P.m * q0 * q1, fix_big);
+        a[7] += to_acc<R>(P.m * q0 * q2, fix_big);
+        a[8] += to_acc<R>(P.m * q1 * q2, fix_big);
       }
 #pragma unroll
       for (int q = 0; q < 9; ++q) a[q] += shfl_pair(a[q]);
@@ -1108,6 +1177,8 @@ __global__ void __launch_bounds__(NT) k_collide(
         cmp[2] = k2 + c2;
       }
     }
+    if (!kFP64 && fix_big >= FIX32_LIMIT)
+      raise_error(err, ERR_FIXPOINT, C.c0 + lc, __float_as_uint(fix_big));
     if (half == 1 && live) {
       s_ang[3 * lc] = ang[0];
       s_ang[3 * lc + 1] = ang[1];

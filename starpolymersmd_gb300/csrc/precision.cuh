@@ -50,10 +50,16 @@ __device__ __forceinline__ float i2f_small(int i) {
   return __fsub_rn(__int_as_float(i + 0x4B400000), 12582912.0f);
 }
 
+// Range of the fixed-point conversions below: |v| < FIX32_LIMIT. They do not
+// clamp. Callers keep the largest |v| they convert (one max per term, cheaper
+// than a clamp) and raise ERR_FIXPOINT when it reaches the limit, since the
+// sums are meaningless then; NaN terms leave the maximum alone and are caught
+// by the non-finite check on the collided velocities.
+constexpr float FIX32_LIMIT = 4095.0f;
+
 // v * 2^32 rounded to an int64, |v| < 2^12: hi = rn(v * 2^10) and the exact
 // remainder v * 2^10 - hi (|.| <= 1/2) scaled by 2^22 give the two parts.
 __device__ __forceinline__ long long f2fix32(float v) {
-  v = fminf(fmaxf(v, -4095.0f), 4095.0f);
   const float a = v * 1024.0f;
   const int hi = f2i_rn_small(a);
   const float r = __fsub_rn(a, i2f_small(hi));
@@ -66,7 +72,6 @@ __device__ __forceinline__ long long f2fix32(float v) {
 // hi * 2^22 + lo. |hi| < 2^22 and |lo| <= 2^21 per term, so 512 terms cannot
 // overflow either part.
 __device__ __forceinline__ void fix32_add(float v, int& hi_acc, int& lo_acc) {
-  v = fminf(fmaxf(v, -4095.0f), 4095.0f);
   const float a = v * 1024.0f;
   const float m = __fadd_rn(a, 12582912.0f);  // rn(a) in the low mantissa bits
   const float r = __fsub_rn(a, __fsub_rn(m, 12582912.0f));  // a - rn(a), exact

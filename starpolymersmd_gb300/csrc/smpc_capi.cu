@@ -124,6 +124,7 @@ struct smpc_ctx {
   double* d_prof = nullptr;    // velocity-profile bins, grown on demand
   size_t prof_cap = 0;
   double* d_c6 = nullptr;      // centre of molecule 0 (position, velocity)
+  double* d_init_part = nullptr;  // solvent initialisation: block sums of the velocities
   double rot_c = 0, rot_s = 0;
   int max_nb = 192;
   bool collided = false;
@@ -637,6 +638,7 @@ int create_buffers(smpc_ctx* ctx) {
   CU(dalloc(&ctx->d_off, C + 1));
   CU(dalloc(&ctx->d_tsum, static_cast<size_t>(smpc::scan_tile_count(static_cast<int>(C)))));
   CU(dalloc(&ctx->d_grand, 1));
+  CU(dalloc(&ctx->d_init_part, static_cast<size_t>(smpc::INIT_PART_DOUBLES)));
   CU(dalloc(reinterpret_cast<R**>(&ctx->d_mpos), 4 * M));
   CU(dalloc(reinterpret_cast<R**>(&ctx->d_mvel), 4 * M));
   CU(dalloc(reinterpret_cast<R**>(&ctx->d_mfrc), 4 * M));
@@ -731,7 +733,7 @@ void free_all(smpc_ctx* ctx) {
                   ctx->d_mimg, ctx->d_bond_start, ctx->d_bonds, ctx->d_nlist, ctx->d_ncount,
                   ctx->d_md_order, ctx->d_inj, ctx->d_err, ctx->d_frames, ctx->d_rep_mols,
                   ctx->d_mols, ctx->d_obs, ctx->d_prof, ctx->d_c6, ctx->d_dstage, ctx->d_mol_obs,
-                  ctx->d_mol_rep};
+                  ctx->d_mol_rep, ctx->d_init_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < 3; ++k)
@@ -1603,11 +1605,11 @@ int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int flags) {
   if (ctx->opt.precision == SMPC_FP64)
     smpc::launch_init_solvent<double>(ctx->d_reps, rep, ri.slot_cap,
                                       static_cast<double*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
-                                      flags, ctx->st);
+                                      flags, ctx->d_init_part, ctx->st);
   else
     smpc::launch_init_solvent<float>(ctx->d_reps, rep, ri.slot_cap,
                                      static_cast<float*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
-                                     flags, ctx->st);
+                                     flags, ctx->d_init_part, ctx->st);
   CU(cudaGetLastError());
   return SMPC_OK;
 }

@@ -31,7 +31,8 @@ enum : uint32_t {
   ERR_TILE_OVF = 16u,      // collide tile larger than its register cache (handled, slow path)
   ERR_GAMMA_ITERS = 32u,   // gamma sampler hit its iteration limit
   ERR_FENE = 64u,          // FENE bond stretched beyond R0 (Potentials.h:29,50)
-  ERR_KEY_MISMATCH = 128u  // collide recomputed a different cell than binning (never expected)
+  ERR_KEY_MISMATCH = 128u, // collide recomputed a different cell than binning (never expected)
+  ERR_FIXPOINT = 256u      // FP32 cell sum term outside the fixed-point range (precision.cuh)
 };
 
 enum : int { POT_REF4824 = 0, POT_LJ126 = 1 };
