@@ -191,7 +191,8 @@ int smpc_cycles(smpc_ctx* ctx, int n);
 int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, double* total_ms);
 /* Launch-shape variants of the FP32 fast-path kernels (solvent binning,
  * collide, MD substeps); index 0 is the default. Changing them re-captures
- * the cycle graph. */
+ * the cycle graph. FP64 contexts of few replicas run each replica's MD on a
+ * cluster of SMs; md = 1 keeps one CTA per replica there instead. */
 int smpc_set_variants(smpc_ctx* ctx, int bin, int collide, int md);
 int smpc_get_variants(const smpc_ctx* ctx, int* bin, int* collide, int* md);
 /* Times every variant of each fast-path kernel over `cycles` live cycles

@@ -14,7 +14,7 @@ namespace smpc {
 // threads x cells-per-tile / staging capacity / gathers in flight.
 int bin_variant_count() { return 4; }
 int collide_variant_count() { return 9; }
-int md_variant_count() { return 4; }
+int md_variant_count() { return 5; }
 int collide_variant_cells(int v) {
   switch (v) {
     case 2: case 3: case 5: case 7: case 8: return 64;
@@ -35,7 +35,8 @@ const char* collide_variant_name(int v) {
 }
 const char* md_variant_name(int v) {
   static const char* n[] = {"1024t 1/thread", "512t 2/thread", "1024t lanes/bead, largest first",
-                            "1024t big + 512t small side by side, lanes/bead"};
-  return v >= 0 && v < 4 ? n[v] : "?";
+                            "1024t big + 512t small side by side, lanes/bead",
+                            "cluster of SMs per replica (few replicas; else 1024t 1/thread)"};
+  return v >= 0 && v < 5 ? n[v] : "?";
 }
 }  // namespace smpc

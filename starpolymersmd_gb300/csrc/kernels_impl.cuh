@@ -333,10 +333,70 @@ void launch_pack_monomers<Real>(const Real* mpos, const Real* mvel, const Real* 
     k_pack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(mpos, mvel, mfrc, n, pos, vel, frc);
 }
 
+template <int CS>
+static cudaError_t launch_md_cluster_cs(const MdArgs& a, int n_rep, Real* mpos, Real* mvel,
+                                        Real* mfrc, Real* mver, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(n_rep * CS));
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MdArgs b = a;
+  b.order = nullptr;
+  return cudaLaunchKernelEx(&cfg, k_md_cluster<Real, 256, CS, 8>, b, mpos, mvel, mfrc, mver);
+}
+
+template <int CS>
+static int cluster_fits() {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CS);
+  cfg.blockDim = dim3(256);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_md_cluster<Real, 256, CS, 8>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+template <>
+int md_cluster_size<Real>() {
+  if (cudaFuncSetAttribute(k_md_cluster<Real, 256, 16, 8>,
+                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+      cluster_fits<16>() > 0)
+    return 16;
+  cudaGetLastError();
+  return cluster_fits<8>() > 0 ? 8 : 0;
+}
+
 template <>
 void launch_md<Real>(const MdArgs& a, int n_rep, Real* mpos, Real* mvel, Real* mfrc, Real* mver,
                      int variant, cudaStream_t st, const MdSplit& split) {
   if (n_rep == 0) return;
+  static_assert(MD_CLUSTER_CAP == MD_CLUSTER_CAP_HOST, "cluster MD capacity");
+  // FP64: whenever the context chose clusters, unless variant 1 asks for one
+  // CTA per replica; FP32: launch-shape variant 4
+  if (split.cluster > 0 && !a.lowe && (SMPC_FAST_F32 ? variant == 4 : variant != 1)) {
+    if (split.cluster == 16)
+      launch_md_cluster_cs<16>(a, n_rep, mpos, mvel, mfrc, mver, st);
+    else
+      launch_md_cluster_cs<8>(a, n_rep, mpos, mvel, mfrc, mver, st);
+    return;
+  }
   MdArgs b = a;
 #if SMPC_FAST_F32
   if (variant == 3 && split.n_big > 0 && split.n_big < n_rep && a.order) {

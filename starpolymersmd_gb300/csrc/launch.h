@@ -89,7 +89,13 @@ struct MdSplit {
   cudaStream_t st2;
   cudaEvent_t fork, join;
   int n_big;
+  int cluster;  // > 0: non-periodic MD on clusters of this many CTAs per replica (k_md_cluster)
 };
+// Largest cluster size (16 or 8) at which k_md_cluster<R> can run on the
+// current device (0: none); enables the non-portable size 16 on the kernel.
+template <typename R>
+int md_cluster_size();
+constexpr int MD_CLUSTER_CAP_HOST = 1024;  // beads per replica k_md_cluster holds (MD_CLUSTER_CAP)
 template <typename R>
 void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, int variant,
                cudaStream_t st, const MdSplit& split);

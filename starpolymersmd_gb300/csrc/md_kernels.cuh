@@ -18,6 +18,7 @@
 // list, and a butterfly over the k lanes sums the partial forces. Small
 // replicas then use the whole CTA instead of n of its threads.
 #pragma once
+#include <cooperative_groups.h>
 #include <stdint.h>
 
 #include "mpc_kernels.cuh"
@@ -641,6 +642,280 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
     }
   }
   if (threadIdx.x == 0) {
+    a.dyn[r].verlet_rebuilds += rebuilds;
+    if (a.n_steps > 0) a.dyn[r].md_step = md_step0 + static_cast<unsigned long long>(a.n_steps);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The same substeps for one replica on a thread-block cluster of CS CTAs (CS
+// SMs), for boxes with few replicas: one CTA's FP64 pipe (2 DFMA per clock
+// per SM on this part) held a 401-bead star's FP64 MD to 150 us per substep.
+// Every CTA keeps a copy of all positions in its shared memory and owns the
+// beads i = rank + CS q; after its drift a bead's lead lane stores the new
+// position into every CTA's copy (distributed shared memory) and, when the
+// bead moved past the Verlet limit, sets every CTA's rebuild flag. Two
+// cluster barriers per substep: after the drift (positions and flags
+// complete everywhere) and after the forces (no copy is rewritten while it
+// is read). A rebuild hashes all beads in every CTA's own grid; each CTA
+// writes the lists of its own beads. Forces, kicks and the Andersen resets
+// are those of k_md_substeps for the owned beads (lanes per bead as there).
+// The barriers are hardware cluster barriers: every CTA of a cluster runs
+// at once, and every CTA reaches every barrier (all branches around them
+// depend on the replica and the rebuild flag only, which agree across the
+// cluster after each barrier). Lowe-Andersen stays on k_md_substeps.
+constexpr int MD_CLUSTER_CAP = 1024;
+
+template <typename R, int NT, int CS, int KMAX>
+__global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel, R* mfrc, R* mver) {
+  namespace cg = cooperative_groups;
+  constexpr int CAP = MD_CLUSTER_CAP;
+  __shared__ R sx[CAP], sy[CAP], sz[CAP];
+  __shared__ unsigned char s_amphi[CAP];
+  __shared__ int s_head[MD_BUCKETS];
+  __shared__ int s_next[CAP];
+  __shared__ int s_ckey[CAP];
+  __shared__ R s_core_ref[3];
+  __shared__ int s_rebuild;
+  __shared__ double s_red[NT / 32];
+  __shared__ double s_epot[CS];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = static_cast<int>(cl.block_rank());
+  const int cidx = static_cast<int>(blockIdx.x) / CS;
+  const int r = a.order ? a.order[cidx] : cidx;
+  const RepInfo ri = a.reps[r];
+  const int n = ri.n_mono;
+  // uniform over the cluster (one replica); no CTA has touched another's memory
+  if (n == 0 || n > CAP || (ri.flags & REP_PERIODIC_MD)) return;
+  const int own = (n - rank + CS - 1) / CS;  // beads rank + CS q, q < own
+  int lk = 0;  // log2 of the lanes per bead
+  if (KMAX > 1)
+    while ((2 << lk) <= KMAX && (own << (lk + 1)) <= NT) ++lk;
+  const int sub = static_cast<int>(threadIdx.x) & ((1 << lk) - 1);
+  const int q = static_cast<int>(threadIdx.x) >> lk;
+  const bool mine = q < own;
+  const int i = rank + CS * q;  // this lane's bead (when mine)
+  const bool lead = sub == 0;
+  const int b = ri.mono_base;
+  const R dt = static_cast<R>(ri.md_dt);
+  const R dth = dt * R(0.50);
+  const R lambda = static_cast<R>(ri.lambda);
+  const R rv2 = static_cast<R>(ri.r_verlet) * static_cast<R>(ri.r_verlet);
+  const R lim = (static_cast<R>(ri.r_verlet) - static_cast<R>(ri.r_cut)) * R(0.5);
+  const int pot = ri.potential;
+  const unsigned long long md_step0 = a.dyn[r].md_step;
+
+  // every CTA: all positions and types; this lane: its bead's state
+  for (int j = threadIdx.x; j < n; j += NT) {
+    const R4<R> p = ld4_rw(mpos, b + j);
+    sx[j] = p.x; sy[j] = p.y; sz[j] = p.z;
+    s_amphi[j] = static_cast<unsigned char>(static_cast<int>(ld4_rw(mvel, b + j).w) & 1);
+  }
+  R x[3] = {R(0), R(0), R(0)}, v[3] = {R(0), R(0), R(0)}, f[3] = {R(0), R(0), R(0)},
+    xv[3] = {R(0), R(0), R(0)}, m = R(1);
+  if (mine) {
+    const R4<R> p = ld4_rw(mpos, b + i), vv = ld4_rw(mvel, b + i), ff = ld4_rw(mfrc, b + i),
+                pv = ld4_rw(mver, b + i);
+    x[0] = p.x; x[1] = p.y; x[2] = p.z; m = p.w;
+    v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
+    f[0] = ff.x; f[1] = ff.y; f[2] = ff.z;
+    xv[0] = pv.x; xv[1] = pv.y; xv[2] = pv.z;
+  }
+  if (threadIdx.x == 0) {
+    s_rebuild = a.force_rebuild;
+    const R4<R> c = ld4_rw(mver, b);
+    s_core_ref[0] = c.x; s_core_ref[1] = c.y; s_core_ref[2] = c.z;
+  }
+  cl.sync();  // every copy loaded before any CTA writes into another's
+  int rebuilds = 0;
+  double epot = 0.0;
+  const int total_steps = a.n_steps > 0 ? a.n_steps : 1;
+  for (int step = 0; step < total_steps; ++step) {
+    if (a.n_steps > 0 && mine && lead) {
+      // kick + drift (Thermostat_None.cpp:22-27), by the bead's lead lane
+      // only (the FP64 pipe is the scarce resource); the other lanes read the
+      // new position from shared memory after the barrier
+      for (int d = 0; d < 3; ++d) {
+        v[d] += a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
+        x[d] += v[d] * dt;
+      }
+      {
+        bool over = false;
+        if (!a.core_relative) {  // Box::check_VerletLists (Box.cpp:182-194)
+          const R d0 = x[0] - xv[0], d1 = x[1] - xv[1], d2 = x[2] - xv[2];
+          over = r_sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim;
+        }
+        for (int c = 0; c < CS; ++c) {
+          cl.map_shared_rank(sx, c)[i] = x[0];
+          cl.map_shared_rank(sy, c)[i] = x[1];
+          cl.map_shared_rank(sz, c)[i] = x[2];
+          if (over) *cl.map_shared_rank(&s_rebuild, c) = 1;
+        }
+      }
+    }
+    cl.sync();  // positions and rebuild flags complete in every CTA
+    if (mine && !lead) { x[0] = sx[i]; x[1] = sy[i]; x[2] = sz[i]; }
+    if (a.core_relative && a.n_steps > 0) {
+      // displacements relative to the core's (see k_md_substeps)
+      const R c0 = sx[0] - s_core_ref[0], c1 = sy[0] - s_core_ref[1], c2 = sz[0] - s_core_ref[2];
+      if (mine && lead) {
+        const R d0 = x[0] - xv[0] - c0, d1 = x[1] - xv[1] - c1, d2 = x[2] - xv[2] - c2;
+        if ((d0 * d0 + d1 * d1) + d2 * d2 > lim * lim)
+          for (int c = 0; c < CS; ++c) *cl.map_shared_rank(&s_rebuild, c) = 1;
+      }
+      cl.sync();
+    }
+    const int rebuild = s_rebuild;  // the same in every CTA
+    __syncthreads();
+    if (threadIdx.x == 0) s_rebuild = 0;  // set again only after the next drift
+    if (rebuild) {
+      ++rebuilds;
+      const R inv_rv = R(1) / static_cast<R>(ri.r_verlet);
+      for (int t = threadIdx.x; t < MD_BUCKETS; t += NT) s_head[t] = -1;
+      __syncthreads();
+      for (int j = threadIdx.x; j < n; j += NT) {
+        const int cx = static_cast<int>(floor(sx[j] * inv_rv));
+        const int cy = static_cast<int>(floor(sy[j] * inv_rv));
+        const int cz = static_cast<int>(floor(sz[j] * inv_rv));
+        s_ckey[j] = md_cell_key(cx, cy, cz);
+        s_next[j] = atomicExch(&s_head[md_bucket(cx, cy, cz)], j);
+      }
+      __syncthreads();
+      if (mine && lead) {
+        const int cx = static_cast<int>(floor(x[0] * inv_rv));
+        const int cy = static_cast<int>(floor(x[1] * inv_rv));
+        const int cz = static_cast<int>(floor(x[2] * inv_rv));
+        int cnt = 0;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              const int tx = cx + dx, ty = cy + dy, tz = cz + dz;
+              const int want = md_cell_key(tx, ty, tz);
+              for (int j = s_head[md_bucket(tx, ty, tz)]; j >= 0; j = s_next[j]) {
+                if (j == i || s_ckey[j] != want) continue;
+                const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
+                if ((d0 * d0 + d1 * d1) + d2 * d2 <= rv2) {
+                  if (cnt < a.max_nb) a.nlist[static_cast<size_t>(cnt) * a.n_mono_total + b + i] = b + j;
+                  ++cnt;
+                }
+              }
+            }
+        if (cnt > a.max_nb) {
+          raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(b + i),
+                      static_cast<uint32_t>(cnt));
+          cnt = a.max_nb;
+        }
+        a.ncount[b + i] = cnt;
+      }
+      if (mine) { xv[0] = x[0]; xv[1] = x[1]; xv[2] = x[2]; }
+      if (threadIdx.x == 0) { s_core_ref[0] = sx[0]; s_core_ref[1] = sy[0]; s_core_ref[2] = sz[0]; }
+      __syncthreads();  // lists written before the lanes of a bead read them
+    }
+    const bool want_epot = a.calc_epot && (step == total_steps - 1);
+    // forces (Box.cpp:243-286)
+    R F0 = R(0), F1 = R(0), F2 = R(0);
+    if (mine) {
+      const bool ai = s_amphi[i] != 0;
+      const int cnt = a.ncount[b + i];
+      const int* nl = a.nlist + b + i;
+      const size_t stride = static_cast<size_t>(a.n_mono_total);
+      constexpr int PF = 4;
+      for (int q0 = sub; q0 < cnt; q0 += PF << lk) {
+        int js[PF];
+#pragma unroll
+        for (int u = 0; u < PF; ++u) {
+          const int qq = q0 + (u << lk);
+          js[u] = qq < cnt ? nl[static_cast<size_t>(qq) * stride] - b : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < PF; ++u) {
+          const int j = js[u];
+          if (j < 0) continue;
+          const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
+          const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+          const bool bb = ai && s_amphi[j] != 0;
+          const R fa = pair_force<R>(pot, bb, r2, lambda);
+          F0 -= d0 * fa;
+          F1 -= d1 * fa;
+          F2 -= d2 * fa;
+          if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
+        }
+      }
+      for (int e = lead ? a.bond_start[b + i] : 0; lead && e < a.bond_start[b + i + 1]; ++e) {
+        const int2 bd = a.bonds[e];
+        const int j = bd.x - b;
+        const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
+        const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+        const bool anch = bd.y != 0;
+        R r2f = r2;
+        if (pot == POT_REF4824) {
+          if (r2 >= (anch ? R(20.25) : R(2.25)))
+            raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + i), static_cast<uint32_t>(b + j));
+        } else {
+          const R cap = (anch ? R(20.25) : R(2.25)) * R(0.98);
+          if (r2f > cap) r2f = cap;
+        }
+        const R fa = fene_force<R>(anch, r2f);
+        F0 -= d0 * fa;
+        F1 -= d1 * fa;
+        F2 -= d2 * fa;
+        if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2f));
+      }
+    }
+    for (int o = 1; KMAX > 1 && o < (1 << lk); o <<= 1) {  // whole warps take part
+      F0 += __shfl_xor_sync(0xFFFFFFFFu, F0, o);
+      F1 += __shfl_xor_sync(0xFFFFFFFFu, F1, o);
+      F2 += __shfl_xor_sync(0xFFFFFFFFu, F2, o);
+    }
+    f[0] = F0; f[1] = F1; f[2] = F2;
+    if (mine && lead) {
+      if (a.n_steps > 0) {
+        for (int d = 0; d < 3; ++d)  // second half-kick
+          v[d] += a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
+        if (a.andersen) {
+          const int* as = a.and_start ? a.and_start + static_cast<size_t>(r) * (a.n_steps + 1)
+                                      : nullptr;
+          if (as && as[0] >= 0) {
+            for (int e = as[step]; e < as[step + 1]; ++e)
+              if (a.and_mono[e] == i)
+                for (int d = 0; d < 3; ++d) v[d] = static_cast<R>(a.and_vel[3 * e + d]);
+          } else {
+            andersen_draw<R>(ri.seed, i, md_step0 + static_cast<unsigned long long>(step),
+                             static_cast<R>(a.andersen_nu * ri.md_dt),
+                             r_sqrt(static_cast<R>(ri.kT)), m, v);
+          }
+        }
+      }
+    }
+    cl.sync();  // every CTA is done reading positions before the next drift rewrites them
+  }
+  if (mine && lead) {
+    R4<R> p = ld4_rw(mpos, b + i);
+    p.x = x[0]; p.y = x[1]; p.z = x[2];
+    st4(mpos, b + i, p);
+    R4<R> vv = ld4_rw(mvel, b + i);
+    vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
+    st4(mvel, b + i, vv);
+    st4(mfrc, b + i, R4<R>{f[0], f[1], f[2], R(0)});
+    st4(mver, b + i, R4<R>{xv[0], xv[1], xv[2], R(0)});
+  }
+  if (a.calc_epot) {
+    for (int o = 16; o > 0; o >>= 1) epot += __shfl_down_sync(0xFFFFFFFFu, epot, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = epot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < NT / 32; ++w) s += s_red[w];
+      cl.map_shared_rank(s_epot, 0)[rank] = s;
+    }
+    cl.sync();  // the partial sums are in CTA 0 (and nobody reads another CTA after this)
+    if (rank == 0 && threadIdx.x == 0) {
+      double s = 0.0;
+      for (int c = 0; c < CS; ++c) s += s_epot[c];
+      a.dyn[r].epot = s;
+    }
+  }
+  if (rank == 0 && threadIdx.x == 0) {
     a.dyn[r].verlet_rebuilds += rebuilds;
     if (a.n_steps > 0) a.dyn[r].md_step = md_step0 + static_cast<unsigned long long>(a.n_steps);
   }

@@ -121,6 +121,9 @@ struct Geo {
   R comv[3];
   R h;
   bool recentre;
+  // FP64 wraps (le_wrap<double>): bit patterns of L/2 (1 - 2^-50), L/2 and
+  // 1.5 L (1 - 2^-50) per axis
+  long long w_lo[3], w_half[3], w_far[3];
 };
 
 template <typename R>
@@ -140,6 +143,12 @@ __device__ __forceinline__ Geo<R> make_geo(const RepInfo& ri, const RepDyn& dn, 
   g.wrap_mono = mono_bin;
   g.h = static_cast<R>(dn.h);
   g.recentre = dn.recentre != 0;
+  for (int d = 0; d < 3; ++d) {
+    const double half = static_cast<double>(ri.L[d]) * 0.5;
+    g.w_lo[d] = __double_as_longlong(half * (1.0 - 0x1.0p-50));
+    g.w_half[d] = __double_as_longlong(half);
+    g.w_far[d] = __double_as_longlong(3.0 * half * (1.0 - 0x1.0p-50));
+  }
   return g;
 }
 
@@ -158,6 +167,51 @@ __device__ __forceinline__ void le_wrap(const Geo<R>& g, R& x, R& y, R& z, R& vx
     x = r_sub(x, r_mul(r_round(r_div(x, g.L[0])), g.L[0]));
     y = r_sub(y, r_mul(r_round(r_div(y, g.L[1])), g.L[1]));
     z = r_sub(z, r_mul(r_round(r_div(z, g.L[2])), g.L[2]));
+  }
+}
+
+// FP64: the same results as the formula above, bit for bit (signed zeros
+// aside), without its divisions and roundings, which on this part run on the
+// narrow FP64 pipe (2 instructions per clock per SM) and made the FP64 solvent
+// kernels FP64-bound. round(x / L) is decided from the magnitude bits of x,
+// whose integer order is the order of non-negative doubles: it is 0 below
+// L/2 (1 - 2^-50) and +-1 from L/2 (x / L >= 1/2 rounds away from zero) up
+// to 1.5 L (1 - 2^-50); in the two narrow bands in between, where rounding
+// x / L can reach 1/2 or 3/2, and beyond, the formula itself decides. x - L
+// and x + L are the formula's x - L round(x / L) for round = +-1 exactly.
+__device__ __forceinline__ double image_d(double y, double L, long long lo, long long half,
+                                          long long far) {
+  const long long bits = __double_as_longlong(y);
+  const long long ax = bits & 0x7FFFFFFFFFFFFFFFll;
+  if (ax < lo) return 0.0;
+  if (ax >= half && ax < far) return bits < 0 ? -1.0 : 1.0;
+  return r_round(r_div(y, L));
+}
+__device__ __forceinline__ double wrap_d(double x, double L, long long lo, long long half,
+                                         long long far) {
+  const long long bits = __double_as_longlong(x);
+  const long long ax = bits & 0x7FFFFFFFFFFFFFFFll;
+  if (ax < lo) return x;
+  if (ax >= half && ax < far) return bits < 0 ? r_add(x, L) : r_sub(x, L);
+  return r_sub(x, r_mul(L, r_round(r_div(x, L))));
+}
+template <>
+__device__ __forceinline__ void le_wrap<double>(const Geo<double>& g, double& x, double& y,
+                                                double& z, double& vx) {
+  if (g.shear_on) {
+    const double cy = image_d(y, g.L[1], g.w_lo[1], g.w_half[1], g.w_far[1]);
+    x = wrap_d(x, g.L[0], g.w_lo[0], g.w_half[0], g.w_far[0]);
+    if (cy != 0.0) x = r_sub(x, r_mul(cy, g.delrx));
+    x = wrap_d(x, g.L[0], g.w_lo[0], g.w_half[0], g.w_far[0]);
+    if (cy != 0.0) {
+      y = r_sub(y, r_mul(g.L[1], cy));
+      vx = r_sub(vx, r_mul(r_mul(cy, g.shear), g.L[1]));
+    }
+    z = wrap_d(z, g.L[2], g.w_lo[2], g.w_half[2], g.w_far[2]);
+  } else {
+    x = wrap_d(x, g.L[0], g.w_lo[0], g.w_half[0], g.w_far[0]);
+    y = wrap_d(y, g.L[1], g.w_lo[1], g.w_half[1], g.w_far[1]);
+    z = wrap_d(z, g.L[2], g.w_lo[2], g.w_half[2], g.w_far[2]);
   }
 }
 

@@ -1060,6 +1060,23 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
   // replicas above 512 monomers lead the MD order (it sorts by size)
   for (int r = 0; r < n_rep; ++r)
     if (ctx->reps[r].n_mono > 512) ++ctx->md_split.n_big;
+  {
+    // Few replicas: each one's MD on a cluster of SMs (k_md_cluster: always in
+    // FP64, whose per-SM rate one CTA cannot get past; an autotuner candidate
+    // in FP32). Many replicas: one CTA per replica already fills the GPU.
+    int sms = 0, local = 0, biggest = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    for (int r = 0; r < n_rep; ++r)
+      if (!(ctx->reps[r].flags & smpc::REP_PERIODIC_MD) && ctx->reps[r].n_mono > 0) {
+        ++local;
+        biggest = std::max(biggest, ctx->reps[r].n_mono);
+      }
+    const int cs = opt->precision == SMPC_FP64 ? smpc::md_cluster_size<double>()
+                                               : smpc::md_cluster_size<float>();
+    if (cs > 0 && local > 0 && local * cs <= sms && biggest <= smpc::MD_CLUSTER_CAP_HOST &&
+        opt->md_thermostat != SMPC_MDTHERMO_LOWE_ANDERSEN)
+      ctx->md_split.cluster = cs;
+  }
   int rc = opt->precision == SMPC_FP64 ? create_buffers<double>(ctx) : create_buffers<float>(ctx);
   if (rc) return bail(rc, ctx->err);
   const int ct = opt->precision == SMPC_FP64 ? smpc::collide_cells_per_tile<double>()

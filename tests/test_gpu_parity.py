@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as orc
-from starpolymersmd_gb300 import capi
+from starpolymersmd_gb300 import capi, system
 from tests import golden_replay as gr
 from tests import gpu_helpers as H
 
@@ -278,28 +278,33 @@ def test_batched_fp64_matches_independent_oracles():
 
 
 def test_batched_fp32_tracks_fp64_oracle():
-    # FP32 state, fixed-point cell sums and FP32 Philox uniforms/gamma against
-    # the FP64 oracle on the same counter-based stream: all but a few per cent
-    # of the solvent (cells whose gamma acceptance or face assignment flips
-    # under FP32 rounding) must agree to FP32 accuracy after two cycles.
-    ctx, oracles, specs = _batch_run(capi.FP32)
+    # FP32 state, fixed-point cell sums and FP32 Philox draws against the FP64
+    # oracle consuming the same 23-bit uniforms, one cycle at a time from the
+    # FP32 state: every particle outside the cells where a particle within
+    # FP32 rounding of a face was binned differently agrees to FP32 accuracy
+    # (tests/gpu_helpers.fp32_cycle_check).
+    ctx, oracles, specs = _batch_run(capi.FP32, cycles=0)
+    for o in oracles:
+        o.set_f32_uniforms(True)
     with ctx:
-        for k, (o, s) in enumerate(zip(oracles, specs)):
-            p, v = ctx.get_fluid(k)
-            op, ov = o.get_fluid()
-            dp = np.abs(H.wrapped_diff(p, op, (s.L,) * 3)).max(axis=1)
-            dv = np.abs(v - ov).max(axis=1)
-            vs = np.abs(ov).max()
-            bad = (dp > 1e-4 * s.L) | (dv > 1e-3 * vs)
-            assert bad.mean() < 0.03, (k, bad.mean())
-            assert abs(ctx.temperature(k) - o.temperature()) < 0.01
-            # the fast path's cell-ordered records give the same membership as its counts
-            tot, fl = ctx.cell_counts(k)
-            fc, mc = ctx.cell_members(k)
-            n = len(tot)
-            np.testing.assert_array_equal(np.bincount(fc, minlength=n), fl)
-            np.testing.assert_array_equal(np.bincount(fc, minlength=n) +
-                                          np.bincount(mc[mc >= 0], minlength=n), tot)
+        from starpolymersmd_gb300 import workloads as W
+        for c in range(3):
+            for k, o in enumerate(oracles):
+                H.resync_oracle(ctx, o, k)
+            ctx.cycles(1)
+            ctx.synchronize()
+            ctx.raise_on_device_error()
+            for k, (o, s) in enumerate(zip(oracles, specs)):
+                o.run(1 + W.N_SUB * c, W.N_SUB, W.H, True)
+                assert o.error() == 0
+                H.fp32_cycle_check(ctx, o, k, s.L)
+                # the fast path's cell-ordered records give the same membership as its counts
+                tot, fl = ctx.cell_counts(k)
+                fc, mc = ctx.cell_members(k)
+                n = len(tot)
+                np.testing.assert_array_equal(np.bincount(fc, minlength=n), fl)
+                np.testing.assert_array_equal(np.bincount(fc, minlength=n) +
+                                              np.bincount(mc[mc >= 0], minlength=n), tot)
 
 
 def test_fp32_launch_variants_agree_bitwise():
@@ -402,12 +407,13 @@ def test_two_phase_step_replays_reference(golden_dir, name):
             assert ctx.delrx(0) == fx["delrx"][t]
 
 
-@pytest.mark.parametrize("md_variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("md_variant", [0, 1, 2, 3, 4])
 def test_fp32_md_variants_track_fp64_oracle(md_variant):
     # MD only (no collisions): every FP32 launch shape of the substep kernel,
-    # including the one that splits a bead's Verlet list over several lanes
-    # and the one that runs stars above 512 beads in a second kernel beside
-    # the rest, follows the FP64 oracle to FP32 round-off over 20 substeps.
+    # including the one that splits a bead's Verlet list over several lanes,
+    # the one that runs stars above 512 beads in a second kernel beside the
+    # rest and the one that spreads each replica over a cluster of SMs,
+    # follows the FP64 oracle to FP32 round-off over 20 substeps.
     from starpolymersmd_gb300 import system, workloads as W
     specs = _batch_specs() + [system.ReplicaSpec(L=16, arms=6, n_arm=20, solvophobic_fraction=0.3,
                                                  shear=0.05, seed=34),
@@ -673,3 +679,89 @@ def test_cycles_io_pinned_input_is_read_in_place():
     finally:
         a.close()
         b.close()
+
+
+@pytest.mark.parametrize("md_variant", [0, 1], ids=["cluster", "one_cta"])
+def test_fp64_md_shapes_match_oracle(md_variant):
+    # FP64 contexts of few replicas run each replica's MD on a cluster of SMs
+    # (variant 0); variant 1 keeps one CTA per replica. Both follow the
+    # oracle at 1e-12 over 3 cycles of the config-1 star with Andersen-free
+    # velocity Verlet, with and without an energy read-out.
+    L, su, h = 20, 10, 0.1
+    star, fpos, fvel = H.small_star_system(L=L, arms=6, n_arm=20, shear=0.05, seed=1)
+    o = H.oracle_for(star, fpos, fvel, L, 1.0, 0.05, su)
+    o.set_philox(seed=5, counter=0)
+    with H.context_for(star, fpos, fvel, L, 1.0, 0.05, su, rng=capi.RNG_PHILOX, seed=5) as ctx:
+        ctx.set_variants(0, 0, md_variant)
+        for t in range(0, 3 * su + 1):
+            o.propagate(t == 3 * su)
+            o.mpc_step(t, h)
+            ctx.md_substeps(1, calc_epot=(t == 3 * su))
+            ctx.mpc_step(t, h)
+        ctx.raise_on_device_error()
+        assert o.error() == 0
+        mp, mv, mf = ctx.get_monomers(0)
+        omp, omv, omf = o.get_monomers()
+        H.close64(mp, omp)
+        H.close64(mv, omv)
+        H.close64(mf, omf, rtol=1e-11)
+        H.close64(ctx.epot(0), o.epot())
+        p, v = ctx.get_fluid(0)
+        op, ov = o.get_fluid()
+        H.close64(p, op)
+        H.close64(v, ov)
+        assert ctx.verlet_rebuilds(0) >= 1
+
+
+@pytest.mark.parametrize("L,shear", [(7, 0.0), (20, 0.3), (29, 0.05)])
+def test_fp64_wraps_bitwise_at_the_faces(L, shear):
+    # The FP64 kernels decide each wrap's image from the magnitude bits of
+    # the coordinate instead of round(x / L); solvent particles at rest
+    # exactly on, and a few ulps either side of, +-L/2 and +-1.5 L (and 2.5 L)
+    # on every axis must come out of a collision (stream, shift, sort,
+    # unshift, with the reference's LEBC at every step) bit for bit as the
+    # oracle's, which evaluates the reference's formula.
+    rng = np.random.default_rng(L)
+    base = []
+    for edge in (0.5, 1.5):
+        for k in range(-4, 5):
+            e = edge * L * (1.0 + k * 2.0 ** -52)
+            base += [e, -e, np.nextafter(e, 0.0), np.nextafter(-e, 0.0)]
+    base += [2.5 * L, -2.5 * L, 0.0]
+    vals = np.array(base)
+    pts = []
+    for ax in range(3):
+        for v in vals:
+            p = (rng.random(3) - 0.5) * 0.5 * L
+            p[ax] = v
+            pts.append(p)
+    edge_pos = np.array(pts)
+    fpos, fvel = system.uniform_fluid((L, L, L), 10, 1.0, rng)
+    fpos = np.concatenate([fpos, edge_pos])
+    fvel = np.concatenate([fvel, np.zeros_like(edge_pos)])
+    n_cell = L ** 3
+    # nonzero shifts: binning happens away from the faces (points a few ulps
+    # inside +L/2 would otherwise hit the reference's own cell aliasing), while
+    # the streaming and the unshift wrap at the edges themselves
+    for shift in (np.array([0.25, -0.125, 0.375]), np.array([-0.3, 0.45, -0.05])):
+        inj = (shift, rng.gamma(13.5, 1.0, n_cell), rng.random(n_cell), rng.random(n_cell))
+        o = orc.OracleSystem((L,) * 3, 1.0, shear, 1, len(fpos))
+        o.delrx = 0.3 * L
+        o.set_fluid(fpos, fvel)
+        o.set_inject(*inj)
+        o.mpc_step(0, 0.1)
+        assert o.error() == 0
+        rep = dict(L=(L,) * 3, n_fluid=len(fpos), kT=1.0, shear=shear, h=0.1)
+        with capi.Context([rep], precision=capi.FP64, rng=capi.RNG_INJECT, step_update=1) as ctx:
+            ctx.set_delrx(0, 0.3 * L)
+            ctx.set_fluid(0, fpos, fvel)
+            ctx.mpc_step(0, 0.1, *inj)
+            ctx.raise_on_device_error()
+            p, v = ctx.get_fluid(0)
+            op, ov = o.get_fluid()
+            np.testing.assert_array_equal(p, op)
+            fc, _ = ctx.cell_members(0)
+            ofc, _ = o.cell_members()
+            np.testing.assert_array_equal(fc, ofc)
+            H.close64(v, ov)
+            assert ctx.delrx(0) == o.delrx
