@@ -163,6 +163,6 @@ void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* g
                  cudaStream_t st);
 int scan_tile_count(int n_cells);
 void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_mono,
-                       const uint32_t* off, uint32_t* perm, cudaStream_t st);
+                       const uint32_t* off, uint32_t* perm, ErrorState* err, cudaStream_t st);
 
 }  // namespace smpc

@@ -672,7 +672,8 @@ __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepIn
 // perm[off[key] + rank] = source for every binned solvent slot and monomer.
 __global__ void k_build_perm(const uint2* __restrict__ keys, int n_slots,
                              const uint2* __restrict__ mkey, int n_mono,
-                             const uint32_t* __restrict__ off, uint32_t* __restrict__ perm);
+                             const uint32_t* __restrict__ off, uint32_t* __restrict__ perm,
+                             ErrorState* err);
 
 // --------------------------------------------------------- collide
 

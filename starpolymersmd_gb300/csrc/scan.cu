@@ -142,13 +142,16 @@ __global__ void __launch_bounds__(SCAN_NT) k_scan_add(uint32_t* __restrict__ off
 
 // perm[off[cell] + rank] = source. Each thread takes PERM_U entries a block
 // apart and issues all key loads, then all offset gathers, then the stores,
-// so PERM_U independent gather chains are in flight per thread.
+// so PERM_U independent gather chains are in flight per thread. A position
+// past the last entry (counts that do not match the keys; never expected) is
+// reported in the error word, not written.
 constexpr int PERM_NT = 256;
 constexpr int PERM_U = 4;
 __global__ void __launch_bounds__(PERM_NT) k_build_perm(const uint2* __restrict__ keys, int n_slots,
                                                         const uint2* __restrict__ mkey, int n_mono,
                                                         const uint32_t* __restrict__ off,
-                                                        uint32_t* __restrict__ perm) {
+                                                        uint32_t* __restrict__ perm,
+                                                        ErrorState* err) {
   const int n = n_slots + n_mono;
   const int base = blockIdx.x * (PERM_NT * PERM_U) + threadIdx.x;
   uint2 k[PERM_U];
@@ -168,8 +171,11 @@ __global__ void __launch_bounds__(PERM_NT) k_build_perm(const uint2* __restrict_
   for (int u = 0; u < PERM_U; ++u) {
     const int i = base + u * PERM_NT;
     if (k[u].x == KEY_NONE) continue;
-    perm[o[u] + k[u].y] =
-        i < n_slots ? static_cast<uint32_t>(i) : (MONO_BIT | static_cast<uint32_t>(i - n_slots));
+    const uint32_t pos = o[u] + k[u].y;
+    if (pos < static_cast<uint32_t>(n))
+      perm[pos] = i < n_slots ? static_cast<uint32_t>(i) : (MONO_BIT | static_cast<uint32_t>(i - n_slots));
+    else
+      raise_error(err, ERR_KEY_MISMATCH, pos, k[u].x);
   }
 }
 
@@ -186,11 +192,11 @@ void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* g
 }
 
 void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_mono,
-                       const uint32_t* off, uint32_t* perm, cudaStream_t st) {
+                       const uint32_t* off, uint32_t* perm, ErrorState* err, cudaStream_t st) {
   const int n = n_slots + n_mono;
   if (n == 0) return;
   k_build_perm<<<(n + PERM_NT * PERM_U - 1) / (PERM_NT * PERM_U), PERM_NT, 0, st>>>(
-      keys, n_slots, mkey, n_mono, off, perm);
+      keys, n_slots, mkey, n_mono, off, perm, err);
 }
 
 }  // namespace smpc

@@ -214,7 +214,8 @@ int launch_binning(smpc_ctx* ctx, int cur) {
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
   smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
-                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->st);
+                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->d_err,
+                          ctx->st);
   return SMPC_OK;
 }
 
@@ -327,7 +328,8 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
                     static_cast<int>(ctx->total_cells), ctx->st);
   cudaEventRecord(ev[1 + PH_SCAN], ctx->st);
   smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
-                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->st);
+                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->d_err,
+                          ctx->st);
   cudaEventRecord(ev[1 + PH_PERM], ctx->st);
   smpc::CollideArgs<R> a = collide_args<R>(ctx, smpc::RNG_PHILOX, cur);
   smpc::launch_collide<R>(a, ctx->st);

@@ -29,18 +29,24 @@ uniform in the box with Maxwell-Boltzmann velocities at kT plus the steady
 flow shear * y, mean removed. Both come from numpy's PCG64 and are regenerated
 by the test with the same calls.
 
-Recorded: after EQUIL cycles, every SAMPLE-th of PROD cycles,
+Recorded: RUNS independent trajectories from the same initial star (solvent
+from numpy seed FLUID_SEED + k, the reference's random stream re-seeded with
+RAND_SEED + k), run in parallel processes. For each, after EQUIL cycles,
+every SAMPLE-th of PROD cycles:
   T_est   MPC::calculateCurrentTemperature (MPC.cpp:405-409),
   obs     Box observables after center_of_mass_reference_frame (R_g, gyration
           tensor, rotation frequency, kinetic energy, polymer temperature;
           Box.cpp:288-379, 635-646),
   prof_y  VelocityX along y with bins of width 1 (Velocity_x.h:76-100),
-as means over BLOCKS consecutive blocks, plus the initial star.
+kept as the means over BLOCKS consecutive blocks of each run. A stretched
+star tumbling in shear flow decorrelates slowly, so the comparison uses the
+spread of the run means, not blocks of one run.
 
     SMPC_REFERENCE=<reference checkout> python tests/golden/make_longrun.py
 """
 from __future__ import annotations
 
+import multiprocessing as mp
 import os
 import sys
 import time
@@ -57,10 +63,12 @@ from starpolymersmd_gb300 import system  # noqa: E402
 L, NC, KT, SHEAR, MASS, LAM = 50, 10, 1.0, 0.05, 5.0, 1.0
 ARMS, A, B = 6, 10, 10
 H_MPC, MD_DT, N_SUB = 0.1, 0.01, 10
-EQUIL, PROD, SAMPLE, BLOCKS = 1000, 10000, 10, 20
+EQUIL, PROD, SAMPLE, BLOCKS = 1000, 10000, 10, 10
+RUNS = 8
 WIDTH = 1.0
 FLUID_SEED = 1
 STAR_SEED = 1
+RAND_SEED = 1000
 
 
 def initial_star():
@@ -75,10 +83,10 @@ def initial_star():
     raise RuntimeError("no compact star")
 
 
-def initial_fluid():
+def initial_fluid(run=0):
     """Uniform positions, Maxwell-Boltzmann velocities at KT, mean removed,
     plus the steady linear flow SHEAR * y along x."""
-    rng = np.random.default_rng(FLUID_SEED)
+    rng = np.random.default_rng(FLUID_SEED + run)
     n = NC * L ** 3
     pos = (rng.random((n, 3)) - 0.5) * L
     vel = rng.normal(0.0, np.sqrt(KT), (n, 3))
@@ -91,18 +99,16 @@ def sample_row(T, obs, prof_y):
     return np.concatenate([[T], obs, prof_y.ravel()])
 
 
-def main():
+def one_run(run):
+    """Block means (BLOCKS x columns) of one trajectory of the reference."""
     ref = orc.RefSystem((L, L, L), KT, LAM, NC, SHEAR, 1)
+    ref.reseed(RAND_SEED + run)
     ref.add_star(A, B, ARMS, MASS)
     star = initial_star()
     ref.set_monomers(star.pos, star.vel)
     ref.make_thermostat(MD_DT)
-    pos, vel = initial_fluid()
+    pos, vel = initial_fluid(run)
     ref.set_fluid(pos, vel)
-    star0 = ref.get_monomers()
-    bsrc, bdst = ref.bonds()
-    assert np.array_equal(star0["amphi"], star.amphi) and np.array_equal(star0["anchor"], star.anchor)
-    t0 = time.time()
     rows = []
     t = 0
     for c in range(EQUIL + PROD):
@@ -117,20 +123,36 @@ def main():
             rows.append(sample_row(T, obs, py))
     rows = np.array(rows)
     per = len(rows) // BLOCKS
-    blocks = rows[: per * BLOCKS].reshape(BLOCKS, per, -1).mean(axis=1)
-    out = os.path.join(HERE, "longrun_config1.npz")
+    return rows[: per * BLOCKS].reshape(BLOCKS, per, -1).mean(axis=1)
+
+
+def main():
+    ref = orc.RefSystem((L, L, L), KT, LAM, NC, SHEAR, 1)
+    ref.add_star(A, B, ARMS, MASS)
+    star = initial_star()
+    ref.set_monomers(star.pos, star.vel)
+    star0 = ref.get_monomers()
+    bsrc, bdst = ref.bonds()
+    assert np.array_equal(star0["amphi"], star.amphi) and np.array_equal(star0["anchor"], star.anchor)
+    del ref
+    t0 = time.time()
+    with mp.get_context("spawn").Pool(min(RUNS, os.cpu_count() or 1)) as pool:
+        blocks = np.array(pool.map(one_run, range(RUNS)))
+    out = os.path.join(HERE, "longrun", "longrun_config1.npz")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
     np.savez_compressed(
         out, blocks=blocks, L=L, n_c=NC, kT=KT, shear=SHEAR, mass=MASS, lam=LAM, arms=ARMS,
         A=A, B=B, h=H_MPC, md_dt=MD_DT, n_sub=N_SUB, equil=EQUIL, prod=PROD, sample=SAMPLE,
-        width=WIDTH, fluid_seed=FLUID_SEED, star_seed=STAR_SEED, star_pos=star0["pos"], star_vel=star0["vel"],
-        star_mass=star0["mass"], star_amphi=star0["amphi"], star_anchor=star0["anchor"],
-        bond_src=bsrc, bond_dst=bdst,
+        width=WIDTH, fluid_seed=FLUID_SEED, star_seed=STAR_SEED, rand_seed=RAND_SEED,
+        star_pos=star0["pos"], star_vel=star0["vel"], star_mass=star0["mass"],
+        star_amphi=star0["amphi"], star_anchor=star0["anchor"], bond_src=bsrc, bond_dst=bdst,
         columns=np.array(["T_est"] + [f"obs{k}" for k in range(16)] +
                          [f"prof{k}_{q}" for k in range(orc.profile_bins(L, WIDTH))
                           for q in ("vx", "vy", "n")]))
-    m = blocks.mean(axis=0)
-    se = blocks.std(axis=0, ddof=1) / np.sqrt(BLOCKS)
-    print(f"{len(rows)} samples in {time.time() - t0:.0f} s -> {out}")
+    runs = blocks.mean(axis=1)
+    m = runs.mean(axis=0)
+    se = runs.std(axis=0, ddof=1) / np.sqrt(RUNS)
+    print(f"{RUNS} runs in {time.time() - t0:.0f} s -> {out}")
     print(f"T_est {m[0]:.5f} +- {se[0]:.5f}; R_g {m[1]:.4f} +- {se[1]:.4f}; "
           f"polymer T {m[15]:.4f} +- {se[15]:.4f}")
 

@@ -102,3 +102,51 @@ def context_for(star, fpos, fvel, L, kT, shear, step_update, h=0.1, md_dt=0.01, 
         ctx.set_bonds(0, star.bond_src, star.bond_dst)
         ctx.init_md()
     return ctx
+
+
+def fp32_cycle_check(ctx, o, rep, L):
+    """One cycle of the FP32 context (already run) against the oracle (run
+    from the same FP32 state on the 23-bit uniforms). Returns the number of
+    particles binned differently."""
+    fc, mc = ctx.cell_members(rep)
+    ofc, omc = o.cell_members()
+    flip_f = np.flatnonzero(fc != ofc)
+    flip_m = np.flatnonzero(mc != omc)
+    n = len(fc) + len(mc)
+    n_flip = len(flip_f) + len(flip_m)
+    # a particle within FP32 rounding of a cell face (|x| ulp ~ 2e-6 here)
+    # lands in the neighbouring cell with probability ~1e-5 per particle
+    assert n_flip <= 5 + 5e-5 * n, n_flip
+    touched = np.unique(np.concatenate([fc[flip_f], ofc[flip_f], mc[flip_m], omc[flip_m]]))
+    ex_f = np.isin(fc, touched) | np.isin(ofc, touched)
+    ex_m = np.isin(mc, touched) | np.isin(omc, touched)
+    p, v = ctx.get_fluid(rep)
+    op, ov = o.get_fluid()
+    dp = np.abs(wrapped_diff(p, op, (L,) * 3)).max(axis=1)
+    dv = np.abs(v - ov).max(axis=1)
+    vs = float(np.abs(ov).max())
+    # one FP32 step from identical inputs: positions to a few ulp of L,
+    # velocities to the stated FP32 tolerance, for every particle of every
+    # cell that holds the same particles on both sides
+    bad = ((dp > 1e-6 * L) | (dv > FP32_VEL_RTOL * vs)) & ~ex_f
+    # a gamma acceptance test within FP32 rounding of its threshold (about
+    # 1e-7 per cell) would change one whole cell: at most one such cell
+    bad_cells = np.unique(ofc[bad])
+    assert len(bad_cells) <= 1, (len(bad_cells), dp[bad].max(), dv[bad].max())
+    mp, mv, _ = ctx.get_monomers(rep)
+    omp, omv, _ = o.get_monomers()
+    keep = ~ex_m
+    assert np.abs(wrapped_diff(mp, omp, (L,) * 3)[keep]).max(initial=0.0) < 1e-4
+    assert np.abs(mv - omv)[keep].max(initial=0.0) < 1e-3
+    assert abs(ctx.temperature(rep) - o.temperature()) < 1e-4
+    assert ctx.delrx(rep) == o.delrx
+    return n_flip
+
+
+def resync_oracle(ctx, o, rep):
+    # the oracle continues from the FP32 state (exact in FP64), so each cycle
+    # is compared on its own
+    p, v = ctx.get_fluid(rep)
+    o.set_fluid(p, v)
+    mp, mv, mf = ctx.get_monomers(rep)
+    o.set_monomers(mp, mv, mf)

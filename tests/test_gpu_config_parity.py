@@ -165,54 +165,6 @@ def test_fp64_largest_batched_replicas_match_oracles():
 
 # ----------------------------------------------------------------- FP32
 
-def _fp32_cycle_check(ctx, o, rep, L):
-    """One cycle of the FP32 context (already run) against the oracle (run
-    from the same FP32 state on the 23-bit uniforms). Returns the number of
-    particles binned differently."""
-    fc, mc = ctx.cell_members(rep)
-    ofc, omc = o.cell_members()
-    flip_f = np.flatnonzero(fc != ofc)
-    flip_m = np.flatnonzero(mc != omc)
-    n = len(fc) + len(mc)
-    n_flip = len(flip_f) + len(flip_m)
-    # a particle within FP32 rounding of a cell face (|x| ulp ~ 2e-6 here)
-    # lands in the neighbouring cell with probability ~1e-5 per particle
-    assert n_flip <= 5 + 5e-5 * n, n_flip
-    touched = np.unique(np.concatenate([fc[flip_f], ofc[flip_f], mc[flip_m], omc[flip_m]]))
-    ex_f = np.isin(fc, touched) | np.isin(ofc, touched)
-    ex_m = np.isin(mc, touched) | np.isin(omc, touched)
-    p, v = ctx.get_fluid(rep)
-    op, ov = o.get_fluid()
-    dp = np.abs(H.wrapped_diff(p, op, (L,) * 3)).max(axis=1)
-    dv = np.abs(v - ov).max(axis=1)
-    vs = float(np.abs(ov).max())
-    # one FP32 step from identical inputs: positions to a few ulp of L,
-    # velocities to the stated FP32 tolerance, for every particle of every
-    # cell that holds the same particles on both sides
-    bad = ((dp > 1e-6 * L) | (dv > H.FP32_VEL_RTOL * vs)) & ~ex_f
-    # a gamma acceptance test within FP32 rounding of its threshold (about
-    # 1e-7 per cell) would change one whole cell: at most one such cell
-    bad_cells = np.unique(ofc[bad])
-    assert len(bad_cells) <= 1, (len(bad_cells), dp[bad].max(), dv[bad].max())
-    mp, mv, _ = ctx.get_monomers(rep)
-    omp, omv, _ = o.get_monomers()
-    keep = ~ex_m
-    assert np.abs(H.wrapped_diff(mp, omp, (L,) * 3)[keep]).max(initial=0.0) < 1e-4
-    assert np.abs(mv - omv)[keep].max(initial=0.0) < 1e-3
-    assert abs(ctx.temperature(rep) - o.temperature()) < 1e-4
-    assert ctx.delrx(rep) == o.delrx
-    return n_flip
-
-
-def _resync(ctx, o, rep):
-    # the oracle continues from the FP32 state (exact in FP64), so each cycle
-    # is compared on its own
-    p, v = ctx.get_fluid(rep)
-    o.set_fluid(p, v)
-    mp, mv, mf = ctx.get_monomers(rep)
-    o.set_monomers(mp, mv, mf)
-
-
 def test_fp32_config1_tracks_f32_uniform_oracle():
     L, shear = 20, 0.05
     star, fpos, fvel = _config1_system(seed=4)
@@ -232,13 +184,13 @@ def test_fp32_config1_tracks_f32_uniform_oracle():
     flips = 0
     with H.context_for(star, fpos, fvel, L, 1.0, shear, N_SUB, **kw) as ctx:
         for c in range(5):
-            _resync(ctx, o, 0)
+            H.resync_oracle(ctx, o, 0)
             ctx.cycles(1)
             ctx.synchronize()
             ctx.raise_on_device_error()
             o.run(1 + N_SUB * c, N_SUB, H_MPC, True)
             assert o.error() == 0
-            flips += _fp32_cycle_check(ctx, o, 0, L)
+            flips += H.fp32_cycle_check(ctx, o, 0, L)
     assert flips <= 20
 
 
@@ -249,14 +201,14 @@ def test_fp32_largest_batched_replicas_track_f32_uniform_oracles():
     with built.ctx as ctx:
         for c in range(2):
             for k, o in enumerate(oracles):
-                _resync(ctx, o, k)
+                H.resync_oracle(ctx, o, k)
             ctx.cycles(1)
             ctx.synchronize()
             ctx.raise_on_device_error()
             for k, (o, s) in enumerate(zip(oracles, specs)):
                 o.run(1 + N_SUB * c, N_SUB, H_MPC, True)
                 assert o.error() == 0
-                _fp32_cycle_check(ctx, o, k, s.L)
+                H.fp32_cycle_check(ctx, o, k, s.L)
 
 
 # ------------------------------------------------------ a very full cell

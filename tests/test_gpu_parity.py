@@ -765,3 +765,73 @@ def test_fp64_wraps_bitwise_at_the_faces(L, shear):
             np.testing.assert_array_equal(fc, ofc)
             H.close64(v, ov)
             assert ctx.delrx(0) == o.delrx
+
+
+def test_fp32_predicted_keys_stale_after_host_changes():
+    # FP32 graph cycles predict the next collision's solvent keys in the
+    # collide; a host change of the solvent between calls must make the next
+    # cycle bin afresh. Context b runs 3 cycles, gets a new solvent state for
+    # replica 0, runs 3 more; context c starts from exactly that state (same
+    # counters, delrx, other replica) and runs 3: the same bits.
+    rng = np.random.default_rng(17)
+    reps, states = [], []
+    for k, L in enumerate((9, 12)):
+        fp, fv = system.uniform_fluid((L, L, L), 10, 1.0, rng)
+        reps.append(dict(L=(L, L, L), n_fluid=len(fp), kT=1.0, shear=0.05 * (k + 1), h=0.1,
+                         seed=70 + k))
+        states.append((fp, fv))
+    new0 = system.uniform_fluid((9, 9, 9), 10, 1.0, rng)
+    kw = dict(precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=1, strict_cells=0)
+    with capi.Context(reps, **kw) as b, capi.Context(reps, **kw) as c:
+        for k, (fp, fv) in enumerate(states):
+            b.set_fluid(k, fp, fv)
+        b.cycles(3)
+        b.set_fluid(0, *new0)
+        mid1 = b.get_fluid(1)
+        c.set_fluid(0, *new0)
+        c.set_fluid(1, *mid1)
+        for k in range(2):
+            c.set_delrx(k, b.delrx(k))
+        c.set_collision_counter(3)
+        b.cycles(3)
+        c.cycles(3)
+        b.raise_on_device_error()
+        c.raise_on_device_error()
+        for k in range(2):
+            for x, y in zip(b.get_fluid(k), c.get_fluid(k)):
+                np.testing.assert_array_equal(x, y)
+
+
+def test_fp32_prediction_with_recentring_in_one_replica():
+    # two boxes in one context, graph cycles against call-by-call cycles (which
+    # always bin afresh): replica 0's star sits at the box face so
+    # MPC::check_bounds recentres it (its predicted keys are dropped), replica
+    # 1's does not (its predicted keys are used) -- the same bits for both
+    L, su, h = 10, 10, 0.1
+    systems = [H.small_star_system(L=L, shear=0.1, seed=5), H.small_star_system(L=L, shear=0.05, seed=6)]
+    systems[0][0].pos[:] += 2.6
+    reps = [dict(L=(L,) * 3, n_fluid=len(fp), n_mono=st.n, mol0_size=st.n, kT=1.0, shear=sh,
+                 h=h, md_dt=0.01, seed=9 + k)
+            for k, ((st, fp, fv), sh) in enumerate(zip(systems, (0.1, 0.05)))]
+    kw = dict(precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=su, strict_cells=0,
+              mono_bin=capi.MONOBIN_WRAPPED, delrx_mode=capi.DELRX_PHYSICAL)
+    with capi.Context(reps, **kw) as a, capi.Context(reps, **kw) as b:
+        for ctx in (a, b):
+            for k, (st, fp, fv) in enumerate(systems):
+                ctx.set_fluid(k, fp, fv)
+                ctx.set_monomers(k, st.pos, st.vel, np.zeros_like(st.pos), np.full(st.n, st.mass),
+                                 st.amphi, st.anchor)
+                ctx.set_bonds(k, st.bond_src, st.bond_dst)
+            ctx.init_md()
+        for t in range(1, 4 * su + 1):
+            a.md_substeps(1)
+            a.mpc_step(t, h)
+        b.cycles(4)
+        b.synchronize()
+        a.raise_on_device_error()
+        b.raise_on_device_error()
+        for k in range(2):
+            for x, y in zip(b.get_fluid(k), a.get_fluid(k)):
+                np.testing.assert_array_equal(x, y)
+            for x, y in zip(b.get_monomers(k), a.get_monomers(k)):
+                np.testing.assert_array_equal(x, y)
