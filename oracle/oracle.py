@@ -295,6 +295,11 @@ class RefSystem:
             "ref_observables": [P, P],
             "ref_velocity_profile": [P, C.c_double, P, C.c_int, P, C.c_int],
             "ref_shift_arg_order": [P], "rand_tape_enable": [C.c_int], "rand_tape_clear": [],
+            "ref_fourier_start": [P, C.c_uint, C.c_double, C.c_double],
+            "ref_fourier_sample": [P], "ref_fourier_dump": [P, P, P, P],
+            "ref_vacf_start": [P, C.c_uint, C.c_double], "ref_vacf_sample": [P],
+            "ref_vacf_dump": [P, P, P],
+            "ref_make_lowe_andersen": [P, C.c_double, C.c_double, C.c_double, C.c_double],
             "rand_tape_copy": [P, P, C.c_long], "rand_tape_reseed": [C.c_ulonglong],
         }.items():
             getattr(lib, name).argtypes = args
@@ -365,6 +370,10 @@ class RefSystem:
     def make_andersen(self, dt, T, nu):
         """AndersenStochastic{box, dt, T, nu} as the propagating thermostat."""
         self.lib.ref_make_andersen(self.h, dt, T, nu)
+
+    def make_lowe_andersen(self, dt, T, nu, r):
+        """Lowe_Andersen{box, dt, T, nu, r} as the propagating thermostat."""
+        self.lib.ref_make_lowe_andersen(self.h, dt, T, nu, r)
 
     def mpc_initialize(self):
         self.lib.ref_mpc_initialize(self.h)
@@ -451,6 +460,36 @@ class RefSystem:
         out = np.zeros(10)
         self.lib.ref_gyration(self.h, _p(out))
         return out
+
+    # analyses ----------------------------------------------------------------
+    def fourier_start(self, entries, dt, L):
+        self._fourier_entries = int(entries)
+        self.lib.ref_fourier_start(self.h, int(entries), float(dt), float(L))
+
+    def fourier_sample(self):
+        self.lib.ref_fourier_sample(self.h)
+
+    def fourier_dump(self):
+        """(last sample's modes (3, 3) complex, Autocorrelation (3, entries), counter)."""
+        m = np.zeros(18)
+        acf = np.zeros(3 * self._fourier_entries)
+        n = C.c_uint()
+        self.lib.ref_fourier_dump(self.h, _p(m), _p(acf), C.byref(n))
+        return (m[0::2] + 1j * m[1::2]).reshape(3, 3), acf.reshape(3, -1), n.value
+
+    def vacf_start(self, entries, dt):
+        self._vacf_entries = int(entries)
+        self.lib.ref_vacf_start(self.h, int(entries), float(dt))
+
+    def vacf_sample(self):
+        self.lib.ref_vacf_sample(self.h)
+
+    def vacf_dump(self):
+        """(Autocorrelation summed over particles per lag, counter)."""
+        s = np.zeros(self._vacf_entries)
+        n = C.c_uint()
+        self.lib.ref_vacf_dump(self.h, _p(s), C.byref(n))
+        return s, n.value
 
     # tape ------------------------------------------------------------------
     def tape_start(self):

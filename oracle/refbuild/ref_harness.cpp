@@ -15,7 +15,10 @@
 #include "Box.h"
 #include "MPC.h"
 #include "Andersen_stochastic.h"
+#include "Fourier_Autocorr.h"
+#include "Lowe_Andersen.h"
 #include "Thermostat_None.h"
+#include "Vel_Autocorr_Fluid.h"
 #include "Velocity_x.h"
 #include "rand_tape.h"
 
@@ -32,12 +35,49 @@ class HarnessMPC : public MPC {
   void set_delrx(double d) { delrx = d; }
 };
 
+// The reference's solvent analyses (Analysis/Fourier_Autocorr.h,
+// Analysis/Vel_Autocorr_Fluid.h) with their protected sums read out.
+class HarnessFourier : public Fourier_Autocorr {
+ public:
+  using Fourier_Autocorr::Fourier_Autocorr;
+  // modes18: the last sample's three modes (x, y, z components, re/im
+  // interleaved); acf[3 * Entries]: Autocorrelation; counter: calculations
+  void dump(double* modes18, double* acf, unsigned* counter) const {
+    for (int j = 0; j < 3; ++j)
+      for (int d = 0; d < 3; ++d) {
+        modes18[6 * j + 2 * d] = Velocity_Fourier[j](d).real();
+        modes18[6 * j + 2 * d + 1] = Velocity_Fourier[j](d).imag();
+      }
+    for (int i = 0; i < 3; ++i)
+      for (unsigned e = 0; e < Entries; ++e)
+        acf[i * Entries + e] = static_cast<double>(Autocorrelation[i][e]);
+    *counter = Counter;
+  }
+};
+
+class HarnessVacf : public Vel_Autocorr_Fluid {
+ public:
+  using Vel_Autocorr_Fluid::Vel_Autocorr_Fluid;
+  // lag_sums[Entries]: Autocorrelation summed over particles (long double sums)
+  void dump(double* lag_sums, unsigned* counter) const {
+    for (unsigned e = 0; e < Entries; ++e) {
+      long double s = 0.0L;
+      for (unsigned i = 0; i < NumberOfParticles; ++i) s += Autocorrelation[i][e];
+      lag_sums[e] = static_cast<double>(s);
+    }
+    *counter = Counter;
+  }
+};
+
 struct RefSys {
   Box* box = nullptr;
   HarnessMPC* mpc = nullptr;
   Thermostat_None* thermo = nullptr;
   AndersenStochastic* andersen = nullptr;
+  Lowe_Andersen* lowe = nullptr;
   Thermostat* active = nullptr;  // the one propagate() drives
+  HarnessFourier* fourier = nullptr;
+  HarnessVacf* vacf = nullptr;
 };
 
 int g_probe_counter = 0;
@@ -56,6 +96,9 @@ RefSys* ref_create(int Lx, int Ly, int Lz, double T, double lambda, int Nc, doub
 }
 
 void ref_destroy(RefSys* s) {
+  delete s->lowe;
+  delete s->fourier;
+  delete s->vacf;
   delete s->thermo;
   delete s->andersen;
   delete s->mpc;
@@ -83,6 +126,15 @@ void ref_make_andersen(RefSys* s, double dt, double T, double nu) {
   delete s->andersen;
   s->andersen = new AndersenStochastic{*s->box, dt, T, nu};
   s->active = s->andersen;
+}
+
+// Lowe_Andersen{box, dt, T, nu, r} (the MPC-off integrator star-polymers.cpp:388
+// and gaussian_chain.cpp:382 construct with nu = 20, r = 1.5) as the
+// propagating thermostat.
+void ref_make_lowe_andersen(RefSys* s, double dt, double T, double nu, double r) {
+  delete s->lowe;
+  s->lowe = new Lowe_Andersen{*s->box, dt, T, nu, r};
+  s->active = s->lowe;
 }
 
 void ref_mpc_initialize(RefSys* s) { s->mpc->initialize(); }
@@ -285,6 +337,23 @@ void ref_velocity_profile(RefSys* s, double width, double* x_out, int n_x, doubl
   vx.dump_x(width, s->box->BoxSize[0], x_out, n_x);
   vx.dump_y(width, s->box->BoxSize[1], y_out, n_y);
 }
+
+// Fourier_Autocorr / Vel_Autocorr_Fluid over every solvent particle, applied
+// through MPC::operator() (MPC.h:110-115) once per sample.
+void ref_fourier_start(RefSys* s, unsigned entries, double dt, double L) {
+  delete s->fourier;
+  s->fourier = new HarnessFourier(static_cast<unsigned>(s->mpc->Fluid.size()), entries, dt, L);
+}
+void ref_fourier_sample(RefSys* s) { (*s->mpc)(*s->fourier); }
+void ref_fourier_dump(RefSys* s, double* modes18, double* acf, unsigned* counter) {
+  s->fourier->dump(modes18, acf, counter);
+}
+void ref_vacf_start(RefSys* s, unsigned entries, double dt) {
+  delete s->vacf;
+  s->vacf = new HarnessVacf(static_cast<unsigned>(s->mpc->Fluid.size()), entries, dt);
+}
+void ref_vacf_sample(RefSys* s) { (*s->mpc)(*s->vacf); }
+void ref_vacf_dump(RefSys* s, double* lag_sums, unsigned* counter) { s->vacf->dump(lag_sums, counter); }
 
 // Runs the star-polymers.cpp loop body (lines 466/530 then 534) for
 // t = t0 .. t0+n-1 without output; used to time the reference.

@@ -68,6 +68,11 @@ SCENARIOS = {
     "andersen_m1_L12": dict(L=(12, 12, 12), n_c=1, kT=0.8, shear=0.0, step_update=1, h=0.1,
                             md_dt=0.005, lam=1.0, star=dict(A=2, B=2, arms=3, mass=1.0),
                             n_loop=40, with_md=True, md_only=True, andersen_nu=5.0),
+    # the reference's solvent analyses, Fourier_Autocorr and Vel_Autocorr_Fluid
+    # over every solvent particle, sampled after every collision of a sheared
+    # solvent (windows of 3 and 4 samples)
+    "analysis_L6": dict(L=(6, 6, 6), n_c=5, kT=1.0, shear=0.2, step_update=1, h=0.1,
+                        star=None, n_loop=9, with_md=False, analysis=(3, 4)),
 }
 
 
@@ -110,6 +115,10 @@ def run_scenario(name: str, sc: dict) -> dict:
     obs, prof_x, prof_y = [], [], []
     m_pos, m_vel, m_frc, delrx, epots = [], [], [], [], []
     and_start, and_idx, and_vel = [0], [], []
+    modes = []
+    if "analysis" in sc:
+        ref.fourier_start(sc["analysis"][0], sc["h"], ref.L[0])
+        ref.vacf_start(sc["analysis"][1], sc["h"])
     for t in range(sc["n_loop"]):
         if st and sc["with_md"]:
             if "andersen_nu" in sc:
@@ -137,6 +146,10 @@ def run_scenario(name: str, sc: dict) -> dict:
                 temps.append(ref.temperature())
                 fc, mc = ref.cell_index()
                 fl_cell.append(fc); mo_cell.append(mc)
+                if "analysis" in sc:
+                    ref.fourier_sample()
+                    modes.append(ref.fourier_dump()[0])
+                    ref.vacf_sample()
                 if st:
                     # output-step observables (star-polymers.cpp:467-473, 483)
                     obs.append(ref.observables())
@@ -167,6 +180,12 @@ def run_scenario(name: str, sc: dict) -> dict:
     if st:
         out.update(mono_pos=np.array(m_pos), mono_vel=np.array(m_vel), mono_force=np.array(m_frc),
                    gyration=ref.gyration())
+    if "analysis" in sc:
+        _, acf, n_f = ref.fourier_dump()
+        sums, n_v = ref.vacf_dump()
+        out.update(fourier_entries=sc["analysis"][0], fourier_modes=np.array(modes),
+                   fourier_acf=acf, fourier_counter=n_f, vacf_entries=sc["analysis"][1],
+                   vacf_lag_sums=sums, vacf_counter=n_v)
     return out
 
 

@@ -109,3 +109,18 @@ def test_recentre_fixture_exercises_check_bounds(golden_dir):
     fx = gr.load(os.path.join(golden_dir, "recentre_L12.npz"))
     assert np.abs(fx["mono_pos0"].mean(axis=0)).max() > 1.0
     assert np.abs(fx["mono_pos"][0].mean(axis=0)).max() < 0.1
+
+
+def test_fourier_bookkeeping_matches_reference(golden_dir):
+    # The host side of the Fourier autocorrelation (the window of samples and
+    # the sums, starpolymersmd_gb300/analysis.py) fed the reference's own
+    # modes gives the reference's Autocorrelation and calculation count
+    # (Fourier_Autocorr.h:58-100).
+    from starpolymersmd_gb300 import analysis
+    fx = gr.load(os.path.join(golden_dir, "analysis_L6.npz"))
+    fa = analysis.FourierAutocorr(int(fx["fourier_entries"]), float(fx["h"]))
+    for m in fx["fourier_modes"]:
+        fa.push(m)
+    assert fa.counter == int(fx["fourier_counter"])
+    _, acf = fa.result()
+    np.testing.assert_allclose(acf.T * fa.counter, fx["fourier_acf"], rtol=1e-13, atol=1e-18)
