@@ -52,3 +52,26 @@ def test_reference_drivers_build_against_dropins(tmp_path):
         # ... and resolve them from the in-tree libsmpc
         ldd = subprocess.run(["ldd", str(path)], capture_output=True, text=True).stdout
         assert os.path.realpath(lib) in ldd or os.path.basename(lib) in ldd
+
+
+def test_call_sequence_program_builds(tmp_path):
+    # tests/dropin_sequence.cpp (the drop-in's call sequence, run against the
+    # reference's fixtures by the GPU tests) builds from include/smpc.h and
+    # links to the in-tree libsmpc, calling what the drop-in calls
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from starpolymersmd_gb300 import build as B
+    lib = B.build()
+    libdir = os.path.dirname(lib)
+    exe = str(tmp_path / "dropin_sequence")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "dropin_sequence.cpp"), "-L", libdir, "-lsmpc",
+                    "-Wl,-rpath," + libdir, "-o", exe], check=True, timeout=300)
+    und = subprocess.run(["nm", "-u", exe], capture_output=True, text=True).stdout
+    for sym in ("smpc_create", "smpc_set_fluid", "smpc_set_monomers", "smpc_set_bonds",
+                "smpc_init_md", "smpc_md_substeps", "smpc_epot", "smpc_set_delrx", "smpc_mpc_bin",
+                "smpc_cell_counts", "smpc_mpc_collide", "smpc_error_word", "smpc_get_fluid",
+                "smpc_cell_members", "smpc_get_monomer_state_all", "smpc_temperature"):
+        assert sym in und, sym
+    order = subprocess.run([exe, "--shift-order"], capture_output=True, text=True, check=True)
+    assert sorted(int(x) for x in order.stdout.split()) == [0, 1, 2]

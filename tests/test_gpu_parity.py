@@ -767,12 +767,12 @@ def test_fp64_wraps_bitwise_at_the_faces(L, shear):
             assert ctx.delrx(0) == o.delrx
 
 
-def test_fp32_predicted_keys_stale_after_host_changes():
-    # FP32 graph cycles predict the next collision's solvent keys in the
-    # collide; a host change of the solvent between calls must make the next
-    # cycle bin afresh. Context b runs 3 cycles, gets a new solvent state for
-    # replica 0, runs 3 more; context c starts from exactly that state (same
-    # counters, delrx, other replica) and runs 3: the same bits.
+def test_fp32_graph_cycles_after_host_solvent_change():
+    # FP32 graph cycles must see a host change of the solvent between calls
+    # (the captured graph reads the device buffers the upload wrote). Context
+    # b runs 3 cycles, gets a new solvent state for replica 0, runs 3 more;
+    # context c starts from exactly that state (same counters, delrx, other
+    # replica) and runs 3: the same bits.
     rng = np.random.default_rng(17)
     reps, states = [], []
     for k, L in enumerate((9, 12)):
@@ -802,11 +802,10 @@ def test_fp32_predicted_keys_stale_after_host_changes():
                 np.testing.assert_array_equal(x, y)
 
 
-def test_fp32_prediction_with_recentring_in_one_replica():
-    # two boxes in one context, graph cycles against call-by-call cycles (which
-    # always bin afresh): replica 0's star sits at the box face so
-    # MPC::check_bounds recentres it (its predicted keys are dropped), replica
-    # 1's does not (its predicted keys are used) -- the same bits for both
+def test_fp32_graph_cycles_with_recentring_in_one_replica():
+    # two boxes in one context, graph cycles against call-by-call cycles:
+    # replica 0's star sits at the box face so MPC::check_bounds recentres it,
+    # replica 1's does not -- the same bits for both
     L, su, h = 10, 10, 0.1
     systems = [H.small_star_system(L=L, shear=0.1, seed=5), H.small_star_system(L=L, shear=0.05, seed=6)]
     systems[0][0].pos[:] += 2.6
