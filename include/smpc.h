@@ -195,9 +195,11 @@ int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, d
  * cluster of SMs; md = 1 keeps one CTA per replica there instead. */
 int smpc_set_variants(smpc_ctx* ctx, int bin, int collide, int md);
 int smpc_get_variants(const smpc_ctx* ctx, int* bin, int* collide, int* md);
-/* Times every variant of each fast-path kernel over `cycles` live cycles
- * (CUDA events on the context stream), keeps the fastest and writes a JSON
- * report (variant -> ms per cycle, chosen). Advances the simulation. */
+/* Times every variant of each fast-path kernel over `cycles` cycles of the
+ * context's own workload (CUDA events on the context stream), keeps the
+ * fastest and writes a JSON report (variant -> ms per cycle, chosen). The
+ * state is saved to host memory before the trials (as smpc_checkpoint_save)
+ * and restored after them, so the simulation does not advance. */
 int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len);
 /* smpc_cycles bracketed by CUDA events on the context stream (ms). */
 int smpc_time_cycles(smpc_ctx* ctx, int n, double* total_ms);

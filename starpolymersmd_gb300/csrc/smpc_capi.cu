@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <new>
 #include <vector>
 
 #include "../../include/smpc.h"
@@ -1554,6 +1555,18 @@ int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len) {
   cudaSetDevice(ctx->device);
   std::string js = "{";
   if (fast_path(ctx)) {
+    // the trial cycles run on the live state: keep a full-precision copy of
+    // it and put it back afterwards, so tuning leaves the trajectory where it was
+    uint64_t snap_bytes = 0;
+    if (int rc = smpc_checkpoint_size(ctx, &snap_bytes)) return rc;
+    std::vector<unsigned char> snap;
+    try {
+      snap.resize(snap_bytes);
+    } catch (const std::bad_alloc&) {
+      return fail(ctx, SMPC_E_ARG, "no host memory for the autotuner's state copy");
+    }
+    if (int rc = smpc_checkpoint_save(ctx, snap.data(), snap_bytes)) return rc;
+    const int var0[3] = {ctx->var_bin, ctx->var_col, ctx->var_md};
     struct Cat {
       const char* name;
       int phase;
@@ -1572,7 +1585,14 @@ int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len) {
       for (int v = 0; v < cats[c].count; ++v) {
         *cats[c].var = v;
         drop_graphs(ctx);
-        if (int rc = run_profiled(ctx, cycles, ph, &tot)) return rc;
+        if (int rc = run_profiled(ctx, cycles, ph, &tot)) {
+          ctx->var_bin = var0[0];
+          ctx->var_col = var0[1];
+          ctx->var_md = var0[2];
+          drop_graphs(ctx);
+          smpc_checkpoint_load(ctx, snap.data(), snap_bytes);
+          return rc;
+        }
         const double ms = ph[cats[c].phase] / cycles;
         char buf[128];
         std::snprintf(buf, sizeof(buf), "%s\"%s\": %.5f", v ? ", " : "", cats[c].label(v), ms);
@@ -1587,6 +1607,8 @@ int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len) {
       js += std::string("}, \"chosen\": \"") + cats[c].label(best) + "\", \"index\": " +
             std::to_string(best) + "}";
     }
+    if (int rc = smpc_checkpoint_load(ctx, snap.data(), snap_bytes)) return rc;
+    drop_graphs(ctx);
   }
   js += "}";
   if (report && report_len > 0) {

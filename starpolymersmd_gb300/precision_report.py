@@ -27,6 +27,11 @@ object.
 
     python -m starpolymersmd_gb300.precision_report --workload large_box_200 \
         --cycles 200 --every 20
+    python -m starpolymersmd_gb300.precision_report --workload single_star_50 \
+        --shear 0,0.01,0.05,0.2 --cycles 10000 --every 100     # the shear sweep
+
+Each cycle stretch between samples is timed with CUDA events on the
+context's stream (ms_per_cycle, sampling excluded).
 """
 from __future__ import annotations
 
@@ -64,16 +69,18 @@ def _sample(ctx, built):
     }
 
 
-def _run(workload, precision, cycles, every):
+def _run(workload, precision, cycles, every, shear=None):
     t0 = time.perf_counter()
-    built = W.WORKLOADS[workload](precision=precision)
+    kw = {} if shear is None else {"shear": shear}
+    built = W.WORKLOADS[workload](precision=precision, **kw)
     ctx = built.ctx
     n = built.particles
     ctx.synchronize()
     p0 = _momentum_yz(ctx, built)
     samples = []
+    cycle_ms = 0.0
     for _ in range(cycles // every):
-        ctx.cycles(every)
+        cycle_ms += ctx.time_cycles(every)  # CUDA events on the context stream
         samples.append(_sample(ctx, built))
     ctx.raise_on_device_error()
     kT = built.specs[0].kT
@@ -86,6 +93,7 @@ def _run(workload, precision, cycles, every):
         "gyration": np.array([s["gyration"] for s in samples]),
         "kT": kT,
         "seconds": time.perf_counter() - t0,
+        "ms_per_cycle": cycle_ms / max(1, (cycles // every) * every),
     }
 
 
@@ -96,11 +104,14 @@ def _mean_err(x):
     return m, err
 
 
-def report(workload="large_box_200", cycles=200, every=20):
-    runs = {name: _run(workload, prec, cycles, every)
+def report(workload="large_box_200", cycles=200, every=20, shear=None):
+    runs = {name: _run(workload, prec, cycles, every, shear)
             for name, prec in (("fp32", capi.FP32), ("fp64", capi.FP64))}
     out = {"workload": workload, "cycles": cycles, "sample_every": every,
-           "seconds": {k: round(v["seconds"], 1) for k, v in runs.items()}}
+           "seconds": {k: round(v["seconds"], 1) for k, v in runs.items()},
+           "ms_per_cycle": {k: round(v["ms_per_cycle"], 4) for k, v in runs.items()}}
+    if shear is not None:
+        out["shear"] = shear
     for key in ("temperature", "temperature_kinetic", "p_xy", "gyration"):
         m32, e32 = _mean_err(runs["fp32"][key])
         m64, e64 = _mean_err(runs["fp64"][key])
@@ -122,8 +133,14 @@ def main():
     ap.add_argument("--workload", default="large_box_200", choices=sorted(W.WORKLOADS))
     ap.add_argument("--cycles", type=int, default=200)
     ap.add_argument("--every", type=int, default=20)
+    ap.add_argument("--shear", default=None,
+                    help="comma-separated shear rates: one report per rate (a sweep)")
     a = ap.parse_args()
-    print(json.dumps(report(a.workload, a.cycles, a.every)), flush=True)
+    if a.shear is None:
+        print(json.dumps(report(a.workload, a.cycles, a.every)), flush=True)
+    else:
+        for g in (float(x) for x in a.shear.split(",")):
+            print(json.dumps(report(a.workload, a.cycles, a.every, g)), flush=True)
 
 
 if __name__ == "__main__":

@@ -64,7 +64,8 @@ def test_call_sequence_program_builds(tmp_path):
     lib = B.build()
     libdir = os.path.dirname(lib)
     exe = str(tmp_path / "dropin_sequence")
-    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-ffp-contract=off",
+                    "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "dropin_sequence.cpp"), "-L", libdir, "-lsmpc",
                     "-Wl,-rpath," + libdir, "-o", exe], check=True, timeout=300)
     und = subprocess.run(["nm", "-u", exe], capture_output=True, text=True).stdout

@@ -40,7 +40,11 @@ def program(tmp_path_factory):
     capi.load()  # the library must have been built
     libdir = os.path.dirname(capi.LIB_PATH)
     exe = str(tmp_path_factory.mktemp("dropin") / "dropin_sequence")
-    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+    # -ffp-contract=off as in the drop-in's Makefile: g++ on aarch64 would
+    # otherwise fuse the delrx advance into an FMA and round it differently
+    # from the reference built on x86
+    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-ffp-contract=off",
+                    "-I", os.path.join(ROOT, "include"),
                     os.path.join(HERE, "dropin_sequence.cpp"), "-L", libdir, "-lsmpc",
                     "-Wl,-rpath," + libdir, "-o", exe], check=True)
     return exe

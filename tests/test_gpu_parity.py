@@ -375,6 +375,45 @@ def test_autotune_reports_and_keeps_a_variant():
         assert abs(ctx.temperature(0) - 1.0) < 0.2
 
 
+def test_autotune_leaves_the_trajectory_where_it_was():
+    # the autotuner's trial cycles run on a saved copy of the state: a context
+    # that tunes between two stretches of cycles ends with the same bits as
+    # one that only switches to the chosen variants at the same point
+    from starpolymersmd_gb300 import system, workloads as W
+    specs = _batch_specs()
+    descs, states = [], []
+    for s in specs:
+        rng = np.random.default_rng(700 + s.seed)
+        st = system.make_star(s.arms, s.n_arm, s.solvophobic_fraction, s.mono_mass, s.kT, rng,
+                              bond=0.97)
+        descs.append(W.replica_desc(s, st))
+        states.append((st, system.uniform_fluid((s.L,) * 3, s.n_c, s.kT, rng)))
+    kw = dict(precision=capi.FP32, rng=capi.RNG_PHILOX, mono_bin=capi.MONOBIN_WRAPPED,
+              delrx_mode=capi.DELRX_PHYSICAL, step_update=W.N_SUB, max_neighbors=W.MAX_NB,
+              strict_cells=0)
+    with capi.Context(descs, **kw) as a, capi.Context(descs, **kw) as b:
+        for ctx in (a, b):
+            for k, (st, (fp, fv)) in enumerate(states):
+                ctx.set_fluid(k, fp, fv)
+                ctx.set_monomers(k, st.pos, st.vel, np.zeros_like(st.pos),
+                                 np.full(st.n, st.mass), st.amphi, st.anchor)
+                ctx.set_bonds(k, st.bond_src, st.bond_dst)
+            ctx.init_md()
+            ctx.cycles(3)
+        a.autotune(2)
+        b.set_variants(*a.get_variants())
+        a.cycles(3)
+        b.cycles(3)
+        a.raise_on_device_error()
+        b.raise_on_device_error()
+        for k in range(len(specs)):
+            for x, y in zip(a.get_fluid(k), b.get_fluid(k)):
+                np.testing.assert_array_equal(x, y)
+            for x, y in zip(a.get_monomers(k), b.get_monomers(k)):
+                np.testing.assert_array_equal(x, y)
+            assert a.delrx(k) == b.delrx(k)
+
+
 @pytest.mark.parametrize("name", ["star_mpc_L12", "mpc_shear_L6"])
 def test_two_phase_step_replays_reference(golden_dir, name):
     # smpc_mpc_bin with the reference's grid shift, occupancies read back
