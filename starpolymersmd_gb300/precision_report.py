@@ -22,8 +22,12 @@ cycles each run reports, with FP64 reductions on the device or on the host:
 * the stars' radius-of-gyration tensor (mean over stars).
 
 The report gives, per quantity, the time averages of both runs, their
-difference and its standard error from the spread of the samples, as one JSON
-object.
+difference and its standard error from ten block averages of each run, as one
+JSON object. In the one-star workloads MPC::check_bounds recentres the world
+on the star (MPC.cpp:183-188), subtracting the star's velocity from every
+particle; the total momentum then changes with every recentring in both
+precisions, so its drift measures precision only in the periodic workloads
+(no recentring).
 
     python -m starpolymersmd_gb300.precision_report --workload large_box_200 \
         --cycles 200 --every 20
@@ -97,11 +101,21 @@ def _run(workload, precision, cycles, every, shear=None):
     }
 
 
+N_BLOCKS = 10
+
+
 def _mean_err(x):
+    """Mean and its standard error from N_BLOCKS block means: samples a few
+    hundred collisions apart are still correlated (a star's shape relaxes
+    slowly), so the spread of single samples would understate the error."""
     x = np.asarray(x, dtype=np.float64)
     m = x.mean(axis=0)
-    err = x.std(axis=0, ddof=1) / np.sqrt(len(x)) if len(x) > 1 else np.zeros_like(m)
-    return m, err
+    nb = min(N_BLOCKS, len(x))
+    if nb < 2:
+        return m, np.zeros_like(m)
+    per = len(x) // nb
+    blocks = x[: per * nb].reshape((nb, per) + x.shape[1:]).mean(axis=1)
+    return m, blocks.std(axis=0, ddof=1) / np.sqrt(nb)
 
 
 def report(workload="large_box_200", cycles=200, every=20, shear=None):

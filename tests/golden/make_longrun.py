@@ -1,5 +1,5 @@
 """Long-run statistics of config 1 from the reference compiled from its own
-sources (oracle/refbuild): the fixture tests/golden/longrun_config1.npz that
+sources (oracle/refbuild): the fixture tests/golden/longrun/longrun_config1.npz that
 tests/test_gpu_longrun.py compares the GPU paths with.
 
 System: the first benchmark configuration's star and solvent -- one star of
