@@ -355,6 +355,33 @@ __device__ __forceinline__ int md_bucket(int cx, int cy, int cz) {
          (MD_BUCKETS - 1);
 }
 
+// The hash chains are built with atomicExch, so each comes out in the order
+// the insertions happened to run, which differs between runs once a replica
+// spans several warps. Putting every chain in ascending bead order (one
+// thread per bucket, insertion sort of a short list) makes the Verlet lists,
+// and with them the force sums, the same bits in every run.
+__device__ __forceinline__ void md_sort_chains(int* s_head, int* s_next, int nt) {
+  for (int q = threadIdx.x; q < MD_BUCKETS; q += nt) {
+    int j = s_head[q];
+    if (j < 0 || s_next[j] < 0) continue;  // empty, or one bead
+    int sorted = -1;
+    while (j >= 0) {
+      const int nxt = s_next[j];
+      if (sorted < 0 || j < sorted) {
+        s_next[j] = sorted;
+        sorted = j;
+      } else {
+        int p = sorted;
+        while (s_next[p] >= 0 && s_next[p] < j) p = s_next[p];
+        s_next[j] = s_next[p];
+        s_next[p] = j;
+      }
+      j = nxt;
+    }
+    s_head[q] = sorted;
+  }
+}
+
 // The 512-thread lanes-per-bead shape is held to 64 registers so that two of
 // its blocks share an SM (the side-by-side MD launch shape).
 template <typename R, int NT, int MPT, int KMAX = 1>
@@ -479,6 +506,8 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
           }
         }
       }
+      __syncthreads();
+      md_sort_chains(s_head, s_next, NT);
       __syncthreads();
 #pragma unroll
       for (int k = 0; k < MPT; ++k) {
@@ -780,6 +809,8 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         s_ckey[j] = md_cell_key(cx, cy, cz);
         s_next[j] = atomicExch(&s_head[md_bucket(cx, cy, cz)], j);
       }
+      __syncthreads();
+      md_sort_chains(s_head, s_next, NT);
       __syncthreads();
       if (mine && lead) {
         const int cx = static_cast<int>(floor(x[0] * inv_rv));

@@ -252,8 +252,9 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
     float mmono = 0.0f;
     float big = 0.0f;  // largest fixed-point term (range check)
     if (j1 - j0 <= 1024) {
-      // at most 512 terms per lane: int32 split accumulators
-      int xh = 0, xl = 0, yh = 0, yl = 0, zh = 0, zl = 0, eh = 0, el = 0;
+      // at most 512 terms per lane: 32-bit split accumulators
+      uint32_t xh = 0, xl = 0, yh = 0, yl = 0, zh = 0, zl = 0, eh = 0, el = 0;
+      int terms = 0;
       for (int j = j0 + half; j < j1; j += 2) {
         float4 v, x;
         if (j < nloc) {
@@ -274,16 +275,17 @@ __device__ __forceinline__ void collide_cells_f32(const CollideF32Args& A, const
         fix32_add(my, yh, yl);
         fix32_add(mz, zh, zl);
         fix32_add(et, eh, el);
+        ++terms;
         if (__float_as_uint(x.w) & MONO_BIT) {
           mmono += v.w;
         } else {
           ++nsol;
         }
       }
-      px = fix32_join(xh, xl);
-      py = fix32_join(yh, yl);
-      pz = fix32_join(zh, zl);
-      e = fix32_join(eh, el);
+      px = fix32_join(xh, xl, terms);
+      py = fix32_join(yh, yl, terms);
+      pz = fix32_join(zh, zl, terms);
+      e = fix32_join(eh, el, terms);
     } else {
       for (int j = j0 + half; j < j1; j += 2) {
         float4 v, x;

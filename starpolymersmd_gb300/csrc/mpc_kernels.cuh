@@ -73,9 +73,13 @@ __device__ __forceinline__ void st_rec(R* st, size_t i, const R4<R>& x, const R4
   st4(st, 2 * i + 1, v);
 }
 
+// The slot's id travels in the .w word as a bit pattern, never as a number:
+// FP32 the word itself, FP64 the low half of the double (a zero or subnormal
+// value that no arithmetic ever reads). Reading it is an integer move, not a
+// conversion, which on GB300 would issue on the narrow FP64 pipe.
 __device__ __forceinline__ uint32_t slot_id(float w) { return __float_as_uint(w); }
 __device__ __forceinline__ uint32_t slot_id(double w) {
-  return w < 0.0 ? SLOT_EMPTY : static_cast<uint32_t>(w);
+  return static_cast<uint32_t>(__double_as_longlong(w));
 }
 template <typename R>
 __device__ __forceinline__ R make_slot_id(uint32_t id);
@@ -83,7 +87,7 @@ template <>
 __device__ __forceinline__ float make_slot_id<float>(uint32_t id) { return __uint_as_float(id); }
 template <>
 __device__ __forceinline__ double make_slot_id<double>(uint32_t id) {
-  return id == SLOT_EMPTY ? -1.0 : static_cast<double>(id);
+  return __longlong_as_double(static_cast<long long>(id));
 }
 
 // ------------------------------------------------------- box geometry
@@ -195,24 +199,62 @@ __device__ __forceinline__ double wrap_d(double x, double L, long long lo, long 
   if (ax >= half && ax < far) return bits < 0 ? r_add(x, L) : r_sub(x, L);
   return r_sub(x, r_mul(L, r_round(r_div(x, L))));
 }
+// The general case of le_wrap<double>, out of line: called only when a
+// coordinate is at or past L/2 (1 - 2^-50), so that its FP64 instructions run
+// for those particles only (inlined, the compiler predicates its short
+// branches and every warp issues them on the FP64 pipe). Everything goes by
+// value, so no caller's state has to live in memory.
+struct WrapD {
+  double x, y, z, vx;
+};
+struct WrapConstD {
+  double L[3];
+  long long lo[3], half[3], far[3];
+  double delrx, shear;
+  int shear_on;
+};
+static __device__ __noinline__ WrapD le_wrap_d_general(WrapD p, WrapConstD c) {
+  if (c.shear_on) {
+    const double cy = image_d(p.y, c.L[1], c.lo[1], c.half[1], c.far[1]);
+    p.x = wrap_d(p.x, c.L[0], c.lo[0], c.half[0], c.far[0]);
+    if (cy != 0.0) p.x = r_sub(p.x, r_mul(cy, c.delrx));
+    p.x = wrap_d(p.x, c.L[0], c.lo[0], c.half[0], c.far[0]);
+    if (cy != 0.0) {
+      p.y = r_sub(p.y, r_mul(c.L[1], cy));
+      p.vx = r_sub(p.vx, r_mul(r_mul(cy, c.shear), c.L[1]));
+    }
+    p.z = wrap_d(p.z, c.L[2], c.lo[2], c.half[2], c.far[2]);
+  } else {
+    p.x = wrap_d(p.x, c.L[0], c.lo[0], c.half[0], c.far[0]);
+    p.y = wrap_d(p.y, c.L[1], c.lo[1], c.half[1], c.far[1]);
+    p.z = wrap_d(p.z, c.L[2], c.lo[2], c.half[2], c.far[2]);
+  }
+  return p;
+}
 template <>
 __device__ __forceinline__ void le_wrap<double>(const Geo<double>& g, double& x, double& y,
                                                 double& z, double& vx) {
-  if (g.shear_on) {
-    const double cy = image_d(y, g.L[1], g.w_lo[1], g.w_half[1], g.w_far[1]);
-    x = wrap_d(x, g.L[0], g.w_lo[0], g.w_half[0], g.w_far[0]);
-    if (cy != 0.0) x = r_sub(x, r_mul(cy, g.delrx));
-    x = wrap_d(x, g.L[0], g.w_lo[0], g.w_half[0], g.w_far[0]);
-    if (cy != 0.0) {
-      y = r_sub(y, r_mul(g.L[1], cy));
-      vx = r_sub(vx, r_mul(r_mul(cy, g.shear), g.L[1]));
-    }
-    z = wrap_d(z, g.L[2], g.w_lo[2], g.w_half[2], g.w_far[2]);
-  } else {
-    x = wrap_d(x, g.L[0], g.w_lo[0], g.w_half[0], g.w_far[0]);
-    y = wrap_d(y, g.L[1], g.w_lo[1], g.w_half[1], g.w_far[1]);
-    z = wrap_d(z, g.L[2], g.w_lo[2], g.w_half[2], g.w_far[2]);
+  // below L/2 (1 - 2^-50) on every axis the formula changes nothing: no
+  // image in y, and every wrap_d returns its argument
+  const long long ax = __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll;
+  const long long ay = __double_as_longlong(y) & 0x7FFFFFFFFFFFFFFFll;
+  const long long az = __double_as_longlong(z) & 0x7FFFFFFFFFFFFFFFll;
+  if (ax < g.w_lo[0] && ay < g.w_lo[1] && az < g.w_lo[2]) return;
+  WrapConstD c;
+  for (int d = 0; d < 3; ++d) {
+    c.L[d] = g.L[d];
+    c.lo[d] = g.w_lo[d];
+    c.half[d] = g.w_half[d];
+    c.far[d] = g.w_far[d];
   }
+  c.delrx = g.delrx;
+  c.shear = g.shear;
+  c.shear_on = g.shear_on ? 1 : 0;
+  const WrapD r = le_wrap_d_general(WrapD{x, y, z, vx}, c);
+  x = r.x;
+  y = r.y;
+  z = r.z;
+  vx = r.vx;
 }
 
 // FP32 fast path: one conditional image shift per axis, exact (x - L is
@@ -714,9 +756,9 @@ struct Particle {
 };
 
 __device__ __forceinline__ float pack_src(float, uint32_t s) { return __uint_as_float(s); }
-__device__ __forceinline__ double pack_src(double, uint32_t s) { return static_cast<double>(s); }
+__device__ __forceinline__ double pack_src(double, uint32_t s) { return make_slot_id<double>(s); }
 __device__ __forceinline__ uint32_t unpack_src(float w) { return __float_as_uint(w); }
-__device__ __forceinline__ uint32_t unpack_src(double w) { return static_cast<uint32_t>(w); }
+__device__ __forceinline__ uint32_t unpack_src(double w) { return slot_id(w); }
 
 template <typename R>
 struct CollideCtx {
@@ -925,6 +967,60 @@ __device__ __forceinline__ void llt_solve3(const R A[3][3], const R b[3], R x[3]
   }
 }
 
+// Thermostat factor of one cell (MPC.cpp:284-291): sqrt(Gamma(1.5 (n - 1),
+// kT) / E) for cells of two or more particles, -1 (no thermostat) otherwise.
+template <typename R>
+__device__ __forceinline__ R cell_scale(uint32_t nn, R ekin, uint32_t cg, uint32_t cl, int rng,
+                                        const double* inj_gamma, unsigned long long seed,
+                                        unsigned long long step, R kT, ErrorState* err) {
+  constexpr bool kFP64 = std::is_same<R, double>::value;
+  if (nn < 2u) return R(-1);
+  R gv;
+  if (rng == RNG_INJECT) {
+    gv = static_cast<R>(inj_gamma[cg]);
+  } else {
+    bool ok = true;
+    const R shape = kFP64 ? static_cast<R>(1.5) * static_cast<R>(nn - 1u)
+                          : static_cast<R>(1.5f * i2f_small(static_cast<int>(nn - 1u)));
+    gv = philox_gamma<R>(seed, cl, step, shape, &ok) * kT;
+    if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
+  }
+  return (ekin > R(0)) ? r_sqrt(gv / ekin) : R(1);
+}
+
+// Rotation matrix of one cell about the random axis (MPC.cpp:244-257).
+template <typename R>
+__device__ __forceinline__ void cell_rotation(uint32_t cg, uint32_t cl, int rng,
+                                              const double* inj_uphi, const double* inj_utheta,
+                                              unsigned long long seed, unsigned long long step,
+                                              R rc, R rs, R (&M)[9]) {
+  R uphi, uth;
+  if (rng == RNG_INJECT) {
+    uphi = static_cast<R>(inj_uphi[cg]);
+    uth = static_cast<R>(inj_utheta[cg]);
+  } else {
+    const Uniform2<R> u = philox_uniforms<R>(seed, cl, step, 0u);
+    uphi = u.a;
+    uth = u.b;
+  }
+  const R two_pi = R(6.283185307179586476925286766559);
+  const R phi = two_pi * uphi;
+  const R theta = R(2) * (uth - R(0.5));
+  const R stt = r_sqrt(R(1) - theta * theta);
+  R sphi, cphi;
+  r_sincos(phi, &sphi, &cphi);
+  const R a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
+  M[0] = a0 * a0 + (R(1) - a0 * a0) * rc;
+  M[1] = a0 * a1 * (R(1) - rc) - a2 * rs;
+  M[2] = a0 * a2 * (R(1) - rc) + a1 * rs;
+  M[3] = a0 * a1 * (R(1) - rc) + a2 * rs;
+  M[4] = a1 * a1 + (R(1) - a1 * a1) * rc;
+  M[5] = a1 * a2 * (R(1) - rc) - a0 * rs;
+  M[6] = a0 * a2 * (R(1) - rc) - a1 * rs;
+  M[7] = a1 * a2 * (R(1) - rc) + a0 * rs;
+  M[8] = a2 * a2 + (R(1) - a2 * a2) * rc;
+}
+
 // One CTA per tile of <= CT cells of one replica.
 //  stage  : gather the tile's particles (perm -> 32-byte records, GU loads in
 //           flight per thread), recompute their collision-frame state, keep
@@ -1110,46 +1206,37 @@ __global__ void __launch_bounds__(NT) k_collide(
     const uint32_t nn = static_cast<uint32_t>(j1 - j0);
     R scale = R(-1);
     R M[9];
+    if (kFP64 && !amc) {
+      // FP64: the draws of each cell by one thread, in full warps. On the two
+      // lanes of a pair the gamma variate and the rotation take divergent
+      // paths, each at half the warp, and the narrow FP64 pipe issues every
+      // warp instruction for the whole warp.
+      if (half == 0 && live) {
+        s_cmv[3 * lc] = cm[0];
+        s_cmv[3 * lc + 1] = cm[1];
+        s_cmv[3 * lc + 2] = cm[2];
+        s_scale[lc] = ekin;
+      }
+      __syncthreads();
+      for (int c = threadIdx.x; c < nc; c += NT) {
+        const uint32_t cgc = C.c0 + c;
+        const uint32_t nnc = s_off[c + 1] - s_off[c];
+        R Mc[9];
+        const R sc = cell_scale<R>(nnc, s_scale[c], cgc, cgc - C.cbase, rng, inj_gamma, ri.seed,
+                                   C.dn.step, kT, err);
+        cell_rotation<R>(cgc, cgc - C.cbase, rng, inj_uphi, inj_utheta, ri.seed, C.dn.step, rc,
+                         rs, Mc);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) s_rot[9 * c + q] = Mc[q];
+        s_scale[c] = sc;
+      }
+      __syncthreads();
+      goto apply;
+    }
     if (half == 0) {
-      if (live && nn >= 2u) {
-        R gv;
-        if (rng == RNG_INJECT) {
-          gv = static_cast<R>(inj_gamma[cg]);
-        } else {
-          bool ok = true;
-          const R shape = kFP64 ? static_cast<R>(1.5) * static_cast<R>(nn - 1u)
-                                : static_cast<R>(1.5f * i2f_small(static_cast<int>(nn - 1u)));
-          gv = philox_gamma<R>(ri.seed, cl, C.dn.step, shape, &ok) * kT;
-          if (!ok) raise_error(err, ERR_GAMMA_ITERS, cg, nn);
-        }
-        scale = (ekin > R(0)) ? r_sqrt(gv / ekin) : R(1);
-      }
+      if (live) scale = cell_scale<R>(nn, ekin, cg, cl, rng, inj_gamma, ri.seed, C.dn.step, kT, err);
     } else if (live) {
-      R uphi, uth;
-      if (rng == RNG_INJECT) {
-        uphi = static_cast<R>(inj_uphi[cg]);
-        uth = static_cast<R>(inj_utheta[cg]);
-      } else {
-        const Uniform2<R> u = philox_uniforms<R>(ri.seed, cl, C.dn.step, 0u);
-        uphi = u.a;
-        uth = u.b;
-      }
-      const R two_pi = R(6.283185307179586476925286766559);
-      const R phi = two_pi * uphi;
-      const R theta = R(2) * (uth - R(0.5));
-      const R stt = r_sqrt(R(1) - theta * theta);
-      R sphi, cphi;
-      r_sincos(phi, &sphi, &cphi);
-      const R a0 = stt * cphi, a1 = stt * sphi, a2 = theta;
-      M[0] = a0 * a0 + (R(1) - a0 * a0) * rc;
-      M[1] = a0 * a1 * (R(1) - rc) - a2 * rs;
-      M[2] = a0 * a2 * (R(1) - rc) + a1 * rs;
-      M[3] = a0 * a1 * (R(1) - rc) + a2 * rs;
-      M[4] = a1 * a1 + (R(1) - a1 * a1) * rc;
-      M[5] = a1 * a2 * (R(1) - rc) - a0 * rs;
-      M[6] = a0 * a2 * (R(1) - rc) - a1 * rs;
-      M[7] = a1 * a2 * (R(1) - rc) + a0 * rs;
-      M[8] = a2 * a2 + (R(1) - a2 * a2) * rc;
+      cell_rotation<R>(cg, cl, rng, inj_uphi, inj_utheta, ri.seed, C.dn.step, rc, rs, M);
     }
     {  // both lanes get lane 0's factor
       const R other = __shfl_xor_sync(0xFFFFFFFFu, scale, 1);
@@ -1257,7 +1344,7 @@ __global__ void __launch_bounds__(NT) k_collide(
   }
   __syncthreads();
 
-  // apply
+apply:
   for (int j = threadIdx.x; j < nloc; j += NT) {
     Particle<R> P;
     tile_particle<R, CAP>(P, j, nloc, p0, p1, s_x, s_v, s_lc, C);

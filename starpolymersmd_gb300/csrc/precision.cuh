@@ -68,18 +68,25 @@ __device__ __forceinline__ long long f2fix32(float v) {
 }
 
 // The same value as f2fix32, added to split accumulators: hi (units of 2^-10)
-// and lo (units of 2^-32), each a plain int32 add; the sum is
-// hi * 2^22 + lo. |hi| < 2^22 and |lo| <= 2^21 per term, so 512 terms cannot
-// overflow either part.
-__device__ __forceinline__ void fix32_add(float v, int& hi_acc, int& lo_acc) {
-  const float a = v * 1024.0f;
-  const float m = __fadd_rn(a, 12582912.0f);  // rn(a) in the low mantissa bits
-  const float r = __fsub_rn(a, __fsub_rn(m, 12582912.0f));  // a - rn(a), exact
-  hi_acc += __float_as_int(m) - 0x4B400000;
-  lo_acc += f2i_rn_small(r * 4194304.0f);
+// and lo (units of 2^-32); the sum is hi * 2^22 + lo. Each part is added as
+// the raw bit pattern of its magic-number float, 0x4B400000 + part, with
+// wrap-around unsigned adds; fix32_join takes the n magic offsets back out.
+// |hi| < 2^22 and |lo| <= 2^21 per term, so 512 terms cannot overflow the
+// signed sums. Three FMAs and an add per term: v 2^10 is exact (a power of
+// two), so fma(v, 2^10, magic) is rn(v 2^10) + magic, and
+// fma(v, 2^10, -rn(v 2^10)) is the remainder exactly.
+constexpr uint32_t FIX32_MAGIC_BITS = 0x4B400000u;
+__device__ __forceinline__ void fix32_add(float v, uint32_t& hi_acc, uint32_t& lo_acc) {
+  const float m = fmaf(v, 1024.0f, 12582912.0f);             // rn(v 2^10) in the low bits
+  const float r = fmaf(v, 1024.0f, -__fsub_rn(m, 12582912.0f));  // v 2^10 - rn(v 2^10), exact
+  const float l = fmaf(r, 4194304.0f, 12582912.0f);          // rn(r 2^22) in the low bits
+  hi_acc += __float_as_uint(m);
+  lo_acc += __float_as_uint(l);
 }
-__device__ __forceinline__ long long fix32_join(int hi, int lo) {
-  return static_cast<long long>(hi) * 4194304ll + lo;
+__device__ __forceinline__ long long fix32_join(uint32_t hi_acc, uint32_t lo_acc, int n_terms) {
+  const uint32_t off = static_cast<uint32_t>(n_terms) * FIX32_MAGIC_BITS;
+  return static_cast<long long>(static_cast<int>(hi_acc - off)) * 4194304ll +
+         static_cast<int>(lo_acc - off);
 }
 
 // int64 2^32 fixed point to float (three exact 21-bit pieces, one rounding).

@@ -370,8 +370,10 @@ uint32_t id_of<float>(float w) {
   return u;
 }
 template <>
-uint32_t id_of<double>(double w) {
-  return w < 0 ? smpc::SLOT_EMPTY : static_cast<uint32_t>(w);
+uint32_t id_of<double>(double w) {  // the low half of the bit pattern (slot_id)
+  uint64_t u;
+  std::memcpy(&u, &w, 8);
+  return u >> 32 ? smpc::SLOT_EMPTY - 1u : static_cast<uint32_t>(u);
 }
 template <typename R>
 R id_to_w(uint32_t id);
@@ -383,7 +385,10 @@ float id_to_w<float>(uint32_t id) {
 }
 template <>
 double id_to_w<double>(uint32_t id) {
-  return id == smpc::SLOT_EMPTY ? -1.0 : static_cast<double>(id);
+  const uint64_t u = id;
+  double w;
+  std::memcpy(&w, &u, 8);
+  return w;
 }
 
 template <typename R>
@@ -2168,7 +2173,9 @@ int smpc_vacf_result(smpc_ctx* ctx, double* lag_sums, uint64_t* calculations) {
 namespace {
 
 constexpr char kCkptMagic[8] = {'S', 'M', 'P', 'C', 'C', 'K', 'P', '1'};
-constexpr uint32_t kCkptVersion = 1;
+// version 2: FP64 solvent records carry the slot id as the low half of the
+// .w bit pattern (version 1: as a number)
+constexpr uint32_t kCkptVersion = 2;
 
 struct CkptHeader {
   char magic[8];

@@ -375,6 +375,42 @@ def test_autotune_reports_and_keeps_a_variant():
         assert abs(ctx.temperature(0) - 1.0) < 0.2
 
 
+@pytest.mark.parametrize("md_variant", [0, 1, 2, 3, 4])
+def test_fp32_md_variants_are_reproducible(md_variant):
+    # two runs of the same replicas give the same bits: the Verlet lists come
+    # out in the same order whatever order the hash-grid insertions ran in
+    # (stars of 16 to 121 beads, so a replica spans several warps)
+    from starpolymersmd_gb300 import system, workloads as W
+    specs = _batch_specs() + [system.ReplicaSpec(L=14, arms=6, n_arm=20, solvophobic_fraction=0.5,
+                                                 shear=0.05, seed=34)]
+    descs, states = [], []
+    for s in specs:
+        rng = np.random.default_rng(900 + s.seed)
+        st = system.make_star(s.arms, s.n_arm, s.solvophobic_fraction, s.mono_mass, s.kT, rng,
+                              bond=0.97)
+        descs.append(W.replica_desc(s, st))
+        states.append((st, system.uniform_fluid((s.L,) * 3, s.n_c, s.kT, rng)))
+    kw = dict(precision=capi.FP32, rng=capi.RNG_PHILOX, mono_bin=capi.MONOBIN_WRAPPED,
+              delrx_mode=capi.DELRX_PHYSICAL, step_update=W.N_SUB, max_neighbors=W.MAX_NB,
+              strict_cells=0)
+    runs = []
+    for _ in range(2):
+        with capi.Context(descs, **kw) as ctx:
+            ctx.set_variants(0, 0, md_variant)
+            for k, (st, (fp, fv)) in enumerate(states):
+                ctx.set_fluid(k, fp, fv)
+                ctx.set_monomers(k, st.pos, st.vel, np.zeros_like(st.pos),
+                                 np.full(st.n, st.mass), st.amphi, st.anchor)
+                ctx.set_bonds(k, st.bond_src, st.bond_dst)
+            ctx.init_md()
+            ctx.cycles(4)
+            ctx.raise_on_device_error()
+            runs.append([ctx.get_fluid(k) + ctx.get_monomers(k) for k in range(len(specs))])
+    for a, b in zip(*runs):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
+
+
 def test_autotune_leaves_the_trajectory_where_it_was():
     # the autotuner's trial cycles run on a saved copy of the state: a context
     # that tunes between two stretches of cycles ends with the same bits as
