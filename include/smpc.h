@@ -195,7 +195,13 @@ int smpc_cycles_profiled(smpc_ctx* ctx, int n, double* phase_ms, int n_phases, d
  * cluster of SMs; md = 1 keeps one CTA per replica there instead. */
 int smpc_set_variants(smpc_ctx* ctx, int bin, int collide, int md);
 int smpc_get_variants(const smpc_ctx* ctx, int* bin, int* collide, int* md);
-/* Times every variant of each fast-path kernel over `cycles` cycles of the
+/* Launch-shape variant of the periodic-MD kernels of FP32 contexts (lanes per
+ * bead of the force kernel, grid of the list builder; index 0 is the
+ * default). Each variant sums a bead's forces in its own fixed order. */
+int smpc_set_pmd_variant(smpc_ctx* ctx, int pmd);
+int smpc_get_pmd_variant(const smpc_ctx* ctx, int* pmd);
+/* Times every variant of each fast-path kernel (and, in contexts with periodic
+ * boxes, of the periodic MD) over `cycles` cycles of the
  * context's own workload (CUDA events on the context stream), keeps the
  * fastest and writes a JSON report (variant -> ms per cycle, chosen). The
  * state is saved to host memory before the trials (as smpc_checkpoint_save)

@@ -1,9 +1,11 @@
 """Launch-shape autotuner front end with a JSON cache.
 
 smpc_autotune (C ABI) times every launch-shape variant of the fast-path
-solvent-binning, collide and MD kernels on the live workload with CUDA events
-and keeps the fastest. This module caches the choice per GPU model and
-workload signature, so later runs of the same workload start tuned.
+solvent-binning, collide and MD kernels (and of the periodic MD, in contexts
+with periodic boxes) on the context's own workload with CUDA events, keeps the
+fastest and restores the state its trial cycles advanced. This module caches
+the choice per GPU model and workload signature, so later runs of the same
+workload start tuned.
 """
 from __future__ import annotations
 
@@ -43,10 +45,13 @@ def tune(ctx, key: str, cycles: int = 3, cache_path: Optional[str] = None,
     path = cache_path or CACHE
     cache = _load(path)
     if not force and key in cache:
-        ctx.set_variants(*cache[key]["index"])
+        index = cache[key]["index"]
+        ctx.set_variants(*index[:3])
+        if len(index) > 3:
+            ctx.set_pmd_variant(index[3])
         return dict(cache[key], cached=True)
     report = ctx.autotune(cycles)
-    entry = {"index": list(ctx.get_variants()), "report": report}
+    entry = {"index": list(ctx.get_variants()) + [ctx.get_pmd_variant()], "report": report}
     cache[key] = entry
     os.makedirs(os.path.dirname(path), exist_ok=True)
     tmp = path + ".tmp%d" % os.getpid()

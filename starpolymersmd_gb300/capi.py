@@ -39,6 +39,7 @@ EXPORTS = ("smpc_create", "smpc_destroy", "smpc_last_error", "smpc_n_cells", "sm
            "smpc_init_solvent", "smpc_temperature_all", "smpc_temperature_all_noalloc",
            "smpc_set_monomer_state_all", "smpc_cycles_io",
            "smpc_get_monomer_state_all", "smpc_set_variants", "smpc_get_variants",
+           "smpc_set_pmd_variant", "smpc_get_pmd_variant",
            "smpc_autotune", "smpc_mpc_bin", "smpc_mpc_collide", "smpc_set_molecules",
            "smpc_molecule_observables_all", "smpc_velocity_profile", "smpc_checkpoint_size",
            "smpc_checkpoint_save", "smpc_checkpoint_load", "smpc_checkpoint_write",
@@ -132,6 +133,8 @@ def load(path: Optional[str] = None):
         "smpc_get_monomer_state_all": ([P, P, P, P], I),
         "smpc_set_variants": ([P, I, I, I], I),
         "smpc_get_variants": ([P, C.POINTER(I), C.POINTER(I), C.POINTER(I)], I),
+        "smpc_set_pmd_variant": ([P, I], I),
+        "smpc_get_pmd_variant": ([P, C.POINTER(I)], I),
         "smpc_autotune": ([P, I, C.c_char_p, I], I),
         "smpc_mpc_bin": ([P, C.c_long, D, P, C.POINTER(I)], I),
         "smpc_mpc_collide": ([P, C.POINTER(Inject)], I),
@@ -333,6 +336,14 @@ class Context:
         self._check(self.lib.smpc_get_variants(self.h, C.byref(b), C.byref(c), C.byref(m)),
                     "get_variants")
         return b.value, c.value, m.value
+
+    def set_pmd_variant(self, pmd):
+        self._check(self.lib.smpc_set_pmd_variant(self.h, pmd), "set_pmd_variant")
+
+    def get_pmd_variant(self):
+        v = C.c_int()
+        self._check(self.lib.smpc_get_pmd_variant(self.h, C.byref(v)), "get_pmd_variant")
+        return v.value
 
     def autotune(self, cycles=3):
         """Times each kernel's launch-shape variants on the live workload and

@@ -33,6 +33,17 @@ const char* collide_variant_name(int v) {
                             "128t 64c cap736 cp.async", "128t 64c cap768 cp.async"};
   return v >= 0 && v < 9 ? n[v] : "?";
 }
+int pmd_variant_count() { return 4; }
+int pmd_variant_lanes(int v) {
+  static const int lanes[] = {8, 4, 16, 8};
+  return v >= 0 && v < 4 ? lanes[v] : 8;
+}
+int pmd_variant_list_blocks_per_sm(int v) { return v == 3 ? 8 : 4; }
+const char* pmd_variant_name(int v) {
+  static const char* n[] = {"8 lanes/bead, lists 4 blocks/SM", "4 lanes/bead, lists 4 blocks/SM",
+                            "16 lanes/bead, lists 4 blocks/SM", "8 lanes/bead, lists 8 blocks/SM"};
+  return v >= 0 && v < 4 ? n[v] : "?";
+}
 const char* md_variant_name(int v) {
   static const char* n[] = {"1024t 1/thread", "512t 2/thread", "1024t lanes/bead, largest first",
                             "1024t big + 512t small side by side, lanes/bead",

@@ -11,7 +11,9 @@
 #include "kernels_impl.cuh"
 
 namespace smpc {
-int fluid_slots_per_tile() { return 4096; }
+// solvent slots per binning block: FP64 blocks hold two records per thread
+// in flight (k_fluid_bin), FP32 blocks four
+int fluid_slots_per_tile(bool fp64) { return fp64 ? 2048 : 4096; }
 int temperature_cells_per_tile() { return 512; }
 int md_max_monomers() { return SMPC_MD_NT * SMPC_MD_MPT; }
 int pmd_block_count(int n_beads) { return (n_beads + PMD_NT - 1) / PMD_NT; }

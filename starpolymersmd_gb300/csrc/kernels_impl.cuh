@@ -216,18 +216,31 @@ void launch_mono_stress<Real>(const RepInfo* reps, const RepDyn* dyn, int n_rep,
 template <>
 void launch_pmd_call<Real>(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, Real* mpos,
                            Real* mnext, Real* mvel, Real* mfrc, Real* mdisp, int n,
-                           double adv_scale, int calc_epot, cudaStream_t st) {
+                           double adv_scale, int calc_epot, int variant, cudaStream_t st) {
   if (a.n == 0) return;
   const int nb = a.n_blocks;
-  // k_pmd_nlist: warps stride over the beads, four blocks per SM of GB300 (a
-  // launch without a rebuild request returns at once and stays short)
-  const int nb_list = std::min((a.n + PMD_NT / 32 - 1) / (PMD_NT / 32), 152 * 4);
-  const int nb_force = pmd_force_block_count<Real>(a.n);
+#if SMPC_FAST_F32
+  const int lanes = pmd_variant_lanes(variant);
+  const int list_bps = pmd_variant_list_blocks_per_sm(variant);
+#else
+  (void)variant;
+  const int lanes = pmd_force_lanes<Real>();
+  const int list_bps = 4;
+#endif
+  // k_pmd_nlist: warps stride over the beads, list_bps blocks per SM of GB300
+  // (a launch without a rebuild request returns at once and stays short)
+  const int nb_list = std::min((a.n + PMD_NT / 32 - 1) / (PMD_NT / 32), 152 * list_bps);
+  const int nb_force = pmd_force_block_count(a.n, lanes);
+  auto forces = k_pmd_forces<Real, pmd_force_lanes<Real>()>;
+#if SMPC_FAST_F32
+  if (lanes == 4) forces = k_pmd_forces<Real, 4>;
+  if (lanes == 16) forces = k_pmd_forces<Real, 16>;
+#endif
   if (n == 0) {
     k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, 0, adv_scale, 0);
     k_pmd_nlist<Real><<<nb_list, PMD_NT, 0, st>>>(a, reps, mpos, mdisp, 0, adv_scale);
-    k_pmd_forces<Real><<<nb_force, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mnext, mvel, mfrc, mdisp,
-                                                    0, adv_scale, 0, 0, calc_epot);
+    forces<<<nb_force, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mnext, mvel, mfrc, mdisp, 0, adv_scale,
+                                        0, 0, calc_epot);
     return;
   }
   k_pmd_drift<Real><<<nb, PMD_NT, 0, st>>>(a, reps, dyn, mpos, mvel, mfrc, mdisp, 1, adv_scale, 1);
@@ -253,7 +266,7 @@ void launch_pmd_call<Real>(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, R
     cudaLaunchKernelEx(&cl, k_pmd_nlist<Real>, a, reps, static_cast<const Real*>(pin), mdisp, k,
                        adv_scale);
     const cudaLaunchConfig_t cf = cfg(nb_force);
-    cudaLaunchKernelEx(&cf, k_pmd_forces<Real>, a, reps, dyn, static_cast<const Real*>(pin), pout,
+    cudaLaunchKernelEx(&cf, forces, a, reps, dyn, static_cast<const Real*>(pin), pout,
                        mvel, mfrc, mdisp, k, adv_scale, 1, static_cast<int>(k < n),
                        static_cast<int>(calc_epot && k == n));
   }

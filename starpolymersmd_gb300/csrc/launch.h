@@ -21,6 +21,12 @@ int collide_variant_cells(int v);     // cells per collide tile of variant v
 const char* bin_variant_name(int v);
 const char* collide_variant_name(int v);
 const char* md_variant_name(int v);
+// periodic-MD shapes: lanes per bead of k_pmd_forces, blocks per SM of the
+// list builder k_pmd_nlist (FP32; FP64 keeps one lane per bead)
+int pmd_variant_count();
+int pmd_variant_lanes(int v);
+int pmd_variant_list_blocks_per_sm(int v);
+const char* pmd_variant_name(int v);
 
 template <typename R>
 struct CollideArgs {
@@ -53,7 +59,7 @@ struct CollideArgs {
 // Tile geometry chosen per precision (register budget of k_collide).
 template <typename R>
 int collide_cells_per_tile();
-int fluid_slots_per_tile();
+int fluid_slots_per_tile(bool fp64);
 int temperature_cells_per_tile();
 int md_max_monomers();
 
@@ -105,7 +111,7 @@ void launch_md(const MdArgs& a, int n_rep, R* mpos, R* mvel, R* mfrc, R* mver, i
 template <typename R>
 void launch_pmd_call(const PmdArgs& a, const RepInfo* reps, RepDyn* dyn, R* mpos, R* mnext,
                      R* mvel, R* mfrc, R* mdisp, int n, double adv_scale, int calc_epot,
-                     cudaStream_t st);
+                     int variant, cudaStream_t st);
 int pmd_block_count(int n_beads);
 
 // Molecules of periodic boxes made whole (observables.cuh); other boxes copied.

@@ -658,7 +658,9 @@ __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepIn
                                                   const RepDyn* dyn, const R* __restrict__ st,
                                                   uint2* __restrict__ keys, uint32_t* count,
                                                   ErrorState* err, int strict) {
-  constexpr int U = 4;
+  // FP64: two records in flight per thread, so that two blocks fit per SM
+  // (the FP64 work is latency-bound on the narrow pipe; more warps hide it)
+  constexpr int U = std::is_same<R, double>::value ? 2 : 4;
   const Tile t = tiles[blockIdx.x];
   const RepInfo& ri = reps[t.rep];
   const RepDyn dn = dyn[t.rep];

@@ -61,15 +61,16 @@ constexpr int PMD_NT = 256;        // threads per block of every periodic-MD ker
 constexpr int PMD_NL_CAP = 256;    // Verlet-list entries one warp of k_pmd_nlist collects
 
 // Lanes per bead in k_pmd_forces: FP64 keeps one (the oracle's order of the
-// sums), FP32 splits each list over eight.
+// sums); FP32 splits each list over eight by default, or over 4 or 16 (the
+// launch-shape variants of the periodic MD, pmd_variant_*).
+constexpr int PMD_MAX_LANES = 16;
 template <typename R>
 constexpr int pmd_force_lanes() {
   return std::is_same<R, float>::value ? 8 : 1;
 }
 
-template <typename R>
-inline int pmd_force_block_count(int n_beads) {
-  return (n_beads * pmd_force_lanes<R>() + PMD_NT - 1) / PMD_NT;
+inline int pmd_force_block_count(int n_beads, int lanes) {
+  return (n_beads * lanes + PMD_NT - 1) / PMD_NT;
 }
 
 struct PmdArgs {
@@ -414,13 +415,13 @@ __global__ void __launch_bounds__(PMD_NT)
 
 // Substep k: forces at positions pin, second half kick; with drift_next,
 // substep k+1's kick, drift, wrap and binning into pout.
-template <typename R>
+template <typename R, int LANES>
 __global__ void __launch_bounds__(PMD_NT)
     k_pmd_forces(PmdArgs a, const RepInfo* reps, RepDyn* dyn, const R* pin, R* pout, R* mvel,
                  R* mfrc, R* mdisp, int adv_k, double adv_scale, int kick, int drift_next,
                  int calc_epot) {
+  static_assert(32 % LANES == 0 && LANES <= PMD_MAX_LANES, "lanes of a bead within one warp");
   pmd_wait_previous();
-  constexpr int LANES = pmd_force_lanes<R>();
   const RepInfo& ri = reps[a.rep];
   const int s = adv_k & 1;
   const PmdBox<R> b = pmd_box<R>(ri, a.dl_slot[s]);

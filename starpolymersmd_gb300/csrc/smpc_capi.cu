@@ -46,7 +46,7 @@ struct smpc_ctx {
   // fast path: collide tiles for each tile size the variants use (64/128/256 cells)
   Tile* d_col_tiles_v[3] = {nullptr, nullptr, nullptr};
   int n_col_tiles_v[3] = {0, 0, 0};
-  int var_bin = 0, var_col = 0, var_md = 0;
+  int var_bin = 0, var_col = 0, var_md = 0, var_pmd = 0;
   std::vector<Tile> h_tmp_tiles;
   Tile* d_tmp_tiles = nullptr;
   TempPartial* d_tpart = nullptr;
@@ -271,7 +271,7 @@ int launch_md_steps(smpc_ctx* ctx, int n, int calc_epot, int force_rebuild) {
     smpc::launch_pmd_call<R>(p, ctx->d_reps, ctx->d_dyn, static_cast<R*>(ctx->d_mpos),
                              static_cast<R*>(ctx->d_mnext), static_cast<R*>(ctx->d_mvel),
                              static_cast<R*>(ctx->d_mfrc), static_cast<R*>(ctx->d_mver), n, adv,
-                             calc_epot, ctx->st);
+                             calc_epot, ctx->var_pmd, ctx->st);
   if (!ctx->any_local_md) return SMPC_OK;
   smpc::MdArgs a;
   a.reps = ctx->d_reps;
@@ -914,8 +914,8 @@ int create_periodic_md(smpc_ctx* ctx) {
     CU(cudaMalloc(&db, sizeof(double)));
     ctx->pmd_mem.push_back(db);
     // per block of k_pmd_forces, whose lanes per bead depend on the precision
-    const int force_blocks = std::max(smpc::pmd_force_block_count<float>(a.n),
-                                      smpc::pmd_force_block_count<double>(a.n));
+    // and the launch-shape variant
+    const int force_blocks = smpc::pmd_force_block_count(a.n, smpc::PMD_MAX_LANES);
     CU(cudaMalloc(&ep, static_cast<size_t>(force_blocks) * sizeof(double)));
     ctx->pmd_mem.push_back(ep);
     CU(cudaMalloc(&slot, 4 * sizeof(double)));
@@ -1089,7 +1089,8 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
   if (rc) return bail(rc, ctx->err);
   const int ct = opt->precision == SMPC_FP64 ? smpc::collide_cells_per_tile<double>()
                                              : smpc::collide_cells_per_tile<float>();
-  std::vector<Tile> bin = make_tiles(ctx->reps, false, smpc::fluid_slots_per_tile());
+  std::vector<Tile> bin =
+      make_tiles(ctx->reps, false, smpc::fluid_slots_per_tile(opt->precision == SMPC_FP64));
   std::vector<Tile> col = make_tiles(ctx->reps, true, ct);
   ctx->h_tmp_tiles = make_tiles(ctx->reps, true, smpc::temperature_cells_per_tile());
   ctx->n_bin_tiles = static_cast<int>(bin.size());
@@ -1545,6 +1546,21 @@ int smpc_set_variants(smpc_ctx* ctx, int bin, int collide, int md) {
   return SMPC_OK;
 }
 
+int smpc_set_pmd_variant(smpc_ctx* ctx, int pmd) {
+  if (!ctx) return SMPC_E_ARG;
+  if (pmd < 0 || pmd >= smpc::pmd_variant_count())
+    return fail(ctx, SMPC_E_ARG, "variant index out of range");
+  if (pmd != ctx->var_pmd) drop_graphs(ctx);
+  ctx->var_pmd = pmd;
+  return SMPC_OK;
+}
+
+int smpc_get_pmd_variant(const smpc_ctx* ctx, int* pmd) {
+  if (!ctx || !pmd) return SMPC_E_ARG;
+  *pmd = ctx->var_pmd;
+  return SMPC_OK;
+}
+
 int smpc_get_variants(const smpc_ctx* ctx, int* bin, int* collide, int* md) {
   if (!ctx) return SMPC_E_ARG;
   if (bin) *bin = ctx->var_bin;
@@ -1571,19 +1587,22 @@ int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len) {
       return fail(ctx, SMPC_E_ARG, "no host memory for the autotuner's state copy");
     }
     if (int rc = smpc_checkpoint_save(ctx, snap.data(), snap_bytes)) return rc;
-    const int var0[3] = {ctx->var_bin, ctx->var_col, ctx->var_md};
+    const int var0[4] = {ctx->var_bin, ctx->var_col, ctx->var_md, ctx->var_pmd};
     struct Cat {
       const char* name;
       int phase;
       int count;
       int* var;
       const char* (*label)(int);
-    } cats[3] = {{"fluid_bin", PH_BIN, smpc::bin_variant_count(), &ctx->var_bin, smpc::bin_variant_name},
+    } cats[4] = {{"fluid_bin", PH_BIN, smpc::bin_variant_count(), &ctx->var_bin, smpc::bin_variant_name},
                  {"collide", PH_COLLIDE, smpc::collide_variant_count(), &ctx->var_col,
                   smpc::collide_variant_name},
-                 {"md_substeps", PH_MD, smpc::md_variant_count(), &ctx->var_md, smpc::md_variant_name}};
+                 {"md_substeps", PH_MD, smpc::md_variant_count(), &ctx->var_md, smpc::md_variant_name},
+                 {"pmd", PH_MD, smpc::pmd_variant_count(), &ctx->var_pmd, smpc::pmd_variant_name}};
+    // periodic-MD shapes only where a box runs the periodic MD
+    const int n_cats = ctx->pmd.empty() ? 3 : 4;
     double ph[PH_COUNT], tot;
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < n_cats; ++c) {
       int best = 0;
       double best_ms = 1e300;
       js += std::string(c ? ", " : "") + "\"" + cats[c].name + "\": {\"ms_per_cycle\": {";
@@ -1594,6 +1613,7 @@ int smpc_autotune(smpc_ctx* ctx, int cycles, char* report, int report_len) {
           ctx->var_bin = var0[0];
           ctx->var_col = var0[1];
           ctx->var_md = var0[2];
+          ctx->var_pmd = var0[3];
           drop_graphs(ctx);
           smpc_checkpoint_load(ctx, snap.data(), snap_bytes);
           return rc;

@@ -183,15 +183,19 @@ def test_fp64_periodic_graph_cycles_match_stepwise():
         assert a.verlet_rebuilds(0) == b.verlet_rebuilds(0)
 
 
-def test_fp32_periodic_md_tracks_fp64_oracle():
+@pytest.mark.parametrize("pmd_variant", [0, 1, 2, 3])
+def test_fp32_periodic_md_tracks_fp64_oracle(pmd_variant):
     # MD only (no collision in 40 substeps), 12-6 preset with LJ attraction to
-    # 2.5 and skin 0.3, shear 0.5: FP32 against the FP64 oracle
+    # 2.5 and skin 0.3, shear 0.5: FP32 against the FP64 oracle, with every
+    # launch shape of the periodic MD (4, 8 or 16 lanes per bead)
     sol = _solution(seed=3, n_stars=6, arms=4, n_arm=6)
     su = 50
     fpos = np.zeros((0, 3))
     kw = dict(potential=capi.POT_LJ126, r_cut=2.5)
     o = _oracle(sol, fpos, fpos, 0.5, su, 2.8, potential=orc.POT_LJ126, r_cut=2.5)
     with _context(sol, fpos, fpos, 0.5, su, 2.8, precision=capi.FP32, **kw) as ctx:
+        ctx.set_pmd_variant(pmd_variant)
+        assert ctx.get_pmd_variant() == pmd_variant
         n = 40
         for t in range(1, n + 1):
             o.propagate(False)
@@ -396,3 +400,28 @@ def _numpy_unwrap_L(pos, vel, src, dst, mol_start, delrx, shear, Lb):
             up[i] = up[p] + d
             uv[i, 0] = vel[i, 0] + np.round((up[i, 1] - pos[i, 1]) / Lb) * shear * Lb
     return up, uv
+
+
+def test_autotune_covers_the_periodic_md_shapes():
+    # a context with a periodic box gets the periodic-MD category, keeps its
+    # choice, and the trial cycles leave the state where it was
+    sol = _solution(seed=4, n_stars=4, arms=4, n_arm=6)
+    rng = np.random.default_rng(12)
+    fpos = (rng.random((3 * L ** 3, 3)) - 0.5) * L
+    fvel = rng.normal(0.0, 1.0, fpos.shape)
+    kw = dict(potential=capi.POT_LJ126, r_cut=2.5)
+    with _context(sol, fpos, fvel, 0.2, 10, 2.8, precision=capi.FP32, **kw) as a, \
+            _context(sol, fpos, fvel, 0.2, 10, 2.8, precision=capi.FP32, **kw) as b:
+        a.cycles(2)
+        b.cycles(2)
+        report = a.autotune(1)
+        assert {"fluid_bin", "collide", "md_substeps", "pmd"} <= set(report)
+        assert a.get_pmd_variant() == report["pmd"]["index"]
+        b.set_variants(*a.get_variants())
+        b.set_pmd_variant(a.get_pmd_variant())
+        a.cycles(2)
+        b.cycles(2)
+        a.raise_on_device_error()
+        b.raise_on_device_error()
+        for x, y in zip(a.get_fluid(0) + a.get_monomers(0), b.get_fluid(0) + b.get_monomers(0)):
+            np.testing.assert_array_equal(x, y)
