@@ -46,3 +46,22 @@ def test_two_gloo_ranks_time_by_the_slowest():
     for r, w, ms, value in out:
         assert w == 2 and ms == 11.0
         assert value == pytest.approx(1000 * 5 * 2 / 0.011)  # whole job over the slowest rank
+
+
+def test_reference_arm_line():
+    # the reference arm on the host cores: the oracle's restatement on every
+    # replica of the workload, warm-up honoured, one JSON line with the keys
+    # the contract names
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--workload", "single_star_20", "--steps", "2", "--warmup", "3"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["steps"] == 2 and line["warmup"] == 3
+    assert line["config"]["replicas"] == 1 and line["config"]["particles"] == 80121
+    assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
