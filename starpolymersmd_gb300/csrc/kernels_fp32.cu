@@ -13,11 +13,11 @@ namespace smpc {
 // Variant tables (index 0 is the default shape). The names read
 // threads x cells-per-tile / staging capacity / gathers in flight.
 int bin_variant_count() { return 4; }
-int collide_variant_count() { return 9; }
+int collide_variant_count() { return 12; }
 int md_variant_count() { return 5; }
 int collide_variant_cells(int v) {
   switch (v) {
-    case 2: case 3: case 5: case 7: case 8: return 64;
+    case 2: case 3: case 5: case 7: case 8: case 9: case 10: case 11: return 64;
     case 4: return 256;
     default: return 128;
   }
@@ -30,8 +30,10 @@ const char* collide_variant_name(int v) {
   static const char* n[] = {"256t 128c cap1408 g4", "256t 128c cap1408 g8", "128t 64c cap704 g4",
                             "128t 64c cap704 g8", "512t 256c cap2816 g4",
                             "128t 64c cap704 cp.async", "256t 128c cap1408 cp.async",
-                            "128t 64c cap736 cp.async", "128t 64c cap768 cp.async"};
-  return v >= 0 && v < 9 ? n[v] : "?";
+                            "128t 64c cap736 cp.async", "128t 64c cap768 cp.async",
+                            "160t 64c cap704 cp.async", "192t 64c cap704 cp.async",
+                            "256t 64c cap704 cp.async"};
+  return v >= 0 && v < 12 ? n[v] : "?";
 }
 int pmd_variant_count() { return 4; }
 int pmd_variant_lanes(int v) {

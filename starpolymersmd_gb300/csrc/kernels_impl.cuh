@@ -124,6 +124,9 @@ void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
       case 6: collide_f32_async<256, 128, 1408>(a, st); return;
       case 7: collide_f32_async<128, 64, 736>(a, st); return;
       case 8: collide_f32_async<128, 64, 768>(a, st); return;
+      case 9: collide_f32_async<160, 64, 704>(a, st); return;
+      case 10: collide_f32_async<192, 64, 704>(a, st); return;
+      case 11: collide_f32_async<256, 64, 704>(a, st); return;
       default: collide_f32<256, 128, 1408, 4>(a, st); return;
     }
   }

@@ -601,7 +601,9 @@ __global__ void __launch_bounds__(NT) k_collide_f32_async(
     const float* __restrict__ st_in, float* __restrict__ st_out, const float* mpos, float* mvel,
     const int* mimg, const double* inj_gamma, const double* inj_uphi, const double* inj_utheta,
     int rng, int mono_bin, ErrorState* err) {
-  static_assert(NT == 2 * CT, "two threads per cell");
+  // two threads per cell in the cell pass; threads past 2 CT take no cell
+  // there and add warps to the particle passes (gather, frame, apply)
+  static_assert(NT >= 2 * CT && NT % 32 == 0, "two threads per cell, whole warps");
   constexpr int J = (CAP + NT - 1) / NT;  // staged particles per thread
   __shared__ float4 s_rc[CT * 3];  // per cell: rows of sR, cell velocity in .w
   __shared__ uint32_t s_off[CT + 1];

@@ -322,7 +322,7 @@ def test_fp32_launch_variants_agree_bitwise():
         states.append((fp, fv))
     finals = []
     lib = capi.load()
-    n_bin, n_col = 4, 9
+    n_bin, n_col = 4, 12
     for vb, vc in [(0, 0)] + [(b, 0) for b in range(1, n_bin)] + [(0, c) for c in range(1, n_col)]:
         with capi.Context(reps, precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=1,
                           strict_cells=0) as ctx:
@@ -343,7 +343,7 @@ def test_fp32_collide_variants_agree_bitwise_with_stars():
     # the same with monomers in the cells (staged from the monomer arrays,
     # written back to them), MD substeps in between
     finals = []
-    for vc in range(9):
+    for vc in range(12):
         ctx, _, specs = _batch_run(capi.FP32, cycles=0)
         with ctx:
             ctx.set_variants(0, vc, 0)
