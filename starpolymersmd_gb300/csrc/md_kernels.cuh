@@ -693,6 +693,11 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
 // at once, and every CTA reaches every barrier (all branches around them
 // depend on the replica and the rebuild flag only, which agree across the
 // cluster after each barrier). Lowe-Andersen stays on k_md_substeps.
+// The kicks, the drift and the position pushes of a CTA's beads run one
+// thread per bead (threads 0 .. own-1, in whole warps), not on the lead lane
+// of each bead's lanes: on the narrow FP64 pipe a warp instruction costs the
+// same with one active lane as with 32. Forces reach those threads through
+// shared memory.
 constexpr int MD_CLUSTER_CAP = 1024;
 
 template <typename R, int NT, int CS, int KMAX>
@@ -708,6 +713,8 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   __shared__ int s_rebuild;
   __shared__ double s_red[NT / 32];
   __shared__ double s_epot[CS];
+  __shared__ R s_f[3 * ((CAP + CS - 1) / CS)];  // forces of this CTA's beads
+  static_assert((CAP + CS - 1) / CS <= NT, "a kick thread for every bead of the CTA");
   cg::cluster_group cl = cg::this_cluster();
   const int rank = static_cast<int>(cl.block_rank());
   const int cidx = static_cast<int>(blockIdx.x) / CS;
@@ -740,12 +747,18 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     sx[j] = p.x; sy[j] = p.y; sz[j] = p.z;
     s_amphi[j] = static_cast<unsigned char>(static_cast<int>(ld4_rw(mvel, b + j).w) & 1);
   }
-  R x[3] = {R(0), R(0), R(0)}, v[3] = {R(0), R(0), R(0)}, f[3] = {R(0), R(0), R(0)},
+  // x: the position of this lane's bead in the force pass (from shared
+  // memory); the bead's dynamic state lives with its kick thread
+  R x[3] = {R(0), R(0), R(0)};
+  const int kq = static_cast<int>(threadIdx.x);  // kick thread of bead slot kq
+  const bool kicker = kq < own;
+  const int ik = rank + CS * kq;
+  R xk[3] = {R(0), R(0), R(0)}, v[3] = {R(0), R(0), R(0)}, f[3] = {R(0), R(0), R(0)},
     xv[3] = {R(0), R(0), R(0)}, m = R(1);
-  if (mine) {
-    const R4<R> p = ld4_rw(mpos, b + i), vv = ld4_rw(mvel, b + i), ff = ld4_rw(mfrc, b + i),
-                pv = ld4_rw(mver, b + i);
-    x[0] = p.x; x[1] = p.y; x[2] = p.z; m = p.w;
+  if (kicker) {
+    const R4<R> p = ld4_rw(mpos, b + ik), vv = ld4_rw(mvel, b + ik), ff = ld4_rw(mfrc, b + ik),
+                pv = ld4_rw(mver, b + ik);
+    xk[0] = p.x; xk[1] = p.y; xk[2] = p.z; m = p.w;
     v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
     f[0] = ff.x; f[1] = ff.y; f[2] = ff.z;
     xv[0] = pv.x; xv[1] = pv.y; xv[2] = pv.z;
@@ -760,35 +773,34 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   double epot = 0.0;
   const int total_steps = a.n_steps > 0 ? a.n_steps : 1;
   for (int step = 0; step < total_steps; ++step) {
-    if (a.n_steps > 0 && mine && lead) {
-      // kick + drift (Thermostat_None.cpp:22-27), by the bead's lead lane
-      // only (the FP64 pipe is the scarce resource); the other lanes read the
+    if (a.n_steps > 0 && kicker) {
+      // kick + drift (Thermostat_None.cpp:22-27); the force lanes read the
       // new position from shared memory after the barrier
       for (int d = 0; d < 3; ++d) {
         v[d] += a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
-        x[d] += v[d] * dt;
+        xk[d] += v[d] * dt;
       }
       {
         bool over = false;
         if (!a.core_relative) {  // Box::check_VerletLists (Box.cpp:182-194)
-          const R d0 = x[0] - xv[0], d1 = x[1] - xv[1], d2 = x[2] - xv[2];
+          const R d0 = xk[0] - xv[0], d1 = xk[1] - xv[1], d2 = xk[2] - xv[2];
           over = r_sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim;
         }
         for (int c = 0; c < CS; ++c) {
-          cl.map_shared_rank(sx, c)[i] = x[0];
-          cl.map_shared_rank(sy, c)[i] = x[1];
-          cl.map_shared_rank(sz, c)[i] = x[2];
+          cl.map_shared_rank(sx, c)[ik] = xk[0];
+          cl.map_shared_rank(sy, c)[ik] = xk[1];
+          cl.map_shared_rank(sz, c)[ik] = xk[2];
           if (over) *cl.map_shared_rank(&s_rebuild, c) = 1;
         }
       }
     }
     cl.sync();  // positions and rebuild flags complete in every CTA
-    if (mine && !lead) { x[0] = sx[i]; x[1] = sy[i]; x[2] = sz[i]; }
+    if (mine) { x[0] = sx[i]; x[1] = sy[i]; x[2] = sz[i]; }
     if (a.core_relative && a.n_steps > 0) {
       // displacements relative to the core's (see k_md_substeps)
       const R c0 = sx[0] - s_core_ref[0], c1 = sy[0] - s_core_ref[1], c2 = sz[0] - s_core_ref[2];
-      if (mine && lead) {
-        const R d0 = x[0] - xv[0] - c0, d1 = x[1] - xv[1] - c1, d2 = x[2] - xv[2] - c2;
+      if (kicker) {
+        const R d0 = xk[0] - xv[0] - c0, d1 = xk[1] - xv[1] - c1, d2 = xk[2] - xv[2] - c2;
         if ((d0 * d0 + d1 * d1) + d2 * d2 > lim * lim)
           for (int c = 0; c < CS; ++c) *cl.map_shared_rank(&s_rebuild, c) = 1;
       }
@@ -838,7 +850,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         }
         a.ncount[b + i] = cnt;
       }
-      if (mine) { xv[0] = x[0]; xv[1] = x[1]; xv[2] = x[2]; }
+      if (kicker) { xv[0] = xk[0]; xv[1] = xk[1]; xv[2] = xk[2]; }
       if (threadIdx.x == 0) { s_core_ref[0] = sx[0]; s_core_ref[1] = sy[0]; s_core_ref[2] = sz[0]; }
       __syncthreads();  // lists written before the lanes of a bead read them
     }
@@ -898,8 +910,16 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       F1 += __shfl_xor_sync(0xFFFFFFFFu, F1, o);
       F2 += __shfl_xor_sync(0xFFFFFFFFu, F2, o);
     }
-    f[0] = F0; f[1] = F1; f[2] = F2;
     if (mine && lead) {
+      s_f[3 * q] = F0;
+      s_f[3 * q + 1] = F1;
+      s_f[3 * q + 2] = F2;
+    }
+    __syncthreads();  // the forces reach the kick threads
+    if (kicker) {
+      f[0] = s_f[3 * kq];
+      f[1] = s_f[3 * kq + 1];
+      f[2] = s_f[3 * kq + 2];
       if (a.n_steps > 0) {
         for (int d = 0; d < 3; ++d)  // second half-kick
           v[d] += a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
@@ -908,10 +928,10 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
                                       : nullptr;
           if (as && as[0] >= 0) {
             for (int e = as[step]; e < as[step + 1]; ++e)
-              if (a.and_mono[e] == i)
+              if (a.and_mono[e] == ik)
                 for (int d = 0; d < 3; ++d) v[d] = static_cast<R>(a.and_vel[3 * e + d]);
           } else {
-            andersen_draw<R>(ri.seed, i, md_step0 + static_cast<unsigned long long>(step),
+            andersen_draw<R>(ri.seed, ik, md_step0 + static_cast<unsigned long long>(step),
                              static_cast<R>(a.andersen_nu * ri.md_dt),
                              r_sqrt(static_cast<R>(ri.kT)), m, v);
           }
@@ -920,15 +940,15 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     }
     cl.sync();  // every CTA is done reading positions before the next drift rewrites them
   }
-  if (mine && lead) {
-    R4<R> p = ld4_rw(mpos, b + i);
-    p.x = x[0]; p.y = x[1]; p.z = x[2];
-    st4(mpos, b + i, p);
-    R4<R> vv = ld4_rw(mvel, b + i);
+  if (kicker) {
+    R4<R> p = ld4_rw(mpos, b + ik);
+    p.x = xk[0]; p.y = xk[1]; p.z = xk[2];
+    st4(mpos, b + ik, p);
+    R4<R> vv = ld4_rw(mvel, b + ik);
     vv.x = v[0]; vv.y = v[1]; vv.z = v[2];
-    st4(mvel, b + i, vv);
-    st4(mfrc, b + i, R4<R>{f[0], f[1], f[2], R(0)});
-    st4(mver, b + i, R4<R>{xv[0], xv[1], xv[2], R(0)});
+    st4(mvel, b + ik, vv);
+    st4(mfrc, b + ik, R4<R>{f[0], f[1], f[2], R(0)});
+    st4(mver, b + ik, R4<R>{xv[0], xv[1], xv[2], R(0)});
   }
   if (a.calc_epot) {
     for (int o = 16; o > 0; o >>= 1) epot += __shfl_down_sync(0xFFFFFFFFu, epot, o);
