@@ -262,15 +262,23 @@ def record_bytes(precision):
     return 32 if precision == "fp32" else 64
 
 
-def kernel_rooflines(phases, cycles, n_solvent, slots, n_cells, rec, peak):
+def key_bytes(precision, specs):
+    """Bytes of one sort key: the FP32 fast path packs (local cell, rank) into
+    32 bits when every box has at most 65,536 cells; otherwise (global cell,
+    rank) pairs of 8 bytes."""
+    return 4 if precision == "fp32" and max(s.L ** 3 for s in specs) <= 65536 else 8
+
+
+def kernel_rooflines(phases, cycles, n_solvent, slots, n_cells, rec, peak, kb=8):
     """Achieved HBM GB/s of the solvent kernels from their CUDA-event times
-    (ms summed over ``cycles``) and their algorithmic bytes per launch:
-      fluid_bin   read a record, write the 8-byte key        (rec + 8) B / particle
-      build_perm  read the key, write the 4-byte sorted entry  12 B / entry
+    (ms summed over ``cycles``) and their algorithmic bytes per launch (kb:
+    bytes of one sort key):
+      fluid_bin   read a record, write the key               (rec + kb) B / particle
+      build_perm  read the key, write the 4-byte sorted entry  (kb + 4) B / entry
       collide     read the entry and the record, write the record back
                   (4 + 2 rec) B / entry + 4 B / cell (offsets)"""
-    alg = {"fluid_bin": n_solvent * (rec + 8),
-           "build_perm": slots * 12,
+    alg = {"fluid_bin": n_solvent * (rec + kb),
+           "build_perm": slots * (kb + 4),
            "collide": slots * (4 + 2 * rec) + (n_cells + 1) * 4}
     out = {}
     for k, nbytes in alg.items():
@@ -344,7 +352,8 @@ def run_ours(args, world, rank, local, dist):
     n_solvent = int(sum(built.n_fluid))
     slots = units  # every solvent particle and monomer passes the collide kernel once
     peak, peak_kind = measured_peaks()
-    per_kernel = kernel_rooflines(phases, K, n_solvent, slots, n_cells, rec, peak)
+    kb = key_bytes(args.precision, built.specs)
+    per_kernel = kernel_rooflines(phases, K, n_solvent, slots, n_cells, rec, peak, kb)
     coll = per_kernel["collide"]
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -384,6 +393,8 @@ def run_ours(args, world, rank, local, dist):
                       "monomers": int(sum(built.n_mono)), "cells": n_cells,
                       "md_substeps_per_cycle": W.N_SUB, "h": W.H, "md_dt": W.MD_DT,
                       "precision": precision_desc,
+                      "sort_keys": "32-bit (local cell << 16 | rank)" if kb == 4
+                                   else "64-bit (global cell, rank)",
                       "l2": "state of %.1f GB per copy, %s" % (
                           units * rec / 1e9, "inputs larger than L2" if units * rec > 129e6
                           else "state fits in the 129 MB L2 (the workload's own size)"),

@@ -55,8 +55,13 @@ void launch_mono_prep<Real>(const RepInfo* reps, RepDyn* dyn, int n_rep, Real* m
 #if SMPC_FAST_F32
 template <int NT, int U>
 void bin_f32(const Tile* tiles, int n_tiles, const RepInfo* reps, const FrameF* frames,
-             const float* rec, uint2* keys, uint32_t* count, cudaStream_t st) {
-  k_fluid_bin_f32<NT, U><<<n_tiles, NT, 0, st>>>(tiles, reps, frames, rec, keys, count);
+             const float* rec, uint2* keys, uint32_t* count, ErrorState* err, bool packed,
+             cudaStream_t st) {
+  if (packed)
+    k_fluid_bin_f32<NT, U, true><<<n_tiles, NT, 0, st>>>(tiles, reps, frames, rec, keys, count, err);
+  else
+    k_fluid_bin_f32<NT, U, false><<<n_tiles, NT, 0, st>>>(tiles, reps, frames, rec, keys, count,
+                                                          err);
 }
 
 template <int NT, int CT, int CAP, int GU>
@@ -92,17 +97,20 @@ template <>
 void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
                             const RepDyn* dyn, const FrameF* frames, const Real* rec, uint2* keys,
                             uint32_t* count, ErrorState* err, int strict, int variant,
-                            cudaStream_t st) {
+                            int packed, cudaStream_t st) {
   if (n_tiles == 0) return;
 #if SMPC_FAST_F32
   if (!strict && variant >= 0) {  // variant < 0: the generic kernel (what k_collide recomputes)
+    const bool pk = packed != 0;
     switch (variant) {
-      case 1: bin_f32<256, 2>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
-      case 2: bin_f32<256, 8>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
-      case 3: bin_f32<128, 8>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
-      default: bin_f32<256, 4>(tiles, n_tiles, reps, frames, rec, keys, count, st); return;
+      case 1: bin_f32<256, 2>(tiles, n_tiles, reps, frames, rec, keys, count, err, pk, st); return;
+      case 2: bin_f32<256, 8>(tiles, n_tiles, reps, frames, rec, keys, count, err, pk, st); return;
+      case 3: bin_f32<128, 8>(tiles, n_tiles, reps, frames, rec, keys, count, err, pk, st); return;
+      default: bin_f32<256, 4>(tiles, n_tiles, reps, frames, rec, keys, count, err, pk, st); return;
     }
   }
+#else
+  (void)packed;
 #endif
   (void)frames;
   (void)variant;

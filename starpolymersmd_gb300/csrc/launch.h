@@ -80,7 +80,7 @@ void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* m
 template <typename R>
 void launch_fluid_bin(const Tile* tiles, int n_tiles, const RepInfo* reps, const RepDyn* dyn,
                       const FrameF* frames, const R* rec, uint2* keys, uint32_t* count,
-                      ErrorState* err, int strict, int variant, cudaStream_t st);
+                      ErrorState* err, int strict, int variant, int packed, cudaStream_t st);
 template <typename R>
 void launch_collide(const CollideArgs<R>& a, cudaStream_t st);
 template <typename R>
@@ -170,5 +170,11 @@ void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* g
 int scan_tile_count(int n_cells);
 void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_mono,
                        const uint32_t* off, uint32_t* perm, ErrorState* err, cudaStream_t st);
+// the same from packed solvent keys (local cell << 16 | rank), one block per
+// binning tile of slots
+void launch_build_perm_packed(const Tile* tiles, int n_tiles, const RepInfo* reps,
+                              const uint32_t* keys, int n_slots, const uint2* mkey, int n_mono,
+                              const uint32_t* off, uint32_t* perm, ErrorState* err,
+                              cudaStream_t st);
 
 }  // namespace smpc

@@ -102,11 +102,16 @@ __device__ __forceinline__ void st_f4(float* p, size_t i, float4 v) {
 
 // --------------------------------------------------------------- binning
 
-template <int NT, int U>
+// PACKED: 32-bit keys (local cell << 16 | rank) for contexts whose boxes
+// have at most 65,536 cells each, half the bytes of the (global cell, rank)
+// pairs between the binning and the permutation. A cell of 65,535 particles
+// or more cannot be packed and raises ERR_KEY_MISMATCH.
+template <int NT, int U, bool PACKED>
 __global__ void __launch_bounds__(NT) k_fluid_bin_f32(const Tile* tiles, const RepInfo* reps,
                                                       const FrameF* frames,
                                                       const float* __restrict__ st,
-                                                      uint2* __restrict__ keys, uint32_t* count) {
+                                                      uint2* __restrict__ keys, uint32_t* count,
+                                                      ErrorState* err) {
   const Tile t = tiles[blockIdx.x];
   const FrameF f = frames[t.rep];
   const uint32_t cbase = static_cast<uint32_t>(reps[t.rep].cell_base);
@@ -148,7 +153,20 @@ __global__ void __launch_bounds__(NT) k_fluid_bin_f32(const Tile* tiles, const R
     for (int u = 0; u < U; ++u) {
       const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, rbase[u], __ffs(peers[u]) - 1);
       const int i = base + u * NT + threadIdx.x;
-      if (i < t.end) keys[i] = make_uint2(key[u], b0 + __popc(peers[u] & below));
+      if (i >= t.end) continue;
+      const uint32_t rank = b0 + __popc(peers[u] & below);
+      if (PACKED) {
+        uint32_t k32 = KEY_NONE;
+        if (key[u] != KEY_NONE) {
+          if (rank >= 0xFFFFu)
+            raise_error(err, ERR_KEY_MISMATCH, static_cast<uint32_t>(i), key[u]);
+          else
+            k32 = ((key[u] - cbase) << 16) | rank;
+        }
+        reinterpret_cast<uint32_t*>(keys)[i] = k32;
+      } else {
+        keys[i] = make_uint2(key[u], rank);
+      }
     }
   }
 }

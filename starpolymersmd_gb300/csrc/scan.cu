@@ -179,6 +179,56 @@ __global__ void __launch_bounds__(PERM_NT) k_build_perm(const uint2* __restrict_
   }
 }
 
+// The same scatter from packed solvent keys (local cell << 16 | rank, written
+// by the packed binning): one block per binning tile of slots, whose replica
+// gives the cell base; the monomers' (global cell, rank) keys in the blocks
+// after the tiles.
+__global__ void __launch_bounds__(PERM_NT) k_build_perm_packed(
+    const Tile* tiles, int n_tiles, const RepInfo* reps, const uint32_t* __restrict__ keys,
+    int n_slots, const uint2* __restrict__ mkey, int n_mono, const uint32_t* __restrict__ off,
+    uint32_t* __restrict__ perm, ErrorState* err) {
+  const uint32_t n = static_cast<uint32_t>(n_slots + n_mono);
+  if (static_cast<int>(blockIdx.x) < n_tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const uint32_t cbase = static_cast<uint32_t>(reps[t.rep].cell_base);
+    for (int base = t.begin + static_cast<int>(threadIdx.x); base < t.end;
+         base += PERM_NT * PERM_U) {
+      uint32_t k[PERM_U], o[PERM_U];
+#pragma unroll
+      for (int u = 0; u < PERM_U; ++u) {
+        const int i = base + u * PERM_NT;
+        k[u] = i < t.end ? keys[i] : KEY_NONE;
+      }
+#pragma unroll
+      for (int u = 0; u < PERM_U; ++u) o[u] = k[u] != KEY_NONE ? off[cbase + (k[u] >> 16)] : 0u;
+#pragma unroll
+      for (int u = 0; u < PERM_U; ++u) {
+        if (k[u] == KEY_NONE) continue;
+        const uint32_t pos = o[u] + (k[u] & 0xFFFFu);
+        if (pos < n)
+          perm[pos] = static_cast<uint32_t>(base + u * PERM_NT);
+        else
+          raise_error(err, ERR_KEY_MISMATCH, pos, k[u]);
+      }
+    }
+    return;
+  }
+  const int base = (static_cast<int>(blockIdx.x) - n_tiles) * (PERM_NT * PERM_U) +
+                   static_cast<int>(threadIdx.x);
+#pragma unroll
+  for (int u = 0; u < PERM_U; ++u) {
+    const int i = base + u * PERM_NT;
+    if (i >= n_mono) continue;
+    const uint2 k = mkey[i];
+    if (k.x == KEY_NONE) continue;
+    const uint32_t pos = off[k.x] + k.y;
+    if (pos < n)
+      perm[pos] = MONO_BIT | static_cast<uint32_t>(i);
+    else
+      raise_error(err, ERR_KEY_MISMATCH, pos, k.x);
+  }
+}
+
 int scan_tile_count(int n_cells) { return (n_cells + SCAN_TILE - 1) / SCAN_TILE; }
 
 void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* grand,
@@ -189,6 +239,17 @@ void launch_scan(uint32_t* count, uint32_t* off, uint32_t* tile_sum, uint32_t* g
   const int per_block = SCAN_NT * SCAN_ADD_U;
   k_scan_add<<<(n_cells + 1 + per_block - 1) / per_block, SCAN_NT, 0, st>>>(off, tile_sum, grand,
                                                                            n_cells);
+}
+
+void launch_build_perm_packed(const Tile* tiles, int n_tiles, const RepInfo* reps,
+                              const uint32_t* keys, int n_slots, const uint2* mkey, int n_mono,
+                              const uint32_t* off, uint32_t* perm, ErrorState* err,
+                              cudaStream_t st) {
+  const int mono_blocks = (n_mono + PERM_NT * PERM_U - 1) / (PERM_NT * PERM_U);
+  if (n_tiles + mono_blocks == 0) return;
+  k_build_perm_packed<<<n_tiles + mono_blocks, PERM_NT, 0, st>>>(tiles, n_tiles, reps, keys,
+                                                                 n_slots, mkey, n_mono, off, perm,
+                                                                 err);
 }
 
 void launch_build_perm(const uint2* keys, int n_slots, const uint2* mkey, int n_mono,

@@ -47,6 +47,8 @@ struct smpc_ctx {
   Tile* d_col_tiles_v[3] = {nullptr, nullptr, nullptr};
   int n_col_tiles_v[3] = {0, 0, 0};
   int var_bin = 0, var_col = 0, var_md = 0, var_pmd = 0;
+  // FP32 fast path, every box at most 65,536 cells: 32-bit sort keys
+  bool packed_keys = false;
   std::vector<Tile> h_tmp_tiles;
   Tile* d_tmp_tiles = nullptr;
   TempPartial* d_tpart = nullptr;
@@ -201,6 +203,20 @@ int upload_host_dyn(smpc_ctx* ctx) {
 template <typename R>
 smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur);
 
+// the counting sort's scatter, from the keys the binning wrote
+void launch_permutation(smpc_ctx* ctx) {
+  if (ctx->packed_keys)
+    smpc::launch_build_perm_packed(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps,
+                                   reinterpret_cast<const uint32_t*>(ctx->d_keys),
+                                   static_cast<int>(ctx->total_slots), ctx->d_mkey,
+                                   static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm,
+                                   ctx->d_err, ctx->st);
+  else
+    smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
+                            static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->d_err,
+                            ctx->st);
+}
+
 template <typename R>
 int launch_binning(smpc_ctx* ctx, int cur) {
   const int strict = ctx->opt.strict_cells;
@@ -211,12 +227,11 @@ int launch_binning(smpc_ctx* ctx, int cur) {
                             ctx->rot_s, ctx->mono_chunks, ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
-                            ctx->opt.angular_momentum ? -1 : ctx->var_bin, ctx->st);
+                            ctx->opt.angular_momentum ? -1 : ctx->var_bin,
+                            ctx->packed_keys ? 1 : 0, ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
-  smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
-                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->d_err,
-                          ctx->st);
+  launch_permutation(ctx);
   return SMPC_OK;
 }
 
@@ -323,14 +338,13 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
   cudaEventRecord(ev[1 + PH_MONO], ctx->st);
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
-                            ctx->opt.angular_momentum ? -1 : ctx->var_bin, ctx->st);
+                            ctx->opt.angular_momentum ? -1 : ctx->var_bin,
+                            ctx->packed_keys ? 1 : 0, ctx->st);
   cudaEventRecord(ev[1 + PH_BIN], ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
   cudaEventRecord(ev[1 + PH_SCAN], ctx->st);
-  smpc::launch_build_perm(ctx->d_keys, static_cast<int>(ctx->total_slots), ctx->d_mkey,
-                          static_cast<int>(ctx->total_mono), ctx->d_off, ctx->d_perm, ctx->d_err,
-                          ctx->st);
+  launch_permutation(ctx);
   cudaEventRecord(ev[1 + PH_PERM], ctx->st);
   smpc::CollideArgs<R> a = collide_args<R>(ctx, smpc::RNG_PHILOX, cur);
   smpc::launch_collide<R>(a, ctx->st);
@@ -641,6 +655,8 @@ int create_buffers(smpc_ctx* ctx) {
   for (int k = 0; k < 2; ++k) CU(dalloc(reinterpret_cast<R**>(&ctx->d_rec[k]), 8 * S));
   CU(dalloc(&ctx->d_keys, S));
   CU(dalloc(&ctx->d_perm, S + M));
+  // a sorted position left unwritten (an error case) holds a valid index
+  CU(cudaMemset(ctx->d_perm, 0, (S + M) * sizeof(uint32_t)));
   CU(dalloc(&ctx->d_count, C));
   CU(cudaMemset(ctx->d_count, 0, C * sizeof(uint32_t)));
   CU(dalloc(&ctx->d_off, C + 1));
@@ -1110,6 +1126,9 @@ int smpc_create(const smpc_replica_desc* descs, int n_rep, const smpc_options* o
        (ctx->h_tmp_tiles.empty() || cudaMemcpy(ctx->d_tmp_tiles, ctx->h_tmp_tiles.data(), ctx->h_tmp_tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice) == cudaSuccess) &&
        cudaMemset(ctx->d_err, 0, sizeof(ErrorState)) == cudaSuccess;
   if (!ok) return bail(SMPC_E_CUDA, "upload");
+  ctx->packed_keys = fast_path(ctx);
+  for (const RepInfo& ri : ctx->reps)
+    if (ri.n_cell > 65536) ctx->packed_keys = false;
   if (fast_path(ctx)) {
     const int cells[3] = {64, 128, 256};
     for (int k = 0; k < 3; ++k) {

@@ -339,6 +339,32 @@ def test_fp32_launch_variants_agree_bitwise():
             np.testing.assert_array_equal(v0, v1)
 
 
+def test_fp32_packed_and_wide_sort_keys_agree_bitwise():
+    # Contexts whose boxes all have at most 65,536 cells sort with 32-bit keys
+    # (local cell << 16 | rank); a box of 41^3 cells sends its context to the
+    # (global cell, rank) pairs. The 12^3 box evolves to the same bits either way.
+    from starpolymersmd_gb300 import system
+    rng = np.random.default_rng(21)
+    small = system.uniform_fluid((12, 12, 12), 10, 1.0, rng)
+    big = system.uniform_fluid((41, 41, 41), 10, 1.0, rng)
+    reps = [dict(L=(12, 12, 12), n_fluid=len(small[0]), kT=1.0, shear=0.05, h=0.1, seed=7),
+            dict(L=(41, 41, 41), n_fluid=len(big[0]), kT=1.0, shear=0.02, h=0.1, seed=8)]
+    kw = dict(precision=capi.FP32, rng=capi.RNG_PHILOX, step_update=1, strict_cells=0)
+    out = []
+    for rs, states in ((reps[:1], [small]), (reps, [small, big])):
+        with capi.Context(rs, **kw) as ctx:
+            for k, (fp, fv) in enumerate(states):
+                ctx.set_fluid(k, fp, fv)
+            ctx.cycles(3)
+            ctx.raise_on_device_error()
+            out.append(ctx.get_fluid(0))
+            tot, fl = ctx.cell_counts(0)
+            fc, _ = ctx.cell_members(0)
+            np.testing.assert_array_equal(np.bincount(fc, minlength=len(tot)), fl)
+    for x, y in zip(*out):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_fp32_collide_variants_agree_bitwise_with_stars():
     # the same with monomers in the cells (staged from the monomer arrays,
     # written back to them), MD substeps in between
