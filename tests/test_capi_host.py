@@ -46,3 +46,4 @@ def test_binding_covers_the_header(lib_path):
 def test_library_is_sm103a_only(lib_path):
     # the build passes exactly one -gencode: compute_103a -> sm_103a
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
