@@ -836,6 +836,21 @@ __device__ __forceinline__ void load_particle(Particle<R>& P, uint32_t p, uint32
   finish_particle(P, p, C);
 }
 
+// Sign and finiteness tests of a per-particle value without FP64 compares:
+// on GB300 DSETP issues on the narrow FP64 pipe, the integer tests do not.
+// not_negative(x) is x >= 0 for every double: +0 up to +inf are the bit
+// patterns 0 .. 0x7FF0000000000000, and -0.0 compares equal to 0; NaNs and
+// negative numbers are false.
+__device__ __forceinline__ bool not_negative(float x) { return x >= 0.0f; }
+__device__ __forceinline__ bool not_negative(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  return b <= 0x7FF0000000000000ull || b == 0x8000000000000000ull;
+}
+__device__ __forceinline__ bool finite_bits(float x) { return isfinite(x); }
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
+}
+
 // Thermostat + rotation of one particle, then the unshift/wrap and store.
 template <typename R>
 __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, const R* s_cmv,
@@ -851,7 +866,7 @@ __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, cons
   R d0, d1, d2;
   if (std::is_same<R, double>::value) {
     // MPC.cpp:291 then MPC.cpp:267, in the reference's operation order
-    if (sc >= R(0)) {
+    if (not_negative(sc)) {
       vx = sc * vx + (R(1) - sc) * cm[0];
       vy = sc * vy + (R(1) - sc) * cm[1];
       vz = sc * vz + (R(1) - sc) * cm[2];
@@ -876,7 +891,7 @@ __device__ __forceinline__ void apply_collision(Particle<R>& P, uint32_t p, cons
     vy += w[2] * q0 - w[0] * q2;
     vz += w[0] * q1 - w[1] * q0;
   }
-  if (!(r_isfinite(vx) && r_isfinite(vy) && r_isfinite(vz)))
+  if (!(finite_bits(vx) && finite_bits(vy) && finite_bits(vz)))
     raise_error(err, ERR_NONFINITE, p, P.src);
   if (P.src & MONO_BIT) {
     const uint32_t m = P.src & ~MONO_BIT;
