@@ -357,13 +357,25 @@ void launch_pack_monomers<Real>(const Real* mpos, const Real* mvel, const Real* 
     k_pack_monomers<Real><<<(n + 255) / 256, 256, 0, st>>>(mpos, mvel, mfrc, n, pos, vel, frc);
 }
 
+// dynamic shared memory of k_md_cluster (the compacted force pass), opted in
+// once per cluster size
+template <int CS>
+static size_t md_cluster_smem() {
+  constexpr size_t bytes = MdcLayout<Real, CS>::bytes;
+  static const bool set = cudaFuncSetAttribute(k_md_cluster<Real, 256, CS, 8>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(bytes)) == cudaSuccess;
+  (void)set;
+  return bytes;
+}
+
 template <int CS>
 static cudaError_t launch_md_cluster_cs(const MdArgs& a, int n_rep, Real* mpos, Real* mvel,
                                         Real* mfrc, Real* mver, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(static_cast<unsigned>(n_rep * CS));
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = md_cluster_smem<CS>();
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -382,6 +394,7 @@ static int cluster_fits() {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CS);
   cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = md_cluster_smem<CS>();
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = CS;

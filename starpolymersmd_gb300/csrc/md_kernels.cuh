@@ -698,7 +698,62 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
 // of each bead's lanes: on the narrow FP64 pipe a warp instruction costs the
 // same with one active lane as with 32. Forces reach those threads through
 // shared memory.
+//
+// Pair forces are compacted. Most Verlet-list entries lie beyond the
+// interaction range, and with lanes per bead walking the lists a warp issued
+// each FP64 force instruction for the few lanes whose pair was in range (7.7
+// active lanes per instruction). Instead, the CTA keeps its beads' lists
+// flattened in shared memory (bead by bead, each in list order), and per
+// substep:
+//  1. every warp tests a contiguous run of entries in FP32 (positions kept
+//     in FP32 beside the FP64 copy) against the pair's cut-off widened by
+//     2^-7, and writes the entries that pass into a candidate list by ballot
+//     (the list stays in flattened order);
+//  2. all threads compute the candidates' FP64 pair forces, every lane busy,
+//     with the exact FP64 range test inside pair_force, and the bonds' FENE
+//     forces, one bond per thread;
+//  3. each bead's kick thread subtracts its pairs' contributions in list
+//     order, then its bonds' in bond order (Box.cpp:253-284).
+// The FP32 test only skips entries whose FP64 force is zero: FP32 rounding
+// of coordinates below 4096 moves r^2 by far less than the margin. A CTA whose
+// lists or bonds outgrow the shared buffers, or a replica with a coordinate
+// of 4096 or more, takes the lanes-per-bead pass instead.
 constexpr int MD_CLUSTER_CAP = 1024;
+constexpr int MDC_ECAP = 8192;  // flattened list entries of a CTA's beads
+constexpr int MDC_CCAP = 2048;  // candidate pairs per force batch
+constexpr int MDC_BCAP = 512;   // bonds of a CTA's beads
+constexpr float MDC_FAR = 4096.0f;
+
+// Dynamic shared memory of k_md_cluster<R, NT, CS, KMAX> (byte offsets).
+template <typename R, int CS>
+struct MdcLayout {
+  static constexpr int OWN = (MD_CLUSTER_CAP + CS - 1) / CS;  // beads per CTA at most
+  static constexpr size_t pf = 0;                                      // R[3 CCAP]
+  static constexpr size_t bf = pf + sizeof(R) * 3 * MDC_CCAP;          // R[3 BCAP]
+  static constexpr size_t xf = bf + sizeof(R) * 3 * MDC_BCAP;          // float[3 CAP], FP64 only
+  static constexpr size_t cand = xf + (sizeof(R) == 8 ? sizeof(float) * 3 * MD_CLUSTER_CAP : 0);
+  static constexpr size_t bj = cand + sizeof(int) * MDC_ECAP;          // int[BCAP]
+  static constexpr size_t lstart = bj + sizeof(int) * MDC_BCAP;        // int[OWN + 1]
+  static constexpr size_t cstart = lstart + sizeof(int) * (OWN + 1);   // int[OWN + 1]
+  static constexpr size_t bstart = cstart + sizeof(int) * (OWN + 1);   // int[OWN + 1]
+  static constexpr size_t ccnt = bstart + sizeof(int) * (OWN + 1);     // int[OWN]
+  static constexpr size_t nb = ccnt + sizeof(int) * OWN;               // uint16[ECAP]
+  static constexpr size_t own = nb + 2 * MDC_ECAP;                     // uint8[ECAP]
+  static constexpr size_t bq = own + MDC_ECAP;                         // uint8[BCAP]
+  static constexpr size_t bytes = bq + MDC_BCAP;
+  static_assert(OWN <= 256, "bead slot of a CTA fits one byte");
+};
+
+// inclusive warp scan
+__device__ __forceinline__ int md_warp_scan(int v) {
+  const int lane = static_cast<int>(threadIdx.x & 31u);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
 
 template <typename R, int NT, int CS, int KMAX>
 __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel, R* mfrc, R* mver) {
@@ -715,6 +770,29 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   __shared__ double s_epot[CS];
   __shared__ R s_f[3 * ((CAP + CS - 1) / CS)];  // forces of this CTA's beads
   static_assert((CAP + CS - 1) / CS <= NT, "a kick thread for every bead of the CTA");
+  constexpr int NW = NT / 32;
+  static_assert((NW & (NW - 1)) == 0, "a power of two of warps (candidate search)");
+  constexpr bool kF64 = sizeof(R) == 8;
+  using L = MdcLayout<R, CS>;
+  __shared__ int s_wcnt[NW], s_woff[NW + 1];
+  __shared__ int s_far, s_fits;  // replica-wide: a coordinate >= MDC_FAR; CTA: lists fit
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  R* s_pf = reinterpret_cast<R*>(s_dyn + L::pf);
+  R* s_bf = reinterpret_cast<R*>(s_dyn + L::bf);
+  float* s_xf = reinterpret_cast<float*>(s_dyn + L::xf);
+  int* s_cand = reinterpret_cast<int*>(s_dyn + L::cand);
+  int* s_bj = reinterpret_cast<int*>(s_dyn + L::bj);
+  int* s_lstart = reinterpret_cast<int*>(s_dyn + L::lstart);
+  int* s_cstart = reinterpret_cast<int*>(s_dyn + L::cstart);
+  int* s_bstart = reinterpret_cast<int*>(s_dyn + L::bstart);
+  int* s_ccnt = reinterpret_cast<int*>(s_dyn + L::ccnt);
+  unsigned short* s_nb = reinterpret_cast<unsigned short*>(s_dyn + L::nb);
+  unsigned char* s_own = s_dyn + L::own;
+  unsigned char* s_bq = s_dyn + L::bq;
+  // FP32 copy of the positions for the range pre-test
+  float* const pxf = kF64 ? s_xf : reinterpret_cast<float*>(sx);
+  float* const pyf = kF64 ? s_xf + CAP : reinterpret_cast<float*>(sy);
+  float* const pzf = kF64 ? s_xf + 2 * CAP : reinterpret_cast<float*>(sz);
   cg::cluster_group cl = cg::this_cluster();
   const int rank = static_cast<int>(cl.block_rank());
   const int cidx = static_cast<int>(blockIdx.x) / CS;
@@ -742,11 +820,80 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   const unsigned long long md_step0 = a.dyn[r].md_step;
 
   // every CTA: all positions and types; this lane: its bead's state
+  if (threadIdx.x == 0) { s_far = 0; s_fits = 0; }
+  __syncthreads();
   for (int j = threadIdx.x; j < n; j += NT) {
     const R4<R> p = ld4_rw(mpos, b + j);
     sx[j] = p.x; sy[j] = p.y; sz[j] = p.z;
+    if (kF64) {
+      pxf[j] = static_cast<float>(p.x); pyf[j] = static_cast<float>(p.y);
+      pzf[j] = static_cast<float>(p.z);
+    }
+    if (!(fabs(p.x) < R(MDC_FAR) && fabs(p.y) < R(MDC_FAR) && fabs(p.z) < R(MDC_FAR))) s_far = 1;
     s_amphi[j] = static_cast<unsigned char>(static_cast<int>(ld4_rw(mvel, b + j).w) & 1);
   }
+  for (int qq = threadIdx.x; qq < L::OWN; qq += NT) s_ccnt[qq] = 0;
+  // flattened bonds of this CTA's beads (bead slot, partner | anchor << 16)
+  bool bonds_fit = false;
+  if (threadIdx.x < 32) {
+    int carry = 0;
+    for (int q0 = 0; q0 < own; q0 += 32) {
+      const int qq = q0 + static_cast<int>(threadIdx.x);
+      const int cnt = qq < own ? a.bond_start[b + rank + CS * qq + 1] - a.bond_start[b + rank + CS * qq] : 0;
+      const int inc = md_warp_scan(cnt);
+      if (qq < own) s_bstart[qq] = carry + inc - cnt;
+      carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
+    }
+    if (threadIdx.x == 0) s_bstart[own] = carry;
+  }
+  __syncthreads();
+  bonds_fit = s_bstart[own] <= MDC_BCAP;
+  if (bonds_fit && static_cast<int>(threadIdx.x) < own) {
+    const int ib = rank + CS * static_cast<int>(threadIdx.x);
+    int o = s_bstart[threadIdx.x];
+    for (int e = a.bond_start[b + ib]; e < a.bond_start[b + ib + 1]; ++e, ++o) {
+      const int2 bd = a.bonds[e];
+      s_bj[o] = (bd.x - b) | (bd.y != 0 ? 0x10000 : 0);
+      s_bq[o] = static_cast<unsigned char>(threadIdx.x);
+    }
+  }
+  // The CTA's Verlet lists flattened into shared memory, bead by bead in list
+  // order, from the global lists (written by this CTA and synchronised).
+  auto flatten = [&]() {
+    if (threadIdx.x < 32) {
+      int carry = 0;
+      bool bad = false;
+      for (int q0 = 0; q0 < own; q0 += 32) {
+        const int qq = q0 + static_cast<int>(threadIdx.x);
+        int cnt = qq < own ? a.ncount[b + rank + CS * qq] : 0;
+        if (cnt < 0 || cnt > a.max_nb) { bad = true; cnt = 0; }
+        const int inc = md_warp_scan(cnt);
+        if (qq < own) s_lstart[qq] = carry + inc - cnt;
+        carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
+      }
+      bad = __any_sync(0xFFFFFFFFu, bad);
+      if (threadIdx.x == 0) {
+        s_lstart[own] = carry;
+        s_fits = !bad && carry <= MDC_ECAP;
+      }
+    }
+    __syncthreads();
+    if (s_fits) {
+      const int E = s_lstart[own];
+      const size_t stride = static_cast<size_t>(a.n_mono_total);
+      for (int k = threadIdx.x; k < E; k += NT) {
+        int lo = 0, hi = own - 1;  // the bead slot q with s_lstart[q] <= k < s_lstart[q + 1]
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_lstart[mid] <= k) lo = mid; else hi = mid - 1;
+        }
+        const int e = k - s_lstart[lo];
+        s_nb[k] = static_cast<unsigned short>(a.nlist[static_cast<size_t>(e) * stride + b + rank + CS * lo] - b);
+        s_own[k] = static_cast<unsigned char>(lo);
+      }
+    }
+    __syncthreads();
+  };
   // x: the position of this lane's bead in the force pass (from shared
   // memory); the bead's dynamic state lives with its kick thread
   R x[3] = {R(0), R(0), R(0)};
@@ -769,6 +916,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     s_core_ref[0] = c.x; s_core_ref[1] = c.y; s_core_ref[2] = c.z;
   }
   cl.sync();  // every copy loaded before any CTA writes into another's
+  if (!a.force_rebuild) flatten();  // (a forced rebuild flattens the new lists)
   int rebuilds = 0;
   double epot = 0.0;
   const int total_steps = a.n_steps > 0 ? a.n_steps : 1;
@@ -786,11 +934,22 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
           const R d0 = xk[0] - xv[0], d1 = xk[1] - xv[1], d2 = xk[2] - xv[2];
           over = r_sqrt((d0 * d0 + d1 * d1) + d2 * d2) > lim;
         }
-        for (int c = 0; c < CS; ++c) {
+        const bool far = !(fabs(xk[0]) < R(MDC_FAR) && fabs(xk[1]) < R(MDC_FAR) &&
+                           fabs(xk[2]) < R(MDC_FAR));
+        const float f0 = static_cast<float>(xk[0]), f1 = static_cast<float>(xk[1]),
+                    f2 = static_cast<float>(xk[2]);
+#pragma unroll 1
+        for (int c = 0; c < CS; ++c) {  // (rolled: no remote addresses held across the substep)
           cl.map_shared_rank(sx, c)[ik] = xk[0];
           cl.map_shared_rank(sy, c)[ik] = xk[1];
           cl.map_shared_rank(sz, c)[ik] = xk[2];
+          if (kF64) {
+            cl.map_shared_rank(pxf, c)[ik] = f0;
+            cl.map_shared_rank(pyf, c)[ik] = f1;
+            cl.map_shared_rank(pzf, c)[ik] = f2;
+          }
           if (over) *cl.map_shared_rank(&s_rebuild, c) = 1;
+          if (far) *cl.map_shared_rank(&s_far, c) = 1;
         }
       }
     }
@@ -824,38 +983,218 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       __syncthreads();
       md_sort_chains(s_head, s_next, NT);
       __syncthreads();
-      if (mine && lead) {
-        const int cx = static_cast<int>(floor(x[0] * inv_rv));
-        const int cy = static_cast<int>(floor(x[1] * inv_rv));
-        const int cz = static_cast<int>(floor(x[2] * inv_rv));
+      // Lists: the lanes of a bead split its 27 cells (cell t to lane t mod
+      // lanes), count their members, then write them at the offsets the
+      // counts give, so a list holds lane 0's cells, then lane 1's, and so
+      // on. Membership is d^2 <= r_v^2 in the state's precision; FP64 states
+      // decide it in FP32 outside a band of 2^-7 around r_v^2 (FP32 rounding
+      // of coordinates below MDC_FAR moves d^2 by far less) and in FP64
+      // inside it.
+      const int nl = 1 << lk;
+      const bool fast = kF64 && !s_far;
+      const float rv2_lo = static_cast<float>(rv2) * (1.0f - 0.0078125f);
+      const float rv2_hi = static_cast<float>(rv2) * (1.0f + 0.0078125f);
+      int ccx = 0, ccy = 0, ccz = 0;
+      float xf0 = 0.f, xf1 = 0.f, xf2 = 0.f;
+      if (mine) {
+        ccx = static_cast<int>(floor(x[0] * inv_rv));
+        ccy = static_cast<int>(floor(x[1] * inv_rv));
+        ccz = static_cast<int>(floor(x[2] * inv_rv));
+        xf0 = pxf[i]; xf1 = pyf[i]; xf2 = pzf[i];
+      }
+      // members of this lane's cells: counted (pos < 0) or written from pos
+      auto walk = [&](int pos) -> int {
         int cnt = 0;
-        for (int dz = -1; dz <= 1; ++dz)
-          for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) {
-              const int tx = cx + dx, ty = cy + dy, tz = cz + dz;
-              const int want = md_cell_key(tx, ty, tz);
-              for (int j = s_head[md_bucket(tx, ty, tz)]; j >= 0; j = s_next[j]) {
-                if (j == i || s_ckey[j] != want) continue;
-                const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
-                if ((d0 * d0 + d1 * d1) + d2 * d2 <= rv2) {
-                  if (cnt < a.max_nb) a.nlist[static_cast<size_t>(cnt) * a.n_mono_total + b + i] = b + j;
-                  ++cnt;
+        for (int t = sub; t < 27; t += nl) {
+          const int tx = ccx + t % 3 - 1, ty = ccy + (t / 3) % 3 - 1, tz = ccz + t / 9 - 1;
+          const int want = md_cell_key(tx, ty, tz);
+          for (int j = s_head[md_bucket(tx, ty, tz)]; j >= 0; j = s_next[j]) {
+            if (j == i || s_ckey[j] != want) continue;
+            bool in;
+            float r2f = 0.f;
+            if (fast) {
+              const float e0 = pxf[j] - xf0, e1 = pyf[j] - xf1, e2 = pzf[j] - xf2;
+              r2f = fmaf(e0, e0, fmaf(e1, e1, e2 * e2));
+            }
+            if (fast && r2f < rv2_lo) {
+              in = true;
+            } else if (fast && r2f > rv2_hi) {
+              in = false;
+            } else {
+              const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
+              in = (d0 * d0 + d1 * d1) + d2 * d2 <= rv2;
+            }
+            if (!in) continue;
+            if (pos >= 0) {
+              const int k = pos + cnt;
+              if (k < a.max_nb) {
+                a.nlist[static_cast<size_t>(k) * a.n_mono_total + b + i] = b + j;
+                if (s_fits) {
+                  s_nb[s_lstart[q] + k] = static_cast<unsigned short>(j);
+                  s_own[s_lstart[q] + k] = static_cast<unsigned char>(q);
                 }
               }
             }
+            ++cnt;
+          }
+        }
+        return cnt;
+      };
+      const int mc = mine ? walk(-1) : 0;
+      int inc = mc;  // the bead's lanes are adjacent: segments of nl lanes
+      for (int o = 1; o < nl; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, inc, o, nl);
+        if (sub >= o) inc += t;
+      }
+      const int total = __shfl_sync(0xFFFFFFFFu, inc, nl - 1, nl);
+      if (mine && lead) {
+        int cnt = total;
         if (cnt > a.max_nb) {
           raise_error(a.err, ERR_NEIGHBOR_OVF, static_cast<uint32_t>(b + i),
                       static_cast<uint32_t>(cnt));
           cnt = a.max_nb;
         }
         a.ncount[b + i] = cnt;
+        s_cstart[q] = cnt;
       }
+      __syncthreads();
+      if (threadIdx.x < 32) {  // list starts of the CTA's beads
+        int carry = 0;
+        for (int q0 = 0; q0 < own; q0 += 32) {
+          const int qq = q0 + static_cast<int>(threadIdx.x);
+          const int cnt = qq < own ? s_cstart[qq] : 0;
+          const int ci = md_warp_scan(cnt);
+          if (qq < own) s_lstart[qq] = carry + ci - cnt;
+          carry += __shfl_sync(0xFFFFFFFFu, ci, 31);
+        }
+        if (threadIdx.x == 0) {
+          s_lstart[own] = carry;
+          s_fits = carry <= MDC_ECAP;
+        }
+      }
+      __syncthreads();
+      if (mine) walk(inc - mc);
       if (kicker) { xv[0] = xk[0]; xv[1] = xk[1]; xv[2] = xk[2]; }
       if (threadIdx.x == 0) { s_core_ref[0] = sx[0]; s_core_ref[1] = sy[0]; s_core_ref[2] = sz[0]; }
       __syncthreads();  // lists written before the lanes of a bead read them
     }
     const bool want_epot = a.calc_epot && (step == total_steps - 1);
     // forces (Box.cpp:243-286)
+    if (bonds_fit && s_fits && !s_far) {
+      // 1. candidates, by warp over contiguous runs of the flattened lists
+      const int E = s_lstart[own];
+      const int w = static_cast<int>(threadIdx.x >> 5), lane = static_cast<int>(threadIdx.x & 31u);
+      const int per = (E + NW - 1) / NW;
+      const int k0 = w * per, k1 = min(E, k0 + per);
+      const float widen = 1.0f + 0.0078125f;
+      const float cut_aa = (pot == POT_REF4824 ? 1.0594631f : 1.2599211f) * widen;
+      const float cut_bb = (pot == POT_REF4824 ? 2.25f : 6.25f) * widen;
+      int nw = 0;
+      for (int kb = k0; kb < k1; kb += 32) {
+        const int k = kb + lane;
+        bool cand = false;
+        int pk = 0, qk = 0;
+        if (k < k1) {
+          qk = s_own[k];
+          const int j = s_nb[k], ii = rank + CS * qk;
+          const float d0 = pxf[j] - pxf[ii], d1 = pyf[j] - pyf[ii], d2 = pzf[j] - pzf[ii];
+          const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+          cand = r2 < ((s_amphi[ii] != 0 && s_amphi[j] != 0) ? cut_bb : cut_aa);
+          pk = (qk << 10) | j;
+        }
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, cand);
+        if (cand) {
+          s_cand[k0 + nw + __popc(m & ((1u << lane) - 1u))] = pk;
+          atomicAdd(&s_ccnt[qk], 1);
+        }
+        nw += __popc(m);
+      }
+      if (lane == 0) s_wcnt[w] = nw;
+      __syncthreads();
+      if (threadIdx.x < 32) {  // candidate offsets by warp and by bead
+        const int v = lane < NW ? s_wcnt[lane] : 0;
+        const int inc = md_warp_scan(v);
+        if (lane < NW) s_woff[lane] = inc - v;
+        if (lane == NW - 1) s_woff[NW] = inc;
+        int carry = 0;
+        for (int q0 = 0; q0 < own; q0 += 32) {
+          const int qq = q0 + lane;
+          const int c = qq < own ? s_ccnt[qq] : 0;
+          const int ci = md_warp_scan(c);
+          if (qq < own) { s_cstart[qq] = carry + ci - c; s_ccnt[qq] = 0; }
+          carry += __shfl_sync(0xFFFFFFFFu, ci, 31);
+        }
+        if (lane == 0) s_cstart[own] = carry;
+      }
+      __syncthreads();
+      const int C = s_woff[NW];
+      R F0 = R(0), F1 = R(0), F2 = R(0);
+      for (int c0 = 0; c0 == 0 || c0 < C; c0 += MDC_CCAP) {
+        const int c1 = min(C, c0 + MDC_CCAP);
+        // 2. FP64 pair forces of the candidates, then the bonds (first batch)
+        for (int c = c0 + static_cast<int>(threadIdx.x); c < c1; c += NT) {
+          int wc = 0;
+#pragma unroll
+          for (int st = NW / 2; st > 0; st >>= 1)
+            if (wc + st < NW && s_woff[wc + st] <= c) wc += st;
+          const int pk = s_cand[wc * per + (c - s_woff[wc])];
+          const int qk = pk >> 10, j = pk & 1023, ii = rank + CS * qk;
+          const R d0 = sx[j] - sx[ii], d1 = sy[j] - sy[ii], d2 = sz[j] - sz[ii];
+          const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+          const bool bb = s_amphi[ii] != 0 && s_amphi[j] != 0;
+          const R fa = pair_force<R>(pot, bb, r2, lambda);
+          R* o = s_pf + 3 * (c - c0);
+          o[0] = d0 * fa;
+          o[1] = d1 * fa;
+          o[2] = d2 * fa;
+          if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
+        }
+        if (c0 == 0) {
+          for (int e = threadIdx.x; e < s_bstart[own]; e += NT) {
+            const int ii = rank + CS * s_bq[e], j = s_bj[e] & 0xFFFF;
+            const bool anch = (s_bj[e] >> 16) != 0;
+            const R d0 = sx[j] - sx[ii], d1 = sy[j] - sy[ii], d2 = sz[j] - sz[ii];
+            const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+            R r2f = r2;
+            if (pot == POT_REF4824) {
+              if (r2 >= (anch ? R(20.25) : R(2.25)))
+                raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + ii), static_cast<uint32_t>(b + j));
+            } else {
+              const R cap = (anch ? R(20.25) : R(2.25)) * R(0.98);
+              if (r2f > cap) r2f = cap;
+            }
+            const R fa = fene_force<R>(anch, r2f);
+            R* o = s_bf + 3 * e;
+            o[0] = d0 * fa;
+            o[1] = d1 * fa;
+            o[2] = d2 * fa;
+            if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2f));
+          }
+        }
+        __syncthreads();
+        // 3. each bead's pairs in list order
+        if (kicker) {
+          const int e1 = min(s_cstart[kq + 1], c1);
+          for (int c = max(s_cstart[kq], c0); c < e1; ++c) {
+            const R* o = s_pf + 3 * (c - c0);
+            F0 -= o[0];
+            F1 -= o[1];
+            F2 -= o[2];
+          }
+        }
+        __syncthreads();  // read before the next batch rewrites the buffer
+      }
+      if (kicker) {  // then its bonds in bond order
+        for (int e = s_bstart[kq]; e < s_bstart[kq + 1]; ++e) {
+          F0 -= s_bf[3 * e];
+          F1 -= s_bf[3 * e + 1];
+          F2 -= s_bf[3 * e + 2];
+        }
+        s_f[3 * kq] = F0;
+        s_f[3 * kq + 1] = F1;
+        s_f[3 * kq + 2] = F2;
+      }
+    } else {
     R F0 = R(0), F1 = R(0), F2 = R(0);
     if (mine) {
       const bool ai = s_amphi[i] != 0;
@@ -914,6 +1253,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       s_f[3 * q] = F0;
       s_f[3 * q + 1] = F1;
       s_f[3 * q + 2] = F2;
+    }
     }
     __syncthreads();  // the forces reach the kick threads
     if (kicker) {
