@@ -681,13 +681,14 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
 // SMs), for boxes with few replicas: one CTA's FP64 pipe (2 DFMA per clock
 // per SM on this part) held a 401-bead star's FP64 MD to 150 us per substep.
 // Every CTA keeps a copy of all positions in its shared memory and owns the
-// beads i = rank + CS q; after its drift a bead's lead lane stores the new
+// beads i = rank + CS q; after its drift a bead's kick thread stores the new
 // position into every CTA's copy (distributed shared memory) and, when the
-// bead moved past the Verlet limit, sets every CTA's rebuild flag. Two
-// cluster barriers per substep: after the drift (positions and flags
-// complete everywhere) and after the forces (no copy is rewritten while it
-// is read). A rebuild hashes all beads in every CTA's own grid; each CTA
-// writes the lists of its own beads. Forces, kicks and the Andersen resets
+// bead moved past the Verlet limit, sets every CTA's rebuild flag. The
+// copies are double-buffered by substep parity, so one cluster barrier per
+// substep, after the drift, suffices (positions and flags complete
+// everywhere); with displacements measured relative to the core, every CTA
+// decides the rebuild for all beads itself. A rebuild hashes all beads in
+// every CTA's own grid; each CTA writes the lists of its own beads. Forces, kicks and the Andersen resets
 // are those of k_md_substeps for the owned beads (lanes per bead as there).
 // The barriers are hardware cluster barriers: every CTA of a cluster runs
 // at once, and every CTA reaches every barrier (all branches around them
@@ -720,7 +721,7 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
 // of 4096 or more, takes the lanes-per-bead pass instead.
 constexpr int MD_CLUSTER_CAP = 1024;
 constexpr int MDC_ECAP = 8192;  // flattened list entries of a CTA's beads
-constexpr int MDC_CCAP = 2048;  // candidate pairs per force batch
+constexpr int MDC_CCAP = 1024;  // candidate pairs per force batch
 constexpr int MDC_BCAP = 512;   // bonds of a CTA's beads
 constexpr float MDC_FAR = 4096.0f;
 
@@ -728,10 +729,12 @@ constexpr float MDC_FAR = 4096.0f;
 template <typename R, int CS>
 struct MdcLayout {
   static constexpr int OWN = (MD_CLUSTER_CAP + CS - 1) / CS;  // beads per CTA at most
-  static constexpr size_t pf = 0;                                      // R[3 CCAP]
+  static constexpr size_t posr = 0;                                    // R[2][3][CAP] positions
+  static constexpr size_t posf = posr + sizeof(R) * 6 * MD_CLUSTER_CAP;  // float[2][3][CAP], FP64 only
+  static constexpr size_t xvf = posf + (sizeof(R) == 8 ? sizeof(float) * 6 * MD_CLUSTER_CAP : 0);
+  static constexpr size_t pf = xvf + sizeof(float) * 3 * MD_CLUSTER_CAP;  // R[3 CCAP]
   static constexpr size_t bf = pf + sizeof(R) * 3 * MDC_CCAP;          // R[3 BCAP]
-  static constexpr size_t xf = bf + sizeof(R) * 3 * MDC_BCAP;          // float[3 CAP], FP64 only
-  static constexpr size_t cand = xf + (sizeof(R) == 8 ? sizeof(float) * 3 * MD_CLUSTER_CAP : 0);
+  static constexpr size_t cand = bf + sizeof(R) * 3 * MDC_BCAP;        // int[ECAP]
   static constexpr size_t bj = cand + sizeof(int) * MDC_ECAP;          // int[BCAP]
   static constexpr size_t lstart = bj + sizeof(int) * MDC_BCAP;        // int[OWN + 1]
   static constexpr size_t cstart = lstart + sizeof(int) * (OWN + 1);   // int[OWN + 1]
@@ -759,13 +762,13 @@ template <typename R, int NT, int CS, int KMAX>
 __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel, R* mfrc, R* mver) {
   namespace cg = cooperative_groups;
   constexpr int CAP = MD_CLUSTER_CAP;
-  __shared__ R sx[CAP], sy[CAP], sz[CAP];
   __shared__ unsigned char s_amphi[CAP];
   __shared__ int s_head[MD_BUCKETS];
   __shared__ int s_next[CAP];
   __shared__ int s_ckey[CAP];
-  __shared__ R s_core_ref[3];
-  __shared__ int s_rebuild;
+  __shared__ float s_coref[3];      // the core's position at the last rebuild (FP32)
+  __shared__ int s_rebuild[2];      // by substep parity: a bead passed the Verlet limit
+  __shared__ int s_farp[2];         // by substep parity: a coordinate reached MDC_FAR
   __shared__ double s_red[NT / 32];
   __shared__ double s_epot[CS];
   __shared__ R s_f[3 * ((CAP + CS - 1) / CS)];  // forces of this CTA's beads
@@ -775,11 +778,17 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   constexpr bool kF64 = sizeof(R) == 8;
   using L = MdcLayout<R, CS>;
   __shared__ int s_wcnt[NW], s_woff[NW + 1];
-  __shared__ int s_far, s_fits;  // replica-wide: a coordinate >= MDC_FAR; CTA: lists fit
+  __shared__ int s_far, s_fits;  // replica-wide: a coordinate >= MDC_FAR so far; CTA: lists fit
   extern __shared__ __align__(16) unsigned char s_dyn[];
+  // Positions, double-buffered by substep parity: substep s pushes into and
+  // reads from buffer s & 1, so one cluster barrier per substep suffices (a
+  // CTA pushing substep s + 1 has passed the barrier of substep s, which
+  // every CTA reached after its last read of buffer (s + 1) & 1).
+  R* const s_posr = reinterpret_cast<R*>(s_dyn + L::posr);
+  float* const s_posf = reinterpret_cast<float*>(s_dyn + L::posf);
+  float* const s_xvf = reinterpret_cast<float*>(s_dyn + L::xvf);  // Verlet reference positions
   R* s_pf = reinterpret_cast<R*>(s_dyn + L::pf);
   R* s_bf = reinterpret_cast<R*>(s_dyn + L::bf);
-  float* s_xf = reinterpret_cast<float*>(s_dyn + L::xf);
   int* s_cand = reinterpret_cast<int*>(s_dyn + L::cand);
   int* s_bj = reinterpret_cast<int*>(s_dyn + L::bj);
   int* s_lstart = reinterpret_cast<int*>(s_dyn + L::lstart);
@@ -789,10 +798,6 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   unsigned short* s_nb = reinterpret_cast<unsigned short*>(s_dyn + L::nb);
   unsigned char* s_own = s_dyn + L::own;
   unsigned char* s_bq = s_dyn + L::bq;
-  // FP32 copy of the positions for the range pre-test
-  float* const pxf = kF64 ? s_xf : reinterpret_cast<float*>(sx);
-  float* const pyf = kF64 ? s_xf + CAP : reinterpret_cast<float*>(sy);
-  float* const pzf = kF64 ? s_xf + 2 * CAP : reinterpret_cast<float*>(sz);
   cg::cluster_group cl = cg::this_cluster();
   const int rank = static_cast<int>(cl.block_rank());
   const int cidx = static_cast<int>(blockIdx.x) / CS;
@@ -820,14 +825,25 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   const unsigned long long md_step0 = a.dyn[r].md_step;
 
   // every CTA: all positions and types; this lane: its bead's state
-  if (threadIdx.x == 0) { s_far = 0; s_fits = 0; }
+  if (threadIdx.x == 0) {
+    s_far = 0; s_fits = 0;
+    s_farp[0] = s_farp[1] = 0;
+    s_rebuild[0] = a.force_rebuild; s_rebuild[1] = 0;
+  }
   __syncthreads();
-  for (int j = threadIdx.x; j < n; j += NT) {
+  for (int j = threadIdx.x; j < n; j += NT) {  // into buffer 0 (substep 0 reads it)
     const R4<R> p = ld4_rw(mpos, b + j);
-    sx[j] = p.x; sy[j] = p.y; sz[j] = p.z;
+    s_posr[j] = p.x; s_posr[CAP + j] = p.y; s_posr[2 * CAP + j] = p.z;
     if (kF64) {
-      pxf[j] = static_cast<float>(p.x); pyf[j] = static_cast<float>(p.y);
-      pzf[j] = static_cast<float>(p.z);
+      s_posf[j] = static_cast<float>(p.x); s_posf[CAP + j] = static_cast<float>(p.y);
+      s_posf[2 * CAP + j] = static_cast<float>(p.z);
+    }
+    const R4<R> pv = ld4_rw(mver, b + j);
+    s_xvf[j] = static_cast<float>(pv.x); s_xvf[CAP + j] = static_cast<float>(pv.y);
+    s_xvf[2 * CAP + j] = static_cast<float>(pv.z);
+    if (j == 0) {
+      s_coref[0] = static_cast<float>(pv.x); s_coref[1] = static_cast<float>(pv.y);
+      s_coref[2] = static_cast<float>(pv.z);
     }
     if (!(fabs(p.x) < R(MDC_FAR) && fabs(p.y) < R(MDC_FAR) && fabs(p.z) < R(MDC_FAR))) s_far = 1;
     s_amphi[j] = static_cast<unsigned char>(static_cast<int>(ld4_rw(mvel, b + j).w) & 1);
@@ -910,17 +926,20 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     f[0] = ff.x; f[1] = ff.y; f[2] = ff.z;
     xv[0] = pv.x; xv[1] = pv.y; xv[2] = pv.z;
   }
-  if (threadIdx.x == 0) {
-    s_rebuild = a.force_rebuild;
-    const R4<R> c = ld4_rw(mver, b);
-    s_core_ref[0] = c.x; s_core_ref[1] = c.y; s_core_ref[2] = c.z;
-  }
   cl.sync();  // every copy loaded before any CTA writes into another's
   if (!a.force_rebuild) flatten();  // (a forced rebuild flattens the new lists)
   int rebuilds = 0;
   double epot = 0.0;
   const int total_steps = a.n_steps > 0 ? a.n_steps : 1;
   for (int step = 0; step < total_steps; ++step) {
+    const int cur = step & 1;
+    R* const sx = s_posr + cur * 3 * CAP;
+    R* const sy = sx + CAP;
+    R* const sz = sy + CAP;
+    // FP32 positions for the range pre-tests (the state itself in FP32)
+    float* const pxf = kF64 ? s_posf + cur * 3 * CAP : reinterpret_cast<float*>(sx);
+    float* const pyf = pxf + CAP;
+    float* const pzf = pyf + CAP;
     if (a.n_steps > 0 && kicker) {
       // kick + drift (Thermostat_None.cpp:22-27); the force lanes read the
       // new position from shared memory after the barrier
@@ -948,26 +967,41 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
             cl.map_shared_rank(pyf, c)[ik] = f1;
             cl.map_shared_rank(pzf, c)[ik] = f2;
           }
-          if (over) *cl.map_shared_rank(&s_rebuild, c) = 1;
-          if (far) *cl.map_shared_rank(&s_far, c) = 1;
+          if (over) *cl.map_shared_rank(&s_rebuild[cur], c) = 1;
+          if (far) *cl.map_shared_rank(&s_farp[cur], c) = 1;
         }
       }
     }
-    cl.sync();  // positions and rebuild flags complete in every CTA
+    cl.sync();  // positions and flags of this substep complete in every CTA
     if (mine) { x[0] = sx[i]; x[1] = sy[i]; x[2] = sz[i]; }
+    const bool far_now = s_far || s_farp[cur];
+    bool over_here = s_rebuild[cur] != 0;
     if (a.core_relative && a.n_steps > 0) {
-      // displacements relative to the core's (see k_md_substeps)
-      const R c0 = sx[0] - s_core_ref[0], c1 = sy[0] - s_core_ref[1], c2 = sz[0] - s_core_ref[2];
-      if (kicker) {
-        const R d0 = xk[0] - xv[0] - c0, d1 = xk[1] - xv[1] - c1, d2 = xk[2] - xv[2] - c2;
-        if ((d0 * d0 + d1 * d1) + d2 * d2 > lim * lim)
-          for (int c = 0; c < CS; ++c) *cl.map_shared_rank(&s_rebuild, c) = 1;
+      // Displacements relative to the core's (see k_md_substeps), decided by
+      // every CTA for every bead from the same FP32 positions, so all CTAs
+      // agree without a second cluster barrier. FP32 states compare with
+      // lim^2 as k_md_substeps; FP64 states with (lim - 2e-3)^2, which
+      // covers the FP32 rounding of coordinates below MDC_FAR (a rebuild a
+      // little early keeps the lists valid), and rebuild at every substep
+      // once a coordinate reaches MDC_FAR.
+      const float limf = static_cast<float>(lim);
+      const float thr = !kF64 ? limf * limf : (limf > 2e-3f ? (limf - 2e-3f) * (limf - 2e-3f) : 0.0f);
+      if (kF64 && far_now) {
+        over_here = true;
+      } else {
+        const float c0 = pxf[0] - s_coref[0], c1 = pyf[0] - s_coref[1], c2 = pzf[0] - s_coref[2];
+        for (int j = threadIdx.x; j < n; j += NT) {
+          const float d0 = pxf[j] - s_xvf[j] - c0, d1 = pyf[j] - s_xvf[CAP + j] - c1,
+                      d2 = pzf[j] - s_xvf[2 * CAP + j] - c2;
+          if ((d0 * d0 + d1 * d1) + d2 * d2 > thr) over_here = true;
+        }
       }
-      cl.sync();
     }
-    const int rebuild = s_rebuild;  // the same in every CTA
-    __syncthreads();
-    if (threadIdx.x == 0) s_rebuild = 0;  // set again only after the next drift
+    const int rebuild = __syncthreads_or(over_here);  // the same in every CTA
+    if (threadIdx.x == 0) {  // set again by the pushes of substep step + 2
+      s_rebuild[cur] = 0;
+      if (far_now) s_far = 1;
+    }
     if (rebuild) {
       ++rebuilds;
       const R inv_rv = R(1) / static_cast<R>(ri.r_verlet);
@@ -991,7 +1025,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       // of coordinates below MDC_FAR moves d^2 by far less) and in FP64
       // inside it.
       const int nl = 1 << lk;
-      const bool fast = kF64 && !s_far;
+      const bool fast = kF64 && !far_now;
       const float rv2_lo = static_cast<float>(rv2) * (1.0f - 0.0078125f);
       const float rv2_hi = static_cast<float>(rv2) * (1.0f + 0.0078125f);
       int ccx = 0, ccy = 0, ccz = 0;
@@ -1075,12 +1109,15 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       __syncthreads();
       if (mine) walk(inc - mc);
       if (kicker) { xv[0] = xk[0]; xv[1] = xk[1]; xv[2] = xk[2]; }
-      if (threadIdx.x == 0) { s_core_ref[0] = sx[0]; s_core_ref[1] = sy[0]; s_core_ref[2] = sz[0]; }
+      for (int j = threadIdx.x; j < n; j += NT) {
+        s_xvf[j] = pxf[j]; s_xvf[CAP + j] = pyf[j]; s_xvf[2 * CAP + j] = pzf[j];
+      }
+      if (threadIdx.x == 0) { s_coref[0] = pxf[0]; s_coref[1] = pyf[0]; s_coref[2] = pzf[0]; }
       __syncthreads();  // lists written before the lanes of a bead read them
     }
     const bool want_epot = a.calc_epot && (step == total_steps - 1);
     // forces (Box.cpp:243-286)
-    if (bonds_fit && s_fits && !s_far) {
+    if (bonds_fit && s_fits && !far_now) {
       // 1. candidates, by warp over contiguous runs of the flattened lists
       const int E = s_lstart[own];
       const int w = static_cast<int>(threadIdx.x >> 5), lane = static_cast<int>(threadIdx.x & 31u);
@@ -1278,7 +1315,6 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         }
       }
     }
-    cl.sync();  // every CTA is done reading positions before the next drift rewrites them
   }
   if (kicker) {
     R4<R> p = ld4_rw(mpos, b + ik);
