@@ -355,31 +355,68 @@ __device__ __forceinline__ int md_bucket(int cx, int cy, int cz) {
          (MD_BUCKETS - 1);
 }
 
-// The hash chains are built with atomicExch, so each comes out in the order
-// the insertions happened to run, which differs between runs once a replica
-// spans several warps. Putting every chain in ascending bead order (one
-// thread per bucket, insertion sort of a short list) makes the Verlet lists,
-// and with them the force sums, the same bits in every run.
-__device__ __forceinline__ void md_sort_chains(int* s_head, int* s_next, int nt) {
-  for (int q = threadIdx.x; q < MD_BUCKETS; q += nt) {
-    int j = s_head[q];
-    if (j < 0 || s_next[j] < 0) continue;  // empty, or one bead
-    int sorted = -1;
-    while (j >= 0) {
-      const int nxt = s_next[j];
-      if (sorted < 0 || j < sorted) {
-        s_next[j] = sorted;
-        sorted = j;
-      } else {
-        int p = sorted;
-        while (s_next[p] >= 0 && s_next[p] < j) p = s_next[p];
-        s_next[j] = s_next[p];
-        s_next[p] = j;
-      }
-      j = nxt;
-    }
-    s_head[q] = sorted;
+// inclusive warp scan
+__device__ __forceinline__ int md_warp_scan(int v) {
+  const int lane = static_cast<int>(threadIdx.x & 31u);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= o) v += t;
   }
+  return v;
+}
+
+// Beads in bucket order, each bucket in ascending bead order (the order the
+// sorted chains give), as a counting sort: one warp ranks the beads within
+// their buckets in bead order, 32 at a time (__match_any_sync groups a
+// batch's beads by bucket), the block scans the counts, and every bead goes
+// to its bucket's start plus its rank. s_bkt[j]: bucket of bead j, set by
+// the caller (the rank is packed beside it: bucket | rank << 11);
+// s_start[MD_BUCKETS + 1]: bucket starts; s_sorted[k]: the k-th bead. Ends
+// with the block synchronised. A cell's members are then a contiguous run to
+// scan, not a chain of dependent loads.
+template <int NT>
+__device__ __forceinline__ void md_bucket_sort(int n, int* s_bkt, int* s_start, int* s_sorted) {
+  static_assert(MD_BUCKETS == 2048, "11-bit bucket field");
+  static_assert(MD_BUCKETS % NT == 0 && NT % 32 == 0, "bucket scan layout");
+  constexpr int PER = MD_BUCKETS / NT;
+  for (int t = threadIdx.x; t <= MD_BUCKETS; t += NT) s_start[t] = 0;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const unsigned lane = threadIdx.x;
+    for (int j0 = 0; j0 < n; j0 += 32) {
+      const int j = j0 + static_cast<int>(lane);
+      const int bk = j < n ? s_bkt[j] : -1 - static_cast<int>(lane);
+      const unsigned peers = __match_any_sync(0xFFFFFFFFu, bk);
+      const int leader = __ffs(peers) - 1;
+      int base = 0;
+      if (j < n && static_cast<int>(lane) == leader) {
+        base = s_start[bk];
+        s_start[bk] = base + __popc(peers);
+      }
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (j < n) s_bkt[j] = bk | ((base + __popc(peers & ((1u << lane) - 1u))) << 11);
+    }
+  }
+  __syncthreads();
+  {  // exclusive scan of the counts: PER consecutive buckets per thread
+    __shared__ int s_wsum[NT / 32];
+    int c[PER], tot = 0;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) { c[u] = s_start[PER * threadIdx.x + u]; tot += c[u]; }
+    const int inc = md_warp_scan(tot);
+    if ((threadIdx.x & 31u) == 31u) s_wsum[threadIdx.x >> 5] = inc;
+    __syncthreads();
+    int wbase = 0;
+    for (int w = 0; w < static_cast<int>(threadIdx.x >> 5); ++w) wbase += s_wsum[w];
+    int run = wbase + inc - tot;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) { s_start[PER * threadIdx.x + u] = run; run += c[u]; }
+    if (threadIdx.x == NT - 1) s_start[MD_BUCKETS] = run;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < n; j += NT) s_sorted[s_start[s_bkt[j] & 2047] + (s_bkt[j] >> 11)] = j;
+  __syncthreads();
 }
 
 // The 512-thread lanes-per-bead shape is held to 64 registers so that two of
@@ -391,9 +428,10 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
   constexpr int CAP = NT * MPT;
   __shared__ R sx[CAP], sy[CAP], sz[CAP];
   __shared__ unsigned char s_amphi[CAP];
-  __shared__ int s_head[MD_BUCKETS];
-  __shared__ int s_next[CAP];
+  __shared__ int s_head[MD_BUCKETS + 1];  // bucket starts in s_sorted
+  __shared__ int s_next[CAP];             // bucket of each bead
   __shared__ int s_ckey[CAP];
+  __shared__ int s_sorted[CAP];
   __shared__ R s_core_ref[3];
   __shared__ int s_rebuild;
   __shared__ int s_lowe_total;
@@ -490,8 +528,6 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
       // through a hashed grid of side r_verlet in shared memory
       ++rebuilds;
       const R inv_rv = R(1) / static_cast<R>(ri.r_verlet);
-      for (int q = threadIdx.x; q < MD_BUCKETS; q += NT) s_head[q] = -1;
-      __syncthreads();
       int cx[MPT], cy[MPT], cz[MPT];
 #pragma unroll
       for (int k = 0; k < MPT; ++k) {
@@ -502,13 +538,12 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
           cz[k] = static_cast<int>(floor(x[k][2] * inv_rv));
           if (lead) {
             s_ckey[i] = md_cell_key(cx[k], cy[k], cz[k]);
-            s_next[i] = atomicExch(&s_head[md_bucket(cx[k], cy[k], cz[k])], i);
+            s_next[i] = md_bucket(cx[k], cy[k], cz[k]);
           }
         }
       }
       __syncthreads();
-      md_sort_chains(s_head, s_next, NT);
-      __syncthreads();
+      md_bucket_sort<NT>(n, s_next, s_head, s_sorted);
 #pragma unroll
       for (int k = 0; k < MPT; ++k) {
         const int i = slot + k * NT;
@@ -519,7 +554,10 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
               for (int dx = -1; dx <= 1; ++dx) {
                 const int tx = cx[k] + dx, ty = cy[k] + dy, tz = cz[k] + dz;
                 const int want = md_cell_key(tx, ty, tz);
-                for (int j = s_head[md_bucket(tx, ty, tz)]; j >= 0; j = s_next[j]) {
+                const int bk = md_bucket(tx, ty, tz);
+                const int kend = s_head[bk + 1];
+                for (int kk = s_head[bk]; kk < kend; ++kk) {
+                  const int j = s_sorted[kk];
                   if (j == i || s_ckey[j] != want) continue;
                   const R d0 = sx[j] - x[k][0], d1 = sy[j] - x[k][1], d2 = sz[j] - x[k][2];
                   if ((d0 * d0 + d1 * d1) + d2 * d2 <= rv2) {
@@ -713,8 +751,10 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
 //  2. all threads compute the candidates' FP64 pair forces, every lane busy,
 //     with the exact FP64 range test inside pair_force, and the bonds' FENE
 //     forces, one bond per thread;
-//  3. each bead's kick thread subtracts its pairs' contributions in list
-//     order, then its bonds' in bond order (Box.cpp:253-284).
+//  3. each bead's lanes subtract its pairs' contributions, lane l taking
+//     every lanes-th one from the l-th, then its bonds' the same way, and
+//     sum over the lanes (Box.cpp:253-284 subtracts them one by one; the
+//     order here is fixed, so runs repeat bit for bit).
 // The FP32 test only skips entries whose FP64 force is zero: FP32 rounding
 // of coordinates below 4096 moves r^2 by far less than the margin. A CTA whose
 // lists or bonds outgrow the shared buffers, or a replica with a coordinate
@@ -747,25 +787,16 @@ struct MdcLayout {
   static_assert(OWN <= 256, "bead slot of a CTA fits one byte");
 };
 
-// inclusive warp scan
-__device__ __forceinline__ int md_warp_scan(int v) {
-  const int lane = static_cast<int>(threadIdx.x & 31u);
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(0xFFFFFFFFu, v, o);
-    if (lane >= o) v += t;
-  }
-  return v;
-}
 
 template <typename R, int NT, int CS, int KMAX>
 __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel, R* mfrc, R* mver) {
   namespace cg = cooperative_groups;
   constexpr int CAP = MD_CLUSTER_CAP;
   __shared__ unsigned char s_amphi[CAP];
-  __shared__ int s_head[MD_BUCKETS];
-  __shared__ int s_next[CAP];
+  __shared__ int s_head[MD_BUCKETS + 1];  // bucket starts in s_sorted
+  __shared__ int s_next[CAP];             // bucket of each bead
   __shared__ int s_ckey[CAP];
+  __shared__ int s_sorted[CAP];
   __shared__ float s_coref[3];      // the core's position at the last rebuild (FP32)
   __shared__ int s_rebuild[2];      // by substep parity: a bead passed the Verlet limit
   __shared__ int s_farp[2];         // by substep parity: a coordinate reached MDC_FAR
@@ -815,6 +846,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   const bool mine = q < own;
   const int i = rank + CS * q;  // this lane's bead (when mine)
   const bool lead = sub == 0;
+  const int nl = 1 << lk;  // lanes per bead
   const int b = ri.mono_base;
   const R dt = static_cast<R>(ri.md_dt);
   const R dth = dt * R(0.50);
@@ -1005,18 +1037,15 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     if (rebuild) {
       ++rebuilds;
       const R inv_rv = R(1) / static_cast<R>(ri.r_verlet);
-      for (int t = threadIdx.x; t < MD_BUCKETS; t += NT) s_head[t] = -1;
-      __syncthreads();
       for (int j = threadIdx.x; j < n; j += NT) {
         const int cx = static_cast<int>(floor(sx[j] * inv_rv));
         const int cy = static_cast<int>(floor(sy[j] * inv_rv));
         const int cz = static_cast<int>(floor(sz[j] * inv_rv));
         s_ckey[j] = md_cell_key(cx, cy, cz);
-        s_next[j] = atomicExch(&s_head[md_bucket(cx, cy, cz)], j);
+        s_next[j] = md_bucket(cx, cy, cz);
       }
       __syncthreads();
-      md_sort_chains(s_head, s_next, NT);
-      __syncthreads();
+      md_bucket_sort<NT>(n, s_next, s_head, s_sorted);
       // Lists: the lanes of a bead split its 27 cells (cell t to lane t mod
       // lanes), count their members, then write them at the offsets the
       // counts give, so a list holds lane 0's cells, then lane 1's, and so
@@ -1024,7 +1053,6 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       // decide it in FP32 outside a band of 2^-7 around r_v^2 (FP32 rounding
       // of coordinates below MDC_FAR moves d^2 by far less) and in FP64
       // inside it.
-      const int nl = 1 << lk;
       const bool fast = kF64 && !far_now;
       const float rv2_lo = static_cast<float>(rv2) * (1.0f - 0.0078125f);
       const float rv2_hi = static_cast<float>(rv2) * (1.0f + 0.0078125f);
@@ -1042,7 +1070,10 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         for (int t = sub; t < 27; t += nl) {
           const int tx = ccx + t % 3 - 1, ty = ccy + (t / 3) % 3 - 1, tz = ccz + t / 9 - 1;
           const int want = md_cell_key(tx, ty, tz);
-          for (int j = s_head[md_bucket(tx, ty, tz)]; j >= 0; j = s_next[j]) {
+          const int bk = md_bucket(tx, ty, tz);
+          const int kend = s_head[bk + 1];
+          for (int kk = s_head[bk]; kk < kend; ++kk) {
+            const int j = s_sorted[kk];
             if (j == i || s_ckey[j] != want) continue;
             bool in;
             float r2f = 0.f;
@@ -1209,10 +1240,12 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
           }
         }
         __syncthreads();
-        // 3. each bead's pairs in list order
-        if (kicker) {
-          const int e1 = min(s_cstart[kq + 1], c1);
-          for (int c = max(s_cstart[kq], c0); c < e1; ++c) {
+        // 3. each bead's lanes: lane sub takes the bead's candidates
+        // cs + sub, cs + sub + lanes, ... (cs its first)
+        if (mine) {
+          const int cs = s_cstart[q], e1 = min(s_cstart[q + 1], c1);
+          const int st = max(cs, c0);
+          for (int c = st + (((sub - (st - cs)) % nl) + nl) % nl; c < e1; c += nl) {
             const R* o = s_pf + 3 * (c - c0);
             F0 -= o[0];
             F1 -= o[1];
@@ -1221,15 +1254,22 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         }
         __syncthreads();  // read before the next batch rewrites the buffer
       }
-      if (kicker) {  // then its bonds in bond order
-        for (int e = s_bstart[kq]; e < s_bstart[kq + 1]; ++e) {
+      if (mine) {  // then its bonds, the same way
+        for (int e = s_bstart[q] + sub; e < s_bstart[q + 1]; e += nl) {
           F0 -= s_bf[3 * e];
           F1 -= s_bf[3 * e + 1];
           F2 -= s_bf[3 * e + 2];
         }
-        s_f[3 * kq] = F0;
-        s_f[3 * kq + 1] = F1;
-        s_f[3 * kq + 2] = F2;
+      }
+      for (int o = 1; o < nl; o <<= 1) {  // whole warps take part
+        F0 += __shfl_xor_sync(0xFFFFFFFFu, F0, o);
+        F1 += __shfl_xor_sync(0xFFFFFFFFu, F1, o);
+        F2 += __shfl_xor_sync(0xFFFFFFFFu, F2, o);
+      }
+      if (mine && lead) {
+        s_f[3 * q] = F0;
+        s_f[3 * q + 1] = F1;
+        s_f[3 * q + 2] = F2;
       }
     } else {
     R F0 = R(0), F1 = R(0), F2 = R(0);
