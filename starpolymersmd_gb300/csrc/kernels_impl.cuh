@@ -97,7 +97,7 @@ template <>
 void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
                             const RepDyn* dyn, const FrameF* frames, const Real* rec, uint2* keys,
                             uint32_t* count, ErrorState* err, int strict, int variant,
-                            int packed, cudaStream_t st) {
+                            int packed, Real* frame, cudaStream_t st) {
   if (n_tiles == 0) return;
 #if SMPC_FAST_F32
   if (!strict && variant >= 0) {  // variant < 0: the generic kernel (what k_collide recomputes)
@@ -115,7 +115,7 @@ void launch_fluid_bin<Real>(const Tile* tiles, int n_tiles, const RepInfo* reps,
   (void)frames;
   (void)variant;
   k_fluid_bin<Real, SMPC_BIN_NT><<<n_tiles, SMPC_BIN_NT, 0, st>>>(tiles, reps, dyn, rec, keys,
-                                                                  count, err, strict);
+                                                                  count, err, strict, frame);
 }
 
 template <>
@@ -149,7 +149,7 @@ void launch_collide<Real>(const CollideArgs<Real>& a, cudaStream_t st) {
   kern<<<a.n_tiles, SMPC_COLLIDE_NT, dyn, st>>>(
       a.tiles, a.reps, a.dyn, a.off, a.perm, a.st_in, a.st_out, a.mpos, a.mvel, a.mkey, a.mimg,
       a.inj_gamma, a.inj_uphi, a.inj_utheta, a.rng, a.rot_c, a.rot_s, a.strict, a.mono_bin, a.amc,
-      a.err);
+      a.err, a.frame);
 }
 
 template <>

@@ -54,6 +54,9 @@ struct CollideArgs {
   int mono_bin;
   int amc;  // angular-momentum-conserving collision (generic kernel only)
   ErrorState* err;
+  // collision-frame records written by the binning just before (generic
+  // kernel; FP64 contexts), or null: the collide recomputes them from st_in
+  const R* frame;
 };
 
 // Tile geometry chosen per precision (register budget of k_collide).
@@ -80,7 +83,8 @@ void launch_mono_prep(const RepInfo* reps, RepDyn* dyn, int n_rep, R* mpos, R* m
 template <typename R>
 void launch_fluid_bin(const Tile* tiles, int n_tiles, const RepInfo* reps, const RepDyn* dyn,
                       const FrameF* frames, const R* rec, uint2* keys, uint32_t* count,
-                      ErrorState* err, int strict, int variant, int packed, cudaStream_t st);
+                      ErrorState* err, int strict, int variant, int packed, R* frame,
+                      cudaStream_t st);
 template <typename R>
 void launch_collide(const CollideArgs<R>& a, cudaStream_t st);
 template <typename R>

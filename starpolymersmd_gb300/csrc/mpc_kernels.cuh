@@ -649,15 +649,33 @@ __global__ void __launch_bounds__(NT) k_mono_prep(const RepInfo* reps, RepDyn* d
   }
 }
 
+// A cell key carried in a record's fourth word, as a bit pattern.
+template <typename R>
+__device__ __forceinline__ R key_word(uint32_t k);
+template <>
+__device__ __forceinline__ double key_word<double>(uint32_t k) {
+  return __longlong_as_double(static_cast<long long>(k));
+}
+template <>
+__device__ __forceinline__ float key_word<float>(uint32_t k) { return __uint_as_float(k); }
+__device__ __forceinline__ uint32_t word_key(double w) {
+  return static_cast<uint32_t>(__double_as_longlong(w));
+}
+__device__ __forceinline__ uint32_t word_key(float w) { return __float_as_uint(w); }
+
 // Stream, shift, wrap and bin every solvent slot of a slot tile. Each thread
 // loads U records (U independent 32-byte loads in flight), computes their
 // keys, then takes ranks with warp-aggregated atomics whose U round trips
 // overlap (all atomics are issued before any result is consumed).
+// With frame, it also stores each binned particle's collision-frame record
+// for the collide that follows (FP64 contexts: the collide then reads it
+// instead of repeating the streaming, shift, wraps and cell index on the
+// narrow FP64 pipe; the values are the same).
 template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepInfo* reps,
                                                   const RepDyn* dyn, const R* __restrict__ st,
                                                   uint2* __restrict__ keys, uint32_t* count,
-                                                  ErrorState* err, int strict) {
+                                                  ErrorState* err, int strict, R* frame) {
   // FP64: two records in flight per thread, so that two blocks fit per SM
   // (the FP64 work is latency-bound on the narrow pipe; more warps hide it)
   constexpr int U = std::is_same<R, double>::value ? 2 : 4;
@@ -691,6 +709,9 @@ __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepIn
           raise_error(err, ERR_FLUID_CELL, static_cast<uint32_t>(t.rep), static_cast<uint32_t>(i));
         } else {
           key[u] = cbase + c;
+          // the collision-frame record for the collide, the key in the
+          // velocity's fourth word (a bit pattern)
+          if (frame) st_rec(frame, i, x[u], R4<R>{v[u].x, v[u].y, v[u].z, key_word<R>(key[u])});
         }
       }
     }
@@ -766,6 +787,10 @@ template <typename R>
 struct CollideCtx {
   const uint32_t* __restrict__ perm;
   const R* __restrict__ st;
+  // collision-frame records the binning wrote (solvent slots: streamed,
+  // shifted, wrapped position with the id; velocity with the cell key), or
+  // null: recomputed from st
+  const R* __restrict__ fr;
   const R* mpos;
   R* mvel;
   const uint2* mkey;
@@ -802,6 +827,9 @@ __device__ __forceinline__ void finish_particle(Particle<R>& P, uint32_t p, cons
       }
     }
     P.lc = static_cast<int>(C.mkey[m].x - C.c0);
+  } else if (C.fr) {
+    P.m = C.solvent_mass;
+    P.lc = static_cast<int>(word_key(P.v.w) - C.c0);
   } else {
     fluid_to_collision_frame(C.g, P.x, P.v);
     P.m = C.solvent_mass;
@@ -822,8 +850,9 @@ __device__ __forceinline__ void fetch_raw(Particle<R>& P, uint32_t src, const Co
     P.v = ld4_rw(C.mvel, m);
     P.m = ld4_rw(C.mpos, m).w;
   } else {
-    P.x = ld_pos(C.st, src);
-    P.v = ld_vel(C.st, src);
+    const R* s = C.fr ? C.fr : C.st;
+    P.x = ld_pos(s, src);
+    P.v = ld_vel(s, src);
   }
 }
 
@@ -1064,7 +1093,7 @@ __global__ void __launch_bounds__(NT) k_collide(
     const uint32_t* __restrict__ perm, const R* __restrict__ st_in, R* __restrict__ st_out,
     const R* mpos, R* mvel, const uint2* mkey, const int* mimg, const double* inj_gamma,
     const double* inj_uphi, const double* inj_utheta, int rng, double rot_c, double rot_s,
-    int strict, int mono_bin, int amc, ErrorState* err) {
+    int strict, int mono_bin, int amc, ErrorState* err, const R* frame) {
   constexpr int GU = 4;
   constexpr bool kFP64 = std::is_same<R, double>::value;
   typedef typename AccT<R>::type Acc;
@@ -1084,6 +1113,7 @@ __global__ void __launch_bounds__(NT) k_collide(
   CollideCtx<R> C;
   C.perm = perm;
   C.st = st_in;
+  C.fr = frame;
   C.mpos = mpos;
   C.mvel = mvel;
   C.mkey = mkey;

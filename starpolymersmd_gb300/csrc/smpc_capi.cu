@@ -132,6 +132,11 @@ struct smpc_ctx {
   int max_nb = 192;
   bool collided = false;
   bool binned = false;      // smpc_mpc_bin done, collide pending
+  // FP64: collision-frame records of the solvent, written by every binning
+  // for the collide that follows; frame_ok while the records still match the
+  // state (host writes of the solvent clear it)
+  void* d_frame = nullptr;
+  bool frame_ok = false;
   // per replica: its solvent records sit in the last sort's cell order (set by
   // a collision, cleared by a host upload or a new binning)
   std::vector<uint8_t> sorted;
@@ -228,7 +233,8 @@ int launch_binning(smpc_ctx* ctx, int cur) {
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
                             ctx->opt.angular_momentum ? -1 : ctx->var_bin,
-                            ctx->packed_keys ? 1 : 0, ctx->st);
+                            ctx->packed_keys ? 1 : 0, static_cast<R*>(ctx->d_frame), ctx->st);
+  ctx->frame_ok = ctx->d_frame != nullptr;
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
   launch_permutation(ctx);
@@ -275,6 +281,7 @@ smpc::CollideArgs<R> collide_args(smpc_ctx* ctx, int rng, int cur) {
   a.mono_bin = ctx->opt.mono_bin;
   a.amc = ctx->opt.angular_momentum ? 1 : 0;
   a.err = ctx->d_err;
+  a.frame = ctx->frame_ok ? static_cast<const R*>(ctx->d_frame) : nullptr;
   return a;
 }
 
@@ -339,7 +346,8 @@ int profiled_cycle(smpc_ctx* ctx, int cur, cudaEvent_t* ev) {
   smpc::launch_fluid_bin<R>(ctx->d_bin_tiles, ctx->n_bin_tiles, ctx->d_reps, ctx->d_dyn,
                             ctx->d_frames, rec_in, ctx->d_keys, ctx->d_count, ctx->d_err, strict,
                             ctx->opt.angular_momentum ? -1 : ctx->var_bin,
-                            ctx->packed_keys ? 1 : 0, ctx->st);
+                            ctx->packed_keys ? 1 : 0, static_cast<R*>(ctx->d_frame), ctx->st);
+  ctx->frame_ok = ctx->d_frame != nullptr;
   cudaEventRecord(ev[1 + PH_BIN], ctx->st);
   smpc::launch_scan(ctx->d_count, ctx->d_off, ctx->d_tsum, ctx->d_grand,
                     static_cast<int>(ctx->total_cells), ctx->st);
@@ -423,6 +431,7 @@ int set_fluid_t(smpc_ctx* ctx, int rep, const double* pos, const double* vel) {
       p[3] = id_to_w<R>(smpc::SLOT_EMPTY);
     }
   }
+  ctx->frame_ok = false;
   CU(cudaMemcpyAsync(static_cast<R*>(ctx->d_rec[ctx->cur]) + 8 * static_cast<size_t>(ri.slot_base),
                      rec.data(), rec.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->st));
   CU(cudaStreamSynchronize(ctx->st));
@@ -653,6 +662,7 @@ int create_buffers(smpc_ctx* ctx) {
   const size_t S = static_cast<size_t>(ctx->total_slots), M = static_cast<size_t>(ctx->total_mono),
                C = static_cast<size_t>(ctx->total_cells);
   for (int k = 0; k < 2; ++k) CU(dalloc(reinterpret_cast<R**>(&ctx->d_rec[k]), 8 * S));
+  if (std::is_same<R, double>::value) CU(dalloc(reinterpret_cast<R**>(&ctx->d_frame), 8 * S));
   CU(dalloc(&ctx->d_keys, S));
   CU(dalloc(&ctx->d_perm, S + M));
   // a sorted position left unwritten (an error case) holds a valid index
@@ -736,6 +746,7 @@ void free_all(smpc_ctx* ctx) {
     if (ctx->graph[k]) cudaGraphExecDestroy(ctx->graph[k]);
     cudaFree(ctx->d_rec[k]);
   }
+  cudaFree(ctx->d_frame);
   for (void* q : ctx->pmd_mem)
     if (q) cudaFree(q);
   ctx->pmd_mem.clear();
@@ -1687,6 +1698,7 @@ int smpc_init_solvent(smpc_ctx* ctx, int rep, uint64_t seed, int flags) {
   cudaSetDevice(ctx->device);
   const RepInfo& ri = ctx->reps[rep];
   ctx->sorted[rep] = 0;
+  ctx->frame_ok = false;
   if (ctx->opt.precision == SMPC_FP64)
     smpc::launch_init_solvent<double>(ctx->d_reps, rep, ri.slot_cap,
                                       static_cast<double*>(ctx->d_rec[ctx->cur]), seed, ri.kT,
@@ -2472,6 +2484,7 @@ int ck_load(smpc_ctx* ctx, CkptIo& io) {
   if (!io.ok) return fail(ctx, SMPC_E_ARG, "truncated checkpoint (context state undefined)");
   ctx->collided = h.collided != 0;
   ctx->binned = false;
+  ctx->frame_ok = false;
   ctx->dyn = dyn;
   ctx->sorted = sorted;
   ctx->bsrc = bsrc;
