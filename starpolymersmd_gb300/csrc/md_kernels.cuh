@@ -26,19 +26,30 @@
 
 namespace smpc {
 
+// r2 < c for a squared distance r2 (a sum of squares: +0 or more, or NaN)
+// and a cut-off c > 0. In FP64 the comparison runs on the bit patterns,
+// whose unsigned integer order is the numeric order for non-negative doubles
+// (NaN patterns lie above every finite one, so a NaN r2 compares false as in
+// FP64), and does not take the narrow FP64 pipe.
+__device__ __forceinline__ bool r2_below(double r2, double c) {
+  return static_cast<unsigned long long>(__double_as_longlong(r2)) <
+         static_cast<unsigned long long>(__double_as_longlong(c));
+}
+__device__ __forceinline__ bool r2_below(float r2, float c) { return r2 < c; }
+
 // Pair force magnitude f such that F_i -= f (x_j - x_i).
 template <typename R>
 __device__ __forceinline__ R pair_force(int pot, bool bb, R r2, R lambda) {
   if (pot == POT_REF4824) {
     // TypeAA_Force / TypeBB_Force (Potentials.h:57-120)
-    if (r2 < R(1.0594631)) {
+    if (r2_below(r2, R(1.0594631))) {
       const R rm2 = R(1) / r2;
       R rm24 = rm2 * rm2 * rm2;
       rm24 *= rm24;
       rm24 *= rm24;
       return R(192.0) * rm2 * rm24 * (rm24 - R(0.5));
     }
-    if (bb && r2 < R(2.25)) {
+    if (bb && r2_below(r2, R(2.25))) {
       const R rm2 = R(1) / r2;
       R rm24 = rm2 * rm2 * rm2;
       rm24 *= rm24;
@@ -48,11 +59,12 @@ __device__ __forceinline__ R pair_force(int pot, bool bb, R r2, R lambda) {
     return R(0);
   }
   // 12-6 preset: WCA core for all pairs, lambda-scaled LJ attraction to 2.5 for BB
-  if (r2 < R(1.2599210498948732) || (bb && r2 < R(6.25))) {
+  const bool core = r2_below(r2, R(1.2599210498948732));
+  if (core || (bb && r2_below(r2, R(6.25)))) {
     const R rm2 = R(1) / r2;
     const R rm6 = rm2 * rm2 * rm2;
     const R f = R(48.0) * rm2 * rm6 * (rm6 - R(0.5));
-    return r2 < R(1.2599210498948732) ? f : lambda * f;
+    return core ? f : lambda * f;
   }
   return R(0);
 }
@@ -759,6 +771,94 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
 // of coordinates below 4096 moves r^2 by far less than the margin. A CTA whose
 // lists or bonds outgrow the shared buffers, or a replica with a coordinate
 // of 4096 or more, takes the lanes-per-bead pass instead.
+// Paths of k_md_cluster that most substeps do not take, out of line, so that
+// the code of a substep stays compact: half the pair and FENE energies (read
+// at the last substep of a call when asked for), the Andersen resets, and the
+// lanes-per-bead force walk over the global lists (a CTA whose lists outgrow
+// the shared buffers).
+template <typename R>
+__device__ __noinline__ double md_pair_epot(int pot, bool bb, R r2, R lambda) {
+  return 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
+}
+template <typename R>
+__device__ __noinline__ double md_fene_epot(bool anch, R r2) {
+  return 0.5 * static_cast<double>(fene_pot<R>(anch, r2));
+}
+template <typename R>
+__device__ __noinline__ void md_andersen_reset(const MdArgs& a, const RepInfo& ri, int r, int step,
+                                               int ik, unsigned long long md_step0, R m, R* v) {
+  const int* as = a.and_start ? a.and_start + static_cast<size_t>(r) * (a.n_steps + 1) : nullptr;
+  if (as && as[0] >= 0) {
+    for (int e = as[step]; e < as[step + 1]; ++e)
+      if (a.and_mono[e] == ik)
+        for (int d = 0; d < 3; ++d) v[d] = static_cast<R>(a.and_vel[3 * e + d]);
+  } else {
+    andersen_draw<R>(ri.seed, ik, md_step0 + static_cast<unsigned long long>(step),
+                     static_cast<R>(a.andersen_nu * ri.md_dt), r_sqrt(static_cast<R>(ri.kT)), m, v);
+  }
+}
+// Forces on bead i (replica-local; mono_base b) from its Verlet list in global
+// memory, every (1 << lk)-th entry from sub, and its bonds on the lead lane;
+// F accumulates them, epot (when asked) half the energies.
+template <typename R>
+__device__ __noinline__ void md_bead_forces_lists(const MdArgs& a, int b, int i, int sub, int lk,
+                                                  bool lead, const R* sx, const R* sy,
+                                                  const R* sz, const unsigned char* s_amphi,
+                                                  int pot, R lambda, bool want_epot, R* F,
+                                                  double* epot) {
+  const R x0 = sx[i], x1 = sy[i], x2 = sz[i];
+  R F0 = F[0], F1 = F[1], F2 = F[2];
+  const bool ai = s_amphi[i] != 0;
+  const int cnt = a.ncount[b + i];
+  const int* nl = a.nlist + b + i;
+  const size_t stride = static_cast<size_t>(a.n_mono_total);
+  constexpr int PF = 4;
+  for (int q0 = sub; q0 < cnt; q0 += PF << lk) {
+    int js[PF];
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int qq = q0 + (u << lk);
+      js[u] = qq < cnt ? nl[static_cast<size_t>(qq) * stride] - b : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int j = js[u];
+      if (j < 0) continue;
+      const R d0 = sx[j] - x0, d1 = sy[j] - x1, d2 = sz[j] - x2;
+      const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+      const bool bb = ai && s_amphi[j] != 0;
+      const R fa = pair_force<R>(pot, bb, r2, lambda);
+      F0 -= d0 * fa;
+      F1 -= d1 * fa;
+      F2 -= d2 * fa;
+      if (want_epot) *epot += md_pair_epot<R>(pot, bb, r2, lambda);
+    }
+  }
+  for (int e = lead ? a.bond_start[b + i] : 0; lead && e < a.bond_start[b + i + 1]; ++e) {
+    const int2 bd = a.bonds[e];
+    const int j = bd.x - b;
+    const R d0 = sx[j] - x0, d1 = sy[j] - x1, d2 = sz[j] - x2;
+    const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+    const bool anch = bd.y != 0;
+    R r2f = r2;
+    if (pot == POT_REF4824) {
+      if (r2 >= (anch ? R(20.25) : R(2.25)))
+        raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + i), static_cast<uint32_t>(b + j));
+    } else {
+      const R cap = (anch ? R(20.25) : R(2.25)) * R(0.98);
+      if (r2f > cap) r2f = cap;
+    }
+    const R fa = fene_force<R>(anch, r2f);
+    F0 -= d0 * fa;
+    F1 -= d1 * fa;
+    F2 -= d2 * fa;
+    if (want_epot) *epot += md_fene_epot<R>(anch, r2f);
+  }
+  F[0] = F0;
+  F[1] = F1;
+  F[2] = F2;
+}
+
 constexpr int MD_CLUSTER_CAP = 1024;
 constexpr int MDC_ECAP = 8192;  // flattened list entries of a CTA's beads
 constexpr int MDC_CCAP = 1024;  // candidate pairs per force batch
@@ -779,8 +879,7 @@ struct MdcLayout {
   static constexpr size_t lstart = bj + sizeof(int) * MDC_BCAP;        // int[OWN + 1]
   static constexpr size_t cstart = lstart + sizeof(int) * (OWN + 1);   // int[OWN + 1]
   static constexpr size_t bstart = cstart + sizeof(int) * (OWN + 1);   // int[OWN + 1]
-  static constexpr size_t ccnt = bstart + sizeof(int) * (OWN + 1);     // int[OWN]
-  static constexpr size_t nb = ccnt + sizeof(int) * OWN;               // uint16[ECAP]
+  static constexpr size_t nb = bstart + sizeof(int) * (OWN + 1);       // uint16[ECAP]
   static constexpr size_t own = nb + 2 * MDC_ECAP;                     // uint8[ECAP]
   static constexpr size_t bq = own + MDC_ECAP;                         // uint8[BCAP]
   static constexpr size_t bytes = bq + MDC_BCAP;
@@ -809,6 +908,11 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   constexpr bool kF64 = sizeof(R) == 8;
   using L = MdcLayout<R, CS>;
   __shared__ int s_wcnt[NW], s_woff[NW + 1];
+  // per warp and round of 32 list entries: candidates before the round, and
+  // the round's ballot of candidates (list position -> candidate position)
+  constexpr int MDC_ROUNDS = (MDC_ECAP / NW + 31) / 32;
+  __shared__ int s_rpre[MDC_ROUNDS][NW];
+  __shared__ unsigned s_rmask[MDC_ROUNDS][NW];
   __shared__ int s_far, s_fits;  // replica-wide: a coordinate >= MDC_FAR so far; CTA: lists fit
   extern __shared__ __align__(16) unsigned char s_dyn[];
   // Positions, double-buffered by substep parity: substep s pushes into and
@@ -825,7 +929,6 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   int* s_lstart = reinterpret_cast<int*>(s_dyn + L::lstart);
   int* s_cstart = reinterpret_cast<int*>(s_dyn + L::cstart);
   int* s_bstart = reinterpret_cast<int*>(s_dyn + L::bstart);
-  int* s_ccnt = reinterpret_cast<int*>(s_dyn + L::ccnt);
   unsigned short* s_nb = reinterpret_cast<unsigned short*>(s_dyn + L::nb);
   unsigned char* s_own = s_dyn + L::own;
   unsigned char* s_bq = s_dyn + L::bq;
@@ -880,7 +983,6 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     if (!(fabs(p.x) < R(MDC_FAR) && fabs(p.y) < R(MDC_FAR) && fabs(p.z) < R(MDC_FAR))) s_far = 1;
     s_amphi[j] = static_cast<unsigned char>(static_cast<int>(ld4_rw(mvel, b + j).w) & 1);
   }
-  for (int qq = threadIdx.x; qq < L::OWN; qq += NT) s_ccnt[qq] = 0;
   // flattened bonds of this CTA's beads (bead slot, partner | anchor << 16)
   bool bonds_fit = false;
   if (threadIdx.x < 32) {
@@ -950,6 +1052,10 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
   const int ik = rank + CS * kq;
   R xk[3] = {R(0), R(0), R(0)}, v[3] = {R(0), R(0), R(0)}, f[3] = {R(0), R(0), R(0)},
     xv[3] = {R(0), R(0), R(0)}, m = R(1);
+  // the half-kick increment f / m dt / 2 (Thermostat_None.cpp:22,34), taken
+  // once per force evaluation: the second half-kick of a substep and the
+  // first of the next use the same force
+  R fk[3] = {R(0), R(0), R(0)};
   if (kicker) {
     const R4<R> p = ld4_rw(mpos, b + ik), vv = ld4_rw(mvel, b + ik), ff = ld4_rw(mfrc, b + ik),
                 pv = ld4_rw(mver, b + ik);
@@ -957,6 +1063,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     v[0] = vv.x; v[1] = vv.y; v[2] = vv.z;
     f[0] = ff.x; f[1] = ff.y; f[2] = ff.z;
     xv[0] = pv.x; xv[1] = pv.y; xv[2] = pv.z;
+    for (int d = 0; d < 3; ++d) fk[d] = a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
   }
   cl.sync();  // every copy loaded before any CTA writes into another's
   if (!a.force_rebuild) flatten();  // (a forced rebuild flattens the new lists)
@@ -976,7 +1083,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       // kick + drift (Thermostat_None.cpp:22-27); the force lanes read the
       // new position from shared memory after the barrier
       for (int d = 0; d < 3; ++d) {
-        v[d] += a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
+        v[d] += fk[d];
         xk[d] += v[d] * dt;
       }
       {
@@ -987,20 +1094,44 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         }
         const bool far = !(fabs(xk[0]) < R(MDC_FAR) && fabs(xk[1]) < R(MDC_FAR) &&
                            fabs(xk[2]) < R(MDC_FAR));
-        const float f0 = static_cast<float>(xk[0]), f1 = static_cast<float>(xk[1]),
-                    f2 = static_cast<float>(xk[2]);
-#pragma unroll 1
-        for (int c = 0; c < CS; ++c) {  // (rolled: no remote addresses held across the substep)
-          cl.map_shared_rank(sx, c)[ik] = xk[0];
-          cl.map_shared_rank(sy, c)[ik] = xk[1];
-          cl.map_shared_rank(sz, c)[ik] = xk[2];
-          if (kF64) {
-            cl.map_shared_rank(pxf, c)[ik] = f0;
-            cl.map_shared_rank(pyf, c)[ik] = f1;
-            cl.map_shared_rank(pzf, c)[ik] = f2;
+        // this CTA's copy here; the other CTAs' below, by all threads
+        sx[ik] = xk[0];
+        sy[ik] = xk[1];
+        sz[ik] = xk[2];
+        if (kF64) {
+          pxf[ik] = static_cast<float>(xk[0]);
+          pyf[ik] = static_cast<float>(xk[1]);
+          pzf[ik] = static_cast<float>(xk[2]);
+        }
+        if (over || far)
+          for (int c = 0; c < CS; ++c) {
+            if (over) *cl.map_shared_rank(&s_rebuild[cur], c) = 1;
+            if (far) *cl.map_shared_rank(&s_farp[cur], c) = 1;
           }
-          if (over) *cl.map_shared_rank(&s_rebuild[cur], c) = 1;
-          if (far) *cl.map_shared_rank(&s_farp[cur], c) = 1;
+      }
+    }
+    if (a.n_steps > 0) {
+      // Positions into the other CTAs' copies: one (bead, CTA) pair per
+      // thread, from this CTA's copy; one address mapping per pair (the
+      // buffers lie at fixed offsets in the dynamic shared memory).
+      __syncthreads();
+      const size_t ox = reinterpret_cast<const unsigned char*>(sx) - s_dyn;
+      const size_t of = reinterpret_cast<const unsigned char*>(pxf) - s_dyn;
+      for (int t = threadIdx.x; t < own * (CS - 1); t += NT) {
+        const int bq = t / (CS - 1);
+        const int c0 = t - bq * (CS - 1);
+        const int c = c0 + (c0 >= rank ? 1 : 0);
+        const int ib = rank + CS * bq;
+        unsigned char* base = cl.map_shared_rank(s_dyn, c);
+        R* rx = reinterpret_cast<R*>(base + ox);
+        rx[ib] = sx[ib];
+        rx[CAP + ib] = sy[ib];
+        rx[2 * CAP + ib] = sz[ib];
+        if (kF64) {
+          float* fx = reinterpret_cast<float*>(base + of);
+          fx[ib] = pxf[ib];
+          fx[CAP + ib] = pyf[ib];
+          fx[2 * CAP + ib] = pzf[ib];
         }
       }
     }
@@ -1065,47 +1196,57 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         xf0 = pxf[i]; xf1 = pyf[i]; xf2 = pzf[i];
       }
       // members of this lane's cells: counted (pos < 0) or written from pos
-      auto walk = [&](int pos) -> int {
-        int cnt = 0;
+      // emit(j) for every member of this lane's cells, in order; members
+      // are examined four at a time, their loads in flight together
+      auto walk = [&](auto&& emit) {
         for (int t = sub; t < 27; t += nl) {
           const int tx = ccx + t % 3 - 1, ty = ccy + (t / 3) % 3 - 1, tz = ccz + t / 9 - 1;
           const int want = md_cell_key(tx, ty, tz);
           const int bk = md_bucket(tx, ty, tz);
           const int kend = s_head[bk + 1];
-          for (int kk = s_head[bk]; kk < kend; ++kk) {
-            const int j = s_sorted[kk];
-            if (j == i || s_ckey[j] != want) continue;
-            bool in;
-            float r2f = 0.f;
-            if (fast) {
-              const float e0 = pxf[j] - xf0, e1 = pyf[j] - xf1, e2 = pzf[j] - xf2;
-              r2f = fmaf(e0, e0, fmaf(e1, e1, e2 * e2));
+          for (int kk = s_head[bk]; kk < kend; kk += 4) {
+            int jj[4], kc[4];
+            float e0[4], e1[4], e2[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) jj[u] = kk + u < kend ? s_sorted[kk + u] : -1;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int j = jj[u] < 0 ? 0 : jj[u];
+              kc[u] = s_ckey[j];
+              e0[u] = pxf[j] - xf0;
+              e1[u] = pyf[j] - xf1;
+              e2[u] = pzf[j] - xf2;
             }
-            if (fast && r2f < rv2_lo) {
-              in = true;
-            } else if (fast && r2f > rv2_hi) {
-              in = false;
-            } else {
-              const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
-              in = (d0 * d0 + d1 * d1) + d2 * d2 <= rv2;
-            }
-            if (!in) continue;
-            if (pos >= 0) {
-              const int k = pos + cnt;
-              if (k < a.max_nb) {
-                a.nlist[static_cast<size_t>(k) * a.n_mono_total + b + i] = b + j;
-                if (s_fits) {
-                  s_nb[s_lstart[q] + k] = static_cast<unsigned short>(j);
-                  s_own[s_lstart[q] + k] = static_cast<unsigned char>(q);
-                }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int j = jj[u];
+              if (j < 0 || j == i || kc[u] != want) continue;
+              bool in;
+              const float r2f = fmaf(e0[u], e0[u], fmaf(e1[u], e1[u], e2[u] * e2[u]));
+              if (fast && r2f < rv2_lo) {
+                in = true;
+              } else if (fast && r2f > rv2_hi) {
+                in = false;
+              } else {
+                const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
+                in = (d0 * d0 + d1 * d1) + d2 * d2 <= rv2;
               }
+              if (in) emit(j);
             }
-            ++cnt;
           }
         }
-        return cnt;
       };
-      const int mc = mine ? walk(-1) : 0;
+      // Pass 1 counts the members and keeps the first MDC_SCRATCH of each
+      // lane in scratch (the candidate buffer, idle here; slot e of thread t
+      // at e NT + t); the lists are then copied from there, or, if any lane
+      // found more, written by a second walk.
+      constexpr int MDC_SCRATCH = MDC_ECAP / NT;
+      int mc = 0;
+      if (mine)
+        walk([&](int j) {
+          if (mc < MDC_SCRATCH) s_cand[mc * NT + threadIdx.x] = j;
+          ++mc;
+        });
       int inc = mc;  // the bead's lanes are adjacent: segments of nl lanes
       for (int o = 1; o < nl; o <<= 1) {
         const int t = __shfl_up_sync(0xFFFFFFFFu, inc, o, nl);
@@ -1122,7 +1263,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         a.ncount[b + i] = cnt;
         s_cstart[q] = cnt;
       }
-      __syncthreads();
+      const int spill = __syncthreads_or(mc > MDC_SCRATCH);
       if (threadIdx.x < 32) {  // list starts of the CTA's beads
         int carry = 0;
         for (int q0 = 0; q0 < own; q0 += 32) {
@@ -1138,7 +1279,24 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         }
       }
       __syncthreads();
-      if (mine) walk(inc - mc);
+      if (mine) {
+        int k = inc - mc;  // this lane's first list position
+        auto put = [&](int j) {
+          if (k < a.max_nb) {
+            a.nlist[static_cast<size_t>(k) * a.n_mono_total + b + i] = b + j;
+            if (s_fits) {
+              s_nb[s_lstart[q] + k] = static_cast<unsigned short>(j);
+              s_own[s_lstart[q] + k] = static_cast<unsigned char>(q);
+            }
+          }
+          ++k;
+        };
+        if (!spill) {
+          for (int e = 0; e < mc; ++e) put(s_cand[e * NT + threadIdx.x]);
+        } else {
+          walk(put);
+        }
+      }
       if (kicker) { xv[0] = xk[0]; xv[1] = xk[1]; xv[2] = xk[2]; }
       for (int j = threadIdx.x; j < n; j += NT) {
         s_xvf[j] = pxf[j]; s_xvf[CAP + j] = pyf[j]; s_xvf[2 * CAP + j] = pzf[j];
@@ -1158,12 +1316,12 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       const float cut_aa = (pot == POT_REF4824 ? 1.0594631f : 1.2599211f) * widen;
       const float cut_bb = (pot == POT_REF4824 ? 2.25f : 6.25f) * widen;
       int nw = 0;
-      for (int kb = k0; kb < k1; kb += 32) {
+      for (int kb = k0, rd = 0; kb < k1; kb += 32, ++rd) {
         const int k = kb + lane;
         bool cand = false;
-        int pk = 0, qk = 0;
+        int pk = 0;
         if (k < k1) {
-          qk = s_own[k];
+          const int qk = s_own[k];
           const int j = s_nb[k], ii = rank + CS * qk;
           const float d0 = pxf[j] - pxf[ii], d1 = pyf[j] - pyf[ii], d2 = pzf[j] - pzf[ii];
           const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
@@ -1171,41 +1329,43 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
           pk = (qk << 10) | j;
         }
         const unsigned m = __ballot_sync(0xFFFFFFFFu, cand);
-        if (cand) {
-          s_cand[k0 + nw + __popc(m & ((1u << lane) - 1u))] = pk;
-          atomicAdd(&s_ccnt[qk], 1);
+        if (cand) s_cand[k0 + nw + __popc(m & ((1u << lane) - 1u))] = pk;
+        if (lane == 0) {
+          s_rpre[rd][w] = nw;
+          s_rmask[rd][w] = m;
         }
         nw += __popc(m);
       }
       if (lane == 0) s_wcnt[w] = nw;
       __syncthreads();
-      if (threadIdx.x < 32) {  // candidate offsets by warp and by bead
-        const int v = lane < NW ? s_wcnt[lane] : 0;
-        const int inc = md_warp_scan(v);
-        if (lane < NW) s_woff[lane] = inc - v;
-        if (lane == NW - 1) s_woff[NW] = inc;
-        int carry = 0;
-        for (int q0 = 0; q0 < own; q0 += 32) {
-          const int qq = q0 + lane;
-          const int c = qq < own ? s_ccnt[qq] : 0;
-          const int ci = md_warp_scan(c);
-          if (qq < own) { s_cstart[qq] = carry + ci - c; s_ccnt[qq] = 0; }
-          carry += __shfl_sync(0xFFFFFFFFu, ci, 31);
-        }
-        if (lane == 0) s_cstart[own] = carry;
+      // candidate offsets by warp, in every thread (eight counts)
+      int woff[NW + 1];
+      woff[0] = 0;
+#pragma unroll
+      for (int u = 0; u < NW; ++u) woff[u + 1] = woff[u] + s_wcnt[u];
+      const int C = woff[NW];
+      if (threadIdx.x <= NW) {  // for the bead ranges below (read after a barrier)
+#pragma unroll
+        for (int u = 0; u <= NW; ++u)
+          if (u == static_cast<int>(threadIdx.x)) s_woff[u] = woff[u];
       }
-      __syncthreads();
-      const int C = s_woff[NW];
+      // candidates before list position kq: those of the earlier warps, of
+      // the earlier rounds of its warp, and of the earlier lanes of its round
+      auto cand_before = [&](int kq) -> int {
+        if (kq >= E) return C;
+        const int wq = kq / per, o = kq - wq * per;
+        return s_woff[wq] + s_rpre[o >> 5][wq] + __popc(s_rmask[o >> 5][wq] & ((1u << (o & 31)) - 1u));
+      };
       R F0 = R(0), F1 = R(0), F2 = R(0);
       for (int c0 = 0; c0 == 0 || c0 < C; c0 += MDC_CCAP) {
         const int c1 = min(C, c0 + MDC_CCAP);
         // 2. FP64 pair forces of the candidates, then the bonds (first batch)
         for (int c = c0 + static_cast<int>(threadIdx.x); c < c1; c += NT) {
-          int wc = 0;
+          int wc = 0, wb = 0;  // the warp whose region holds candidate c
 #pragma unroll
-          for (int st = NW / 2; st > 0; st >>= 1)
-            if (wc + st < NW && s_woff[wc + st] <= c) wc += st;
-          const int pk = s_cand[wc * per + (c - s_woff[wc])];
+          for (int u = 1; u < NW; ++u)
+            if (woff[u] <= c) { wc = u; wb = woff[u]; }
+          const int pk = s_cand[wc * per + (c - wb)];
           const int qk = pk >> 10, j = pk & 1023, ii = rank + CS * qk;
           const R d0 = sx[j] - sx[ii], d1 = sy[j] - sy[ii], d2 = sz[j] - sz[ii];
           const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
@@ -1215,7 +1375,7 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
           o[0] = d0 * fa;
           o[1] = d1 * fa;
           o[2] = d2 * fa;
-          if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
+          if (want_epot) epot += md_pair_epot<R>(pot, bb, r2, lambda);
         }
         if (c0 == 0) {
           for (int e = threadIdx.x; e < s_bstart[own]; e += NT) {
@@ -1236,14 +1396,14 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
             o[0] = d0 * fa;
             o[1] = d1 * fa;
             o[2] = d2 * fa;
-            if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2f));
+            if (want_epot) epot += md_fene_epot<R>(anch, r2f);
           }
         }
         __syncthreads();
         // 3. each bead's lanes: lane sub takes the bead's candidates
         // cs + sub, cs + sub + lanes, ... (cs its first)
         if (mine) {
-          const int cs = s_cstart[q], e1 = min(s_cstart[q + 1], c1);
+          const int cs = cand_before(s_lstart[q]), e1 = min(cand_before(s_lstart[q + 1]), c1);
           const int st = max(cs, c0);
           for (int c = st + (((sub - (st - cs)) % nl) + nl) % nl; c < e1; c += nl) {
             const R* o = s_pf + 3 * (c - c0);
@@ -1272,55 +1432,11 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
         s_f[3 * q + 2] = F2;
       }
     } else {
-    R F0 = R(0), F1 = R(0), F2 = R(0);
-    if (mine) {
-      const bool ai = s_amphi[i] != 0;
-      const int cnt = a.ncount[b + i];
-      const int* nl = a.nlist + b + i;
-      const size_t stride = static_cast<size_t>(a.n_mono_total);
-      constexpr int PF = 4;
-      for (int q0 = sub; q0 < cnt; q0 += PF << lk) {
-        int js[PF];
-#pragma unroll
-        for (int u = 0; u < PF; ++u) {
-          const int qq = q0 + (u << lk);
-          js[u] = qq < cnt ? nl[static_cast<size_t>(qq) * stride] - b : -1;
-        }
-#pragma unroll
-        for (int u = 0; u < PF; ++u) {
-          const int j = js[u];
-          if (j < 0) continue;
-          const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
-          const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
-          const bool bb = ai && s_amphi[j] != 0;
-          const R fa = pair_force<R>(pot, bb, r2, lambda);
-          F0 -= d0 * fa;
-          F1 -= d1 * fa;
-          F2 -= d2 * fa;
-          if (want_epot) epot += 0.5 * static_cast<double>(pair_pot<R>(pot, bb, r2, lambda));
-        }
-      }
-      for (int e = lead ? a.bond_start[b + i] : 0; lead && e < a.bond_start[b + i + 1]; ++e) {
-        const int2 bd = a.bonds[e];
-        const int j = bd.x - b;
-        const R d0 = sx[j] - x[0], d1 = sy[j] - x[1], d2 = sz[j] - x[2];
-        const R r2 = (d0 * d0 + d1 * d1) + d2 * d2;
-        const bool anch = bd.y != 0;
-        R r2f = r2;
-        if (pot == POT_REF4824) {
-          if (r2 >= (anch ? R(20.25) : R(2.25)))
-            raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + i), static_cast<uint32_t>(b + j));
-        } else {
-          const R cap = (anch ? R(20.25) : R(2.25)) * R(0.98);
-          if (r2f > cap) r2f = cap;
-        }
-        const R fa = fene_force<R>(anch, r2f);
-        F0 -= d0 * fa;
-        F1 -= d1 * fa;
-        F2 -= d2 * fa;
-        if (want_epot) epot += 0.5 * static_cast<double>(fene_pot<R>(anch, r2f));
-      }
-    }
+    R F[3] = {R(0), R(0), R(0)};
+    if (mine)
+      md_bead_forces_lists<R>(a, b, i, sub, lk, lead, sx, sy, sz, s_amphi, pot, lambda, want_epot,
+                              F, &epot);
+    R F0 = F[0], F1 = F[1], F2 = F[2];
     for (int o = 1; KMAX > 1 && o < (1 << lk); o <<= 1) {  // whole warps take part
       F0 += __shfl_xor_sync(0xFFFFFFFFu, F0, o);
       F1 += __shfl_xor_sync(0xFFFFFFFFu, F1, o);
@@ -1337,22 +1453,11 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       f[0] = s_f[3 * kq];
       f[1] = s_f[3 * kq + 1];
       f[2] = s_f[3 * kq + 2];
+      for (int d = 0; d < 3; ++d) fk[d] = a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
       if (a.n_steps > 0) {
         for (int d = 0; d < 3; ++d)  // second half-kick
-          v[d] += a.andersen ? f[d] * (dth / m) : (f[d] / m) * dth;
-        if (a.andersen) {
-          const int* as = a.and_start ? a.and_start + static_cast<size_t>(r) * (a.n_steps + 1)
-                                      : nullptr;
-          if (as && as[0] >= 0) {
-            for (int e = as[step]; e < as[step + 1]; ++e)
-              if (a.and_mono[e] == ik)
-                for (int d = 0; d < 3; ++d) v[d] = static_cast<R>(a.and_vel[3 * e + d]);
-          } else {
-            andersen_draw<R>(ri.seed, ik, md_step0 + static_cast<unsigned long long>(step),
-                             static_cast<R>(a.andersen_nu * ri.md_dt),
-                             r_sqrt(static_cast<R>(ri.kT)), m, v);
-          }
-        }
+          v[d] += fk[d];
+        if (a.andersen) md_andersen_reset<R>(a, ri, r, step, ik, md_step0, m, v);
       }
     }
   }
