@@ -427,7 +427,8 @@ __device__ __forceinline__ void md_bucket_sort(int n, int* s_bkt, int* s_start, 
     if (threadIdx.x == NT - 1) s_start[MD_BUCKETS] = run;
   }
   __syncthreads();
-  for (int j = threadIdx.x; j < n; j += NT) s_sorted[s_start[s_bkt[j] & 2047] + (s_bkt[j] >> 11)] = j;
+  for (int j = threadIdx.x; j < n; j += NT)
+    s_sorted[s_start[s_bkt[j] & 2047] + (s_bkt[j] >> 11)] = j;
   __syncthreads();
 }
 
@@ -726,51 +727,6 @@ __global__ void __launch_bounds__(NT, (NT == 512 && KMAX > 1) ? 2 : 1)
   }
 }
 
-// ---------------------------------------------------------------------------
-// The same substeps for one replica on a thread-block cluster of CS CTAs (CS
-// SMs), for boxes with few replicas: one CTA's FP64 pipe (2 DFMA per clock
-// per SM on this part) held a 401-bead star's FP64 MD to 150 us per substep.
-// Every CTA keeps a copy of all positions in its shared memory and owns the
-// beads i = rank + CS q; after its drift a bead's kick thread stores the new
-// position into every CTA's copy (distributed shared memory) and, when the
-// bead moved past the Verlet limit, sets every CTA's rebuild flag. The
-// copies are double-buffered by substep parity, so one cluster barrier per
-// substep, after the drift, suffices (positions and flags complete
-// everywhere); with displacements measured relative to the core, every CTA
-// decides the rebuild for all beads itself. A rebuild hashes all beads in
-// every CTA's own grid; each CTA writes the lists of its own beads. Forces, kicks and the Andersen resets
-// are those of k_md_substeps for the owned beads (lanes per bead as there).
-// The barriers are hardware cluster barriers: every CTA of a cluster runs
-// at once, and every CTA reaches every barrier (all branches around them
-// depend on the replica and the rebuild flag only, which agree across the
-// cluster after each barrier). Lowe-Andersen stays on k_md_substeps.
-// The kicks, the drift and the position pushes of a CTA's beads run one
-// thread per bead (threads 0 .. own-1, in whole warps), not on the lead lane
-// of each bead's lanes: on the narrow FP64 pipe a warp instruction costs the
-// same with one active lane as with 32. Forces reach those threads through
-// shared memory.
-//
-// Pair forces are compacted. Most Verlet-list entries lie beyond the
-// interaction range, and with lanes per bead walking the lists a warp issued
-// each FP64 force instruction for the few lanes whose pair was in range (7.7
-// active lanes per instruction). Instead, the CTA keeps its beads' lists
-// flattened in shared memory (bead by bead, each in list order), and per
-// substep:
-//  1. every warp tests a contiguous run of entries in FP32 (positions kept
-//     in FP32 beside the FP64 copy) against the pair's cut-off widened by
-//     2^-7, and writes the entries that pass into a candidate list by ballot
-//     (the list stays in flattened order);
-//  2. all threads compute the candidates' FP64 pair forces, every lane busy,
-//     with the exact FP64 range test inside pair_force, and the bonds' FENE
-//     forces, one bond per thread;
-//  3. each bead's lanes subtract its pairs' contributions, lane l taking
-//     every lanes-th one from the l-th, then its bonds' the same way, and
-//     sum over the lanes (Box.cpp:253-284 subtracts them one by one; the
-//     order here is fixed, so runs repeat bit for bit).
-// The FP32 test only skips entries whose FP64 force is zero: FP32 rounding
-// of coordinates below 4096 moves r^2 by far less than the margin. A CTA whose
-// lists or bonds outgrow the shared buffers, or a replica with a coordinate
-// of 4096 or more, takes the lanes-per-bead pass instead.
 // Paths of k_md_cluster that most substeps do not take, out of line, so that
 // the code of a substep stays compact: half the pair and FENE energies (read
 // at the last substep of a call when asked for), the Andersen resets, and the
@@ -859,6 +815,50 @@ __device__ __noinline__ void md_bead_forces_lists(const MdArgs& a, int b, int i,
   F[2] = F2;
 }
 
+
+// ---------------------------------------------------------------------------
+// The same substeps for one replica on a thread-block cluster of CS CTAs (CS
+// SMs), for boxes with few replicas: one CTA's FP64 pipe (2 DFMA per clock
+// per SM on this part) held a 401-bead star's FP64 MD to 150 us per substep.
+// Every CTA keeps a copy of all positions in its shared memory and owns the
+// beads i = rank + CS q. After the drift each CTA's beads go into its own
+// copy, then into every other CTA's (distributed shared memory, one (bead,
+// CTA) pair per thread); a bead past the Verlet limit sets every CTA's
+// rebuild flag. The copies are double-buffered by substep parity, so one
+// cluster barrier per substep, after the drift, suffices (positions and
+// flags complete everywhere); with displacements measured relative to the
+// core, every CTA decides the rebuild for all beads itself. A rebuild hashes
+// all beads in every CTA's own grid; each CTA writes the lists of its own
+// beads. Forces, kicks and the Andersen resets are those of k_md_substeps
+// for the owned beads. The barriers are hardware cluster barriers: every CTA
+// of a cluster runs at once, and every CTA reaches every barrier (no branch
+// around one). Lowe-Andersen stays on k_md_substeps.
+// The kicks and the drift of a CTA's beads run one thread per bead (threads
+// 0 .. own-1, in whole warps), not on the lead lane of each bead's lanes: on
+// the narrow FP64 pipe a warp instruction costs the same with one active
+// lane as with 32. Forces reach those threads through shared memory.
+//
+// Pair forces are compacted. Most Verlet-list entries lie beyond the
+// interaction range, and with lanes per bead walking the lists a warp issued
+// each FP64 force instruction for the few lanes whose pair was in range (7.7
+// active lanes per instruction). Instead, the CTA keeps its beads' lists
+// flattened in shared memory (bead by bead, each in list order), and per
+// substep:
+//  1. every warp tests a contiguous run of entries in FP32 (positions kept
+//     in FP32 beside the FP64 copy) against the pair's cut-off widened by
+//     2^-7, and writes the entries that pass into a candidate list by ballot
+//     (the list stays in flattened order);
+//  2. all threads compute the candidates' FP64 pair forces, every lane busy,
+//     with the exact FP64 range test inside pair_force, and the bonds' FENE
+//     forces, one bond per thread;
+//  3. each bead's lanes subtract its pairs' contributions, lane l taking
+//     every lanes-th one from the l-th, then its bonds' the same way, and
+//     sum over the lanes (Box.cpp:253-284 subtracts them one by one; the
+//     order here is fixed, so runs repeat bit for bit).
+// The FP32 test only skips entries whose FP64 force is zero: FP32 rounding
+// of coordinates below 4096 moves r^2 by far less than the margin. A CTA whose
+// lists or bonds outgrow the shared buffers, or a replica with a coordinate
+// of 4096 or more, takes the lanes-per-bead pass instead.
 constexpr int MD_CLUSTER_CAP = 1024;
 constexpr int MDC_ECAP = 8192;  // flattened list entries of a CTA's beads
 constexpr int MDC_CCAP = 1024;  // candidate pairs per force batch
@@ -870,7 +870,8 @@ template <typename R, int CS>
 struct MdcLayout {
   static constexpr int OWN = (MD_CLUSTER_CAP + CS - 1) / CS;  // beads per CTA at most
   static constexpr size_t posr = 0;                                    // R[2][3][CAP] positions
-  static constexpr size_t posf = posr + sizeof(R) * 6 * MD_CLUSTER_CAP;  // float[2][3][CAP], FP64 only
+  // float[2][3][CAP], FP64 only
+  static constexpr size_t posf = posr + sizeof(R) * 6 * MD_CLUSTER_CAP;
   static constexpr size_t xvf = posf + (sizeof(R) == 8 ? sizeof(float) * 6 * MD_CLUSTER_CAP : 0);
   static constexpr size_t pf = xvf + sizeof(float) * 3 * MD_CLUSTER_CAP;  // R[3 CCAP]
   static constexpr size_t bf = pf + sizeof(R) * 3 * MDC_CCAP;          // R[3 BCAP]
@@ -989,7 +990,8 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
     int carry = 0;
     for (int q0 = 0; q0 < own; q0 += 32) {
       const int qq = q0 + static_cast<int>(threadIdx.x);
-      const int cnt = qq < own ? a.bond_start[b + rank + CS * qq + 1] - a.bond_start[b + rank + CS * qq] : 0;
+      const int ib = b + rank + CS * qq;
+      const int cnt = qq < own ? a.bond_start[ib + 1] - a.bond_start[ib] : 0;
       const int inc = md_warp_scan(cnt);
       if (qq < own) s_bstart[qq] = carry + inc - cnt;
       carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
@@ -1038,7 +1040,8 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
           if (s_lstart[mid] <= k) lo = mid; else hi = mid - 1;
         }
         const int e = k - s_lstart[lo];
-        s_nb[k] = static_cast<unsigned short>(a.nlist[static_cast<size_t>(e) * stride + b + rank + CS * lo] - b);
+        const int* row = a.nlist + static_cast<size_t>(e) * stride;
+        s_nb[k] = static_cast<unsigned short>(row[b + rank + CS * lo] - b);
         s_own[k] = static_cast<unsigned char>(lo);
       }
     }
@@ -1148,7 +1151,8 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       // little early keeps the lists valid), and rebuild at every substep
       // once a coordinate reaches MDC_FAR.
       const float limf = static_cast<float>(lim);
-      const float thr = !kF64 ? limf * limf : (limf > 2e-3f ? (limf - 2e-3f) * (limf - 2e-3f) : 0.0f);
+      const float limm = limf > 2e-3f ? limf - 2e-3f : 0.0f;
+      const float thr = kF64 ? limm * limm : limf * limf;
       if (kF64 && far_now) {
         over_here = true;
       } else {
@@ -1354,7 +1358,8 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
       auto cand_before = [&](int kq) -> int {
         if (kq >= E) return C;
         const int wq = kq / per, o = kq - wq * per;
-        return s_woff[wq] + s_rpre[o >> 5][wq] + __popc(s_rmask[o >> 5][wq] & ((1u << (o & 31)) - 1u));
+        const unsigned below = (1u << (o & 31)) - 1u;
+        return s_woff[wq] + s_rpre[o >> 5][wq] + __popc(s_rmask[o >> 5][wq] & below);
       };
       R F0 = R(0), F1 = R(0), F2 = R(0);
       for (int c0 = 0; c0 == 0 || c0 < C; c0 += MDC_CCAP) {
@@ -1386,7 +1391,8 @@ __global__ void __launch_bounds__(NT, 1) k_md_cluster(MdArgs a, R* mpos, R* mvel
             R r2f = r2;
             if (pot == POT_REF4824) {
               if (r2 >= (anch ? R(20.25) : R(2.25)))
-                raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + ii), static_cast<uint32_t>(b + j));
+                raise_error(a.err, ERR_FENE, static_cast<uint32_t>(b + ii),
+                            static_cast<uint32_t>(b + j));
             } else {
               const R cap = (anch ? R(20.25) : R(2.25)) * R(0.98);
               if (r2f > cap) r2f = cap;
