@@ -670,7 +670,7 @@ __device__ __forceinline__ uint32_t word_key(float w) { return __float_as_uint(w
 // With frame, it also stores each binned particle's collision-frame record
 // for the collide that follows (FP64 contexts: the collide then reads it
 // instead of repeating the streaming, shift, wraps and cell index on the
-// narrow FP64 pipe; the values are the same).
+// narrow FP64 pipe; the arithmetic is the same).
 template <typename R, int NT>
 __global__ void __launch_bounds__(NT) k_fluid_bin(const Tile* tiles, const RepInfo* reps,
                                                   const RepDyn* dyn, const R* __restrict__ st,

@@ -935,3 +935,33 @@ def test_fp32_graph_cycles_with_recentring_in_one_replica():
                 np.testing.assert_array_equal(x, y)
             for x, y in zip(b.get_monomers(k), a.get_monomers(k)):
                 np.testing.assert_array_equal(x, y)
+
+
+def test_fp64_collide_same_values_from_frame_records_and_recomputed():
+    # The FP64 binning stores each solvent particle's collision-frame record
+    # (streamed, shifted, wrapped, with its cell key) for the collide that
+    # follows. A host write of the solvent between the two phases marks the
+    # records stale and the collide recomputes them from the state; writing
+    # back the state the binning saw must give the same positions bit for
+    # bit either way. Velocities are compared at 1e-13: the FP64 cell sums
+    # follow the order the binning's atomics give each cell's particles, so
+    # two FP64 runs differ in their last bits even on the same path.
+    L, su, h = 10, 1, 0.1
+    star, fpos, fvel = H.small_star_system(L=L, shear=0.05, seed=4)
+    out = []
+    for rewrite in (False, True):
+        with H.context_for(star, fpos, fvel, L, 1.0, 0.05, su, rng=capi.RNG_PHILOX,
+                           seed=9) as ctx:
+            assert ctx.mpc_bin(0, h)
+            if rewrite:
+                ctx.set_fluid(0, fpos, fvel)
+            ctx.mpc_collide()
+            ctx.raise_on_device_error()
+            p, v = ctx.get_fluid(0)
+            mp, mv, _ = ctx.get_monomers(0)
+            out.append((p, v, mp, mv))
+    (p0, v0, mp0, mv0), (p1, v1, mp1, mv1) = out
+    np.testing.assert_array_equal(p0, p1)
+    np.testing.assert_array_equal(mp0, mp1)
+    H.close64(v0, v1, rtol=1e-13)
+    H.close64(mv0, mv1, rtol=1e-13)
